@@ -1,0 +1,434 @@
+"""NumPy oracle for the iso-acoustic FDTD hot path (test infrastructure only).
+
+This module is the CPU restatement that the CUDA path is checked against. It is
+imported only by ``tests/``, by ``__graft_entry__.smoke()`` and by the CPU legs of
+``bench.py``; the product path never calls it.
+
+Parity status: **unpinned against Devito.** The reference builds its time loop
+with Devito (a third-party JIT compiler that is not vendored and cannot be
+imported here), and the reference ships no tests or golden vectors for this
+path. What pins this restatement instead: the analytic 2D/3D Green's-function
+known-answer check of the reference's own example
+(``stride_examples/examples/homogeneous_acoustic/utils.py:5-59``), exact
+dot-product tests of the discrete adjoint, central finite differences, and
+agreement with the independent C restatement in ``oracle/fdtd_oracle.c``.
+
+Every function cites the reference lines whose behaviour it restates (paths
+relative to the reference repository root).
+"""
+
+from fractions import Fraction
+
+import numpy as np
+import scipy.signal
+
+__all__ = [
+    'second_derivative_weights', 'staggered_weights', 'damping_profile',
+    'linear_stencil', 'select_kernel', 'select_undersampling', 'bandwidth',
+    'tone_burst', 'tukey', 'forward', 'adjoint', 'grad_vp_chain',
+    'DB_TO_NEPER',
+]
+
+# dB/cm -> Np/m for attenuation power 0 (stride/physics/iso_acoustic/devito.py:487-497)
+DB_TO_NEPER = 100 * (1e-6 / (2 * np.pi)) ** 0 / (20 * np.log10(np.exp(1)))
+
+
+def _fornberg(m, x0, xs):
+    """Fornberg's recursion with exact rationals (published algorithm, 1988)."""
+    n = len(xs)
+    c = [[Fraction(0)] * (m + 1) for _ in range(n)]
+    c1 = Fraction(1)
+    c4 = xs[0] - x0
+    c[0][0] = Fraction(1)
+    for i in range(1, n):
+        mn = min(i, m)
+        c2 = Fraction(1)
+        c5 = c4
+        c4 = xs[i] - x0
+        for j in range(i):
+            c3 = xs[i] - xs[j]
+            c2 *= c3
+            if j == i - 1:
+                for k in range(mn, 0, -1):
+                    c[i][k] = c1 * (k * c[i - 1][k - 1] - c5 * c[i - 1][k]) / c2
+                c[i][0] = -c1 * c5 * c[i - 1][0] / c2
+            for k in range(mn, 0, -1):
+                c[j][k] = (c4 * c[j][k] - k * c[j][k - 1]) / c3
+            c[j][0] = c4 * c[j][0] / c3
+        c1 = c2
+    return [c[i][m] for i in range(n)]
+
+
+def second_derivative_weights(order=10):
+    """Centred 2nd-derivative weights c0..c_{order/2} (Devito ``laplace`` at space_order 10,
+    stride/physics/iso_acoustic/devito.py:1652)."""
+    r = order // 2
+    w = _fornberg(2, Fraction(0), [Fraction(i) for i in range(-r, r + 1)])
+    return [float(w[r + k]) for k in range(r + 1)]
+
+
+def staggered_weights(order=10):
+    """Staggered 1st-derivative weights at offsets 1/2..(order-1)/2, antisymmetric
+    (Devito ``grad(shift=+.5)`` / ``div(shift=-.5)``, iso_acoustic/devito.py:1655-1663)."""
+    r = order // 2
+    xs = [Fraction(2 * i + 1, 2) for i in range(-r, r)]
+    w = _fornberg(1, Fraction(0), xs)
+    return [float(w[r + k]) for k in range(r)]  # weight of +(k+1/2); -(k+1/2) is its negative
+
+
+def damping_profile(shape, spacing, absorbing, vp_ext, dt):
+    """Sponge damping ``damp`` of SpongeBoundary2 (stride/physics/boundaries/devito.py:49-60)
+    built with Boundary.damping (stride/physics/boundaries/boundary.py:59-170), sine profile,
+    power_degree 2, reflection coefficient from the absorbing width. FP32 like the reference."""
+    dim = len(shape)
+    refl = 10 ** (-(np.log10(max(*absorbing)) - 1) / np.log10(2) - 3)
+    damp = np.zeros(shape, dtype=np.float32)
+    for d in range(dim):
+        A = absorbing[d]
+        coef = (2 + 1) / 2 * np.log(1.0 / refl)
+        coef = coef / (A * spacing[d]) if A > 15 else 0.67 / spacing[d]
+        for index in range(A):
+            pos = np.abs((A - index - 1) / float(A - 1))
+            pos = pos - np.sin(2 * np.pi * pos) / (2 * np.pi)
+            val = coef * pos
+            sl = [slice(index, s - index) for s in shape]
+            sl[d] = slice(index, index + 1)
+            damp[tuple(sl)] += val
+            sl = [slice(index, s - index) for s in shape]
+            sl[d] = slice(shape[d] - index - 1, shape[d] - index)
+            damp[tuple(sl)] += val
+    damp *= vp_ext.astype(np.float32)
+    damp = 7 * damp * np.float32(dt)
+    return damp.astype(np.float32)
+
+
+def linear_stencil(coords, origin, spacing):
+    """Bi/trilinear corner indices and weights of Devito's linear SparseTimeFunction
+    (stride/physics/common/devito.py:580-653). ``coords`` are the float32 point
+    coordinates already shifted by +1e-3*h (iso_acoustic/devito.py:307-309).
+    Returns (base [n, dim] int64, weights [n, 2**dim] float64 in corner order
+    (bit d of the corner id = +1 along axis d, axis 0 is the most significant bit))."""
+    coords = np.asarray(coords, dtype=np.float32).astype(np.float64)
+    origin = np.asarray(origin, dtype=np.float64)
+    spacing = np.asarray(spacing, dtype=np.float64)
+    rel = (coords - origin) / spacing
+    base = np.floor(rel).astype(np.int64)
+    frac = rel - base
+    n, dim = coords.shape
+    ncorner = 2 ** dim
+    w = np.ones((n, ncorner), dtype=np.float64)
+    for c in range(ncorner):
+        for d in range(dim):
+            bit = (c >> (dim - 1 - d)) & 1
+            w[:, c] *= frac[:, d] if bit else (1.0 - frac[:, d])
+    return base, w
+
+
+def _corner_offsets(dim):
+    return [tuple((c >> (dim - 1 - d)) & 1 for d in range(dim)) for c in range(2 ** dim)]
+
+
+def select_kernel(dt, h, vp_max, dim):
+    """OT2/OT4 auto-selection (stride/physics/iso_acoustic/devito.py:1412-1431,1688-1689)."""
+    dt_ot2 = (2.0 / np.pi) * h / vp_max / np.sqrt(dim)
+    return 'OT2' if dt <= dt_ot2 else 'OT4'
+
+
+def bandwidth(signal, dt, cutoff=-10):
+    """-10 dB bandwidth (stride/utils/fft.py:97-141 with magnitude_spectrum in dB)."""
+    num = signal.shape[-1]
+    freqs = np.fft.rfftfreq(num, dt)
+    mag = np.abs(np.fft.rfft(signal, axis=-1, norm='forward'))
+    mag = 20 * np.log10((mag + 1e-31) / (np.max(mag) + 1e-31))
+    if mag.ndim > 1:
+        mag = np.mean(mag, axis=0)
+    above = np.nonzero(mag > cutoff)[0]
+    f_min = freqs[above[0]] if len(above) else 0
+    f_max = freqs[above[-1]] if len(above) else mag.shape[-1]
+    return f_min, freqs[np.argmax(mag)], f_max
+
+
+def select_undersampling(wavelets, dt):
+    """f = min(max(4, int(1/(4 f_max dt))), 10) (iso_acoustic/devito.py:1360-1375,1447-1456)."""
+    f_maxs = [bandwidth(w, dt)[2] for w in np.atleast_2d(wavelets) if np.any(w)]
+    f_max = np.max(f_maxs) if f_maxs else 0.05 / dt
+    return min(max(4, int((1 / (4 * f_max)) / dt)), 10)
+
+
+def tone_burst(centre_freq, n_cycles, n_samples, dt, offset=0):
+    """Gaussian tone burst (stride/utils/wavelets.py:6-53)."""
+    tone_length = n_cycles / centre_freq
+    t = np.linspace(0, tone_length, int(tone_length // dt + 1), endpoint=False)
+    sig = np.sin(2 * np.pi * centre_freq * t)
+    n_tone = sig.shape[0]
+    win = np.exp(-np.linspace(-3, 3, n_tone) ** 2 / 2)
+    sig = sig * win * scipy.signal.get_window(('tukey', 0.05), n_tone, False)
+    return np.pad(sig, ((offset, n_samples - offset - n_tone),), mode='constant')
+
+
+def tukey(nt, lo=0, hi=None, total=None):
+    """Source/adjoint-source time window (iso_acoustic/devito.py:505-509, 865-869)."""
+    hi = nt if hi is None else hi
+    total = nt if total is None else total
+    w = scipy.signal.get_window(('tukey', 0.001), hi - lo, False)
+    return np.pad(w, ((lo, total - hi),), mode='constant')
+
+
+# --------------------------------------------------------------------------------------
+# spatial operators on the extended grid, zero halo for the field (common/devito.py:805-841)
+# --------------------------------------------------------------------------------------
+
+def _shift(u, d, k):
+    """u[i+k] along axis d with zeros outside."""
+    out = np.zeros_like(u)
+    n = u.shape[d]
+    src = [slice(None)] * u.ndim
+    dst = [slice(None)] * u.ndim
+    if k >= 0:
+        src[d] = slice(k, n)
+        dst[d] = slice(0, n - k)
+    else:
+        src[d] = slice(0, n + k)
+        dst[d] = slice(-k, n)
+    out[tuple(dst)] = u[tuple(src)]
+    return out
+
+
+def _laplace(u, spacing, w2):
+    """10th-order Laplacian (Devito ``field.laplace``, iso_acoustic/devito.py:1652)."""
+    out = np.zeros_like(u)
+    for d in range(u.ndim):
+        h2 = u.dtype.type(spacing[d] ** 2)
+        acc = u.dtype.type(w2[0]) * u
+        for k in range(1, len(w2)):
+            acc = acc + u.dtype.type(w2[k]) * (_shift(u, d, k) + _shift(u, d, -k))
+        out = out + acc / h2
+    return out
+
+
+def _half_buoy(buoy, d, R):
+    """Buoyancy at half points j+1/2 along axis d for j = -R .. n+R-2: arithmetic mean of
+    the two neighbouring nodes, the nodes beyond the grid taking the edge value (materials
+    are padded with 'edge', common/devito.py:805-841; the averaging rule is unpinned)."""
+    n = buoy.shape[d]
+    j = np.arange(-R, n + R - 1)
+    b0 = np.take(buoy, np.clip(j, 0, n - 1), axis=d)
+    b1 = np.take(buoy, np.clip(j + 1, 0, n - 1), axis=d)
+    return buoy.dtype.type(0.5) * (b0 + b1)
+
+
+def _stagger_div_grad(u, spacing, ws, bhalf):
+    """sum_d D-_d[ b(i+1/2) D+_d u ] with 10th-order staggered weights
+    (iso_acoustic/devito.py:1655-1665). ``bhalf`` None means b == 1 (the rho-constant
+    branch, :1654)."""
+    R = len(ws)
+    out = np.zeros_like(u)
+    t = u.dtype.type
+    for d in range(u.ndim):
+        n = u.shape[d]
+        h = t(spacing[d])
+        pad = [(0, 0)] * u.ndim
+        pad[d] = (2 * R, 2 * R)
+        up = np.pad(u, pad)  # zero halo
+        m = n + 2 * R - 1    # half points j+1/2, j = -R .. n+R-2 (F index j+R)
+        F = None
+        for k in range(R):
+            a = [slice(None)] * u.ndim
+            b = [slice(None)] * u.ndim
+            a[d] = slice(R + 1 + k, R + 1 + k + m)
+            b[d] = slice(R - k, R - k + m)
+            term = t(ws[k]) * (up[tuple(a)] - up[tuple(b)])
+            F = term if F is None else F + term
+        F = F / h
+        if bhalf is not None:
+            F = F * bhalf[d]
+        acc = None
+        for k in range(R):
+            a = [slice(None)] * u.ndim
+            b = [slice(None)] * u.ndim
+            a[d] = slice(R + k, R + k + n)
+            b[d] = slice(R - k - 1, R - k - 1 + n)
+            term = t(ws[k]) * (F[tuple(a)] - F[tuple(b)])
+            acc = term if acc is None else acc + term
+        out = out + acc / h
+    return out
+
+
+class _Medium:
+    """Per-point material arrays on the extended grid in the reference's FP32 form
+    (iso_acoustic/devito.py:476-497)."""
+
+    def __init__(self, vp, rho, alpha_db, spacing, dtype):
+        t = dtype
+        self.vp = vp.astype(np.float32).astype(t)
+        self.vp2 = self.vp * self.vp
+        self.rho_mode = 0
+        self.rho = None
+        self.bhalf = None
+        if rho is not None:
+            rho32 = rho.astype(np.float32)
+            if np.isclose(np.min(rho32), np.max(rho32)):
+                self.rho_mode = 2  # staggered operator, no rho/buoyancy (:1472-1475,1654)
+            else:
+                self.rho_mode = 1
+                self.rho = rho32.astype(t)
+                buoy = (1 / rho32).astype(t)
+                self.bhalf = [_half_buoy(buoy, d, 5) for d in range(vp.ndim)]
+        self.alpha = None
+        if alpha_db is not None:
+            self.alpha = (alpha_db.astype(np.float32).astype(np.float64) * DB_TO_NEPER).astype(np.float32).astype(t)
+        self.spacing = spacing
+
+    def L(self, u, w2, ws):
+        if self.rho_mode == 0:
+            return self.vp2 * _laplace(u, self.spacing, w2)
+        if self.rho_mode == 2:
+            return self.vp2 * _stagger_div_grad(u, self.spacing, ws, None)
+        return self.vp2 * self.rho * _stagger_div_grad(u, self.spacing, ws, self.bhalf)
+
+
+def _Lt(med, u, kernel, dt, w2, ws):
+    """Spatial term of the time update: L u (OT2) or L u + dt^2/12 L(L u) (OT4),
+    iso_acoustic/devito.py:1503-1534,1632-1644; the intermediate has a zero halo."""
+    lap = med.L(u, w2, ws)
+    if kernel == 'OT2':
+        return lap
+    return lap + u.dtype.type(dt * dt / 12) * med.L(lap, w2, ws)
+
+
+def _update(med, damp, Lt, u, um, dt):
+    """Solve p.dt2 - Lt + 2 a vp p.dt + vp^2 (2 d p.dtc + d^2 p) = 0 for the new level
+    (iso_acoustic/devito.py:1575-1581, boundaries/devito.py:62-67). Centred first
+    derivatives; the backward direction uses the transposed (negated) ones, which is the
+    same formula with the roles of p[t+1] and p[t-1] exchanged."""
+    t = u.dtype.type
+    dt_ = t(dt)
+    beta = damp * med.vp2 / t(1)  # vp^2 d
+    if med.alpha is not None:
+        beta = beta + med.alpha * med.vp
+    beta = dt_ * beta
+    num = dt_ * dt_ * Lt + (t(2) - dt_ * dt_ * med.vp2 * damp * damp) * u - (t(1) - beta) * um
+    return num / (t(1) + beta)
+
+
+def _scatter(field, base, w, amp, dim):
+    offs = _corner_offsets(dim)
+    for c, off in enumerate(offs):
+        idx = tuple(base[:, d] + off[d] for d in range(dim))
+        np.add.at(field, idx, (w[:, c] * amp).astype(field.dtype))
+
+
+def _gather(field, base, w, dim):
+    offs = _corner_offsets(dim)
+    out = np.zeros(base.shape[0], dtype=np.float64)
+    for c, off in enumerate(offs):
+        idx = tuple(base[:, d] + off[d] for d in range(dim))
+        out += w[:, c] * field[idx]
+    return out
+
+
+def forward(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, origin,
+            rho=None, alpha=None, kernel=None, save=False, undersampling=4,
+            dtype=np.float32, diff_source=False):
+    """Forward modelling of one shot (iso_acoustic/devito.py:220-581).
+
+    Arrays are on the extended grid. ``wavelets`` [n_src, nt] raw (the Tukey window
+    of :505-509 is applied here). Returns traces [n_rec, nt] (float32) and, when
+    ``save``, the undersampled second time derivative snapshots [n_snap, *shape]
+    (:398-418, common/devito.py:492-578).
+    """
+    dim = vp.ndim
+    shape = vp.shape
+    h = max(spacing)
+    if kernel is None:
+        kernel = select_kernel(dt, h, float(np.max(vp)), dim)
+    w2 = second_derivative_weights()
+    ws = staggered_weights()
+    med = _Medium(vp, rho, alpha, spacing, dtype)
+    damp = damping_profile(shape, spacing, absorbing, vp, dt).astype(dtype)
+    eps = 1e-3 * np.asarray(spacing)
+    sb, sw = linear_stencil(np.asarray(src_coords, np.float32) + eps, origin, spacing)
+    rb, rw = linear_stencil(np.asarray(rec_coords, np.float32) + eps, origin, spacing)
+    wav = np.asarray(wavelets, np.float64)
+    if diff_source:
+        wav = np.gradient(wav, dt, axis=-1)
+    src = (wav.T * tukey(nt)[:, None]).astype(np.float32)  # [nt, n_src]
+    scale = 2 * dt * dt / h
+    if not diff_source:
+        scale /= dt
+    rec = np.zeros((nt, rb.shape[0]), dtype=np.float64)
+    f = undersampling
+    n_snap = (nt + f) // f + 1
+    snaps = np.zeros((n_snap,) + shape, dtype=np.float32) if save else None
+    pm = np.zeros(shape, dtype=dtype)
+    p = np.zeros(shape, dtype=dtype)
+    offs = _corner_offsets(dim)
+    for t in range(1, nt - 1):
+        Lt = _Lt(med, p, kernel, dt, w2, ws)
+        pn = _update(med, damp, Lt, p, pm, dt)
+        # src.inject(p.forward, src * 2 dt^2 vp / h / dt): vp at each corner (H1 reading)
+        for c, off in enumerate(offs):
+            idx = tuple(sb[:, d] + off[d] for d in range(dim))
+            amp = src[t].astype(np.float64) * scale * med.vp[idx].astype(np.float64)
+            np.add.at(pn, idx, (sw[:, c] * amp).astype(dtype))
+        rec[t] = _gather(pn, rb, rw, dim)
+        if save and t % f == 0:
+            snaps[t // f] = (pn - 2 * p + pm) / dtype(dt * dt)
+        pm, p = p, pn
+    return rec.T.astype(np.float32), snaps
+
+
+def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
+            rho=None, alpha=None, kernel=None, undersampling=4, dtype=np.float32):
+    """Reverse-time adjoint and vp imaging condition of the reference
+    (iso_acoustic/devito.py:689-920, 985-1043): backward update of p_a[t-1],
+    injection of -res[t] dt^2 vp^2 at the receivers (fw3d_mode, :725,748-753), and on
+    t % f == 0 in the interior: grad += snap[t/f] p_a[t], prec += snap[t/f]^2.
+    Returns raw (grad, prec) on the extended grid (zero outside the interior)."""
+    dim = vp.ndim
+    shape = vp.shape
+    h = max(spacing)
+    if kernel is None:
+        kernel = select_kernel(dt, h, float(np.max(vp)), dim)
+    w2 = second_derivative_weights()
+    ws = staggered_weights()
+    med = _Medium(vp, rho, alpha, spacing, dtype)
+    damp = damping_profile(shape, spacing, absorbing, vp, dt).astype(dtype)
+    eps = 1e-3 * np.asarray(spacing)
+    rb, rw = linear_stencil(np.asarray(rec_coords, np.float32) + eps, origin, spacing)
+    res = (np.asarray(residual, np.float64).T * tukey(nt)[:, None]).astype(np.float32)
+    f = undersampling
+    interior = tuple(slice(a, n - a) for a, n in zip(absorbing, shape))
+    grad = np.zeros(shape, dtype=np.float64)
+    prec = np.zeros(shape, dtype=np.float64)
+    qp = np.zeros(shape, dtype=dtype)  # p_a[t+1]
+    q = np.zeros(shape, dtype=dtype)   # p_a[t]
+    offs = _corner_offsets(dim)
+    for t in range(nt - 1 - f, 0, -1):
+        Lt = _Lt(med, q, kernel, dt, w2, ws)
+        qn = _update(med, damp, Lt, q, qp, dt)
+        for c, off in enumerate(offs):
+            idx = tuple(rb[:, d] + off[d] for d in range(dim))
+            amp = -res[t].astype(np.float64) * dt * dt * med.vp2[idx].astype(np.float64)
+            np.add.at(qn, idx, (rw[:, c] * amp).astype(dtype))
+        if t % f == 0:
+            s = snaps[t // f].astype(np.float64)
+            grad[interior] += (s * q.astype(np.float64))[interior]
+            prec[interior] += (s * s)[interior]
+        qp, q = q, qn
+    return grad.astype(np.float32), prec.astype(np.float32)
+
+
+def grad_vp_chain(grad, prec, vp_inner, slowness=True):
+    """get_grad_vp chain rule on the inner grid (iso_acoustic/devito.py:1045-1081).
+    The non-slowness preconditioner keeps the reference's ``(2/vp)**3**2`` precedence."""
+    g = grad.astype(np.float32).copy()
+    p = prec.astype(np.float32).copy()
+    vp = vp_inner.astype(np.float32)
+    if slowness:
+        g *= +1 / vp
+        p *= (1 / vp) ** 2
+    else:
+        g *= -2 / vp ** 3
+        p *= (2 / vp) ** 3 ** 2
+    return g, p
