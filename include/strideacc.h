@@ -1,0 +1,112 @@
+/*
+ * strideacc.h -- C ABI of the GB300 iso-acoustic FDTD library (libstrideacc.so).
+ *
+ * The library replaces the Devito-generated time loop that Stride's
+ * IsoAcousticDevito builds and runs per shot. Each entry point names the
+ * reference interface it stands in for (paths relative to the Stride
+ * repository root). Every call returns an int status: SA_OK (0) or a negative
+ * SA_E* code; sa_last_error() gives the message of the last failure on the
+ * calling thread. No exception crosses the ABI. A plan is not thread-safe:
+ * use one plan per host thread / stream.
+ *
+ * Pointers marked "host or device" are classified with cudaPointerGetAttributes:
+ * device (or managed) pointers are used in place, host pointers are copied on
+ * the call's stream (pageable or pinned).
+ */
+#ifndef STRIDEACC_H
+#define STRIDEACC_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SA_OK 0
+#define SA_E_INVALID (-1)     /* bad argument, shape or state (reference: ValueError) */
+#define SA_E_UNSUPPORTED (-2) /* option the reference rejects or this build lacks (NotImplementedError) */
+#define SA_E_CUDA (-3)        /* CUDA runtime error */
+#define SA_E_NOMEM (-4)       /* device allocation failed */
+#define SA_E_TIMEOUT (-5)     /* a bounded device wait gave up (error flag set by a kernel) */
+
+#define SA_KERNEL_OT2 2
+#define SA_KERNEL_OT4 4
+
+#define SA_DENSITY_NONE 0     /* rho not given: vp^2 * laplace(p) */
+#define SA_DENSITY_VARIABLE 1 /* vp^2 rho div(b grad p), staggered, b = 1/rho */
+#define SA_DENSITY_CONSTANT 2 /* rho given but constant: vp^2 div(grad p), staggered */
+
+#define SA_SAVE_NONE 0        /* forward only */
+#define SA_SAVE_SNAPSHOTS 1   /* store p.dt2 every f steps (reference algorithm) */
+
+#define SA_GRAD_PARITY 0      /* reference imaging condition: sum_{t%f==0} p_tt * p_a, interior only */
+
+/* Plan description (stride/physics/iso_acoustic/devito.py:119-183 defaults; shapes are the
+ * extended grid of stride/problem/domain.py:48-74). */
+typedef struct sa_desc {
+    int dim;               /* 2 or 3 */
+    int shape[3];          /* extended grid shape (x, y, z), z unused in 2D; last axis contiguous */
+    double spacing[3];     /* metres */
+    int extra[3];          /* padding cells per side: pml origin = -extra * spacing */
+    int absorbing[3];      /* sponge cells per side (<= extra) */
+    double dt;             /* seconds */
+    int nt;                /* time samples (time.extended_num) */
+    int kernel;            /* SA_KERNEL_OT2 or SA_KERNEL_OT4 */
+    int density;           /* SA_DENSITY_* */
+    int attenuation;       /* 0 none, 1 alpha given with attenuation power 0 */
+    int undersampling;     /* f of the saved wavefield, >= 1 */
+    int max_shots;         /* shots advanced together per launch */
+} sa_desc;
+
+typedef struct sa_plan sa_plan;
+
+/* Creates a plan: validates the description and allocates the per-shot wavefields.
+ * Replaces OperatorDevito.set_operator/compile (stride/physics/common/devito.py:909-1023). */
+int sa_plan_create(const sa_desc* desc, sa_plan** out);
+
+/* Frees every device buffer the plan owns (GridDevito.deallocate, common/devito.py:700-741). */
+int sa_plan_destroy(sa_plan* plan);
+
+/* Medium on the extended grid, C order, host or device float32: vp [m/s], rho [kg/m^3]
+ * (NULL when desc.density == NONE), alpha [dB/cm] (NULL when desc.attenuation == 0).
+ * Mirrors the vp/rho/buoy/alpha fills of before_forward (iso_acoustic/devito.py:476-497):
+ * buoyancy is 1/rho and alpha is converted to Np/m with 100/(20 log10 e). */
+int sa_set_medium(sa_plan* plan, const float* vp, const float* rho, const float* alpha);
+
+/* Geometry of n_shots shots in CSR form (uneven counts allowed). src_offsets/rec_offsets have
+ * n_shots+1 entries; src_xyz/rec_xyz are [total, dim] float32 coordinates in the inner-domain
+ * frame (metres), already shifted by +1e-3*h as before_forward does (devito.py:307-309).
+ * Host pointers. Replaces the src/rec SparseTimeFunction set-up (common/devito.py:580-653). */
+int sa_set_geometry(sa_plan* plan, int n_shots, const int* src_offsets, const float* src_xyz,
+                    const int* rec_offsets, const float* rec_xyz);
+
+/* Forward modelling of every shot of the geometry. wavelets [n_src_total, nt] float32 are
+ * the source samples as the reference stores them in src.data (Tukey-windowed; for
+ * diff_source the caller passes dt * d/dt of the wavelet). traces [n_rec_total, nt] float32
+ * receive rec.data.T (rows 0 and nt-1 of each trace are zero as in the reference's
+ * time_m=1, time_M=nt-2 loop). save_mode SA_SAVE_SNAPSHOTS keeps p.dt2 every f steps for
+ * sa_adjoint. Host or device pointers; stream is a cudaStream_t (NULL = legacy default).
+ * Replaces run_forward/after_forward (iso_acoustic/devito.py:515-685). */
+int sa_forward(sa_plan* plan, const float* wavelets, float* traces, int save_mode, void* stream);
+
+/* Adjoint of every shot: residuals [n_rec_total, nt] float32, the adjoint source as the
+ * reference stores it in rec.data.T (Tukey-windowed as before_adjoint does, devito.py:863-869).
+ * grad_vp/prec_vp [N] float32 on the extended grid receive the raw imaging condition summed
+ * over the shots (Devito grad_vp/prec_vp data, zero outside the interior) before the
+ * get_grad_vp chain rule. grad_mode SA_GRAD_PARITY. Requires a prior sa_forward with
+ * SA_SAVE_SNAPSHOTS. Replaces run_adjoint/after_adjoint (devito.py:875-981). */
+int sa_adjoint(sa_plan* plan, const float* residuals, float* grad_vp, float* prec_vp, int grad_mode,
+               void* stream);
+
+/* Picks the CTA width and row chunking for the current geometry by timing the candidates
+ * (no counterpart in the reference, whose Devito autotuner is optional: common/devito.py:1043). */
+int sa_autotune(sa_plan* plan, void* stream);
+
+/* Copies the message of the last failed call on this thread (NUL-terminated, truncated to len). */
+int sa_last_error(char* buf, int len);
+
+/* Kernel launches the last sa_forward/sa_adjoint issued (for throughput accounting). */
+long long sa_launch_count(const sa_plan* plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,178 @@
+"""ctypes binding of libstrideacc.so (declared in include/strideacc.h).
+
+The library is the only compute path: loading fails loudly when it has not been built
+(``python -m stride_gb300.build`` or ``__graft_entry__.build()``); there is no CPU fallback.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, '_build', 'libstrideacc.so')
+
+SA_OK = 0
+SA_E_INVALID = -1
+SA_E_UNSUPPORTED = -2
+SA_E_CUDA = -3
+SA_E_NOMEM = -4
+SA_E_TIMEOUT = -5
+
+SA_KERNEL_OT2 = 2
+SA_KERNEL_OT4 = 4
+SA_DENSITY_NONE = 0
+SA_DENSITY_VARIABLE = 1
+SA_DENSITY_CONSTANT = 2
+SA_SAVE_NONE = 0
+SA_SAVE_SNAPSHOTS = 1
+SA_GRAD_PARITY = 0
+
+# every symbol include/strideacc.h declares
+EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometry', 'sa_forward',
+           'sa_adjoint', 'sa_autotune', 'sa_last_error', 'sa_launch_count')
+
+
+class SaDesc(ctypes.Structure):
+    _fields_ = [('dim', ctypes.c_int), ('shape', ctypes.c_int * 3), ('spacing', ctypes.c_double * 3),
+                ('extra', ctypes.c_int * 3), ('absorbing', ctypes.c_int * 3), ('dt', ctypes.c_double),
+                ('nt', ctypes.c_int), ('kernel', ctypes.c_int), ('density', ctypes.c_int),
+                ('attenuation', ctypes.c_int), ('undersampling', ctypes.c_int), ('max_shots', ctypes.c_int)]
+
+
+class StrideAccError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__('strideacc error %d: %s' % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def load():
+    """Loads the library (raises ImportError when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError('libstrideacc.so is not built (%s); run stride_gb300.build.build()' % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    I = ctypes.c_int
+    lib.sa_plan_create.argtypes = [ctypes.POINTER(SaDesc), ctypes.POINTER(P)]
+    lib.sa_plan_destroy.argtypes = [P]
+    lib.sa_set_medium.argtypes = [P, P, P, P]
+    lib.sa_set_geometry.argtypes = [P, I, P, P, P, P]
+    lib.sa_forward.argtypes = [P, P, P, I, P]
+    lib.sa_adjoint.argtypes = [P, P, P, P, I, P]
+    lib.sa_autotune.argtypes = [P, P]
+    lib.sa_last_error.argtypes = [ctypes.c_char_p, I]
+    lib.sa_launch_count.argtypes = [P]
+    lib.sa_launch_count.restype = ctypes.c_longlong
+    for name in EXPORTS:
+        if name not in ('sa_launch_count',):
+            getattr(lib, name).restype = I
+    _lib = lib
+    return lib
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(512)
+    load().sa_last_error(buf, 512)
+    return buf.value.decode(errors='replace')
+
+
+def check(code):
+    if code != SA_OK:
+        raise StrideAccError(code, last_error())
+
+
+def _ptr(x):
+    """Raw pointer of a numpy array or a torch tensor (None stays NULL)."""
+    if x is None:
+        return None
+    if isinstance(x, np.ndarray):
+        if not x.flags['C_CONTIGUOUS']:
+            raise ValueError('array must be C-contiguous')
+        return x.ctypes.data_as(ctypes.c_void_p)
+    if hasattr(x, 'data_ptr'):
+        if not x.is_contiguous():
+            raise ValueError('tensor must be contiguous')
+        return ctypes.c_void_p(x.data_ptr())
+    raise TypeError('unsupported buffer type %r' % type(x))
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    if hasattr(stream, 'cuda_stream'):
+        return ctypes.c_void_p(stream.cuda_stream)
+    return ctypes.c_void_p(int(stream))
+
+
+class Plan:
+    """Owner of one sa_plan (one batch of shots on one grid)."""
+
+    def __init__(self, dim, shape, spacing, extra, absorbing, dt, nt, kernel='OT4', density=SA_DENSITY_NONE,
+                 attenuation=False, undersampling=4, max_shots=1):
+        lib = load()
+        d = SaDesc()
+        d.dim = dim
+        for i in range(3):
+            d.shape[i] = int(shape[i]) if i < dim else 1
+            d.spacing[i] = float(spacing[i]) if i < dim else 1.0
+            d.extra[i] = int(extra[i]) if i < dim else 0
+            d.absorbing[i] = int(absorbing[i]) if i < dim else 0
+        d.dt = float(dt)
+        d.nt = int(nt)
+        d.kernel = SA_KERNEL_OT4 if kernel == 'OT4' else SA_KERNEL_OT2
+        d.density = int(density)
+        d.attenuation = int(bool(attenuation))
+        d.undersampling = int(undersampling)
+        d.max_shots = int(max_shots)
+        self.desc = d
+        h = ctypes.c_void_p()
+        check(lib.sa_plan_create(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+        self.dim = dim
+        self.nt = int(nt)
+        self.n_src = 0
+        self.n_rec = 0
+
+    def close(self):
+        if getattr(self, '_h', None) is not None and self._h.value:
+            load().sa_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_medium(self, vp, rho=None, alpha=None):
+        check(load().sa_set_medium(self._h, _ptr(vp), _ptr(rho), _ptr(alpha)))
+
+    def set_geometry(self, src_offsets, src_xyz, rec_offsets, rec_xyz):
+        so = np.ascontiguousarray(src_offsets, dtype=np.int32)
+        ro = np.ascontiguousarray(rec_offsets, dtype=np.int32)
+        sx = np.ascontiguousarray(src_xyz, dtype=np.float32).reshape(-1, self.dim)
+        rx = np.ascontiguousarray(rec_xyz, dtype=np.float32).reshape(-1, self.dim)
+        check(load().sa_set_geometry(self._h, len(so) - 1, _ptr(so), _ptr(sx), _ptr(ro), _ptr(rx)))
+        self.n_src = int(so[-1])
+        self.n_rec = int(ro[-1])
+
+    def forward(self, wavelets, traces, save=False, stream=None):
+        check(load().sa_forward(self._h, _ptr(wavelets), _ptr(traces),
+                                SA_SAVE_SNAPSHOTS if save else SA_SAVE_NONE, _stream(stream)))
+
+    def adjoint(self, residuals, grad, prec, stream=None):
+        check(load().sa_adjoint(self._h, _ptr(residuals), _ptr(grad), _ptr(prec), SA_GRAD_PARITY,
+                                _stream(stream)))
+
+    def autotune(self, stream=None):
+        check(load().sa_autotune(self._h, _stream(stream)))
+
+    @property
+    def launches(self):
+        return int(load().sa_launch_count(self._h))

@@ -1,0 +1,23 @@
+// Instantiations of the 2D step kernel for operator kind 2 (0 laplace, 1 variable density,
+// 2 constant density); split per kind so the build compiles them in parallel.
+#include "fdtd2d.cuh"
+#include "launch.h"
+
+namespace sa {
+
+template <bool OT4, int NT>
+static cudaError_t go(dim3 grid, cudaStream_t s, const Step2D& a) {
+    fdtd2d_step<2, OT4, NT><<<grid, NT, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step2d_k2(bool ot4, int nt_threads, dim3 grid, cudaStream_t s, const Step2D& a) {
+    switch (nt_threads) {
+        case 128: return ot4 ? go<true, 128>(grid, s, a) : go<false, 128>(grid, s, a);
+        case 160: return ot4 ? go<true, 160>(grid, s, a) : go<false, 160>(grid, s, a);
+        case 256: return ot4 ? go<true, 256>(grid, s, a) : go<false, 256>(grid, s, a);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace sa

@@ -1,0 +1,122 @@
+// Small device helpers of the plan: medium preparation, sparse-trace transposes, the final
+// receiver gather and the reduction of per-shot gradients.
+#include "fdtd2d.cuh"
+#include "helpers.h"
+
+namespace sa {
+
+// vp, rho, alpha (dB/cm) on the unpadded extended grid -> pitched W, vp, alpha (Np/m), and
+// buoyancy b = 1/rho into a pitched scratch (iso_acoustic/devito.py:476-497).
+__global__ void k_medium2d(const float* __restrict__ vp_in, const float* __restrict__ rho_in,
+                           const float* __restrict__ alpha_in, int nx, int ny, int pitch, int density,
+                           double db_to_np, float* W, float* vp, float* alpha, float* buoy) {
+    const long long n = (long long)nx * ny;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(q / ny), y = (int)(q % ny);
+        const long long p = (long long)x * pitch + y;
+        const float v = vp_in[q];
+        vp[p] = v;
+        float w = v * v;
+        if (density == 1) {
+            const float r = rho_in[q];
+            w = w * r;
+            buoy[p] = 1.f / r;
+        }
+        W[p] = w;
+        if (alpha_in) alpha[p] = (float)((double)alpha_in[q] * db_to_np);
+    }
+}
+
+// Buoyancy at half points: bxh[(x+5)*pitch + y] = b(x+1/2, y) for x = -5..nx+3 and
+// byh[x*pitch_b + y + 5] = b(x, y+1/2) for y = -5..ny+3; nodes beyond the grid take the edge
+// value as the reference's edge-padded halo (common/devito.py:805-841), the half point is the
+// arithmetic mean of its two nodes.
+__global__ void k_bhalf2d(const float* __restrict__ buoy, int nx, int ny, int pitch, int pitch_b, float* bxh,
+                          float* byh) {
+    const long long nxa = (long long)(nx + 9) * ny;
+    const long long nya = (long long)nx * (ny + 9);
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nxa + nya;
+         q += (long long)gridDim.x * blockDim.x) {
+        if (q < nxa) {
+            const int xr = (int)(q / ny), y = (int)(q % ny);
+            const int x = xr - 5;
+            const int x0 = min(max(x, 0), nx - 1), x1 = min(max(x + 1, 0), nx - 1);
+            bxh[(long long)xr * pitch + y] = 0.5f * (buoy[(long long)x0 * pitch + y] + buoy[(long long)x1 * pitch + y]);
+        } else {
+            const long long r = q - nxa;
+            const int x = (int)(r / (ny + 9)), yr = (int)(r % (ny + 9));
+            const int y = yr - 5;
+            const int y0 = min(max(y, 0), ny - 1), y1 = min(max(y + 1, 0), ny - 1);
+            byh[(long long)x * pitch_b + yr] = 0.5f * (buoy[(long long)x * pitch + y0] + buoy[(long long)x * pitch + y1]);
+        }
+    }
+}
+
+// out[c][r] = in[r][c] for an rows x cols matrix (both dense).
+__global__ void k_transpose(const float* __restrict__ in, int rows, int cols, float* __restrict__ out) {
+    __shared__ float tile[32][33];
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int r = by + k, c = bx + threadIdx.x;
+        if (r < rows && c < cols) tile[k][threadIdx.x] = in[(long long)r * cols + c];
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int c = bx + k, r = by + threadIdx.x;
+        if (r < rows && c < cols) out[(long long)c * rows + r] = tile[threadIdx.x][k];
+    }
+}
+
+__global__ void gather_final2d(const float* __restrict__ field, long long shot_stride, int pitch,
+                               const Gather* __restrict__ g, int n, float* out, int ld, int trow) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const Gather G = g[e];
+    const float* f = field + (long long)G.pad * shot_stride;
+    const long long i0 = (long long)G.row * pitch + G.col, i1 = i0 + pitch;
+    out[(long long)trow * ld + G.point] = G.w00 * f[i0] + G.w01 * f[i0 + 1] + G.w10 * f[i1] + G.w11 * f[i1 + 1];
+}
+
+__global__ void reduce_shots2d(const float* __restrict__ buf, long long shot_stride, int nshots, int nx, int ny,
+                               int pitch, float* __restrict__ out) {
+    const long long n = (long long)nx * ny;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(q / ny), y = (int)(q % ny);
+        const long long p = (long long)x * pitch + y;
+        float s = 0.f;
+        for (int b = 0; b < nshots; b++) s += buf[(long long)b * shot_stride + p];
+        out[q] = s;
+    }
+}
+
+cudaError_t medium2d(const float* vp_in, const float* rho_in, const float* alpha_in, int nx, int ny, int pitch,
+                     int pitch_b, int density, double db_to_np, float* W, float* vp, float* alpha, float* buoy,
+                     float* bxh, float* byh, cudaStream_t s) {
+    k_medium2d<<<1024, 256, 0, s>>>(vp_in, rho_in, alpha_in, nx, ny, pitch, density, db_to_np, W, vp, alpha, buoy);
+    if (density == 1) k_bhalf2d<<<1024, 256, 0, s>>>(buoy, nx, ny, pitch, pitch_b, bxh, byh);
+    return cudaGetLastError();
+}
+
+cudaError_t transpose(const float* in, int rows, int cols, float* out, cudaStream_t s) {
+    if (rows == 0 || cols == 0) return cudaSuccess;
+    dim3 grid((cols + 31) / 32, (rows + 31) / 32);
+    k_transpose<<<grid, dim3(32, 8), 0, s>>>(in, rows, cols, out);
+    return cudaGetLastError();
+}
+
+cudaError_t final_gather2d(const float* field, long long shot_stride, int pitch, const Gather* g, int n, float* out,
+                           int ld, int trow, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    gather_final2d<<<(n + 127) / 128, 128, 0, s>>>(field, shot_stride, pitch, g, n, out, ld, trow);
+    return cudaGetLastError();
+}
+
+cudaError_t reduce_shots(const float* buf, long long shot_stride, int nshots, int nx, int ny, int pitch, float* out,
+                         cudaStream_t s) {
+    reduce_shots2d<<<1024, 256, 0, s>>>(buf, shot_stride, nshots, nx, ny, pitch, out);
+    return cudaGetLastError();
+}
+
+}  // namespace sa

@@ -1,0 +1,720 @@
+// libstrideacc: C ABI of the GB300 iso-acoustic FDTD path (declarations and reference
+// citations in include/strideacc.h). A plan owns the device state of a batch of shots: two
+// wavefield levels per shot, the medium, per-CTA source/receiver lists, the undersampled
+// wavefield of the reference's gradient algorithm and per-shot gradient accumulators. The
+// time loop is captured once into a CUDA graph per mode and replayed.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/strideacc.h"
+#include "common.cuh"
+#include "helpers.h"
+#include "launch.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(x)                                                                                    \
+    do {                                                                                         \
+        cudaError_t e_ = (x);                                                                    \
+        if (e_ != cudaSuccess) return fail(SA_E_CUDA, "%s: %s", #x, cudaGetErrorString(e_));     \
+    } while (0)
+
+#define CKR(x)                                                                                   \
+    do {                                                                                         \
+        int r_ = (x);                                                                            \
+        if (r_ != SA_OK) return r_;                                                              \
+    } while (0)
+
+bool is_device(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+template <class T>
+int ensure(T** ptr, size_t* cap, size_t n) {
+    if (n <= *cap && *ptr) return SA_OK;
+    if (*ptr) cudaFree(*ptr);
+    *ptr = nullptr;
+    *cap = 0;
+    if (n == 0) n = 1;
+    if (cudaMalloc((void**)ptr, n * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return fail(SA_E_NOMEM, "device allocation of %zu bytes failed", n * sizeof(T));
+    }
+    *cap = n;
+    return SA_OK;
+}
+
+constexpr double kDbToNeper = 100.0 / (20.0 * 0.43429448190325176);  // 100 / (20 log10 e)
+
+}  // namespace
+
+struct sa_plan {
+    sa_desc d{};
+    int nx = 0, ny = 0, pitch = 0, pitch_b = 0;
+    long long shot_stride = 0;
+    int kind = 0;
+    bool ot4 = true;
+    float* field[2] = {nullptr, nullptr};
+    size_t field_cap[2] = {0, 0};
+    float *W = nullptr, *vp = nullptr, *alpha = nullptr, *buoy = nullptr, *bxh = nullptr, *byh = nullptr;
+    size_t cap_W = 0, cap_vp = 0, cap_alpha = 0, cap_buoy = 0, cap_bxh = 0, cap_byh = 0;
+    float* medium_stage = nullptr;
+    size_t cap_medium_stage = 0;
+    bool medium_set = false;
+    // geometry (host copy)
+    int n_shots = 0, n_src = 0, n_rec = 0;
+    std::vector<int> src_off, rec_off;
+    std::vector<int> src_bx, src_by, rec_bx, rec_by;
+    std::vector<double> src_fx, src_fy, rec_fx, rec_fy;
+    bool geometry_set = false;
+    // per-CTA lists for the current layout
+    sa::Inject *inj_src = nullptr, *inj_rec = nullptr;
+    int *inj_src_off = nullptr, *inj_rec_off = nullptr, *gat_off = nullptr;
+    sa::Gather *gat = nullptr, *gat_flat = nullptr;
+    size_t cap_inj_src = 0, cap_inj_rec = 0, cap_inj_src_off = 0, cap_inj_rec_off = 0, cap_gat_off = 0, cap_gat = 0,
+           cap_gat_flat = 0;
+    // sparse traces, time-major
+    float *src_amp = nullptr, *rec_amp = nullptr, *stage = nullptr;
+    size_t cap_src_amp = 0, cap_rec_amp = 0, cap_stage = 0;
+    // saved wavefield and gradient accumulators
+    float* snaps = nullptr;
+    size_t cap_snaps = 0;
+    int n_snap = 0;
+    long long snap_stride = 0, snap_shot_stride = 0;
+    bool snaps_valid = false;
+    float *gradb = nullptr, *precb = nullptr;
+    size_t cap_gradb = 0, cap_precb = 0;
+    // layout
+    int NT = 128, by = 110, chunk_rows = 1, nstrips = 1, nchunks = 1;
+    bool layout_fixed = false;
+    float sx[sa::MAX_ABS] = {}, sy[sa::MAX_ABS] = {};
+    // graphs
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t g_fwd[2] = {nullptr, nullptr};
+    cudaGraphExec_t g_adj = nullptr;
+    bool use_graphs = true;
+    long long launches = 0;
+};
+
+namespace {
+
+int halo1(const sa_plan* p) { return p->ot4 ? (p->kind == 0 ? 5 : 9) : 0; }
+int radius(const sa_plan* p) { return p->kind == 0 ? 5 : 9; }
+
+void drop_graphs(sa_plan* p) {
+    for (auto& g : p->g_fwd)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    if (p->g_adj) {
+        cudaGraphExecDestroy(p->g_adj);
+        p->g_adj = nullptr;
+    }
+}
+
+// Sponge ramp of Boundary.damping for one axis (stride/physics/boundaries/boundary.py:98-151),
+// before the multiplication by vp and 7 dt (done per point in the kernel).
+void damping_table(int A, double h, double refl, float* out) {
+    for (int e = 0; e < sa::MAX_ABS; e++) out[e] = 0.f;
+    if (A <= 0) return;
+    double coef = (2 + 1) / 2.0 * std::log(1.0 / refl);
+    coef = A > 15 ? coef / (A * h) : 0.67 / h;
+    for (int e = 0; e < A; e++) {
+        double pos = std::fabs((A - e - 1) / (double)(A - 1));
+        pos = pos - std::sin(2 * M_PI * pos) / (2 * M_PI);
+        out[e] = (float)(coef * pos);
+    }
+}
+
+void default_layout(sa_plan* p) {
+    if (p->layout_fixed) return;
+    const int H1 = halo1(p);
+    int best_nt = 128, best_cost = 1 << 30;
+    for (int nt : {128, 160, 256}) {
+        const int bymax = nt - 2 * H1;
+        const int strips = (p->ny + bymax - 1) / bymax;
+        const int cost = strips * nt;
+        if (cost < best_cost) {
+            best_cost = cost;
+            best_nt = nt;
+        }
+    }
+    p->NT = best_nt;
+    const int bymax = p->NT - 2 * H1;
+    p->nstrips = (p->ny + bymax - 1) / bymax;
+    p->by = (p->ny + p->nstrips - 1) / p->nstrips;
+    // enough CTAs to fill 152 SMs several times; each chunk keeps >= 4 pipeline depths of rows
+    const int S = p->ot4 ? 2 : 1;
+    const int minrows = 4 * S * radius(p);
+    const int shots = std::max(1, p->n_shots);
+    const int target = 152 * 6;
+    int nchunks = (target + p->nstrips * shots - 1) / (p->nstrips * shots);
+    nchunks = std::max(1, std::min(nchunks, p->nx / minrows));
+    p->chunk_rows = (p->nx + nchunks - 1) / nchunks;
+    p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
+}
+
+struct HostInject {
+    int cta, row, col, point;
+    float coef;
+};
+
+// Builds the per-CTA source/receiver lists for the current layout.
+int build_lists(sa_plan* p) {
+    drop_graphs(p);
+    const int nc = p->nchunks, ns = p->nstrips;
+    const int ncta = p->n_shots * nc * ns;
+    const double h = std::max(p->d.spacing[0], p->d.spacing[1]);
+    const double dt = p->d.dt;
+    auto cta_of = [&](int shot, int x, int y) { return (shot * nc + x / p->chunk_rows) * ns + y / p->by; };
+    auto make_inj = [&](const std::vector<int>& off, const std::vector<int>& bx, const std::vector<int>& by,
+                        const std::vector<double>& fx, const std::vector<double>& fy, double scale,
+                        std::vector<HostInject>& out) {
+        out.clear();
+        for (int s = 0; s < p->n_shots; s++)
+            for (int i = off[s]; i < off[s + 1]; i++)
+                for (int cx = 0; cx < 2; cx++)
+                    for (int cy = 0; cy < 2; cy++) {
+                        const int x = bx[i] + cx, y = by[i] + cy;
+                        const double w = (cx ? fx[i] : 1.0 - fx[i]) * (cy ? fy[i] : 1.0 - fy[i]);
+                        out.push_back({cta_of(s, x, y), x, y, i, (float)(w * scale)});
+                    }
+        std::stable_sort(out.begin(), out.end(), [](const HostInject& a, const HostInject& b) {
+            return a.cta != b.cta ? a.cta < b.cta : a.row < b.row;
+        });
+    };
+    auto upload_inj = [&](const std::vector<HostInject>& in, sa::Inject** dl, size_t* capl, int** doff,
+                          size_t* capo) -> int {
+        std::vector<sa::Inject> l(in.size());
+        std::vector<int> off(ncta + 1, 0);
+        for (size_t k = 0; k < in.size(); k++) {
+            l[k] = {in[k].row, in[k].col, in[k].point, in[k].coef};
+            off[in[k].cta + 1]++;
+        }
+        for (int c = 0; c < ncta; c++) off[c + 1] += off[c];
+        CKR(ensure(dl, capl, l.size()));
+        CKR(ensure(doff, capo, off.size()));
+        if (!l.empty()) CK(cudaMemcpy(*dl, l.data(), l.size() * sizeof(sa::Inject), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(*doff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
+        return SA_OK;
+    };
+    std::vector<HostInject> tmp;
+    // forward source: src * 2 dt^2 vp / h / dt (iso_acoustic/devito.py:349-363), vp in the kernel
+    make_inj(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, 2.0 * dt / h, tmp);
+    CKR(upload_inj(tmp, &p->inj_src, &p->cap_inj_src, &p->inj_src_off, &p->cap_inj_src_off));
+    // adjoint receiver: -rec * dt^2 * vp^2 (devito.py:748-753), vp^2 in the kernel
+    make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, -dt * dt, tmp);
+    CKR(upload_inj(tmp, &p->inj_rec, &p->cap_inj_rec, &p->inj_rec_off, &p->cap_inj_rec_off));
+    // receiver gathers, one per receiver, owned by the CTA of its base corner
+    std::vector<std::pair<int, sa::Gather>> g;
+    std::vector<sa::Gather> flat;
+    for (int s = 0; s < p->n_shots; s++)
+        for (int r = p->rec_off[s]; r < p->rec_off[s + 1]; r++) {
+            const double fx = p->rec_fx[r], fy = p->rec_fy[r];
+            sa::Gather G;
+            G.row = p->rec_bx[r];
+            G.col = p->rec_by[r];
+            G.point = r;
+            G.pad = s;
+            G.w00 = (float)((1 - fx) * (1 - fy));
+            G.w01 = (float)((1 - fx) * fy);
+            G.w10 = (float)(fx * (1 - fy));
+            G.w11 = (float)(fx * fy);
+            g.push_back({cta_of(s, G.row, G.col), G});
+            flat.push_back(G);
+        }
+    std::stable_sort(g.begin(), g.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    std::vector<sa::Gather> gl(g.size());
+    std::vector<int> goff(ncta + 1, 0);
+    for (size_t k = 0; k < g.size(); k++) {
+        gl[k] = g[k].second;
+        goff[g[k].first + 1]++;
+    }
+    for (int c = 0; c < ncta; c++) goff[c + 1] += goff[c];
+    CKR(ensure(&p->gat, &p->cap_gat, gl.size()));
+    CKR(ensure(&p->gat_off, &p->cap_gat_off, goff.size()));
+    CKR(ensure(&p->gat_flat, &p->cap_gat_flat, flat.size()));
+    if (!gl.empty()) CK(cudaMemcpy(p->gat, gl.data(), gl.size() * sizeof(sa::Gather), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(p->gat_off, goff.data(), goff.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (!flat.empty())
+        CK(cudaMemcpy(p->gat_flat, flat.data(), flat.size() * sizeof(sa::Gather), cudaMemcpyHostToDevice));
+    return SA_OK;
+}
+
+sa::Step2D base_args(const sa_plan* p) {
+    sa::Step2D a{};
+    a.nx = p->nx;
+    a.ny = p->ny;
+    a.pitch = p->pitch;
+    a.shot_stride = p->shot_stride;
+    a.chunk_rows = p->chunk_rows;
+    a.by = p->by;
+    a.W = p->W;
+    a.vp = p->vp;
+    a.alpha = p->d.attenuation ? p->alpha : nullptr;
+    a.bxh = p->bxh;
+    a.byh = p->byh;
+    a.pitch_b = p->pitch_b;
+    a.hx = (float)p->d.spacing[0];
+    a.hy = (float)p->d.spacing[1];
+    a.dt = (float)p->d.dt;
+    for (int e = 0; e < sa::MAX_ABS; e++) {
+        a.sx[e] = p->sx[e];
+        a.sy[e] = p->sy[e];
+    }
+    a.ax = p->d.absorbing[0];
+    a.ay = p->d.absorbing[1];
+    a.f = p->d.undersampling;
+    a.snaps = p->snaps;
+    a.snap_stride = p->snap_stride;
+    a.snap_shot_stride = p->snap_shot_stride;
+    a.gradb = p->gradb;
+    a.precb = p->precb;
+    a.ix0 = p->d.absorbing[0];
+    a.ix1 = p->nx - p->d.absorbing[0];
+    a.iy0 = p->d.absorbing[1];
+    a.iy1 = p->ny - p->d.absorbing[1];
+    return a;
+}
+
+// Issues the forward time loop t = 1..nt-2 (iso_acoustic/devito.py:575-581) on stream s.
+int issue_forward(sa_plan* p, bool save, cudaStream_t s) {
+    const size_t fbytes = (size_t)p->n_shots * p->shot_stride * sizeof(float);
+    CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
+    CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
+    CK(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * p->n_rec * sizeof(float), s));
+    sa::Step2D a = base_args(p);
+    a.adjoint = 0;
+    a.inj = p->n_src ? p->inj_src : nullptr;
+    a.inj_off = p->inj_src_off;
+    a.inj_amp = p->src_amp;
+    a.inj_ld = p->n_src;
+    a.inj_vp_power = 1;
+    a.gat_off = p->gat_off;
+    a.gat_out = p->rec_amp;
+    a.gat_ld = p->n_rec;
+    a.save = save ? 1 : 0;
+    a.grad = 0;
+    const dim3 grid(p->nstrips, p->nchunks, p->n_shots);
+    long long n = 0;
+    for (int t = 1; t <= p->d.nt - 2; t++) {
+        a.t = t;
+        a.cur = (t & 1) ? p->field[1] : p->field[0];
+        a.prev = (t & 1) ? p->field[0] : p->field[1];
+        a.gat = (t >= 2 && p->n_rec) ? p->gat : nullptr;
+        CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
+        n++;
+    }
+    // rec[nt-2] = interp(p[nt-1])
+    const int tl = p->d.nt - 1;
+    const float* last = (tl & 1) ? p->field[1] : p->field[0];
+    if (p->d.nt >= 3) {
+        CK(sa::final_gather2d(last, p->shot_stride, p->pitch, p->gat_flat, p->n_rec, p->rec_amp, p->n_rec, p->d.nt - 2,
+                              s));
+        n++;
+    }
+    p->launches = n;
+    return SA_OK;
+}
+
+// Issues the reverse-time adjoint loop t = nt-1-f .. 1 (devito.py:915-920).
+int issue_adjoint(sa_plan* p, cudaStream_t s) {
+    const size_t fbytes = (size_t)p->n_shots * p->shot_stride * sizeof(float);
+    CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
+    CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
+    CK(cudaMemsetAsync(p->gradb, 0, fbytes, s));
+    CK(cudaMemsetAsync(p->precb, 0, fbytes, s));
+    sa::Step2D a = base_args(p);
+    a.adjoint = 1;
+    a.inj = p->n_rec ? p->inj_rec : nullptr;
+    a.inj_off = p->inj_rec_off;
+    a.inj_amp = p->rec_amp;
+    a.inj_ld = p->n_rec;
+    a.inj_vp_power = 2;
+    a.gat = nullptr;
+    a.save = 0;
+    a.grad = 1;
+    const dim3 grid(p->nstrips, p->nchunks, p->n_shots);
+    const int T0 = p->d.nt - 1 - p->d.undersampling;
+    long long n = 0;
+    for (int t = T0; t >= 1; t--) {
+        a.t = t;
+        const bool even = ((T0 - t) & 1) == 0;
+        a.cur = even ? p->field[1] : p->field[0];
+        a.prev = even ? p->field[0] : p->field[1];
+        CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
+        n++;
+    }
+    p->launches = n;
+    return SA_OK;
+}
+
+// Runs `issue` through a cached CUDA graph (captured on the plan's own stream) or directly.
+template <class F>
+int run_loop(sa_plan* p, cudaGraphExec_t* slot, cudaStream_t s, F issue) {
+    if (!p->use_graphs) return issue(s);
+    if (!*slot) {
+        if (!p->cap) CK(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking));
+        CK(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
+        const int rc = issue(p->cap);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(p->cap, &graph);
+        if (rc != SA_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (ce != cudaSuccess) return fail(SA_E_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+        const cudaError_t ie = cudaGraphInstantiate(slot, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            *slot = nullptr;
+            return fail(SA_E_CUDA, "graph instantiate: %s", cudaGetErrorString(ie));
+        }
+    }
+    CK(cudaGraphLaunch(*slot, s));
+    return SA_OK;
+}
+
+// Copies an [rows, cols] user matrix (host or device) into the time-major [cols, rows] buffer.
+int load_transposed(sa_plan* p, const float* user, int rows, int cols, float* dst, cudaStream_t s) {
+    const size_t n = (size_t)rows * cols;
+    if (n == 0) return SA_OK;
+    const float* src = user;
+    if (!is_device(user)) {
+        CKR(ensure(&p->stage, &p->cap_stage, n));
+        CK(cudaMemcpyAsync(p->stage, user, n * sizeof(float), cudaMemcpyHostToDevice, s));
+        src = p->stage;
+    }
+    CK(sa::transpose(src, rows, cols, dst, s));
+    return SA_OK;
+}
+
+int store_transposed(sa_plan* p, const float* tm, int rows, int cols, float* user, cudaStream_t s) {
+    // tm is [rows(time), cols(points)] -> user [cols, rows]
+    const size_t n = (size_t)rows * cols;
+    if (n == 0) return SA_OK;
+    if (is_device(user)) {
+        CK(sa::transpose(tm, rows, cols, user, s));
+        return SA_OK;
+    }
+    CKR(ensure(&p->stage, &p->cap_stage, n));
+    CK(sa::transpose(tm, rows, cols, p->stage, s));
+    CK(cudaMemcpyAsync(user, p->stage, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return SA_OK;
+}
+
+int ensure_fields(sa_plan* p) {
+    const size_t n = (size_t)std::max(1, p->d.max_shots) * p->shot_stride;
+    CKR(ensure(&p->field[0], &p->field_cap[0], n));
+    CKR(ensure(&p->field[1], &p->field_cap[1], n));
+    return SA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sa_last_error(char* buf, int len) {
+    if (!buf || len <= 0) return SA_E_INVALID;
+    snprintf(buf, (size_t)len, "%s", g_err.c_str());
+    return SA_OK;
+}
+
+long long sa_launch_count(const sa_plan* p) { return p ? p->launches : -1; }
+
+int sa_plan_create(const sa_desc* desc, sa_plan** out) {
+    if (!desc || !out) return fail(SA_E_INVALID, "null argument");
+    *out = nullptr;
+    const sa_desc& d = *desc;
+    if (d.dim != 2) return fail(SA_E_UNSUPPORTED, "dim %d: this build implements the 2D operator", d.dim);
+    if (d.kernel != SA_KERNEL_OT2 && d.kernel != SA_KERNEL_OT4)
+        return fail(SA_E_INVALID, "Unrecognized kernel %d", d.kernel);
+    if (d.density < 0 || d.density > 2) return fail(SA_E_INVALID, "density mode %d", d.density);
+    if (d.nt < 3 || d.undersampling < 1 || d.max_shots < 1) return fail(SA_E_INVALID, "nt/undersampling/max_shots");
+    for (int a = 0; a < d.dim; a++) {
+        if (d.shape[a] < 24) return fail(SA_E_INVALID, "shape[%d] = %d is below 24 cells", a, d.shape[a]);
+        if (!(d.spacing[a] > 0)) return fail(SA_E_INVALID, "spacing[%d]", a);
+        if (d.absorbing[a] < 0 || d.absorbing[a] > d.extra[a] || d.absorbing[a] > sa::MAX_ABS ||
+            d.absorbing[a] == 1 || 2 * d.absorbing[a] > d.shape[a])
+            return fail(SA_E_INVALID, "absorbing[%d] = %d (extra %d)", a, d.absorbing[a], d.extra[a]);
+    }
+    if (!(d.dt > 0)) return fail(SA_E_INVALID, "dt");
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    sa_plan* p = new sa_plan();
+    p->d = d;
+    p->nx = d.shape[0];
+    p->ny = d.shape[1];
+    p->pitch = (p->ny + 31) / 32 * 32;
+    p->pitch_b = (p->ny + 9 + 31) / 32 * 32;
+    p->shot_stride = (long long)p->nx * p->pitch;
+    p->kind = d.density == SA_DENSITY_NONE ? 0 : (d.density == SA_DENSITY_VARIABLE ? 1 : 2);
+    p->ot4 = d.kernel == SA_KERNEL_OT4;
+    p->n_snap = (d.nt + d.undersampling) / d.undersampling + 1;
+    p->snap_stride = p->shot_stride;
+    p->snap_shot_stride = (long long)p->n_snap * p->shot_stride;
+    const char* env = getenv("STRIDEACC_NO_GRAPHS");
+    p->use_graphs = !(env && env[0] == '1');
+    int amax = 0;
+    for (int a = 0; a < d.dim; a++) amax = std::max(amax, d.absorbing[a]);
+    if (amax > 1) {
+        const double refl = std::pow(10.0, -(std::log10((double)amax) - 1) / std::log10(2.0) - 3);
+        damping_table(d.absorbing[0], d.spacing[0], refl, p->sx);
+        damping_table(d.absorbing[1], d.spacing[1], refl, p->sy);
+    }
+    int rc = ensure_fields(p);
+    const size_t N = (size_t)p->shot_stride;
+    if (rc == SA_OK) rc = ensure(&p->W, &p->cap_W, N);
+    if (rc == SA_OK) rc = ensure(&p->vp, &p->cap_vp, N);
+    if (rc == SA_OK && d.attenuation) rc = ensure(&p->alpha, &p->cap_alpha, N);
+    if (rc == SA_OK && p->kind == 1) {
+        rc = ensure(&p->buoy, &p->cap_buoy, N);
+        if (rc == SA_OK) rc = ensure(&p->bxh, &p->cap_bxh, (size_t)(p->nx + 9) * p->pitch);
+        if (rc == SA_OK) rc = ensure(&p->byh, &p->cap_byh, (size_t)p->nx * p->pitch_b);
+    }
+    if (rc != SA_OK) {
+        sa_plan_destroy(p);
+        return rc;
+    }
+    *out = p;
+    return SA_OK;
+}
+
+int sa_plan_destroy(sa_plan* p) {
+    if (!p) return SA_OK;
+    drop_graphs(p);
+    void* bufs[] = {p->field[0], p->field[1], p->W, p->vp, p->alpha, p->buoy, p->bxh, p->byh, p->medium_stage,
+                    p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
+                    p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    if (p->cap) cudaStreamDestroy(p->cap);
+    delete p;
+    return SA_OK;
+}
+
+int sa_set_medium(sa_plan* p, const float* vp, const float* rho, const float* alpha) {
+    if (!p || !vp) return fail(SA_E_INVALID, "null plan or vp");
+    if (p->d.density != SA_DENSITY_NONE && !rho) return fail(SA_E_INVALID, "rho required by the plan's density mode");
+    if (p->d.attenuation && !alpha) return fail(SA_E_INVALID, "alpha required by the plan");
+    const size_t N = (size_t)p->nx * p->ny;
+    const float* in[3] = {vp, p->d.density == SA_DENSITY_VARIABLE ? rho : nullptr, p->d.attenuation ? alpha : nullptr};
+    const float* dev[3] = {nullptr, nullptr, nullptr};
+    const bool any_host = (in[0] && !is_device(in[0])) || (in[1] && !is_device(in[1])) || (in[2] && !is_device(in[2]));
+    if (any_host) CKR(ensure(&p->medium_stage, &p->cap_medium_stage, 3 * N));
+    for (int k = 0; k < 3; k++) {
+        if (!in[k]) continue;
+        if (is_device(in[k])) {
+            dev[k] = in[k];
+        } else {
+            CK(cudaMemcpy(p->medium_stage + k * N, in[k], N * sizeof(float), cudaMemcpyHostToDevice));
+            dev[k] = p->medium_stage + k * N;
+        }
+    }
+    CK(sa::medium2d(dev[0], dev[1], dev[2], p->nx, p->ny, p->pitch, p->pitch_b, p->kind == 1 ? 1 : 0, kDbToNeper,
+                    p->W, p->vp, p->alpha, p->buoy, p->bxh, p->byh, 0));
+    CK(cudaDeviceSynchronize());
+    p->medium_set = true;
+    p->snaps_valid = false;
+    return SA_OK;
+}
+
+int sa_set_geometry(sa_plan* p, int n_shots, const int* src_offsets, const float* src_xyz, const int* rec_offsets,
+                    const float* rec_xyz) {
+    if (!p || n_shots < 1 || !src_offsets || !rec_offsets) return fail(SA_E_INVALID, "bad geometry arguments");
+    if (n_shots > p->d.max_shots) return fail(SA_E_INVALID, "%d shots exceed max_shots %d", n_shots, p->d.max_shots);
+    for (int s = 0; s < n_shots; s++)
+        if (src_offsets[s + 1] < src_offsets[s] || rec_offsets[s + 1] < rec_offsets[s])
+            return fail(SA_E_INVALID, "offsets must be non-decreasing");
+    if (src_offsets[0] != 0 || rec_offsets[0] != 0) return fail(SA_E_INVALID, "offsets must start at 0");
+    const int ns = src_offsets[n_shots], nr = rec_offsets[n_shots];
+    if ((ns && !src_xyz) || (nr && !rec_xyz)) return fail(SA_E_INVALID, "missing coordinates");
+    const int dim = p->d.dim;
+    auto convert = [&](const float* xyz, int n, std::vector<int>& bx, std::vector<int>& by, std::vector<double>& fx,
+                       std::vector<double>& fy) -> int {
+        bx.resize(n);
+        by.resize(n);
+        fx.resize(n);
+        fy.resize(n);
+        for (int i = 0; i < n; i++) {
+            double rel[2];
+            int base[2];
+            for (int a = 0; a < 2; a++) {
+                const double origin = -p->d.extra[a] * p->d.spacing[a];
+                rel[a] = ((double)xyz[i * dim + a] - origin) / p->d.spacing[a];
+                base[a] = (int)std::floor(rel[a]);
+                const int n_a = a == 0 ? p->nx : p->ny;
+                if (!(base[a] >= 0 && base[a] + 1 <= n_a - 1))
+                    return fail(SA_E_INVALID, "point %d lies outside the grid along axis %d", i, a);
+            }
+            bx[i] = base[0];
+            by[i] = base[1];
+            fx[i] = rel[0] - base[0];
+            fy[i] = rel[1] - base[1];
+        }
+        return SA_OK;
+    };
+    CKR(convert(src_xyz, ns, p->src_bx, p->src_by, p->src_fx, p->src_fy));
+    CKR(convert(rec_xyz, nr, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy));
+    p->n_shots = n_shots;
+    p->n_src = ns;
+    p->n_rec = nr;
+    p->src_off.assign(src_offsets, src_offsets + n_shots + 1);
+    p->rec_off.assign(rec_offsets, rec_offsets + n_shots + 1);
+    default_layout(p);
+    CKR(build_lists(p));
+    CKR(ensure(&p->src_amp, &p->cap_src_amp, (size_t)p->d.nt * ns));
+    CKR(ensure(&p->rec_amp, &p->cap_rec_amp, (size_t)p->d.nt * nr));
+    p->geometry_set = true;
+    p->snaps_valid = false;
+    return SA_OK;
+}
+
+int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, void* stream) {
+    if (!p) return fail(SA_E_INVALID, "null plan");
+    if (!p->medium_set || !p->geometry_set) return fail(SA_E_INVALID, "medium and geometry must be set first");
+    if ((p->n_src && !wavelets) || (p->n_rec && !traces)) return fail(SA_E_INVALID, "null wavelets or traces");
+    if (save_mode != SA_SAVE_NONE && save_mode != SA_SAVE_SNAPSHOTS) return fail(SA_E_INVALID, "save_mode");
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool save = save_mode == SA_SAVE_SNAPSHOTS;
+    if (save) {
+        const size_t n = (size_t)p->n_shots * p->snap_shot_stride;
+        float* old = p->snaps;
+        CKR(ensure(&p->snaps, &p->cap_snaps, n));
+        if (old != p->snaps) drop_graphs(p);
+        // every slot the adjoint reads (t % f == 0, f <= t <= nt-1-f) is written by this forward
+    }
+    CKR(load_transposed(p, wavelets, p->n_src, p->d.nt, p->src_amp, s));
+    CKR(run_loop(p, &p->g_fwd[save ? 1 : 0], s, [&](cudaStream_t cs) { return issue_forward(p, save, cs); }));
+    CKR(store_transposed(p, p->rec_amp, p->d.nt, p->n_rec, traces, s));
+    if (save) p->snaps_valid = true;
+    return SA_OK;
+}
+
+int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_vp, int grad_mode, void* stream) {
+    if (!p) return fail(SA_E_INVALID, "null plan");
+    if (grad_mode != SA_GRAD_PARITY) return fail(SA_E_UNSUPPORTED, "grad_mode %d", grad_mode);
+    if (!p->snaps_valid) return fail(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS");
+    if ((p->n_rec && !residuals) || !grad_vp || !prec_vp) return fail(SA_E_INVALID, "null residuals or outputs");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t fe = (size_t)p->n_shots * p->shot_stride;
+    float *og = p->gradb, *op = p->precb;
+    CKR(ensure(&p->gradb, &p->cap_gradb, fe));
+    CKR(ensure(&p->precb, &p->cap_precb, fe));
+    if (og != p->gradb || op != p->precb) drop_graphs(p);
+    CKR(load_transposed(p, residuals, p->n_rec, p->d.nt, p->rec_amp, s));
+    CKR(run_loop(p, &p->g_adj, s, [&](cudaStream_t cs) { return issue_adjoint(p, cs); }));
+    const size_t N = (size_t)p->nx * p->ny;
+    for (int k = 0; k < 2; k++) {
+        float* user = k == 0 ? grad_vp : prec_vp;
+        const float* buf = k == 0 ? p->gradb : p->precb;
+        if (is_device(user)) {
+            CK(sa::reduce_shots(buf, p->shot_stride, p->n_shots, p->nx, p->ny, p->pitch, user, s));
+        } else {
+            CKR(ensure(&p->stage, &p->cap_stage, N));
+            CK(sa::reduce_shots(buf, p->shot_stride, p->n_shots, p->nx, p->ny, p->pitch, p->stage, s));
+            CK(cudaMemcpyAsync(user, p->stage, N * sizeof(float), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+        }
+    }
+    return SA_OK;
+}
+
+int sa_autotune(sa_plan* p, void* stream) {
+    if (!p || !p->geometry_set || !p->medium_set) return fail(SA_E_INVALID, "autotune needs medium and geometry");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int H1 = halo1(p);
+    const int S = p->ot4 ? 2 : 1;
+    struct Cand {
+        int nt, nchunks;
+    };
+    std::vector<Cand> cands;
+    for (int nt : {128, 160, 256})
+        for (int nc : {1, 2, 3, 4, 6, 8, 12, 16}) {
+            if (p->nx / nc < 4 * S * radius(p)) continue;
+            cands.push_back({nt, nc});
+        }
+    const int steps = std::min(24, p->d.nt - 2);
+    float best = 1e30f;
+    Cand bc = {p->NT, p->nchunks};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    p->layout_fixed = true;
+    for (const Cand& c : cands) {
+        p->NT = c.nt;
+        const int bymax = c.nt - 2 * H1;
+        p->nstrips = (p->ny + bymax - 1) / bymax;
+        p->by = (p->ny + p->nstrips - 1) / p->nstrips;
+        p->chunk_rows = (p->nx + c.nchunks - 1) / c.nchunks;
+        p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
+        CKR(build_lists(p));
+        sa::Step2D a = base_args(p);
+        a.inj = nullptr;
+        a.gat = nullptr;
+        a.cur = p->field[0];
+        a.prev = p->field[1];
+        const dim3 grid(p->nstrips, p->nchunks, p->n_shots);
+        for (int w = 0; w < 3; w++) {
+            a.t = 1 + w;
+            CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
+        }
+        CK(cudaEventRecord(e0, s));
+        for (int t = 0; t < steps; t++) {
+            a.t = 1 + t;
+            float* nc = const_cast<float*>(a.cur);
+            a.cur = a.prev;
+            a.prev = nc;
+            CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
+        }
+        CK(cudaEventRecord(e1, s));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            bc = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    p->NT = bc.nt;
+    const int bymax = bc.nt - 2 * H1;
+    p->nstrips = (p->ny + bymax - 1) / bymax;
+    p->by = (p->ny + p->nstrips - 1) / p->nstrips;
+    p->chunk_rows = (p->nx + bc.nchunks - 1) / bc.nchunks;
+    p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
+    CKR(build_lists(p));
+    p->snaps_valid = false;
+    return SA_OK;
+}
+
+}  // extern "C"
