@@ -28,8 +28,11 @@ __host__ __device__ constexpr float kWS(int k) {
                   : (float)(35.0 / 294912.0);
 }
 
+constexpr int GUARD = 40;  // zero rows above and below every pitched medium array (>= 3R + RB + 5)
+
 // One corner contribution of an injected point (source in the forward, receiver in the
-// adjoint). The injected value is coef * amp[t][point] * vp(row,col)^vp_power.
+// adjoint): new_level(row, col) += coef * amp[t][point]. coef carries the bilinear weight and
+// the reference's scaling at that corner (2 dt vp / h forward, -dt^2 vp^2 adjoint).
 struct Inject {
     int row, col, point;
     float coef;
@@ -48,26 +51,23 @@ struct Step2D {
     int chunk_rows;           // output rows per CTA
     int by;                   // output columns per CTA (<= NT - 2*halo)
     int t;                    // time index of the current level (cur = p[t])
-    int adjoint;              // 0: p[t+1] from p[t], p[t-1];  1: p_a[t-1] from p_a[t], p_a[t+1]
     const float* cur;         // p[t]                      [shots][nx][pitch]
     float* prev;              // other level in, new level out (in place)
-    // medium
+    // medium (shared by all shots); pointers address row 0, GUARD zero rows on both sides
     const float* W;           // node coefficient: vp^2 (density none/constant) or vp^2 rho
-    const float* vp;
-    const float* alpha;       // Np/m or nullptr
-    const float* bxh;         // buoyancy at (x+1/2, y), x = -5..nx+3 stored at row x+5, pitch
-    const float* byh;         // buoyancy at (x, y+1/2), y = -5..ny+3 stored at col y+5, pitch_b
+    const float* bxh;         // buoyancy at (x+1/2, y), half-rows -5..nx+3 valid
+    const float* byh;         // buoyancy at (x, y+1/2): column y+5 holds y = -5..ny+3
     int pitch_b;
+    const float* C1;          // update p_new = C1 Lt + C2 p - C3 p_other (damping, attenuation)
+    const float* C2;
+    const float* C3;
     float hx, hy;             // spacing
     float dt;
-    float sx[MAX_ABS], sy[MAX_ABS];  // damping ramp per distance to the edge, in 1/m
-    int ax, ay;               // absorbing widths
     // sparse points (CSR over CTAs in launch order: shot-major, then chunk, then strip)
     const Inject* inj;
     const int* inj_off;
     const float* inj_amp;     // [nt][n_inj_points] time-major amplitudes
-    int inj_ld;               // leading dimension of inj_amp
-    int inj_vp_power;         // 1: forward source (vp), 2: adjoint receiver (vp^2)
+    int inj_ld;
     const Gather* gat;
     const int* gat_off;
     float* gat_out;           // [nt][n_gather_points]

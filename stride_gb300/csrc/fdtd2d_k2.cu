@@ -5,9 +5,20 @@
 
 namespace sa {
 
+constexpr int RB = 2;  // rows per iteration
+constexpr int PF = 2;  // iterations prefetched ahead
+
 template <bool OT4, int NT>
 static cudaError_t go(dim3 grid, cudaStream_t s, const Step2D& a) {
-    fdtd2d_step<2, OT4, NT><<<grid, NT, 0, s>>>(a);
+    constexpr size_t bytes = Smem2D<2, OT4, NT, RB, PF>::bytes;
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(fdtd2d_step<2, OT4, NT, RB, PF>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    fdtd2d_step<2, OT4, NT, RB, PF><<<grid, NT, bytes, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -5,8 +5,8 @@
 
 namespace sa {
 
-// vp, rho, alpha (dB/cm) on the unpadded extended grid -> pitched W, vp, alpha (Np/m), and
-// buoyancy b = 1/rho into a pitched scratch (iso_acoustic/devito.py:476-497).
+// vp, rho, alpha (dB/cm) on the unpadded extended grid -> pitched W (guarded layout, pointer
+// at row 0), vp, alpha (Np/m) and buoyancy b = 1/rho scratch (iso_acoustic/devito.py:476-497).
 __global__ void k_medium2d(const float* __restrict__ vp_in, const float* __restrict__ rho_in,
                            const float* __restrict__ alpha_in, int nx, int ny, int pitch, int density,
                            double db_to_np, float* W, float* vp, float* alpha, float* buoy) {
@@ -24,14 +24,14 @@ __global__ void k_medium2d(const float* __restrict__ vp_in, const float* __restr
             buoy[p] = 1.f / r;
         }
         W[p] = w;
-        if (alpha_in) alpha[p] = (float)((double)alpha_in[q] * db_to_np);
+        alpha[p] = alpha_in ? (float)((double)alpha_in[q] * db_to_np) : 0.f;
     }
 }
 
-// Buoyancy at half points: bxh[(x+5)*pitch + y] = b(x+1/2, y) for x = -5..nx+3 and
-// byh[x*pitch_b + y + 5] = b(x, y+1/2) for y = -5..ny+3; nodes beyond the grid take the edge
-// value as the reference's edge-padded halo (common/devito.py:805-841), the half point is the
-// arithmetic mean of its two nodes.
+// Buoyancy at half points: bxh[x*pitch + y] = b(x+1/2, y) for x = -5..nx+3 (pointer at x = 0)
+// and byh[x*pitch_b + y + 5] = b(x, y+1/2) for y = -5..ny+3; nodes beyond the grid take the
+// edge value as the reference's edge-padded halo (common/devito.py:805-841), the half point is
+// the arithmetic mean of its two nodes.
 __global__ void k_bhalf2d(const float* __restrict__ buoy, int nx, int ny, int pitch, int pitch_b, float* bxh,
                           float* byh) {
     const long long nxa = (long long)(nx + 9) * ny;
@@ -39,10 +39,9 @@ __global__ void k_bhalf2d(const float* __restrict__ buoy, int nx, int ny, int pi
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nxa + nya;
          q += (long long)gridDim.x * blockDim.x) {
         if (q < nxa) {
-            const int xr = (int)(q / ny), y = (int)(q % ny);
-            const int x = xr - 5;
+            const int x = (int)(q / ny) - 5, y = (int)(q % ny);
             const int x0 = min(max(x, 0), nx - 1), x1 = min(max(x + 1, 0), nx - 1);
-            bxh[(long long)xr * pitch + y] = 0.5f * (buoy[(long long)x0 * pitch + y] + buoy[(long long)x1 * pitch + y]);
+            bxh[(long long)x * pitch + y] = 0.5f * (buoy[(long long)x0 * pitch + y] + buoy[(long long)x1 * pitch + y]);
         } else {
             const long long r = q - nxa;
             const int x = (int)(r / (ny + 9)), yr = (int)(r % (ny + 9));
@@ -51,6 +50,44 @@ __global__ void k_bhalf2d(const float* __restrict__ buoy, int nx, int ny, int pi
             byh[(long long)x * pitch_b + yr] = 0.5f * (buoy[(long long)x * pitch + y0] + buoy[(long long)x * pitch + y1]);
         }
     }
+}
+
+// Update coefficients of p_new = C1 Lt + C2 p - C3 p_other, the solved form of
+// p.dt2 - Lt + 2 alpha vp p.dt + vp^2 (2 d p.dtc + d^2 p) = 0 (iso_acoustic/devito.py:1575-1581)
+// with the SpongeBoundary2 damping d = 7 dt vp S(x) (boundaries/devito.py:52-67). S follows
+// Boundary.damping's slab rule (boundary.py:116-160): the x slab at layer e covers y layers
+// >= e and vice versa, so corner points take the outer slab (both on the diagonal).
+__global__ void k_coef2d(const float* __restrict__ vp, const float* __restrict__ alpha, int nx, int ny, int pitch,
+                         Sponge sp, float dt, float* C1, float* C2, float* C3) {
+    const long long n = (long long)nx * ny;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(q / ny), y = (int)(q % ny);
+        const long long p = (long long)x * pitch + y;
+        const int ex = min(x, nx - 1 - x), ey = min(y, ny - 1 - y);
+        float s = 0.f;
+        if (ex < sp.a[0] && ex <= ey) s += sp.s[0][ex];
+        if (ey < sp.a[1] && ey <= ex) s += sp.s[1][ey];
+        const float v = vp[p], v2 = v * v;
+        const float d = 7.f * (s * v) * dt;
+        float beta = v2 * d;
+        beta = beta + alpha[p] * v;
+        beta = dt * beta;
+        const float den = 1.f + beta;
+        C1[p] = (dt * dt) / den;
+        C2[p] = (2.f - dt * dt * v2 * d * d) / den;
+        C3[p] = (1.f - beta) / den;
+    }
+}
+
+cudaError_t medium2d(const float* vp_in, const float* rho_in, const float* alpha_in, int nx, int ny, int pitch,
+                     int pitch_b, int density, double db_to_np, const Sponge& sp, float dt, float* W, float* vp,
+                     float* alpha, float* buoy, float* bxh, float* byh, float* C1, float* C2, float* C3,
+                     cudaStream_t s) {
+    k_medium2d<<<1024, 256, 0, s>>>(vp_in, rho_in, alpha_in, nx, ny, pitch, density, db_to_np, W, vp, alpha, buoy);
+    if (density == 1) k_bhalf2d<<<1024, 256, 0, s>>>(buoy, nx, ny, pitch, pitch_b, bxh, byh);
+    k_coef2d<<<1024, 256, 0, s>>>(vp, alpha, nx, ny, pitch, sp, dt, C1, C2, C3);
+    return cudaGetLastError();
 }
 
 // out[c][r] = in[r][c] for an rows x cols matrix (both dense).
@@ -89,14 +126,6 @@ __global__ void reduce_shots2d(const float* __restrict__ buf, long long shot_str
         for (int b = 0; b < nshots; b++) s += buf[(long long)b * shot_stride + p];
         out[q] = s;
     }
-}
-
-cudaError_t medium2d(const float* vp_in, const float* rho_in, const float* alpha_in, int nx, int ny, int pitch,
-                     int pitch_b, int density, double db_to_np, float* W, float* vp, float* alpha, float* buoy,
-                     float* bxh, float* byh, cudaStream_t s) {
-    k_medium2d<<<1024, 256, 0, s>>>(vp_in, rho_in, alpha_in, nx, ny, pitch, density, db_to_np, W, vp, alpha, buoy);
-    if (density == 1) k_bhalf2d<<<1024, 256, 0, s>>>(buoy, nx, ny, pitch, pitch_b, bxh, byh);
-    return cudaGetLastError();
 }
 
 cudaError_t transpose(const float* in, int rows, int cols, float* out, cudaStream_t s) {

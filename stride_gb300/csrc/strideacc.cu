@@ -82,8 +82,13 @@ struct sa_plan {
     bool ot4 = true;
     float* field[2] = {nullptr, nullptr};
     size_t field_cap[2] = {0, 0};
+    // medium: W, bxh, byh, C1..C3 have GUARD zero rows on both sides (the *_0 pointers address
+    // row 0 / half-row 0); vp, alpha, buoy are unguarded scratch of the preparation kernels
     float *W = nullptr, *vp = nullptr, *alpha = nullptr, *buoy = nullptr, *bxh = nullptr, *byh = nullptr;
-    size_t cap_W = 0, cap_vp = 0, cap_alpha = 0, cap_buoy = 0, cap_bxh = 0, cap_byh = 0;
+    float *C1 = nullptr, *C2 = nullptr, *C3 = nullptr;
+    size_t cap_W = 0, cap_vp = 0, cap_alpha = 0, cap_buoy = 0, cap_bxh = 0, cap_byh = 0, cap_C1 = 0, cap_C2 = 0,
+           cap_C3 = 0;
+    std::vector<float> vp_host;  // for the injection coefficients (vp at the corners)
     float* medium_stage = nullptr;
     size_t cap_medium_stage = 0;
     bool medium_set = false;
@@ -113,7 +118,7 @@ struct sa_plan {
     // layout
     int NT = 128, by = 110, chunk_rows = 1, nstrips = 1, nchunks = 1;
     bool layout_fixed = false;
-    float sx[sa::MAX_ABS] = {}, sy[sa::MAX_ABS] = {};
+    sa::Sponge sponge{};
     // graphs
     cudaStream_t cap = nullptr;
     cudaGraphExec_t g_fwd[2] = {nullptr, nullptr};
@@ -141,7 +146,7 @@ void drop_graphs(sa_plan* p) {
 
 // Sponge ramp of Boundary.damping for one axis (stride/physics/boundaries/boundary.py:98-151),
 // before the multiplication by vp and 7 dt (done per point in the kernel).
-void damping_table(int A, double h, double refl, float* out) {
+void damping_table(int A, double h, double refl, float* out) {  // out: MAX_ABS entries
     for (int e = 0; e < sa::MAX_ABS; e++) out[e] = 0.f;
     if (A <= 0) return;
     double coef = (2 + 1) / 2.0 * std::log(1.0 / refl);
@@ -195,7 +200,7 @@ int build_lists(sa_plan* p) {
     const double dt = p->d.dt;
     auto cta_of = [&](int shot, int x, int y) { return (shot * nc + x / p->chunk_rows) * ns + y / p->by; };
     auto make_inj = [&](const std::vector<int>& off, const std::vector<int>& bx, const std::vector<int>& by,
-                        const std::vector<double>& fx, const std::vector<double>& fy, double scale,
+                        const std::vector<double>& fx, const std::vector<double>& fy, double scale, int vp_power,
                         std::vector<HostInject>& out) {
         out.clear();
         for (int s = 0; s < p->n_shots; s++)
@@ -204,7 +209,9 @@ int build_lists(sa_plan* p) {
                     for (int cy = 0; cy < 2; cy++) {
                         const int x = bx[i] + cx, y = by[i] + cy;
                         const double w = (cx ? fx[i] : 1.0 - fx[i]) * (cy ? fy[i] : 1.0 - fy[i]);
-                        out.push_back({cta_of(s, x, y), x, y, i, (float)(w * scale)});
+                        const float v = p->vp_host.empty() ? 0.f : p->vp_host[(size_t)x * p->ny + y];
+                        const double vpow = vp_power == 2 ? (double)(v * v) : (double)v;
+                        out.push_back({cta_of(s, x, y), x, y, i, (float)(w * scale * vpow)});
                     }
         std::stable_sort(out.begin(), out.end(), [](const HostInject& a, const HostInject& b) {
             return a.cta != b.cta ? a.cta < b.cta : a.row < b.row;
@@ -226,11 +233,11 @@ int build_lists(sa_plan* p) {
         return SA_OK;
     };
     std::vector<HostInject> tmp;
-    // forward source: src * 2 dt^2 vp / h / dt (iso_acoustic/devito.py:349-363), vp in the kernel
-    make_inj(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, 2.0 * dt / h, tmp);
+    // forward source: src * 2 dt^2 vp / h / dt (iso_acoustic/devito.py:349-363), vp at the corner
+    make_inj(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, 2.0 * dt / h, 1, tmp);
     CKR(upload_inj(tmp, &p->inj_src, &p->cap_inj_src, &p->inj_src_off, &p->cap_inj_src_off));
-    // adjoint receiver: -rec * dt^2 * vp^2 (devito.py:748-753), vp^2 in the kernel
-    make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, -dt * dt, tmp);
+    // adjoint receiver: -rec * dt^2 * vp^2 (devito.py:748-753), vp^2 at the corner
+    make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, -dt * dt, 2, tmp);
     CKR(upload_inj(tmp, &p->inj_rec, &p->cap_inj_rec, &p->inj_rec_off, &p->cap_inj_rec_off));
     // receiver gathers, one per receiver, owned by the CTA of its base corner
     std::vector<std::pair<int, sa::Gather>> g;
@@ -250,7 +257,9 @@ int build_lists(sa_plan* p) {
             g.push_back({cta_of(s, G.row, G.col), G});
             flat.push_back(G);
         }
-    std::stable_sort(g.begin(), g.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    std::stable_sort(g.begin(), g.end(), [](const auto& a, const auto& b) {
+        return a.first != b.first ? a.first < b.first : a.second.row < b.second.row;
+    });
     std::vector<sa::Gather> gl(g.size());
     std::vector<int> goff(ncta + 1, 0);
     for (size_t k = 0; k < g.size(); k++) {
@@ -268,6 +277,10 @@ int build_lists(sa_plan* p) {
     return SA_OK;
 }
 
+const float* row0(const sa_plan* p, const float* alloc, int pitch, int extra_rows = 0) {
+    return alloc + (long long)(sa::GUARD + extra_rows) * pitch;
+}
+
 sa::Step2D base_args(const sa_plan* p) {
     sa::Step2D a{};
     a.nx = p->nx;
@@ -276,21 +289,16 @@ sa::Step2D base_args(const sa_plan* p) {
     a.shot_stride = p->shot_stride;
     a.chunk_rows = p->chunk_rows;
     a.by = p->by;
-    a.W = p->W;
-    a.vp = p->vp;
-    a.alpha = p->d.attenuation ? p->alpha : nullptr;
-    a.bxh = p->bxh;
-    a.byh = p->byh;
+    a.W = row0(p, p->W, p->pitch);
+    a.bxh = p->bxh ? row0(p, p->bxh, p->pitch, 5) : nullptr;
+    a.byh = p->byh ? row0(p, p->byh, p->pitch_b) : nullptr;
     a.pitch_b = p->pitch_b;
+    a.C1 = row0(p, p->C1, p->pitch);
+    a.C2 = row0(p, p->C2, p->pitch);
+    a.C3 = row0(p, p->C3, p->pitch);
     a.hx = (float)p->d.spacing[0];
     a.hy = (float)p->d.spacing[1];
     a.dt = (float)p->d.dt;
-    for (int e = 0; e < sa::MAX_ABS; e++) {
-        a.sx[e] = p->sx[e];
-        a.sy[e] = p->sy[e];
-    }
-    a.ax = p->d.absorbing[0];
-    a.ay = p->d.absorbing[1];
     a.f = p->d.undersampling;
     a.snaps = p->snaps;
     a.snap_stride = p->snap_stride;
@@ -311,12 +319,10 @@ int issue_forward(sa_plan* p, bool save, cudaStream_t s) {
     CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
     CK(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * p->n_rec * sizeof(float), s));
     sa::Step2D a = base_args(p);
-    a.adjoint = 0;
     a.inj = p->n_src ? p->inj_src : nullptr;
     a.inj_off = p->inj_src_off;
     a.inj_amp = p->src_amp;
     a.inj_ld = p->n_src;
-    a.inj_vp_power = 1;
     a.gat_off = p->gat_off;
     a.gat_out = p->rec_amp;
     a.gat_ld = p->n_rec;
@@ -352,12 +358,10 @@ int issue_adjoint(sa_plan* p, cudaStream_t s) {
     CK(cudaMemsetAsync(p->gradb, 0, fbytes, s));
     CK(cudaMemsetAsync(p->precb, 0, fbytes, s));
     sa::Step2D a = base_args(p);
-    a.adjoint = 1;
     a.inj = p->n_rec ? p->inj_rec : nullptr;
     a.inj_off = p->inj_rec_off;
     a.inj_amp = p->rec_amp;
     a.inj_ld = p->n_rec;
-    a.inj_vp_power = 2;
     a.gat = nullptr;
     a.save = 0;
     a.grad = 1;
@@ -483,26 +487,43 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
     p->snap_shot_stride = (long long)p->n_snap * p->shot_stride;
     const char* env = getenv("STRIDEACC_NO_GRAPHS");
     p->use_graphs = !(env && env[0] == '1');
+    p->sponge.a[0] = d.absorbing[0];
+    p->sponge.a[1] = d.absorbing[1];
     int amax = 0;
     for (int a = 0; a < d.dim; a++) amax = std::max(amax, d.absorbing[a]);
     if (amax > 1) {
         const double refl = std::pow(10.0, -(std::log10((double)amax) - 1) / std::log10(2.0) - 3);
-        damping_table(d.absorbing[0], d.spacing[0], refl, p->sx);
-        damping_table(d.absorbing[1], d.spacing[1], refl, p->sy);
+        damping_table(d.absorbing[0], d.spacing[0], refl, p->sponge.s[0]);
+        damping_table(d.absorbing[1], d.spacing[1], refl, p->sponge.s[1]);
     }
     int rc = ensure_fields(p);
     const size_t N = (size_t)p->shot_stride;
-    if (rc == SA_OK) rc = ensure(&p->W, &p->cap_W, N);
+    const size_t NG = (size_t)(p->nx + 2 * sa::GUARD) * p->pitch;
+    if (rc == SA_OK) rc = ensure(&p->W, &p->cap_W, NG);
+    if (rc == SA_OK) rc = ensure(&p->C1, &p->cap_C1, NG);
+    if (rc == SA_OK) rc = ensure(&p->C2, &p->cap_C2, NG);
+    if (rc == SA_OK) rc = ensure(&p->C3, &p->cap_C3, NG);
     if (rc == SA_OK) rc = ensure(&p->vp, &p->cap_vp, N);
-    if (rc == SA_OK && d.attenuation) rc = ensure(&p->alpha, &p->cap_alpha, N);
+    if (rc == SA_OK) rc = ensure(&p->alpha, &p->cap_alpha, N);
     if (rc == SA_OK && p->kind == 1) {
         rc = ensure(&p->buoy, &p->cap_buoy, N);
-        if (rc == SA_OK) rc = ensure(&p->bxh, &p->cap_bxh, (size_t)(p->nx + 9) * p->pitch);
-        if (rc == SA_OK) rc = ensure(&p->byh, &p->cap_byh, (size_t)p->nx * p->pitch_b);
+        if (rc == SA_OK) rc = ensure(&p->bxh, &p->cap_bxh, (size_t)(p->nx + 9 + 2 * sa::GUARD) * p->pitch);
+        if (rc == SA_OK) rc = ensure(&p->byh, &p->cap_byh, (size_t)(p->nx + 2 * sa::GUARD) * p->pitch_b);
     }
     if (rc != SA_OK) {
         sa_plan_destroy(p);
         return rc;
+    }
+    // pitch padding of every pitched array is read by the kernels' 16-byte row copies: zero
+    const std::pair<float*, size_t> zero_bufs[] = {
+        {p->field[0], p->field_cap[0]}, {p->field[1], p->field_cap[1]}, {p->W, p->cap_W}, {p->vp, p->cap_vp},
+        {p->alpha, p->cap_alpha}, {p->buoy, p->cap_buoy}, {p->bxh, p->cap_bxh}, {p->byh, p->cap_byh},
+        {p->C1, p->cap_C1}, {p->C2, p->cap_C2}, {p->C3, p->cap_C3}};
+    for (const auto& zb : zero_bufs) {
+        if (zb.first && cudaMemset(zb.first, 0, zb.second * sizeof(float)) != cudaSuccess) {
+            sa_plan_destroy(p);
+            return fail(SA_E_CUDA, "cudaMemset of plan buffers failed");
+        }
     }
     *out = p;
     return SA_OK;
@@ -511,7 +532,8 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
 int sa_plan_destroy(sa_plan* p) {
     if (!p) return SA_OK;
     drop_graphs(p);
-    void* bufs[] = {p->field[0], p->field[1], p->W, p->vp, p->alpha, p->buoy, p->bxh, p->byh, p->medium_stage,
+    void* bufs[] = {p->field[0], p->field[1], p->W, p->vp, p->alpha, p->buoy, p->bxh, p->byh, p->C1, p->C2, p->C3,
+                    p->medium_stage,
                     p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb};
     for (void* b : bufs)
@@ -540,9 +562,16 @@ int sa_set_medium(sa_plan* p, const float* vp, const float* rho, const float* al
         }
     }
     CK(sa::medium2d(dev[0], dev[1], dev[2], p->nx, p->ny, p->pitch, p->pitch_b, p->kind == 1 ? 1 : 0, kDbToNeper,
-                    p->W, p->vp, p->alpha, p->buoy, p->bxh, p->byh, 0));
+                    p->sponge, (float)p->d.dt, const_cast<float*>(row0(p, p->W, p->pitch)), p->vp, p->alpha, p->buoy,
+                    p->bxh ? const_cast<float*>(row0(p, p->bxh, p->pitch, 5)) : nullptr,
+                    p->byh ? const_cast<float*>(row0(p, p->byh, p->pitch_b)) : nullptr,
+                    const_cast<float*>(row0(p, p->C1, p->pitch)), const_cast<float*>(row0(p, p->C2, p->pitch)),
+                    const_cast<float*>(row0(p, p->C3, p->pitch)), 0));
     CK(cudaDeviceSynchronize());
+    p->vp_host.resize(N);
+    CK(cudaMemcpy(p->vp_host.data(), dev[0], N * sizeof(float), cudaMemcpyDeviceToHost));
     p->medium_set = true;
+    if (p->geometry_set) CKR(build_lists(p));
     p->snaps_valid = false;
     return SA_OK;
 }

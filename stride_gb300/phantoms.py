@@ -119,7 +119,8 @@ def workload(name, seed=0, nt=None, n_shots=None, inner=None):
     geo = circle_geometry(ntr, radius, centre, jitter=0.5 if name == 'batched' else 0.0, spacing=spacing, rng=rng)
     dt = 0.6 * h / 1650.
     nt = steps if nt is None else nt
-    wav = _wavelets.tone_burst(f0, 3, nt, dt)
+    n_tone = int((3 / f0) // dt + 1)
+    wav = _wavelets.tone_burst(f0, 3, max(nt, n_tone), dt)[:nt]
     if name == 'single':
         shots = [0] if n_shots is None else list(range(n_shots))
     else:
