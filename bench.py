@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the iso-acoustic FDTD hot path (forward + adjoint vp gradient).
+
+Workload (one "step"): the 2D adjoint-state vp gradient of a batch of shots, i.e. the forward
+modelling of every shot with the undersampled wavefield saved, the L2 residual against
+observed traces, and the reverse-time adjoint with the vp imaging condition, summed over the
+shots:
+
+    512 x 512 inner grid at 0.25 mm + 20 absorbing cells per side (552 x 552 extended),
+    seeded vp/rho/alpha ellipse phantom ('true' model, observed data) and a 1500 m/s starting
+    vp, 1 MHz 3-cycle tone burst, 256 jittered transducers on a 55 mm circle, 64 shots (every
+    4th transducer fires, all 256 receive), 4000 steps at CFL 0.6 (OT4), undersampling 4.
+
+The inputs are synthetic (seeded phantoms) with the shapes of the reference's breast-imaging
+examples; no dataset is involved. Throughput follows Devito's convention: extended grid points
+x time steps executed (forward and adjoint) / seconds.
+
+Arms: ``--impl gb300`` (default) runs libstrideacc.so; ``--impl reference`` times the
+reference algorithm's CPU implementation on this machine's host cores (the C restatement in
+oracle/, because the reference's Devito operator cannot be installed here).
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of fdtd2d_step on this workload's
+# batch (64 shots of 552^2), from the ncu capture summarised in
+# profiles/fdtd2d_step_fwdadj_552sq_64shots.md (None when no capture exists yet).
+NCU_TRAFFIC_PER_LAUNCH = None
+
+
+def workload_config(nt=None, n_shots=64, rank=0):
+    from stride_gb300 import phantoms
+    w = phantoms.workload('batched', seed=0, nt=nt)
+    ntr = len(w['geometry'])
+    stride = max(1, ntr // n_shots)
+    first = rank % stride
+    shots = list(range(first, ntr, stride))[:n_shots]
+    w['shots'] = shots
+    w['src'] = [w['geometry'][[s]] for s in shots]
+    w['rec'] = [w['geometry'] for _ in shots]
+    return w
+
+
+def sponge_fraction(w):
+    n = np.prod(w['shape'])
+    inner = np.prod([s - 2 * a for s, a in zip(w['shape'], w['absorbing'])])
+    return 1.0 - inner / n
+
+
+def alg_bytes_per_point(w):
+    """Compulsory FP32 traffic per grid point and time step with no temporal reuse:
+    p[t], p[t-1] read, p[t+1] written, one read per medium field (vp, rho, alpha), the damping
+    profile in the sponge; +4/f forward (snapshot write), +20/f adjoint (snapshot read,
+    grad/prec read-modify-write)."""
+    n_mat = 1 + (w['rho'] is not None) + (w['alpha'] is not None)
+    base = 4.0 * (3 + n_mat) + 4.0 * sponge_fraction(w)
+    f = 4
+    return base + 4.0 / f, base + 20.0 / f
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix='.csv')
+        os.close(fd)
+        q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), '--query-gpu=' + q,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        out = {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': []}
+        try:
+            rows = [l.split(',') for l in open(self.path).read().strip().splitlines() if l.strip()]
+            os.unlink(self.path)
+        except Exception:
+            return out
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() == 'active':
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if sm:
+            out['sm_mhz'] = statistics.median(sm)
+            out['sm_max_mhz'] = max(mx)
+            out['samples'] = len(sm)
+        out['reasons'] = sorted(reasons)
+        return out
+
+
+def measured_hbm():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            return float(json.load(f)['hbm_gbs']), 'measured'
+    except Exception:
+        return HBM_FALLBACK_GBS, 'fallback'
+
+
+def cpu_arm(w, target_s=15.0, threads=None, calib=True):
+    """Times the oracle's C restatement of the reference operator (forward with save +
+    adjoint, one shot) on the host cores; returns GPts/s and the sample description."""
+    from oracle import c_oracle
+    threads = threads or os.cpu_count()
+    origin = tuple(-e * h for e, h in zip(w['extra'], w['spacing']))
+    N = int(np.prod(w['shape']))
+
+    def run(nt):
+        wav = w['wavelet'][:nt][None]
+        t0 = time.perf_counter()
+        tr, snaps = c_oracle.forward(w['vp'], w['spacing'], w['dt'], nt, w['absorbing'], w['src'][0], w['rec'][0],
+                                     wav, origin, rho=w['rho'], alpha=w['alpha'], kernel='OT4', save=True,
+                                     nthreads=threads)
+        c_oracle.adjoint(w['vp'], w['spacing'], w['dt'], nt, w['absorbing'], w['rec'][0], tr, origin, snaps,
+                         rho=w['rho'], alpha=w['alpha'], kernel='OT4', nthreads=threads)
+        dt = time.perf_counter() - t0
+        return N * ((nt - 2) + (nt - 1 - 4)) / dt / 1e9, dt
+
+    nt = 64
+    rate, dt = run(nt)
+    if calib:
+        nt = int(min(w['nt'], max(64, nt * target_s / max(dt, 1e-3))))
+        rate, dt = run(nt)
+    sample = '1 shot of the workload, forward (save) + adjoint, %d of %d steps, %.1f s' % (nt, w['nt'], dt)
+    return rate, threads, sample, dt
+
+
+def reference_arm(args):
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return 0
+    w = workload_config(nt=args.nt, n_shots=args.shots)
+    threads = os.cpu_count()
+    rates = []
+    for _ in range(args.warmup):
+        cpu_arm(w, target_s=2.0, threads=threads, calib=False)
+    samples = []
+    for _ in range(args.steps):
+        r, _, sample, dt = cpu_arm(w, target_s=args.cpu_seconds / max(1, args.steps), threads=threads)
+        rates.append(r)
+        samples.append(dt)
+    value = statistics.median(rates)
+    N = int(np.prod(w['shape']))
+    pts_step = N * len(w['shots']) * ((w['nt'] - 2) + (w['nt'] - 1 - 4))
+    line = {
+        'impl': 'reference', 'metric': 'GPts/s (forward+adjoint vp gradient)', 'value': value, 'unit': 'GPts/s',
+        'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': pts_step / (value * 1e9) * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded phantoms)',
+        'config': {'workload': WORKLOAD_NAME, 'grid': list(w['shape']), 'shots': len(w['shots']), 'nt': w['nt'],
+                   'kernel': 'OT4', 'l2_flush': 'inputs larger than L2'},
+        'cpu_baseline': {'value': value, 'unit': 'GPts/s', 'cores': threads, 'kind': 'port',
+                         'sample': sample + ' per step (the reference Devito operator cannot be installed here; '
+                                            'this is the oracle C/OpenMP restatement of it)'},
+        'e2e': {'value': value, 'unit': 'GPts/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+WORKLOAD_NAME = ('2D fwd+adj vp gradient: 552^2 extended (512^2 at 0.25 mm + 20 sponge), vp/rho/alpha '
+                 'phantom, 64 shots x 256 receivers, 4000 steps, OT4, f=4')
+
+
+def gb300_arm(args):
+    import torch
+    import torch.distributed as dist
+    from stride_gb300 import _lib
+
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if world > 1:
+        dist.init_process_group('nccl')
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    stream = torch.cuda.current_stream()
+
+    w = workload_config(nt=args.nt, n_shots=args.shots, rank=rank)
+    nt = w['nt']
+    n_shots = len(w['shots'])
+    N = int(np.prod(w['shape']))
+    eps = 1e-3 * np.asarray(w['spacing'])
+    so = np.cumsum([0] + [len(s) for s in w['src']])
+    ro = np.cumsum([0] + [len(r) for r in w['rec']])
+    sx = np.concatenate(w['src']).astype(np.float32) + eps.astype(np.float32)
+    rx = np.concatenate(w['rec']).astype(np.float32) + eps.astype(np.float32)
+    import scipy.signal
+    win = scipy.signal.get_window(('tukey', 0.001), nt, False).astype(np.float32)
+
+    plan = _lib.Plan(2, w['shape'], w['spacing'], w['extra'], w['absorbing'], w['dt'], nt, kernel='OT4',
+                     density=_lib.SA_DENSITY_VARIABLE, attenuation=True, undersampling=4, max_shots=n_shots)
+    plan.set_geometry(so, sx, ro, rx)
+    wav = torch.from_numpy(np.tile((w['wavelet'] * win)[None].astype(np.float32), (plan.n_src, 1))).to(dev)
+    win_d = torch.from_numpy(win).to(dev)
+    # observed data from the true phantom
+    plan.set_medium(w['vp'], w['rho'], w['alpha'])
+    observed = torch.zeros((plan.n_rec, nt), device=dev)
+    plan.forward(wav, observed, stream=stream)
+    # starting model: 1500 m/s water speed, known rho/alpha
+    vp0 = np.full(w['shape'], 1500., np.float32)
+    plan.set_medium(vp0, w['rho'], w['alpha'])
+    plan.autotune(stream=stream)
+    traces = torch.zeros((plan.n_rec, nt), device=dev)
+    grad = torch.zeros(w['shape'], device=dev)
+    prec = torch.zeros(w['shape'], device=dev)
+
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    fwd_ms, adj_ms = [], []
+    launches = {'n': 0, 'steps': 0}
+
+    def step(timed=False):
+        e0, e1, e2 = ev(), ev(), ev()
+        e0.record(stream)
+        plan.forward(wav, traces, save=True, stream=stream)
+        launches['n'] += plan.launches
+        e1.record(stream)
+        res = (traces - observed) * win_d[None, :]  # L2 residual, adjoint-source window
+        plan.adjoint(res, grad, prec, stream=stream)
+        launches['n'] += plan.launches
+        e2.record(stream)
+        if world > 1:
+            dist.all_reduce(grad)
+            dist.all_reduce(prec)
+        if timed:
+            fwd_ms.append((e0, e1))
+            adj_ms.append((e1, e2))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches['n'] = 0
+    with ClockSampler(local) as clk:
+        t0, t1 = ev(), ev()
+        t0.record(stream)
+        for _ in range(args.steps):
+            step(timed=True)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ms = t0.elapsed_time(t1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    pts_fwd = N * n_shots * (nt - 2)
+    pts_adj = N * n_shots * (nt - 1 - 4)
+    pts_step = pts_fwd + pts_adj
+    value = pts_step * world / (ms_step * 1e-3) / 1e9
+    assert torch.isfinite(grad).all() and float(grad.abs().max()) > 0, 'gradient is empty or not finite'
+
+    # roofline of the step kernel: algorithmic bytes per launch / average launch time
+    t_fwd = sum(a.elapsed_time(b) for a, b in fwd_ms) / len(fwd_ms)
+    t_adj = sum(a.elapsed_time(b) for a, b in adj_ms) / len(adj_ms)
+    b_fwd, b_adj = alg_bytes_per_point(w)
+    n_launch = (nt - 2) + (nt - 1 - 4)
+    alg_bytes = N * n_shots * ((nt - 2) * b_fwd + (nt - 1 - 4) * b_adj)
+    per_launch_s = (t_fwd + t_adj) * 1e-3 / n_launch
+    achieved = alg_bytes / n_launch / per_launch_s / 1e9
+    peak, peak_kind = measured_hbm()
+
+    # end to end through the C ABI with host buffers (pinned), residual formed on the host
+    e2e = None
+    if not args.no_e2e:
+        wav_h = wav.cpu().pin_memory()
+        obs_h = observed.cpu().numpy()
+        tr_h = torch.zeros((plan.n_rec, nt)).pin_memory()
+        res_h = torch.zeros((plan.n_rec, nt)).pin_memory()
+        g_h = torch.zeros(w['shape']).pin_memory()
+        p_h = torch.zeros(w['shape']).pin_memory()
+        tr_n, res_n, win_n = tr_h.numpy(), res_h.numpy(), win[None, :]
+
+        def e2e_step():
+            plan.forward(wav_h, tr_h, save=True, stream=stream)
+            np.multiply(np.subtract(tr_n, obs_h, out=res_n), win_n, out=res_n)
+            plan.adjoint(res_h, g_h, p_h, stream=stream)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        s0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        es = (time.perf_counter() - s0) / args.steps
+        if world > 1:
+            t = torch.tensor([es], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            es = float(t.item())
+        e2e = {'value': pts_step * world / es / 1e9, 'unit': 'GPts/s',
+               'h2d_bytes_per_step': int(wav_h.numel() * 4 + res_h.numel() * 4),
+               'd2h_bytes_per_step': int(tr_h.numel() * 4 + 2 * g_h.numel() * 4)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, cores, sample, _ = cpu_arm(w, target_s=args.cpu_seconds)
+        cpu = {'value': rate, 'unit': 'GPts/s', 'cores': cores, 'kind': 'port', 'sample': sample}
+
+    if rank == 0:
+        line = {
+            'metric': 'GPts/s (forward+adjoint vp gradient)', 'value': value, 'unit': 'GPts/s', 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_step, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded phantoms)',
+            'config': {'workload': WORKLOAD_NAME, 'grid': list(w['shape']), 'shots_per_gpu': n_shots, 'nt': nt,
+                       'kernel': 'OT4', 'parallelism': 'shots sharded over %d GPU(s), gradient all-reduce' % world,
+                       'l2_flush': 'inputs larger than L2 (%.0f GB of wavefields per step)'
+                                   % (2 * N * n_shots * 4 / 1e9 + N * n_shots * (nt // 4) * 4 / 1e9)},
+            'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                         'frac': achieved / peak, 'peak_source': peak_kind,
+                         'traffic': NCU_TRAFFIC_PER_LAUNCH,
+                         'alg_bytes_per_point': {'forward': b_fwd, 'adjoint': b_adj},
+                         'kernel': 'fdtd2d_step', 'launch_ms': per_launch_s * 1e3},
+            'cpu_baseline': cpu, 'e2e': e2e, 'gpu_launches': launches['n'], 'clocks': clk.summary(),
+            'forward_ms': t_fwd, 'adjoint_ms': t_adj,
+        }
+        print(json.dumps(line))
+    plan.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split('\n')[0])
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=3)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--nt', type=int, default=None, help='time steps (default: the workload\'s 4000)')
+    ap.add_argument('--shots', type=int, default=64)
+    ap.add_argument('--cpu-seconds', type=float, default=15.0)
+    ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--no-cpu', action='store_true')
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        return reference_arm(args)
+    return gb300_arm(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

@@ -49,14 +49,14 @@ struct Step2D {
     int nx, ny, pitch;        // extended grid, row pitch (floats)
     long long shot_stride;    // floats between shots in a field buffer
     int chunk_rows;           // output rows per CTA
-    int by;                   // output columns per CTA (<= NT - 2*halo)
+    int by;                   // output columns per CTA (even, <= Cols2D::BYMAX)
     int t;                    // time index of the current level (cur = p[t])
     const float* cur;         // p[t]                      [shots][nx][pitch]
     float* prev;              // other level in, new level out (in place)
     // medium (shared by all shots); pointers address row 0, GUARD zero rows on both sides
     const float* W;           // node coefficient: vp^2 (density none/constant) or vp^2 rho
     const float* bxh;         // buoyancy at (x+1/2, y), half-rows -5..nx+3 valid
-    const float* byh;         // buoyancy at (x, y+1/2): column y+5 holds y = -5..ny+3
+    const float* byh;         // buoyancy at (x, y+1/2): column y+6 holds y = -6..ny+3
     int pitch_b;
     const float* C1;          // update p_new = C1 Lt + C2 p - C3 p_other (damping, attenuation)
     const float* C2;

@@ -24,9 +24,9 @@ static cudaError_t go(dim3 grid, cudaStream_t s, const Step2D& a) {
 
 cudaError_t launch_step2d_k1(bool ot4, int nt_threads, dim3 grid, cudaStream_t s, const Step2D& a) {
     switch (nt_threads) {
+        case 64: return ot4 ? go<true, 64>(grid, s, a) : go<false, 64>(grid, s, a);
+        case 96: return ot4 ? go<true, 96>(grid, s, a) : go<false, 96>(grid, s, a);
         case 128: return ot4 ? go<true, 128>(grid, s, a) : go<false, 128>(grid, s, a);
-        case 160: return ot4 ? go<true, 160>(grid, s, a) : go<false, 160>(grid, s, a);
-        case 256: return ot4 ? go<true, 256>(grid, s, a) : go<false, 256>(grid, s, a);
         default: return cudaErrorInvalidValue;
     }
 }

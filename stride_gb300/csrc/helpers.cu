@@ -29,13 +29,13 @@ __global__ void k_medium2d(const float* __restrict__ vp_in, const float* __restr
 }
 
 // Buoyancy at half points: bxh[x*pitch + y] = b(x+1/2, y) for x = -5..nx+3 (pointer at x = 0)
-// and byh[x*pitch_b + y + 5] = b(x, y+1/2) for y = -5..ny+3; nodes beyond the grid take the
+// and byh[x*pitch_b + y + 6] = b(x, y+1/2) for y = -6..ny+3; nodes beyond the grid take the
 // edge value as the reference's edge-padded halo (common/devito.py:805-841), the half point is
 // the arithmetic mean of its two nodes.
 __global__ void k_bhalf2d(const float* __restrict__ buoy, int nx, int ny, int pitch, int pitch_b, float* bxh,
                           float* byh) {
     const long long nxa = (long long)(nx + 9) * ny;
-    const long long nya = (long long)nx * (ny + 9);
+    const long long nya = (long long)nx * (ny + 10);
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nxa + nya;
          q += (long long)gridDim.x * blockDim.x) {
         if (q < nxa) {
@@ -44,8 +44,8 @@ __global__ void k_bhalf2d(const float* __restrict__ buoy, int nx, int ny, int pi
             bxh[(long long)x * pitch + y] = 0.5f * (buoy[(long long)x0 * pitch + y] + buoy[(long long)x1 * pitch + y]);
         } else {
             const long long r = q - nxa;
-            const int x = (int)(r / (ny + 9)), yr = (int)(r % (ny + 9));
-            const int y = yr - 5;
+            const int x = (int)(r / (ny + 10)), yr = (int)(r % (ny + 10));
+            const int y = yr - 6;
             const int y0 = min(max(y, 0), ny - 1), y1 = min(max(y + 1, 0), ny - 1);
             byh[(long long)x * pitch_b + yr] = 0.5f * (buoy[(long long)x * pitch + y0] + buoy[(long long)x * pitch + y1]);
         }

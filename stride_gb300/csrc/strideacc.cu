@@ -123,14 +123,29 @@ struct sa_plan {
     cudaStream_t cap = nullptr;
     cudaGraphExec_t g_fwd[2] = {nullptr, nullptr};
     cudaGraphExec_t g_adj = nullptr;
+    long long loop_launches[3] = {0, 0, 0};  // kernels in the forward (no save, save) and adjoint loops
     bool use_graphs = true;
-    long long launches = 0;
+    long long launches = 0;                   // kernels launched by the last sa_forward / sa_adjoint
 };
 
 namespace {
 
 int halo1(const sa_plan* p) { return p->ot4 ? (p->kind == 0 ? 5 : 9) : 0; }
 int radius(const sa_plan* p) { return p->kind == 0 ? 5 : 9; }
+// output columns of a CTA of `nt` threads (each thread owns a column pair; the stage-1 columns
+// start at an even column HL = H1 rounded up to even before the strip)
+int bymax(const sa_plan* p, int nt) {
+    const int H1 = halo1(p);
+    return (2 * nt - (H1 + (H1 & 1)) - H1) & ~1;
+}
+const int kThreads[] = {64, 96, 128};
+void set_strips(sa_plan* p, int nt) {
+    p->NT = nt;
+    const int bm = bymax(p, nt);
+    p->nstrips = (p->ny + bm - 1) / bm;
+    const int by = (p->ny + p->nstrips - 1) / p->nstrips;
+    p->by = (by + 1) & ~1;
+}
 
 void drop_graphs(sa_plan* p) {
     for (auto& g : p->g_fwd)
@@ -160,21 +175,17 @@ void damping_table(int A, double h, double refl, float* out) {  // out: MAX_ABS 
 
 void default_layout(sa_plan* p) {
     if (p->layout_fixed) return;
-    const int H1 = halo1(p);
     int best_nt = 128, best_cost = 1 << 30;
-    for (int nt : {128, 160, 256}) {
-        const int bymax = nt - 2 * H1;
-        const int strips = (p->ny + bymax - 1) / bymax;
+    for (int nt : kThreads) {
+        const int bm = bymax(p, nt);
+        const int strips = (p->ny + bm - 1) / bm;
         const int cost = strips * nt;
         if (cost < best_cost) {
             best_cost = cost;
             best_nt = nt;
         }
     }
-    p->NT = best_nt;
-    const int bymax = p->NT - 2 * H1;
-    p->nstrips = (p->ny + bymax - 1) / bymax;
-    p->by = (p->ny + p->nstrips - 1) / p->nstrips;
+    set_strips(p, best_nt);
     // enough CTAs to fill 152 SMs several times; each chunk keeps >= 4 pipeline depths of rows
     const int S = p->ot4 ? 2 : 1;
     const int minrows = 4 * S * radius(p);
@@ -346,7 +357,7 @@ int issue_forward(sa_plan* p, bool save, cudaStream_t s) {
                               s));
         n++;
     }
-    p->launches = n;
+    p->loop_launches[save ? 1 : 0] = n;
     return SA_OK;
 }
 
@@ -376,7 +387,7 @@ int issue_adjoint(sa_plan* p, cudaStream_t s) {
         CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
         n++;
     }
-    p->launches = n;
+    p->loop_launches[2] = n;
     return SA_OK;
 }
 
@@ -477,8 +488,8 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
     p->d = d;
     p->nx = d.shape[0];
     p->ny = d.shape[1];
-    p->pitch = (p->ny + 31) / 32 * 32;
-    p->pitch_b = (p->ny + 9 + 31) / 32 * 32;
+    p->pitch = (p->ny + 2 + 31) / 32 * 32;     // a column pair starting at ny-1 stays in the row
+    p->pitch_b = (p->ny + 12 + 31) / 32 * 32;  // half-cols -6..ny+3 at storage column y+6
     p->shot_stride = (long long)p->nx * p->pitch;
     p->kind = d.density == SA_DENSITY_NONE ? 0 : (d.density == SA_DENSITY_VARIABLE ? 1 : 2);
     p->ot4 = d.kernel == SA_KERNEL_OT4;
@@ -644,6 +655,7 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
     CKR(load_transposed(p, wavelets, p->n_src, p->d.nt, p->src_amp, s));
     CKR(run_loop(p, &p->g_fwd[save ? 1 : 0], s, [&](cudaStream_t cs) { return issue_forward(p, save, cs); }));
     CKR(store_transposed(p, p->rec_amp, p->d.nt, p->n_rec, traces, s));
+    p->launches = (p->n_src ? 1 : 0) + p->loop_launches[save ? 1 : 0] + (p->n_rec ? 1 : 0);
     if (save) p->snaps_valid = true;
     return SA_OK;
 }
@@ -674,19 +686,19 @@ int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_v
             CK(cudaStreamSynchronize(s));
         }
     }
+    p->launches = (p->n_rec ? 1 : 0) + p->loop_launches[2] + 2;
     return SA_OK;
 }
 
 int sa_autotune(sa_plan* p, void* stream) {
     if (!p || !p->geometry_set || !p->medium_set) return fail(SA_E_INVALID, "autotune needs medium and geometry");
     cudaStream_t s = (cudaStream_t)stream;
-    const int H1 = halo1(p);
     const int S = p->ot4 ? 2 : 1;
     struct Cand {
         int nt, nchunks;
     };
     std::vector<Cand> cands;
-    for (int nt : {128, 160, 256})
+    for (int nt : kThreads)
         for (int nc : {1, 2, 3, 4, 6, 8, 12, 16}) {
             if (p->nx / nc < 4 * S * radius(p)) continue;
             cands.push_back({nt, nc});
@@ -699,10 +711,7 @@ int sa_autotune(sa_plan* p, void* stream) {
     CK(cudaEventCreate(&e1));
     p->layout_fixed = true;
     for (const Cand& c : cands) {
-        p->NT = c.nt;
-        const int bymax = c.nt - 2 * H1;
-        p->nstrips = (p->ny + bymax - 1) / bymax;
-        p->by = (p->ny + p->nstrips - 1) / p->nstrips;
+        set_strips(p, c.nt);
         p->chunk_rows = (p->nx + c.nchunks - 1) / c.nchunks;
         p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
         CKR(build_lists(p));
@@ -735,10 +744,7 @@ int sa_autotune(sa_plan* p, void* stream) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    p->NT = bc.nt;
-    const int bymax = bc.nt - 2 * H1;
-    p->nstrips = (p->ny + bymax - 1) / bymax;
-    p->by = (p->ny + p->nstrips - 1) / p->nstrips;
+    set_strips(p, bc.nt);
     p->chunk_rows = (p->nx + bc.nchunks - 1) / bc.nchunks;
     p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
     CKR(build_lists(p));
