@@ -36,9 +36,12 @@ constexpr int GUARD = 40;  // zero rows above and below every pitched medium arr
 struct Inject {
     int row, col, point;
     float coef;
+    int lane;  // shot of the shot pair (0 or 1)
+    int pad[3];
 };
 
-// One receiver of a gather: rec[t][point] = sum of the four bilinear corner terms.
+// One receiver of a gather: rec[t][point] = sum of the four bilinear corner terms; `pad` is
+// the receiver's shot (its pair is pad / 2, its lane pad % 2).
 struct Gather {
     int row, col, point, pad;
     float w00, w01, w10, w11;
@@ -46,12 +49,13 @@ struct Gather {
 
 // Arguments of one 2D time step over a batch of shots.
 struct Step2D {
-    int nx, ny, pitch;        // extended grid, row pitch (floats)
-    long long shot_stride;    // floats between shots in a field buffer
+    int nx, ny, pitch;        // extended grid, row pitch (columns)
+    long long shot_stride;    // float2 elements per shot pair in a field buffer (nx * pitch)
+    long long grad_stride;    // floats per shot pair in the gradient buffers (nx * pitch)
     int chunk_rows;           // output rows per CTA
     int by;                   // output columns per CTA (even, <= Cols2D::BYMAX)
     int t;                    // time index of the current level (cur = p[t])
-    const float* cur;         // p[t]                      [shots][nx][pitch]
+    const float* cur;         // p[t] of shot pairs, interleaved: [pairs][nx][pitch][2]
     float* prev;              // other level in, new level out (in place)
     // medium (shared by all shots); pointers address row 0, GUARD zero rows on both sides
     const float* W;           // node coefficient: vp^2 (density none/constant) or vp^2 rho
@@ -76,9 +80,9 @@ struct Step2D {
     int f;                    // undersampling factor
     int save;                 // forward: store p.dt2 on t % f == 0
     int grad;                 // adjoint: accumulate grad/prec on t % f == 0
-    float* snaps;             // [shots][n_snap][nx][pitch]
-    long long snap_shot_stride, snap_stride;
-    float* gradb;             // [shots][nx][pitch]
+    float* snaps;             // [pairs][n_snap][nx][pitch][2]
+    long long snap_shot_stride, snap_stride;  // in float2 elements: per pair, per snapshot
+    float* gradb;             // [pairs][nx][pitch], both shots of a pair summed
     float* precb;
     int ix0, ix1, iy0, iy1;   // interior (imaging condition) bounds
 };

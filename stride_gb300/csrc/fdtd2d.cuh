@@ -41,83 +41,56 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
 
-// Staggered first derivative between register-queue entries: sum_m w_m (q[hi+m] - q[lo-m]).
-template <int QL>
-__device__ __forceinline__ float2 dstag2(const float2 (&q)[QL], int hi, int lo) {
-    float2 a = mul2(f2(kWS(0)), q[hi]);
-    float2 b = mul2(f2(kWS(0)), q[lo]);
+// Staggered first derivative sum_m w_m (v[hi+m] - v[lo-m]) over float2 values (queue or shared).
+template <class A>
+__device__ __forceinline__ float2 dstag2(const A& v, int hi, int lo) {
+    float2 a = mul2(f2(kWS(0)), v[hi]);
+    float2 b = mul2(f2(kWS(0)), v[lo]);
 #pragma unroll
     for (int m = 1; m < 5; m++) {
-        a = fma2(f2(kWS(m)), q[hi + m], a);
-        b = fma2(f2(kWS(m)), q[lo - m], b);
+        a = fma2(f2(kWS(m)), v[hi + m], a);
+        b = fma2(f2(kWS(m)), v[lo - m], b);
     }
     return sub2(a, b);
 }
-// Centred second derivative sum_k w_k (q[c+k] + q[c-k]) + w_0 q[c].
-template <int QL>
-__device__ __forceinline__ float2 dcent2(const float2 (&q)[QL], int cidx) {
-    float2 a = mul2(f2(kW2(0)), q[cidx]);
+// Centred second derivative sum_k w_k (v[c+k] + v[c-k]) + w_0 v[c].
+template <class A>
+__device__ __forceinline__ float2 dcent2(const A& v, int cidx) {
+    float2 a = mul2(f2(kW2(0)), v[cidx]);
 #pragma unroll
-    for (int k = 1; k <= 5; k++) a = fma2(f2(kW2(k)), add2(q[cidx + k], q[cidx - k]), a);
+    for (int k = 1; k <= 5; k++) a = fma2(f2(kW2(k)), add2(v[cidx + k], v[cidx - k]), a);
     return a;
 }
-// Scalar versions over a local array (y derivatives from shared memory).
-__device__ __forceinline__ float dstag1(const float* v, int hi, int lo) {
-    float a = kWS(0) * v[hi], b = kWS(0) * v[lo];
-#pragma unroll
-    for (int m = 1; m < 5; m++) {
-        a = fmaf(kWS(m), v[hi + m], a);
-        b = fmaf(kWS(m), v[lo - m], b);
-    }
-    return a - b;
-}
-__device__ __forceinline__ float dcent1(const float* v, int cidx) {
-    float a = kW2(0) * v[cidx];
-#pragma unroll
-    for (int k = 1; k <= 5; k++) a = fmaf(kW2(k), v[cidx + k] + v[cidx - k], a);
-    return a;
-}
-// n consecutive floats from shared memory as float2 loads (8-byte aligned source).
-template <int N>
-__device__ __forceinline__ void lds_pairs(float (&v)[N], const float* src) {
-#pragma unroll
-    for (int k = 0; k < N / 2; k++) {
-        const float2 p = *reinterpret_cast<const float2*>(src + 2 * k);
-        v[2 * k] = p.x;
-        v[2 * k + 1] = p.y;
-    }
-}
-__device__ __forceinline__ float2 ldg2(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
 
-// Column layout of one CTA. Each thread owns the column pair (c0, c0+1), c0 = Lc + 2t even.
+// Column layout of one CTA: thread t owns column c = L1 + t; every value is a float2 holding
+// the same grid point of the two shots of a shot pair.
 template <int KIND, bool OT4, int NT>
 struct Cols2D {
     static constexpr bool STAG = KIND != 0;
     static constexpr int R = STAG ? 9 : 5;            // radius of one operator application
     static constexpr int S = OT4 ? 2 : 1;             // pipeline stages
     static constexpr int H1 = (S - 1) * R;            // halo of the stage-1 output columns
-    static constexpr int HL = H1 + (H1 & 1);          // left halo rounded to even: Lc = y0 - HL
-    static constexpr int NC = 2 * NT;                 // stage-1 columns of the CTA
-    static constexpr int BYMAX = (NC - HL - H1) & ~1; // output columns (even)
+    static constexpr int BYMAX = NT - 2 * H1;         // output columns
 };
 
-// Shared-memory layout of one CTA (floats).
+// Shared-memory layout of one CTA, in float2 units.
 template <int KIND, bool OT4, int NT, int RB, int PF>
 struct Smem2D {
     using C = Cols2D<KIND, OT4, NT>;
     static constexpr bool STAG = C::STAG;
-    static constexpr int R = C::R, S = C::S, NC = C::NC;
-    static constexpr int WU = round4(NC + 2 * R + 3) + 8;  // u row from floor4(Lc - R), slack for pair reads
-    static constexpr int QU = S * R + RB * (PF + 1);        // u rows kept: o .. i + RB*(PF+1) - 1
-    static constexpr int QLR = R + RB;                      // rows of the intermediate kept (OT4)
-    static constexpr int WL = NC + 8;
-    static constexpr int WF = NC + 12;
+    static constexpr int R = C::R, S = C::S;
+    static constexpr int C0 = NT + 2 * R;                 // u columns [L0, L0 + C0)
+    static constexpr int WU = ((C0 + 1 + 1) & ~1) + 2;    // u row from floor2(L0), even
+    static constexpr int QU = S * R + RB * (PF + 1);      // u rows kept: o .. i + RB*(PF+1) - 1
+    static constexpr int QLR = R + RB;                    // rows of the intermediate kept (OT4)
+    static constexpr int WL = NT + 2;
+    static constexpr int WF = NT + 10;
     static constexpr int oU = 0;
     static constexpr int oL = oU + QU * WU;
     static constexpr int oF = oL + (OT4 ? QLR * WL : 0);
     static constexpr int oF2 = oF + (STAG ? RB * WF : 0);
     static constexpr int total = oF2 + ((OT4 && STAG) ? RB * WF : 0);
-    static constexpr size_t bytes = (size_t)total * sizeof(float);
+    static constexpr size_t bytes = (size_t)total * sizeof(float2);
 };
 
 // Register queue shift by RB (the oldest RB entries leave).
@@ -127,69 +100,71 @@ __device__ __forceinline__ void qshift(float2 (&q)[QL]) {
     for (int k = 0; k + RB < QL; k++) q[k] = q[k + RB];
 }
 
+#ifndef SA_MINBLOCKS
+#define SA_MINBLOCKS 3  // CTAs per SM the register allocation must allow (latency hiding)
+#endif
+
 template <int KIND, bool OT4, int NT, int RB, int PF>
-__global__ void __launch_bounds__(NT) fdtd2d_step(const __grid_constant__ Step2D a) {
+__global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_constant__ Step2D a) {
     using L = Smem2D<KIND, OT4, NT, RB, PF>;
     using CL = Cols2D<KIND, OT4, NT>;
     constexpr bool STAG = CL::STAG;           // staggered div(b grad) operator
     constexpr bool VARB = KIND == 1;          // variable buoyancy
-    constexpr int R = CL::R, S = CL::S, H1 = CL::H1, HL = CL::HL, NC = CL::NC;
+    constexpr int R = CL::R, S = CL::S, H1 = CL::H1;
     constexpr int QU = L::QU, QLR = L::QLR;
-    // register queues along x (float2 = the thread's column pair):
-    // u rows i-QB..i+RB-1; fluxes at half-rows i-QB-5..i-6+RB (STAG)
+    // register queues along x: u rows i-QB..i+RB-1; fluxes at half-rows i-QB-5..i-6+RB (STAG)
     constexpr int QB = STAG ? 9 : 10;
     constexpr int QL = QB + RB;
-    (void)H1;
-    (void)NC;
 
-    extern __shared__ __align__(16) float smem[];
-    float* const sU = smem + L::oU;
-    float* const sLr = smem + L::oL;
-    float* const sF = smem + L::oF;
-    float* const sF2 = smem + L::oF2;
+    extern __shared__ __align__(16) float2 smem2[];
+    float2* const sU = smem2 + L::oU;
+    float2* const sLr = smem2 + L::oL;
+    float2* const sF = smem2 + L::oF;
+    float2* const sF2 = smem2 + L::oF2;
 
     const int tid = threadIdx.x;
-    const int strip = blockIdx.x, chunk = blockIdx.y, shot = blockIdx.z;
-    const int BY = a.by;                      // even, <= BYMAX
-    const int y0 = strip * BY;                // even
-    const int Lc = y0 - HL;                   // first stage-1 column (even)
-    const int QU0 = (Lc - R) & ~3;            // u rows start at floor4(Lc - R)
-    const int c0 = Lc + 2 * tid;              // this thread's column pair (c0, c0+1)
-    const bool in0 = c0 >= 0 && c0 < a.ny, in1 = c0 + 1 >= 0 && c0 + 1 < a.ny;
-    const bool outp = (c0 >= y0) && (c0 < y0 + BY) && in0;  // output pair (c0+1 checked by in1)
-    const int cg = min(max(c0, 0), a.pitch - 2);            // clamped pair column for medium rows
+    const int strip = blockIdx.x, chunk = blockIdx.y, pair = blockIdx.z;
+    const int BY = a.by;
+    const int y0 = strip * BY;
+    const int L1 = y0 - H1;                   // first stage-1 output column
+    const int L0 = L1 - R;                    // first stage-1 input column
+    const int QU0 = L0 & ~1;                  // u rows start at an even column (16-byte copies)
+    const int c = L1 + tid;                   // this thread's column
+    const bool c_in = (c >= 0) && (c < a.ny);
+    const bool out_col = (tid >= H1) && (tid < H1 + BY) && c_in;
+    const int cc = min(max(c, 0), a.ny - 1);
     const int xo0 = chunk * a.chunk_rows;
     const int xo1 = min(a.nx, xo0 + a.chunk_rows);
     const int i0 = xo0 - S * R, i1 = xo1 + S * R;
     const int pitch = a.pitch, pitch_b = a.pitch_b;
 
-    const long long soff = (long long)shot * a.shot_stride;
-    const float* __restrict__ cur = a.cur;
-    float* __restrict__ prev = a.prev + soff;
+    const long long poff = (long long)pair * a.shot_stride;  // float2 elements per pair: nx*pitch
+    const float2* __restrict__ cur = reinterpret_cast<const float2*>(a.cur);
+    float2* __restrict__ prev = reinterpret_cast<float2*>(a.prev) + poff;
 
-    const int cta = (shot * gridDim.y + chunk) * gridDim.x + strip;
+    const int cta = (pair * gridDim.y + chunk) * gridDim.x + strip;
     const int inj_b = a.inj ? a.inj_off[cta] : 0, inj_e = a.inj ? a.inj_off[cta + 1] : 0;
     const int gat_b = a.gat ? a.gat_off[cta] : 0, gat_e = a.gat ? a.gat_off[cta + 1] : 0;
 
-    const float ihx = 1.f / a.hx, ihy = 1.f / a.hy;
-    const float ihx2 = 1.f / (a.hx * a.hx), ihy2 = 1.f / (a.hy * a.hy);
+    const float2 ihx = f2(1.f / a.hx), ihy = f2(1.f / a.hy);
+    const float2 ihx2 = f2(1.f / (a.hx * a.hx)), ihy2 = f2(1.f / (a.hy * a.hy));
     const float dt2 = a.dt * a.dt;
-    const float k12 = (float)((double)a.dt * (double)a.dt / 12.0);
+    const float2 k12 = f2((float)((double)a.dt * (double)a.dt / 12.0));
 
-    // medium pointers at row 0 of this thread's pair (GUARD zero rows make rows beyond the
-    // grid addressable; their values only reach discarded lanes)
-    const float* __restrict__ pW = a.W + cg;
-    const float* __restrict__ pBX = a.bxh + cg;
-    // byh storage column of half-col h is h + 6; flux pairs start at even half-cols
-    const int kb1 = min(max(Lc + 2 * tid, 0), pitch_b - 2);        // stage-1 flux pair f = 2t
-    const int kb1b = min(max(Lc + 2 * (NT + tid), 0), pitch_b - 2); // extra pair f = 2(NT+t), t < 5
-    const int kb2 = min(max(y0 + 2 * tid, 0), pitch_b - 2);        // stage-2 flux pair
-    const float* __restrict__ pC1 = a.C1 + cg;
-    const float* __restrict__ pC2 = a.C2 + cg;
-    const float* __restrict__ pC3 = a.C3 + cg;
+    // per-thread medium pointers at row 0 of this thread's column (GUARD zero rows make rows
+    // beyond the grid addressable; their values only reach discarded lanes)
+    const float* __restrict__ pW = a.W + cc;
+    const float* __restrict__ pBX = a.bxh + cc;
+    // byh storage column of half-col h is h + 6
+    const int kb1 = min(max(L1 + 1 + tid, 0), pitch_b - 1);        // stage-1 flux k = tid
+    const int kb1b = min(max(L1 + 1 + NT + tid, 0), pitch_b - 1);  // stage-1 flux k = NT + tid
+    const int kb2 = min(max(y0 + 1 + tid, 0), pitch_b - 1);        // stage-2 flux k = tid
+    const float* __restrict__ pC1 = a.C1 + cc;
+    const float* __restrict__ pC2 = a.C2 + cc;
+    const float* __restrict__ pC3 = a.C3 + cc;
 
     // u ring: row r in slot (r - i0) mod QU
-    constexpr int NQU = L::WU / 4;
+    constexpr int NQU = L::WU / 2;  // 16-byte copies (2 columns x 2 shots)
     auto wrapU = [](int sl) { return sl < 0 ? sl + QU : (sl >= QU ? sl - QU : sl); };
     auto rowU = [&](int sl) { return sU + sl * L::WU - QU0; };  // rowU(s)[col] = u(row, col)
     int sI = 0;  // slot of row i
@@ -198,13 +173,13 @@ __global__ void __launch_bounds__(NT) fdtd2d_step(const __grid_constant__ Step2D
         for (int rr = 0; rr < RB; rr++) {
             const int r = ii + rr;
             if (r < i1) {
-                float* dst = sU + wrapU(slot + rr) * L::WU;
+                float2* dst = sU + wrapU(slot + rr) * L::WU;
                 const bool row_ok = r >= 0 && r < a.nx;
-                const float* rowp = cur + soff + (long long)r * pitch;
+                const float2* rowp = cur + poff + (long long)r * pitch;
                 for (int k = tid; k < NQU; k += NT) {
-                    const int q = QU0 + 4 * k;
-                    const bool ok = row_ok && q >= 0 && q + 4 <= pitch;
-                    cp_async16(dst + 4 * k, ok ? rowp + q : cur, ok);
+                    const int q = QU0 + 2 * k;
+                    const bool ok = row_ok && q >= 0 && q + 2 <= pitch;
+                    cp_async16(dst + 2 * k, ok ? rowp + q : cur, ok);
                 }
             }
         }
@@ -234,15 +209,15 @@ __global__ void __launch_bounds__(NT) fdtd2d_step(const __grid_constant__ Step2D
         const int j = i - R;        // first stage-1 output row of this iteration
         const int o = i - S * R;    // first output row of this iteration
         // ---- stage-1 medium of this iteration, loaded before the barrier --------------
-        float2 Wj[RB], bxi[RB], by1[RB], by1b[RB];
+        float Wj[RB], bxi[RB], by1[RB], by1b[RB];
 #pragma unroll
         for (int r = 0; r < RB; r++) {
-            Wj[r] = ldg2(pW + (long long)(j + r) * pitch);
+            Wj[r] = __ldg(pW + (long long)(j + r) * pitch);
             if constexpr (VARB) {
-                bxi[r] = ldg2(pBX + (long long)(i - 5 + r) * pitch);
+                bxi[r] = __ldg(pBX + (long long)(i - 5 + r) * pitch);
                 const float* byr = a.byh + (long long)(j + r) * pitch_b;
-                by1[r] = ldg2(byr + kb1);
-                by1b[r] = tid < 5 ? ldg2(byr + kb1b) : f2(0.f);
+                by1[r] = __ldg(byr + kb1);
+                by1b[r] = tid < 9 ? __ldg(byr + kb1b) : 0.f;
             }
         }
 
@@ -255,70 +230,64 @@ __global__ void __launch_bounds__(NT) fdtd2d_step(const __grid_constant__ Step2D
         for (int e = gat_ptr + tid; e < gat_e; e += NT) {
             const Gather G = a.gat[e];
             if (G.row + 1 >= i + RB) break;
-            const float* s0 = rowU(wrapU(sI + G.row - i));
-            const float* s1 = rowU(wrapU(sI + G.row + 1 - i));
-            const float v = G.w00 * s0[G.col] + G.w01 * s0[G.col + 1] + G.w10 * s1[G.col] + G.w11 * s1[G.col + 1];
+            const float2* s0 = rowU(wrapU(sI + G.row - i));
+            const float2* s1 = rowU(wrapU(sI + G.row + 1 - i));
+            const bool hi = G.pad & 1;
+            const float2 a00 = s0[G.col], a01 = s0[G.col + 1], a10 = s1[G.col], a11 = s1[G.col + 1];
+            const float v = G.w00 * (hi ? a00.y : a00.x) + G.w01 * (hi ? a01.y : a01.x) +
+                            G.w10 * (hi ? a10.y : a10.x) + G.w11 * (hi ? a11.y : a11.x);
             a.gat_out[(long long)(a.t - 1) * a.gat_ld + G.point] = v;
         }
 
         // stage-2 and update medium of this iteration (used after the next barrier)
-        float2 Wo[RB], bxj[RB], by2[RB], c1[RB], c2[RB], c3[RB], pmo[RB];
+        float Wo[RB], bxj[RB], by2[RB], c1[RB], c2[RB], c3[RB];
+        float2 pmo[RB];
 #pragma unroll
         for (int r = 0; r < RB; r++) {
             if constexpr (OT4) {
-                Wo[r] = ldg2(pW + (long long)(o + r) * pitch);
+                Wo[r] = __ldg(pW + (long long)(o + r) * pitch);
                 if constexpr (VARB) {
-                    bxj[r] = ldg2(pBX + (long long)(j - 5 + r) * pitch);
-                    by2[r] = ldg2(a.byh + (long long)(o + r) * pitch_b + kb2);
+                    bxj[r] = __ldg(pBX + (long long)(j - 5 + r) * pitch);
+                    by2[r] = __ldg(a.byh + (long long)(o + r) * pitch_b + kb2);
                 }
             }
-            const bool o_ok = (o + r >= xo0) && (o + r < xo1) && outp;
+            const bool o_ok = (o + r >= xo0) && (o + r < xo1) && out_col;
             const long long orow = (long long)(o + r) * pitch;
-            c1[r] = o_ok ? ldg2(pC1 + orow) : f2(0.f);
-            c2[r] = o_ok ? ldg2(pC2 + orow) : f2(0.f);
-            c3[r] = o_ok ? ldg2(pC3 + orow) : f2(0.f);
-            pmo[r] = o_ok ? *reinterpret_cast<const float2*>(prev + orow + c0) : f2(0.f);
+            c1[r] = o_ok ? __ldg(pC1 + orow) : 0.f;
+            c2[r] = o_ok ? __ldg(pC2 + orow) : 0.f;
+            c3[r] = o_ok ? __ldg(pC3 + orow) : 0.f;
+            pmo[r] = o_ok ? prev[orow + c] : f2(0.f);
         }
         (void)Wo; (void)bxj; (void)by2; (void)bxi; (void)by1; (void)by1b;
 
         // ---- stage 1: l = W * G(u) at rows j .. j+RB-1 ----------------------------------
 #pragma unroll
-        for (int r = 0; r < RB; r++) uq[QB + r] = *reinterpret_cast<const float2*>(rowU(wrapU(sI + r)) + c0);
-        float gy[RB][2];
+        for (int r = 0; r < RB; r++) uq[QB + r] = rowU(wrapU(sI + r))[c];
+        float2 gy[RB];
         if constexpr (STAG) {
 #pragma unroll
             for (int r = 0; r < RB; r++) {
-                const float* su = rowU(wrapU(sI - R + r));  // u(j+r, col)
-                float* F = sF + r * L::WF;                  // F[f] = flux at half-col Lc-6+f
-#pragma unroll
-                for (int pass = 0; pass < 2; pass++) {
-                    if (pass == 1 && tid >= 5) break;
-                    const int f = 2 * (pass == 0 ? tid : NT + tid);
-                    const int jh = Lc - 6 + f;  // even half-col
-                    float uv[12];
-                    lds_pairs<12>(uv, su + jh - 4);
-                    float2 fl = make_float2(dstag1(uv, 5, 4), dstag1(uv, 6, 5));
-                    fl = mul2(fl, f2(ihy));
-                    if constexpr (VARB) fl = mul2(fl, pass == 0 ? by1[r] : by1b[r]);
-                    *reinterpret_cast<float2*>(F + f) = fl;
+                const float2* su = rowU(wrapU(sI - R + r)) + L0;  // su[k] = u(j+r, L0 + k)
+                float2* F = sF + r * L::WF;                         // F[k]: half-col L1-5+k
+                {
+                    const int k = tid;
+                    float2 v = mul2(dstag2(su, k + 5, k + 4), ihy);
+                    if constexpr (VARB) v = mul2(v, f2(by1[r]));
+                    F[k] = v;
+                }
+                if (tid < 9) {
+                    const int k = NT + tid;
+                    float2 v = mul2(dstag2(su, k + 5, k + 4), ihy);
+                    if constexpr (VARB) v = mul2(v, f2(by1b[r]));
+                    F[k] = v;
                 }
             }
             __syncthreads();
 #pragma unroll
-            for (int r = 0; r < RB; r++) {
-                float fv[12];
-                lds_pairs<12>(fv, sF + r * L::WF + 2 * tid);
-                gy[r][0] = dstag1(fv, 6, 5) * ihy;
-                gy[r][1] = dstag1(fv, 7, 6) * ihy;
-            }
+            for (int r = 0; r < RB; r++) gy[r] = mul2(dstag2(sF + r * L::WF, tid + 5, tid + 4), ihy);
         } else {
 #pragma unroll
-            for (int r = 0; r < RB; r++) {
-                float uv[14];
-                lds_pairs<14>(uv, rowU(wrapU(sI - R + r)) + c0 - 6);
-                gy[r][0] = dcent1(uv, 6) * ihy2;
-                gy[r][1] = dcent1(uv, 7) * ihy2;
-            }
+            for (int r = 0; r < RB; r++) gy[r] = mul2(dcent2(rowU(wrapU(sI - R + r)), c), ihy2);
         }
         float2 lj[RB];
 #pragma unroll
@@ -326,17 +295,16 @@ __global__ void __launch_bounds__(NT) fdtd2d_step(const __grid_constant__ Step2D
             float2 gx;
             if constexpr (STAG) {
                 // flux at half-row (i-5+r)+1/2 from u rows i-9+r .. i+r (queue index r .. r+9)
-                float2 v = mul2(dstag2<QL>(uq, r + 5, r + 4), f2(ihx));
-                if constexpr (VARB) v = mul2(v, bxi[r]);
+                float2 v = mul2(dstag2(uq, r + 5, r + 4), ihx);
+                if constexpr (VARB) v = mul2(v, f2(bxi[r]));
                 fq[QB + r] = v;
                 // D- at row j+r from fluxes at half-rows j+r-5 .. j+r+4 (queue index r .. r+9)
-                gx = mul2(dstag2<QL>(fq, r + 5, r + 4), f2(ihx));
+                gx = mul2(dstag2(fq, r + 5, r + 4), ihx);
             } else {
-                gx = mul2(dcent2<QL>(uq, r + 5), f2(ihx2));  // rows i+r-10 .. i+r
+                gx = mul2(dcent2(uq, r + 5), ihx2);  // rows i+r-10 .. i+r
             }
-            const bool row_in = j + r >= 0 && j + r < a.nx;
-            float2 v = mul2(Wj[r], add2(gx, make_float2(gy[r][0], gy[r][1])));
-            lj[r] = make_float2(row_in && in0 ? v.x : 0.f, row_in && in1 ? v.y : 0.f);  // zero halo
+            const bool keep = j + r >= 0 && j + r < a.nx && c_in;  // zero halo of the intermediate
+            lj[r] = keep ? mul2(f2(Wj[r]), add2(gx, gy[r])) : f2(0.f);
         }
         qshift<QL, RB>(uq);
         if constexpr (STAG) qshift<QL, RB>(fq);
@@ -347,62 +315,46 @@ __global__ void __launch_bounds__(NT) fdtd2d_step(const __grid_constant__ Step2D
             auto wrapL = [](int sl) { return sl < 0 ? sl + QLR : (sl >= QLR ? sl - QLR : sl); };
 #pragma unroll
             for (int r = 0; r < RB; r++) {
-                *reinterpret_cast<float2*>(sLr + wrapL(sJ + r) * L::WL + 2 * tid) = lj[r];  // l(j+r, Lc+k)
+                sLr[wrapL(sJ + r) * L::WL + tid] = lj[r];  // l(j+r, L1 + k)
                 lq[QB + r] = lj[r];
             }
             __syncthreads();
-            float gy2[RB][2];
+            float2 gy2[RB];
+            const bool s2 = (tid >= H1) && (tid < H1 + BY);
             if constexpr (STAG) {
 #pragma unroll
                 for (int r = 0; r < RB; r++) {
-                    const float* sl = sLr + wrapL(sJ - R + r) * L::WL;  // l(o+r, Lc + k)
-                    if (2 * tid < BY + 10) {
-                        const int f = 2 * tid;  // flux at half-col y0-6+f: l index f .. f+11
-                        float lv[12];
-                        lds_pairs<12>(lv, sl + f);
-                        float2 fl = make_float2(dstag1(lv, 5, 4), dstag1(lv, 6, 5));
-                        fl = mul2(fl, f2(ihy));
-                        if constexpr (VARB) fl = mul2(fl, by2[r]);
-                        *reinterpret_cast<float2*>(sF2 + r * L::WF + f) = fl;
+                    const float2* sl = sLr + wrapL(sJ - R + r) * L::WL;  // l(o+r, L1 + k)
+                    if (tid < BY + 9) {
+                        const int k = tid;  // flux at half-col y0-5+k from l index k .. k+9
+                        float2 v = mul2(dstag2(sl, k + 5, k + 4), ihy);
+                        if constexpr (VARB) v = mul2(v, f2(by2[r]));
+                        sF2[r * L::WF + k] = v;
                     }
                 }
                 __syncthreads();
 #pragma unroll
-                for (int r = 0; r < RB; r++) {
-                    gy2[r][0] = gy2[r][1] = 0.f;
-                    if (outp) {
-                        float fv[12];
-                        lds_pairs<12>(fv, sF2 + r * L::WF + (c0 - y0));
-                        gy2[r][0] = dstag1(fv, 6, 5) * ihy;
-                        gy2[r][1] = dstag1(fv, 7, 6) * ihy;
-                    }
-                }
+                for (int r = 0; r < RB; r++)
+                    gy2[r] = s2 ? mul2(dstag2(sF2 + r * L::WF, tid - H1 + 5, tid - H1 + 4), ihy) : f2(0.f);
             } else {
 #pragma unroll
-                for (int r = 0; r < RB; r++) {
-                    gy2[r][0] = gy2[r][1] = 0.f;
-                    if (outp) {
-                        float lv[14];
-                        lds_pairs<14>(lv, sLr + wrapL(sJ - R + r) * L::WL + 2 * tid - 6);
-                        gy2[r][0] = dcent1(lv, 6) * ihy2;
-                        gy2[r][1] = dcent1(lv, 7) * ihy2;
-                    }
-                }
+                for (int r = 0; r < RB; r++)
+                    gy2[r] = s2 ? mul2(dcent2(sLr + wrapL(sJ - R + r) * L::WL, tid), ihy2) : f2(0.f);
             }
 #pragma unroll
             for (int r = 0; r < RB; r++) {
                 float2 gx2;
                 if constexpr (STAG) {
-                    float2 v = mul2(dstag2<QL>(lq, r + 5, r + 4), f2(ihx));
-                    if constexpr (VARB) v = mul2(v, bxj[r]);
+                    float2 v = mul2(dstag2(lq, r + 5, r + 4), ihx);
+                    if constexpr (VARB) v = mul2(v, f2(bxj[r]));
                     f2q[QB + r] = v;
-                    gx2 = mul2(dstag2<QL>(f2q, r + 5, r + 4), f2(ihx));
+                    gx2 = mul2(dstag2(f2q, r + 5, r + 4), ihx);
                 } else {
-                    gx2 = mul2(dcent2<QL>(lq, r + 5), f2(ihx2));
+                    gx2 = mul2(dcent2(lq, r + 5), ihx2);
                 }
                 // l(o+r): queue index r (STAG, rows j-9..) or r+5 (laplace, rows j-10..)
                 const float2 lo = STAG ? lq[r] : lq[r + 5];
-                Lt[r] = fma2(f2(k12), mul2(Wo[r], add2(gx2, make_float2(gy2[r][0], gy2[r][1]))), lo);
+                Lt[r] = fma2(k12, mul2(f2(Wo[r]), add2(gx2, gy2[r])), lo);
             }
             qshift<QL, RB>(lq);
             if constexpr (STAG) qshift<QL, RB>(f2q);
@@ -415,41 +367,34 @@ __global__ void __launch_bounds__(NT) fdtd2d_step(const __grid_constant__ Step2D
 #pragma unroll
         for (int r = 0; r < RB; r++) {
             const int orow = o + r;
-            if (orow >= xo0 && orow < xo1 && outp) {
-                const long long idx = (long long)orow * pitch + c0;
-                const float2 u_o = *reinterpret_cast<const float2*>(rowU(wrapU(sI - S * R + r)) + c0);
+            if (orow >= xo0 && orow < xo1 && out_col) {
+                const long long idx = (long long)orow * pitch + c;  // float2 index within the pair
+                const float2 u_o = rowU(wrapU(sI - S * R + r))[c];
                 const float2 pm = pmo[r];
-                float2 pn = fma2(c1[r], Lt[r], fma2(c2[r], u_o, mul2(c3[r], make_float2(-pm.x, -pm.y))));
+                float2 pn = fma2(f2(c1[r]), Lt[r], fma2(f2(c2[r]), u_o, mul2(f2(-c3[r]), pm)));
                 // injection into the new level (sources forward, receivers adjoint)
                 while (inj_ptr < inj_e && a.inj[inj_ptr].row < orow) inj_ptr++;
                 for (int q = inj_ptr; q < inj_e; q++) {
                     const Inject E = a.inj[q];
                     if (E.row != orow) break;
-                    const float amp = E.coef * a.inj_amp[(long long)a.t * a.inj_ld + E.point];
-                    if (E.col == c0) pn.x = pn.x + amp;
-                    if (E.col == c0 + 1) pn.y = pn.y + amp;
+                    if (E.col == c) {
+                        const float amp = E.coef * a.inj_amp[(long long)a.t * a.inj_ld + E.point];
+                        if (E.lane) pn.y = pn.y + amp;
+                        else pn.x = pn.x + amp;
+                    }
                 }
-                const long long sbase = (long long)shot * a.snap_shot_stride + (long long)(a.t / a.f) * a.snap_stride + idx;
+                float2* snap = reinterpret_cast<float2*>(a.snaps) + (long long)pair * a.snap_shot_stride +
+                               (long long)(a.t / a.f) * a.snap_stride + idx;
                 if (do_save) {
-                    const float2 sv = make_float2((pn.x - 2.f * u_o.x + pm.x) / dt2, (pn.y - 2.f * u_o.y + pm.y) / dt2);
-                    if (in1) *reinterpret_cast<float2*>(a.snaps + sbase) = sv;
-                    else a.snaps[sbase] = sv.x;
+                    *snap = make_float2((pn.x - 2.f * u_o.x + pm.x) / dt2, (pn.y - 2.f * u_o.y + pm.y) / dt2);
                 }
-                if (do_grad && orow >= a.ix0 && orow < a.ix1) {
-                    const long long gi = soff + idx;
-                    if (c0 >= a.iy0 && c0 < a.iy1) {
-                        const float sv = a.snaps[sbase];
-                        a.gradb[gi] += sv * u_o.x;
-                        a.precb[gi] += sv * sv;
-                    }
-                    if (c0 + 1 >= a.iy0 && c0 + 1 < a.iy1) {
-                        const float sv = a.snaps[sbase + 1];
-                        a.gradb[gi + 1] += sv * u_o.y;
-                        a.precb[gi + 1] += sv * sv;
-                    }
+                if (do_grad && orow >= a.ix0 && orow < a.ix1 && c >= a.iy0 && c < a.iy1) {
+                    const float2 sv = *snap;
+                    const long long gi = (long long)pair * a.grad_stride + (long long)orow * pitch + c;
+                    a.gradb[gi] += sv.x * u_o.x + sv.y * u_o.y;
+                    a.precb[gi] += sv.x * sv.x + sv.y * sv.y;
                 }
-                if (in1) *reinterpret_cast<float2*>(prev + idx) = pn;
-                else prev[idx] = pn.x;
+                prev[idx] = pn;
             }
         }
         sI = sI + RB >= QU ? sI + RB - QU : sI + RB;

@@ -6,7 +6,10 @@
 namespace sa {
 
 constexpr int RB = 2;  // rows per iteration
-constexpr int PF = 2;  // iterations prefetched ahead
+#ifndef SA_PF
+#define SA_PF 2
+#endif
+constexpr int PF = SA_PF;  // iterations prefetched ahead
 
 template <bool OT4, int NT>
 static cudaError_t go(dim3 grid, cudaStream_t s, const Step2D& a) {
@@ -16,6 +19,9 @@ static cudaError_t go(dim3 grid, cudaStream_t s, const Step2D& a) {
         cudaError_t e = cudaFuncSetAttribute(fdtd2d_step<2, OT4, NT, RB, PF>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
         if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(fdtd2d_step<2, OT4, NT, RB, PF>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
         configured = true;
     }
     fdtd2d_step<2, OT4, NT, RB, PF><<<grid, NT, bytes, s>>>(a);
@@ -24,9 +30,10 @@ static cudaError_t go(dim3 grid, cudaStream_t s, const Step2D& a) {
 
 cudaError_t launch_step2d_k2(bool ot4, int nt_threads, dim3 grid, cudaStream_t s, const Step2D& a) {
     switch (nt_threads) {
-        case 64: return ot4 ? go<true, 64>(grid, s, a) : go<false, 64>(grid, s, a);
         case 96: return ot4 ? go<true, 96>(grid, s, a) : go<false, 96>(grid, s, a);
         case 128: return ot4 ? go<true, 128>(grid, s, a) : go<false, 128>(grid, s, a);
+        case 160: return ot4 ? go<true, 160>(grid, s, a) : go<false, 160>(grid, s, a);
+        case 192: return ot4 ? go<true, 192>(grid, s, a) : go<false, 192>(grid, s, a);
         default: return cudaErrorInvalidValue;
     }
 }

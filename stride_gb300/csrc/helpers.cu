@@ -109,10 +109,10 @@ __global__ void gather_final2d(const float* __restrict__ field, long long shot_s
                                const Gather* __restrict__ g, int n, float* out, int ld, int trow) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
-    const Gather G = g[e];
-    const float* f = field + (long long)G.pad * shot_stride;
-    const long long i0 = (long long)G.row * pitch + G.col, i1 = i0 + pitch;
-    out[(long long)trow * ld + G.point] = G.w00 * f[i0] + G.w01 * f[i0 + 1] + G.w10 * f[i1] + G.w11 * f[i1 + 1];
+    const Gather G = g[e];  // pad = shot: pair pad / 2, lane pad % 2 of the interleaved field
+    const float* f = field + (long long)(G.pad / 2) * shot_stride * 2 + (G.pad & 1);
+    const long long i0 = 2 * ((long long)G.row * pitch + G.col), i1 = i0 + 2 * (long long)pitch;
+    out[(long long)trow * ld + G.point] = G.w00 * f[i0] + G.w01 * f[i0 + 2] + G.w10 * f[i1] + G.w11 * f[i1 + 2];
 }
 
 __global__ void reduce_shots2d(const float* __restrict__ buf, long long shot_stride, int nshots, int nx, int ny,

@@ -77,7 +77,7 @@ constexpr double kDbToNeper = 100.0 / (20.0 * 0.43429448190325176);  // 100 / (2
 struct sa_plan {
     sa_desc d{};
     int nx = 0, ny = 0, pitch = 0, pitch_b = 0;
-    long long shot_stride = 0;
+    long long shot_stride = 0;  // nx * pitch: float2 elements per shot pair (wavefields are pair-interleaved)
     int kind = 0;
     bool ot4 = true;
     float* field[2] = {nullptr, nullptr};
@@ -130,21 +130,17 @@ struct sa_plan {
 
 namespace {
 
+int npairs(const sa_plan* p) { return (p->n_shots + 1) / 2; }
 int halo1(const sa_plan* p) { return p->ot4 ? (p->kind == 0 ? 5 : 9) : 0; }
 int radius(const sa_plan* p) { return p->kind == 0 ? 5 : 9; }
-// output columns of a CTA of `nt` threads (each thread owns a column pair; the stage-1 columns
-// start at an even column HL = H1 rounded up to even before the strip)
-int bymax(const sa_plan* p, int nt) {
-    const int H1 = halo1(p);
-    return (2 * nt - (H1 + (H1 & 1)) - H1) & ~1;
-}
-const int kThreads[] = {64, 96, 128};
+// output columns of a CTA of `nt` threads (one column per thread, halo H1 on both sides)
+int bymax(const sa_plan* p, int nt) { return nt - 2 * halo1(p); }
+const int kThreads[] = {96, 128, 160, 192};
 void set_strips(sa_plan* p, int nt) {
     p->NT = nt;
     const int bm = bymax(p, nt);
     p->nstrips = (p->ny + bm - 1) / bm;
-    const int by = (p->ny + p->nstrips - 1) / p->nstrips;
-    p->by = (by + 1) & ~1;
+    p->by = (p->ny + p->nstrips - 1) / p->nstrips;
 }
 
 void drop_graphs(sa_plan* p) {
@@ -189,7 +185,7 @@ void default_layout(sa_plan* p) {
     // enough CTAs to fill 152 SMs several times; each chunk keeps >= 4 pipeline depths of rows
     const int S = p->ot4 ? 2 : 1;
     const int minrows = 4 * S * radius(p);
-    const int shots = std::max(1, p->n_shots);
+    const int shots = std::max(1, npairs(p));
     const int target = 152 * 6;
     int nchunks = (target + p->nstrips * shots - 1) / (p->nstrips * shots);
     nchunks = std::max(1, std::min(nchunks, p->nx / minrows));
@@ -200,16 +196,18 @@ void default_layout(sa_plan* p) {
 struct HostInject {
     int cta, row, col, point;
     float coef;
+    int lane;
 };
 
 // Builds the per-CTA source/receiver lists for the current layout.
 int build_lists(sa_plan* p) {
     drop_graphs(p);
     const int nc = p->nchunks, ns = p->nstrips;
-    const int ncta = p->n_shots * nc * ns;
+    const int ncta = npairs(p) * nc * ns;
     const double h = std::max(p->d.spacing[0], p->d.spacing[1]);
     const double dt = p->d.dt;
-    auto cta_of = [&](int shot, int x, int y) { return (shot * nc + x / p->chunk_rows) * ns + y / p->by; };
+    // shots advance in pairs (the two lanes of a float2); CTA index of (pair, chunk, strip)
+    auto cta_of = [&](int shot, int x, int y) { return ((shot / 2) * nc + x / p->chunk_rows) * ns + y / p->by; };
     auto make_inj = [&](const std::vector<int>& off, const std::vector<int>& bx, const std::vector<int>& by,
                         const std::vector<double>& fx, const std::vector<double>& fy, double scale, int vp_power,
                         std::vector<HostInject>& out) {
@@ -222,7 +220,7 @@ int build_lists(sa_plan* p) {
                         const double w = (cx ? fx[i] : 1.0 - fx[i]) * (cy ? fy[i] : 1.0 - fy[i]);
                         const float v = p->vp_host.empty() ? 0.f : p->vp_host[(size_t)x * p->ny + y];
                         const double vpow = vp_power == 2 ? (double)(v * v) : (double)v;
-                        out.push_back({cta_of(s, x, y), x, y, i, (float)(w * scale * vpow)});
+                        out.push_back({cta_of(s, x, y), x, y, i, (float)(w * scale * vpow), s & 1});
                     }
         std::stable_sort(out.begin(), out.end(), [](const HostInject& a, const HostInject& b) {
             return a.cta != b.cta ? a.cta < b.cta : a.row < b.row;
@@ -233,7 +231,7 @@ int build_lists(sa_plan* p) {
         std::vector<sa::Inject> l(in.size());
         std::vector<int> off(ncta + 1, 0);
         for (size_t k = 0; k < in.size(); k++) {
-            l[k] = {in[k].row, in[k].col, in[k].point, in[k].coef};
+            l[k] = {in[k].row, in[k].col, in[k].point, in[k].coef, in[k].lane, {0, 0, 0}};
             off[in[k].cta + 1]++;
         }
         for (int c = 0; c < ncta; c++) off[c + 1] += off[c];
@@ -298,6 +296,7 @@ sa::Step2D base_args(const sa_plan* p) {
     a.ny = p->ny;
     a.pitch = p->pitch;
     a.shot_stride = p->shot_stride;
+    a.grad_stride = p->shot_stride;
     a.chunk_rows = p->chunk_rows;
     a.by = p->by;
     a.W = row0(p, p->W, p->pitch);
@@ -325,7 +324,7 @@ sa::Step2D base_args(const sa_plan* p) {
 
 // Issues the forward time loop t = 1..nt-2 (iso_acoustic/devito.py:575-581) on stream s.
 int issue_forward(sa_plan* p, bool save, cudaStream_t s) {
-    const size_t fbytes = (size_t)p->n_shots * p->shot_stride * sizeof(float);
+    const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
     CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
     CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
     CK(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * p->n_rec * sizeof(float), s));
@@ -339,7 +338,7 @@ int issue_forward(sa_plan* p, bool save, cudaStream_t s) {
     a.gat_ld = p->n_rec;
     a.save = save ? 1 : 0;
     a.grad = 0;
-    const dim3 grid(p->nstrips, p->nchunks, p->n_shots);
+    const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     long long n = 0;
     for (int t = 1; t <= p->d.nt - 2; t++) {
         a.t = t;
@@ -363,11 +362,12 @@ int issue_forward(sa_plan* p, bool save, cudaStream_t s) {
 
 // Issues the reverse-time adjoint loop t = nt-1-f .. 1 (devito.py:915-920).
 int issue_adjoint(sa_plan* p, cudaStream_t s) {
-    const size_t fbytes = (size_t)p->n_shots * p->shot_stride * sizeof(float);
+    const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
+    const size_t gbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float);
     CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
     CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
-    CK(cudaMemsetAsync(p->gradb, 0, fbytes, s));
-    CK(cudaMemsetAsync(p->precb, 0, fbytes, s));
+    CK(cudaMemsetAsync(p->gradb, 0, gbytes, s));
+    CK(cudaMemsetAsync(p->precb, 0, gbytes, s));
     sa::Step2D a = base_args(p);
     a.inj = p->n_rec ? p->inj_rec : nullptr;
     a.inj_off = p->inj_rec_off;
@@ -376,7 +376,7 @@ int issue_adjoint(sa_plan* p, cudaStream_t s) {
     a.gat = nullptr;
     a.save = 0;
     a.grad = 1;
-    const dim3 grid(p->nstrips, p->nchunks, p->n_shots);
+    const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     const int T0 = p->d.nt - 1 - p->d.undersampling;
     long long n = 0;
     for (int t = T0; t >= 1; t--) {
@@ -447,7 +447,7 @@ int store_transposed(sa_plan* p, const float* tm, int rows, int cols, float* use
 }
 
 int ensure_fields(sa_plan* p) {
-    const size_t n = (size_t)std::max(1, p->d.max_shots) * p->shot_stride;
+    const size_t n = (size_t)((std::max(1, p->d.max_shots) + 1) / 2) * p->shot_stride * 2;
     CKR(ensure(&p->field[0], &p->field_cap[0], n));
     CKR(ensure(&p->field[1], &p->field_cap[1], n));
     return SA_OK;
@@ -646,7 +646,7 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
     cudaStream_t s = (cudaStream_t)stream;
     const bool save = save_mode == SA_SAVE_SNAPSHOTS;
     if (save) {
-        const size_t n = (size_t)p->n_shots * p->snap_shot_stride;
+        const size_t n = (size_t)npairs(p) * p->snap_shot_stride * 2;
         float* old = p->snaps;
         CKR(ensure(&p->snaps, &p->cap_snaps, n));
         if (old != p->snaps) drop_graphs(p);
@@ -666,7 +666,7 @@ int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_v
     if (!p->snaps_valid) return fail(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS");
     if ((p->n_rec && !residuals) || !grad_vp || !prec_vp) return fail(SA_E_INVALID, "null residuals or outputs");
     cudaStream_t s = (cudaStream_t)stream;
-    const size_t fe = (size_t)p->n_shots * p->shot_stride;
+    const size_t fe = (size_t)npairs(p) * p->shot_stride;
     float *og = p->gradb, *op = p->precb;
     CKR(ensure(&p->gradb, &p->cap_gradb, fe));
     CKR(ensure(&p->precb, &p->cap_precb, fe));
@@ -678,10 +678,10 @@ int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_v
         float* user = k == 0 ? grad_vp : prec_vp;
         const float* buf = k == 0 ? p->gradb : p->precb;
         if (is_device(user)) {
-            CK(sa::reduce_shots(buf, p->shot_stride, p->n_shots, p->nx, p->ny, p->pitch, user, s));
+            CK(sa::reduce_shots(buf, p->shot_stride, npairs(p), p->nx, p->ny, p->pitch, user, s));
         } else {
             CKR(ensure(&p->stage, &p->cap_stage, N));
-            CK(sa::reduce_shots(buf, p->shot_stride, p->n_shots, p->nx, p->ny, p->pitch, p->stage, s));
+            CK(sa::reduce_shots(buf, p->shot_stride, npairs(p), p->nx, p->ny, p->pitch, p->stage, s));
             CK(cudaMemcpyAsync(user, p->stage, N * sizeof(float), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
         }
@@ -720,7 +720,7 @@ int sa_autotune(sa_plan* p, void* stream) {
         a.gat = nullptr;
         a.cur = p->field[0];
         a.prev = p->field[1];
-        const dim3 grid(p->nstrips, p->nchunks, p->n_shots);
+        const dim3 grid(p->nstrips, p->nchunks, npairs(p));
         for (int w = 0; w < 3; w++) {
             a.t = 1 + w;
             CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
