@@ -115,7 +115,7 @@ def workload(name, seed=0, nt=None, n_shots=None, inner=None):
     else:
         vpi, rhoi, ali = ellipse_phantom(shape, spacing, ne, rng, rho_range=(950., 1100.), alpha_range=(0., 1.))
     centre = ((n - 1) * h / 2, (n - 1) * h / 2)
-    radius = min(55e-3, 0.42 * (n - 1) * h)
+    radius = min(55e-3, 0.45 * (n - 1) * h)  # 55 mm, or less on reduced test grids
     geo = circle_geometry(ntr, radius, centre, jitter=0.5 if name == 'batched' else 0.0, spacing=spacing, rng=rng)
     dt = 0.6 * h / 1650.
     nt = steps if nt is None else nt
