@@ -36,10 +36,10 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 HBM_FALLBACK_GBS = 6800.0
-# dram__bytes_read.sum + dram__bytes_write.sum per launch of fdtd2d_step on this workload's
-# batch (64 shots of 552^2), from the ncu capture summarised in
-# profiles/fdtd2d_step_fwdadj_552sq_64shots.md (None when no capture exists yet).
-NCU_TRAFFIC_PER_LAUNCH = None
+# dram__bytes_read.sum + dram__bytes_write.sum of one fdtd2d_step launch on this workload's
+# batch (64 shots of 552^2, forward step with wavefield save), from the ncu capture summarised
+# in profiles/fdtd2d_step_fwdadj_552sq_64shots.md.
+NCU_TRAFFIC_PER_LAUNCH = 180.294656e6 + 102.961664e6
 
 
 def workload_config(nt=None, n_shots=64, rank=0):
@@ -291,7 +291,9 @@ def gb300_arm(args):
     pts_adj = N * n_shots * (nt - 1 - 4)
     pts_step = pts_fwd + pts_adj
     value = pts_step * world / (ms_step * 1e-3) / 1e9
-    assert torch.isfinite(grad).all() and float(grad.abs().max()) > 0, 'gradient is empty or not finite'
+    assert torch.isfinite(grad).all(), 'gradient is not finite'
+    if nt >= 1000:  # by then the waves have reached the receivers
+        assert float(grad.abs().max()) > 0, 'gradient is empty'
 
     # roofline of the step kernel: algorithmic bytes per launch / average launch time
     t_fwd = sum(a.elapsed_time(b) for a, b in fwd_ms) / len(fwd_ms)
