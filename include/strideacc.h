@@ -100,6 +100,22 @@ int sa_adjoint(sa_plan* plan, const float* residuals, float* grad_vp, float* pre
  * (no counterpart in the reference, whose Devito autotuner is optional: common/devito.py:1043). */
 int sa_autotune(sa_plan* plan, void* stream);
 
+/* Single-shot 2D forward modelling that allocates no device memory (no counterpart in the
+ * reference). For callers that cannot let a library allocate GPU memory, e.g. an application
+ * whose memory pool owns the whole device, or a loop that must not pay the device-wide
+ * synchronisation of cudaFree. It runs the same time-step kernel as sa_forward with every
+ * scratch buffer in one 32 MiB __device__ array of the library (held by each GPU that loads the
+ * library until exit). Limits: extended grid at most 640 x 640, 16 sources, 1024 receivers,
+ * and everything must fit the array (else SA_E_INVALID). desc gives the grid, dt, nt, kernel,
+ * density and attenuation modes (max_shots and undersampling are not used). vp/rho/alpha
+ * (unpadded extended grid), wavelets [n_src, nt] (as src.data) and traces [n_rec, nt] are
+ * device pointers; src_xyz/rec_xyz are host [n, 2] coordinates, already shifted by +1e-3*h.
+ * The first call on a device looks up the array's address with that device current: make it
+ * before any stream capture. Calls share the array, so calls that overlap on the GPU race. */
+int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const float* rho, const float* alpha, int n_src,
+                          const float* src_xyz, const float* wavelets, int n_rec, const float* rec_xyz, float* traces,
+                          void* stream);
+
 /* Copies the message of the last failed call on this thread (NUL-terminated, truncated to len). */
 int sa_last_error(char* buf, int len);
 

@@ -30,7 +30,7 @@ SA_GRAD_PARITY = 0
 
 # every symbol include/strideacc.h declares
 EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometry', 'sa_forward',
-           'sa_adjoint', 'sa_autotune', 'sa_last_error', 'sa_launch_count')
+           'sa_adjoint', 'sa_autotune', 'sa_last_error', 'sa_launch_count', 'sa_forward_2d_noalloc')
 
 
 class SaDesc(ctypes.Structure):

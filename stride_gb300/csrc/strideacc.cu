@@ -74,6 +74,11 @@ constexpr double kDbToNeper = 100.0 / (20.0 * 0.43429448190325176);  // 100 / (2
 
 }  // namespace
 
+namespace sa {
+// Message returned by sa_last_error for entry points defined in other translation units.
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace sa
+
 struct sa_plan {
     sa_desc d{};
     int nx = 0, ny = 0, pitch = 0, pitch_b = 0;
