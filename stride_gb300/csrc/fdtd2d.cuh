@@ -34,12 +34,26 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 
 __host__ __device__ constexpr int round4(int x) { return (x + 3) / 4 * 4; }
 
-// ---- packed FP32 helpers (sm_100 family f32x2 instructions) ----------------------------------
+// ---- arithmetic on the two lanes of a shot pair ---------------------------------------------
+// SA_PACKED=1 issues the sm_100-family f32x2 instructions; 0 issues two scalar FP32
+// instructions, which take immediate operands (the FD weights) without register pairs.
+#ifndef SA_PACKED
+#define SA_PACKED 0
+#endif
 __device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+#if SA_PACKED
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
+#else
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return make_float2(a.x * b.x, a.y * b.y); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+#endif
 
 // Staggered first derivative sum_m w_m (v[hi+m] - v[lo-m]) over float2 values (queue or shared).
 template <class A>

@@ -1,0 +1,31 @@
+// Instantiations of the 3D passes for operator kind 0 (0 laplace, 1 variable density,
+// 2 constant density).
+#include "fdtd3d.cuh"
+#include "launch.h"
+
+namespace sa {
+
+namespace {
+constexpr int TY = 8, TZ = 32, RB = 2, PF = 1;
+
+template <bool FINAL, bool OT4>
+cudaError_t go(dim3 grid, cudaStream_t s, const Step3D& a) {
+    constexpr size_t bytes = Smem3D<0, TY, TZ, RB, PF>::bytes;
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(fdtd3d_pass<0, FINAL, OT4, TY, TZ, RB, PF>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    fdtd3d_pass<0, FINAL, OT4, TY, TZ, RB, PF><<<grid, TY * TZ, bytes, s>>>(a);
+    return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_step3d_k0(bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a) {
+    if (!final_pass) return go<false, true>(grid, s, a);
+    return ot4 ? go<true, true>(grid, s, a) : go<true, false>(grid, s, a);
+}
+
+}  // namespace sa

@@ -13,6 +13,24 @@ cudaError_t medium2d(const float* vp_in, const float* rho_in, const float* alpha
                      float* alpha, float* buoy, float* bxh, float* byh, float* C1, float* C2, float* C3,
                      cudaStream_t s);
 void set_last_error(const char* msg);
+
+// 3D plans
+struct Sponge3 {
+    int a[3];
+    float s[3][MAX_ABS];
+};
+struct Sparse3D;
+cudaError_t medium3d(const float* vp_in, const float* rho_in, const float* alpha_in, int nx, int ny, int nz, int zp,
+                     int zpb, int density, double db_to_np, const Sponge3& sp, float dt, float* W, float* vp,
+                     float* alpha, float* buoy, float* bxh, float* byh, float* bzh, float* C1, float* C2, float* C3,
+                     cudaStream_t s);
+cudaError_t sparse3d_inject(const Sparse3D& sp, int n, const float* amp, int ld, int t, float* field,
+                            long long shot_stride, int ny, int zp, float* snap, long long snap_shot_stride,
+                            long long snap_off, float inv_dt2, cudaStream_t s);
+cudaError_t sparse3d_gather(const Sparse3D& sp, int n, const float* field, long long shot_stride, int ny, int zp,
+                            float* out, int ld, int trow, cudaStream_t s);
+cudaError_t reduce3d(const float* buf, long long shot_stride, int nshots, int nx, int ny, int nz, int zp, float* out,
+                     cudaStream_t s);
 cudaError_t transpose(const float* in, int rows, int cols, float* out, cudaStream_t s);
 cudaError_t final_gather2d(const float* field, long long shot_stride, int pitch, const Gather* g, int n, float* out,
                            int ld, int trow, cudaStream_t s);

@@ -1,0 +1,165 @@
+// Device helpers of 3D plans: medium preparation, sparse injection / interpolation and the
+// reduction of per-shot gradients. Layout [x][y][zp], z contiguous.
+#include "fdtd3d.cuh"
+#include "helpers.h"
+
+namespace sa {
+
+// W = vp^2 (or vp^2 rho), buoyancy 1/rho, vp and alpha (Np/m) scratch
+// (iso_acoustic/devito.py:476-497). Inputs unpadded [nx][ny][nz].
+__global__ void k_medium3d(const float* __restrict__ vp_in, const float* __restrict__ rho_in,
+                           const float* __restrict__ alpha_in, int nx, int ny, int nz, int zp, int density,
+                           double db_to_np, float* W, float* vp, float* alpha, float* buoy) {
+    const long long n = (long long)nx * ny * nz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const long long xy = q / nz;
+        const int z = (int)(q % nz);
+        const long long p = xy * zp + z;
+        const float v = vp_in[q];
+        vp[p] = v;
+        float w = v * v;
+        if (density == 1) {
+            const float r = rho_in[q];
+            w = w * r;
+            buoy[p] = 1.f / r;
+        }
+        W[p] = w;
+        alpha[p] = alpha_in ? (float)((double)alpha_in[q] * db_to_np) : 0.f;
+    }
+}
+
+// Buoyancy at half points along x, y and z (arithmetic mean of the two nodes, edge values
+// beyond the grid): bxh half-planes x = -5..nx+3 (pointer at x = 0, plane ny*zp);
+// byh[x][y+6][z] (row length zp, ny+12 rows per plane); bzh[x][y][z+6] (pitch zpb).
+__global__ void k_bhalf3d(const float* __restrict__ b, int nx, int ny, int nz, int zp, int zpb, float* bxh,
+                          float* byh, float* bzh) {
+    const long long nxa = (long long)(nx + 9) * ny * nz;
+    const long long nya = (long long)nx * (ny + 10) * nz;
+    const long long nza = (long long)nx * ny * (nz + 10);
+    const long long plane = (long long)ny * zp;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nxa + nya + nza;
+         q += (long long)gridDim.x * blockDim.x) {
+        if (q < nxa) {
+            const int z = (int)(q % nz), y = (int)((q / nz) % ny), x = (int)(q / ((long long)nz * ny)) - 5;
+            const int x0 = min(max(x, 0), nx - 1), x1 = min(max(x + 1, 0), nx - 1);
+            bxh[(long long)x * plane + (long long)y * zp + z] =
+                0.5f * (b[x0 * plane + (long long)y * zp + z] + b[x1 * plane + (long long)y * zp + z]);
+        } else if (q < nxa + nya) {
+            const long long r = q - nxa;
+            const int z = (int)(r % nz), yr = (int)((r / nz) % (ny + 10)), x = (int)(r / ((long long)nz * (ny + 10)));
+            const int y = yr - 6;
+            const int y0 = min(max(y, 0), ny - 1), y1 = min(max(y + 1, 0), ny - 1);
+            byh[(long long)x * (ny + 12) * zp + (long long)yr * zp + z] =
+                0.5f * (b[x * plane + (long long)y0 * zp + z] + b[x * plane + (long long)y1 * zp + z]);
+        } else {
+            const long long r = q - nxa - nya;
+            const int zr = (int)(r % (nz + 10)), y = (int)((r / (nz + 10)) % ny), x = (int)(r / ((long long)(nz + 10) * ny));
+            const int z = zr - 6;
+            const int z0 = min(max(z, 0), nz - 1), z1 = min(max(z + 1, 0), nz - 1);
+            bzh[(long long)x * ny * zpb + (long long)y * zpb + zr] =
+                0.5f * (b[x * plane + (long long)y * zp + z0] + b[x * plane + (long long)y * zp + z1]);
+        }
+    }
+}
+
+// Update coefficients (iso_acoustic/devito.py:1575-1581) with the SpongeBoundary2 damping; the
+// slab of axis a at layer e covers the points whose layers on the other axes are >= e
+// (boundaries/boundary.py:116-160).
+__global__ void k_coef3d(const float* __restrict__ vp, const float* __restrict__ alpha, int nx, int ny, int nz, int zp,
+                         Sponge3 sp, float dt, float* C1, float* C2, float* C3) {
+    const long long n = (long long)nx * ny * nz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(q % nz), y = (int)((q / nz) % ny), x = (int)(q / ((long long)nz * ny));
+        const long long p = ((long long)x * ny + y) * zp + z;
+        const int e[3] = {min(x, nx - 1 - x), min(y, ny - 1 - y), min(z, nz - 1 - z)};
+        float s = 0.f;
+        for (int a = 0; a < 3; a++) {
+            bool ok = e[a] < sp.a[a];
+            for (int b2 = 0; b2 < 3; b2++)
+                if (b2 != a && e[b2] < e[a]) ok = false;
+            if (ok) s += sp.s[a][e[a]];
+        }
+        const float v = vp[p], v2 = v * v;
+        const float d = 7.f * (s * v) * dt;
+        float beta = v2 * d;
+        beta = beta + alpha[p] * v;
+        beta = dt * beta;
+        const float den = 1.f + beta;
+        C1[p] = (dt * dt) / den;
+        C2[p] = (2.f - dt * dt * v2 * d * d) / den;
+        C3[p] = (1.f - beta) / den;
+    }
+}
+
+__global__ void inject3d(const Sparse3D s, int n, const float* amp, int ld, int t, float* field, long long shot_stride,
+                         int ny, int zp, float* snap, long long snap_shot_stride, long long snap_off, float inv_dt2) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 8 * n) return;
+    const int pnt = k >> 3, c = k & 7;
+    const int* b = s.base + 3 * pnt;
+    const int x = b[0] + ((c >> 2) & 1), y = b[1] + ((c >> 1) & 1), z = b[2] + (c & 1);
+    const long long idx = ((long long)x * ny + y) * zp + z;
+    const float v = s.coef[8 * pnt + c] * amp[(long long)t * ld + pnt];
+    const int sh = s.shot[pnt];
+    atomicAdd(field + (long long)sh * shot_stride + idx, v);
+    if (snap) atomicAdd(snap + (long long)sh * snap_shot_stride + snap_off + idx, v * inv_dt2);
+}
+
+__global__ void gather3d(const Sparse3D s, int n, const float* field, long long shot_stride, int ny, int zp, float* out,
+                         int ld, int trow) {
+    const int pnt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pnt >= n) return;
+    const int* b = s.base + 3 * pnt;
+    const float* f = field + (long long)s.shot[pnt] * shot_stride;
+    float acc = 0.f;
+    for (int c = 0; c < 8; c++) {
+        const int x = b[0] + ((c >> 2) & 1), y = b[1] + ((c >> 1) & 1), z = b[2] + (c & 1);
+        acc += s.w[8 * pnt + c] * f[((long long)x * ny + y) * zp + z];
+    }
+    out[(long long)trow * ld + pnt] = acc;
+}
+
+__global__ void k_reduce3d(const float* __restrict__ buf, long long shot_stride, int nshots, int nx, int ny, int nz,
+                           int zp, float* __restrict__ out) {
+    const long long n = (long long)nx * ny * nz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const long long p = (q / nz) * zp + q % nz;
+        float acc = 0.f;
+        for (int b2 = 0; b2 < nshots; b2++) acc += buf[(long long)b2 * shot_stride + p];
+        out[q] = acc;
+    }
+}
+
+cudaError_t medium3d(const float* vp_in, const float* rho_in, const float* alpha_in, int nx, int ny, int nz, int zp,
+                     int zpb, int density, double db_to_np, const Sponge3& sp, float dt, float* W, float* vp,
+                     float* alpha, float* buoy, float* bxh, float* byh, float* bzh, float* C1, float* C2, float* C3,
+                     cudaStream_t s) {
+    k_medium3d<<<2048, 256, 0, s>>>(vp_in, rho_in, alpha_in, nx, ny, nz, zp, density, db_to_np, W, vp, alpha, buoy);
+    if (density == 1) k_bhalf3d<<<2048, 256, 0, s>>>(buoy, nx, ny, nz, zp, zpb, bxh, byh, bzh);
+    k_coef3d<<<2048, 256, 0, s>>>(vp, alpha, nx, ny, nz, zp, sp, dt, C1, C2, C3);
+    return cudaGetLastError();
+}
+
+cudaError_t sparse3d_inject(const Sparse3D& sp, int n, const float* amp, int ld, int t, float* field,
+                            long long shot_stride, int ny, int zp, float* snap, long long snap_shot_stride,
+                            long long snap_off, float inv_dt2, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    inject3d<<<(8 * n + 127) / 128, 128, 0, s>>>(sp, n, amp, ld, t, field, shot_stride, ny, zp, snap, snap_shot_stride,
+                                                 snap_off, inv_dt2);
+    return cudaGetLastError();
+}
+
+cudaError_t sparse3d_gather(const Sparse3D& sp, int n, const float* field, long long shot_stride, int ny, int zp,
+                            float* out, int ld, int trow, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    gather3d<<<(n + 127) / 128, 128, 0, s>>>(sp, n, field, shot_stride, ny, zp, out, ld, trow);
+    return cudaGetLastError();
+}
+
+cudaError_t reduce3d(const float* buf, long long shot_stride, int nshots, int nx, int ny, int nz, int zp, float* out,
+                     cudaStream_t s) {
+    k_reduce3d<<<2048, 256, 0, s>>>(buf, shot_stride, nshots, nx, ny, nz, zp, out);
+    return cudaGetLastError();
+}
+
+}  // namespace sa

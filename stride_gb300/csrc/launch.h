@@ -7,6 +7,20 @@ cudaError_t launch_step2d_k0(bool ot4, int nt_threads, dim3 grid, cudaStream_t s
 cudaError_t launch_step2d_k1(bool ot4, int nt_threads, dim3 grid, cudaStream_t s, const Step2D& a);
 cudaError_t launch_step2d_k2(bool ot4, int nt_threads, dim3 grid, cudaStream_t s, const Step2D& a);
 
+struct Step3D;
+cudaError_t launch_step3d_k0(bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
+cudaError_t launch_step3d_k1(bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
+cudaError_t launch_step3d_k2(bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
+constexpr int kTile3dY = 8, kTile3dZ = 32;  // (y, z) tile of a 3D CTA (threads = their product)
+
+inline cudaError_t launch_step3d(int kind, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a) {
+    switch (kind) {
+        case 0: return launch_step3d_k0(final_pass, ot4, grid, s, a);
+        case 1: return launch_step3d_k1(final_pass, ot4, grid, s, a);
+        default: return launch_step3d_k2(final_pass, ot4, grid, s, a);
+    }
+}
+
 inline cudaError_t launch_step2d(int kind, bool ot4, int nt_threads, dim3 grid, cudaStream_t s, const Step2D& a) {
     switch (kind) {
         case 0: return launch_step2d_k0(ot4, nt_threads, grid, s, a);

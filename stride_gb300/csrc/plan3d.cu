@@ -1,0 +1,444 @@
+// 3D plans behind the same C ABI (include/strideacc.h): wavefields of every shot, the medium,
+// trilinear source/receiver lists, the undersampled wavefield and per-shot gradient
+// accumulators, and the time loops of the forward (iso_acoustic/devito.py:515-581) and of the
+// reverse-time adjoint with the vp imaging condition (devito.py:875-920, 985-1043).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "../../include/strideacc.h"
+#include "fdtd3d.cuh"
+#include "helpers.h"
+#include "launch.h"
+#include "plan3d.h"
+
+namespace sa {
+
+namespace {
+
+int fail3(int code, const char* msg) {
+    set_last_error(msg);
+    return code;
+}
+
+#define CK3(x)                                                                                 \
+    do {                                                                                       \
+        cudaError_t e_ = (x);                                                                  \
+        if (e_ != cudaSuccess) {                                                               \
+            char b_[512];                                                                      \
+            snprintf(b_, sizeof(b_), "%s: %s", #x, cudaGetErrorString(e_));                    \
+            return fail3(SA_E_CUDA, b_);                                                       \
+        }                                                                                      \
+    } while (0)
+
+template <class T>
+int alloc3(T** p, size_t n) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    if (cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail3(SA_E_NOMEM, "device allocation failed (3D plan)");
+    }
+    if (cudaMemset(*p, 0, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return fail3(SA_E_CUDA, "cudaMemset failed");
+    return SA_OK;
+}
+
+bool dev_ptr(const void* p) {
+    cudaPointerAttributes at;
+    if (!p || cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+void ramp(int A, double h, double refl, float* out) {
+    for (int e = 0; e < MAX_ABS; e++) out[e] = 0.f;
+    if (A <= 0) return;
+    double coef = 1.5 * std::log(1.0 / refl);
+    coef = A > 15 ? coef / (A * h) : 0.67 / h;
+    for (int e = 0; e < A; e++) {
+        double pos = std::fabs((A - e - 1) / (double)(A - 1));
+        pos = pos - std::sin(2 * M_PI * pos) / (2 * M_PI);
+        out[e] = (float)(coef * pos);
+    }
+}
+
+}  // namespace
+
+struct Plan3D {
+    sa_desc d{};
+    int nx = 0, ny = 0, nz = 0, zp = 0, zpb = 0, kind = 0;
+    bool ot4 = true;
+    long long plane = 0, field = 0;  // floats per x plane and per shot
+    float *F[2] = {nullptr, nullptr}, *Lbuf = nullptr;
+    float *W = nullptr, *C1 = nullptr, *C2 = nullptr, *C3 = nullptr, *bxh = nullptr, *byh = nullptr, *bzh = nullptr;
+    float *vp = nullptr, *alpha = nullptr, *buoy = nullptr, *stage = nullptr;
+    std::vector<float> vp_host;
+    Sponge3 sponge{};
+    int n_shots = 0, n_src = 0, n_rec = 0;
+    std::vector<int> so, ro;
+    std::vector<float> sx, rx;
+    // lists (device): shot, base, weights, injection coefficients
+    int *s_shot = nullptr, *s_base = nullptr, *r_shot = nullptr, *r_base = nullptr;
+    float *s_w = nullptr, *s_coef = nullptr, *r_w = nullptr, *r_coef = nullptr;
+    float *src_amp = nullptr, *rec_amp = nullptr, *tstage = nullptr;
+    size_t cap_tstage = 0;
+    float* snaps = nullptr;
+    int n_snap = 0;
+    long long snap_stride = 0;
+    bool snaps_valid = false, medium_set = false, geometry_set = false;
+    float *gradb = nullptr, *precb = nullptr;
+    long long launches = 0;
+    int chunk_rows = 0, nchunks = 1, ty0n = 1, tz0n = 1;
+};
+
+long long plan3d_launches(const Plan3D* p) { return p->launches; }
+
+int plan3d_create(const sa_desc& d, Plan3D** out) {
+    *out = nullptr;
+    Plan3D* p = new Plan3D();
+    p->d = d;
+    p->nx = d.shape[0];
+    p->ny = d.shape[1];
+    p->nz = d.shape[2];
+    p->zp = (p->nz + 2 + 31) / 32 * 32;
+    p->zpb = (p->nz + 12 + 31) / 32 * 32;
+    p->kind = d.density == SA_DENSITY_NONE ? 0 : (d.density == SA_DENSITY_VARIABLE ? 1 : 2);
+    p->ot4 = d.kernel == SA_KERNEL_OT4;
+    p->plane = (long long)p->ny * p->zp;
+    p->field = (long long)p->nx * p->plane;
+    p->n_snap = (d.nt + d.undersampling) / d.undersampling + 1;
+    p->snap_stride = p->field;
+    int amax = 0;
+    for (int a = 0; a < 3; a++) {
+        p->sponge.a[a] = d.absorbing[a];
+        amax = std::max(amax, d.absorbing[a]);
+    }
+    if (amax > 1) {
+        const double refl = std::pow(10.0, -(std::log10((double)amax) - 1) / std::log10(2.0) - 3);
+        for (int a = 0; a < 3; a++) ramp(d.absorbing[a], d.spacing[a], refl, p->sponge.s[a]);
+    }
+    const long long G = GUARD;
+    const size_t shots = std::max(1, d.max_shots);
+    int rc = SA_OK;
+    for (int k = 0; k < 2 && rc == SA_OK; k++) rc = alloc3(&p->F[k], shots * p->field);
+    if (rc == SA_OK && p->ot4) rc = alloc3(&p->Lbuf, shots * p->field);
+    const size_t guarded = (size_t)(p->nx + 2 * G) * p->plane;
+    if (rc == SA_OK) rc = alloc3(&p->W, guarded);
+    if (rc == SA_OK) rc = alloc3(&p->C1, guarded);
+    if (rc == SA_OK) rc = alloc3(&p->C2, guarded);
+    if (rc == SA_OK) rc = alloc3(&p->C3, guarded);
+    if (rc == SA_OK) rc = alloc3(&p->vp, (size_t)p->field);
+    if (rc == SA_OK) rc = alloc3(&p->alpha, (size_t)p->field);
+    if (rc == SA_OK && p->kind == 1) {
+        rc = alloc3(&p->buoy, (size_t)p->field);
+        if (rc == SA_OK) rc = alloc3(&p->bxh, (size_t)(p->nx + 9 + 2 * G) * p->plane);
+        if (rc == SA_OK) rc = alloc3(&p->byh, (size_t)(p->nx + 2 * G) * (p->ny + 12) * p->zp);
+        if (rc == SA_OK) rc = alloc3(&p->bzh, (size_t)(p->nx + 2 * G) * p->ny * p->zpb);
+    }
+    if (rc != SA_OK) {
+        plan3d_destroy(p);
+        return rc;
+    }
+    p->ty0n = (p->ny + kTile3dY - 1) / kTile3dY;
+    p->tz0n = (p->nz + kTile3dZ - 1) / kTile3dZ;
+    *out = p;
+    return SA_OK;
+}
+
+void plan3d_destroy(Plan3D* p) {
+    if (!p) return;
+    float* fb[] = {p->F[0], p->F[1], p->Lbuf, p->W, p->C1, p->C2, p->C3, p->bxh, p->byh, p->bzh, p->vp, p->alpha,
+                   p->buoy, p->stage, p->s_w, p->s_coef, p->r_w, p->r_coef, p->src_amp, p->rec_amp, p->tstage,
+                   p->snaps, p->gradb, p->precb};
+    for (float* b : fb)
+        if (b) cudaFree(b);
+    int* ib[] = {p->s_shot, p->s_base, p->r_shot, p->r_base};
+    for (int* b : ib)
+        if (b) cudaFree(b);
+    delete p;
+}
+
+int plan3d_set_medium(Plan3D* p, const float* vp, const float* rho, const float* alpha) {
+    const size_t N = (size_t)p->nx * p->ny * p->nz;
+    const float* in[3] = {vp, p->kind == 1 ? rho : nullptr, p->d.attenuation ? alpha : nullptr};
+    const float* dv[3] = {nullptr, nullptr, nullptr};
+    for (int k = 0; k < 3; k++) {
+        if (!in[k]) continue;
+        if (dev_ptr(in[k])) {
+            dv[k] = in[k];
+        } else {
+            if (!p->stage) {
+                int rc = alloc3(&p->stage, 3 * N);
+                if (rc != SA_OK) return rc;
+            }
+            CK3(cudaMemcpy(p->stage + k * N, in[k], N * sizeof(float), cudaMemcpyHostToDevice));
+            dv[k] = p->stage + k * N;
+        }
+    }
+    const long long g0 = (long long)GUARD * p->plane;
+    CK3(medium3d(dv[0], dv[1], dv[2], p->nx, p->ny, p->nz, p->zp, p->zpb, p->kind == 1 ? 1 : 0,
+                 100.0 / (20.0 * 0.43429448190325176), p->sponge, (float)p->d.dt, p->W + g0, p->vp, p->alpha, p->buoy,
+                 p->bxh ? p->bxh + (long long)(GUARD + 5) * p->plane : nullptr,
+                 p->byh ? p->byh + (long long)GUARD * (p->ny + 12) * p->zp : nullptr,
+                 p->bzh ? p->bzh + (long long)GUARD * p->ny * p->zpb : nullptr, p->C1 + g0, p->C2 + g0, p->C3 + g0, 0));
+    CK3(cudaDeviceSynchronize());
+    p->vp_host.resize(N);
+    CK3(cudaMemcpy(p->vp_host.data(), dv[0], N * sizeof(float), cudaMemcpyDeviceToHost));
+    p->medium_set = true;
+    p->snaps_valid = false;
+    if (p->geometry_set) return plan3d_set_geometry(p, p->n_shots, p->so.data(), p->sx.data(), p->ro.data(), p->rx.data());
+    return SA_OK;
+}
+
+// Trilinear corner weights of Devito's linear SparseTimeFunction (common/devito.py:580-653);
+// the injection coefficient at a corner carries the reference's scale and vp^k there.
+static int build_points(Plan3D* p, int n_shots, const int* off, const float* xyz, double scale, int vp_power,
+                        int** d_shot, int** d_base, float** d_w, float** d_coef) {
+    const int n = off[n_shots];
+    std::vector<int> shot(n), base(3 * n);
+    std::vector<float> w(8 * n), coef(8 * n);
+    for (int s = 0; s < n_shots; s++)
+        for (int i = off[s]; i < off[s + 1]; i++) {
+            double fr[3];
+            for (int a = 0; a < 3; a++) {
+                const double rel = ((double)xyz[3 * i + a] + p->d.extra[a] * p->d.spacing[a]) / p->d.spacing[a];
+                const int b = (int)std::floor(rel);
+                if (!(b >= 0 && b + 1 <= p->d.shape[a] - 1)) return fail3(SA_E_INVALID, "point outside the 3D grid");
+                base[3 * i + a] = b;
+                fr[a] = rel - b;
+            }
+            shot[i] = s;
+            for (int c = 0; c < 8; c++) {
+                const int cx = (c >> 2) & 1, cy = (c >> 1) & 1, cz = c & 1;
+                const double ww = (cx ? fr[0] : 1 - fr[0]) * (cy ? fr[1] : 1 - fr[1]) * (cz ? fr[2] : 1 - fr[2]);
+                w[8 * i + c] = (float)ww;
+                const int x = base[3 * i] + cx, y = base[3 * i + 1] + cy, z = base[3 * i + 2] + cz;
+                const float v = p->vp_host.empty() ? 0.f : p->vp_host[((size_t)x * p->ny + y) * p->nz + z];
+                const double vpow = vp_power == 2 ? (double)(v * v) : (double)v;
+                coef[8 * i + c] = (float)(ww * scale * vpow);
+            }
+        }
+    int rc = alloc3(d_shot, n);
+    if (rc == SA_OK) rc = alloc3(d_base, 3 * (size_t)n);
+    if (rc == SA_OK) rc = alloc3(d_w, 8 * (size_t)n);
+    if (rc == SA_OK) rc = alloc3(d_coef, 8 * (size_t)n);
+    if (rc != SA_OK) return rc;
+    if (n) {
+        CK3(cudaMemcpy(*d_shot, shot.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+        CK3(cudaMemcpy(*d_base, base.data(), 3 * n * sizeof(int), cudaMemcpyHostToDevice));
+        CK3(cudaMemcpy(*d_w, w.data(), 8 * n * sizeof(float), cudaMemcpyHostToDevice));
+        CK3(cudaMemcpy(*d_coef, coef.data(), 8 * n * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    return SA_OK;
+}
+
+int plan3d_set_geometry(Plan3D* p, int n_shots, const int* so, const float* sx, const int* ro, const float* rx) {
+    std::vector<int> so_(so, so + n_shots + 1), ro_(ro, ro + n_shots + 1);
+    std::vector<float> sx_(sx ? sx : nullptr, sx ? sx + 3 * (size_t)so[n_shots] : nullptr);
+    std::vector<float> rx_(rx ? rx : nullptr, rx ? rx + 3 * (size_t)ro[n_shots] : nullptr);
+    const double h = std::max(p->d.spacing[0], std::max(p->d.spacing[1], p->d.spacing[2]));
+    int rc = build_points(p, n_shots, so_.data(), sx_.data(), 2.0 * p->d.dt / h, 1, &p->s_shot, &p->s_base, &p->s_w,
+                          &p->s_coef);
+    if (rc == SA_OK)
+        rc = build_points(p, n_shots, ro_.data(), rx_.data(), -p->d.dt * p->d.dt, 2, &p->r_shot, &p->r_base, &p->r_w,
+                          &p->r_coef);
+    if (rc != SA_OK) return rc;
+    p->so = so_;
+    p->ro = ro_;
+    p->sx = sx_;
+    p->rx = rx_;
+    p->n_shots = n_shots;
+    p->n_src = so_[n_shots];
+    p->n_rec = ro_[n_shots];
+    if ((rc = alloc3(&p->src_amp, (size_t)p->d.nt * std::max(1, p->n_src))) != SA_OK) return rc;
+    if ((rc = alloc3(&p->rec_amp, (size_t)p->d.nt * std::max(1, p->n_rec))) != SA_OK) return rc;
+    const int R = p->kind == 0 ? 5 : 9;
+    const int ctas = p->ty0n * p->tz0n * n_shots;
+    p->nchunks = std::max(1, std::min((152 * 4 + ctas - 1) / ctas, p->nx / (4 * R)));
+    p->chunk_rows = (p->nx + p->nchunks - 1) / p->nchunks;
+    p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
+    p->geometry_set = true;
+    p->snaps_valid = false;
+    return SA_OK;
+}
+
+static int load_tm(Plan3D* p, const float* user, int rows, int cols, float* dst, cudaStream_t s) {
+    const size_t n = (size_t)rows * cols;
+    if (!n) return SA_OK;
+    const float* src = user;
+    if (!dev_ptr(user)) {
+        if (n > p->cap_tstage) {
+            int rc = alloc3(&p->tstage, n);
+            if (rc != SA_OK) return rc;
+            p->cap_tstage = n;
+        }
+        CK3(cudaMemcpyAsync(p->tstage, user, n * sizeof(float), cudaMemcpyHostToDevice, s));
+        src = p->tstage;
+    }
+    CK3(transpose(src, rows, cols, dst, s));
+    return SA_OK;
+}
+
+static Step3D args3(const Plan3D* p) {
+    Step3D a{};
+    a.nx = p->nx;
+    a.ny = p->ny;
+    a.nz = p->nz;
+    a.zp = p->zp;
+    a.shot_stride = p->field;
+    a.chunk_rows = p->chunk_rows;
+    a.ty0n = p->ty0n;
+    const long long G = GUARD;
+    a.W = p->W + G * p->plane;
+    a.bxh = p->bxh ? p->bxh + (G + 5) * p->plane : nullptr;
+    a.byh = p->byh ? p->byh + G * (p->ny + 12) * p->zp : nullptr;
+    a.bzh = p->bzh ? p->bzh + G * p->ny * p->zpb : nullptr;
+    a.zpb = p->zpb;
+    a.C1 = p->C1 + G * p->plane;
+    a.C2 = p->C2 + G * p->plane;
+    a.C3 = p->C3 + G * p->plane;
+    a.hx = (float)p->d.spacing[0];
+    a.hy = (float)p->d.spacing[1];
+    a.hz = (float)p->d.spacing[2];
+    a.dt = (float)p->d.dt;
+    a.f = p->d.undersampling;
+    a.snaps = p->snaps;
+    a.snap_stride = p->snap_stride;
+    a.snap_shot_stride = (long long)p->n_snap * p->snap_stride;
+    a.gradb = p->gradb;
+    a.precb = p->precb;
+    a.ix0 = p->d.absorbing[0];
+    a.ix1 = p->nx - p->d.absorbing[0];
+    a.iy0 = p->d.absorbing[1];
+    a.iy1 = p->ny - p->d.absorbing[1];
+    a.iz0 = p->d.absorbing[2];
+    a.iz1 = p->nz - p->d.absorbing[2];
+    return a;
+}
+
+// One time level: [pass A] + pass B, then injection into the new level (and its snapshot).
+static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, const Sparse3D& inj, int n_inj,
+                 const float* amp, bool save_now, cudaStream_t s, long long& n) {
+    const dim3 grid(p->ty0n * p->tz0n, p->nchunks, p->n_shots);
+    a.cur = cur;
+    a.prev = prev;
+    if (p->ot4) {
+        a.in = cur;
+        a.out_l = p->Lbuf;
+        CK3(launch_step3d(p->kind, false, true, grid, s, a));
+        a.in = p->Lbuf;
+        n++;
+    } else {
+        a.in = cur;
+    }
+    CK3(launch_step3d(p->kind, true, p->ot4, grid, s, a));
+    n++;
+    const float inv_dt2 = (float)(1.0 / ((double)a.dt * (double)a.dt));
+    CK3(sparse3d_inject(inj, n_inj, amp, n_inj, a.t, prev, p->field, p->ny, p->zp, save_now ? p->snaps : nullptr,
+                        (long long)p->n_snap * p->snap_stride, (long long)(a.t / a.f) * p->snap_stride,
+                        inv_dt2, s));
+    if (n_inj) n++;
+    return SA_OK;
+}
+
+int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mode, cudaStream_t s) {
+    if (!p->medium_set || !p->geometry_set) return fail3(SA_E_INVALID, "medium and geometry must be set first");
+    const bool save = save_mode == SA_SAVE_SNAPSHOTS;
+    if (save && !p->snaps) {
+        int rc = alloc3(&p->snaps, (size_t)p->n_shots * p->n_snap * p->snap_stride);
+        if (rc != SA_OK) return rc;
+    }
+    int rc = load_tm(p, wavelets, p->n_src, p->d.nt, p->src_amp, s);
+    if (rc != SA_OK) return rc;
+    const size_t fb = (size_t)p->n_shots * p->field * sizeof(float);
+    CK3(cudaMemsetAsync(p->F[0], 0, fb, s));
+    CK3(cudaMemsetAsync(p->F[1], 0, fb, s));
+    CK3(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * std::max(1, p->n_rec) * sizeof(float), s));
+    Step3D a = args3(p);
+    a.save = save ? 1 : 0;
+    a.grad = 0;
+    const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
+    const Sparse3D rec{p->r_shot, p->r_base, p->r_w, p->r_coef};
+    long long n = p->n_src ? 1 : 0;
+    for (int t = 1; t <= p->d.nt - 2; t++) {
+        a.t = t;
+        float* cur = (t & 1) ? p->F[1] : p->F[0];
+        float* prev = (t & 1) ? p->F[0] : p->F[1];
+        rc = step3(p, a, cur, prev, src, p->n_src, p->src_amp, save && t % a.f == 0, s, n);
+        if (rc != SA_OK) return rc;
+        if (p->n_rec) {  // rec[t] = interp(p[t+1])
+            CK3(sparse3d_gather(rec, p->n_rec, prev, p->field, p->ny, p->zp, p->rec_amp, p->n_rec, t, s));
+            n++;
+        }
+    }
+    if (p->n_rec) {
+        if (dev_ptr(traces)) {
+            CK3(transpose(p->rec_amp, p->d.nt, p->n_rec, traces, s));
+        } else {
+            const size_t m = (size_t)p->d.nt * p->n_rec;
+            if (m > p->cap_tstage) {
+                if ((rc = alloc3(&p->tstage, m)) != SA_OK) return rc;
+                p->cap_tstage = m;
+            }
+            CK3(transpose(p->rec_amp, p->d.nt, p->n_rec, p->tstage, s));
+            CK3(cudaMemcpyAsync(traces, p->tstage, m * sizeof(float), cudaMemcpyDeviceToHost, s));
+            CK3(cudaStreamSynchronize(s));
+        }
+        n++;
+    }
+    p->launches = n;
+    if (save) p->snaps_valid = true;
+    return SA_OK;
+}
+
+int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s) {
+    if (!p->snaps_valid) return fail3(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS");
+    int rc = SA_OK;
+    if (!p->gradb && (rc = alloc3(&p->gradb, (size_t)p->n_shots * p->field)) != SA_OK) return rc;
+    if (!p->precb && (rc = alloc3(&p->precb, (size_t)p->n_shots * p->field)) != SA_OK) return rc;
+    if ((rc = load_tm(p, residuals, p->n_rec, p->d.nt, p->rec_amp, s)) != SA_OK) return rc;
+    const size_t fb = (size_t)p->n_shots * p->field * sizeof(float);
+    CK3(cudaMemsetAsync(p->F[0], 0, fb, s));
+    CK3(cudaMemsetAsync(p->F[1], 0, fb, s));
+    CK3(cudaMemsetAsync(p->gradb, 0, fb, s));
+    CK3(cudaMemsetAsync(p->precb, 0, fb, s));
+    Step3D a = args3(p);
+    a.save = 0;
+    a.grad = 1;
+    const Sparse3D rec{p->r_shot, p->r_base, p->r_w, p->r_coef};
+    const int T0 = p->d.nt - 1 - p->d.undersampling;
+    long long n = p->n_rec ? 1 : 0;
+    for (int t = T0; t >= 1; t--) {
+        a.t = t;
+        const bool even = ((T0 - t) & 1) == 0;
+        float* cur = even ? p->F[1] : p->F[0];
+        float* prev = even ? p->F[0] : p->F[1];
+        rc = step3(p, a, cur, prev, rec, p->n_rec, p->rec_amp, false, s, n);
+        if (rc != SA_OK) return rc;
+    }
+    const size_t N = (size_t)p->nx * p->ny * p->nz;
+    for (int k = 0; k < 2; k++) {
+        float* user = k == 0 ? grad : prec;
+        const float* buf = k == 0 ? p->gradb : p->precb;
+        if (dev_ptr(user)) {
+            CK3(reduce3d(buf, p->field, p->n_shots, p->nx, p->ny, p->nz, p->zp, user, s));
+        } else {
+            if (N > p->cap_tstage) {
+                if ((rc = alloc3(&p->tstage, N)) != SA_OK) return rc;
+                p->cap_tstage = N;
+            }
+            CK3(reduce3d(buf, p->field, p->n_shots, p->nx, p->ny, p->nz, p->zp, p->tstage, s));
+            CK3(cudaMemcpyAsync(user, p->tstage, N * sizeof(float), cudaMemcpyDeviceToHost, s));
+            CK3(cudaStreamSynchronize(s));
+        }
+        n++;
+    }
+    p->launches = n;
+    return SA_OK;
+}
+
+}  // namespace sa

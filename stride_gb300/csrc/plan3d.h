@@ -1,0 +1,16 @@
+// 3D plans (plan3d.cu), used by the C ABI entry points when sa_desc.dim == 3.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/strideacc.h"
+
+namespace sa {
+struct Plan3D;
+int plan3d_create(const sa_desc& d, Plan3D** out);
+void plan3d_destroy(Plan3D* p);
+int plan3d_set_medium(Plan3D* p, const float* vp, const float* rho, const float* alpha);
+int plan3d_set_geometry(Plan3D* p, int n_shots, const int* so, const float* sx, const int* ro, const float* rx);
+int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mode, cudaStream_t s);
+int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s);
+long long plan3d_launches(const Plan3D* p);
+}  // namespace sa

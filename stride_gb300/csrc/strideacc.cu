@@ -17,6 +17,7 @@
 #include "common.cuh"
 #include "helpers.h"
 #include "launch.h"
+#include "plan3d.h"
 
 namespace {
 
@@ -81,6 +82,7 @@ void set_last_error(const char* msg) { g_err = msg; }
 
 struct sa_plan {
     sa_desc d{};
+    sa::Plan3D* p3 = nullptr;  // dim == 3: the 3D plan (plan3d.cu) serves every entry point
     int nx = 0, ny = 0, pitch = 0, pitch_b = 0;
     long long shot_stride = 0;  // nx * pitch: float2 elements per shot pair (wavefields are pair-interleaved)
     int kind = 0;
@@ -468,13 +470,16 @@ int sa_last_error(char* buf, int len) {
     return SA_OK;
 }
 
-long long sa_launch_count(const sa_plan* p) { return p ? p->launches : -1; }
+long long sa_launch_count(const sa_plan* p) {
+    if (!p) return -1;
+    return p->p3 ? sa::plan3d_launches(p->p3) : p->launches;
+}
 
 int sa_plan_create(const sa_desc* desc, sa_plan** out) {
     if (!desc || !out) return fail(SA_E_INVALID, "null argument");
     *out = nullptr;
     const sa_desc& d = *desc;
-    if (d.dim != 2) return fail(SA_E_UNSUPPORTED, "dim %d: this build implements the 2D operator", d.dim);
+    if (d.dim != 2 && d.dim != 3) return fail(SA_E_UNSUPPORTED, "dim %d: the operator is 2D or 3D", d.dim);
     if (d.kernel != SA_KERNEL_OT2 && d.kernel != SA_KERNEL_OT4)
         return fail(SA_E_INVALID, "Unrecognized kernel %d", d.kernel);
     if (d.density < 0 || d.density > 2) return fail(SA_E_INVALID, "density mode %d", d.density);
@@ -489,6 +494,19 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
     if (!(d.dt > 0)) return fail(SA_E_INVALID, "dt");
     int dev = 0;
     CK(cudaGetDevice(&dev));
+    if (d.dim == 3) {
+        if (d.shape[2] < 24 || !(d.spacing[2] > 0) || d.absorbing[2] < 0 || d.absorbing[2] > d.extra[2] ||
+            d.absorbing[2] > sa::MAX_ABS || d.absorbing[2] == 1 || 2 * d.absorbing[2] > d.shape[2])
+            return fail(SA_E_INVALID, "third axis of the description");
+        sa::Plan3D* p3 = nullptr;
+        const int rc = sa::plan3d_create(d, &p3);
+        if (rc != SA_OK) return rc;
+        sa_plan* p = new sa_plan();
+        p->d = d;
+        p->p3 = p3;
+        *out = p;
+        return SA_OK;
+    }
     sa_plan* p = new sa_plan();
     p->d = d;
     p->nx = d.shape[0];
@@ -547,6 +565,11 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
 
 int sa_plan_destroy(sa_plan* p) {
     if (!p) return SA_OK;
+    if (p->p3) {
+        sa::plan3d_destroy(p->p3);
+        delete p;
+        return SA_OK;
+    }
     drop_graphs(p);
     void* bufs[] = {p->field[0], p->field[1], p->W, p->vp, p->alpha, p->buoy, p->bxh, p->byh, p->C1, p->C2, p->C3,
                     p->medium_stage,
@@ -563,6 +586,7 @@ int sa_set_medium(sa_plan* p, const float* vp, const float* rho, const float* al
     if (!p || !vp) return fail(SA_E_INVALID, "null plan or vp");
     if (p->d.density != SA_DENSITY_NONE && !rho) return fail(SA_E_INVALID, "rho required by the plan's density mode");
     if (p->d.attenuation && !alpha) return fail(SA_E_INVALID, "alpha required by the plan");
+    if (p->p3) return sa::plan3d_set_medium(p->p3, vp, rho, alpha);
     const size_t N = (size_t)p->nx * p->ny;
     const float* in[3] = {vp, p->d.density == SA_DENSITY_VARIABLE ? rho : nullptr, p->d.attenuation ? alpha : nullptr};
     const float* dev[3] = {nullptr, nullptr, nullptr};
@@ -602,6 +626,7 @@ int sa_set_geometry(sa_plan* p, int n_shots, const int* src_offsets, const float
     if (src_offsets[0] != 0 || rec_offsets[0] != 0) return fail(SA_E_INVALID, "offsets must start at 0");
     const int ns = src_offsets[n_shots], nr = rec_offsets[n_shots];
     if ((ns && !src_xyz) || (nr && !rec_xyz)) return fail(SA_E_INVALID, "missing coordinates");
+    if (p->p3) return sa::plan3d_set_geometry(p->p3, n_shots, src_offsets, src_xyz, rec_offsets, rec_xyz);
     const int dim = p->d.dim;
     auto convert = [&](const float* xyz, int n, std::vector<int>& bx, std::vector<int>& by, std::vector<double>& fx,
                        std::vector<double>& fy) -> int {
@@ -645,6 +670,10 @@ int sa_set_geometry(sa_plan* p, int n_shots, const int* src_offsets, const float
 
 int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, void* stream) {
     if (!p) return fail(SA_E_INVALID, "null plan");
+    if (p->p3) {
+        if (save_mode != SA_SAVE_NONE && save_mode != SA_SAVE_SNAPSHOTS) return fail(SA_E_INVALID, "save_mode");
+        return sa::plan3d_forward(p->p3, wavelets, traces, save_mode, (cudaStream_t)stream);
+    }
     if (!p->medium_set || !p->geometry_set) return fail(SA_E_INVALID, "medium and geometry must be set first");
     if ((p->n_src && !wavelets) || (p->n_rec && !traces)) return fail(SA_E_INVALID, "null wavelets or traces");
     if (save_mode != SA_SAVE_NONE && save_mode != SA_SAVE_SNAPSHOTS) return fail(SA_E_INVALID, "save_mode");
@@ -668,6 +697,10 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
 int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_vp, int grad_mode, void* stream) {
     if (!p) return fail(SA_E_INVALID, "null plan");
     if (grad_mode != SA_GRAD_PARITY) return fail(SA_E_UNSUPPORTED, "grad_mode %d", grad_mode);
+    if (p->p3) {
+        if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
+        return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream);
+    }
     if (!p->snaps_valid) return fail(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS");
     if ((p->n_rec && !residuals) || !grad_vp || !prec_vp) return fail(SA_E_INVALID, "null residuals or outputs");
     cudaStream_t s = (cudaStream_t)stream;
@@ -696,6 +729,7 @@ int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_v
 }
 
 int sa_autotune(sa_plan* p, void* stream) {
+    if (p && p->p3) return SA_OK;  // 3D plans use a fixed tile (8 x 32 columns per CTA)
     if (!p || !p->geometry_set || !p->medium_set) return fail(SA_E_INVALID, "autotune needs medium and geometry");
     cudaStream_t s = (cudaStream_t)stream;
     const int S = p->ot4 ? 2 : 1;

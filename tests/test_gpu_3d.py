@@ -1,0 +1,93 @@
+"""3D parity of the CUDA path (through the C ABI) with the C oracle on identical seeded inputs:
+traces relative L2 <= 1e-4, parity-mode vp gradient cosine >= 0.999 and relative L2 <= 1e-3."""
+
+import numpy as np
+import pytest
+
+from oracle import c_oracle
+from oracle import numpy_oracle as npo
+from stride_gb300 import _lib, phantoms
+from tests import _cases as C
+
+pytestmark = pytest.mark.gpu
+
+
+def case3d(kernel='OT4', density='variable', alpha=True, inner=24, nt=160, seed=2, n_shots=1):
+    rng = np.random.default_rng(seed)
+    e = 8
+    h = 0.5e-3
+    shape_i = (inner, inner + 2, inner + 5)
+    vpi, rhoi, ali = phantoms.ellipse_phantom(shape_i, (h, h, h), 3, rng, rho_range=(950., 1100.),
+                                              alpha_range=(0., 1.), disk_radius=3e-3, axes=(1.5e-3, 4e-3))
+    ext = (e, e, e)
+    vp = phantoms.extend(vpi, ext)
+    rho = None
+    if density == 'variable':
+        rho = phantoms.extend(rhoi, ext)
+    elif density == 'constant':
+        rho = np.full(vp.shape, 1000., np.float32)
+    al = phantoms.extend(ali, ext) if alpha else None
+    dt = (0.6 if kernel == 'OT4' else 0.35) * h / 1650.
+    c = np.array([(s - 1) * h / 2 for s in shape_i])
+    pts = c + 0.35 * (inner - 1) * h * np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [-1, 0, 0], [0, -1, 0.3],
+                                                  [0.5, 0.5, -0.6], [-0.6, 0.4, 0.2]])
+    wav = npo.tone_burst(1.0e6, 3, nt, dt)
+    srcs = [pts[[s % len(pts)]] for s in range(n_shots)]
+    recs = [pts for _ in range(n_shots)]
+    return dict(vp=vp, rho=rho, alpha=al, spacing=(h, h, h), dt=dt, nt=nt, extra=ext, absorbing=ext, kernel=kernel,
+                srcs=srcs, recs=recs, wav=wav)
+
+
+def make_plan3(c):
+    plan = _lib.Plan(3, c['vp'].shape, c['spacing'], c['extra'], c['absorbing'], c['dt'], c['nt'], kernel=c['kernel'],
+                     density=C.density_mode(c['rho']), attenuation=c['alpha'] is not None, undersampling=4,
+                     max_shots=len(c['srcs']))
+    plan.set_medium(np.ascontiguousarray(c['vp']), None if c['rho'] is None else np.ascontiguousarray(c['rho']),
+                    None if c['alpha'] is None else np.ascontiguousarray(c['alpha']))
+    eps = 1e-3 * np.asarray(c['spacing'])
+    so = np.cumsum([0] + [len(s) for s in c['srcs']])
+    ro = np.cumsum([0] + [len(r) for r in c['recs']])
+    sx = np.concatenate([np.asarray(s, np.float32) + eps for s in c['srcs']]).astype(np.float32)
+    rx = np.concatenate([np.asarray(r, np.float32) + eps for r in c['recs']]).astype(np.float32)
+    plan.set_geometry(so, sx, ro, rx)
+    return plan
+
+
+def oracle3(c, shot, save=False):
+    origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
+    return c_oracle.forward(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][shot], c['recs'][shot],
+                            np.tile(c['wav'][None], (len(c['srcs'][shot]), 1)), origin, rho=c['rho'],
+                            alpha=c['alpha'], kernel=c['kernel'], save=save, undersampling=4)
+
+
+@pytest.mark.parametrize('kernel', ['OT2', 'OT4'])
+@pytest.mark.parametrize('density,alpha', [('none', False), ('variable', True), ('constant', True)])
+def test_forward_3d(kernel, density, alpha):
+    c = case3d(kernel=kernel, density=density, alpha=alpha)
+    got, _ = C.gpu_forward(c, plan=make_plan3(c))
+    ref, _ = oracle3(c, 0)
+    assert np.abs(ref).max() > 0
+    assert C.rel_l2(got[0], ref) <= 1e-4
+
+
+def test_gradient_3d_two_shots():
+    c = case3d(kernel='OT4', density='variable', alpha=True, n_shots=2)
+    plan = make_plan3(c)
+    got, plan = C.gpu_forward(c, plan=plan, save=True)
+    res = [g * np.float32(0.8) for g in got]
+    resw = np.ascontiguousarray((np.concatenate(res).astype(np.float64) * C.window(c['nt'])[None, :]).astype(np.float32))
+    grad = np.zeros(c['vp'].shape, np.float32)
+    prec = np.zeros(c['vp'].shape, np.float32)
+    plan.adjoint(resw, grad, prec)
+    origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
+    g_ref = np.zeros(c['vp'].shape)
+    p_ref = np.zeros(c['vp'].shape)
+    for s in range(2):
+        _, snaps = oracle3(c, s, save=True)
+        g, p = c_oracle.adjoint(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['recs'][s], res[s], origin,
+                                snaps, rho=c['rho'], alpha=c['alpha'], kernel='OT4', undersampling=4)
+        g_ref += g
+        p_ref += p
+    assert C.cosine(grad, g_ref) >= 0.999
+    assert C.rel_l2(grad, g_ref) <= 1e-3
+    assert C.rel_l2(prec, p_ref) <= 1e-4
