@@ -42,9 +42,35 @@ HBM_FALLBACK_GBS = 6800.0
 NCU_TRAFFIC_PER_LAUNCH = 180.294656e6 + 102.961664e6
 
 
-def workload_config(nt=None, n_shots=64, rank=0):
+WORKLOADS = {
+    # name: (generator, shots per GPU, mode)
+    'fwdadj64': ('batched', 64, 'fwdadj'),  # default: the fwd+adj vp gradient of the headline metric
+    'fwd256': ('batched', 256, 'fwd'),      # batched forward, one shot per transducer
+    'single': ('single', 1, 'fwd'),         # single-shot forward, 256^2 at 0.5 mm, vp only
+    '3d': ('3d', 8, 'fwd'),                 # 3D forward, 296^3, 8 shots per launch
+    '3dgrad': ('3d', 1, 'fwdadj'),          # 3D fwd+adj vp gradient of one shot (snapshots in HBM)
+}
+WORKLOAD_NAMES = {
+    'fwdadj64': '2D fwd+adj vp gradient: 552^2 extended (512^2 at 0.25 mm + 20 sponge), vp/rho/alpha phantom, '
+                '64 shots x 256 receivers, 4000 steps, OT4, f=4',
+    'fwd256': '2D batched forward: 552^2 extended, vp/rho/alpha phantom, 256 shots x 256 receivers, 4000 steps, OT4',
+    'single': '2D single-shot forward: 296^2 extended (256^2 at 0.5 mm + 20 sponge), vp phantom, 128 receivers, '
+              '2000 steps, OT4',
+    '3d': '3D forward: 296^3 extended (256^3 at 0.5 mm + 20 sponge), vp/rho/alpha phantom, 8 shots x 512 receivers, '
+          '3000 steps, OT4',
+    '3dgrad': '3D fwd+adj vp gradient: 296^3 extended, vp/rho/alpha phantom, 1 shot x 512 receivers, 3000 steps, '
+              'OT4, f=4',
+}
+
+
+def workload_config(name='fwdadj64', nt=None, n_shots=None, rank=0):
     from stride_gb300 import phantoms
-    w = phantoms.workload('batched', seed=0, nt=nt)
+    gen, default_shots, _ = WORKLOADS[name]
+    n_shots = default_shots if n_shots is None else n_shots
+    if gen == '3d':
+        w = phantoms.workload3d(seed=0, nt=nt, n_shots=n_shots)
+    else:
+        w = phantoms.workload(gen, seed=0, nt=nt)
     ntr = len(w['geometry'])
     stride = max(1, ntr // n_shots)
     first = rank % stride
@@ -136,74 +162,95 @@ def measured_hbm():
         return HBM_FALLBACK_GBS, 'fallback'
 
 
-def cpu_arm(w, target_s=15.0, threads=None, calib=True):
-    """Times the oracle's C restatement of the reference operator (forward with save +
-    adjoint, one shot) on the host cores; returns GPts/s and the sample description."""
+def cpu_arm(w, target_s=15.0, threads=None, calib=True, mode='fwdadj'):
+    """Times the oracle's C restatement of the reference operator (one shot: forward, plus
+    the adjoint for mode 'fwdadj') on the host cores; returns GPts/s and the sample description."""
     from oracle import c_oracle
     threads = threads or os.cpu_count()
     origin = tuple(-e * h for e, h in zip(w['extra'], w['spacing']))
     N = int(np.prod(w['shape']))
+    grad = mode == 'fwdadj'
 
     def run(nt):
         wav = w['wavelet'][:nt][None]
         t0 = time.perf_counter()
         tr, snaps = c_oracle.forward(w['vp'], w['spacing'], w['dt'], nt, w['absorbing'], w['src'][0], w['rec'][0],
-                                     wav, origin, rho=w['rho'], alpha=w['alpha'], kernel='OT4', save=True,
+                                     wav, origin, rho=w['rho'], alpha=w['alpha'], kernel='OT4', save=grad,
                                      nthreads=threads)
-        c_oracle.adjoint(w['vp'], w['spacing'], w['dt'], nt, w['absorbing'], w['rec'][0], tr, origin, snaps,
-                         rho=w['rho'], alpha=w['alpha'], kernel='OT4', nthreads=threads)
+        pts = N * (nt - 2)
+        if grad:
+            c_oracle.adjoint(w['vp'], w['spacing'], w['dt'], nt, w['absorbing'], w['rec'][0], tr, origin, snaps,
+                             rho=w['rho'], alpha=w['alpha'], kernel='OT4', nthreads=threads)
+            pts += N * (nt - 1 - 4)
         dt = time.perf_counter() - t0
-        return N * ((nt - 2) + (nt - 1 - 4)) / dt / 1e9, dt
+        return pts / dt / 1e9, dt
 
-    nt = 64
+    nt = 24
     rate, dt = run(nt)
     if calib:
-        nt = int(min(w['nt'], max(64, nt * target_s / max(dt, 1e-3))))
+        nt = int(min(w['nt'], max(24, nt * target_s / max(dt, 1e-3))))
         rate, dt = run(nt)
-    sample = '1 shot of the workload, forward (save) + adjoint, %d of %d steps, %.1f s' % (nt, w['nt'], dt)
+    sample = '1 shot of the workload, %s, %d of %d steps, %.1f s' % (
+        'forward (save) + adjoint' if grad else 'forward', nt, w['nt'], dt)
     return rate, threads, sample, dt
+
+
+def _density(w):
+    from stride_gb300 import _lib
+    if w['rho'] is None:
+        return _lib.SA_DENSITY_NONE
+    r = w['rho']
+    return _lib.SA_DENSITY_CONSTANT if np.isclose(np.min(r), np.max(r)) else _lib.SA_DENSITY_VARIABLE
+
+
+def _points(w, workload):
+    mode = WORKLOADS[workload][2]
+    N = int(np.prod(w['shape']))
+    nt = w['nt']
+    pts = N * len(w['shots']) * (nt - 2)
+    if mode == 'fwdadj':
+        pts += N * len(w['shots']) * (nt - 1 - 4)
+    return pts
+
+
+METRIC = {'fwdadj': 'GPts/s (forward+adjoint vp gradient)', 'fwd': 'GPts/s (forward)'}
 
 
 def reference_arm(args):
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
         return 0
-    w = workload_config(nt=args.nt, n_shots=args.shots)
+    w = workload_config(args.workload, nt=args.nt, n_shots=args.shots)
+    mode = WORKLOADS[args.workload][2]
     threads = os.cpu_count()
-    rates = []
+    rates, samples = [], []
     for _ in range(args.warmup):
-        cpu_arm(w, target_s=2.0, threads=threads, calib=False)
-    samples = []
+        cpu_arm(w, target_s=1.0, threads=threads, calib=False, mode=mode)
     for _ in range(args.steps):
-        r, _, sample, dt = cpu_arm(w, target_s=args.cpu_seconds / max(1, args.steps), threads=threads)
+        r, _, sample, dt = cpu_arm(w, target_s=args.cpu_seconds / max(1, args.steps), threads=threads, mode=mode)
         rates.append(r)
-        samples.append(dt)
+        samples.append(sample)
     value = statistics.median(rates)
-    N = int(np.prod(w['shape']))
-    pts_step = N * len(w['shots']) * ((w['nt'] - 2) + (w['nt'] - 1 - 4))
     line = {
-        'impl': 'reference', 'metric': 'GPts/s (forward+adjoint vp gradient)', 'value': value, 'unit': 'GPts/s',
+        'impl': 'reference', 'metric': METRIC[mode], 'value': value, 'unit': 'GPts/s',
         'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': pts_step / (value * 1e9) * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+        'ms_per_step': _points(w, args.workload) / (value * 1e9) * 1e3, 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded phantoms)',
-        'config': {'workload': WORKLOAD_NAME, 'grid': list(w['shape']), 'shots': len(w['shots']), 'nt': w['nt'],
-                   'kernel': 'OT4', 'l2_flush': 'inputs larger than L2'},
+        'config': {'workload': WORKLOAD_NAMES[args.workload], 'grid': list(w['shape']), 'shots': len(w['shots']),
+                   'nt': w['nt'], 'kernel': 'OT4', 'l2_flush': 'inputs larger than L2'},
         'cpu_baseline': {'value': value, 'unit': 'GPts/s', 'cores': threads, 'kind': 'port',
-                         'sample': sample + ' per step (the reference Devito operator cannot be installed here; '
-                                            'this is the oracle C/OpenMP restatement of it)'},
+                         'sample': samples[-1] + ' per step (the reference Devito operator cannot be installed here; '
+                                                 'this is the oracle C/OpenMP restatement of it)'},
         'e2e': {'value': value, 'unit': 'GPts/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
     }
     print(json.dumps(line))
     return 0
 
 
-WORKLOAD_NAME = ('2D fwd+adj vp gradient: 552^2 extended (512^2 at 0.25 mm + 20 sponge), vp/rho/alpha '
-                 'phantom, 64 shots x 256 receivers, 4000 steps, OT4, f=4')
-
-
 def gb300_arm(args):
     import torch
     import torch.distributed as dist
+    import scipy.signal
     from stride_gb300 import _lib
 
     world = int(os.environ.get('WORLD_SIZE', '1'))
@@ -214,31 +261,33 @@ def gb300_arm(args):
     torch.cuda.set_device(local)
     dev = torch.device('cuda', local)
     stream = torch.cuda.current_stream()
+    mode = WORKLOADS[args.workload][2]
+    grad_mode = mode == 'fwdadj'
 
-    w = workload_config(nt=args.nt, n_shots=args.shots, rank=rank)
+    w = workload_config(args.workload, nt=args.nt, n_shots=args.shots, rank=rank)
     nt = w['nt']
+    dim = len(w['shape'])
     n_shots = len(w['shots'])
     N = int(np.prod(w['shape']))
     eps = 1e-3 * np.asarray(w['spacing'])
-    so = np.cumsum([0] + [len(s) for s in w['src']])
-    ro = np.cumsum([0] + [len(r) for r in w['rec']])
-    sx = np.concatenate(w['src']).astype(np.float32) + eps.astype(np.float32)
-    rx = np.concatenate(w['rec']).astype(np.float32) + eps.astype(np.float32)
-    import scipy.signal
+    so = np.cumsum([0] + [len(x) for x in w['src']])
+    ro = np.cumsum([0] + [len(x) for x in w['rec']])
+    sx = (np.concatenate(w['src']) + eps).astype(np.float32)
+    rx = (np.concatenate(w['rec']) + eps).astype(np.float32)
     win = scipy.signal.get_window(('tukey', 0.001), nt, False).astype(np.float32)
 
-    plan = _lib.Plan(2, w['shape'], w['spacing'], w['extra'], w['absorbing'], w['dt'], nt, kernel='OT4',
-                     density=_lib.SA_DENSITY_VARIABLE, attenuation=True, undersampling=4, max_shots=n_shots)
+    plan = _lib.Plan(dim, w['shape'], w['spacing'], w['extra'], w['absorbing'], w['dt'], nt, kernel='OT4',
+                     density=_density(w), attenuation=w['alpha'] is not None, undersampling=4, max_shots=n_shots)
     plan.set_geometry(so, sx, ro, rx)
     wav = torch.from_numpy(np.tile((w['wavelet'] * win)[None].astype(np.float32), (plan.n_src, 1))).to(dev)
     win_d = torch.from_numpy(win).to(dev)
-    # observed data from the true phantom
-    plan.set_medium(w['vp'], w['rho'], w['alpha'])
     observed = torch.zeros((plan.n_rec, nt), device=dev)
-    plan.forward(wav, observed, stream=stream)
-    # starting model: 1500 m/s water speed, known rho/alpha
-    vp0 = np.full(w['shape'], 1500., np.float32)
-    plan.set_medium(vp0, w['rho'], w['alpha'])
+    if grad_mode:  # observed data from the true phantom; the gradient is taken at 1500 m/s
+        plan.set_medium(w['vp'], w['rho'], w['alpha'])
+        plan.forward(wav, observed, stream=stream)
+        plan.set_medium(np.full(w['shape'], 1500., np.float32), w['rho'], w['alpha'])
+    else:
+        plan.set_medium(w['vp'], w['rho'], w['alpha'])
     plan.autotune(stream=stream)
     traces = torch.zeros((plan.n_rec, nt), device=dev)
     grad = torch.zeros(w['shape'], device=dev)
@@ -246,19 +295,20 @@ def gb300_arm(args):
 
     ev = lambda: torch.cuda.Event(enable_timing=True)
     fwd_ms, adj_ms = [], []
-    launches = {'n': 0, 'steps': 0}
+    launches = {'n': 0}
 
     def step(timed=False):
         e0, e1, e2 = ev(), ev(), ev()
         e0.record(stream)
-        plan.forward(wav, traces, save=True, stream=stream)
+        plan.forward(wav, traces, save=grad_mode, stream=stream)
         launches['n'] += plan.launches
         e1.record(stream)
-        res = (traces - observed) * win_d[None, :]  # L2 residual, adjoint-source window
-        plan.adjoint(res, grad, prec, stream=stream)
-        launches['n'] += plan.launches
+        if grad_mode:
+            res = (traces - observed) * win_d[None, :]  # L2 residual, adjoint-source window
+            plan.adjoint(res, grad, prec, stream=stream)
+            launches['n'] += plan.launches
         e2.record(stream)
-        if world > 1:
+        if world > 1 and grad_mode:
             dist.all_reduce(grad)
             dist.all_reduce(prec)
         if timed:
@@ -287,22 +337,24 @@ def gb300_arm(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     ms_step = ms / args.steps
-    pts_fwd = N * n_shots * (nt - 2)
-    pts_adj = N * n_shots * (nt - 1 - 4)
-    pts_step = pts_fwd + pts_adj
+    pts_step = _points(w, args.workload)
     value = pts_step * world / (ms_step * 1e-3) / 1e9
-    assert torch.isfinite(grad).all(), 'gradient is not finite'
-    if nt >= 1000:  # by then the waves have reached the receivers
-        assert float(grad.abs().max()) > 0, 'gradient is empty'
+    assert torch.isfinite(traces).all(), 'traces are not finite'
+    if grad_mode:
+        assert torch.isfinite(grad).all(), 'gradient is not finite'
+        if nt >= 1000:  # by then the waves have reached the receivers
+            assert float(grad.abs().max()) > 0, 'gradient is empty'
 
-    # roofline of the step kernel: algorithmic bytes per launch / average launch time
+    # roofline of the step kernel(s): algorithmic bytes of a time step / average step time
     t_fwd = sum(a.elapsed_time(b) for a, b in fwd_ms) / len(fwd_ms)
     t_adj = sum(a.elapsed_time(b) for a, b in adj_ms) / len(adj_ms)
     b_fwd, b_adj = alg_bytes_per_point(w)
-    n_launch = (nt - 2) + (nt - 1 - 4)
-    alg_bytes = N * n_shots * ((nt - 2) * b_fwd + (nt - 1 - 4) * b_adj)
-    per_launch_s = (t_fwd + t_adj) * 1e-3 / n_launch
-    achieved = alg_bytes / n_launch / per_launch_s / 1e9
+    if not grad_mode:
+        b_fwd -= 4.0 / 4  # no snapshot write
+    steps_f, steps_a = nt - 2, (nt - 1 - 4) if grad_mode else 0
+    alg_bytes = N * n_shots * (steps_f * b_fwd + steps_a * b_adj)
+    per_step_s = (t_fwd + t_adj) * 1e-3 / (steps_f + steps_a)
+    achieved = alg_bytes / (steps_f + steps_a) / per_step_s / 1e9
     peak, peak_kind = measured_hbm()
 
     # end to end through the C ABI with host buffers (pinned), residual formed on the host
@@ -317,9 +369,10 @@ def gb300_arm(args):
         tr_n, res_n, win_n = tr_h.numpy(), res_h.numpy(), win[None, :]
 
         def e2e_step():
-            plan.forward(wav_h, tr_h, save=True, stream=stream)
-            np.multiply(np.subtract(tr_n, obs_h, out=res_n), win_n, out=res_n)
-            plan.adjoint(res_h, g_h, p_h, stream=stream)
+            plan.forward(wav_h, tr_h, save=grad_mode, stream=stream)
+            if grad_mode:
+                np.multiply(np.subtract(tr_n, obs_h, out=res_n), win_n, out=res_n)
+                plan.adjoint(res_h, g_h, p_h, stream=stream)
 
         e2e_step()
         torch.cuda.synchronize()
@@ -334,31 +387,35 @@ def gb300_arm(args):
             t = torch.tensor([es], device=dev)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             es = float(t.item())
-        e2e = {'value': pts_step * world / es / 1e9, 'unit': 'GPts/s',
-               'h2d_bytes_per_step': int(wav_h.numel() * 4 + res_h.numel() * 4),
-               'd2h_bytes_per_step': int(tr_h.numel() * 4 + 2 * g_h.numel() * 4)}
+        h2d = wav_h.numel() * 4 + (res_h.numel() * 4 if grad_mode else 0)
+        d2h = tr_h.numel() * 4 + (2 * g_h.numel() * 4 if grad_mode else 0)
+        e2e = {'value': pts_step * world / es / 1e9, 'unit': 'GPts/s', 'h2d_bytes_per_step': int(h2d),
+               'd2h_bytes_per_step': int(d2h)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, cores, sample, _ = cpu_arm(w, target_s=args.cpu_seconds)
+        rate, cores, sample, _ = cpu_arm(w, target_s=args.cpu_seconds, mode=mode)
         cpu = {'value': rate, 'unit': 'GPts/s', 'cores': cores, 'kind': 'port', 'sample': sample}
 
     if rank == 0:
+        snap_gb = N * n_shots * (nt // 4) * 4 / 1e9 if grad_mode else 0.0
         line = {
-            'metric': 'GPts/s (forward+adjoint vp gradient)', 'value': value, 'unit': 'GPts/s', 'n_gpus': world,
+            'metric': METRIC[mode], 'value': value, 'unit': 'GPts/s', 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_step, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded phantoms)',
-            'config': {'workload': WORKLOAD_NAME, 'grid': list(w['shape']), 'shots_per_gpu': n_shots, 'nt': nt,
-                       'kernel': 'OT4', 'parallelism': 'shots sharded over %d GPU(s), gradient all-reduce' % world,
-                       'l2_flush': 'inputs larger than L2 (%.0f GB of wavefields per step)'
-                                   % (2 * N * n_shots * 4 / 1e9 + N * n_shots * (nt // 4) * 4 / 1e9)},
+            'config': {'workload': WORKLOAD_NAMES[args.workload], 'grid': list(w['shape']),
+                       'shots_per_gpu': n_shots, 'nt': nt, 'kernel': 'OT4',
+                       'parallelism': 'shots sharded over %d GPU(s)%s' % (world, ', gradient all-reduce' if grad_mode else ''),
+                       'l2_flush': 'inputs larger than L2 (%.1f GB of wavefields per step)'
+                                   % (2 * N * n_shots * 4 / 1e9 + snap_gb)},
             'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                          'frac': achieved / peak, 'peak_source': peak_kind,
-                         'traffic': NCU_TRAFFIC_PER_LAUNCH,
-                         'alg_bytes_per_point': {'forward': b_fwd, 'adjoint': b_adj},
-                         'kernel': 'fdtd2d_step', 'launch_ms': per_launch_s * 1e3},
+                         'traffic': NCU_TRAFFIC_PER_LAUNCH if args.workload == 'fwdadj64' else None,
+                         'alg_bytes_per_point': {'forward': b_fwd, 'adjoint': b_adj if grad_mode else None},
+                         'kernel': 'fdtd2d_step' if dim == 2 else 'fdtd3d_pass',
+                         'step_ms': per_step_s * 1e3},
             'cpu_baseline': cpu, 'e2e': e2e, 'gpu_launches': launches['n'], 'clocks': clk.summary(),
-            'forward_ms': t_fwd, 'adjoint_ms': t_adj,
+            'forward_ms': t_fwd, 'adjoint_ms': t_adj if grad_mode else None,
         }
         print(json.dumps(line))
     plan.close()
@@ -374,7 +431,8 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--nt', type=int, default=None, help='time steps (default: the workload\'s 4000)')
-    ap.add_argument('--shots', type=int, default=64)
+    ap.add_argument('--workload', default='fwdadj64', choices=sorted(WORKLOADS))
+    ap.add_argument('--shots', type=int, default=None, help='shots per GPU (default: the workload\'s)')
     ap.add_argument('--cpu-seconds', type=float, default=15.0)
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')

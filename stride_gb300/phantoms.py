@@ -134,3 +134,34 @@ def workload(name, seed=0, nt=None, n_shots=None, inner=None):
         vp_inner=vpi, geometry=geo.astype(np.float32), shots=shots,
         src=[geo[[s]] for s in shots], rec=[geo for _ in shots], wavelet=wav,
     )
+
+
+def workload3d(seed=0, nt=None, n_shots=8, inner=None):
+    """Synthetic 3D workload: 256^3 inner grid at 0.5 mm + 20 absorbing cells per side
+    (296^3 extended), seeded vp/rho/alpha ellipsoid phantom in water, 512 transducers on a
+    55 mm hemisphere, 500 kHz 3-cycle burst, 3000 steps at CFL 0.6; ``n_shots`` shots fire
+    from evenly spaced transducers."""
+    rng = np.random.default_rng(seed)
+    extra = 20
+    n = 256 if inner is None else inner
+    h = 0.5e-3
+    shape = (n, n, n)
+    spacing = (h, h, h)
+    vpi, rhoi, ali = ellipse_phantom(shape, spacing, 6, rng, rho_range=(950., 1100.), alpha_range=(0., 1.),
+                                     disk_radius=min(40e-3, 0.3 * (n - 1) * h), axes=(min(5e-3, 0.05 * n * h),
+                                                                                      min(20e-3, 0.15 * n * h)))
+    centre = tuple((n - 1) * h / 2 for _ in range(3))
+    radius = min(55e-3, 0.42 * (n - 1) * h)
+    geo = hemisphere_geometry(512, radius, centre)
+    dt = 0.6 * h / 1650.
+    nt = 3000 if nt is None else nt
+    n_tone = int((3 / 0.5e6) // dt + 1)
+    wav = _wavelets.tone_burst(0.5e6, 3, max(nt, n_tone), dt)[:nt]
+    shots = list(range(0, len(geo), max(1, len(geo) // n_shots)))[:n_shots]
+    ext = (extra,) * 3
+    return dict(
+        name='3d', shape=tuple(s + 2 * extra for s in shape), inner_shape=shape, spacing=spacing, extra=ext,
+        absorbing=ext, dt=dt, nt=nt, f0=0.5e6, vp=extend(vpi, ext), rho=extend(rhoi, ext), alpha=extend(ali, ext),
+        vp_inner=vpi, geometry=geo.astype(np.float32), shots=shots, src=[geo[[s]] for s in shots],
+        rec=[geo for _ in shots], wavelet=wav,
+    )
