@@ -22,7 +22,9 @@ struct Step3D {
     int nx, ny, nz, zp;       // extended grid and z pitch
     long long shot_stride;    // floats per shot in a field buffer (nx*ny*zp)
     int chunk_rows;           // output x rows per CTA
-    int ty0n;                 // tiles along y (blockIdx.x = tile_y + ty0n * tile_z)
+    int ty0n;                 // tiles along y
+    int nshots;               // blockIdx.x = shot + nshots * (tile_y + ty0n * tile_z): the shots of a
+                              // tile run together and share the tile's medium through L2
     int t;
     const float* in;          // streamed field: u (OT2 / INTERMEDIATE) or l (OT4 FINAL)
     const float* cur;         // p[t] (FINAL: the current level at the output)
@@ -103,8 +105,9 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
 
     const int tid = threadIdx.x;
     const int tz = tid % TZ, ty = tid / TZ;
-    const int tile_y = blockIdx.x % a.ty0n, tile_z = blockIdx.x / a.ty0n;
-    const int chunk = blockIdx.y, shot = blockIdx.z;
+    const int shot = blockIdx.x % a.nshots, tile = blockIdx.x / a.nshots;
+    const int tile_y = tile % a.ty0n, tile_z = tile / a.ty0n;
+    const int chunk = blockIdx.y;
     const int y0 = tile_y * TY, z0 = tile_z * TZ;
     const int y = y0 + ty, z = z0 + tz;
     const bool col_in = y < a.ny && z < a.nz;
@@ -158,12 +161,42 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
 #pragma unroll 1
     for (int i = i0; i < i1; i += RB) {
         const int j = i - R;  // output row of this iteration's first input row
-        float Wj[RB], bxi[RB];
+        constexpr int KY = ((TY + 9) * TZ + NT - 1) / NT, KZ = (TY * (TZ + 9) + NT - 1) / NT;
+        float Wj[RB], bxi[RB], byv[RB][VARB ? KY : 1], bzv[RB][VARB ? KZ : 1];
+        float c1v[RB], c2v[RB], c3v[RB], uov[RB], pmv[RB];
 #pragma unroll
         for (int r = 0; r < RB; r++) {
             Wj[r] = __ldg(a.W + (long long)(j + r) * plane + col);
-            if constexpr (VARB) bxi[r] = __ldg(a.bxh + (long long)(i - 5 + r) * plane + col);
+            if constexpr (VARB) {
+                bxi[r] = __ldg(a.bxh + (long long)(i - 5 + r) * plane + col);
+                const int xx = min(max(j + r, -sa::GUARD), a.nx + sa::GUARD - 1);
+#pragma unroll
+                for (int q = 0; q < KY; q++) {
+                    const int k = tid + q * NT;
+                    const int ky = min(k / TZ, TY + 8), kz = k % TZ;
+                    const int zz = min(z0 + kz, a.nz - 1), yy = min(max(y0 - 5 + ky + 6, 0), a.ny + 9);
+                    byv[r][q] = __ldg(a.byh + (long long)xx * (a.ny + 12) * a.zp + (long long)yy * a.zp + zz);
+                }
+#pragma unroll
+                for (int q = 0; q < KZ; q++) {
+                    const int k = tid + q * NT;
+                    const int ky = min(k / (TZ + 9), TY - 1), kz = k % (TZ + 9);
+                    const int yy = min(y0 + ky, a.ny - 1), zz = min(max(z0 - 5 + kz + 6, 0), a.zpb - 1);
+                    bzv[r][q] = __ldg(a.bzh + (long long)xx * a.ny * a.zpb + (long long)yy * a.zpb + zz);
+                }
+            }
+            if constexpr (FINAL) {
+                const int row = j + r;
+                const bool ok = row >= xo0 && row < xo1 && col_in;
+                const long long idx = (long long)row * plane + (long long)y * a.zp + z;
+                c1v[r] = ok ? __ldg(a.C1 + idx) : 0.f;
+                c2v[r] = ok ? __ldg(a.C2 + idx) : 0.f;
+                c3v[r] = ok ? __ldg(a.C3 + idx) : 0.f;
+                uov[r] = ok ? a.cur[soff + idx] : 0.f;
+                pmv[r] = ok ? a.prev[soff + idx] : 0.f;
+            }
         }
+        (void)byv; (void)bzv; (void)c1v; (void)c2v; (void)c3v; (void)uov; (void)pmv;
         cp_async_wait<PF - 1>();
         __syncthreads();
         prefetch(i + PF * RB);
@@ -172,29 +205,29 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
 #pragma unroll
             for (int r = 0; r < RB; r++) {
                 const float* pl = slot(j + r);
-                for (int k = tid; k < (TY + 9) * TZ; k += NT) {
-                    const int ky = k / TZ, kz = k % TZ;
-                    const int hy = y0 - 5 + ky;  // half row hy + 1/2
-                    const int base = (hy - y0 + R) * PZ + (z0 + kz - Z0);
-                    float v = dstag_1(pl, base + PZ, base, PZ) * ihy;
-                    if constexpr (VARB) {
-                        const int zz = min(z0 + kz, a.nz - 1), yy = min(max(hy + 6, 0), a.ny + 9);
-                        const int xx = min(max(j + r, -sa::GUARD), a.nx + sa::GUARD - 1);
-                        v *= __ldg(a.byh + (long long)xx * (a.ny + 12) * a.zp + (long long)yy * a.zp + zz);
+#pragma unroll
+                for (int q = 0; q < KY; q++) {
+                    const int k = tid + q * NT;
+                    if (k < (TY + 9) * TZ) {
+                        const int ky = k / TZ, kz = k % TZ;
+                        const int hy = y0 - 5 + ky;  // half row hy + 1/2
+                        const int base = (hy - y0 + R) * PZ + (z0 + kz - Z0);
+                        float v = dstag_1(pl, base + PZ, base, PZ) * ihy;
+                        if constexpr (VARB) v *= byv[r][q];
+                        sFY[r * ((TY + 9) * TZ) + k] = v;
                     }
-                    sFY[r * ((TY + 9) * TZ) + k] = v;
                 }
-                for (int k = tid; k < TY * (TZ + 9); k += NT) {
-                    const int ky = k / (TZ + 9), kz = k % (TZ + 9);
-                    const int hz = z0 - 5 + kz;  // half column hz + 1/2
-                    const int base = (ky + R) * PZ + (hz - Z0);
-                    float v = dstag_1(pl, base + 1, base, 1) * ihz;
-                    if constexpr (VARB) {
-                        const int yy = min(y0 + ky, a.ny - 1), zz = min(max(hz + 6, 0), a.zpb - 1);
-                        const int xx = min(max(j + r, -sa::GUARD), a.nx + sa::GUARD - 1);
-                        v *= __ldg(a.bzh + (long long)xx * a.ny * a.zpb + (long long)yy * a.zpb + zz);
+#pragma unroll
+                for (int q = 0; q < KZ; q++) {
+                    const int k = tid + q * NT;
+                    if (k < TY * (TZ + 9)) {
+                        const int ky = k / (TZ + 9), kz = k % (TZ + 9);
+                        const int hz = z0 - 5 + kz;  // half column hz + 1/2
+                        const int base = (ky + R) * PZ + (hz - Z0);
+                        float v = dstag_1(pl, base + 1, base, 1) * ihz;
+                        if constexpr (VARB) v *= bzv[r][q];
+                        sFZ[r * (TY * (TZ + 9)) + k] = v;
                     }
-                    sFZ[r * (TY * (TZ + 9)) + k] = v;
                 }
             }
             __syncthreads();
@@ -242,9 +275,9 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
             if constexpr (!FINAL) {
                 a.out_l[soff + idx] = res[r];
             } else {
-                const float u_o = a.cur[soff + idx];
-                const float pm = a.prev[soff + idx];
-                const float pn = a.C1[idx] * res[r] + a.C2[idx] * u_o - a.C3[idx] * pm;
+                const float u_o = uov[r];
+                const float pm = pmv[r];
+                const float pn = c1v[r] * res[r] + c2v[r] * u_o - c3v[r] * pm;
                 if (do_save) {
                     a.snaps[(long long)shot * a.snap_shot_stride + (long long)(a.t / a.f) * a.snap_stride + idx] =
                         (pn - 2.f * u_o + pm) / dt2;

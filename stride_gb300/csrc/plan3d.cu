@@ -292,6 +292,7 @@ static Step3D args3(const Plan3D* p) {
     a.shot_stride = p->field;
     a.chunk_rows = p->chunk_rows;
     a.ty0n = p->ty0n;
+    a.nshots = p->n_shots;
     const long long G = GUARD;
     a.W = p->W + G * p->plane;
     a.bxh = p->bxh ? p->bxh + (G + 5) * p->plane : nullptr;
@@ -323,7 +324,7 @@ static Step3D args3(const Plan3D* p) {
 // One time level: [pass A] + pass B, then injection into the new level (and its snapshot).
 static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, const Sparse3D& inj, int n_inj,
                  const float* amp, bool save_now, cudaStream_t s, long long& n) {
-    const dim3 grid(p->ty0n * p->tz0n, p->nchunks, p->n_shots);
+    const dim3 grid(p->ty0n * p->tz0n * p->n_shots, p->nchunks, 1);
     a.cur = cur;
     a.prev = prev;
     if (p->ot4) {

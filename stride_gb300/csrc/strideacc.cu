@@ -737,9 +737,13 @@ int sa_autotune(sa_plan* p, void* stream) {
         int nt, nchunks;
     };
     std::vector<Cand> cands;
+    // row chunks: short chunks (more CTAs, more pipeline warm-up rows) only pay off when the
+    // batch alone cannot fill the GPU
+    const int ctas1 = npairs(p) * ((p->ny + bymax(p, 128) - 1) / bymax(p, 128));
     for (int nt : kThreads)
-        for (int nc : {1, 2, 3, 4, 6, 8, 12, 16}) {
-            if (p->nx / nc < 4 * S * radius(p)) continue;
+        for (int nc : {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48}) {
+            const int min_rows = ctas1 >= 456 ? 4 * S * radius(p) : 8;
+            if (p->nx / nc < min_rows) continue;
             cands.push_back({nt, nc});
         }
     const int steps = std::min(24, p->d.nt - 2);
