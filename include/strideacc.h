@@ -36,6 +36,8 @@ extern "C" {
 
 #define SA_SAVE_NONE 0        /* forward only */
 #define SA_SAVE_SNAPSHOTS 1   /* store p.dt2 every f steps (reference algorithm) */
+#define SA_SAVE_CHECKPOINTS 2 /* store the state every checkpoint interval; the adjoint recomputes each
+                                 segment's p.dt2 from its checkpoint (same gradient, less memory) */
 
 #define SA_GRAD_PARITY 0      /* reference imaging condition: sum_{t%f==0} p_tt * p_a, interior only */
 
@@ -54,6 +56,8 @@ typedef struct sa_desc {
     int attenuation;       /* 0 none, 1 alpha given with attenuation power 0 */
     int undersampling;     /* f of the saved wavefield, >= 1 */
     int max_shots;         /* shots advanced together per launch */
+    int checkpoint_interval;   /* steps between checkpoints for SA_SAVE_CHECKPOINTS (0: 50) */
+    double checkpoint_budget;  /* bytes the checkpoints may use (0: no limit); widens the interval */
 } sa_desc;
 
 typedef struct sa_plan sa_plan;
@@ -83,7 +87,9 @@ int sa_set_geometry(sa_plan* plan, int n_shots, const int* src_offsets, const fl
  * diff_source the caller passes dt * d/dt of the wavelet). traces [n_rec_total, nt] float32
  * receive rec.data.T (rows 0 and nt-1 of each trace are zero as in the reference's
  * time_m=1, time_M=nt-2 loop). save_mode SA_SAVE_SNAPSHOTS keeps p.dt2 every f steps for
- * sa_adjoint. Host or device pointers; stream is a cudaStream_t (NULL = legacy default).
+ * sa_adjoint; SA_SAVE_CHECKPOINTS keeps the two state levels every checkpoint interval instead and
+ * sa_adjoint recomputes each segment (the reference's layered/compressed wavefield storage,
+ * devito.py:325-403, is the memory-saving counterpart). Host or device pointers; stream is a cudaStream_t (NULL = legacy default).
  * Replaces run_forward/after_forward (iso_acoustic/devito.py:515-685). */
 int sa_forward(sa_plan* plan, const float* wavelets, float* traces, int save_mode, void* stream);
 
@@ -92,7 +98,7 @@ int sa_forward(sa_plan* plan, const float* wavelets, float* traces, int save_mod
  * grad_vp/prec_vp [N] float32 on the extended grid receive the raw imaging condition summed
  * over the shots (Devito grad_vp/prec_vp data, zero outside the interior) before the
  * get_grad_vp chain rule. grad_mode SA_GRAD_PARITY. Requires a prior sa_forward with
- * SA_SAVE_SNAPSHOTS. Replaces run_adjoint/after_adjoint (devito.py:875-981). */
+ * SA_SAVE_SNAPSHOTS or SA_SAVE_CHECKPOINTS (then each segment is recomputed from its checkpoint). Replaces run_adjoint/after_adjoint (devito.py:875-981). */
 int sa_adjoint(sa_plan* plan, const float* residuals, float* grad_vp, float* prec_vp, int grad_mode,
                void* stream);
 

@@ -26,6 +26,7 @@ SA_DENSITY_VARIABLE = 1
 SA_DENSITY_CONSTANT = 2
 SA_SAVE_NONE = 0
 SA_SAVE_SNAPSHOTS = 1
+SA_SAVE_CHECKPOINTS = 2
 SA_GRAD_PARITY = 0
 
 # every symbol include/strideacc.h declares
@@ -37,7 +38,8 @@ class SaDesc(ctypes.Structure):
     _fields_ = [('dim', ctypes.c_int), ('shape', ctypes.c_int * 3), ('spacing', ctypes.c_double * 3),
                 ('extra', ctypes.c_int * 3), ('absorbing', ctypes.c_int * 3), ('dt', ctypes.c_double),
                 ('nt', ctypes.c_int), ('kernel', ctypes.c_int), ('density', ctypes.c_int),
-                ('attenuation', ctypes.c_int), ('undersampling', ctypes.c_int), ('max_shots', ctypes.c_int)]
+                ('attenuation', ctypes.c_int), ('undersampling', ctypes.c_int), ('max_shots', ctypes.c_int),
+                ('checkpoint_interval', ctypes.c_int), ('checkpoint_budget', ctypes.c_double)]
 
 
 class StrideAccError(RuntimeError):
@@ -114,7 +116,7 @@ class Plan:
     """Owner of one sa_plan (one batch of shots on one grid)."""
 
     def __init__(self, dim, shape, spacing, extra, absorbing, dt, nt, kernel='OT4', density=SA_DENSITY_NONE,
-                 attenuation=False, undersampling=4, max_shots=1):
+                 attenuation=False, undersampling=4, max_shots=1, checkpoint_interval=0, checkpoint_budget=0.0):
         lib = load()
         d = SaDesc()
         d.dim = dim
@@ -130,6 +132,8 @@ class Plan:
         d.attenuation = int(bool(attenuation))
         d.undersampling = int(undersampling)
         d.max_shots = int(max_shots)
+        d.checkpoint_interval = int(checkpoint_interval)
+        d.checkpoint_budget = float(checkpoint_budget)
         self.desc = d
         h = ctypes.c_void_p()
         check(lib.sa_plan_create(ctypes.byref(d), ctypes.byref(h)))
@@ -163,8 +167,10 @@ class Plan:
         self.n_rec = int(ro[-1])
 
     def forward(self, wavelets, traces, save=False, stream=None):
-        check(load().sa_forward(self._h, _ptr(wavelets), _ptr(traces),
-                                SA_SAVE_SNAPSHOTS if save else SA_SAVE_NONE, _stream(stream)))
+        """save: False, True / 'snapshots' (p.dt2 every f steps) or 'checkpoints'."""
+        mode = {False: SA_SAVE_NONE, None: SA_SAVE_NONE, True: SA_SAVE_SNAPSHOTS, 'snapshots': SA_SAVE_SNAPSHOTS,
+                'checkpoints': SA_SAVE_CHECKPOINTS}[save]
+        check(load().sa_forward(self._h, _ptr(wavelets), _ptr(traces), mode, _stream(stream)))
 
     def adjoint(self, residuals, grad, prec, stream=None):
         check(load().sa_adjoint(self._h, _ptr(residuals), _ptr(grad), _ptr(prec), SA_GRAD_PARITY,

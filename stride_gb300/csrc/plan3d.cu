@@ -4,6 +4,7 @@
 // reverse-time adjoint with the vp imaging condition (devito.py:875-920, 985-1043).
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <vector>
 
@@ -68,6 +69,34 @@ void ramp(int A, double h, double refl, float* out) {
 
 }  // namespace
 
+// The requested interval (50 by default), unless the checkpoints and one segment's snapshots
+// exceed the byte budget; then the multiple of f nearest to it that fits.
+int choose_checkpoints(const sa_desc& d, double level, int* K_out, int* n_out) {
+    const int f = d.undersampling;
+    const int T0 = d.nt - 1 - f;
+    int K = d.checkpoint_interval > 0 ? d.checkpoint_interval : 50;
+    K = (K + f - 1) / f * f;
+    auto bytes = [&](int k) { return (T0 >= 1 ? (T0 - 1) / k : 0) * 2 * level + (k / f) * level; };
+    if (d.checkpoint_budget > 0 && bytes(K) > d.checkpoint_budget) {
+        int best = -1;
+        double least = 1e300;
+        for (int k = f; k <= std::max(f, T0); k += f) {
+            least = std::min(least, bytes(k));
+            if (bytes(k) <= d.checkpoint_budget && (best < 0 || std::abs(k - K) < std::abs(best - K))) best = k;
+        }
+        if (best < 0) {
+            char b[256];
+            snprintf(b, sizeof(b), "no checkpoint interval fits %.0f bytes (at least %.0f needed)",
+                     d.checkpoint_budget, least);
+            return fail3(SA_E_NOMEM, b);
+        }
+        K = best;
+    }
+    *K_out = K;
+    *n_out = T0 >= 1 ? (T0 - 1) / K : 0;
+    return SA_OK;
+}
+
 struct Plan3D {
     sa_desc d{};
     int nx = 0, ny = 0, nz = 0, zp = 0, zpb = 0, kind = 0;
@@ -87,9 +116,16 @@ struct Plan3D {
     float *src_amp = nullptr, *rec_amp = nullptr, *tstage = nullptr;
     size_t cap_tstage = 0;
     float* snaps = nullptr;
+    size_t cap_snaps = 0;
     int n_snap = 0;
     long long snap_stride = 0;
     bool snaps_valid = false, medium_set = false, geometry_set = false;
+    // checkpoints (SA_SAVE_CHECKPOINTS): both levels after every ck_K-th step, one segment's
+    // recomputed snapshots, the adjoint's own two levels
+    float *ckpt = nullptr, *segsnaps = nullptr, *A[2] = {nullptr, nullptr};
+    size_t cap_ckpt = 0, cap_segsnaps = 0;
+    int ck_K = 0, ck_n = 0;
+    bool ckpt_valid = false;
     float *gradb = nullptr, *precb = nullptr;
     long long launches = 0;
     int chunk_rows = 0, nchunks = 1, ty0n = 1, tz0n = 1;
@@ -153,7 +189,7 @@ void plan3d_destroy(Plan3D* p) {
     if (!p) return;
     float* fb[] = {p->F[0], p->F[1], p->Lbuf, p->W, p->C1, p->C2, p->C3, p->bxh, p->byh, p->bzh, p->vp, p->alpha,
                    p->buoy, p->stage, p->s_w, p->s_coef, p->r_w, p->r_coef, p->src_amp, p->rec_amp, p->tstage,
-                   p->snaps, p->gradb, p->precb};
+                   p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps, p->A[0], p->A[1]};
     for (float* b : fb)
         if (b) cudaFree(b);
     int* ib[] = {p->s_shot, p->s_base, p->r_shot, p->r_base};
@@ -190,6 +226,7 @@ int plan3d_set_medium(Plan3D* p, const float* vp, const float* rho, const float*
     CK3(cudaMemcpy(p->vp_host.data(), dv[0], N * sizeof(float), cudaMemcpyDeviceToHost));
     p->medium_set = true;
     p->snaps_valid = false;
+    p->ckpt_valid = false;
     if (p->geometry_set) return plan3d_set_geometry(p, p->n_shots, p->so.data(), p->sx.data(), p->ro.data(), p->rx.data());
     return SA_OK;
 }
@@ -263,6 +300,7 @@ int plan3d_set_geometry(Plan3D* p, int n_shots, const int* so, const float* sx, 
     p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
     p->geometry_set = true;
     p->snaps_valid = false;
+    p->ckpt_valid = false;
     return SA_OK;
 }
 
@@ -339,9 +377,8 @@ static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, const Spar
     CK3(launch_step3d(p->kind, true, p->ot4, grid, s, a));
     n++;
     const float inv_dt2 = (float)(1.0 / ((double)a.dt * (double)a.dt));
-    CK3(sparse3d_inject(inj, n_inj, amp, n_inj, a.t, prev, p->field, p->ny, p->zp, save_now ? p->snaps : nullptr,
-                        (long long)p->n_snap * p->snap_stride, (long long)(a.t / a.f) * p->snap_stride,
-                        inv_dt2, s));
+    CK3(sparse3d_inject(inj, n_inj, amp, n_inj, a.t, prev, p->field, p->ny, p->zp, save_now ? a.snaps : nullptr,
+                        a.snap_shot_stride, (long long)(a.t / a.f) * a.snap_stride, inv_dt2, s));
     if (n_inj) n++;
     return SA_OK;
 }
@@ -349,9 +386,23 @@ static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, const Spar
 int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mode, cudaStream_t s) {
     if (!p->medium_set || !p->geometry_set) return fail3(SA_E_INVALID, "medium and geometry must be set first");
     const bool save = save_mode == SA_SAVE_SNAPSHOTS;
-    if (save && !p->snaps) {
-        int rc = alloc3(&p->snaps, (size_t)p->n_shots * p->n_snap * p->snap_stride);
+    const bool ckpt = save_mode == SA_SAVE_CHECKPOINTS;
+    p->ckpt_valid = false;  // the wavelets the checkpointed adjoint re-injects are replaced
+    if (save && (size_t)p->n_shots * p->n_snap * p->snap_stride > p->cap_snaps) {
+        p->cap_snaps = (size_t)p->n_shots * p->n_snap * p->snap_stride;
+        int rc = alloc3(&p->snaps, p->cap_snaps);
         if (rc != SA_OK) return rc;
+    }
+    const size_t level = (size_t)p->n_shots * p->field;  // floats of one level of every shot
+    if (ckpt) {
+        int rc = choose_checkpoints(p->d, (double)level * sizeof(float), &p->ck_K, &p->ck_n);
+        if (rc != SA_OK) return rc;
+        const size_t need = std::max<size_t>(1, (size_t)p->ck_n * 2 * level);
+        if (need > p->cap_ckpt) {
+            if ((rc = alloc3(&p->ckpt, need)) != SA_OK) return rc;
+            p->cap_ckpt = need;
+        }
+        p->snaps_valid = false;
     }
     int rc = load_tm(p, wavelets, p->n_src, p->d.nt, p->src_amp, s);
     if (rc != SA_OK) return rc;
@@ -375,6 +426,11 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
             CK3(sparse3d_gather(rec, p->n_rec, prev, p->field, p->ny, p->zp, p->rec_amp, p->n_rec, t, s));
             n++;
         }
+        if (ckpt && t % p->ck_K == 0 && t / p->ck_K <= p->ck_n) {  // (p[t+1], p[t]) into slot t/K - 1
+            float* slot = p->ckpt + (size_t)(t / p->ck_K - 1) * 2 * level;
+            CK3(cudaMemcpyAsync(slot, p->F[0], level * sizeof(float), cudaMemcpyDeviceToDevice, s));
+            CK3(cudaMemcpyAsync(slot + level, p->F[1], level * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        }
     }
     if (p->n_rec) {
         if (dev_ptr(traces)) {
@@ -393,12 +449,73 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
     }
     p->launches = n;
     if (save) p->snaps_valid = true;
+    if (ckpt) p->ckpt_valid = true;
+    return SA_OK;
+}
+
+// Reverse-time adjoint from checkpoints: segment k covers t = kK+1 .. min((k+1)K, T0); from
+// last to first its start state is restored (zero for k = 0), its forward steps are re-run
+// with p.dt2 saved into a K/f-slot segment buffer, and the adjoint steps run back through it
+// on their own two levels. The recomputed snapshots are bitwise the stored ones.
+static int adjoint_segments(Plan3D* p, Step3D& aa, const Sparse3D& rec, cudaStream_t s, long long& n) {
+    const size_t level = (size_t)p->n_shots * p->field;
+    const size_t lb = level * sizeof(float);
+    const int f = p->d.undersampling, K = p->ck_K;
+    const int T0 = p->d.nt - 1 - f;
+    CK3(cudaMemsetAsync(p->A[0], 0, lb, s));
+    CK3(cudaMemsetAsync(p->A[1], 0, lb, s));
+    Step3D fa = args3(p);
+    fa.save = 1;
+    fa.grad = 0;
+    fa.snap_shot_stride = aa.snap_shot_stride = (long long)(K / f) * p->snap_stride;
+    const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
+    for (int k = T0 >= 1 ? (T0 - 1) / K : -1; k >= 0; k--) {
+        const int t_lo = k * K + 1, t_hi = std::min((k + 1) * K, T0);
+        if (k == 0) {
+            CK3(cudaMemsetAsync(p->F[0], 0, lb, s));
+            CK3(cudaMemsetAsync(p->F[1], 0, lb, s));
+        } else {
+            const float* slot = p->ckpt + (size_t)(k - 1) * 2 * level;
+            CK3(cudaMemcpyAsync(p->F[0], slot, lb, cudaMemcpyDeviceToDevice, s));
+            CK3(cudaMemcpyAsync(p->F[1], slot + level, lb, cudaMemcpyDeviceToDevice, s));
+        }
+        // the kernels address snapshot t/f; slot t/f - (kK/f + 1) of the segment buffer is meant
+        const long long first = (long long)k * K / f + 1;
+        float* base = reinterpret_cast<float*>(reinterpret_cast<uintptr_t>(p->segsnaps) -
+                                               (uintptr_t)(first * p->snap_stride * (long long)sizeof(float)));
+        fa.snaps = aa.snaps = base;
+        for (int t = t_lo; t <= t_hi; t++) {
+            fa.t = t;
+            int rc = step3(p, fa, (t & 1) ? p->F[1] : p->F[0], (t & 1) ? p->F[0] : p->F[1], src, p->n_src,
+                           p->src_amp, t % f == 0, s, n);
+            if (rc != SA_OK) return rc;
+        }
+        for (int t = t_hi; t >= t_lo; t--) {
+            aa.t = t;
+            const bool even = ((T0 - t) & 1) == 0;
+            int rc = step3(p, aa, even ? p->A[1] : p->A[0], even ? p->A[0] : p->A[1], rec, p->n_rec, p->rec_amp,
+                           false, s, n);
+            if (rc != SA_OK) return rc;
+        }
+    }
     return SA_OK;
 }
 
 int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s) {
-    if (!p->snaps_valid) return fail3(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS");
+    const bool ck = p->ckpt_valid;
+    if (!p->snaps_valid && !ck)
+        return fail3(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS or SA_SAVE_CHECKPOINTS");
     int rc = SA_OK;
+    if (ck) {
+        const size_t level = (size_t)std::max(1, p->d.max_shots) * p->field;
+        for (int k = 0; k < 2; k++)
+            if (!p->A[k] && (rc = alloc3(&p->A[k], level)) != SA_OK) return rc;
+        const size_t need = (size_t)(p->ck_K / p->d.undersampling) * p->n_shots * p->field;
+        if (need > p->cap_segsnaps) {
+            if ((rc = alloc3(&p->segsnaps, need)) != SA_OK) return rc;
+            p->cap_segsnaps = need;
+        }
+    }
     if (!p->gradb && (rc = alloc3(&p->gradb, (size_t)p->n_shots * p->field)) != SA_OK) return rc;
     if (!p->precb && (rc = alloc3(&p->precb, (size_t)p->n_shots * p->field)) != SA_OK) return rc;
     if ((rc = load_tm(p, residuals, p->n_rec, p->d.nt, p->rec_amp, s)) != SA_OK) return rc;
@@ -413,7 +530,8 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
     const Sparse3D rec{p->r_shot, p->r_base, p->r_w, p->r_coef};
     const int T0 = p->d.nt - 1 - p->d.undersampling;
     long long n = p->n_rec ? 1 : 0;
-    for (int t = T0; t >= 1; t--) {
+    if (ck && (rc = adjoint_segments(p, a, rec, s, n)) != SA_OK) return rc;
+    for (int t = ck ? 0 : T0; t >= 1; t--) {
         a.t = t;
         const bool even = ((T0 - t) & 1) == 0;
         float* cur = even ? p->F[1] : p->F[0];

@@ -13,4 +13,7 @@ int plan3d_set_geometry(Plan3D* p, int n_shots, const int* so, const float* sx, 
 int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mode, cudaStream_t s);
 int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s);
 long long plan3d_launches(const Plan3D* p);
+// Checkpoint interval K (a multiple of f) and the number of stored checkpoints for a plan whose
+// two state levels take `level_bytes` (SA_SAVE_CHECKPOINTS, both dimensions).
+int choose_checkpoints(const sa_desc& d, double level_bytes, int* K, int* n_ckpt);
 }  // namespace sa

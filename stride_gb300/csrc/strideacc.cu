@@ -7,6 +7,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -122,15 +123,22 @@ struct sa_plan {
     bool snaps_valid = false;
     float *gradb = nullptr, *precb = nullptr;
     size_t cap_gradb = 0, cap_precb = 0;
+    // checkpoints (SA_SAVE_CHECKPOINTS): both levels after every ck_K-th forward step, the
+    // recomputed snapshots of one segment, and the adjoint's own two levels
+    float *ckpt = nullptr, *segsnaps = nullptr, *afield[2] = {nullptr, nullptr};
+    size_t cap_ckpt = 0, cap_segsnaps = 0, afield_cap[2] = {0, 0};
+    int ck_K = 0, ck_n = 0;
+    bool ckpt_valid = false;
     // layout
     int NT = 128, by = 110, chunk_rows = 1, nstrips = 1, nchunks = 1;
     bool layout_fixed = false;
     sa::Sponge sponge{};
     // graphs
     cudaStream_t cap = nullptr;
-    cudaGraphExec_t g_fwd[2] = {nullptr, nullptr};
-    cudaGraphExec_t g_adj = nullptr;
-    long long loop_launches[3] = {0, 0, 0};  // kernels in the forward (no save, save) and adjoint loops
+    cudaGraphExec_t g_fwd[3] = {nullptr, nullptr, nullptr};  // by save mode
+    cudaGraphExec_t g_adj[2] = {nullptr, nullptr};           // from snapshots, from checkpoints
+    long long fwd_launches[3] = {0, 0, 0};                   // kernels in each forward loop (by save mode)
+    long long adj_launches[2] = {0, 0};                      // kernels in each adjoint loop
     bool use_graphs = true;
     long long launches = 0;                   // kernels launched by the last sa_forward / sa_adjoint
 };
@@ -156,10 +164,11 @@ void drop_graphs(sa_plan* p) {
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
-    if (p->g_adj) {
-        cudaGraphExecDestroy(p->g_adj);
-        p->g_adj = nullptr;
-    }
+    for (auto& g : p->g_adj)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
 }
 
 // Sponge ramp of Boundary.damping for one axis (stride/physics/boundaries/boundary.py:98-151),
@@ -330,7 +339,10 @@ sa::Step2D base_args(const sa_plan* p) {
 }
 
 // Issues the forward time loop t = 1..nt-2 (iso_acoustic/devito.py:575-581) on stream s.
-int issue_forward(sa_plan* p, bool save, cudaStream_t s) {
+// SA_SAVE_SNAPSHOTS saves p.dt2 every f steps; SA_SAVE_CHECKPOINTS copies both levels
+// (p[t+1], p[t]) after every step t = kK, k = 1..ck_n, into checkpoint slot k-1.
+int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
+    const bool save = mode == SA_SAVE_SNAPSHOTS;
     const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
     CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
     CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
@@ -354,6 +366,11 @@ int issue_forward(sa_plan* p, bool save, cudaStream_t s) {
         a.gat = (t >= 2 && p->n_rec) ? p->gat : nullptr;
         CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
         n++;
+        if (mode == SA_SAVE_CHECKPOINTS && t % p->ck_K == 0 && t / p->ck_K <= p->ck_n) {
+            float* slot = p->ckpt + (size_t)(t / p->ck_K - 1) * 2 * (fbytes / sizeof(float));
+            CK(cudaMemcpyAsync(slot, p->field[0], fbytes, cudaMemcpyDeviceToDevice, s));
+            CK(cudaMemcpyAsync(slot + fbytes / sizeof(float), p->field[1], fbytes, cudaMemcpyDeviceToDevice, s));
+        }
     }
     // rec[nt-2] = interp(p[nt-1])
     const int tl = p->d.nt - 1;
@@ -363,7 +380,7 @@ int issue_forward(sa_plan* p, bool save, cudaStream_t s) {
                               s));
         n++;
     }
-    p->loop_launches[save ? 1 : 0] = n;
+    p->fwd_launches[mode] = n;
     return SA_OK;
 }
 
@@ -394,8 +411,84 @@ int issue_adjoint(sa_plan* p, cudaStream_t s) {
         CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
         n++;
     }
-    p->loop_launches[2] = n;
+    p->adj_launches[0] = n;
     return SA_OK;
+}
+
+// Reverse-time adjoint from checkpoints: the same steps and gradient as issue_adjoint, with
+// the snapshots recomputed per segment. Segment k covers t = kK+1 .. min((k+1)K, T0); from
+// last to first, its start state (checkpoint k, zero for k = 0) is restored, the forward
+// steps of the segment are re-run with p.dt2 saved into a segment buffer of K/f slots, and
+// the adjoint steps run back through the segment on their own two levels. The recomputed
+// steps are the forward's own launches (no receiver gather), so the snapshots are bitwise
+// the ones SA_SAVE_SNAPSHOTS stores.
+int issue_adjoint_ckpt(sa_plan* p, cudaStream_t s) {
+    const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
+    const size_t ffloats = fbytes / sizeof(float);
+    const size_t gbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float);
+    CK(cudaMemsetAsync(p->afield[0], 0, fbytes, s));
+    CK(cudaMemsetAsync(p->afield[1], 0, fbytes, s));
+    CK(cudaMemsetAsync(p->gradb, 0, gbytes, s));
+    CK(cudaMemsetAsync(p->precb, 0, gbytes, s));
+    const int f = p->d.undersampling, K = p->ck_K;
+    const int T0 = p->d.nt - 1 - f;
+    sa::Step2D fa = base_args(p);
+    fa.inj = p->n_src ? p->inj_src : nullptr;
+    fa.inj_off = p->inj_src_off;
+    fa.inj_amp = p->src_amp;
+    fa.inj_ld = p->n_src;
+    fa.gat = nullptr;
+    fa.save = 1;
+    fa.grad = 0;
+    fa.snap_shot_stride = (long long)(K / f) * p->shot_stride;
+    sa::Step2D aa = base_args(p);
+    aa.inj = p->n_rec ? p->inj_rec : nullptr;
+    aa.inj_off = p->inj_rec_off;
+    aa.inj_amp = p->rec_amp;
+    aa.inj_ld = p->n_rec;
+    aa.gat = nullptr;
+    aa.save = 0;
+    aa.grad = 1;
+    aa.snap_shot_stride = fa.snap_shot_stride;
+    const dim3 grid(p->nstrips, p->nchunks, npairs(p));
+    long long n = 0;
+    for (int k = T0 >= 1 ? (T0 - 1) / K : -1; k >= 0; k--) {
+        const int t_lo = k * K + 1, t_hi = std::min((k + 1) * K, T0);
+        if (k == 0) {
+            CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
+            CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
+        } else {
+            const float* slot = p->ckpt + (size_t)(k - 1) * 2 * ffloats;
+            CK(cudaMemcpyAsync(p->field[0], slot, fbytes, cudaMemcpyDeviceToDevice, s));
+            CK(cudaMemcpyAsync(p->field[1], slot + ffloats, fbytes, cudaMemcpyDeviceToDevice, s));
+        }
+        // the kernels address snapshot t/f; slot t/f - (kK/f + 1) of the segment buffer is meant
+        const long long first = (long long)k * K / f + 1;
+        float* base = reinterpret_cast<float*>(reinterpret_cast<uintptr_t>(p->segsnaps) -
+                                               (uintptr_t)(first * p->shot_stride * (long long)sizeof(float2)));
+        fa.snaps = aa.snaps = base;
+        for (int t = t_lo; t <= t_hi; t++) {
+            fa.t = t;
+            fa.cur = (t & 1) ? p->field[1] : p->field[0];
+            fa.prev = (t & 1) ? p->field[0] : p->field[1];
+            CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, fa));
+            n++;
+        }
+        for (int t = t_hi; t >= t_lo; t--) {
+            aa.t = t;
+            const bool even = ((T0 - t) & 1) == 0;
+            aa.cur = even ? p->afield[1] : p->afield[0];
+            aa.prev = even ? p->afield[0] : p->afield[1];
+            CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, aa));
+            n++;
+        }
+    }
+    p->adj_launches[1] = n;
+    return SA_OK;
+}
+
+int plan_checkpoints(sa_plan* p) {
+    return sa::choose_checkpoints(p->d, (double)npairs(p) * p->shot_stride * sizeof(float2), &p->ck_K, &p->ck_n);
 }
 
 // Runs `issue` through a cached CUDA graph (captured on the plan's own stream) or directly.
@@ -574,7 +667,8 @@ int sa_plan_destroy(sa_plan* p) {
     void* bufs[] = {p->field[0], p->field[1], p->W, p->vp, p->alpha, p->buoy, p->bxh, p->byh, p->C1, p->C2, p->C3,
                     p->medium_stage,
                     p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
-                    p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb};
+                    p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
+                    p->afield[0], p->afield[1]};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (p->cap) cudaStreamDestroy(p->cap);
@@ -613,6 +707,7 @@ int sa_set_medium(sa_plan* p, const float* vp, const float* rho, const float* al
     p->medium_set = true;
     if (p->geometry_set) CKR(build_lists(p));
     p->snaps_valid = false;
+    p->ckpt_valid = false;
     return SA_OK;
 }
 
@@ -665,32 +760,41 @@ int sa_set_geometry(sa_plan* p, int n_shots, const int* src_offsets, const float
     CKR(ensure(&p->rec_amp, &p->cap_rec_amp, (size_t)p->d.nt * nr));
     p->geometry_set = true;
     p->snaps_valid = false;
+    p->ckpt_valid = false;
     return SA_OK;
 }
 
 int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, void* stream) {
     if (!p) return fail(SA_E_INVALID, "null plan");
-    if (p->p3) {
-        if (save_mode != SA_SAVE_NONE && save_mode != SA_SAVE_SNAPSHOTS) return fail(SA_E_INVALID, "save_mode");
-        return sa::plan3d_forward(p->p3, wavelets, traces, save_mode, (cudaStream_t)stream);
-    }
+    if (save_mode != SA_SAVE_NONE && save_mode != SA_SAVE_SNAPSHOTS && save_mode != SA_SAVE_CHECKPOINTS)
+        return fail(SA_E_INVALID, "save_mode %d", save_mode);
+    if (p->p3) return sa::plan3d_forward(p->p3, wavelets, traces, save_mode, (cudaStream_t)stream);
     if (!p->medium_set || !p->geometry_set) return fail(SA_E_INVALID, "medium and geometry must be set first");
     if ((p->n_src && !wavelets) || (p->n_rec && !traces)) return fail(SA_E_INVALID, "null wavelets or traces");
-    if (save_mode != SA_SAVE_NONE && save_mode != SA_SAVE_SNAPSHOTS) return fail(SA_E_INVALID, "save_mode");
     cudaStream_t s = (cudaStream_t)stream;
-    const bool save = save_mode == SA_SAVE_SNAPSHOTS;
-    if (save) {
+    // a forward replaces the plan's wavelets, which the checkpointed adjoint re-injects
+    p->ckpt_valid = false;
+    if (save_mode == SA_SAVE_SNAPSHOTS) {
         const size_t n = (size_t)npairs(p) * p->snap_shot_stride * 2;
         float* old = p->snaps;
         CKR(ensure(&p->snaps, &p->cap_snaps, n));
         if (old != p->snaps) drop_graphs(p);
         // every slot the adjoint reads (t % f == 0, f <= t <= nt-1-f) is written by this forward
+    } else if (save_mode == SA_SAVE_CHECKPOINTS) {
+        const int oldK = p->ck_K;
+        CKR(plan_checkpoints(p));
+        const size_t n = std::max<size_t>(1, (size_t)p->ck_n * 2 * npairs(p) * p->shot_stride * 2);
+        float* old = p->ckpt;
+        CKR(ensure(&p->ckpt, &p->cap_ckpt, n));
+        if (old != p->ckpt || oldK != p->ck_K) drop_graphs(p);
+        p->snaps_valid = false;
     }
     CKR(load_transposed(p, wavelets, p->n_src, p->d.nt, p->src_amp, s));
-    CKR(run_loop(p, &p->g_fwd[save ? 1 : 0], s, [&](cudaStream_t cs) { return issue_forward(p, save, cs); }));
+    CKR(run_loop(p, &p->g_fwd[save_mode], s, [&](cudaStream_t cs) { return issue_forward(p, save_mode, cs); }));
     CKR(store_transposed(p, p->rec_amp, p->d.nt, p->n_rec, traces, s));
-    p->launches = (p->n_src ? 1 : 0) + p->loop_launches[save ? 1 : 0] + (p->n_rec ? 1 : 0);
-    if (save) p->snaps_valid = true;
+    p->launches = (p->n_src ? 1 : 0) + p->fwd_launches[save_mode] + (p->n_rec ? 1 : 0);
+    if (save_mode == SA_SAVE_SNAPSHOTS) p->snaps_valid = true;
+    if (save_mode == SA_SAVE_CHECKPOINTS) p->ckpt_valid = true;
     return SA_OK;
 }
 
@@ -701,7 +805,9 @@ int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_v
         if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
         return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream);
     }
-    if (!p->snaps_valid) return fail(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS");
+    const bool ck = p->ckpt_valid;
+    if (!p->snaps_valid && !ck)
+        return fail(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS or SA_SAVE_CHECKPOINTS");
     if ((p->n_rec && !residuals) || !grad_vp || !prec_vp) return fail(SA_E_INVALID, "null residuals or outputs");
     cudaStream_t s = (cudaStream_t)stream;
     const size_t fe = (size_t)npairs(p) * p->shot_stride;
@@ -709,8 +815,16 @@ int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_v
     CKR(ensure(&p->gradb, &p->cap_gradb, fe));
     CKR(ensure(&p->precb, &p->cap_precb, fe));
     if (og != p->gradb || op != p->precb) drop_graphs(p);
+    if (ck) {
+        float *o0 = p->afield[0], *o1 = p->afield[1], *os = p->segsnaps;
+        CKR(ensure(&p->afield[0], &p->afield_cap[0], 2 * fe));
+        CKR(ensure(&p->afield[1], &p->afield_cap[1], 2 * fe));
+        CKR(ensure(&p->segsnaps, &p->cap_segsnaps, (size_t)(p->ck_K / p->d.undersampling) * 2 * fe));
+        if (o0 != p->afield[0] || o1 != p->afield[1] || os != p->segsnaps) drop_graphs(p);
+    }
     CKR(load_transposed(p, residuals, p->n_rec, p->d.nt, p->rec_amp, s));
-    CKR(run_loop(p, &p->g_adj, s, [&](cudaStream_t cs) { return issue_adjoint(p, cs); }));
+    CKR(run_loop(p, &p->g_adj[ck ? 1 : 0], s,
+                 [&](cudaStream_t cs) { return ck ? issue_adjoint_ckpt(p, cs) : issue_adjoint(p, cs); }));
     const size_t N = (size_t)p->nx * p->ny;
     for (int k = 0; k < 2; k++) {
         float* user = k == 0 ? grad_vp : prec_vp;
@@ -724,7 +838,7 @@ int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_v
             CK(cudaStreamSynchronize(s));
         }
     }
-    p->launches = (p->n_rec ? 1 : 0) + p->loop_launches[2] + 2;
+    p->launches = (p->n_rec ? 1 : 0) + p->adj_launches[ck ? 1 : 0] + 2;
     return SA_OK;
 }
 
@@ -792,6 +906,7 @@ int sa_autotune(sa_plan* p, void* stream) {
     p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
     CKR(build_lists(p));
     p->snaps_valid = false;
+    p->ckpt_valid = false;
     return SA_OK;
 }
 

@@ -51,12 +51,12 @@ def window(nt):
     return npo.tukey(nt)
 
 
-def make_plan(c, max_shots=None):
+def make_plan(c, max_shots=None, **plan_kw):
     from stride_gb300 import _lib
     n_shots = len(c['srcs'])
     plan = _lib.Plan(2, c['vp'].shape, c['spacing'], c['extra'], c['absorbing'], c['dt'], c['nt'],
                      kernel=c['kernel'], density=density_mode(c['rho']), attenuation=c['alpha'] is not None,
-                     undersampling=4, max_shots=max_shots or n_shots)
+                     undersampling=4, max_shots=max_shots or n_shots, **plan_kw)
     plan.set_medium(np.ascontiguousarray(c['vp']),
                     None if c['rho'] is None else np.ascontiguousarray(c['rho']),
                     None if c['alpha'] is None else np.ascontiguousarray(c['alpha']))

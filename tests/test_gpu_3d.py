@@ -38,10 +38,10 @@ def case3d(kernel='OT4', density='variable', alpha=True, inner=24, nt=160, seed=
                 srcs=srcs, recs=recs, wav=wav)
 
 
-def make_plan3(c):
+def make_plan3(c, **plan_kw):
     plan = _lib.Plan(3, c['vp'].shape, c['spacing'], c['extra'], c['absorbing'], c['dt'], c['nt'], kernel=c['kernel'],
                      density=C.density_mode(c['rho']), attenuation=c['alpha'] is not None, undersampling=4,
-                     max_shots=len(c['srcs']))
+                     max_shots=len(c['srcs']), **plan_kw)
     plan.set_medium(np.ascontiguousarray(c['vp']), None if c['rho'] is None else np.ascontiguousarray(c['rho']),
                     None if c['alpha'] is None else np.ascontiguousarray(c['alpha']))
     eps = 1e-3 * np.asarray(c['spacing'])
