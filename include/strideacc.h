@@ -40,6 +40,9 @@ extern "C" {
                                  segment's p.dt2 from its checkpoint (same gradient, less memory) */
 
 #define SA_GRAD_PARITY 0      /* reference imaging condition: sum_{t%f==0} p_tt * p_a, interior only */
+#define SA_GRAD_EXACT 1       /* gradient of the discrete forward map (its exact transpose), every grid
+                                 point; needs SA_SAVE_CHECKPOINTS; 2D plans. No counterpart in the
+                                 reference (whose gradient is SA_GRAD_PARITY) */
 
 /* Plan description (stride/physics/iso_acoustic/devito.py:119-183 defaults; shapes are the
  * extended grid of stride/problem/domain.py:48-74). */
@@ -98,7 +101,11 @@ int sa_forward(sa_plan* plan, const float* wavelets, float* traces, int save_mod
  * grad_vp/prec_vp [N] float32 on the extended grid receive the raw imaging condition summed
  * over the shots (Devito grad_vp/prec_vp data, zero outside the interior) before the
  * get_grad_vp chain rule. grad_mode SA_GRAD_PARITY. Requires a prior sa_forward with
- * SA_SAVE_SNAPSHOTS or SA_SAVE_CHECKPOINTS (then each segment is recomputed from its checkpoint). Replaces run_adjoint/after_adjoint (devito.py:875-981). */
+ * SA_SAVE_SNAPSHOTS or SA_SAVE_CHECKPOINTS (then each segment is recomputed from its
+ * checkpoint). Replaces run_adjoint/after_adjoint (devito.py:875-981).
+ * grad_mode SA_GRAD_EXACT (2D, after SA_SAVE_CHECKPOINTS): residuals are dL/dtraces and grad_vp
+ * receives dL/dvp of the discrete forward map at every point (no window, no interior cut, no
+ * chain rule); prec_vp receives sum over all steps of p.dt2^2. */
 int sa_adjoint(sa_plan* plan, const float* residuals, float* grad_vp, float* prec_vp, int grad_mode,
                void* stream);
 

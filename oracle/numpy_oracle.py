@@ -25,7 +25,7 @@ import scipy.signal
 __all__ = [
     'second_derivative_weights', 'staggered_weights', 'damping_profile',
     'linear_stencil', 'select_kernel', 'select_undersampling', 'bandwidth',
-    'tone_burst', 'tukey', 'forward', 'adjoint', 'grad_vp_chain',
+    'tone_burst', 'tukey', 'forward', 'adjoint', 'grad_vp_chain', 'adjoint_exact',
     'DB_TO_NEPER',
 ]
 
@@ -375,7 +375,7 @@ def forward(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, or
         if save and t % f == 0:
             snaps[t // f] = (pn - 2 * p + pm) / dtype(dt * dt)
         pm, p = p, pn
-    return rec.T.astype(np.float32), snaps
+    return rec.T.astype(np.float32 if dtype == np.float32 else np.float64), snaps
 
 
 def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
@@ -432,3 +432,92 @@ def grad_vp_chain(grad, prec, vp_inner, slowness=True):
         g *= -2 / vp ** 3
         p *= (2 / vp) ** 3 ** 2
     return g, p
+
+
+def _coefficient_derivatives(med, damp, dt):
+    """Per-point update coefficients C1, C2, C3 of ``_update`` and their derivatives with respect
+    to vp, with the damping's own vp factor (``damping_profile`` multiplies by vp) included:
+    beta = dt (vp^2 d + a vp), C1 = dt^2/(1+beta), C2 = (2 - dt^2 vp^2 d^2)/(1+beta),
+    C3 = (1-beta)/(1+beta)."""
+    vp = med.vp.astype(np.float64)
+    d = damp.astype(np.float64)
+    a = np.zeros_like(vp) if med.alpha is None else med.alpha.astype(np.float64)
+    beta = dt * (vp * vp * d + a * vp)
+    dbeta = dt * (3 * vp * d + a)                  # d(vp^2 d)/dvp = 3 vp d since d is proportional to vp
+    q = 1 + beta
+    C1 = dt * dt / q
+    C2 = (2 - dt * dt * vp * vp * d * d) / q
+    C3 = (1 - beta) / q
+    dC1 = -dt * dt * dbeta / q ** 2
+    dC2 = (-dt * dt * 4 * vp * d * d * q - (2 - dt * dt * vp * vp * d * d) * dbeta) / q ** 2
+    dC3 = -2 * dbeta / q ** 2
+    return C1, C2, C3, dC1, dC2, dC3
+
+
+def adjoint_exact(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, rec_weights, origin,
+                  rho=None, alpha=None, kernel=None):
+    """Exact discrete adjoint of ``forward`` (FP64): the gradient of L = sum(rec_weights * traces)
+    with respect to vp at every grid point and to the raw wavelets, i.e. the transpose of the
+    linearised forward map applied to ``rec_weights`` [n_rec, nt] (dL/dtraces).
+
+    The forward is u[n+1] = C1 Lt(u[n]) + C2 u[n] - C3 u[n-1] + s[n] (n = 1..nt-2) with
+    rec[n] = P u[n+1]. With mu[n] = dL/du[n], the recursion runs backwards from mu[nt] = 0:
+    mu[n] = P^T r[n-1] + Lt^T(C1 mu[n+1]) + C2 mu[n+1] - C3 mu[n+2]. Because Lt = W G (OT2) or
+    W G + dt^2/12 W G W G (OT4) with G symmetric, Lt^T x = Lt(W x) / W, so z = C1 W mu obeys the
+    forward recursion itself. The vp gradient collects, per step, mu[n+1] times the vp
+    derivative of the update: the coefficients (attenuation and damping included), W inside Lt
+    (dW/dvp = 2 W / vp), the OT4 term's inner W (dt^2/12 dW (G u)(G z)) and the source
+    injection's vp factor. This is the ``exact`` gradient mode (no counterpart in the
+    reference, whose imaging condition is iso_acoustic/devito.py:985-1043)."""
+    dim = vp.ndim
+    shape = vp.shape
+    h = max(spacing)
+    if kernel is None:
+        kernel = select_kernel(dt, h, float(np.max(vp)), dim)
+    w2 = second_derivative_weights()
+    ws = staggered_weights()
+    t64 = np.float64
+    med = _Medium(vp, rho, alpha, spacing, t64)
+    damp = damping_profile(shape, spacing, absorbing, vp, dt).astype(t64)
+    eps = 1e-3 * np.asarray(spacing)
+    sb, sw = linear_stencil(np.asarray(src_coords, np.float32) + eps, origin, spacing)
+    rb, rw = linear_stencil(np.asarray(rec_coords, np.float32) + eps, origin, spacing)
+    win = tukey(nt)
+    src = np.asarray(wavelets, np.float64).T * win[:, None]
+    scale = 2 * dt / h
+    offs = _corner_offsets(dim)
+    # forward levels u[0..nt-1]
+    u = np.zeros((nt,) + shape)
+    for n in range(1, nt - 1):
+        pn = _update(med, damp, _Lt(med, u[n], kernel, dt, w2, ws), u[n], u[n - 1], dt)
+        for c, off in enumerate(offs):
+            idx = tuple(sb[:, d] + off[d] for d in range(dim))
+            np.add.at(pn, idx, sw[:, c] * src[n] * scale * med.vp[idx])
+        u[n + 1] = pn
+    C1, C2, C3, dC1, dC2, dC3 = _coefficient_derivatives(med, damp, dt)
+    W = med.L(np.ones(shape), w2, ws) * 0 + (med.vp2 if med.rho_mode != 1 else med.vp2 * med.rho)
+    vpf = med.vp.astype(np.float64)
+    r = np.asarray(rec_weights, np.float64).T  # [nt, n_rec]
+    grad = np.zeros(shape)
+    gsrc = np.zeros((nt, sb.shape[0]))
+    z1 = np.zeros(shape)  # z[n+1]
+    z2 = np.zeros(shape)  # z[n+2]
+    for n in range(nt - 1, 1, -1):
+        zn = _update(med, damp, _Lt(med, z1, kernel, dt, w2, ws), z1, z2, dt) if n < nt - 1 else np.zeros(shape)
+        if 1 <= n - 1 <= nt - 2:
+            for c, off in enumerate(offs):
+                idx = tuple(rb[:, d] + off[d] for d in range(dim))
+                np.add.at(zn, idx, rw[:, c] * r[n - 1] * (C1 * W)[idx])
+        # contributions of step m = n-1 (u[n] = RHS(u[n-1], u[n-2])) with mu[n] = z[n] / (C1 W)
+        m = n - 1
+        mu = zn / (C1 * W)
+        Ltu = _Lt(med, u[m], kernel, dt, w2, ws)
+        grad += mu * (dC1 * Ltu + C1 * (2 / vpf) * Ltu + dC2 * u[m] - dC3 * u[m - 1])
+        if kernel == 'OT4':
+            grad += dt * dt / 12 * (2 * W / vpf) * (med.L(u[m], w2, ws) / W) * (med.L(zn, w2, ws) / W)
+        for c, off in enumerate(offs):
+            idx = tuple(sb[:, d] + off[d] for d in range(dim))
+            np.add.at(grad, idx, mu[idx] * sw[:, c] * src[m] * scale)
+            gsrc[m] += mu[idx] * sw[:, c] * scale * med.vp[idx]
+        z2, z1 = z1, zn
+    return grad, (gsrc * win[:, None]).T

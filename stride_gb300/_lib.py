@@ -28,6 +28,7 @@ SA_SAVE_NONE = 0
 SA_SAVE_SNAPSHOTS = 1
 SA_SAVE_CHECKPOINTS = 2
 SA_GRAD_PARITY = 0
+SA_GRAD_EXACT = 1
 
 # every symbol include/strideacc.h declares
 EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometry', 'sa_forward',
@@ -172,9 +173,11 @@ class Plan:
                 'checkpoints': SA_SAVE_CHECKPOINTS}[save]
         check(load().sa_forward(self._h, _ptr(wavelets), _ptr(traces), mode, _stream(stream)))
 
-    def adjoint(self, residuals, grad, prec, stream=None):
-        check(load().sa_adjoint(self._h, _ptr(residuals), _ptr(grad), _ptr(prec), SA_GRAD_PARITY,
-                                _stream(stream)))
+    def adjoint(self, residuals, grad, prec, stream=None, exact=False):
+        """exact=False: the reference's imaging condition; exact=True: dL/dvp of the discrete forward
+        map for residuals = dL/dtraces (needs a forward with save='checkpoints')."""
+        check(load().sa_adjoint(self._h, _ptr(residuals), _ptr(grad), _ptr(prec),
+                                SA_GRAD_EXACT if exact else SA_GRAD_PARITY, _stream(stream)))
 
     def autotune(self, stream=None):
         check(load().sa_autotune(self._h, _stream(stream)))

@@ -13,6 +13,16 @@ cudaError_t medium2d(const float* vp_in, const float* rho_in, const float* alpha
                      float* alpha, float* buoy, float* bxh, float* byh, float* C1, float* C2, float* C3,
                      cudaStream_t s);
 void set_last_error(const char* msg);
+// exact-gradient mode (exact2d.cu)
+cudaError_t exact_coef2d(const float* vp, const float* alpha, const float* W, int nx, int ny, int pitch,
+                         const Sponge& sp, float dt, float* EA, float* EB, float* EC, float* EG4, float* ES,
+                         cudaStream_t s);
+cudaError_t exact_grad2d(const float* z, const float* u0, const float* u1, const float* u2, const float* Lu,
+                         const float* Lz, const float* EA, const float* EB, const float* EC, const float* EG4, int nx,
+                         int ny, int pitch, int npairs, long long shot_stride, float inv_dt2, float* gradb,
+                         float* precb, cudaStream_t s);
+cudaError_t exact_src2d(const float* z, const Gather* g, int n, const float* amp, int ld, int trow, float scale,
+                        const float* ES, int pitch, long long shot_stride, float* gradb, cudaStream_t s);
 
 // 3D plans
 struct Sponge3 {

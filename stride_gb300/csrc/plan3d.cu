@@ -76,7 +76,9 @@ int choose_checkpoints(const sa_desc& d, double level, int* K_out, int* n_out) {
     const int T0 = d.nt - 1 - f;
     int K = d.checkpoint_interval > 0 ? d.checkpoint_interval : 50;
     K = (K + f - 1) / f * f;
-    auto bytes = [&](int k) { return (T0 >= 1 ? (T0 - 1) / k : 0) * 2 * level + (k / f) * level; };
+    // checkpoints after steps K, 2K, .. <= nt-2 (the exact adjoint's segments reach that far) and
+    // one segment's K/f snapshots
+    auto bytes = [&](int k) { return ((d.nt - 2) / k) * 2 * level + (k / f) * level; };
     if (d.checkpoint_budget > 0 && bytes(K) > d.checkpoint_budget) {
         int best = -1;
         double least = 1e300;
@@ -93,7 +95,7 @@ int choose_checkpoints(const sa_desc& d, double level, int* K_out, int* n_out) {
         K = best;
     }
     *K_out = K;
-    *n_out = T0 >= 1 ? (T0 - 1) / K : 0;
+    *n_out = (d.nt - 2) / K;
     return SA_OK;
 }
 

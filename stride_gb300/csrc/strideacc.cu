@@ -129,6 +129,19 @@ struct sa_plan {
     size_t cap_ckpt = 0, cap_segsnaps = 0, afield_cap[2] = {0, 0};
     int ck_K = 0, ck_n = 0;
     bool ckpt_valid = false;
+    // exact-gradient mode: per-point derivative coefficients, every level of a segment, the
+    // W G(.) of a forward and an adjoint level, unit/zero update coefficients (guarded), the
+    // receiver injection with coefficient C1 W, flat source list
+    float *EA = nullptr, *EB = nullptr, *EC = nullptr, *EG4 = nullptr, *ES = nullptr, *levels = nullptr;
+    float *Lu = nullptr, *Lz = nullptr, *ones_g = nullptr, *zeros_g = nullptr;
+    size_t cap_EA = 0, cap_EB = 0, cap_EC = 0, cap_EG4 = 0, cap_ES = 0, cap_levels = 0, cap_Lu = 0, cap_Lz = 0,
+           cap_ones = 0, cap_zeros = 0;
+    bool exact_coef_valid = false;
+    std::vector<float> c1w_host;
+    sa::Inject* inj_recx = nullptr;
+    int* inj_recx_off = nullptr;
+    sa::Gather* src_flat = nullptr;
+    size_t cap_inj_recx = 0, cap_inj_recx_off = 0, cap_src_flat = 0;
     // layout
     int NT = 128, by = 110, chunk_rows = 1, nstrips = 1, nchunks = 1;
     bool layout_fixed = false;
@@ -136,9 +149,9 @@ struct sa_plan {
     // graphs
     cudaStream_t cap = nullptr;
     cudaGraphExec_t g_fwd[3] = {nullptr, nullptr, nullptr};  // by save mode
-    cudaGraphExec_t g_adj[2] = {nullptr, nullptr};           // from snapshots, from checkpoints
+    cudaGraphExec_t g_adj[3] = {nullptr, nullptr, nullptr};  // from snapshots, from checkpoints, exact
     long long fwd_launches[3] = {0, 0, 0};                   // kernels in each forward loop (by save mode)
-    long long adj_launches[2] = {0, 0};                      // kernels in each adjoint loop
+    long long adj_launches[3] = {0, 0, 0};                   // kernels in each adjoint loop
     bool use_graphs = true;
     long long launches = 0;                   // kernels launched by the last sa_forward / sa_adjoint
 };
@@ -224,8 +237,9 @@ int build_lists(sa_plan* p) {
     const double dt = p->d.dt;
     // shots advance in pairs (the two lanes of a float2); CTA index of (pair, chunk, strip)
     auto cta_of = [&](int shot, int x, int y) { return ((shot / 2) * nc + x / p->chunk_rows) * ns + y / p->by; };
+    // corner(x, y): the per-corner factor of the coefficient (vp, vp^2 or C1 W there)
     auto make_inj = [&](const std::vector<int>& off, const std::vector<int>& bx, const std::vector<int>& by,
-                        const std::vector<double>& fx, const std::vector<double>& fy, double scale, int vp_power,
+                        const std::vector<double>& fx, const std::vector<double>& fy, double scale, auto corner,
                         std::vector<HostInject>& out) {
         out.clear();
         for (int s = 0; s < p->n_shots; s++)
@@ -234,9 +248,7 @@ int build_lists(sa_plan* p) {
                     for (int cy = 0; cy < 2; cy++) {
                         const int x = bx[i] + cx, y = by[i] + cy;
                         const double w = (cx ? fx[i] : 1.0 - fx[i]) * (cy ? fy[i] : 1.0 - fy[i]);
-                        const float v = p->vp_host.empty() ? 0.f : p->vp_host[(size_t)x * p->ny + y];
-                        const double vpow = vp_power == 2 ? (double)(v * v) : (double)v;
-                        out.push_back({cta_of(s, x, y), x, y, i, (float)(w * scale * vpow), s & 1});
+                        out.push_back({cta_of(s, x, y), x, y, i, (float)(w * scale * corner(x, y)), s & 1});
                     }
         std::stable_sort(out.begin(), out.end(), [](const HostInject& a, const HostInject& b) {
             return a.cta != b.cta ? a.cta < b.cta : a.row < b.row;
@@ -259,11 +271,32 @@ int build_lists(sa_plan* p) {
     };
     std::vector<HostInject> tmp;
     // forward source: src * 2 dt^2 vp / h / dt (iso_acoustic/devito.py:349-363), vp at the corner
-    make_inj(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, 2.0 * dt / h, 1, tmp);
+    auto vp_at = [&](int x, int y) { return p->vp_host.empty() ? 0.0 : (double)p->vp_host[(size_t)x * p->ny + y]; };
+    auto vp2_at = [&](int x, int y) {
+        const float v = p->vp_host.empty() ? 0.f : p->vp_host[(size_t)x * p->ny + y];
+        return (double)(v * v);
+    };
+    auto c1w_at = [&](int x, int y) { return p->c1w_host.empty() ? 0.0 : (double)p->c1w_host[(size_t)x * p->ny + y]; };
+    make_inj(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, 2.0 * dt / h, vp_at, tmp);
     CKR(upload_inj(tmp, &p->inj_src, &p->cap_inj_src, &p->inj_src_off, &p->cap_inj_src_off));
     // adjoint receiver: -rec * dt^2 * vp^2 (devito.py:748-753), vp^2 at the corner
-    make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, -dt * dt, 2, tmp);
+    make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, -dt * dt, vp2_at, tmp);
     CKR(upload_inj(tmp, &p->inj_rec, &p->cap_inj_rec, &p->inj_rec_off, &p->cap_inj_rec_off));
+    // exact-gradient adjoint: dL/drec injected with the update's own C1 W at the corner
+    make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, 1.0, c1w_at, tmp);
+    CKR(upload_inj(tmp, &p->inj_recx, &p->cap_inj_recx, &p->inj_recx_off, &p->cap_inj_recx_off));
+    {  // flat source list (pad = shot) for the exact gradient's source term
+        std::vector<sa::Gather> sf;
+        for (int s = 0; s < p->n_shots; s++)
+            for (int i = p->src_off[s]; i < p->src_off[s + 1]; i++) {
+                const double fx = p->src_fx[i], fy = p->src_fy[i];
+                sf.push_back({p->src_bx[i], p->src_by[i], i, s, (float)((1 - fx) * (1 - fy)), (float)((1 - fx) * fy),
+                              (float)(fx * (1 - fy)), (float)(fx * fy)});
+            }
+        CKR(ensure(&p->src_flat, &p->cap_src_flat, sf.size()));
+        if (!sf.empty())
+            CK(cudaMemcpy(p->src_flat, sf.data(), sf.size() * sizeof(sa::Gather), cudaMemcpyHostToDevice));
+    }
     // receiver gathers, one per receiver, owned by the CTA of its base corner
     std::vector<std::pair<int, sa::Gather>> g;
     std::vector<sa::Gather> flat;
@@ -491,6 +524,102 @@ int plan_checkpoints(sa_plan* p) {
     return sa::choose_checkpoints(p->d, (double)npairs(p) * p->shot_stride * sizeof(float2), &p->ck_K, &p->ck_n);
 }
 
+// Exact gradient of the discrete forward map (SA_GRAD_EXACT) from checkpoints. With z = C1 W mu
+// the adjoint obeys the forward recursion: adjoint step t (t = nt .. 2) computes z[t-1] from
+// z[t], z[t+1] with dL/drec[t-2] injected with coefficient C1 W, and for t <= nt-1 adds the
+// contribution of forward step t-1 (exact2d.cu), which needs the levels u[t], u[t-1], u[t-2]
+// and, for OT4, W G u[t-1] and W G z[t]. Segment k covers t = kK+2 .. min((k+1)K+1, nt): its
+// levels u[kK] .. are rebuilt from checkpoint k into `levels` (slot = level - kK); W G(.) is the
+// OT2 step kernel with C1 = 1, C2 = C3 = 0.
+int issue_adjoint_exact(sa_plan* p, cudaStream_t s) {
+    const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
+    const size_t ffl = fbytes / sizeof(float);
+    const size_t gbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float);
+    const int nt = p->d.nt, K = p->ck_K;
+    CK(cudaMemsetAsync(p->afield[0], 0, fbytes, s));
+    CK(cudaMemsetAsync(p->afield[1], 0, fbytes, s));
+    CK(cudaMemsetAsync(p->gradb, 0, gbytes, s));
+    CK(cudaMemsetAsync(p->precb, 0, gbytes, s));
+    sa::Step2D fa = base_args(p);  // forward recompute
+    fa.inj = p->n_src ? p->inj_src : nullptr;
+    fa.inj_off = p->inj_src_off;
+    fa.inj_amp = p->src_amp;
+    fa.inj_ld = p->n_src;
+    fa.gat = nullptr;
+    fa.save = 0;
+    fa.grad = 0;
+    sa::Step2D aa = fa;  // adjoint: dL/drec[t-2] at step t
+    aa.inj = p->n_rec ? p->inj_recx : nullptr;
+    aa.inj_off = p->inj_recx_off;
+    aa.inj_amp = p->rec_amp - 2 * (long long)p->n_rec;  // read at t >= 2 only
+    aa.inj_ld = p->n_rec;
+    sa::Step2D la = fa;  // W G(cur) into prev
+    la.inj = nullptr;
+    la.C1 = row0(p, p->ones_g, p->pitch);
+    la.C2 = la.C3 = row0(p, p->zeros_g, p->pitch);
+    const dim3 grid(p->nstrips, p->nchunks, npairs(p));
+    const float inv_dt2 = (float)(1.0 / (p->d.dt * p->d.dt));
+    const float src_scale = (float)(2.0 * p->d.dt / std::max(p->d.spacing[0], p->d.spacing[1]));
+    auto level = [&](int k, int m) { return p->levels + (size_t)(m - k * K) * ffl; };
+    long long n = 0;
+    for (int k = (nt - 2) / K; k >= 0; k--) {
+        const int t_lo = std::max(2, k * K + 2), t_hi = std::min((k + 1) * K + 1, nt);
+        if (t_lo > t_hi) continue;
+        if (k == 0) {
+            CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
+            CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
+        } else {
+            const float* slot = p->ckpt + (size_t)(k - 1) * 2 * ffl;
+            CK(cudaMemcpyAsync(p->field[0], slot, fbytes, cudaMemcpyDeviceToDevice, s));
+            CK(cudaMemcpyAsync(p->field[1], slot + ffl, fbytes, cudaMemcpyDeviceToDevice, s));
+        }
+        // u[kK] lives in field[kK & 1], u[kK+1] in the other
+        CK(cudaMemcpyAsync(level(k, k * K), p->field[(k * K) & 1], fbytes, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(level(k, k * K + 1), p->field[(k * K + 1) & 1], fbytes, cudaMemcpyDeviceToDevice, s));
+        for (int m = k * K + 1; m <= std::min((k + 1) * K, nt - 2); m++) {  // forward step m -> u[m+1]
+            fa.t = m;
+            fa.cur = p->field[m & 1];
+            fa.prev = p->field[(m + 1) & 1];
+            CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, fa));
+            CK(cudaMemcpyAsync(level(k, m + 1), p->field[(m + 1) & 1], fbytes, cudaMemcpyDeviceToDevice, s));
+            n++;
+        }
+        for (int t = t_hi; t >= t_lo; t--) {
+            float* zt = p->afield[t & 1];
+            aa.t = t;
+            aa.cur = zt;
+            aa.prev = p->afield[(t + 1) & 1];
+            CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, aa));
+            n++;
+            if (t > nt - 1) continue;  // z[nt] = 0
+            const float *Lu = nullptr, *Lz = nullptr;
+            if (p->ot4) {
+                la.t = t - 1;
+                la.cur = level(k, t - 1);
+                la.prev = p->Lu;
+                CK(sa::launch_step2d(p->kind, false, p->NT, grid, s, la));
+                la.t = t;
+                la.cur = zt;
+                la.prev = p->Lz;
+                CK(sa::launch_step2d(p->kind, false, p->NT, grid, s, la));
+                Lu = p->Lu;
+                Lz = p->Lz;
+                n += 2;
+            }
+            CK(sa::exact_grad2d(zt, level(k, t), level(k, t - 1), level(k, t - 2), Lu, Lz, p->EA, p->EB, p->EC, p->EG4,
+                                p->nx, p->ny, p->pitch, npairs(p), p->shot_stride, inv_dt2, p->gradb, p->precb, s));
+            n++;
+            if (p->n_src) {
+                CK(sa::exact_src2d(zt, p->src_flat, p->n_src, p->src_amp, p->n_src, t - 1, src_scale, p->ES, p->pitch,
+                                   p->shot_stride, p->gradb, s));
+                n++;
+            }
+        }
+    }
+    p->adj_launches[2] = n;
+    return SA_OK;
+}
+
 // Runs `issue` through a cached CUDA graph (captured on the plan's own stream) or directly.
 template <class F>
 int run_loop(sa_plan* p, cudaGraphExec_t* slot, cudaStream_t s, F issue) {
@@ -668,7 +797,8 @@ int sa_plan_destroy(sa_plan* p) {
                     p->medium_stage,
                     p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
-                    p->afield[0], p->afield[1]};
+                    p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
+                    p->ones_g, p->zeros_g, p->inj_recx, p->inj_recx_off, p->src_flat};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (p->cap) cudaStreamDestroy(p->cap);
@@ -704,6 +834,16 @@ int sa_set_medium(sa_plan* p, const float* vp, const float* rho, const float* al
     CK(cudaDeviceSynchronize());
     p->vp_host.resize(N);
     CK(cudaMemcpy(p->vp_host.data(), dev[0], N * sizeof(float), cudaMemcpyDeviceToHost));
+    {  // C1 W per point: the exact-gradient adjoint's receiver injection coefficient
+        std::vector<float> c1((size_t)p->nx * p->pitch), w((size_t)p->nx * p->pitch);
+        CK(cudaMemcpy(c1.data(), row0(p, p->C1, p->pitch), c1.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(w.data(), row0(p, p->W, p->pitch), w.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        p->c1w_host.resize(N);
+        for (int x = 0; x < p->nx; x++)
+            for (int y = 0; y < p->ny; y++)
+                p->c1w_host[(size_t)x * p->ny + y] = c1[(size_t)x * p->pitch + y] * w[(size_t)x * p->pitch + y];
+    }
+    p->exact_coef_valid = false;
     p->medium_set = true;
     if (p->geometry_set) CKR(build_lists(p));
     p->snaps_valid = false;
@@ -800,12 +940,15 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
 
 int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_vp, int grad_mode, void* stream) {
     if (!p) return fail(SA_E_INVALID, "null plan");
-    if (grad_mode != SA_GRAD_PARITY) return fail(SA_E_UNSUPPORTED, "grad_mode %d", grad_mode);
+    if (grad_mode != SA_GRAD_PARITY && grad_mode != SA_GRAD_EXACT) return fail(SA_E_INVALID, "grad_mode %d", grad_mode);
+    const bool exact = grad_mode == SA_GRAD_EXACT;
     if (p->p3) {
+        if (exact) return fail(SA_E_UNSUPPORTED, "SA_GRAD_EXACT is implemented for 2D plans");
         if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
         return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream);
     }
     const bool ck = p->ckpt_valid;
+    if (exact && !ck) return fail(SA_E_INVALID, "SA_GRAD_EXACT needs a prior sa_forward with SA_SAVE_CHECKPOINTS");
     if (!p->snaps_valid && !ck)
         return fail(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS or SA_SAVE_CHECKPOINTS");
     if ((p->n_rec && !residuals) || !grad_vp || !prec_vp) return fail(SA_E_INVALID, "null residuals or outputs");
@@ -819,12 +962,42 @@ int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_v
         float *o0 = p->afield[0], *o1 = p->afield[1], *os = p->segsnaps;
         CKR(ensure(&p->afield[0], &p->afield_cap[0], 2 * fe));
         CKR(ensure(&p->afield[1], &p->afield_cap[1], 2 * fe));
-        CKR(ensure(&p->segsnaps, &p->cap_segsnaps, (size_t)(p->ck_K / p->d.undersampling) * 2 * fe));
+        if (!exact) CKR(ensure(&p->segsnaps, &p->cap_segsnaps, (size_t)(p->ck_K / p->d.undersampling) * 2 * fe));
         if (o0 != p->afield[0] || o1 != p->afield[1] || os != p->segsnaps) drop_graphs(p);
     }
+    if (exact) {
+        const size_t NG = (size_t)(p->nx + 2 * sa::GUARD) * p->pitch;
+        float* old[] = {p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz, p->ones_g, p->zeros_g};
+        CKR(ensure(&p->EA, &p->cap_EA, (size_t)p->shot_stride));
+        CKR(ensure(&p->EB, &p->cap_EB, (size_t)p->shot_stride));
+        CKR(ensure(&p->EC, &p->cap_EC, (size_t)p->shot_stride));
+        CKR(ensure(&p->EG4, &p->cap_EG4, (size_t)p->shot_stride));
+        CKR(ensure(&p->ES, &p->cap_ES, (size_t)p->shot_stride));
+        CKR(ensure(&p->levels, &p->cap_levels, (size_t)(p->ck_K + 2) * 2 * fe));
+        CKR(ensure(&p->Lu, &p->cap_Lu, 2 * fe));
+        CKR(ensure(&p->Lz, &p->cap_Lz, 2 * fe));
+        CKR(ensure(&p->ones_g, &p->cap_ones, NG));
+        CKR(ensure(&p->zeros_g, &p->cap_zeros, NG));
+        float* now[] = {p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz, p->ones_g, p->zeros_g};
+        if (!std::equal(std::begin(old), std::end(old), std::begin(now)) || !p->exact_coef_valid) {
+            drop_graphs(p);
+            // W G(.) outputs start finite (their kernel multiplies the old value by C3 = 0)
+            CK(cudaMemset(p->Lu, 0, 2 * fe * sizeof(float)));
+            CK(cudaMemset(p->Lz, 0, 2 * fe * sizeof(float)));
+            CK(cudaMemset(p->zeros_g, 0, NG * sizeof(float)));
+            std::vector<float> ones(NG, 1.f);
+            CK(cudaMemcpy(p->ones_g, ones.data(), NG * sizeof(float), cudaMemcpyHostToDevice));
+            CK(sa::exact_coef2d(p->vp, p->alpha, row0(p, p->W, p->pitch), p->nx, p->ny, p->pitch, p->sponge,
+                                (float)p->d.dt, p->EA, p->EB, p->EC, p->EG4, p->ES, 0));
+            CK(cudaDeviceSynchronize());
+            p->exact_coef_valid = true;
+        }
+    }
     CKR(load_transposed(p, residuals, p->n_rec, p->d.nt, p->rec_amp, s));
-    CKR(run_loop(p, &p->g_adj[ck ? 1 : 0], s,
-                 [&](cudaStream_t cs) { return ck ? issue_adjoint_ckpt(p, cs) : issue_adjoint(p, cs); }));
+    const int am = exact ? 2 : (ck ? 1 : 0);
+    CKR(run_loop(p, &p->g_adj[am], s, [&](cudaStream_t cs) {
+        return exact ? issue_adjoint_exact(p, cs) : (ck ? issue_adjoint_ckpt(p, cs) : issue_adjoint(p, cs));
+    }));
     const size_t N = (size_t)p->nx * p->ny;
     for (int k = 0; k < 2; k++) {
         float* user = k == 0 ? grad_vp : prec_vp;
@@ -838,7 +1011,7 @@ int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_v
             CK(cudaStreamSynchronize(s));
         }
     }
-    p->launches = (p->n_rec ? 1 : 0) + p->adj_launches[ck ? 1 : 0] + 2;
+    p->launches = (p->n_rec ? 1 : 0) + p->adj_launches[am] + 2;
     return SA_OK;
 }
 

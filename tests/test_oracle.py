@@ -137,3 +137,54 @@ def test_linear_interpolation_weights():
     base, w = O.linear_stencil(np.array([[1.25e-3, 2.0e-3]], np.float32), (-1e-3, -1e-3), (0.5e-3, 0.5e-3))
     assert list(base[0]) == [4, 5] or list(base[0]) == [4, 6]
     np.testing.assert_allclose(w.sum(), 1.0, rtol=1e-12)
+
+
+def _exact_case(kernel, rho_mode, alpha, seed=0, nt=110):
+    rng = np.random.default_rng(seed)
+    h, e, n = 0.5e-3, 8, 20
+    shape = (n + 2 * e, n + 3 + 2 * e)
+    vp = (1500 + 100 * rng.random(shape)).astype(np.float64)
+    rho = None if rho_mode == 'none' else (
+        np.full(shape, 1000.) if rho_mode == 'constant' else 950 + 150 * rng.random(shape))
+    al = 20 * rng.random(shape) if alpha else None
+    dt = (0.6 if kernel == 'OT4' else 0.4) * h / 1650
+    src = np.array([[4.1e-3, 5.3e-3], [6.2e-3, 2.1e-3]])
+    rec = np.array([[1.3e-3, 1.1e-3], [8.7e-3, 9.2e-3], [2.2e-3, 8.8e-3]])
+    wav = np.stack([O.tone_burst(1.0e6, 3, nt, dt), O.tone_burst(0.8e6, 3, nt, dt)])
+    return dict(vp=vp, rho=rho, alpha=al, spacing=(h, h), dt=dt, nt=nt, ab=(e, e), origin=(-e * h, -e * h), src=src,
+                rec=rec, wav=wav, kernel=kernel, rng=rng)
+
+
+def _exact_traces(c, vp, wav):
+    return O.forward(vp, c['spacing'], c['dt'], c['nt'], c['ab'], c['src'], c['rec'], wav, c['origin'], rho=c['rho'],
+                     alpha=c['alpha'], kernel=c['kernel'], dtype=np.float64)[0]
+
+
+@pytest.mark.parametrize('kernel,rho_mode,alpha', [('OT4', 'variable', True), ('OT2', 'none', False),
+                                                   ('OT4', 'constant', True)])
+def test_exact_adjoint_dot_product(kernel, rho_mode, alpha):
+    """<F w, r> = <w, F^T r> for the (linear) wavelets -> traces map of the FP64 oracle."""
+    c = _exact_case(kernel, rho_mode, alpha)
+    r = c['rng'].standard_normal((len(c['rec']), c['nt']))
+    w = c['rng'].standard_normal(c['wav'].shape).astype(np.float32).astype(np.float64)
+    _, gw = O.adjoint_exact(c['vp'], c['spacing'], c['dt'], c['nt'], c['ab'], c['src'], c['rec'], w, r, c['origin'],
+                            rho=c['rho'], alpha=c['alpha'], kernel=kernel)
+    lhs = float(np.sum(_exact_traces(c, c['vp'], w) * r))
+    rhs = float(np.sum(gw * w))
+    assert abs(lhs - rhs) <= 1e-6 * abs(lhs)
+
+
+@pytest.mark.parametrize('kernel,rho_mode,alpha', [('OT4', 'variable', True), ('OT2', 'constant', False)])
+def test_exact_adjoint_central_differences(kernel, rho_mode, alpha):
+    """dJ/dvp of the FP64 oracle against central differences, J = sum(r * traces), along random
+    directions over the whole grid (sponge included)."""
+    c = _exact_case(kernel, rho_mode, alpha, seed=1)
+    r = c['rng'].standard_normal((len(c['rec']), c['nt']))
+    g, _ = O.adjoint_exact(c['vp'], c['spacing'], c['dt'], c['nt'], c['ab'], c['src'], c['rec'], c['wav'], r,
+                           c['origin'], rho=c['rho'], alpha=c['alpha'], kernel=kernel)
+    for _ in range(3):
+        d = c['rng'].standard_normal(c['vp'].shape)
+        eps = 1.0  # vp is rounded to FP32 as the reference stores it; 1 m/s keeps that below 1e-4
+        fd = (np.sum(r * _exact_traces(c, c['vp'] + eps * d, c['wav']))
+              - np.sum(r * _exact_traces(c, c['vp'] - eps * d, c['wav']))) / (2 * eps)
+        assert abs(fd - np.sum(g * d)) <= 2e-3 * abs(fd)
