@@ -49,6 +49,15 @@ WORKLOADS = {
     'single': ('single', 1, 'fwd'),         # single-shot forward, 256^2 at 0.5 mm, vp only
     '3d': ('3d', 8, 'fwd'),                 # 3D forward, 296^3, 8 shots per launch
     '3dgrad': ('3d', 1, 'fwdadj'),          # 3D fwd+adj vp gradient of one shot (snapshots in HBM)
+    'exact64': ('batched', 64, 'fwdadj'),   # exact gradient (autograd backward), checkpoints every 50 steps
+    '3dgrad8': ('3d', 8, 'fwdadj'),         # 3D gradient of 8 shots, checkpoints under a 150 GB budget
+}
+# gradient method per workload: the reference imaging condition from snapshots (default), the
+# same from checkpoints with recompute, or the exact discrete adjoint from checkpoints
+# (plan arguments: undersampling, checkpoint interval, checkpoint byte budget)
+GRADIENT = {
+    'exact64': ('exact', dict(undersampling=1, checkpoint_interval=50)),
+    '3dgrad8': ('checkpoints', dict(undersampling=4, checkpoint_budget=150e9)),
 }
 WORKLOAD_NAMES = {
     'fwdadj64': '2D fwd+adj vp gradient: 552^2 extended (512^2 at 0.25 mm + 20 sponge), vp/rho/alpha phantom, '
@@ -60,6 +69,11 @@ WORKLOAD_NAMES = {
           '3000 steps, OT4',
     '3dgrad': '3D fwd+adj vp gradient: 296^3 extended, vp/rho/alpha phantom, 1 shot x 512 receivers, 3000 steps, '
               'OT4, f=4',
+    'exact64': '2D exact vp gradient (torch.autograd backward of the discrete forward map): 552^2 extended, '
+               'vp/rho/alpha phantom, 64 shots x 256 receivers, 4000 steps, OT4, checkpoints every 50 steps with '
+               'recompute',
+    '3dgrad8': '3D fwd+adj vp gradient: 296^3 extended, vp/rho/alpha phantom, 8 shots per launch x 512 receivers, '
+               '3000 steps, OT4, f=4, checkpoints under a 150 GB budget with recompute',
 }
 
 
@@ -276,8 +290,11 @@ def gb300_arm(args):
     rx = (np.concatenate(w['rec']) + eps).astype(np.float32)
     win = scipy.signal.get_window(('tukey', 0.001), nt, False).astype(np.float32)
 
+    method, plan_kw = GRADIENT.get(args.workload, ('snapshots', dict(undersampling=4)))
+    save = {'snapshots': True, 'checkpoints': 'checkpoints', 'exact': 'checkpoints'}[method] if grad_mode else False
+    exact = method == 'exact'
     plan = _lib.Plan(dim, w['shape'], w['spacing'], w['extra'], w['absorbing'], w['dt'], nt, kernel='OT4',
-                     density=_density(w), attenuation=w['alpha'] is not None, undersampling=4, max_shots=n_shots)
+                     density=_density(w), attenuation=w['alpha'] is not None, max_shots=n_shots, **plan_kw)
     plan.set_geometry(so, sx, ro, rx)
     wav = torch.from_numpy(np.tile((w['wavelet'] * win)[None].astype(np.float32), (plan.n_src, 1))).to(dev)
     win_d = torch.from_numpy(win).to(dev)
@@ -300,12 +317,12 @@ def gb300_arm(args):
     def step(timed=False):
         e0, e1, e2 = ev(), ev(), ev()
         e0.record(stream)
-        plan.forward(wav, traces, save=grad_mode, stream=stream)
+        plan.forward(wav, traces, save=save, stream=stream)
         launches['n'] += plan.launches
         e1.record(stream)
         if grad_mode:
             res = (traces - observed) * win_d[None, :]  # L2 residual, adjoint-source window
-            plan.adjoint(res, grad, prec, stream=stream)
+            plan.adjoint(res, grad, prec, stream=stream, exact=exact)
             launches['n'] += plan.launches
         e2.record(stream)
         if world > 1 and grad_mode:
@@ -369,10 +386,10 @@ def gb300_arm(args):
         tr_n, res_n, win_n = tr_h.numpy(), res_h.numpy(), win[None, :]
 
         def e2e_step():
-            plan.forward(wav_h, tr_h, save=grad_mode, stream=stream)
+            plan.forward(wav_h, tr_h, save=save, stream=stream)
             if grad_mode:
                 np.multiply(np.subtract(tr_n, obs_h, out=res_n), win_n, out=res_n)
-                plan.adjoint(res_h, g_h, p_h, stream=stream)
+                plan.adjoint(res_h, g_h, p_h, stream=stream, exact=exact)
 
         e2e_step()
         torch.cuda.synchronize()
@@ -398,13 +415,15 @@ def gb300_arm(args):
         cpu = {'value': rate, 'unit': 'GPts/s', 'cores': cores, 'kind': 'port', 'sample': sample}
 
     if rank == 0:
-        snap_gb = N * n_shots * (nt // 4) * 4 / 1e9 if grad_mode else 0.0
+        snap_gb = N * n_shots * (nt // 4) * 4 / 1e9 if grad_mode and method == 'snapshots' else 0.0
         line = {
             'metric': METRIC[mode], 'value': value, 'unit': 'GPts/s', 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_step, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded phantoms)',
             'config': {'workload': WORKLOAD_NAMES[args.workload], 'grid': list(w['shape']),
                        'shots_per_gpu': n_shots, 'nt': nt, 'kernel': 'OT4',
+                       'gradient': (method + (' (adjoint time includes the forward recompute from checkpoints)'
+                                              if method != 'snapshots' else '')) if grad_mode else None,
                        'parallelism': 'shots sharded over %d GPU(s)%s' % (world, ', gradient all-reduce' if grad_mode else ''),
                        'l2_flush': 'inputs larger than L2 (%.1f GB of wavefields per step)'
                                    % (2 * N * n_shots * 4 / 1e9 + snap_gb)},
