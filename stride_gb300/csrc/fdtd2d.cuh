@@ -101,9 +101,11 @@ struct Smem2D {
     static constexpr int WF = NT + 10;
     static constexpr int oU = 0;
     static constexpr int oL = oU + QU * WU;
+    // y-flux rows of both stages, double-buffered by iteration parity (written before the
+    // iteration's barrier, read after it)
     static constexpr int oF = oL + (OT4 ? QLR * WL : 0);
-    static constexpr int oF2 = oF + (STAG ? RB * WF : 0);
-    static constexpr int total = oF2 + ((OT4 && STAG) ? RB * WF : 0);
+    static constexpr int oF2 = oF + (STAG ? 2 * RB * WF : 0);
+    static constexpr int total = oF2 + ((OT4 && STAG) ? 2 * RB * WF : 0);
     static constexpr size_t bytes = (size_t)total * sizeof(float2);
 };
 
@@ -218,12 +220,19 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
     for (int k = 0; k < PF; k++) prefetch(i0 + k * RB, wrapU(k * RB % QU));
 
     int sJ = 0;  // ring slot of intermediate row j (slot of row x is (x - (i0 - R)) mod QLR)
+    auto wrapL = [](int sl) { return sl < 0 ? sl + QLR : (sl >= QLR ? sl - QLR : sl); };
+    int par = 0;  // flux buffer of this iteration
+    // One barrier per iteration. Before it, the y-fluxes of both stages are computed from rows
+    // that became visible in earlier iterations (u rows j.., intermediate rows o..) into this
+    // iteration's flux buffers; after it, the rows that just landed (cp.async) and the fluxes
+    // are read. Ring slots written after the barrier (new intermediate rows, prefetched u rows)
+    // hold rows no thread reads before the next barrier.
 #pragma unroll 1
     for (int i = i0; i < i1; i += RB) {
         const int j = i - R;        // first stage-1 output row of this iteration
         const int o = i - S * R;    // first output row of this iteration
-        // ---- stage-1 medium of this iteration, loaded before the barrier --------------
-        float Wj[RB], bxi[RB], by1[RB], by1b[RB];
+        // ---- stage-1 medium, stage-2 y medium -----------------------------------------
+        float Wj[RB], bxi[RB], by1[RB], by1b[RB], by2[RB];
 #pragma unroll
         for (int r = 0; r < RB; r++) {
             Wj[r] = __ldg(pW + (long long)(j + r) * pitch);
@@ -232,11 +241,47 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
                 const float* byr = a.byh + (long long)(j + r) * pitch_b;
                 by1[r] = __ldg(byr + kb1);
                 by1b[r] = tid < 9 ? __ldg(byr + kb1b) : 0.f;
+                if constexpr (OT4) by2[r] = __ldg(a.byh + (long long)(o + r) * pitch_b + kb2);
+            }
+        }
+        (void)bxi; (void)by1; (void)by1b; (void)by2;
+        float2* const F = sF + par * RB * L::WF;
+        float2* const F2 = sF2 + par * RB * L::WF;
+        if constexpr (STAG) {
+            // stage-1 y-fluxes at half-cols L1-5+k from u rows j+r (F[k])
+#pragma unroll
+            for (int r = 0; r < RB; r++) {
+                const float2* su = rowU(wrapU(sI - R + r)) + L0;  // su[k] = u(j+r, L0 + k)
+                {
+                    const int k = tid;
+                    float2 v = mul2(dstag2(su, k + 5, k + 4), ihy);
+                    if constexpr (VARB) v = mul2(v, f2(by1[r]));
+                    F[r * L::WF + k] = v;
+                }
+                if (tid < 9) {
+                    const int k = NT + tid;
+                    float2 v = mul2(dstag2(su, k + 5, k + 4), ihy);
+                    if constexpr (VARB) v = mul2(v, f2(by1b[r]));
+                    F[r * L::WF + k] = v;
+                }
+            }
+            if constexpr (OT4) {
+                // stage-2 y-fluxes at half-cols y0-5+k from intermediate rows o+r (F2[k])
+#pragma unroll
+                for (int r = 0; r < RB; r++) {
+                    const float2* sl = sLr + wrapL(sJ - R + r) * L::WL;  // l(o+r, L1 + k)
+                    if (tid < BY + 9) {
+                        const int k = tid;
+                        float2 v = mul2(dstag2(sl, k + 5, k + 4), ihy);
+                        if constexpr (VARB) v = mul2(v, f2(by2[r]));
+                        F2[r * L::WF + k] = v;
+                    }
+                }
             }
         }
 
         cp_async_wait<PF - 1>();
-        __syncthreads();  // rows i..i+RB-1 visible; every thread is done with the last iteration
+        __syncthreads();  // rows i..i+RB-1 and this iteration's fluxes visible; last iteration done
         prefetch(i + PF * RB, sI + PF * RB >= QU ? sI + PF * RB - QU : sI + PF * RB);
 
         // ---- receiver interpolation of p[t] -> rec[t-1]: base rows i-1 .. i+RB-2 ----------
@@ -253,17 +298,14 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
             a.gat_out[(long long)(a.t - 1) * a.gat_ld + G.point] = v;
         }
 
-        // stage-2 and update medium of this iteration (used after the next barrier)
-        float Wo[RB], bxj[RB], by2[RB], c1[RB], c2[RB], c3[RB];
+        // stage-2 and update medium of this iteration
+        float Wo[RB], bxj[RB], c1[RB], c2[RB], c3[RB];
         float2 pmo[RB];
 #pragma unroll
         for (int r = 0; r < RB; r++) {
             if constexpr (OT4) {
                 Wo[r] = __ldg(pW + (long long)(o + r) * pitch);
-                if constexpr (VARB) {
-                    bxj[r] = __ldg(pBX + (long long)(j - 5 + r) * pitch);
-                    by2[r] = __ldg(a.byh + (long long)(o + r) * pitch_b + kb2);
-                }
+                if constexpr (VARB) bxj[r] = __ldg(pBX + (long long)(j - 5 + r) * pitch);
             }
             const bool o_ok = (o + r >= xo0) && (o + r < xo1) && out_col;
             const long long orow = (long long)(o + r) * pitch;
@@ -272,7 +314,7 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
             c3[r] = o_ok ? __ldg(pC3 + orow) : 0.f;
             pmo[r] = o_ok ? prev[orow + c] : f2(0.f);
         }
-        (void)Wo; (void)bxj; (void)by2; (void)bxi; (void)by1; (void)by1b;
+        (void)Wo; (void)bxj;
 
         // ---- stage 1: l = W * G(u) at rows j .. j+RB-1 ----------------------------------
 #pragma unroll
@@ -280,25 +322,7 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
         float2 gy[RB];
         if constexpr (STAG) {
 #pragma unroll
-            for (int r = 0; r < RB; r++) {
-                const float2* su = rowU(wrapU(sI - R + r)) + L0;  // su[k] = u(j+r, L0 + k)
-                float2* F = sF + r * L::WF;                         // F[k]: half-col L1-5+k
-                {
-                    const int k = tid;
-                    float2 v = mul2(dstag2(su, k + 5, k + 4), ihy);
-                    if constexpr (VARB) v = mul2(v, f2(by1[r]));
-                    F[k] = v;
-                }
-                if (tid < 9) {
-                    const int k = NT + tid;
-                    float2 v = mul2(dstag2(su, k + 5, k + 4), ihy);
-                    if constexpr (VARB) v = mul2(v, f2(by1b[r]));
-                    F[k] = v;
-                }
-            }
-            __syncthreads();
-#pragma unroll
-            for (int r = 0; r < RB; r++) gy[r] = mul2(dstag2(sF + r * L::WF, tid + 5, tid + 4), ihy);
+            for (int r = 0; r < RB; r++) gy[r] = mul2(dstag2(F + r * L::WF, tid + 5, tid + 4), ihy);
         } else {
 #pragma unroll
             for (int r = 0; r < RB; r++) gy[r] = mul2(dcent2(rowU(wrapU(sI - R + r)), c), ihy2);
@@ -326,30 +350,17 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
         // ---- stage 2 (OT4): Lt = l + dt^2/12 W G(l) at rows o .. o+RB-1 ------------------
         float2 Lt[RB];
         if constexpr (OT4) {
-            auto wrapL = [](int sl) { return sl < 0 ? sl + QLR : (sl >= QLR ? sl - QLR : sl); };
 #pragma unroll
             for (int r = 0; r < RB; r++) {
-                sLr[wrapL(sJ + r) * L::WL + tid] = lj[r];  // l(j+r, L1 + k)
+                sLr[wrapL(sJ + r) * L::WL + tid] = lj[r];  // l(j+r, L1 + k), read R rows later
                 lq[QB + r] = lj[r];
             }
-            __syncthreads();
             float2 gy2[RB];
             const bool s2 = (tid >= H1) && (tid < H1 + BY);
             if constexpr (STAG) {
 #pragma unroll
-                for (int r = 0; r < RB; r++) {
-                    const float2* sl = sLr + wrapL(sJ - R + r) * L::WL;  // l(o+r, L1 + k)
-                    if (tid < BY + 9) {
-                        const int k = tid;  // flux at half-col y0-5+k from l index k .. k+9
-                        float2 v = mul2(dstag2(sl, k + 5, k + 4), ihy);
-                        if constexpr (VARB) v = mul2(v, f2(by2[r]));
-                        sF2[r * L::WF + k] = v;
-                    }
-                }
-                __syncthreads();
-#pragma unroll
                 for (int r = 0; r < RB; r++)
-                    gy2[r] = s2 ? mul2(dstag2(sF2 + r * L::WF, tid - H1 + 5, tid - H1 + 4), ihy) : f2(0.f);
+                    gy2[r] = s2 ? mul2(dstag2(F2 + r * L::WF, tid - H1 + 5, tid - H1 + 4), ihy) : f2(0.f);
             } else {
 #pragma unroll
                 for (int r = 0; r < RB; r++)
@@ -413,6 +424,7 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
         }
         sI = sI + RB >= QU ? sI + RB - QU : sI + RB;
         if constexpr (OT4) sJ = sJ + RB >= QLR ? sJ + RB - QLR : sJ + RB;
+        par ^= 1;
     }
     cp_async_wait<0>();
 }
