@@ -129,6 +129,70 @@ int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const float* rho
                           const float* src_xyz, const float* wavelets, int n_rec, const float* rec_xyz, float* traces,
                           void* stream);
 
+/* ---- Trace and field processing of the optimisation pipelines (device pointers, stream-ordered) ----
+ * Traces are [n, nt] float32 row-major (Traces.extended_data); fields are float32 row-major. */
+
+/* Cascaded second-order sections (scipy.signal.sosfilt, FP64 state), n_sections rows of
+ * (b0 b1 b2 a0 a1 a2) in host memory; adjoint runs on the time-reversed traces.
+ * Replaces the butterworth filters of stride/utils/filters.py:14-170 (zero_phase=False) as
+ * FilterTraces calls them (optimisation/pipelines/steps/filter_traces.py:57-96). in may equal out. */
+int sa_traces_sosfilt(const float* in, float* out, int n, int nt, const double* sos, int n_sections, int adjoint,
+                      void* stream);
+
+/* FIR filter out[t] = sum_k taps[k] in[t + k - center] (zero outside the trace), taps FP64 on the
+ * device; adjoint: the same on the time-reversed traces. With the cosine table of
+ * utils/filters.py:400-410 and center = 2 * period it is lowpass_filter_cos(zero_phase=False)
+ * (:413-465); with reversed firwin taps and center = ntaps - 1 it is the causal FIR filters
+ * (:213-397). out must not alias in. */
+int sa_traces_fir(const float* in, float* out, int n, int nt, const double* taps, int ntaps, int center,
+                  int adjoint, void* stream);
+
+/* Per-trace NaN/inf flags (flags [n] int on the device) and, with zero_bad, the flagged traces
+ * zeroed (CheckTraces, optimisation/pipelines/steps/check_traces.py:44-78). */
+int sa_traces_check(float* traces, int n, int nt, int* flags, int zero_bad, void* stream);
+
+/* out = in / (sqrt(sum of squares of the shot's traces / its trace count) + 1e-31) per shot, the
+ * shots given by device CSR trace offsets [n_shots + 1]; scratch: n_shots doubles on the device
+ * (NormPerShot, optimisation/pipelines/steps/norm_traces.py:43-69). in may equal out. */
+int sa_traces_norm_per_shot(const float* in, float* out, const int* offsets, int n_shots, int nt, double* scratch,
+                            void* stream);
+
+/* out = modelled * lowpass(observed != 0), the cosine lowpass centred (MuteTraces,
+ * optimisation/pipelines/steps/mute_traces.py:25-57); taps FP64 on the device, odd count. */
+int sa_traces_mute(const float* modelled, const float* observed, float* out, int n, int nt, const double* taps,
+                   int ntaps, void* stream);
+
+/* x *= m elementwise (MaskField's mask, optimisation/pipelines/steps/mask_field.py:52-70). */
+int sa_field_mul(float* x, const float* m, long long n, void* stream);
+
+/* Clip to [*lo, *hi] (either pointer NULL: no bound; Clip, steps/clip.py:25-36). */
+int sa_field_clip(float* x, long long n, const float* lo, const float* hi, void* stream);
+
+/* x += a * d elementwise (the update of optimisers/optimiser.py:273-298 without a transform). */
+int sa_field_axpy(float* x, const float* d, long long n, float a, void* stream);
+
+/* vp = 1 / (1 / vp - step * direction): the update in slowness, as the vp variable's transform
+ * makes it. */
+int sa_field_slowness_step(float* vp, const float* direction, long long n, float step, void* stream);
+
+/* out4[0..2] = min, max, max |x|; *sum_abs = sum |x| (FP64). Synchronises the stream. n >= 1.
+ * (NormField, steps/norm_field.py:24-52; apply_prec's sum, problem/data.py:437.) */
+int sa_field_stats(const float* x, long long n, float* out4, double* sum_abs, void* stream);
+
+/* x *= a (in FP64, rounded once). */
+int sa_field_scale(float* x, long long n, double a, void* stream);
+
+/* In-place Gaussian smoothing as scipy.ndimage.gaussian_filter (truncate 4, one pass per axis,
+ * FP32 between passes); shape[dim], sigma[dim] on the host; border 0 'nearest' (SmoothField,
+ * steps/smooth_field.py:27-47), 1 'reflect' (apply_prec, problem/data.py:432); scratch: a device
+ * array of the field's size. Synchronises the stream. */
+int sa_field_gaussian(float* x, int dim, const int* shape, const double* sigma, int border, float* scratch,
+                      void* stream);
+
+/* prec = prec * factor + 1 (FP64, rounded once) and grad *= 1 / prec (FP32) where prec != 0
+ * (Data.apply_prec, stride/problem/data.py:411-446, after its smoothing and factor). */
+int sa_field_apply_prec(float* grad, float* prec, long long n, double factor, void* stream);
+
 /* Copies the message of the last failed call on this thread (NUL-terminated, truncated to len). */
 int sa_last_error(char* buf, int len);
 

@@ -32,7 +32,10 @@ SA_GRAD_EXACT = 1
 
 # every symbol include/strideacc.h declares
 EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometry', 'sa_forward',
-           'sa_adjoint', 'sa_autotune', 'sa_last_error', 'sa_launch_count', 'sa_forward_2d_noalloc')
+           'sa_adjoint', 'sa_autotune', 'sa_last_error', 'sa_launch_count', 'sa_forward_2d_noalloc',
+           'sa_traces_sosfilt', 'sa_traces_fir', 'sa_traces_check', 'sa_traces_norm_per_shot', 'sa_traces_mute',
+           'sa_field_mul', 'sa_field_clip', 'sa_field_axpy', 'sa_field_slowness_step', 'sa_field_stats',
+           'sa_field_scale', 'sa_field_gaussian', 'sa_field_apply_prec')
 
 
 class SaDesc(ctypes.Structure):
@@ -72,6 +75,22 @@ def load():
     lib.sa_last_error.argtypes = [ctypes.c_char_p, I]
     lib.sa_launch_count.argtypes = [P]
     lib.sa_launch_count.restype = ctypes.c_longlong
+    L = ctypes.c_longlong
+    F = ctypes.c_float
+    D = ctypes.c_double
+    lib.sa_traces_sosfilt.argtypes = [P, P, I, I, P, I, I, P]
+    lib.sa_traces_fir.argtypes = [P, P, I, I, P, I, I, I, P]
+    lib.sa_traces_check.argtypes = [P, I, I, P, I, P]
+    lib.sa_traces_norm_per_shot.argtypes = [P, P, P, I, I, P, P]
+    lib.sa_traces_mute.argtypes = [P, P, P, I, I, P, I, P]
+    lib.sa_field_mul.argtypes = [P, P, L, P]
+    lib.sa_field_clip.argtypes = [P, L, P, P, P]
+    lib.sa_field_axpy.argtypes = [P, P, L, F, P]
+    lib.sa_field_slowness_step.argtypes = [P, P, L, F, P]
+    lib.sa_field_stats.argtypes = [P, L, P, P, P]
+    lib.sa_field_scale.argtypes = [P, L, D, P]
+    lib.sa_field_gaussian.argtypes = [P, I, P, P, I, P, P]
+    lib.sa_field_apply_prec.argtypes = [P, P, L, D, P]
     for name in EXPORTS:
         if name not in ('sa_launch_count',):
             getattr(lib, name).restype = I

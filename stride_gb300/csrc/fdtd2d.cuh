@@ -35,10 +35,11 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 __host__ __device__ constexpr int round4(int x) { return (x + 3) / 4 * 4; }
 
 // ---- arithmetic on the two lanes of a shot pair ---------------------------------------------
-// SA_PACKED=1 issues the sm_100-family f32x2 instructions; 0 issues two scalar FP32
-// instructions, which take immediate operands (the FD weights) without register pairs.
+// SA_PACKED=1 issues the sm_100-family f32x2 instructions (one instruction for both shots;
+// 4 % faster on the 64-shot gradient); 0 issues two scalar FP32 instructions, which take
+// immediate operands (the FD weights) without register pairs. Both round identically.
 #ifndef SA_PACKED
-#define SA_PACKED 0
+#define SA_PACKED 1
 #endif
 __device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
 #if SA_PACKED
