@@ -193,6 +193,14 @@ int sa_field_gaussian(float* x, int dim, const int* shape, const double* sigma, 
  * (Data.apply_prec, stride/problem/data.py:411-446, after its smoothing and factor). */
 int sa_field_apply_prec(float* grad, float* prec, long long n, double factor, void* stream);
 
+/* ---- Learned preconditioner (no counterpart in the reference) ----
+ * BF16 GEMM on the tcgen05 tensor cores: C[M][N] = (accumulate ? C : 0) + A[M][K] * B[N][K]^T
+ * (+ bias[N], then ReLU if relu), A and B bf16 with K contiguous (lda, ldb elements, multiples of
+ * 8, 16-byte aligned bases), C fp32 (ldc); Cb (optional, ldcb) receives C as bf16. M multiple of
+ * 128, K of 64, N of 32. *err (device int) is set to 1 if an internal wait timed out. */
+int sa_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb, int M, int N,
+                 int K, const float* bias, int relu, int accumulate, int* err, void* stream);
+
 /* Copies the message of the last failed call on this thread (NUL-terminated, truncated to len). */
 int sa_last_error(char* buf, int len);
 

@@ -35,7 +35,7 @@ EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometr
            'sa_adjoint', 'sa_autotune', 'sa_last_error', 'sa_launch_count', 'sa_forward_2d_noalloc',
            'sa_traces_sosfilt', 'sa_traces_fir', 'sa_traces_check', 'sa_traces_norm_per_shot', 'sa_traces_mute',
            'sa_field_mul', 'sa_field_clip', 'sa_field_axpy', 'sa_field_slowness_step', 'sa_field_stats',
-           'sa_field_scale', 'sa_field_gaussian', 'sa_field_apply_prec')
+           'sa_field_scale', 'sa_field_gaussian', 'sa_field_apply_prec', 'sa_gemm_bf16')
 
 
 class SaDesc(ctypes.Structure):
@@ -91,6 +91,7 @@ def load():
     lib.sa_field_scale.argtypes = [P, L, D, P]
     lib.sa_field_gaussian.argtypes = [P, I, P, P, I, P, P]
     lib.sa_field_apply_prec.argtypes = [P, P, L, D, P]
+    lib.sa_gemm_bf16.argtypes = [P, I, P, I, P, I, P, I, I, I, I, P, I, I, P, P]
     for name in EXPORTS:
         if name not in ('sa_launch_count',):
             getattr(lib, name).restype = I

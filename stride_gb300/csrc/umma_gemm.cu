@@ -1,0 +1,231 @@
+// BF16 GEMM on the 5th-generation tensor cores (tcgen05, accumulator in tensor memory) for the
+// learned preconditioner's convolutions:  C[M][N] (+)= A[M][K] * B[N][K]^T  (+ bias[N], ReLU),
+// A and B bf16 with K contiguous, C fp32 (optionally also written as bf16).
+//
+// One CTA of 128 threads computes a 128 x BN tile. K advances in 64-wide chunks staged in shared
+// memory (two stages, 16-byte cp.async) in the no-swizzle K-major canonical layout: 8-row x
+// 16-byte core matrices, the core matrices of one 8-wide k group stacked along M (stride 128 B),
+// k groups one after another (stride rows * 16 B). Thread 0 issues four kind::f16 MMAs (K = 16
+// each) per chunk into a TMEM accumulator of BN fp32 columns and commits them to the stage's
+// mbarrier, which releases the stage for the next load. The epilogue reads the accumulator with
+// tcgen05.ld (warp w owns TMEM lanes / tile rows 32w .. 32w+31).
+//
+// Every mbarrier wait is bounded: on timeout the kernel records it in *err, skips the remaining
+// MMAs and still waits (bounded) for the ones in flight before freeing its TMEM.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/strideacc.h"
+#include "helpers.h"
+
+namespace {
+
+constexpr int kBM = 128;
+constexpr int kBK = 64;
+constexpr long long kSpinLimit = 20000000;  // try_wait polls before giving up (far beyond any MMA chunk)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+}
+
+// tcgen05 shared-memory matrix descriptor: start >> 4 (bits 0-13), leading byte offset >> 4
+// (16-29), stride byte offset >> 4 (32-45), fixed 0b001 (46-48), no swizzle (61-63 = 0).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+
+// kind::f16 instruction descriptor: D f32 (bits 4-5 = 1), A and B bf16 (7-9 = 1, 10-12 = 1),
+// both K-major (15, 16 = 0), N >> 3 (17-22), M >> 4 (24-28).
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (long long i = 0; i < kSpinLimit; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <int BN>
+__global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restrict__ A, int lda,
+                                                   const __nv_bfloat16* __restrict__ B, int ldb, float* C, int ldc,
+                                                   __nv_bfloat16* Cb, int ldcb, int K, const float* __restrict__ bias,
+                                                   int relu, int accumulate, int* err) {
+    constexpr int A_BYTES = kBM * kBK * 2;  // 16 KB
+    constexpr int B_BYTES = BN * kBK * 2;
+    constexpr int STAGE = A_BYTES + B_BYTES;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ uint32_t tmem_base_sh;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
+    const uint32_t sbase = smem_u32(smem);
+    const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
+
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar1));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base_sh)),
+                     "r"(BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_base_sh;
+
+    // stage loader: A rows m (128) and B rows n (BN), k group g (8 per chunk), 16 bytes each
+    auto load = [&](int kb, int stage) {
+        const uint32_t sa = sbase + stage * STAGE, sb = sa + A_BYTES;
+        const int k0 = kb * kBK;
+        for (int c = tid; c < kBM * 8; c += 128) {
+            const int m = c >> 3, g = c & 7;
+            cp_async16(sa + g * (kBM * 16) + (m >> 3) * 128 + (m & 7) * 16, A + (long long)(m0 + m) * lda + k0 + g * 8);
+        }
+        for (int c = tid; c < BN * 8; c += 128) {
+            const int n = c >> 3, g = c & 7;
+            cp_async16(sb + g * (BN * 16) + (n >> 3) * 128 + (n & 7) * 16, B + (long long)(n0 + n) * ldb + k0 + g * 8);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+
+    const int nk = K / kBK;
+    constexpr uint32_t idesc = idesc_bf16(kBM, BN);
+    bool ok = true;
+    int issued[2] = {0, 0};  // commits made to each stage's barrier (thread 0)
+    load(0, 0);
+    for (int kb = 0; kb < nk && ok; kb++) {
+        const int st = kb & 1;
+        if (kb + 1 < nk) {
+            const int s1 = (kb + 1) & 1;
+            if (kb + 1 >= 2) {  // the MMAs of chunk kb-1 read stage s1: wait for their commit
+                if (!mbar_wait(s1 ? bar1 : bar0, (uint32_t)(((kb - 1) >> 1) & 1))) {
+                    ok = false;
+                }
+            }
+            if (ok) load(kb + 1, s1);
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        ok = __syncthreads_and(ok ? 1 : 0) != 0;
+        if (!ok) break;
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t sa = sbase + st * STAGE, sb = sa + A_BYTES;
+#pragma unroll
+            for (int j = 0; j < kBK / 16; j++) {  // two k groups per MMA
+                const uint64_t ad = smem_desc(sa + 2 * j * (kBM * 16), kBM * 16, 128);
+                const uint64_t bd = smem_desc(sb + 2 * j * (BN * 16), BN * 16, 128);
+                const uint32_t acc = (kb > 0 || j > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             st ? bar1 : bar0)
+                         : "memory");
+            issued[st]++;
+        }
+    }
+    // wait for every committed MMA (each barrier's last phase), bounded
+    bool done = true;
+    if (tid == 0) {
+        for (int s = 0; s < 2; s++)
+            if (issued[s] > 0 && !mbar_wait(s ? bar1 : bar0, (uint32_t)((issued[s] - 1) & 1))) done = false;
+    }
+    ok = __syncthreads_and((ok && (tid != 0 || done)) ? 1 : 0) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (ok) {
+        // epilogue: warp w reads lanes 32w..32w+31 (tile rows), 16 columns per load
+        const int m = m0 + warp * 32 + lane;
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            uint32_t r[16];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];\n"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            float* crow = C + (long long)m * ldc + n0 + c0;
+#pragma unroll
+            for (int q = 0; q < 16; q++) {
+                float v = __uint_as_float(r[q]);
+                if (accumulate) v += crow[q];
+                if (bias) v += bias[n0 + c0 + q];
+                if (relu) v = fmaxf(v, 0.f);
+                crow[q] = v;
+                if (Cb) Cb[(long long)m * ldcb + n0 + c0 + q] = __float2bfloat16_rn(v);
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN));
+}
+
+template <int BN>
+cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C, int ldc,
+                   __nv_bfloat16* Cb, int ldcb, int M, int N, int K, const float* bias, int relu, int accumulate,
+                   int* err, cudaStream_t s) {
+    const size_t bytes = 2 * (size_t)(kBM * kBK * 2 + BN * kBK * 2);
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_umma_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    const dim3 grid(M / kBM, N / BN);
+    k_umma_gemm<BN><<<grid, 128, bytes, s>>>(A, lda, B, ldb, C, ldc, Cb, ldcb, K, bias, relu, accumulate, err);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+extern "C" int sa_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb,
+                            int M, int N, int K, const float* bias, int relu, int accumulate, int* err, void* stream) {
+    if (!A || !B || !C || !err || M <= 0 || N <= 0 || K <= 0 || M % kBM || K % kBK || (N % 32))
+        return (sa::set_last_error("sa_gemm_bf16: M must be a multiple of 128, K of 64, N of 32"), SA_E_INVALID);
+    if (lda % 8 || ldb % 8 || lda < K || ldb < K || ldc < N || (Cb && ldcb < N) ||
+        ((uintptr_t)A & 15) || ((uintptr_t)B & 15))
+        return (sa::set_last_error("sa_gemm_bf16: leading dimensions and bases must allow 16-byte rows"),
+                SA_E_INVALID);
+    const auto* a = static_cast<const __nv_bfloat16*>(A);
+    const auto* b = static_cast<const __nv_bfloat16*>(B);
+    auto* cb = static_cast<__nv_bfloat16*>(Cb);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e;
+    if (N % 128 == 0)
+        e = launch<128>(a, lda, b, ldb, C, ldc, cb, ldcb, M, N, K, bias, relu, accumulate, err, s);
+    else if (N % 64 == 0)
+        e = launch<64>(a, lda, b, ldb, C, ldc, cb, ldcb, M, N, K, bias, relu, accumulate, err, s);
+    else
+        e = launch<32>(a, lda, b, ldb, C, ldc, cb, ldcb, M, N, K, bias, relu, accumulate, err, s);
+    if (e != cudaSuccess) return (sa::set_last_error(cudaGetErrorString(e)), SA_E_CUDA);
+    return SA_OK;
+}
