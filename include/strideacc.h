@@ -197,9 +197,45 @@ int sa_field_apply_prec(float* grad, float* prec, long long n, double factor, vo
  * BF16 GEMM on the tcgen05 tensor cores: C[M][N] = (accumulate ? C : 0) + A[M][K] * B[N][K]^T
  * (+ bias[N], then ReLU if relu), A and B bf16 with K contiguous (lda, ldb elements, multiples of
  * 8, 16-byte aligned bases), C fp32 (ldc); Cb (optional, ldcb) receives C as bf16. M multiple of
- * 128, K of 64, N of 32. *err (device int) is set to 1 if an internal wait timed out. */
+ * 128, K of 16, N of 32. ksplit > 1 splits K over that many CTAs per tile, which add their partial
+ * products into C atomically (accumulate only, no bias/ReLU/Cb). *err (device int) is set to 1 if
+ * an internal wait timed out. */
 int sa_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb, int M, int N,
-                 int K, const float* bias, int relu, int accumulate, int* err, void* stream);
+                 int K, const float* bias, int relu, int accumulate, int ksplit, int* err, void* stream);
+
+/* U-Net layer kernels (NHWC fp32 activations [pixels][channels] with channel stride ld; bf16 GEMM
+ * operands; B images of H x W). No counterpart in the reference. */
+/* col bf16 [B*H*W][Kp]: column (ky*3+kx)*Cin+ci of pixel p = x at the 3x3 neighbour (zero outside
+ * the image and for columns >= 9*Cin). */
+int sa_nn_im2col(const float* x, int ldx, int B, int H, int W, int Cin, void* col, int Kp, void* stream);
+/* dx (= or +=) the gather of dcol fp32 [B*H*W][Kp] back to the pixels its columns read. */
+int sa_nn_col2im(const float* dcol, int Kp, int B, int H, int W, int Cin, float* dx, int ldx, int accumulate,
+                 void* stream);
+/* out[c][r] = in[r][c] (bf16), r < R, c < C; output rows C..Cp-1 are zero. */
+int sa_nn_transpose_bf16(const void* in, int ldi, int R, int C, void* out, int ldo, int Cp, void* stream);
+int sa_nn_to_bf16(const float* x, int ldx, long long rows, int C, void* y, int ldy, void* stream);
+/* dy = 0 where y <= 0 (ReLU backward from the activation output). */
+int sa_nn_relu_bwd(float* dy, int ldd, const float* y, int ldy, long long rows, int C, void* stream);
+/* db[c] = sum over rows of dy[r][c]. */
+int sa_nn_bias_grad(const float* dy, int ldd, long long rows, int C, float* db, void* stream);
+/* 2x2 max pooling (H, W of the input, even) and its backward (gradient to the first maximum). */
+int sa_nn_maxpool(const float* x, int ldx, int B, int H, int W, int C, float* y, int ldy, void* stream);
+int sa_nn_maxpool_bwd(const float* x, int ldx, const float* dy, int ldd, int B, int H, int W, int C, float* dx,
+                      int lddx, int accumulate, void* stream);
+/* Nearest x2 upsampling (H, W of the output, even) and its backward (sum of the 4 children). */
+int sa_nn_upsample(const float* x, int ldx, int B, int H, int W, int C, float* y, int ldy, void* stream);
+int sa_nn_upsample_bwd(const float* dy, int ldd, int B, int H, int W, int C, float* dx, int lddx, void* stream);
+/* dst[r][c] (= or +=) src[r][c], c < C (channel concatenation and split). */
+int sa_nn_copy_channels(const float* src, int lds, long long rows, int C, float* dst, int ldd, int accumulate,
+                        void* stream);
+/* fp32 weights [Cout][Kr] -> bf16 [Coutp][Kp] (GEMM B operand) and its transpose [Kp][Coutp]. */
+int sa_nn_pack_weights(const float* w, int Cout, int Kr, void* wb, void* wt, int Coutp, int Kp, void* stream);
+/* Adam step (bias-corrected, step >= 1) on fp32 master weights. */
+int sa_nn_adam(float* w, const float* g, float* m, float* v, long long n, float lr, float b1, float b2, float eps,
+               int step, void* stream);
+/* *loss = mean (out - target)^2 (FP64, device), dout = 2 (out - target) / n. */
+int sa_nn_mse(const float* out, int ldo, const float* target, long long n, float* dout, int ldd, double* loss,
+              void* stream);
 
 /* Copies the message of the last failed call on this thread (NUL-terminated, truncated to len). */
 int sa_last_error(char* buf, int len);

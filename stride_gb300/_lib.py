@@ -35,7 +35,10 @@ EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometr
            'sa_adjoint', 'sa_autotune', 'sa_last_error', 'sa_launch_count', 'sa_forward_2d_noalloc',
            'sa_traces_sosfilt', 'sa_traces_fir', 'sa_traces_check', 'sa_traces_norm_per_shot', 'sa_traces_mute',
            'sa_field_mul', 'sa_field_clip', 'sa_field_axpy', 'sa_field_slowness_step', 'sa_field_stats',
-           'sa_field_scale', 'sa_field_gaussian', 'sa_field_apply_prec', 'sa_gemm_bf16')
+           'sa_field_scale', 'sa_field_gaussian', 'sa_field_apply_prec', 'sa_gemm_bf16', 'sa_nn_im2col',
+           'sa_nn_col2im', 'sa_nn_transpose_bf16', 'sa_nn_to_bf16', 'sa_nn_relu_bwd', 'sa_nn_bias_grad',
+           'sa_nn_maxpool', 'sa_nn_maxpool_bwd', 'sa_nn_upsample', 'sa_nn_upsample_bwd', 'sa_nn_copy_channels',
+           'sa_nn_pack_weights', 'sa_nn_adam', 'sa_nn_mse')
 
 
 class SaDesc(ctypes.Structure):
@@ -91,7 +94,21 @@ def load():
     lib.sa_field_scale.argtypes = [P, L, D, P]
     lib.sa_field_gaussian.argtypes = [P, I, P, P, I, P, P]
     lib.sa_field_apply_prec.argtypes = [P, P, L, D, P]
-    lib.sa_gemm_bf16.argtypes = [P, I, P, I, P, I, P, I, I, I, I, P, I, I, P, P]
+    lib.sa_gemm_bf16.argtypes = [P, I, P, I, P, I, P, I, I, I, I, P, I, I, I, P, P]
+    lib.sa_nn_im2col.argtypes = [P, I, I, I, I, I, P, I, P]
+    lib.sa_nn_col2im.argtypes = [P, I, I, I, I, I, P, I, I, P]
+    lib.sa_nn_transpose_bf16.argtypes = [P, I, I, I, P, I, I, P]
+    lib.sa_nn_to_bf16.argtypes = [P, I, L, I, P, I, P]
+    lib.sa_nn_relu_bwd.argtypes = [P, I, P, I, L, I, P]
+    lib.sa_nn_bias_grad.argtypes = [P, I, L, I, P, P]
+    lib.sa_nn_maxpool.argtypes = [P, I, I, I, I, I, P, I, P]
+    lib.sa_nn_maxpool_bwd.argtypes = [P, I, P, I, I, I, I, I, P, I, I, P]
+    lib.sa_nn_upsample.argtypes = [P, I, I, I, I, I, P, I, P]
+    lib.sa_nn_upsample_bwd.argtypes = [P, I, I, I, I, I, P, I, P]
+    lib.sa_nn_copy_channels.argtypes = [P, I, L, I, P, I, I, P]
+    lib.sa_nn_pack_weights.argtypes = [P, I, I, P, P, I, I, P]
+    lib.sa_nn_adam.argtypes = [P, P, P, P, L, F, F, F, F, I, P]
+    lib.sa_nn_mse.argtypes = [P, I, P, L, P, I, P, P]
     for name in EXPORTS:
         if name not in ('sa_launch_count',):
             getattr(lib, name).restype = I

@@ -23,7 +23,7 @@
 namespace {
 
 constexpr int kBM = 128;
-constexpr int kBK = 64;
+constexpr int kBK = 64;  // k columns per staged chunk
 constexpr long long kSpinLimit = 20000000;  // try_wait polls before giving up (far beyond any MMA chunk)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -62,7 +62,7 @@ template <int BN>
 __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restrict__ A, int lda,
                                                    const __nv_bfloat16* __restrict__ B, int ldb, float* C, int ldc,
                                                    __nv_bfloat16* Cb, int ldcb, int K, const float* __restrict__ bias,
-                                                   int relu, int accumulate, int* err) {
+                                                   int relu, int accumulate, int chunks_per_split, int* err) {
     constexpr int A_BYTES = kBM * kBK * 2;  // 16 KB
     constexpr int B_BYTES = BN * kBK * 2;
     constexpr int STAGE = A_BYTES + B_BYTES;
@@ -91,31 +91,42 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
     const uint32_t tmem = tmem_base_sh;
 
     // stage loader: A rows m (128) and B rows n (BN), k group g (8 per chunk), 16 bytes each
+    // (the last chunk may be shorter: K is a multiple of 16, a chunk holds K - k0 <= 64 columns)
     auto load = [&](int kb, int stage) {
         const uint32_t sa = sbase + stage * STAGE, sb = sa + A_BYTES;
         const int k0 = kb * kBK;
+        const int ng = min(kBK, K - k0) >> 3;  // k groups of 8 in this chunk
         for (int c = tid; c < kBM * 8; c += 128) {
             const int m = c >> 3, g = c & 7;
-            cp_async16(sa + g * (kBM * 16) + (m >> 3) * 128 + (m & 7) * 16, A + (long long)(m0 + m) * lda + k0 + g * 8);
+            if (g < ng)
+                cp_async16(sa + g * (kBM * 16) + (m >> 3) * 128 + (m & 7) * 16,
+                           A + (long long)(m0 + m) * lda + k0 + g * 8);
         }
         for (int c = tid; c < BN * 8; c += 128) {
             const int n = c >> 3, g = c & 7;
-            cp_async16(sb + g * (BN * 16) + (n >> 3) * 128 + (n & 7) * 16, B + (long long)(n0 + n) * ldb + k0 + g * 8);
+            if (g < ng)
+                cp_async16(sb + g * (BN * 16) + (n >> 3) * 128 + (n & 7) * 16,
+                           B + (long long)(n0 + n) * ldb + k0 + g * 8);
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     };
 
-    const int nk = K / kBK;
+    // split K (gridDim.z > 1): this CTA takes chunks [kb0, kb1) and adds its partial tile to C
+    const int nk_all = (K + kBK - 1) / kBK;
+    const int kb0 = blockIdx.z * chunks_per_split, kb1 = min(nk_all, kb0 + chunks_per_split);
+    const int nk = max(0, kb1 - kb0);
+    const bool split = gridDim.z > 1;
     constexpr uint32_t idesc = idesc_bf16(kBM, BN);
     bool ok = true;
     int issued[2] = {0, 0};  // commits made to each stage's barrier (thread 0)
-    load(0, 0);
-    for (int kb = 0; kb < nk && ok; kb++) {
-        const int st = kb & 1;
-        if (kb + 1 < nk) {
-            const int s1 = (kb + 1) & 1;
-            if (kb + 1 >= 2) {  // the MMAs of chunk kb-1 read stage s1: wait for their commit
-                if (!mbar_wait(s1 ? bar1 : bar0, (uint32_t)(((kb - 1) >> 1) & 1))) {
+    if (nk > 0) load(kb0, 0);
+    for (int i = 0; i < nk && ok; i++) {
+        const int kb = kb0 + i;
+        const int st = i & 1;
+        if (i + 1 < nk) {
+            const int s1 = (i + 1) & 1;
+            if (i + 1 >= 2) {  // the MMAs of chunk i-1 read stage s1: wait for their commit
+                if (!mbar_wait(s1 ? bar1 : bar0, (uint32_t)(((i - 1) >> 1) & 1))) {
                     ok = false;
                 }
             }
@@ -131,11 +142,13 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const uint32_t sa = sbase + st * STAGE, sb = sa + A_BYTES;
+            const int nmma = min(kBK, K - kb * kBK) >> 4;
 #pragma unroll
             for (int j = 0; j < kBK / 16; j++) {  // two k groups per MMA
+                if (j >= nmma) break;
                 const uint64_t ad = smem_desc(sa + 2 * j * (kBM * 16), kBM * 16, 128);
                 const uint64_t bd = smem_desc(sb + 2 * j * (BN * 16), BN * 16, 128);
-                const uint32_t acc = (kb > 0 || j > 0) ? 1u : 0u;
+                const uint32_t acc = (i > 0 || j > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
@@ -155,7 +168,7 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
     }
     ok = __syncthreads_and((ok && (tid != 0 || done)) ? 1 : 0) != 0;
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (ok) {
+    if (ok && nk > 0) {
         // epilogue: warp w reads lanes 32w..32w+31 (tile rows), 16 columns per load
         const int m = m0 + warp * 32 + lane;
 #pragma unroll 1
@@ -171,6 +184,11 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
             float* crow = C + (long long)m * ldc + n0 + c0;
+            if (split) {
+#pragma unroll
+                for (int q = 0; q < 16; q++) atomicAdd(crow + q, __uint_as_float(r[q]));
+                continue;
+            }
 #pragma unroll
             for (int q = 0; q < 16; q++) {
                 float v = __uint_as_float(r[q]);
@@ -181,7 +199,7 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
                 if (Cb) Cb[(long long)m * ldcb + n0 + c0 + q] = __float2bfloat16_rn(v);
             }
         }
-    } else if (tid == 0) {
+    } else if (!ok && tid == 0) {
         atomicExch(err, 1);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -192,7 +210,7 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
 template <int BN>
 cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C, int ldc,
                    __nv_bfloat16* Cb, int ldcb, int M, int N, int K, const float* bias, int relu, int accumulate,
-                   int* err, cudaStream_t s) {
+                   int ksplit, int* err, cudaStream_t s) {
     const size_t bytes = 2 * (size_t)(kBM * kBK * 2 + BN * kBK * 2);
     static bool configured = false;
     if (!configured) {
@@ -200,17 +218,23 @@ cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int 
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    const dim3 grid(M / kBM, N / BN);
-    k_umma_gemm<BN><<<grid, 128, bytes, s>>>(A, lda, B, ldb, C, ldc, Cb, ldcb, K, bias, relu, accumulate, err);
+    const int nk = (K + kBK - 1) / kBK;
+    const int per = (nk + ksplit - 1) / ksplit;
+    const dim3 grid(M / kBM, N / BN, (nk + per - 1) / per);
+    k_umma_gemm<BN><<<grid, 128, bytes, s>>>(A, lda, B, ldb, C, ldc, Cb, ldcb, K, bias, relu, accumulate, per, err);
     return cudaGetLastError();
 }
 
 }  // namespace
 
 extern "C" int sa_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb,
-                            int M, int N, int K, const float* bias, int relu, int accumulate, int* err, void* stream) {
-    if (!A || !B || !C || !err || M <= 0 || N <= 0 || K <= 0 || M % kBM || K % kBK || (N % 32))
-        return (sa::set_last_error("sa_gemm_bf16: M must be a multiple of 128, K of 64, N of 32"), SA_E_INVALID);
+                            int M, int N, int K, const float* bias, int relu, int accumulate, int ksplit, int* err,
+                            void* stream) {
+    if (ksplit < 1 || (ksplit > 1 && (bias || relu || Cb || !accumulate)))
+        return (sa::set_last_error("sa_gemm_bf16: split K adds plain partial products into C (accumulate only)"),
+                SA_E_INVALID);
+    if (!A || !B || !C || !err || M <= 0 || N <= 0 || K <= 0 || M % kBM || K % 16 || (N % 32))
+        return (sa::set_last_error("sa_gemm_bf16: M must be a multiple of 128, K of 16, N of 32"), SA_E_INVALID);
     if (lda % 8 || ldb % 8 || lda < K || ldb < K || ldc < N || (Cb && ldcb < N) ||
         ((uintptr_t)A & 15) || ((uintptr_t)B & 15))
         return (sa::set_last_error("sa_gemm_bf16: leading dimensions and bases must allow 16-byte rows"),
@@ -221,11 +245,11 @@ extern "C" int sa_gemm_bf16(const void* A, int lda, const void* B, int ldb, floa
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e;
     if (N % 128 == 0)
-        e = launch<128>(a, lda, b, ldb, C, ldc, cb, ldcb, M, N, K, bias, relu, accumulate, err, s);
+        e = launch<128>(a, lda, b, ldb, C, ldc, cb, ldcb, M, N, K, bias, relu, accumulate, ksplit, err, s);
     else if (N % 64 == 0)
-        e = launch<64>(a, lda, b, ldb, C, ldc, cb, ldcb, M, N, K, bias, relu, accumulate, err, s);
+        e = launch<64>(a, lda, b, ldb, C, ldc, cb, ldcb, M, N, K, bias, relu, accumulate, ksplit, err, s);
     else
-        e = launch<32>(a, lda, b, ldb, C, ldc, cb, ldcb, M, N, K, bias, relu, accumulate, err, s);
+        e = launch<32>(a, lda, b, ldb, C, ldc, cb, ldcb, M, N, K, bias, relu, accumulate, ksplit, err, s);
     if (e != cudaSuccess) return (sa::set_last_error(cudaGetErrorString(e)), SA_E_CUDA);
     return SA_OK;
 }

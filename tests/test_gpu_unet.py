@@ -11,21 +11,22 @@ from stride_gb300 import _lib  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 
-def _gemm(A, B, C=None, bias=None, relu=False, accumulate=False, want_bf16=False):
+def _gemm(A, B, C=None, bias=None, relu=False, accumulate=False, want_bf16=False, ksplit=1):
     M, K = A.shape
     N = B.shape[0]
     C = torch.zeros((M, N), device='cuda') if C is None else C
     Cb = torch.zeros((M, N), dtype=torch.bfloat16, device='cuda') if want_bf16 else None
     err = torch.zeros(1, dtype=torch.int32, device='cuda')
     _lib.check(_lib.load().sa_gemm_bf16(_lib._ptr(A), A.stride(0), _lib._ptr(B), B.stride(0), _lib._ptr(C), C.stride(0),
-                                        _lib._ptr(Cb), N, M, N, K, _lib._ptr(bias), int(relu), int(accumulate),
+                                        _lib._ptr(Cb), N, M, N, K, _lib._ptr(bias), int(relu), int(accumulate), ksplit,
                                         _lib._ptr(err), _lib._stream(torch.cuda.current_stream())))
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     return C, Cb
 
 
-@pytest.mark.parametrize('M,N,K', [(128, 32, 64), (256, 64, 128), (384, 128, 192), (128, 256, 64), (256, 96, 320)])
+@pytest.mark.parametrize("M,N,K", [(128, 32, 64), (256, 64, 128), (384, 128, 192), (128, 256, 64), (256, 96, 320),
+                                   (128, 64, 32), (256, 32, 80), (128, 128, 288)])
 def test_gemm_bf16(M, N, K):
     g = torch.Generator(device='cpu').manual_seed(M + N + K)
     A = torch.randn((M, K), generator=g).to(torch.bfloat16).cuda()
@@ -47,3 +48,98 @@ def test_gemm_epilogue():
     ref = torch.relu(C0.double() + A.double() @ B.double().T + bias.double())
     assert float((C.double() - ref).norm() / ref.norm()) <= 1e-5
     assert torch.equal(Cb, C.to(torch.bfloat16))
+
+
+def test_gemm_split_k():
+    g = torch.Generator(device='cpu').manual_seed(3)
+    M, N, K = 128, 64, 64 * 37 + 32
+    A = torch.randn((M, K), generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn((N, K), generator=g).to(torch.bfloat16).cuda()
+    C0 = torch.randn((M, N), generator=g).cuda()
+    C, _ = _gemm(A, B, C=C0.clone(), accumulate=True, ksplit=5)
+    ref = C0.double() + A.double() @ B.double().T
+    assert float((C.double() - ref).norm() / ref.norm()) <= 1e-5
+
+
+def _reference_net(net, x, target):
+    """The same U-Net in float64 PyTorch on the CPU (weights as the BF16 the GEMMs use)."""
+    F = torch.nn.functional
+
+    def conv(layer, a):
+        w = layer.w.detach().cpu().to(torch.bfloat16).double()
+        k = layer.k
+        w = w.reshape(layer.cout, k, k, layer.cin).permute(0, 3, 1, 2).contiguous().requires_grad_(True)
+        b = layer.b.detach().cpu()[:layer.cout].double().requires_grad_(True)
+        y = F.conv2d(a, w, b, padding=k // 2)
+        return (F.relu(y) if layer.relu else y), w, b
+
+    params = []
+    a = x.permute(0, 3, 1, 2).double()
+    skips = []
+    for l in range(net.levels):
+        for layer in net.enc[l]:
+            a, w, b = conv(layer, a)
+            params.append((layer, w, b))
+        if l < net.levels - 1:
+            skips.append(a)
+            a = F.max_pool2d(a, 2)
+    for l in reversed(range(net.levels - 1)):
+        u = F.interpolate(a, scale_factor=2, mode='nearest')
+        u, w, b = conv(net.up[l], u)
+        params.append((net.up[l], w, b))
+        a = torch.cat([u, skips[l]], dim=1)
+        for layer in net.dec[l]:
+            a, w, b = conv(layer, a)
+            params.append((layer, w, b))
+    out, w, b = conv(net.out, a)
+    params.append((net.out, w, b))
+    loss = ((out[:, 0] - target.double()) ** 2).mean()
+    loss.backward()
+    return out[:, 0].detach(), loss.item(), params
+
+
+def test_unet_forward_backward_against_torch():
+    """Output and loss within 2 % and every layer's weight and bias gradient with cosine >= 0.99
+    against an FP64 reference: the GEMM operands (activations, weights, back-propagated
+    gradients) are BF16, whose rounding accumulates over the 23 layers of the backward pass."""
+    from stride_gb300.unet import UNet
+    torch.manual_seed(0)
+    B, H, W = 2, 64, 64
+    net = UNet(seed=1)
+    x = torch.randn(B, H, W, 2)
+    target = torch.randn(B, H, W)
+    y = net.forward(x.cuda())
+    loss, d = net.mse(y, target.cuda())
+    net.backward(d)
+    torch.cuda.synchronize()
+    assert net.errors() == 0
+    out = net.output(y, B, H, W)[..., 0].cpu().double()
+    ref_out, ref_loss, params = _reference_net(net, x, target)
+    assert float((out - ref_out).norm() / ref_out.norm()) <= 2e-2
+    assert abs(float(loss.item()) - ref_loss) <= 2e-2 * ref_loss
+    for layer, w, b in params:
+        g = layer.gw.cpu().double().reshape(layer.cout, layer.k, layer.k, layer.cin).permute(0, 3, 1, 2)
+        cos = float((g * w.grad).sum() / (g.norm() * w.grad.norm() + 1e-30))
+        assert cos >= 0.99, (layer.cin, layer.cout, cos)
+        gb = layer.gb.cpu().double()[:layer.cout]
+        cosb = float((gb * b.grad).sum() / (gb.norm() * b.grad.norm() + 1e-30))
+        assert cosb >= 0.99, (layer.cin, layer.cout, cosb)
+
+
+def test_unet_training_reduces_loss():
+    from stride_gb300.unet import UNet
+    torch.manual_seed(1)
+    B, H, W = 4, 64, 64
+    net = UNet(seed=2)
+    x = torch.randn(B, H, W, 2, device='cuda')
+    yy, xx = torch.meshgrid(torch.linspace(-1, 1, H), torch.linspace(-1, 1, W), indexing='ij')
+    target = (x[..., 0] * 0.5 + torch.exp(-(yy ** 2 + xx ** 2) * 4).cuda()).contiguous()
+    losses = []
+    for _ in range(60):
+        y = net.forward(x)
+        loss, d = net.mse(y, target)
+        net.backward(d)
+        net.adam_step(lr=1e-3)
+        losses.append(float(loss.item()))
+    assert net.errors() == 0
+    assert losses[-1] < 0.3 * losses[0], losses[::10]
