@@ -51,6 +51,7 @@ WORKLOADS = {
     '3dgrad': ('3d', 1, 'fwdadj'),          # 3D fwd+adj vp gradient of one shot (snapshots in HBM)
     'exact64': ('batched', 64, 'fwdadj'),   # exact gradient (autograd backward), checkpoints every 50 steps
     '3dgrad8': ('3d', 8, 'fwdadj'),         # 3D gradient of 8 shots, checkpoints under a 150 GB budget
+    'fwi': ('single', 32, 'fwi'),           # plain vs learned-preconditioned FWI, wall time to a vp error
 }
 # gradient method per workload: the reference imaging condition from snapshots (default), the
 # same from checkpoints with recompute, or the exact discrete adjoint from checkpoints
@@ -74,6 +75,9 @@ WORKLOAD_NAMES = {
                'recompute',
     '3dgrad8': '3D fwd+adj vp gradient: 296^3 extended, vp/rho/alpha phantom, 8 shots per launch x 512 receivers, '
                '3000 steps, OT4, f=4, checkpoints under a 150 GB budget with recompute',
+    'fwi': 'FWI of seeded 256^2 ellipse phantoms at 0.5 mm (296^2 extended), 32 shots x 128 receivers, 2000 steps, '
+           '500 kHz, f_max 0.5 MHz: plain (reference loop, GPU pipelines) vs U-Net-preconditioned (BF16 tcgen05, '
+           'trained on plain-FWI paths of held-out seeds), wall time to the target relative vp error',
 }
 
 
@@ -227,7 +231,71 @@ def _points(w, workload):
     return pts
 
 
-METRIC = {'fwdadj': 'GPts/s (forward+adjoint vp gradient)', 'fwd': 'GPts/s (forward)'}
+METRIC = {'fwdadj': 'GPts/s (forward+adjoint vp gradient)', 'fwd': 'GPts/s (forward)',
+          'fwi': 'seconds to the target relative vp error (learned-preconditioned FWI, median over test phantoms)'}
+
+
+def _fwi_workload(seed):
+    from stride_gb300 import phantoms
+    w = phantoms.workload('single', seed=seed)
+    shots = list(range(0, 128, 4))
+    w['shots'] = shots
+    w['src'] = [w['geometry'][[s]] for s in shots]
+    w['rec'] = [w['geometry'] for _ in shots]
+    return w
+
+
+def fwi_arm(args):
+    """Plain vs learned FWI on one GPU: training pairs from plain-FWI paths of training seeds, U-Net
+    training, then wall time to the target error on test seeds (both methods, same GPU)."""
+    import torch
+    from stride_gb300.fwi import LearnedFWI, PlainFWI, generate_pairs, run_to_error, train_unet
+    from stride_gb300.unet import UNet
+    torch.cuda.set_device(0)
+    step, target, fmax = args.fwi_step, args.fwi_target, 0.5e6
+    w0 = _fwi_workload(1000)
+    t0 = time.perf_counter()
+    plain = PlainFWI(w0, step_size=step)
+    X, T = generate_pairs(plain, [_fwi_workload(1000 + i)['vp'] for i in range(args.fwi_train)], iterations=5,
+                          f_max=fmax)
+    torch.cuda.synchronize()
+    t_pairs = time.perf_counter() - t0
+    net = UNet(seed=0)
+    t0 = time.perf_counter()
+    losses = train_unet(net, X, T, epochs=args.fwi_epochs, batch=4, lr=1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    learned = LearnedFWI(w0, net, step_size=step)
+    rows = []
+    for seed in range(args.fwi_test):
+        vt = _fwi_workload(seed)['vp']
+        tp, ip, ep = run_to_error(plain, vt, target, max_iter=args.fwi_iters, f_max=fmax)
+        tl, il, el = run_to_error(learned, vt, target, max_iter=args.fwi_iters, f_max=fmax)
+        rows.append({'seed': seed, 'initial_error': ep[0], 'plain_s': tp, 'plain_iters': ip, 'plain_final': ep[-1],
+                     'learned_s': tl, 'learned_iters': il, 'learned_final': el[-1],
+                     'learned_steps_accepted': sum(h.get('learned', False) for h in learned.history)})
+
+    def med(key):
+        v = [r[key] if r[key] is not None else float('inf') for r in rows]
+        return float(statistics.median(v))
+
+    line = {
+        'metric': METRIC['fwi'], 'value': med('learned_s'), 'unit': 's', 'n_gpus': 1, 'steps': len(rows),
+        'warmup': 0, 'ms_per_step': None, 'higher_is_better': False, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32 solver, bf16 network', 'data': 'synthetic (seeded ellipse phantoms)',
+        'config': {'workload': WORKLOAD_NAMES['fwi'], 'target_error': target, 'step_size': step,
+                   'train_phantoms': args.fwi_train, 'pairs': int(X.shape[0]), 'epochs': args.fwi_epochs,
+                   'test_phantoms': args.fwi_test, 'max_iterations': args.fwi_iters},
+        'plain_median_s': med('plain_s'), 'learned_median_s': med('learned_s'),
+        'plain_reached': sum(r['plain_s'] is not None for r in rows),
+        'learned_reached': sum(r['learned_s'] is not None for r in rows),
+        'pair_generation_s': t_pairs, 'training_s': t_train, 'training_loss': [losses[0], losses[-1]],
+        'gemm_timeouts': net.errors(), 'per_phantom': rows,
+    }
+    print(json.dumps(line))
+    plain.close()
+    learned.close()
+    return 0
 
 
 def reference_arm(args):
@@ -455,7 +523,19 @@ def main():
     ap.add_argument('--cpu-seconds', type=float, default=15.0)
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--fwi-train', type=int, default=48, help='training phantoms (fwi workload)')
+    ap.add_argument('--fwi-epochs', type=int, default=15)
+    ap.add_argument('--fwi-test', type=int, default=4, help='test phantoms (fwi workload)')
+    ap.add_argument('--fwi-step', type=float, default=2.0)
+    ap.add_argument('--fwi-target', type=float, default=0.01)
+    ap.add_argument('--fwi-iters', type=int, default=25)
     args = ap.parse_args()
+    if args.workload == 'fwi':
+        if args.impl == 'reference':
+            print(json.dumps({'impl': 'reference', 'unavailable': 'the fwi workload compares two GPU methods; its '
+                              'solver throughput against the CPU port is the fwdadj/single workloads\' line'}))
+            return 0
+        return fwi_arm(args)
     if args.impl == 'reference':
         return reference_arm(args)
     return gb300_arm(args)

@@ -228,9 +228,24 @@ struct HostInject {
     int lane;
 };
 
-// Builds the per-CTA source/receiver lists for the current layout.
+// Builds the per-CTA source/receiver lists for the current layout. The captured graphs hold the
+// list pointers (not their contents): they are dropped only when a list moves.
+int build_lists_impl(sa_plan* p);
 int build_lists(sa_plan* p) {
-    drop_graphs(p);
+    const void* before[] = {p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
+                            p->inj_recx, p->inj_recx_off, p->src_flat};
+    const int rc = build_lists_impl(p);
+    const void* after[] = {p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
+                           p->inj_recx, p->inj_recx_off, p->src_flat};
+    for (size_t k = 0; k < sizeof(before) / sizeof(before[0]); k++)
+        if (before[k] != after[k]) {
+            drop_graphs(p);
+            break;
+        }
+    return rc;
+}
+
+int build_lists_impl(sa_plan* p) {
     const int nc = p->nchunks, ns = p->nstrips;
     const int ncta = npairs(p) * nc * ns;
     const double h = std::max(p->d.spacing[0], p->d.spacing[1]);
@@ -894,6 +909,7 @@ int sa_set_geometry(sa_plan* p, int n_shots, const int* src_offsets, const float
     p->n_rec = nr;
     p->src_off.assign(src_offsets, src_offsets + n_shots + 1);
     p->rec_off.assign(rec_offsets, rec_offsets + n_shots + 1);
+    drop_graphs(p);  // shot count, point counts and layout are baked into the captured loops
     default_layout(p);
     CKR(build_lists(p));
     CKR(ensure(&p->src_amp, &p->cap_src_amp, (size_t)p->d.nt * ns));
@@ -1040,6 +1056,7 @@ int sa_autotune(sa_plan* p, void* stream) {
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     p->layout_fixed = true;
+    drop_graphs(p);  // the launch shape is baked into the captured loops
     for (const Cand& c : cands) {
         set_strips(p, c.nt);
         p->chunk_rows = (p->nx + c.nchunks - 1) / c.nchunks;

@@ -25,7 +25,7 @@ from . import _lib
 from .pipelines import (CheckTraces, Clip, FilterTraces, GradientDescent, MaskField, MuteTraces, NormField,
                         NormPerShot, SmoothField, apply_prec)
 
-__all__ = ['PlainFWI', 'relative_error']
+__all__ = ['PlainFWI', 'LearnedFWI', 'relative_error', 'features', 'generate_pairs', 'train_unet', 'run_to_error']
 
 
 def relative_error(vp, vp_true, inner):
@@ -93,21 +93,38 @@ class PlainFWI:
         self.optimiser = GradientDescent(step_size=step_size, slowness=True)
         self.history = []
 
+    def reset(self, vp_true, vp0=1500.):
+        """A new true model on the same grid and acquisition: observed data recomputed, vp restarted."""
+        self.vp_true = torch.as_tensor(np.ascontiguousarray(vp_true, np.float32), device=self.device)
+        self.plan.set_medium(self.vp_true, self.rho, self.alpha)
+        self.plan.forward((self.wavelets * self.win[None]).contiguous(), self.observed)
+        self.vp.fill_(float(vp0))
+        self.history = []
+
     def close(self):
         self.plan.close()
 
     def error(self):
         return relative_error(self.vp, self.vp_true, self.inner)
 
-    def gradient(self, f_max=None):
-        """Misfit, and the raw slowness gradient and preconditioner of the current model."""
+    def _modelled(self, vp, f_max, save):
         dt = self.dt
         filt = FilterTraces(f_max=f_max)
         wav = filt.forward(self.check.forward(self.wavelets), dt=dt) if f_max else self.wavelets
         obs = filt.forward(self.check.forward(self.observed), dt=dt) if f_max else self.observed
-        self.plan.set_medium(self.vp, self.rho, self.alpha)
+        self.plan.set_medium(vp, self.rho, self.alpha)
         modelled = torch.zeros_like(self.observed)
-        self.plan.forward((wav * self.win[None]).contiguous(), modelled, save=True)
+        self.plan.forward((wav * self.win[None]).contiguous(), modelled, save=save)
+        return modelled, obs
+
+    def misfit(self, vp, f_max=None):
+        """Misfit of a model (forward only, the same trace processing as the gradient)."""
+        modelled, obs = self._modelled(vp, f_max, False)
+        res, _ = self._residual(modelled, obs, f_max)
+        return 0.5 * float((res.double() ** 2).sum())
+
+    def _residual(self, modelled, obs, f_max):
+        dt = self.dt
         mod = self.check.forward(modelled)
         if self.mute is not None:
             mod, _ = self.mute.forward(mod, obs, dt)
@@ -118,7 +135,13 @@ class PlainFWI:
         if self.norm is not None:
             mod = self.norm.forward(mod, offsets=self.rec_offsets)
             obs = self.norm.forward(obs, offsets=self.rec_offsets)
-        res = mod - obs
+        return mod - obs, tfilt
+
+    def gradient(self, f_max=None):
+        """Misfit, and the raw slowness gradient and preconditioner of the current model."""
+        dt = self.dt
+        modelled, obs = self._modelled(self.vp, f_max, True)
+        res, tfilt = self._residual(modelled, obs, f_max)
         misfit = 0.5 * float((res.double() ** 2).sum())
         # adjoint of the trace steps (norm and mute pass through, as the reference's)
         if f_max:
@@ -149,3 +172,100 @@ class PlainFWI:
         rec = dict(misfit=misfit, error=self.error(), seconds=time.perf_counter() - t0, f_max=f_max)
         self.history.append(rec)
         return rec
+
+
+# ---- learned preconditioner -------------------------------------------------------------------
+
+VP_REF, VP_SCALE = 1500., 100.  # network units: (vp - 1500) / 100 and vp updates / 100
+
+
+def features(grad, vp, inner):
+    """Network input [1, H, W, 2] on the inner grid: the raw slowness gradient scaled to max |g| = 1
+    and (vp - 1500) / 100."""
+    g = grad[inner]
+    g = g / (g.abs().max() + 1e-30)
+    v = (vp[inner] - VP_REF) / VP_SCALE
+    return torch.stack([g, v], dim=-1)[None].contiguous()
+
+
+class LearnedFWI(PlainFWI):
+    """FWI whose update is the U-Net's prediction from [gradient, model], accepted only when the
+    plain misfit decreases; otherwise the plain gradient step of ``PlainFWI`` is taken."""
+
+    def __init__(self, w, net, **kwargs):
+        super().__init__(w, **kwargs)
+        self.net = net
+
+    def iterate(self, f_max=None):
+        t0 = time.perf_counter()
+        misfit, grad, prec = self.gradient(f_max)
+        x = features(grad, self.vp, self.inner)
+        y = self.net.forward(x)
+        H, W = x.shape[1], x.shape[2]
+        dvp = self.net.output(y, 1, H, W)[0, ..., 0] * VP_SCALE
+        cand = self.vp.clone()
+        cand[self.inner] += dvp
+        cand = self.clip.forward(cand)
+        accepted = self.misfit(cand, f_max) < misfit
+        if accepted:
+            self.vp.copy_(cand)
+        else:
+            d = self.direction(grad, prec)
+            self.optimiser.step(self.vp, d)
+            self.vp.copy_(self.clip.forward(self.vp))
+        torch.cuda.synchronize(self.device)
+        rec = dict(misfit=misfit, error=self.error(), seconds=time.perf_counter() - t0, f_max=f_max,
+                   learned=bool(accepted))
+        self.history.append(rec)
+        return rec
+
+
+def generate_pairs(fwi, phantoms_vp, iterations=5, f_max=None):
+    """Training pairs along plain-FWI paths: for each true model, ``iterations`` plain updates from
+    the start model, each contributing (features(gradient, vp), (vp_true - vp) / 100)."""
+    xs, ts = [], []
+    for vp_true in phantoms_vp:
+        fwi.reset(vp_true)
+        for _ in range(iterations):
+            _, grad, prec = fwi.gradient(f_max)
+            xs.append(features(grad, fwi.vp, fwi.inner))
+            ts.append(((fwi.vp_true - fwi.vp)[fwi.inner] / VP_SCALE)[None].contiguous())
+            d = fwi.direction(grad, prec)
+            fwi.optimiser.step(fwi.vp, d)
+            fwi.vp.copy_(fwi.clip.forward(fwi.vp))
+    return torch.cat(xs), torch.cat(ts)
+
+
+def train_unet(net, X, T, epochs=20, batch=4, lr=1e-3, seed=0):
+    """Adam on the mean squared error of the predicted update; returns the per-epoch losses."""
+    g = torch.Generator(device='cpu').manual_seed(seed)
+    n = X.shape[0]
+    losses = []
+    for _ in range(epochs):
+        perm = torch.randperm(n, generator=g)
+        tot = 0.
+        for i in range(0, n - batch + 1, batch):
+            idx = perm[i:i + batch].to(X.device)
+            y = net.forward(X[idx].contiguous())
+            loss, d = net.mse(y, T[idx].contiguous())
+            net.backward(d)
+            net.adam_step(lr=lr)
+            tot += float(loss.item())
+        losses.append(tot / max(1, n // batch))
+    return losses
+
+
+def run_to_error(fwi, vp_true, target, max_iter=30, f_max=None):
+    """Iterates from the start model until the relative vp error is <= target; returns (wall
+    seconds or None if not reached, iterations, errors)."""
+    fwi.reset(vp_true)
+    torch.cuda.synchronize(fwi.device)
+    t0 = time.perf_counter()
+    errs = [fwi.error()]
+    if errs[0] <= target:
+        return 0.0, 0, errs
+    for it in range(max_iter):
+        errs.append(fwi.iterate(f_max)['error'])
+        if errs[-1] <= target:
+            return time.perf_counter() - t0, it + 1, errs
+    return None, max_iter, errs
