@@ -265,6 +265,19 @@ def fwi_arm(args):
     losses = train_unet(net, X, T, epochs=args.fwi_epochs, batch=4, lr=1e-3)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
+    # tensor-core rate of the network's forward pass (batch 4, the training shape): GEMM FLOPs of
+    # every convolution over the CUDA-event time of the whole forward
+    xb = X[:4].contiguous()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    net.forward(xb)
+    ev0.record()
+    for _ in range(5):
+        net.forward(xb)
+    ev1.record()
+    torch.cuda.synchronize()
+    fwd_ms = ev0.elapsed_time(ev1) / 5
+    flops = sum(2.0 * layer.saved[2] * layer.saved[3] * layer.saved[4] * layer.coutp * layer.kp
+                for layer in net.layers())
     learned = LearnedFWI(w0, net, step_size=step)
     rows = []
     for seed in range(args.fwi_test):
@@ -290,7 +303,8 @@ def fwi_arm(args):
         'plain_reached': sum(r['plain_s'] is not None for r in rows),
         'learned_reached': sum(r['learned_s'] is not None for r in rows),
         'pair_generation_s': t_pairs, 'training_s': t_train, 'training_loss': [losses[0], losses[-1]],
-        'gemm_timeouts': net.errors(), 'per_phantom': rows,
+        'gemm_timeouts': net.errors(), 'unet_forward_ms_batch4': fwd_ms,
+        'unet_forward_tflops': flops / (fwd_ms * 1e-3) / 1e12, 'per_phantom': rows,
     }
     print(json.dumps(line))
     plain.close()
