@@ -109,6 +109,13 @@ int sa_forward(sa_plan* plan, const float* wavelets, float* traces, int save_mod
 int sa_adjoint(sa_plan* plan, const float* residuals, float* grad_vp, float* prec_vp, int grad_mode,
                void* stream);
 
+/* sa_adjoint plus the gradient with respect to the wavelets: grad_wavelets [n_src_total, nt]
+ * (host or device) receives -interp(p_a[t]) at the sources for t = 1 .. nt-1-f and zero
+ * elsewhere, the reference's src.interpolate(expr=-p_a) (iso_acoustic/devito.py:755-756) read back
+ * by get_grad_wavelets (:1226-1262). 2D, grad_mode SA_GRAD_PARITY. */
+int sa_adjoint_wavelets(sa_plan* plan, const float* residuals, float* grad_vp, float* prec_vp, float* grad_wavelets,
+                        int grad_mode, void* stream);
+
 /* Picks the CTA width and row chunking for the current geometry by timing the candidates
  * (no counterpart in the reference, whose Devito autotuner is optional: common/devito.py:1043). */
 int sa_autotune(sa_plan* plan, void* stream);

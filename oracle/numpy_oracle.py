@@ -379,12 +379,14 @@ def forward(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, or
 
 
 def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
-            rho=None, alpha=None, kernel=None, undersampling=4, dtype=np.float32):
+            rho=None, alpha=None, kernel=None, undersampling=4, dtype=np.float32, src_coords=None):
     """Reverse-time adjoint and vp imaging condition of the reference
     (iso_acoustic/devito.py:689-920, 985-1043): backward update of p_a[t-1],
     injection of -res[t] dt^2 vp^2 at the receivers (fw3d_mode, :725,748-753), and on
     t % f == 0 in the interior: grad += snap[t/f] p_a[t], prec += snap[t/f]^2.
-    Returns raw (grad, prec) on the extended grid (zero outside the interior)."""
+    Returns raw (grad, prec) on the extended grid (zero outside the interior); with src_coords
+    also the wavelet gradient [n_src, nt], src[t] = -interp(p_a[t]) (src.interpolate(expr=-p_a),
+    :755-756)."""
     dim = vp.ndim
     shape = vp.shape
     h = max(spacing)
@@ -404,7 +406,13 @@ def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
     qp = np.zeros(shape, dtype=dtype)  # p_a[t+1]
     q = np.zeros(shape, dtype=dtype)   # p_a[t]
     offs = _corner_offsets(dim)
+    gsrc = None
+    if src_coords is not None:
+        sb, sw = linear_stencil(np.asarray(src_coords, np.float32) + eps, origin, spacing)
+        gsrc = np.zeros((nt, sb.shape[0]))
     for t in range(nt - 1 - f, 0, -1):
+        if gsrc is not None:
+            gsrc[t] = -_gather(q, sb, sw, dim)
         Lt = _Lt(med, q, kernel, dt, w2, ws)
         qn = _update(med, damp, Lt, q, qp, dt)
         for c, off in enumerate(offs):
@@ -416,6 +424,8 @@ def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
             grad[interior] += (s * q.astype(np.float64))[interior]
             prec[interior] += (s * s)[interior]
         qp, q = q, qn
+    if gsrc is not None:
+        return grad.astype(np.float32), prec.astype(np.float32), gsrc.T.astype(np.float32)
     return grad.astype(np.float32), prec.astype(np.float32)
 
 

@@ -32,7 +32,8 @@ SA_GRAD_EXACT = 1
 
 # every symbol include/strideacc.h declares
 EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometry', 'sa_forward',
-           'sa_adjoint', 'sa_autotune', 'sa_last_error', 'sa_launch_count', 'sa_forward_2d_noalloc',
+           'sa_adjoint', 'sa_adjoint_wavelets', 'sa_autotune', 'sa_last_error', 'sa_launch_count',
+           'sa_forward_2d_noalloc',
            'sa_traces_sosfilt', 'sa_traces_fir', 'sa_traces_check', 'sa_traces_norm_per_shot', 'sa_traces_mute',
            'sa_field_mul', 'sa_field_clip', 'sa_field_axpy', 'sa_field_slowness_step', 'sa_field_stats',
            'sa_field_scale', 'sa_field_gaussian', 'sa_field_apply_prec', 'sa_gemm_bf16', 'sa_nn_im2col',
@@ -74,6 +75,7 @@ def load():
     lib.sa_set_geometry.argtypes = [P, I, P, P, P, P]
     lib.sa_forward.argtypes = [P, P, P, I, P]
     lib.sa_adjoint.argtypes = [P, P, P, P, I, P]
+    lib.sa_adjoint_wavelets.argtypes = [P, P, P, P, P, I, P]
     lib.sa_autotune.argtypes = [P, P]
     lib.sa_last_error.argtypes = [ctypes.c_char_p, I]
     lib.sa_launch_count.argtypes = [P]
@@ -210,11 +212,12 @@ class Plan:
                 'checkpoints': SA_SAVE_CHECKPOINTS}[save]
         check(load().sa_forward(self._h, _ptr(wavelets), _ptr(traces), mode, _stream(stream)))
 
-    def adjoint(self, residuals, grad, prec, stream=None, exact=False):
+    def adjoint(self, residuals, grad, prec, stream=None, exact=False, grad_wavelets=None):
         """exact=False: the reference's imaging condition; exact=True: dL/dvp of the discrete forward
-        map for residuals = dL/dtraces (needs a forward with save='checkpoints')."""
-        check(load().sa_adjoint(self._h, _ptr(residuals), _ptr(grad), _ptr(prec),
-                                SA_GRAD_EXACT if exact else SA_GRAD_PARITY, _stream(stream)))
+        map for residuals = dL/dtraces (needs a forward with save='checkpoints'). grad_wavelets
+        [n_src, nt]: also the reference's wavelet gradient -interp(p_a) (parity mode)."""
+        check(load().sa_adjoint_wavelets(self._h, _ptr(residuals), _ptr(grad), _ptr(prec), _ptr(grad_wavelets),
+                                         SA_GRAD_EXACT if exact else SA_GRAD_PARITY, _stream(stream)))
 
     def autotune(self, stream=None):
         check(load().sa_autotune(self._h, _stream(stream)))

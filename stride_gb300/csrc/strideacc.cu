@@ -142,6 +142,11 @@ struct sa_plan {
     int* inj_recx_off = nullptr;
     sa::Gather* src_flat = nullptr;
     size_t cap_inj_recx = 0, cap_inj_recx_off = 0, cap_src_flat = 0;
+    // wavelet gradient: per-CTA source gathers (negated weights) and its time-major buffer
+    sa::Gather* gat_src = nullptr;
+    int* gat_src_off = nullptr;
+    float* wgrad = nullptr;
+    size_t cap_gat_src = 0, cap_gat_src_off = 0, cap_wgrad = 0;
     // layout
     int NT = 128, by = 110, chunk_rows = 1, nstrips = 1, nchunks = 1;
     bool layout_fixed = false;
@@ -149,7 +154,7 @@ struct sa_plan {
     // graphs
     cudaStream_t cap = nullptr;
     cudaGraphExec_t g_fwd[3] = {nullptr, nullptr, nullptr};  // by save mode
-    cudaGraphExec_t g_adj[3] = {nullptr, nullptr, nullptr};  // from snapshots, from checkpoints, exact
+    cudaGraphExec_t g_adj[3][2] = {};  // [from snapshots, from checkpoints, exact][wavelet gradient]
     long long fwd_launches[3] = {0, 0, 0};                   // kernels in each forward loop (by save mode)
     long long adj_launches[3] = {0, 0, 0};                   // kernels in each adjoint loop
     bool use_graphs = true;
@@ -177,11 +182,12 @@ void drop_graphs(sa_plan* p) {
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
-    for (auto& g : p->g_adj)
-        if (g) {
-            cudaGraphExecDestroy(g);
-            g = nullptr;
-        }
+    for (auto& row : p->g_adj)
+        for (auto& g : row)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
 }
 
 // Sponge ramp of Boundary.damping for one axis (stride/physics/boundaries/boundary.py:98-151),
@@ -233,10 +239,10 @@ struct HostInject {
 int build_lists_impl(sa_plan* p);
 int build_lists(sa_plan* p) {
     const void* before[] = {p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
-                            p->inj_recx, p->inj_recx_off, p->src_flat};
+                            p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off};
     const int rc = build_lists_impl(p);
     const void* after[] = {p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
-                           p->inj_recx, p->inj_recx_off, p->src_flat};
+                           p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off};
     for (size_t k = 0; k < sizeof(before) / sizeof(before[0]); k++)
         if (before[k] != after[k]) {
             drop_graphs(p);
@@ -312,41 +318,53 @@ int build_lists_impl(sa_plan* p) {
         if (!sf.empty())
             CK(cudaMemcpy(p->src_flat, sf.data(), sf.size() * sizeof(sa::Gather), cudaMemcpyHostToDevice));
     }
-    // receiver gathers, one per receiver, owned by the CTA of its base corner
-    std::vector<std::pair<int, sa::Gather>> g;
-    std::vector<sa::Gather> flat;
-    for (int s = 0; s < p->n_shots; s++)
-        for (int r = p->rec_off[s]; r < p->rec_off[s + 1]; r++) {
-            const double fx = p->rec_fx[r], fy = p->rec_fy[r];
-            sa::Gather G;
-            G.row = p->rec_bx[r];
-            G.col = p->rec_by[r];
-            G.point = r;
-            G.pad = s;
-            G.w00 = (float)((1 - fx) * (1 - fy));
-            G.w01 = (float)((1 - fx) * fy);
-            G.w10 = (float)(fx * (1 - fy));
-            G.w11 = (float)(fx * fy);
-            g.push_back({cta_of(s, G.row, G.col), G});
-            flat.push_back(G);
+    // gathers, one per point, owned by the CTA of its base corner: receivers (the forward's traces)
+    // and sources with negated weights (the adjoint's wavelet gradient, -interp(p_a))
+    auto make_gathers = [&](const std::vector<int>& off, const std::vector<int>& bx, const std::vector<int>& by,
+                            const std::vector<double>& fx, const std::vector<double>& fy, float sign,
+                            sa::Gather** dl, size_t* capl, int** doff, size_t* capo, sa::Gather** dflat,
+                            size_t* capf) -> int {
+        std::vector<std::pair<int, sa::Gather>> g;
+        std::vector<sa::Gather> flat;
+        for (int s = 0; s < p->n_shots; s++)
+            for (int r = off[s]; r < off[s + 1]; r++) {
+                sa::Gather G;
+                G.row = bx[r];
+                G.col = by[r];
+                G.point = r;
+                G.pad = s;
+                G.w00 = sign * (float)((1 - fx[r]) * (1 - fy[r]));
+                G.w01 = sign * (float)((1 - fx[r]) * fy[r]);
+                G.w10 = sign * (float)(fx[r] * (1 - fy[r]));
+                G.w11 = sign * (float)(fx[r] * fy[r]);
+                g.push_back({cta_of(s, G.row, G.col), G});
+                flat.push_back(G);
+            }
+        std::stable_sort(g.begin(), g.end(), [](const auto& a, const auto& b) {
+            return a.first != b.first ? a.first < b.first : a.second.row < b.second.row;
+        });
+        std::vector<sa::Gather> gl(g.size());
+        std::vector<int> goff(ncta + 1, 0);
+        for (size_t k = 0; k < g.size(); k++) {
+            gl[k] = g[k].second;
+            goff[g[k].first + 1]++;
         }
-    std::stable_sort(g.begin(), g.end(), [](const auto& a, const auto& b) {
-        return a.first != b.first ? a.first < b.first : a.second.row < b.second.row;
-    });
-    std::vector<sa::Gather> gl(g.size());
-    std::vector<int> goff(ncta + 1, 0);
-    for (size_t k = 0; k < g.size(); k++) {
-        gl[k] = g[k].second;
-        goff[g[k].first + 1]++;
-    }
-    for (int c = 0; c < ncta; c++) goff[c + 1] += goff[c];
-    CKR(ensure(&p->gat, &p->cap_gat, gl.size()));
-    CKR(ensure(&p->gat_off, &p->cap_gat_off, goff.size()));
-    CKR(ensure(&p->gat_flat, &p->cap_gat_flat, flat.size()));
-    if (!gl.empty()) CK(cudaMemcpy(p->gat, gl.data(), gl.size() * sizeof(sa::Gather), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(p->gat_off, goff.data(), goff.size() * sizeof(int), cudaMemcpyHostToDevice));
-    if (!flat.empty())
-        CK(cudaMemcpy(p->gat_flat, flat.data(), flat.size() * sizeof(sa::Gather), cudaMemcpyHostToDevice));
+        for (int c = 0; c < ncta; c++) goff[c + 1] += goff[c];
+        CKR(ensure(dl, capl, gl.size()));
+        CKR(ensure(doff, capo, goff.size()));
+        if (!gl.empty()) CK(cudaMemcpy(*dl, gl.data(), gl.size() * sizeof(sa::Gather), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(*doff, goff.data(), goff.size() * sizeof(int), cudaMemcpyHostToDevice));
+        if (dflat) {
+            CKR(ensure(dflat, capf, flat.size()));
+            if (!flat.empty())
+                CK(cudaMemcpy(*dflat, flat.data(), flat.size() * sizeof(sa::Gather), cudaMemcpyHostToDevice));
+        }
+        return SA_OK;
+    };
+    CKR(make_gathers(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, 1.f, &p->gat, &p->cap_gat, &p->gat_off,
+                     &p->cap_gat_off, &p->gat_flat, &p->cap_gat_flat));
+    CKR(make_gathers(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, -1.f, &p->gat_src, &p->cap_gat_src,
+                     &p->gat_src_off, &p->cap_gat_src_off, nullptr, nullptr));
     return SA_OK;
 }
 
@@ -433,7 +451,17 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
 }
 
 // Issues the reverse-time adjoint loop t = nt-1-f .. 1 (devito.py:915-920).
-int issue_adjoint(sa_plan* p, cudaStream_t s) {
+// The adjoint's source gathers write -interp(p_a[t]) into wgrad[t] (the kernel writes row t-1 at
+// step t, so the output base is one row ahead) when the wavelet gradient is requested.
+void wavelet_gather(const sa_plan* p, sa::Step2D& a, bool wav) {
+    if (!wav || !p->n_src) return;
+    a.gat = p->gat_src;
+    a.gat_off = p->gat_src_off;
+    a.gat_out = p->wgrad + p->n_src;
+    a.gat_ld = p->n_src;
+}
+
+int issue_adjoint(sa_plan* p, bool wav, cudaStream_t s) {
     const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
     const size_t gbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float);
     CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
@@ -448,6 +476,8 @@ int issue_adjoint(sa_plan* p, cudaStream_t s) {
     a.gat = nullptr;
     a.save = 0;
     a.grad = 1;
+    if (wav) CK(cudaMemsetAsync(p->wgrad, 0, (size_t)p->d.nt * p->n_src * sizeof(float), s));
+    wavelet_gather(p, a, wav);
     const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     const int T0 = p->d.nt - 1 - p->d.undersampling;
     long long n = 0;
@@ -470,7 +500,7 @@ int issue_adjoint(sa_plan* p, cudaStream_t s) {
 // the adjoint steps run back through the segment on their own two levels. The recomputed
 // steps are the forward's own launches (no receiver gather), so the snapshots are bitwise
 // the ones SA_SAVE_SNAPSHOTS stores.
-int issue_adjoint_ckpt(sa_plan* p, cudaStream_t s) {
+int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
     const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
     const size_t ffloats = fbytes / sizeof(float);
     const size_t gbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float);
@@ -498,6 +528,8 @@ int issue_adjoint_ckpt(sa_plan* p, cudaStream_t s) {
     aa.save = 0;
     aa.grad = 1;
     aa.snap_shot_stride = fa.snap_shot_stride;
+    if (wav) CK(cudaMemsetAsync(p->wgrad, 0, (size_t)p->d.nt * p->n_src * sizeof(float), s));
+    wavelet_gather(p, aa, wav);
     const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     long long n = 0;
     for (int k = T0 >= 1 ? (T0 - 1) / K : -1; k >= 0; k--) {
@@ -813,7 +845,8 @@ int sa_plan_destroy(sa_plan* p) {
                     p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
-                    p->ones_g, p->zeros_g, p->inj_recx, p->inj_recx_off, p->src_flat};
+                    p->ones_g, p->zeros_g, p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off,
+                    p->wgrad};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (p->cap) cudaStreamDestroy(p->cap);
@@ -955,10 +988,18 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
 }
 
 int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_vp, int grad_mode, void* stream) {
+    return sa_adjoint_wavelets(p, residuals, grad_vp, prec_vp, nullptr, grad_mode, stream);
+}
+
+int sa_adjoint_wavelets(sa_plan* p, const float* residuals, float* grad_vp, float* prec_vp, float* grad_wavelets,
+                        int grad_mode, void* stream) {
     if (!p) return fail(SA_E_INVALID, "null plan");
     if (grad_mode != SA_GRAD_PARITY && grad_mode != SA_GRAD_EXACT) return fail(SA_E_INVALID, "grad_mode %d", grad_mode);
     const bool exact = grad_mode == SA_GRAD_EXACT;
+    const bool wav = grad_wavelets != nullptr;
+    if (wav && exact) return fail(SA_E_UNSUPPORTED, "the wavelet gradient is the parity mode's (src.interpolate(-p_a))");
     if (p->p3) {
+        if (wav) return fail(SA_E_UNSUPPORTED, "the wavelet gradient is implemented for 2D plans");
         if (exact) return fail(SA_E_UNSUPPORTED, "SA_GRAD_EXACT is implemented for 2D plans");
         if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
         return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream);
@@ -1009,11 +1050,17 @@ int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_v
             p->exact_coef_valid = true;
         }
     }
+    if (wav) {
+        float* ow = p->wgrad;
+        CKR(ensure(&p->wgrad, &p->cap_wgrad, (size_t)p->d.nt * std::max(1, p->n_src)));
+        if (ow != p->wgrad) drop_graphs(p);
+    }
     CKR(load_transposed(p, residuals, p->n_rec, p->d.nt, p->rec_amp, s));
     const int am = exact ? 2 : (ck ? 1 : 0);
-    CKR(run_loop(p, &p->g_adj[am], s, [&](cudaStream_t cs) {
-        return exact ? issue_adjoint_exact(p, cs) : (ck ? issue_adjoint_ckpt(p, cs) : issue_adjoint(p, cs));
+    CKR(run_loop(p, &p->g_adj[am][wav ? 1 : 0], s, [&](cudaStream_t cs) {
+        return exact ? issue_adjoint_exact(p, cs) : (ck ? issue_adjoint_ckpt(p, wav, cs) : issue_adjoint(p, wav, cs));
     }));
+    if (wav) CKR(store_transposed(p, p->wgrad, p->d.nt, p->n_src, grad_wavelets, s));
     const size_t N = (size_t)p->nx * p->ny;
     for (int k = 0; k < 2; k++) {
         float* user = k == 0 ? grad_vp : prec_vp;

@@ -122,7 +122,7 @@ class IsoAcousticGB300(ProblemTypeBase):
     ``attenuation_power=0``, ``diff_source``, ``save_undersampling``, ``save_wavefield``.
     ``platform``, ``devito_config`` and ``devito_args`` are accepted and ignored (the time
     loop always runs on the GPU). Options the reference supports but this build does not
-    (CFS-PML boundary, Hicks interpolation, attenuation power 2, rho/alpha/wavelet gradients)
+    (CFS-PML boundary, Hicks interpolation, attenuation power 2, rho/alpha gradients)
     raise NotImplementedError; unknown values raise ValueError as in the reference.
     """
 
@@ -174,8 +174,6 @@ class IsoAcousticGB300(ProblemTypeBase):
         for v in (rho, alpha):
             if v is not None and getattr(v, 'needs_grad', False):
                 raise NotImplementedError('rho/alpha gradients are not implemented in this build')
-        if getattr(wavelets, 'needs_grad', False):
-            raise NotImplementedError('wavelet gradients are not implemented in this build')
         self._check_conditions(wavelets, vp, rho, alpha, kwargs.get('kernel', None),
                                kwargs.get('save_undersampling', None), **kwargs)
 
@@ -270,10 +268,10 @@ class IsoAcousticGB300(ProblemTypeBase):
         return np.ascontiguousarray((data * self._window()[None, :]).astype(np.float32))
 
     @staticmethod
-    def _save_wavefield(vp, rho, alpha, kwargs):
+    def _save_wavefield(vp, rho, alpha, kwargs, wavelets=None):
         save = kwargs.get('save_wavefield', False)
         if save is False:
-            save = bool(getattr(vp, 'needs_grad', False))
+            save = bool(getattr(vp, 'needs_grad', False)) or bool(getattr(wavelets, 'needs_grad', False))
         return bool(save)
 
     # ---------------------------------------------------------------------------- forward
@@ -295,7 +293,7 @@ class IsoAcousticGB300(ProblemTypeBase):
             self.logger.warning('(ShotID %d) Empty wavelets, not running forward', problem.shot.id)
             self._saved = False
             return
-        save = self._save_wavefield(vp, rho, alpha, kwargs)
+        save = self._save_wavefield(vp, rho, alpha, kwargs, wavelets)
         self._plan.forward(self._src, self._traces, save=save)
         self._saved = save
 
@@ -320,10 +318,13 @@ class IsoAcousticGB300(ProblemTypeBase):
         shape = self.space.extended_shape
         self._grad = np.zeros(shape, np.float32)
         self._prec = np.zeros(shape, np.float32)
+        self._wgrad = None
+        if getattr(wavelets, 'needs_grad', False):
+            self._wgrad = np.zeros((self._plan.n_src, self.time.extended_num), np.float32)
         if np.linalg.norm(np.asarray(adjoint_source.data)) < 1e-31:
             self.logger.warning('(ShotID %d) Empty adjoint source, not running adjoint', problem.shot.id)
             return
-        self._plan.adjoint(self._res, self._grad, self._prec)
+        self._plan.adjoint(self._res, self._grad, self._prec, grad_wavelets=self._wgrad)
 
     def after_adjoint(self, adjoint_source, wavelets, vp, rho=None, alpha=None, **kwargs):
         """Retrieve the gradients (devito.py:922-981)."""
@@ -363,6 +364,19 @@ class IsoAcousticGB300(ProblemTypeBase):
         grad = vp.alike(name='vp_grad', data=g, shape=g.shape, extended_shape=g.shape, inner=None)
         grad.prec = vp.alike(name='vp_prec', data=p, shape=p.shape, extended_shape=p.shape, inner=None)
         return grad
+
+    def prepare_grad_wavelets(self, wavelets, **kwargs):
+        """The wavelet gradient is gathered inside the adjoint kernel (devito.py:755-756, 1189-1203)."""
+        return ()
+
+    def init_grad_wavelets(self, wavelets, **kwargs):
+        """The gradient buffer starts at zero (devito.py:1205-1224)."""
+        self._wgrad = None
+
+    def get_grad_wavelets(self, wavelets, **kwargs):
+        """-interp(p_a[t]) at the source points, [n_src, nt] (devito.py:1226-1262)."""
+        g = self._wgrad if self._wgrad is not None else np.zeros(np.atleast_2d(wavelets.data).shape, np.float32)
+        return wavelets.alike(name='wavelets_grad', data=g, shape=g.shape, extended_shape=g.shape, inner=None)
 
     # ---------------------------------------------------------------------------- batches
 

@@ -73,3 +73,21 @@ def test_empty_wavelets_skip_the_run():
     shot.wavelets.data[:] = 0
     traces = pde(shot.wavelets, vp, problem=sub)
     assert not np.any(traces.data)
+
+
+def test_pde_wavelet_gradient():
+    """wavelets.needs_grad: the adjoint returns (wavelets_grad, vp_grad, None, None) with the
+    reference's -interp(p_a) at the sources."""
+    space, time, vp, rho, al, shot, sub, geo, w = _setup(True, True)
+    pde = iso_acoustic.IsoAcousticGB300(space=space, time=time)
+    shot.wavelets.needs_grad = True
+    traces = pde(shot.wavelets, vp, rho=rho, alpha=al, problem=sub)
+    residual = shot.observed.alike(name='residual', data=traces.data * np.float32(0.7))
+    grads = pde.adjoint(residual, shot.wavelets, vp, rho, al, problem=sub)
+    assert grads[0] is not None and grads[0].name == 'wavelets_grad' and grads[1] is not None
+    kw = dict(rho=rho.extended_data, alpha=al.extended_data)
+    _, snaps = c_oracle.forward(vp.extended_data, space.spacing, time.step, time.num, space.absorbing, geo[:1], geo,
+                                w[None], space.pml_origin, kernel='OT4', save=True, **kw)
+    _, _, gw = O.adjoint(vp.extended_data, space.spacing, time.step, time.num, space.absorbing, geo,
+                         traces.data * np.float32(0.7), space.pml_origin, snaps, kernel='OT4', src_coords=geo[:1], **kw)
+    assert C.rel_l2(grads[0].data, gw) <= 1e-4
