@@ -5,7 +5,10 @@
 
 namespace sa {
 
-constexpr int RB = 2;  // rows per iteration
+#ifndef SA_RB
+#define SA_RB 2
+#endif
+constexpr int RB = SA_RB;  // rows per iteration
 #ifndef SA_PF
 #define SA_PF 2
 #endif
