@@ -39,6 +39,10 @@ extern "C" {
 #define SA_SAVE_CHECKPOINTS 2 /* store the state every checkpoint interval; the adjoint recomputes each
                                  segment's p.dt2 from its checkpoint (same gradient, less memory) */
 
+#define SA_INTERP_LINEAR 0    /* bilinear / trilinear SparseTimeFunction (common/devito.py:580-653) */
+#define SA_INTERP_HICKS 1     /* Kaiser-windowed sinc, 8 points per axis (common/devito.py:640-648,843-885);
+                                 2D, sources smoothed as the reference's src, receivers not */
+
 #define SA_GRAD_PARITY 0      /* reference imaging condition: sum_{t%f==0} p_tt * p_a, interior only */
 #define SA_GRAD_EXACT 1       /* gradient of the discrete forward map (its exact transpose), every grid
                                  point; needs SA_SAVE_CHECKPOINTS; 2D plans. No counterpart in the
@@ -61,6 +65,7 @@ typedef struct sa_desc {
     int max_shots;         /* shots advanced together per launch */
     int checkpoint_interval;   /* steps between checkpoints for SA_SAVE_CHECKPOINTS (0: 50) */
     double checkpoint_budget;  /* bytes the checkpoints may use (0: no limit); widens the interval */
+    int interpolation;         /* SA_INTERP_LINEAR or SA_INTERP_HICKS (2D): sparse-point interpolation */
 } sa_desc;
 
 typedef struct sa_plan sa_plan;

@@ -124,6 +124,53 @@ def linear_stencil(coords, origin, spacing):
     return base, w
 
 
+def hicks_stencil(coords, origin, spacing, smooth=False):
+    """Hicks (Kaiser-windowed sinc) coefficients of GridDevito._calculate_hicks
+    (stride/physics/common/devito.py:843-885) on the support of Devito's
+    PrecomputedSparseTimeFunction with r = 8 (common/devito.py:640-648): grid points
+    floor(x) - 3 .. floor(x) + 4 along each axis (the last coefficient is zero). ``smooth``: the
+    reference's smoothing of the central coefficients (sources are smooth, receivers are not).
+    Returns (base [n, dim], weights [n, 8**dim], offsets [8**dim, dim])."""
+    import itertools
+    import scipy.special
+    coords = np.asarray(coords, dtype=np.float32).astype(np.float64)
+    grid = (coords - np.asarray(origin, np.float64)) / np.asarray(spacing, np.float64)
+    base = np.floor(grid).astype(np.int64)
+    frac = grid - base
+    n, dim = coords.shape
+    kaiser_b, half = 4.14, 3
+    den = scipy.special.iv(0, kaiser_b)
+    ext = half / 0.99
+    coef = np.zeros((n, dim, 2 * half + 2))
+    for gp in range(-half, half + 1):
+        x = frac - gp
+        wgt = (x / ext) ** 2
+        wgt[wgt > 1] = 1
+        coef[:, :, half + gp] = np.sinc(x) * scipy.special.iv(0, kaiser_b * np.sqrt(1 - wgt)) / den
+    if smooth:
+        m = half - 1
+        a, b, c = coef[:, :, m].copy(), coef[:, :, m + 1].copy(), coef[:, :, m + 2].copy()
+        coef[:, :, m - 1] = coef[:, :, m - 1] + a * 0.01
+        coef[:, :, m] = a * 0.98 + b * 0.03
+        coef[:, :, m + 1] = b * 0.94 + (a + c) * 0.01
+        coef[:, :, m + 2] = c * 0.98 + b * 0.03
+        coef[:, :, m + 3] = coef[:, :, m + 3] + c * 0.01
+    offs = np.array(list(itertools.product(range(-half, half + 2), repeat=dim)), dtype=np.int64)
+    w = np.ones((n, len(offs)))
+    for k, off in enumerate(offs):
+        for d in range(dim):
+            w[:, k] *= coef[:, d, off[d] + half]
+    return base, w, offs
+
+
+def sparse_stencil(interpolation, coords, origin, spacing, smooth):
+    """(base, weights, offsets) of a SparseTimeFunction with the given interpolation."""
+    if interpolation == 'hicks':
+        return hicks_stencil(coords, origin, spacing, smooth)
+    base, w = linear_stencil(coords, origin, spacing)
+    return base, w, _corner_offsets(base.shape[1])
+
+
 def _corner_offsets(dim):
     return [tuple((c >> (dim - 1 - d)) & 1 for d in range(dim)) for c in range(2 ** dim)]
 
@@ -311,15 +358,15 @@ def _update(med, damp, Lt, u, um, dt):
     return num / (t(1) + beta)
 
 
-def _scatter(field, base, w, amp, dim):
-    offs = _corner_offsets(dim)
+def _scatter(field, base, w, amp, dim, offs=None):
+    offs = _corner_offsets(dim) if offs is None else offs
     for c, off in enumerate(offs):
         idx = tuple(base[:, d] + off[d] for d in range(dim))
         np.add.at(field, idx, (w[:, c] * amp).astype(field.dtype))
 
 
-def _gather(field, base, w, dim):
-    offs = _corner_offsets(dim)
+def _gather(field, base, w, dim, offs=None):
+    offs = _corner_offsets(dim) if offs is None else offs
     out = np.zeros(base.shape[0], dtype=np.float64)
     for c, off in enumerate(offs):
         idx = tuple(base[:, d] + off[d] for d in range(dim))
@@ -329,7 +376,7 @@ def _gather(field, base, w, dim):
 
 def forward(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, origin,
             rho=None, alpha=None, kernel=None, save=False, undersampling=4,
-            dtype=np.float32, diff_source=False):
+            dtype=np.float32, diff_source=False, interpolation='linear'):
     """Forward modelling of one shot (iso_acoustic/devito.py:220-581).
 
     Arrays are on the extended grid. ``wavelets`` [n_src, nt] raw (the Tukey window
@@ -347,8 +394,8 @@ def forward(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, or
     med = _Medium(vp, rho, alpha, spacing, dtype)
     damp = damping_profile(shape, spacing, absorbing, vp, dt).astype(dtype)
     eps = 1e-3 * np.asarray(spacing)
-    sb, sw = linear_stencil(np.asarray(src_coords, np.float32) + eps, origin, spacing)
-    rb, rw = linear_stencil(np.asarray(rec_coords, np.float32) + eps, origin, spacing)
+    sb, sw, soffs = sparse_stencil(interpolation, np.asarray(src_coords, np.float32) + eps, origin, spacing, True)
+    rb, rw, roffs = sparse_stencil(interpolation, np.asarray(rec_coords, np.float32) + eps, origin, spacing, False)
     wav = np.asarray(wavelets, np.float64)
     if diff_source:
         wav = np.gradient(wav, dt, axis=-1)
@@ -362,16 +409,15 @@ def forward(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, or
     snaps = np.zeros((n_snap,) + shape, dtype=np.float32) if save else None
     pm = np.zeros(shape, dtype=dtype)
     p = np.zeros(shape, dtype=dtype)
-    offs = _corner_offsets(dim)
     for t in range(1, nt - 1):
         Lt = _Lt(med, p, kernel, dt, w2, ws)
         pn = _update(med, damp, Lt, p, pm, dt)
-        # src.inject(p.forward, src * 2 dt^2 vp / h / dt): vp at each corner (H1 reading)
-        for c, off in enumerate(offs):
+        # src.inject(p.forward, src * 2 dt^2 vp / h / dt): vp at each support point (H1 reading)
+        for c, off in enumerate(soffs):
             idx = tuple(sb[:, d] + off[d] for d in range(dim))
             amp = src[t].astype(np.float64) * scale * med.vp[idx].astype(np.float64)
             np.add.at(pn, idx, (sw[:, c] * amp).astype(dtype))
-        rec[t] = _gather(pn, rb, rw, dim)
+        rec[t] = _gather(pn, rb, rw, dim, roffs)
         if save and t % f == 0:
             snaps[t // f] = (pn - 2 * p + pm) / dtype(dt * dt)
         pm, p = p, pn
@@ -379,7 +425,8 @@ def forward(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, or
 
 
 def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
-            rho=None, alpha=None, kernel=None, undersampling=4, dtype=np.float32, src_coords=None):
+            rho=None, alpha=None, kernel=None, undersampling=4, dtype=np.float32, src_coords=None,
+            interpolation='linear'):
     """Reverse-time adjoint and vp imaging condition of the reference
     (iso_acoustic/devito.py:689-920, 985-1043): backward update of p_a[t-1],
     injection of -res[t] dt^2 vp^2 at the receivers (fw3d_mode, :725,748-753), and on
@@ -397,7 +444,7 @@ def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
     med = _Medium(vp, rho, alpha, spacing, dtype)
     damp = damping_profile(shape, spacing, absorbing, vp, dt).astype(dtype)
     eps = 1e-3 * np.asarray(spacing)
-    rb, rw = linear_stencil(np.asarray(rec_coords, np.float32) + eps, origin, spacing)
+    rb, rw, roffs = sparse_stencil(interpolation, np.asarray(rec_coords, np.float32) + eps, origin, spacing, False)
     res = (np.asarray(residual, np.float64).T * tukey(nt)[:, None]).astype(np.float32)
     f = undersampling
     interior = tuple(slice(a, n - a) for a, n in zip(absorbing, shape))
@@ -405,14 +452,15 @@ def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
     prec = np.zeros(shape, dtype=np.float64)
     qp = np.zeros(shape, dtype=dtype)  # p_a[t+1]
     q = np.zeros(shape, dtype=dtype)   # p_a[t]
-    offs = _corner_offsets(dim)
+    offs = roffs
     gsrc = None
     if src_coords is not None:
-        sb, sw = linear_stencil(np.asarray(src_coords, np.float32) + eps, origin, spacing)
+        sb, sw, soffs = sparse_stencil(interpolation, np.asarray(src_coords, np.float32) + eps, origin, spacing,
+                                       True)
         gsrc = np.zeros((nt, sb.shape[0]))
     for t in range(nt - 1 - f, 0, -1):
         if gsrc is not None:
-            gsrc[t] = -_gather(q, sb, sw, dim)
+            gsrc[t] = -_gather(q, sb, sw, dim, soffs)
         Lt = _Lt(med, q, kernel, dt, w2, ws)
         qn = _update(med, damp, Lt, q, qp, dt)
         for c, off in enumerate(offs):

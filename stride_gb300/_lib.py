@@ -28,6 +28,8 @@ SA_SAVE_NONE = 0
 SA_SAVE_SNAPSHOTS = 1
 SA_SAVE_CHECKPOINTS = 2
 SA_GRAD_PARITY = 0
+SA_INTERP_LINEAR = 0
+SA_INTERP_HICKS = 1
 SA_GRAD_EXACT = 1
 
 # every symbol include/strideacc.h declares
@@ -47,7 +49,8 @@ class SaDesc(ctypes.Structure):
                 ('extra', ctypes.c_int * 3), ('absorbing', ctypes.c_int * 3), ('dt', ctypes.c_double),
                 ('nt', ctypes.c_int), ('kernel', ctypes.c_int), ('density', ctypes.c_int),
                 ('attenuation', ctypes.c_int), ('undersampling', ctypes.c_int), ('max_shots', ctypes.c_int),
-                ('checkpoint_interval', ctypes.c_int), ('checkpoint_budget', ctypes.c_double)]
+                ('checkpoint_interval', ctypes.c_int), ('checkpoint_budget', ctypes.c_double),
+                ('interpolation', ctypes.c_int)]
 
 
 class StrideAccError(RuntimeError):
@@ -156,7 +159,8 @@ class Plan:
     """Owner of one sa_plan (one batch of shots on one grid)."""
 
     def __init__(self, dim, shape, spacing, extra, absorbing, dt, nt, kernel='OT4', density=SA_DENSITY_NONE,
-                 attenuation=False, undersampling=4, max_shots=1, checkpoint_interval=0, checkpoint_budget=0.0):
+                 attenuation=False, undersampling=4, max_shots=1, checkpoint_interval=0, checkpoint_budget=0.0,
+                 interpolation='linear'):
         lib = load()
         d = SaDesc()
         d.dim = dim
@@ -174,6 +178,7 @@ class Plan:
         d.max_shots = int(max_shots)
         d.checkpoint_interval = int(checkpoint_interval)
         d.checkpoint_budget = float(checkpoint_budget)
+        d.interpolation = {'linear': SA_INTERP_LINEAR, 'hicks': SA_INTERP_HICKS}[interpolation]
         self.desc = d
         h = ctypes.c_void_p()
         check(lib.sa_plan_create(ctypes.byref(d), ctypes.byref(h)))

@@ -42,6 +42,12 @@ struct Inject {
 
 // One receiver of a gather: rec[t][point] = sum of the four bilinear corner terms; `pad` is
 // the receiver's shot (its pair is pad / 2, its lane pad % 2).
+// A receiver with Hicks interpolation: 8 x 8 support from (row, col), weights wx[i] * wy[j].
+struct HicksGather {
+    int row, col, point, shot;
+    float wx[8], wy[8];
+};
+
 struct Gather {
     int row, col, point, pad;
     float w00, w01, w10, w11;

@@ -115,6 +115,30 @@ __global__ void gather_final2d(const float* __restrict__ field, long long shot_s
     out[(long long)trow * ld + G.point] = G.w00 * f[i0] + G.w01 * f[i0 + 2] + G.w10 * f[i1] + G.w11 * f[i1 + 2];
 }
 
+// rec[trow][point] = sum over the 8 x 8 Hicks support of wx[i] wy[j] field(row + i, col + j).
+__global__ void k_hicks_gather2d(const float* __restrict__ field, long long shot_stride, int pitch,
+                                 const HicksGather* __restrict__ g, int n, float* out, int ld, int trow) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const HicksGather G = g[e];
+    const float* f = field + (long long)(G.shot / 2) * shot_stride * 2 + (G.shot & 1);
+    float v = 0.f;
+    for (int i = 0; i < 8; i++) {
+        const float* row = f + 2 * (long long)(G.row + i) * pitch;
+        float r = 0.f;
+        for (int j = 0; j < 8; j++) r += G.wy[j] * row[2 * (G.col + j)];
+        v += G.wx[i] * r;
+    }
+    out[(long long)trow * ld + G.point] = v;
+}
+
+cudaError_t hicks_gather2d(const float* field, long long shot_stride, int pitch, const HicksGather* g, int n, float* out,
+                           int ld, int trow, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_hicks_gather2d<<<(n + 127) / 128, 128, 0, s>>>(field, shot_stride, pitch, g, n, out, ld, trow);
+    return cudaGetLastError();
+}
+
 __global__ void reduce_shots2d(const float* __restrict__ buf, long long shot_stride, int nshots, int nx, int ny,
                                int pitch, float* __restrict__ out) {
     const long long n = (long long)nx * ny;

@@ -42,6 +42,8 @@ cudaError_t sparse3d_gather(const Sparse3D& sp, int n, const float* field, long 
 cudaError_t reduce3d(const float* buf, long long shot_stride, int nshots, int nx, int ny, int nz, int zp, float* out,
                      cudaStream_t s);
 cudaError_t transpose(const float* in, int rows, int cols, float* out, cudaStream_t s);
+cudaError_t hicks_gather2d(const float* field, long long shot_stride, int pitch, const HicksGather* g, int n, float* out,
+                           int ld, int trow, cudaStream_t s);
 cudaError_t final_gather2d(const float* field, long long shot_stride, int pitch, const Gather* g, int n, float* out,
                            int ld, int trow, cudaStream_t s);
 cudaError_t reduce_shots(const float* buf, long long shot_stride, int nshots, int nx, int ny, int pitch, float* out,

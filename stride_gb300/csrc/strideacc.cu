@@ -147,6 +147,9 @@ struct sa_plan {
     int* gat_src_off = nullptr;
     float* wgrad = nullptr;
     size_t cap_gat_src = 0, cap_gat_src_off = 0, cap_wgrad = 0;
+    // Hicks interpolation: receiver gathers run as their own kernel after each step
+    sa::HicksGather* hgat = nullptr;
+    size_t cap_hgat = 0;
     // layout
     int NT = 128, by = 110, chunk_rows = 1, nstrips = 1, nchunks = 1;
     bool layout_fixed = false;
@@ -204,6 +207,30 @@ void damping_table(int A, double h, double refl, float* out) {  // out: MAX_ABS 
     }
 }
 
+// Hicks coefficients of one axis (GridDevito._calculate_hicks, common/devito.py:843-885): Kaiser-
+// windowed sinc at offsets -3..3 from the base point (index 3 + offset; index 7 is zero), with the
+// reference's smoothing of the central coefficients for sources.
+void hicks_coefs(double frac, bool smooth, double c[8]) {
+    const double kb = 4.14, half = 3.0, ext = half / 0.99, den = std::cyl_bessel_i(0.0, kb);
+    for (int k = 0; k < 8; k++) c[k] = 0.0;
+    for (int gp = -3; gp <= 3; gp++) {
+        const double x = frac - gp;
+        double w = (x / ext) * (x / ext);
+        if (w > 1) w = 1;
+        const double sinc = x == 0.0 ? 1.0 : std::sin(M_PI * x) / (M_PI * x);
+        c[3 + gp] = sinc * std::cyl_bessel_i(0.0, kb * std::sqrt(1 - w)) / den;
+    }
+    if (smooth) {
+        const int m = 2;
+        const double a = c[m], b = c[m + 1], cc = c[m + 2];
+        c[m - 1] = c[m - 1] + a * 0.01;
+        c[m] = a * 0.98 + b * 0.03;
+        c[m + 1] = b * 0.94 + (a + cc) * 0.01;
+        c[m + 2] = cc * 0.98 + b * 0.03;
+        c[m + 3] = c[m + 3] + cc * 0.01;
+    }
+}
+
 void default_layout(sa_plan* p) {
     if (p->layout_fixed) return;
     int best_nt = 128, best_cost = 1 << 30;
@@ -239,10 +266,10 @@ struct HostInject {
 int build_lists_impl(sa_plan* p);
 int build_lists(sa_plan* p) {
     const void* before[] = {p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
-                            p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off};
+                            p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off, p->hgat};
     const int rc = build_lists_impl(p);
     const void* after[] = {p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
-                           p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off};
+                           p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off, p->hgat};
     for (size_t k = 0; k < sizeof(before) / sizeof(before[0]); k++)
         if (before[k] != after[k]) {
             drop_graphs(p);
@@ -259,18 +286,34 @@ int build_lists_impl(sa_plan* p) {
     // shots advance in pairs (the two lanes of a float2); CTA index of (pair, chunk, strip)
     auto cta_of = [&](int shot, int x, int y) { return ((shot / 2) * nc + x / p->chunk_rows) * ns + y / p->by; };
     // corner(x, y): the per-corner factor of the coefficient (vp, vp^2 or C1 W there)
+    // linear: the 4 corners; Hicks: the 8 x 8 support from base - 3 (smooth: the sources' smoothing)
+    const bool hicks = p->d.interpolation == SA_INTERP_HICKS;
     auto make_inj = [&](const std::vector<int>& off, const std::vector<int>& bx, const std::vector<int>& by,
                         const std::vector<double>& fx, const std::vector<double>& fy, double scale, auto corner,
-                        std::vector<HostInject>& out) {
+                        std::vector<HostInject>& out, bool smooth) {
         out.clear();
         for (int s = 0; s < p->n_shots; s++)
-            for (int i = off[s]; i < off[s + 1]; i++)
+            for (int i = off[s]; i < off[s + 1]; i++) {
+                if (hicks) {
+                    double cxs[8], cys[8];
+                    hicks_coefs(fx[i], smooth, cxs);
+                    hicks_coefs(fy[i], smooth, cys);
+                    for (int a = 0; a < 8; a++)
+                        for (int b = 0; b < 8; b++) {
+                            const double w = cxs[a] * cys[b];
+                            if (w == 0.0) continue;
+                            const int x = bx[i] - 3 + a, y = by[i] - 3 + b;
+                            out.push_back({cta_of(s, x, y), x, y, i, (float)(w * scale * corner(x, y)), s & 1});
+                        }
+                    continue;
+                }
                 for (int cx = 0; cx < 2; cx++)
                     for (int cy = 0; cy < 2; cy++) {
                         const int x = bx[i] + cx, y = by[i] + cy;
                         const double w = (cx ? fx[i] : 1.0 - fx[i]) * (cy ? fy[i] : 1.0 - fy[i]);
                         out.push_back({cta_of(s, x, y), x, y, i, (float)(w * scale * corner(x, y)), s & 1});
                     }
+            }
         std::stable_sort(out.begin(), out.end(), [](const HostInject& a, const HostInject& b) {
             return a.cta != b.cta ? a.cta < b.cta : a.row < b.row;
         });
@@ -298,13 +341,13 @@ int build_lists_impl(sa_plan* p) {
         return (double)(v * v);
     };
     auto c1w_at = [&](int x, int y) { return p->c1w_host.empty() ? 0.0 : (double)p->c1w_host[(size_t)x * p->ny + y]; };
-    make_inj(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, 2.0 * dt / h, vp_at, tmp);
+    make_inj(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, 2.0 * dt / h, vp_at, tmp, true);
     CKR(upload_inj(tmp, &p->inj_src, &p->cap_inj_src, &p->inj_src_off, &p->cap_inj_src_off));
     // adjoint receiver: -rec * dt^2 * vp^2 (devito.py:748-753), vp^2 at the corner
-    make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, -dt * dt, vp2_at, tmp);
+    make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, -dt * dt, vp2_at, tmp, false);
     CKR(upload_inj(tmp, &p->inj_rec, &p->cap_inj_rec, &p->inj_rec_off, &p->cap_inj_rec_off));
     // exact-gradient adjoint: dL/drec injected with the update's own C1 W at the corner
-    make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, 1.0, c1w_at, tmp);
+    make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, 1.0, c1w_at, tmp, false);
     CKR(upload_inj(tmp, &p->inj_recx, &p->cap_inj_recx, &p->inj_recx_off, &p->cap_inj_recx_off));
     {  // flat source list (pad = shot) for the exact gradient's source term
         std::vector<sa::Gather> sf;
@@ -365,6 +408,28 @@ int build_lists_impl(sa_plan* p) {
                      &p->cap_gat_off, &p->gat_flat, &p->cap_gat_flat));
     CKR(make_gathers(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, -1.f, &p->gat_src, &p->cap_gat_src,
                      &p->gat_src_off, &p->cap_gat_src_off, nullptr, nullptr));
+    if (hicks) {  // receivers gathered by their own kernel over the 8 x 8 support
+        std::vector<sa::HicksGather> hg;
+        for (int s = 0; s < p->n_shots; s++)
+            for (int r = p->rec_off[s]; r < p->rec_off[s + 1]; r++) {
+                sa::HicksGather G;
+                G.row = p->rec_bx[r] - 3;
+                G.col = p->rec_by[r] - 3;
+                G.point = r;
+                G.shot = s;
+                double cx[8], cy[8];
+                hicks_coefs(p->rec_fx[r], false, cx);
+                hicks_coefs(p->rec_fy[r], false, cy);
+                for (int k = 0; k < 8; k++) {
+                    G.wx[k] = (float)cx[k];
+                    G.wy[k] = (float)cy[k];
+                }
+                hg.push_back(G);
+            }
+        CKR(ensure(&p->hgat, &p->cap_hgat, hg.size()));
+        if (!hg.empty())
+            CK(cudaMemcpy(p->hgat, hg.data(), hg.size() * sizeof(sa::HicksGather), cudaMemcpyHostToDevice));
+    }
     return SA_OK;
 }
 
@@ -409,6 +474,7 @@ sa::Step2D base_args(const sa_plan* p) {
 // (p[t+1], p[t]) after every step t = kK, k = 1..ck_n, into checkpoint slot k-1.
 int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
     const bool save = mode == SA_SAVE_SNAPSHOTS;
+    const bool hicks = p->d.interpolation == SA_INTERP_HICKS;
     const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
     CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
     CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
@@ -429,9 +495,13 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
         a.t = t;
         a.cur = (t & 1) ? p->field[1] : p->field[0];
         a.prev = (t & 1) ? p->field[0] : p->field[1];
-        a.gat = (t >= 2 && p->n_rec) ? p->gat : nullptr;
+        a.gat = (t >= 2 && p->n_rec && !hicks) ? p->gat : nullptr;
         CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
         n++;
+        if (hicks && p->n_rec) {  // rec[t] = interp(p[t+1]) over the Hicks support
+            CK(sa::hicks_gather2d(a.prev, p->shot_stride, p->pitch, p->hgat, p->n_rec, p->rec_amp, p->n_rec, t, s));
+            n++;
+        }
         if (mode == SA_SAVE_CHECKPOINTS && t % p->ck_K == 0 && t / p->ck_K <= p->ck_n) {
             float* slot = p->ckpt + (size_t)(t / p->ck_K - 1) * 2 * (fbytes / sizeof(float));
             CK(cudaMemcpyAsync(slot, p->field[0], fbytes, cudaMemcpyDeviceToDevice, s));
@@ -441,7 +511,7 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
     // rec[nt-2] = interp(p[nt-1])
     const int tl = p->d.nt - 1;
     const float* last = (tl & 1) ? p->field[1] : p->field[0];
-    if (p->d.nt >= 3) {
+    if (p->d.nt >= 3 && !hicks) {
         CK(sa::final_gather2d(last, p->shot_stride, p->pitch, p->gat_flat, p->n_rec, p->rec_amp, p->n_rec, p->d.nt - 2,
                               s));
         n++;
@@ -752,6 +822,10 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
     if (d.kernel != SA_KERNEL_OT2 && d.kernel != SA_KERNEL_OT4)
         return fail(SA_E_INVALID, "Unrecognized kernel %d", d.kernel);
     if (d.density < 0 || d.density > 2) return fail(SA_E_INVALID, "density mode %d", d.density);
+    if (d.interpolation != SA_INTERP_LINEAR && d.interpolation != SA_INTERP_HICKS)
+        return fail(SA_E_INVALID, "interpolation %d", d.interpolation);
+    if (d.interpolation == SA_INTERP_HICKS && d.dim != 2)
+        return fail(SA_E_UNSUPPORTED, "Hicks interpolation is implemented for 2D plans");
     if (d.nt < 3 || d.undersampling < 1 || d.max_shots < 1) return fail(SA_E_INVALID, "nt/undersampling/max_shots");
     for (int a = 0; a < d.dim; a++) {
         if (d.shape[a] < 24) return fail(SA_E_INVALID, "shape[%d] = %d is below 24 cells", a, d.shape[a]);
@@ -846,7 +920,7 @@ int sa_plan_destroy(sa_plan* p) {
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
                     p->ones_g, p->zeros_g, p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off,
-                    p->wgrad};
+                    p->wgrad, p->hgat};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (p->cap) cudaStreamDestroy(p->cap);
@@ -911,6 +985,7 @@ int sa_set_geometry(sa_plan* p, int n_shots, const int* src_offsets, const float
     if ((ns && !src_xyz) || (nr && !rec_xyz)) return fail(SA_E_INVALID, "missing coordinates");
     if (p->p3) return sa::plan3d_set_geometry(p->p3, n_shots, src_offsets, src_xyz, rec_offsets, rec_xyz);
     const int dim = p->d.dim;
+    const bool hicks = p->d.interpolation == SA_INTERP_HICKS;
     auto convert = [&](const float* xyz, int n, std::vector<int>& bx, std::vector<int>& by, std::vector<double>& fx,
                        std::vector<double>& fy) -> int {
         bx.resize(n);
@@ -925,7 +1000,8 @@ int sa_set_geometry(sa_plan* p, int n_shots, const int* src_offsets, const float
                 rel[a] = ((double)xyz[i * dim + a] - origin) / p->d.spacing[a];
                 base[a] = (int)std::floor(rel[a]);
                 const int n_a = a == 0 ? p->nx : p->ny;
-                if (!(base[a] >= 0 && base[a] + 1 <= n_a - 1))
+                const int lo = hicks ? 3 : 0, hi = hicks ? 4 : 1;  // support base-lo .. base+hi
+                if (!(base[a] - lo >= 0 && base[a] + hi <= n_a - 1))
                     return fail(SA_E_INVALID, "point %d lies outside the grid along axis %d", i, a);
             }
             bx[i] = base[0];
@@ -998,6 +1074,8 @@ int sa_adjoint_wavelets(sa_plan* p, const float* residuals, float* grad_vp, floa
     const bool exact = grad_mode == SA_GRAD_EXACT;
     const bool wav = grad_wavelets != nullptr;
     if (wav && exact) return fail(SA_E_UNSUPPORTED, "the wavelet gradient is the parity mode's (src.interpolate(-p_a))");
+    if ((wav || exact) && p->d.interpolation == SA_INTERP_HICKS)
+        return fail(SA_E_UNSUPPORTED, "wavelet and exact gradients use linear interpolation");
     if (p->p3) {
         if (wav) return fail(SA_E_UNSUPPORTED, "the wavelet gradient is implemented for 2D plans");
         if (exact) return fail(SA_E_UNSUPPORTED, "SA_GRAD_EXACT is implemented for 2D plans");

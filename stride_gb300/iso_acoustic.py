@@ -32,7 +32,7 @@ except Exception:  # noqa: BLE001
 DB_TO_NEPER = 100 * (1e-6 / (2 * np.pi)) ** 0 / (20 * np.log10(np.exp(1)))
 SUPPORTED_BOUNDARIES = ('sponge_boundary_2',)
 KNOWN_BOUNDARIES = ('sponge_boundary_2', 'complex_frequency_shift_PML_2', 'sponge_boundary_1')
-SUPPORTED_INTERPOLATION = ('linear',)
+SUPPORTED_INTERPOLATION = ('linear', 'hicks')
 KNOWN_INTERPOLATION = ('linear', 'hicks', 'sinc')
 
 
@@ -155,7 +155,7 @@ class IsoAcousticGB300(ProblemTypeBase):
         if boundary_type not in SUPPORTED_BOUNDARIES:
             raise NotImplementedError('boundary_type %s is not implemented in this build' % boundary_type)
         self.boundary_type = boundary_type
-        interpolation_type = kwargs.get('interpolation_type', 'linear')
+        interpolation_type = kwargs.get('interpolation_type', self.interpolation_type)
         if interpolation_type not in KNOWN_INTERPOLATION:
             raise ValueError('Only "linear" and "hicks" interpolations are allowed.')
         if interpolation_type not in SUPPORTED_INTERPOLATION:
@@ -231,13 +231,14 @@ class IsoAcousticGB300(ProblemTypeBase):
     def _get_plan(self, vp, rho, alpha, n_shots=1):
         space, time = self.space, self.time
         key = (space.extended_shape, space.spacing, space.extra, space.absorbing, time.step, time.extended_num,
-               self.kernel, self._density_mode(rho), alpha is not None, self.undersampling_factor, n_shots)
+               self.kernel, self._density_mode(rho), alpha is not None, self.undersampling_factor, n_shots,
+               self.interpolation_type)
         plan = self._plans.get(key)
         if plan is None:
             plan = _lib.Plan(space.dim, space.extended_shape, space.spacing, space.extra, space.absorbing,
                              time.step, time.extended_num, kernel=self.kernel, density=key[7],
                              attenuation=alpha is not None, undersampling=self.undersampling_factor,
-                             max_shots=n_shots)
+                             max_shots=n_shots, interpolation=self.interpolation_type)
             self._plans = {key: plan}  # one live plan: the previous one's device memory is released
         self._plan = plan
         return plan

@@ -101,3 +101,36 @@ def test_wavelet_gradient_parity():
     C.gpu_forward(c, plan=plan, save=True)
     plan.adjoint(resw, g2, np.zeros_like(prec))
     assert np.array_equal(grad, g2)
+
+
+@pytest.mark.parametrize('density', ['none', 'variable'])
+def test_hicks_interpolation_parity(density):
+    """Hicks (Kaiser-windowed sinc) sources and receivers: traces and the vp gradient against the
+    NumPy oracle with the same interpolation."""
+    from oracle import numpy_oracle as npo
+    c = C.small_case(kernel='OT4', density=density, alpha=True, n_shots=2, uneven=True, nt=200, inner=48)
+    plan = C.make_plan(c, interpolation='hicks')
+    got, plan = C.gpu_forward(c, plan=plan, save=True)
+    origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
+    snaps_all = []
+    for s in range(2):
+        wav = np.tile(c['wav'][None], (len(c['srcs'][s]), 1))
+        ref, snaps = npo.forward(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][s], c['recs'][s],
+                                 wav, origin, rho=c['rho'], alpha=c['alpha'], kernel='OT4', save=True,
+                                 interpolation='hicks')
+        assert np.abs(ref).max() > 0
+        assert C.rel_l2(got[s], ref) <= 1e-4
+        snaps_all.append(snaps)
+    rng = np.random.default_rng(8)
+    res = [rng.standard_normal(g.shape).astype(np.float32) * np.abs(g).max() for g in got]
+    resw = np.ascontiguousarray((np.concatenate(res).astype(np.float64) * C.window(c['nt'])[None, :]).astype(np.float32))
+    grad = np.zeros(c['vp'].shape, np.float32)
+    prec = np.zeros(c['vp'].shape, np.float32)
+    plan.adjoint(resw, grad, prec)
+    g_ref = np.zeros(c['vp'].shape)
+    for s in range(2):
+        g, _ = npo.adjoint(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['recs'][s], res[s], origin,
+                           snaps_all[s], rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation='hicks')
+        g_ref += g
+    assert C.cosine(grad, g_ref) >= 0.999
+    assert C.rel_l2(grad, g_ref) <= 1e-3
