@@ -33,7 +33,7 @@ def test_kernel_selection_matches_reference_rule():
     (dict(boundary_type='nonsense'), ValueError),
     (dict(boundary_type='complex_frequency_shift_PML_2'), NotImplementedError),
     (dict(interpolation_type='cubic'), ValueError),
-    (dict(interpolation_type='hicks'), NotImplementedError),
+    (dict(interpolation_type='sinc'), NotImplementedError),
     (dict(kernel='OT6'), ValueError),
 ])
 def test_option_errors(kw, exc):
