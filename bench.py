@@ -290,7 +290,7 @@ def fwi_arm(args):
 
     def med(key):
         v = [r[key] if r[key] is not None else float('inf') for r in rows]
-        return float(statistics.median(v))
+        return float(statistics.median(v)) if v else None
 
     line = {
         'metric': METRIC['fwi'], 'value': med('learned_s'), 'unit': 's', 'n_gpus': 1, 'steps': len(rows),
