@@ -3,7 +3,7 @@
 // A and B bf16 with K contiguous, C fp32 (optionally also written as bf16).
 //
 // One CTA of 128 threads computes a 128 x BN tile. K advances in 64-wide chunks staged in shared
-// memory (two stages, 16-byte cp.async) in the no-swizzle K-major canonical layout: 8-row x
+// memory (3-4 stages, 16-byte cp.async) in the no-swizzle K-major canonical layout: 8-row x
 // 16-byte core matrices, the core matrices of one 8-wide k group stacked along M (stride 128 B),
 // k groups one after another (stride rows * 16 B). Thread 0 issues four kind::f16 MMAs (K = 16
 // each) per chunk into a TMEM accumulator of BN fp32 columns and commits them to the stage's
@@ -58,7 +58,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-template <int BN>
+template <int BN, int NS>
 __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restrict__ A, int lda,
                                                    const __nv_bfloat16* __restrict__ B, int ldb, float* C, int ldc,
                                                    __nv_bfloat16* Cb, int ldcb, int K, const float* __restrict__ bias,
@@ -67,17 +67,16 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
     constexpr int B_BYTES = BN * kBK * 2;
     constexpr int STAGE = A_BYTES + B_BYTES;
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ __align__(8) uint64_t bars[NS];  // one per stage: its MMAs have finished reading it
     __shared__ uint32_t tmem_base_sh;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
     const uint32_t sbase = smem_u32(smem);
-    const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
+    auto bar = [&](int st) { return smem_u32(&bars[st]); };
 
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar1));
+        for (int st = 0; st < NS; st++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar(st)));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     if (warp == 0) {
@@ -118,23 +117,25 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
     const bool split = gridDim.z > 1;
     constexpr uint32_t idesc = idesc_bf16(kBM, BN);
     bool ok = true;
-    int issued[2] = {0, 0};  // commits made to each stage's barrier (thread 0)
-    if (nk > 0) load(kb0, 0);
+    int issued = 0;  // MMA chunks committed (thread 0); chunk i commits to bar(i % NS)
+    // prologue: chunks 0 .. NS-2 in flight (one commit group each, empty past the end)
+    for (int i = 0; i < NS - 1; i++) {
+        if (i < nk) load(kb0 + i, i);
+        else asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
     for (int i = 0; i < nk && ok; i++) {
         const int kb = kb0 + i;
-        const int st = i & 1;
-        if (i + 1 < nk) {
-            const int s1 = (i + 1) & 1;
-            if (i + 1 >= 2) {  // the MMAs of chunk i-1 read stage s1: wait for their commit
-                if (!mbar_wait(s1 ? bar1 : bar0, (uint32_t)(((i - 1) >> 1) & 1))) {
-                    ok = false;
-                }
-            }
-            if (ok) load(kb + 1, s1);
-            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        const int st = i % NS;
+        // refill the stage chunk i-1 used with chunk i+NS-1, once chunk i-1's MMAs are done
+        if (i + NS - 1 < nk) {
+            const int s1 = (i + NS - 1) % NS;
+            if (i >= 1 && !mbar_wait(bar(s1), (uint32_t)(((i - 1) / NS) & 1))) ok = false;
+            if (ok) load(kb + NS - 1, s1);
+            else asm volatile("cp.async.commit_group;\n" ::: "memory");
         } else {
-            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
         }
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(NS - 1) : "memory");  // chunk i has landed
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
         ok = __syncthreads_and(ok ? 1 : 0) != 0;
@@ -155,16 +156,18 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
                     "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                             st ? bar1 : bar0)
+                             bar(st))
                          : "memory");
-            issued[st]++;
+            issued++;
         }
     }
-    // wait for every committed MMA (each barrier's last phase), bounded
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    // wait for every committed MMA: the last commit of each stage's barrier, bounded (a commit
+    // tracks all earlier tcgen05 operations of the thread, so the last chunk's suffices)
     bool done = true;
-    if (tid == 0) {
-        for (int s = 0; s < 2; s++)
-            if (issued[s] > 0 && !mbar_wait(s ? bar1 : bar0, (uint32_t)((issued[s] - 1) & 1))) done = false;
+    if (tid == 0 && issued > 0) {
+        const int last = issued - 1;
+        if (!mbar_wait(bar(last % NS), (uint32_t)((last / NS) & 1))) done = false;
     }
     ok = __syncthreads_and((ok && (tid != 0 || done)) ? 1 : 0) != 0;
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
@@ -211,17 +214,20 @@ template <int BN>
 cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C, int ldc,
                    __nv_bfloat16* Cb, int ldcb, int M, int N, int K, const float* bias, int relu, int accumulate,
                    int ksplit, int* err, cudaStream_t s) {
-    const size_t bytes = 2 * (size_t)(kBM * kBK * 2 + BN * kBK * 2);
+    constexpr int NS = BN >= 128 ? 3 : 4;  // stages: 96 KB (BN 128) or <= 96 KB (BN <= 64) of shared memory
+    const size_t bytes = NS * (size_t)(kBM * kBK * 2 + BN * kBK * 2);
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_umma_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        cudaError_t e =
+            cudaFuncSetAttribute(k_umma_gemm<BN, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
         if (e != cudaSuccess) return e;
         configured = true;
     }
     const int nk = (K + kBK - 1) / kBK;
     const int per = (nk + ksplit - 1) / ksplit;
     const dim3 grid(M / kBM, N / BN, (nk + per - 1) / per);
-    k_umma_gemm<BN><<<grid, 128, bytes, s>>>(A, lda, B, ldb, C, ldc, Cb, ldcb, K, bias, relu, accumulate, per, err);
+    k_umma_gemm<BN, NS><<<grid, 128, bytes, s>>>(A, lda, B, ldb, C, ldc, Cb, ldcb, K, bias, relu, accumulate, per,
+                                                 err);
     return cudaGetLastError();
 }
 
