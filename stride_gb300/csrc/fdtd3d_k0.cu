@@ -6,7 +6,7 @@
 namespace sa {
 
 namespace {
-constexpr int TY = 8, TZ = 32, RB = 2, PF = 1;
+constexpr int TY = kTile3dY, TZ = kTile3dZ, RB = 2, PF = 1;
 
 template <bool FINAL, bool OT4>
 cudaError_t go(dim3 grid, cudaStream_t s, const Step3D& a) {

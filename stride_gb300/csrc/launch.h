@@ -11,7 +11,13 @@ struct Step3D;
 cudaError_t launch_step3d_k0(bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
 cudaError_t launch_step3d_k1(bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
 cudaError_t launch_step3d_k2(bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
-constexpr int kTile3dY = 8, kTile3dZ = 32;  // (y, z) tile of a 3D CTA (threads = their product)
+#ifndef SA_TY3
+#define SA_TY3 16
+#endif
+#ifndef SA_TZ3
+#define SA_TZ3 32
+#endif
+constexpr int kTile3dY = SA_TY3, kTile3dZ = SA_TZ3;  // (y, z) tile of a 3D CTA (threads = their product)
 
 inline cudaError_t launch_step3d(int kind, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a) {
     switch (kind) {

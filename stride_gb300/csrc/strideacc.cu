@@ -1157,7 +1157,7 @@ int sa_adjoint_wavelets(sa_plan* p, const float* residuals, float* grad_vp, floa
 }
 
 int sa_autotune(sa_plan* p, void* stream) {
-    if (p && p->p3) return SA_OK;  // 3D plans use a fixed tile (8 x 32 columns per CTA)
+    if (p && p->p3) return SA_OK;  // 3D plans use a fixed tile (kTile3dY x kTile3dZ columns per CTA)
     if (!p || !p->geometry_set || !p->medium_set) return fail(SA_E_INVALID, "autotune needs medium and geometry");
     cudaStream_t s = (cudaStream_t)stream;
     const int S = p->ot4 ? 2 : 1;
