@@ -57,7 +57,6 @@ struct Gather {
 struct Step2D {
     int nx, ny, pitch;        // extended grid, row pitch (columns)
     long long shot_stride;    // float2 elements per shot pair in a field buffer (nx * pitch)
-    long long grad_stride;    // floats per shot pair in the gradient buffers (nx * pitch)
     int chunk_rows;           // output rows per CTA
     int by;                   // output columns per CTA (even, <= Cols2D::BYMAX)
     int t;                    // time index of the current level (cur = p[t])
@@ -85,12 +84,8 @@ struct Step2D {
     // wavefield save (forward) / imaging condition (adjoint)
     int f;                    // undersampling factor
     int save;                 // forward: store p.dt2 on t % f == 0
-    int grad;                 // adjoint: accumulate grad/prec on t % f == 0
     float* snaps;             // [pairs][n_snap][nx][pitch][2]
     long long snap_shot_stride, snap_stride;  // in float2 elements: per pair, per snapshot
-    float* gradb;             // [pairs][nx][pitch], both shots of a pair summed
-    float* precb;
-    int ix0, ix1, iy0, iy1;   // interior (imaging condition) bounds
 };
 
 }  // namespace sa

@@ -215,7 +215,6 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
     }
     int inj_ptr = inj_b, gat_ptr = gat_b;
     const bool do_save = a.save && (a.t % a.f == 0);
-    const bool do_grad = a.grad && (a.t % a.f == 0);
 
 #pragma unroll 1
     for (int k = 0; k < PF; k++) prefetch(i0 + k * RB, wrapU(k * RB % QU));
@@ -409,16 +408,10 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
                         else pn.x = pn.x + amp;
                     }
                 }
-                float2* snap = reinterpret_cast<float2*>(a.snaps) + (long long)pair * a.snap_shot_stride +
-                               (long long)(a.t / a.f) * a.snap_stride + idx;
                 if (do_save) {
+                    float2* snap = reinterpret_cast<float2*>(a.snaps) + (long long)pair * a.snap_shot_stride +
+                                   (long long)(a.t / a.f) * a.snap_stride + idx;
                     *snap = make_float2((pn.x - 2.f * u_o.x + pm.x) / dt2, (pn.y - 2.f * u_o.y + pm.y) / dt2);
-                }
-                if (do_grad && orow >= a.ix0 && orow < a.ix1 && c >= a.iy0 && c < a.iy1) {
-                    const float2 sv = *snap;
-                    const long long gi = (long long)pair * a.grad_stride + (long long)orow * pitch + c;
-                    a.gradb[gi] += sv.x * u_o.x + sv.y * u_o.y;
-                    a.precb[gi] += sv.x * sv.x + sv.y * sv.y;
                 }
                 prev[idx] = pn;
             }

@@ -40,13 +40,10 @@ struct Step3D {
     const float* C2;
     const float* C3;
     float hx, hy, hz, dt;
-    // save / imaging condition
-    int f, save, grad;
+    // wavefield save
+    int f, save;
     float* snaps;             // [shots][n_snap][nx][ny][zp]
     long long snap_shot_stride, snap_stride;
-    float* gradb;             // [shots][nx][ny][zp]
-    float* precb;
-    int ix0, ix1, iy0, iy1, iz0, iz1;
 };
 
 template <int KIND, int TY, int TZ, int RB, int PF>
@@ -153,7 +150,6 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
         if constexpr (STAG) fq[k] = 0.f;
     }
     const bool do_save = FINAL && a.save && (a.t % a.f == 0);
-    const bool do_grad = FINAL && a.grad && (a.t % a.f == 0);
 
 #pragma unroll 1
     for (int k = 0; k < PF; k++) prefetch(i0 + k * RB);
@@ -281,12 +277,6 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
                 if (do_save) {
                     a.snaps[(long long)shot * a.snap_shot_stride + (long long)(a.t / a.f) * a.snap_stride + idx] =
                         (pn - 2.f * u_o + pm) / dt2;
-                }
-                if (do_grad && row >= a.ix0 && row < a.ix1 && y >= a.iy0 && y < a.iy1 && z >= a.iz0 && z < a.iz1) {
-                    const float sv =
-                        a.snaps[(long long)shot * a.snap_shot_stride + (long long)(a.t / a.f) * a.snap_stride + idx];
-                    a.gradb[soff + idx] += sv * u_o;
-                    a.precb[soff + idx] += sv * sv;
                 }
                 a.prev[soff + idx] = pn;
             }

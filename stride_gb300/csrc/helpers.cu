@@ -1,3 +1,4 @@
+#include <algorithm>
 // Small device helpers of the plan: medium preparation, sparse-trace transposes, the final
 // receiver gather and the reduction of per-shot gradients.
 #include "fdtd2d.cuh"
@@ -136,6 +137,37 @@ cudaError_t hicks_gather2d(const float* field, long long shot_stride, int pitch,
                            int ld, int trow, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_hicks_gather2d<<<(n + 127) / 128, 128, 0, s>>>(field, shot_stride, pitch, g, n, out, ld, trow);
+    return cudaGetLastError();
+}
+
+// Imaging condition of one adjoint level t (t % f == 0), interior only: grad[pair] += snap . q,
+// prec[pair] += snap . snap (both shots of a pair summed), q = p_a[t] (pair-interleaved).
+__global__ void k_image2d(const float2* __restrict__ q, const float2* __restrict__ snap, float* gradb, float* precb,
+                          int ix0, int ix1, int iy0, int iy1, int pitch, int npairs, long long shot_stride,
+                          long long snap_shot_stride) {
+    const int w = iy1 - iy0;
+    const long long per = (long long)(ix1 - ix0) * w;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < per * npairs;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int pair = (int)(e / per);
+        const long long r = e - (long long)pair * per;
+        const int x = ix0 + (int)(r / w), y = iy0 + (int)(r % w);
+        const long long idx = (long long)x * pitch + y;
+        const float2 sv = snap[(long long)pair * snap_shot_stride + idx];
+        const float2 u = q[(long long)pair * shot_stride + idx];
+        const long long gi = (long long)pair * shot_stride + idx;
+        gradb[gi] += sv.x * u.x + sv.y * u.y;
+        precb[gi] += sv.x * sv.x + sv.y * sv.y;
+    }
+}
+
+cudaError_t image2d(const float* q, const float* snap, float* gradb, float* precb, int ix0, int ix1, int iy0, int iy1,
+                    int pitch, int npairs, long long shot_stride, long long snap_shot_stride, cudaStream_t s) {
+    const long long n = (long long)(ix1 - ix0) * (iy1 - iy0) * npairs;
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 8);
+    k_image2d<<<blocks, 256, 0, s>>>(reinterpret_cast<const float2*>(q), reinterpret_cast<const float2*>(snap), gradb,
+                                     precb, ix0, ix1, iy0, iy1, pitch, npairs, shot_stride, snap_shot_stride);
     return cudaGetLastError();
 }
 

@@ -39,9 +39,13 @@ cudaError_t sparse3d_inject(const Sparse3D& sp, int n, const float* amp, int ld,
                             long long snap_off, float inv_dt2, cudaStream_t s);
 cudaError_t sparse3d_gather(const Sparse3D& sp, int n, const float* field, long long shot_stride, int ny, int zp,
                             float* out, int ld, int trow, cudaStream_t s);
+cudaError_t image3d(const float* q, const float* snap, float* gradb, float* precb, const int* lo, const int* hi,
+                    int ny, int zp, int nshots, long long field, long long snap_shot_stride, cudaStream_t s);
 cudaError_t reduce3d(const float* buf, long long shot_stride, int nshots, int nx, int ny, int nz, int zp, float* out,
                      cudaStream_t s);
 cudaError_t transpose(const float* in, int rows, int cols, float* out, cudaStream_t s);
+cudaError_t image2d(const float* q, const float* snap, float* gradb, float* precb, int ix0, int ix1, int iy0, int iy1,
+                    int pitch, int npairs, long long shot_stride, long long snap_shot_stride, cudaStream_t s);
 cudaError_t hicks_gather2d(const float* field, long long shot_stride, int pitch, const HicksGather* g, int n, float* out,
                            int ld, int trow, cudaStream_t s);
 cudaError_t final_gather2d(const float* field, long long shot_stride, int pitch, const Gather* g, int n, float* out,

@@ -1,3 +1,4 @@
+#include <algorithm>
 // Device helpers of 3D plans: medium preparation, sparse injection / interpolation and the
 // reduction of per-shot gradients. Layout [x][y][zp], z contiguous.
 #include "fdtd3d.cuh"
@@ -153,6 +154,39 @@ cudaError_t sparse3d_gather(const Sparse3D& sp, int n, const float* field, long 
                             float* out, int ld, int trow, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     gather3d<<<(n + 127) / 128, 128, 0, s>>>(sp, n, field, shot_stride, ny, zp, out, ld, trow);
+    return cudaGetLastError();
+}
+
+// Imaging condition of one adjoint level (t % f == 0), interior only, per shot:
+// grad += snap q, prec += snap^2, q = p_a[t].
+__global__ void k_image3d(const float* __restrict__ q, const float* __restrict__ snap, float* gradb, float* precb,
+                          int ix0, int ix1, int iy0, int iy1, int iz0, int iz1, int ny, int zp, int nshots,
+                          long long field, long long snap_shot_stride) {
+    const int wz = iz1 - iz0, wy = iy1 - iy0;
+    const long long per = (long long)(ix1 - ix0) * wy * wz;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < per * nshots;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int shot = (int)(e / per);
+        long long r = e - (long long)shot * per;
+        const int z = iz0 + (int)(r % wz);
+        r /= wz;
+        const int y = iy0 + (int)(r % wy);
+        const int x = ix0 + (int)(r / wy);
+        const long long idx = ((long long)x * ny + y) * zp + z;
+        const float sv = snap[(long long)shot * snap_shot_stride + idx];
+        const long long gi = (long long)shot * field + idx;
+        gradb[gi] += sv * q[gi];
+        precb[gi] += sv * sv;
+    }
+}
+
+cudaError_t image3d(const float* q, const float* snap, float* gradb, float* precb, const int* lo, const int* hi,
+                    int ny, int zp, int nshots, long long field, long long snap_shot_stride, cudaStream_t s) {
+    const long long n = (long long)(hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]) * nshots;
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 16);
+    k_image3d<<<blocks, 256, 0, s>>>(q, snap, gradb, precb, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], ny, zp, nshots,
+                                     field, snap_shot_stride);
     return cudaGetLastError();
 }
 

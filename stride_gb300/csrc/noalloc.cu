@@ -312,7 +312,6 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
     a.ny = ny;
     a.pitch = pitch;
     a.shot_stride = pe;
-    a.grad_stride = pe;
     a.chunk_rows = chunk_rows;
     a.by = by;
     a.W = W + g0;

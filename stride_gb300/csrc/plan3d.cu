@@ -350,15 +350,18 @@ static Step3D args3(const Plan3D* p) {
     a.snaps = p->snaps;
     a.snap_stride = p->snap_stride;
     a.snap_shot_stride = (long long)p->n_snap * p->snap_stride;
-    a.gradb = p->gradb;
-    a.precb = p->precb;
-    a.ix0 = p->d.absorbing[0];
-    a.ix1 = p->nx - p->d.absorbing[0];
-    a.iy0 = p->d.absorbing[1];
-    a.iy1 = p->ny - p->d.absorbing[1];
-    a.iz0 = p->d.absorbing[2];
-    a.iz1 = p->nz - p->d.absorbing[2];
     return a;
+}
+
+// Imaging condition of adjoint level t (t % f == 0) as its own streaming kernel, q = p_a[t].
+static int image_level(Plan3D* p, const Step3D& a, const float* q, cudaStream_t s, long long& n) {
+    if (a.t % a.f) return SA_OK;
+    const int lo[3] = {p->d.absorbing[0], p->d.absorbing[1], p->d.absorbing[2]};
+    const int hi[3] = {p->nx - p->d.absorbing[0], p->ny - p->d.absorbing[1], p->nz - p->d.absorbing[2]};
+    CK3(image3d(q, a.snaps + (long long)(a.t / a.f) * a.snap_stride, p->gradb, p->precb, lo, hi, p->ny, p->zp,
+                p->n_shots, p->field, a.snap_shot_stride, s));
+    n++;
+    return SA_OK;
 }
 
 // One time level: [pass A] + pass B, then injection into the new level (and its snapshot).
@@ -414,7 +417,6 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
     CK3(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * std::max(1, p->n_rec) * sizeof(float), s));
     Step3D a = args3(p);
     a.save = save ? 1 : 0;
-    a.grad = 0;
     const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
     const Sparse3D rec{p->r_shot, p->r_base, p->r_w, p->r_coef};
     long long n = p->n_src ? 1 : 0;
@@ -468,7 +470,6 @@ static int adjoint_segments(Plan3D* p, Step3D& aa, const Sparse3D& rec, cudaStre
     CK3(cudaMemsetAsync(p->A[1], 0, lb, s));
     Step3D fa = args3(p);
     fa.save = 1;
-    fa.grad = 0;
     fa.snap_shot_stride = aa.snap_shot_stride = (long long)(K / f) * p->snap_stride;
     const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
     for (int k = T0 >= 1 ? (T0 - 1) / K : -1; k >= 0; k--) {
@@ -498,6 +499,7 @@ static int adjoint_segments(Plan3D* p, Step3D& aa, const Sparse3D& rec, cudaStre
             int rc = step3(p, aa, even ? p->A[1] : p->A[0], even ? p->A[0] : p->A[1], rec, p->n_rec, p->rec_amp,
                            false, s, n);
             if (rc != SA_OK) return rc;
+            if ((rc = image_level(p, aa, even ? p->A[1] : p->A[0], s, n)) != SA_OK) return rc;
         }
     }
     return SA_OK;
@@ -528,7 +530,6 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
     CK3(cudaMemsetAsync(p->precb, 0, fb, s));
     Step3D a = args3(p);
     a.save = 0;
-    a.grad = 1;
     const Sparse3D rec{p->r_shot, p->r_base, p->r_w, p->r_coef};
     const int T0 = p->d.nt - 1 - p->d.undersampling;
     long long n = p->n_rec ? 1 : 0;
@@ -540,6 +541,7 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
         float* prev = even ? p->F[0] : p->F[1];
         rc = step3(p, a, cur, prev, rec, p->n_rec, p->rec_amp, false, s, n);
         if (rc != SA_OK) return rc;
+        if ((rc = image_level(p, a, cur, s, n)) != SA_OK) return rc;
     }
     const size_t N = (size_t)p->nx * p->ny * p->nz;
     for (int k = 0; k < 2; k++) {
