@@ -171,6 +171,26 @@ cudaError_t image2d(const float* q, const float* snap, float* gradb, float* prec
     return cudaGetLastError();
 }
 
+// field[idx[k]] += sum over the target's entries of coef[e] * amp[t][point[e]] (one thread per
+// target point; entries in a fixed order).
+__global__ void k_inject_targets2d(float* field, const long long* __restrict__ idx, const int* __restrict__ off,
+                                   const float* __restrict__ coef, const int* __restrict__ point, int n,
+                                   const float* __restrict__ amp, int ld, int t) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    float v = 0.f;
+    const float* a = amp + (long long)t * ld;
+    for (int e = off[k]; e < off[k + 1]; e++) v += coef[e] * a[point[e]];
+    field[idx[k]] += v;
+}
+
+cudaError_t inject_targets2d(float* field, const long long* idx, const int* off, const float* coef, const int* point,
+                             int n, const float* amp, int ld, int t, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_inject_targets2d<<<(n + 255) / 256, 256, 0, s>>>(field, idx, off, coef, point, n, amp, ld, t);
+    return cudaGetLastError();
+}
+
 __global__ void reduce_shots2d(const float* __restrict__ buf, long long shot_stride, int nshots, int nx, int ny,
                                int pitch, float* __restrict__ out) {
     const long long n = (long long)nx * ny;

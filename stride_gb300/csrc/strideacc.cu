@@ -150,6 +150,12 @@ struct sa_plan {
     // Hicks interpolation: receiver gathers run as their own kernel after each step
     sa::HicksGather* hgat = nullptr;
     size_t cap_hgat = 0;
+    // adjoint receiver injection grouped by target point (its own kernel after each adjoint step)
+    long long* rtgt_idx = nullptr;
+    int *rtgt_off = nullptr, *rtgt_point = nullptr;
+    float* rtgt_coef = nullptr;
+    size_t cap_rtgt_idx = 0, cap_rtgt_off = 0, cap_rtgt_point = 0, cap_rtgt_coef = 0;
+    int n_rtgt = 0;
     // layout
     int NT = 128, by = 110, chunk_rows = 1, nstrips = 1, nchunks = 1;
     bool layout_fixed = false;
@@ -266,10 +272,14 @@ struct HostInject {
 int build_lists_impl(sa_plan* p);
 int build_lists(sa_plan* p) {
     const void* before[] = {p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
-                            p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off, p->hgat};
+                            p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off, p->hgat,
+                            p->rtgt_idx, p->rtgt_off, p->rtgt_point, p->rtgt_coef};
+    const int n_before = p->n_rtgt;
     const int rc = build_lists_impl(p);
     const void* after[] = {p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
-                           p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off, p->hgat};
+                           p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off, p->hgat,
+                           p->rtgt_idx, p->rtgt_off, p->rtgt_point, p->rtgt_coef};
+    if (n_before != p->n_rtgt) drop_graphs(p);  // the injection kernel's launch size is captured
     for (size_t k = 0; k < sizeof(before) / sizeof(before[0]); k++)
         if (before[k] != after[k]) {
             drop_graphs(p);
@@ -346,6 +356,39 @@ int build_lists_impl(sa_plan* p) {
     // adjoint receiver: -rec * dt^2 * vp^2 (devito.py:748-753), vp^2 at the corner
     make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, -dt * dt, vp2_at, tmp, false);
     CKR(upload_inj(tmp, &p->inj_rec, &p->cap_inj_rec, &p->inj_rec_off, &p->cap_inj_rec_off));
+    {  // the same entries grouped by target point for the adjoint's injection kernel (one thread per
+       // target, entries summed in a fixed order: deterministic without atomics)
+        std::vector<std::pair<long long, size_t>> keyed(tmp.size());
+        for (size_t k = 0; k < tmp.size(); k++) {
+            const long long pair = tmp[k].cta / (nc * ns);
+            keyed[k] = {2 * (pair * p->shot_stride + (long long)tmp[k].row * p->pitch + tmp[k].col) + tmp[k].lane, k};
+        }
+        std::stable_sort(keyed.begin(), keyed.end(),
+                         [](const auto& a, const auto& b) { return a.first < b.first; });
+        std::vector<long long> tidx;
+        std::vector<int> toff, tpoint;
+        std::vector<float> tcoef;
+        for (size_t k = 0; k < keyed.size(); k++) {
+            if (k == 0 || keyed[k].first != keyed[k - 1].first) {
+                tidx.push_back(keyed[k].first);
+                toff.push_back((int)k);
+            }
+            tcoef.push_back(tmp[keyed[k].second].coef);
+            tpoint.push_back(tmp[keyed[k].second].point);
+        }
+        toff.push_back((int)keyed.size());
+        p->n_rtgt = (int)tidx.size();
+        CKR(ensure(&p->rtgt_idx, &p->cap_rtgt_idx, tidx.size()));
+        CKR(ensure(&p->rtgt_off, &p->cap_rtgt_off, toff.size()));
+        CKR(ensure(&p->rtgt_coef, &p->cap_rtgt_coef, tcoef.size()));
+        CKR(ensure(&p->rtgt_point, &p->cap_rtgt_point, tpoint.size()));
+        if (!tidx.empty()) {
+            CK(cudaMemcpy(p->rtgt_idx, tidx.data(), tidx.size() * sizeof(long long), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(p->rtgt_coef, tcoef.data(), tcoef.size() * sizeof(float), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(p->rtgt_point, tpoint.data(), tpoint.size() * sizeof(int), cudaMemcpyHostToDevice));
+        }
+        CK(cudaMemcpy(p->rtgt_off, toff.data(), toff.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
     // exact-gradient adjoint: dL/drec injected with the update's own C1 W at the corner
     make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, 1.0, c1w_at, tmp, false);
     CKR(upload_inj(tmp, &p->inj_recx, &p->cap_inj_recx, &p->inj_recx_off, &p->cap_inj_recx_off));
@@ -526,6 +569,16 @@ void wavelet_gather(const sa_plan* p, sa::Step2D& a, bool wav) {
 // The imaging condition (grad += snap q, prec += snap^2, interior, t % f == 0) runs as its own
 // streaming kernel after the step of level t: in the step kernel's epilogue its dependent loads
 // stalled the adjoint (6 % slower overall).
+// Adjoint receiver injection into the new level q[t-1] (devito.py:748-753): res[t] at every
+// target point, its entries summed in a fixed order.
+int inject_receivers(const sa_plan* p, float* level, int t, cudaStream_t s, long long& n) {
+    if (!p->n_rtgt) return SA_OK;
+    CK(sa::inject_targets2d(level, p->rtgt_idx, p->rtgt_off, p->rtgt_coef, p->rtgt_point, p->n_rtgt, p->rec_amp,
+                            p->n_rec, t, s));
+    n++;
+    return SA_OK;
+}
+
 int image_step(const sa_plan* p, const float* q, const float* snaps_base, long long snap_shot_stride, int t,
                cudaStream_t s, long long& n) {
     const int f = p->d.undersampling;
@@ -545,10 +598,7 @@ int issue_adjoint(sa_plan* p, bool wav, cudaStream_t s) {
     CK(cudaMemsetAsync(p->gradb, 0, gbytes, s));
     CK(cudaMemsetAsync(p->precb, 0, gbytes, s));
     sa::Step2D a = base_args(p);
-    a.inj = p->n_rec ? p->inj_rec : nullptr;
-    a.inj_off = p->inj_rec_off;
-    a.inj_amp = p->rec_amp;
-    a.inj_ld = p->n_rec;
+    a.inj = nullptr;  // receivers are injected by inject_targets2d after the step
     a.gat = nullptr;
     a.save = 0;
     if (wav) CK(cudaMemsetAsync(p->wgrad, 0, (size_t)p->d.nt * p->n_src * sizeof(float), s));
@@ -563,6 +613,7 @@ int issue_adjoint(sa_plan* p, bool wav, cudaStream_t s) {
         a.prev = even ? p->field[0] : p->field[1];
         CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
         n++;
+        CKR(inject_receivers(p, a.prev, t, s, n));
         CKR(image_step(p, a.cur, p->snaps, p->snap_shot_stride, t, s, n));
     }
     p->adj_launches[0] = n;
@@ -595,10 +646,7 @@ int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
     fa.save = 1;
     fa.snap_shot_stride = (long long)(K / f) * p->shot_stride;
     sa::Step2D aa = base_args(p);
-    aa.inj = p->n_rec ? p->inj_rec : nullptr;
-    aa.inj_off = p->inj_rec_off;
-    aa.inj_amp = p->rec_amp;
-    aa.inj_ld = p->n_rec;
+    aa.inj = nullptr;  // receivers are injected by inject_targets2d after the step
     aa.gat = nullptr;
     aa.save = 0;
     aa.snap_shot_stride = fa.snap_shot_stride;
@@ -635,6 +683,7 @@ int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
             aa.prev = even ? p->afield[0] : p->afield[1];
             CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, aa));
             n++;
+            CKR(inject_receivers(p, aa.prev, t, s, n));
             CKR(image_step(p, aa.cur, base, aa.snap_shot_stride, t, s, n));
         }
     }
@@ -924,7 +973,7 @@ int sa_plan_destroy(sa_plan* p) {
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
                     p->ones_g, p->zeros_g, p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off,
-                    p->wgrad, p->hgat};
+                    p->wgrad, p->hgat, p->rtgt_idx, p->rtgt_off, p->rtgt_point, p->rtgt_coef};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (p->cap) cudaStreamDestroy(p->cap);
