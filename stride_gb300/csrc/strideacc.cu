@@ -530,11 +530,16 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
         a.t = t;
         a.cur = (t & 1) ? p->field[1] : p->field[0];
         a.prev = (t & 1) ? p->field[0] : p->field[1];
-        a.gat = (t >= 2 && p->n_rec && !hicks) ? p->gat : nullptr;
+        a.gat = nullptr;  // receivers are gathered by their own kernel after the step
         CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
         n++;
-        if (hicks && p->n_rec) {  // rec[t] = interp(p[t+1]) over the Hicks support
-            CK(sa::hicks_gather2d(a.prev, p->shot_stride, p->pitch, p->hgat, p->n_rec, p->rec_amp, p->n_rec, t, s));
+        if (p->n_rec) {  // rec[t] = interp(p[t+1]) (linear or over the Hicks support)
+            if (hicks)
+                CK(sa::hicks_gather2d(a.prev, p->shot_stride, p->pitch, p->hgat, p->n_rec, p->rec_amp, p->n_rec, t,
+                                      s));
+            else
+                CK(sa::final_gather2d(a.prev, p->shot_stride, p->pitch, p->gat_flat, p->n_rec, p->rec_amp, p->n_rec,
+                                      t, s));
             n++;
         }
         if (mode == SA_SAVE_CHECKPOINTS && t % p->ck_K == 0 && t / p->ck_K <= p->ck_n) {
@@ -542,14 +547,6 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
             CK(cudaMemcpyAsync(slot, p->field[0], fbytes, cudaMemcpyDeviceToDevice, s));
             CK(cudaMemcpyAsync(slot + fbytes / sizeof(float), p->field[1], fbytes, cudaMemcpyDeviceToDevice, s));
         }
-    }
-    // rec[nt-2] = interp(p[nt-1])
-    const int tl = p->d.nt - 1;
-    const float* last = (tl & 1) ? p->field[1] : p->field[0];
-    if (p->d.nt >= 3 && !hicks) {
-        CK(sa::final_gather2d(last, p->shot_stride, p->pitch, p->gat_flat, p->n_rec, p->rec_amp, p->n_rec, p->d.nt - 2,
-                              s));
-        n++;
     }
     p->fwd_launches[mode] = n;
     return SA_OK;
