@@ -172,22 +172,31 @@ cudaError_t image2d(const float* q, const float* snap, float* gradb, float* prec
 }
 
 // field[idx[k]] += sum over the target's entries of coef[e] * amp[t][point[e]] (one thread per
-// target point; entries in a fixed order).
+// target point; entries in a fixed order). With snap, the same sum times inv_dt2 also enters the
+// pair-interleaved snapshot level (shot-pair stride snap_shot_stride instead of shot_stride).
 __global__ void k_inject_targets2d(float* field, const long long* __restrict__ idx, const int* __restrict__ off,
                                    const float* __restrict__ coef, const int* __restrict__ point, int n,
-                                   const float* __restrict__ amp, int ld, int t) {
+                                   const float* __restrict__ amp, int ld, int t, float* snap, long long shot_stride,
+                                   long long snap_shot_stride, float inv_dt2) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     float v = 0.f;
     const float* a = amp + (long long)t * ld;
     for (int e = off[k]; e < off[k + 1]; e++) v += coef[e] * a[point[e]];
-    field[idx[k]] += v;
+    const long long i = idx[k];
+    field[i] += v;
+    if (snap) {
+        const long long pair = i / (2 * shot_stride);
+        snap[pair * 2 * snap_shot_stride + (i - pair * 2 * shot_stride)] += v * inv_dt2;
+    }
 }
 
 cudaError_t inject_targets2d(float* field, const long long* idx, const int* off, const float* coef, const int* point,
-                             int n, const float* amp, int ld, int t, cudaStream_t s) {
+                             int n, const float* amp, int ld, int t, float* snap, long long shot_stride,
+                             long long snap_shot_stride, int, float inv_dt2, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_inject_targets2d<<<(n + 255) / 256, 256, 0, s>>>(field, idx, off, coef, point, n, amp, ld, t);
+    k_inject_targets2d<<<(n + 255) / 256, 256, 0, s>>>(field, idx, off, coef, point, n, amp, ld, t, snap, shot_stride,
+                                                       snap_shot_stride, inv_dt2);
     return cudaGetLastError();
 }
 

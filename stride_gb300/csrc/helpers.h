@@ -45,7 +45,8 @@ cudaError_t reduce3d(const float* buf, long long shot_stride, int nshots, int nx
                      cudaStream_t s);
 cudaError_t transpose(const float* in, int rows, int cols, float* out, cudaStream_t s);
 cudaError_t inject_targets2d(float* field, const long long* idx, const int* off, const float* coef, const int* point,
-                             int n, const float* amp, int ld, int t, cudaStream_t s);
+                             int n, const float* amp, int ld, int t, float* snap, long long shot_stride,
+                             long long snap_shot_stride, int unused, float inv_dt2, cudaStream_t s);
 cudaError_t image2d(const float* q, const float* snap, float* gradb, float* precb, int ix0, int ix1, int iy0, int iy1,
                     int pitch, int npairs, long long shot_stride, long long snap_shot_stride, cudaStream_t s);
 cudaError_t hicks_gather2d(const float* field, long long shot_stride, int pitch, const HicksGather* g, int n, float* out,

@@ -81,6 +81,16 @@ namespace sa {
 void set_last_error(const char* msg) { g_err = msg; }
 }  // namespace sa
 
+// Injection entries grouped by target point: field[idx[k]] += sum of coef[e] * amp[t][point[e]]
+// over e in [off[k], off[k+1]).
+struct Targets {
+    long long* idx = nullptr;
+    int *off = nullptr, *point = nullptr;
+    float* coef = nullptr;
+    size_t cap_idx = 0, cap_off = 0, cap_point = 0, cap_coef = 0;
+    int n = 0;
+};
+
 struct sa_plan {
     sa_desc d{};
     sa::Plan3D* p3 = nullptr;  // dim == 3: the 3D plan (plan3d.cu) serves every entry point
@@ -150,12 +160,9 @@ struct sa_plan {
     // Hicks interpolation: receiver gathers run as their own kernel after each step
     sa::HicksGather* hgat = nullptr;
     size_t cap_hgat = 0;
-    // adjoint receiver injection grouped by target point (its own kernel after each adjoint step)
-    long long* rtgt_idx = nullptr;
-    int *rtgt_off = nullptr, *rtgt_point = nullptr;
-    float* rtgt_coef = nullptr;
-    size_t cap_rtgt_idx = 0, cap_rtgt_off = 0, cap_rtgt_point = 0, cap_rtgt_coef = 0;
-    int n_rtgt = 0;
+    // source (forward) and receiver (adjoint) injection grouped by target point, each applied by
+    // its own kernel after the step
+    Targets stgt, rtgt;
     // layout
     int NT = 128, by = 110, chunk_rows = 1, nstrips = 1, nchunks = 1;
     bool layout_fixed = false;
@@ -273,13 +280,15 @@ int build_lists_impl(sa_plan* p);
 int build_lists(sa_plan* p) {
     const void* before[] = {p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
                             p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off, p->hgat,
-                            p->rtgt_idx, p->rtgt_off, p->rtgt_point, p->rtgt_coef};
-    const int n_before = p->n_rtgt;
+                            p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx, p->stgt.off,
+                            p->stgt.point, p->stgt.coef};
+    const int n_before = p->rtgt.n + 7919 * p->stgt.n;
     const int rc = build_lists_impl(p);
     const void* after[] = {p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
                            p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off, p->hgat,
-                           p->rtgt_idx, p->rtgt_off, p->rtgt_point, p->rtgt_coef};
-    if (n_before != p->n_rtgt) drop_graphs(p);  // the injection kernel's launch size is captured
+                           p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx, p->stgt.off,
+                           p->stgt.point, p->stgt.coef};
+    if (n_before != p->rtgt.n + 7919 * p->stgt.n) drop_graphs(p);  // injection launch sizes are captured
     for (size_t k = 0; k < sizeof(before) / sizeof(before[0]); k++)
         if (before[k] != after[k]) {
             drop_graphs(p);
@@ -328,6 +337,40 @@ int build_lists_impl(sa_plan* p) {
             return a.cta != b.cta ? a.cta < b.cta : a.row < b.row;
         });
     };
+    // the entries grouped by target point for the injection kernels (one thread per target, entries
+    // summed in a fixed order: deterministic without atomics)
+    auto make_targets = [&](const std::vector<HostInject>& in, Targets& T) -> int {
+        std::vector<std::pair<long long, size_t>> keyed(in.size());
+        for (size_t k = 0; k < in.size(); k++) {
+            const long long pair = in[k].cta / (nc * ns);
+            keyed[k] = {2 * (pair * p->shot_stride + (long long)in[k].row * p->pitch + in[k].col) + in[k].lane, k};
+        }
+        std::stable_sort(keyed.begin(), keyed.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+        std::vector<long long> tidx;
+        std::vector<int> toff, tpoint;
+        std::vector<float> tcoef;
+        for (size_t k = 0; k < keyed.size(); k++) {
+            if (k == 0 || keyed[k].first != keyed[k - 1].first) {
+                tidx.push_back(keyed[k].first);
+                toff.push_back((int)k);
+            }
+            tcoef.push_back(in[keyed[k].second].coef);
+            tpoint.push_back(in[keyed[k].second].point);
+        }
+        toff.push_back((int)keyed.size());
+        T.n = (int)tidx.size();
+        CKR(ensure(&T.idx, &T.cap_idx, tidx.size()));
+        CKR(ensure(&T.off, &T.cap_off, toff.size()));
+        CKR(ensure(&T.coef, &T.cap_coef, tcoef.size()));
+        CKR(ensure(&T.point, &T.cap_point, tpoint.size()));
+        if (!tidx.empty()) {
+            CK(cudaMemcpy(T.idx, tidx.data(), tidx.size() * sizeof(long long), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(T.coef, tcoef.data(), tcoef.size() * sizeof(float), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(T.point, tpoint.data(), tpoint.size() * sizeof(int), cudaMemcpyHostToDevice));
+        }
+        CK(cudaMemcpy(T.off, toff.data(), toff.size() * sizeof(int), cudaMemcpyHostToDevice));
+        return SA_OK;
+    };
     auto upload_inj = [&](const std::vector<HostInject>& in, sa::Inject** dl, size_t* capl, int** doff,
                           size_t* capo) -> int {
         std::vector<sa::Inject> l(in.size());
@@ -353,42 +396,11 @@ int build_lists_impl(sa_plan* p) {
     auto c1w_at = [&](int x, int y) { return p->c1w_host.empty() ? 0.0 : (double)p->c1w_host[(size_t)x * p->ny + y]; };
     make_inj(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, 2.0 * dt / h, vp_at, tmp, true);
     CKR(upload_inj(tmp, &p->inj_src, &p->cap_inj_src, &p->inj_src_off, &p->cap_inj_src_off));
+    CKR(make_targets(tmp, p->stgt));
     // adjoint receiver: -rec * dt^2 * vp^2 (devito.py:748-753), vp^2 at the corner
     make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, -dt * dt, vp2_at, tmp, false);
     CKR(upload_inj(tmp, &p->inj_rec, &p->cap_inj_rec, &p->inj_rec_off, &p->cap_inj_rec_off));
-    {  // the same entries grouped by target point for the adjoint's injection kernel (one thread per
-       // target, entries summed in a fixed order: deterministic without atomics)
-        std::vector<std::pair<long long, size_t>> keyed(tmp.size());
-        for (size_t k = 0; k < tmp.size(); k++) {
-            const long long pair = tmp[k].cta / (nc * ns);
-            keyed[k] = {2 * (pair * p->shot_stride + (long long)tmp[k].row * p->pitch + tmp[k].col) + tmp[k].lane, k};
-        }
-        std::stable_sort(keyed.begin(), keyed.end(),
-                         [](const auto& a, const auto& b) { return a.first < b.first; });
-        std::vector<long long> tidx;
-        std::vector<int> toff, tpoint;
-        std::vector<float> tcoef;
-        for (size_t k = 0; k < keyed.size(); k++) {
-            if (k == 0 || keyed[k].first != keyed[k - 1].first) {
-                tidx.push_back(keyed[k].first);
-                toff.push_back((int)k);
-            }
-            tcoef.push_back(tmp[keyed[k].second].coef);
-            tpoint.push_back(tmp[keyed[k].second].point);
-        }
-        toff.push_back((int)keyed.size());
-        p->n_rtgt = (int)tidx.size();
-        CKR(ensure(&p->rtgt_idx, &p->cap_rtgt_idx, tidx.size()));
-        CKR(ensure(&p->rtgt_off, &p->cap_rtgt_off, toff.size()));
-        CKR(ensure(&p->rtgt_coef, &p->cap_rtgt_coef, tcoef.size()));
-        CKR(ensure(&p->rtgt_point, &p->cap_rtgt_point, tpoint.size()));
-        if (!tidx.empty()) {
-            CK(cudaMemcpy(p->rtgt_idx, tidx.data(), tidx.size() * sizeof(long long), cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(p->rtgt_coef, tcoef.data(), tcoef.size() * sizeof(float), cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(p->rtgt_point, tpoint.data(), tpoint.size() * sizeof(int), cudaMemcpyHostToDevice));
-        }
-        CK(cudaMemcpy(p->rtgt_off, toff.data(), toff.size() * sizeof(int), cudaMemcpyHostToDevice));
-    }
+    CKR(make_targets(tmp, p->rtgt));
     // exact-gradient adjoint: dL/drec injected with the update's own C1 W at the corner
     make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, 1.0, c1w_at, tmp, false);
     CKR(upload_inj(tmp, &p->inj_recx, &p->cap_inj_recx, &p->inj_recx_off, &p->cap_inj_recx_off));
@@ -505,6 +517,42 @@ sa::Step2D base_args(const sa_plan* p) {
     return a;
 }
 
+// Adjoint receiver injection into the new level q[t-1] (devito.py:748-753): res[t] at every
+// target point, its entries summed in a fixed order.
+int inject_receivers(const sa_plan* p, float* level, int t, cudaStream_t s, long long& n) {
+    if (!p->rtgt.n) return SA_OK;
+    CK(sa::inject_targets2d(level, p->rtgt.idx, p->rtgt.off, p->rtgt.coef, p->rtgt.point, p->rtgt.n, p->rec_amp,
+                            p->n_rec, t, nullptr, 0, 0, 0, 0.f, s));
+    n++;
+    return SA_OK;
+}
+
+// Forward source injection into the new level p[t+1] (devito.py:357-363); on a save step the
+// injected amount / dt^2 also enters that level's p.dt2 snapshot (snaps_base: the snapshot
+// array as the step kernel addresses it, slot t/f).
+int inject_sources(const sa_plan* p, float* level, int t, const float* snaps_base, long long snap_shot_stride,
+                   bool save_now, cudaStream_t s, long long& n) {
+    if (!p->stgt.n) return SA_OK;
+    float* snap = save_now ? const_cast<float*>(snaps_base) + 2 * (long long)(t / p->d.undersampling) * p->snap_stride
+                           : nullptr;
+    CK(sa::inject_targets2d(level, p->stgt.idx, p->stgt.off, p->stgt.coef, p->stgt.point, p->stgt.n, p->src_amp,
+                            p->n_src, t, snap, p->shot_stride, snap_shot_stride, 0,
+                            (float)(1.0 / (p->d.dt * p->d.dt)), s));
+    n++;
+    return SA_OK;
+}
+
+int image_step(const sa_plan* p, const float* q, const float* snaps_base, long long snap_shot_stride, int t,
+               cudaStream_t s, long long& n) {
+    const int f = p->d.undersampling;
+    if (t % f) return SA_OK;
+    const float* snap = snaps_base + (long long)(t / f) * p->snap_stride * 2;
+    CK(sa::image2d(q, snap, p->gradb, p->precb, p->d.absorbing[0], p->nx - p->d.absorbing[0], p->d.absorbing[1],
+                   p->ny - p->d.absorbing[1], p->pitch, npairs(p), p->shot_stride, snap_shot_stride, s));
+    n++;
+    return SA_OK;
+}
+
 // Issues the forward time loop t = 1..nt-2 (iso_acoustic/devito.py:575-581) on stream s.
 // SA_SAVE_SNAPSHOTS saves p.dt2 every f steps; SA_SAVE_CHECKPOINTS copies both levels
 // (p[t+1], p[t]) after every step t = kK, k = 1..ck_n, into checkpoint slot k-1.
@@ -516,10 +564,7 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
     CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
     CK(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * p->n_rec * sizeof(float), s));
     sa::Step2D a = base_args(p);
-    a.inj = p->n_src ? p->inj_src : nullptr;
-    a.inj_off = p->inj_src_off;
-    a.inj_amp = p->src_amp;
-    a.inj_ld = p->n_src;
+    a.inj = nullptr;  // sources are injected by inject_targets2d after the step
     a.gat_off = p->gat_off;
     a.gat_out = p->rec_amp;
     a.gat_ld = p->n_rec;
@@ -533,6 +578,7 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
         a.gat = nullptr;  // receivers are gathered by their own kernel after the step
         CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
         n++;
+        CKR(inject_sources(p, a.prev, t, p->snaps, p->snap_shot_stride, save && t % p->d.undersampling == 0, s, n));
         if (p->n_rec) {  // rec[t] = interp(p[t+1]) (linear or over the Hicks support)
             if (hicks)
                 CK(sa::hicks_gather2d(a.prev, p->shot_stride, p->pitch, p->hgat, p->n_rec, p->rec_amp, p->n_rec, t,
@@ -566,27 +612,6 @@ void wavelet_gather(const sa_plan* p, sa::Step2D& a, bool wav) {
 // The imaging condition (grad += snap q, prec += snap^2, interior, t % f == 0) runs as its own
 // streaming kernel after the step of level t: in the step kernel's epilogue its dependent loads
 // stalled the adjoint (6 % slower overall).
-// Adjoint receiver injection into the new level q[t-1] (devito.py:748-753): res[t] at every
-// target point, its entries summed in a fixed order.
-int inject_receivers(const sa_plan* p, float* level, int t, cudaStream_t s, long long& n) {
-    if (!p->n_rtgt) return SA_OK;
-    CK(sa::inject_targets2d(level, p->rtgt_idx, p->rtgt_off, p->rtgt_coef, p->rtgt_point, p->n_rtgt, p->rec_amp,
-                            p->n_rec, t, s));
-    n++;
-    return SA_OK;
-}
-
-int image_step(const sa_plan* p, const float* q, const float* snaps_base, long long snap_shot_stride, int t,
-               cudaStream_t s, long long& n) {
-    const int f = p->d.undersampling;
-    if (t % f) return SA_OK;
-    const float* snap = snaps_base + (long long)(t / f) * p->snap_stride * 2;
-    CK(sa::image2d(q, snap, p->gradb, p->precb, p->d.absorbing[0], p->nx - p->d.absorbing[0], p->d.absorbing[1],
-                   p->ny - p->d.absorbing[1], p->pitch, npairs(p), p->shot_stride, snap_shot_stride, s));
-    n++;
-    return SA_OK;
-}
-
 int issue_adjoint(sa_plan* p, bool wav, cudaStream_t s) {
     const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
     const size_t gbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float);
@@ -635,10 +660,7 @@ int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
     const int f = p->d.undersampling, K = p->ck_K;
     const int T0 = p->d.nt - 1 - f;
     sa::Step2D fa = base_args(p);
-    fa.inj = p->n_src ? p->inj_src : nullptr;
-    fa.inj_off = p->inj_src_off;
-    fa.inj_amp = p->src_amp;
-    fa.inj_ld = p->n_src;
+    fa.inj = nullptr;  // sources are injected by inject_targets2d after the step
     fa.gat = nullptr;
     fa.save = 1;
     fa.snap_shot_stride = (long long)(K / f) * p->shot_stride;
@@ -672,6 +694,7 @@ int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
             fa.prev = (t & 1) ? p->field[0] : p->field[1];
             CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, fa));
             n++;
+            CKR(inject_sources(p, fa.prev, t, base, fa.snap_shot_stride, t % f == 0, s, n));
         }
         for (int t = t_hi; t >= t_lo; t--) {
             aa.t = t;
@@ -708,11 +731,8 @@ int issue_adjoint_exact(sa_plan* p, cudaStream_t s) {
     CK(cudaMemsetAsync(p->afield[1], 0, fbytes, s));
     CK(cudaMemsetAsync(p->gradb, 0, gbytes, s));
     CK(cudaMemsetAsync(p->precb, 0, gbytes, s));
-    sa::Step2D fa = base_args(p);  // forward recompute
-    fa.inj = p->n_src ? p->inj_src : nullptr;
-    fa.inj_off = p->inj_src_off;
-    fa.inj_amp = p->src_amp;
-    fa.inj_ld = p->n_src;
+    sa::Step2D fa = base_args(p);  // forward recompute (sources injected after each step)
+    fa.inj = nullptr;
     fa.gat = nullptr;
     fa.save = 0;
     sa::Step2D aa = fa;  // adjoint: dL/drec[t-2] at step t
@@ -748,6 +768,7 @@ int issue_adjoint_exact(sa_plan* p, cudaStream_t s) {
             fa.cur = p->field[m & 1];
             fa.prev = p->field[(m + 1) & 1];
             CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, fa));
+            CKR(inject_sources(p, fa.prev, m, nullptr, 0, false, s, n));
             CK(cudaMemcpyAsync(level(k, m + 1), p->field[(m + 1) & 1], fbytes, cudaMemcpyDeviceToDevice, s));
             n++;
         }
@@ -970,7 +991,8 @@ int sa_plan_destroy(sa_plan* p) {
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
                     p->ones_g, p->zeros_g, p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off,
-                    p->wgrad, p->hgat, p->rtgt_idx, p->rtgt_off, p->rtgt_point, p->rtgt_coef};
+                    p->wgrad, p->hgat, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
+                    p->stgt.off, p->stgt.point, p->stgt.coef};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (p->cap) cudaStreamDestroy(p->cap);
