@@ -30,24 +30,14 @@ __host__ __device__ constexpr float kWS(int k) {
 
 constexpr int GUARD = 40;  // zero rows above and below every pitched medium array (>= 3R + RB + 5)
 
-// One corner contribution of an injected point (source in the forward, receiver in the
-// adjoint): new_level(row, col) += coef * amp[t][point]. coef carries the bilinear weight and
-// the reference's scaling at that corner (2 dt vp / h forward, -dt^2 vp^2 adjoint).
-struct Inject {
-    int row, col, point;
-    float coef;
-    int lane;  // shot of the shot pair (0 or 1)
-    int pad[3];
-};
-
-// One receiver of a gather: rec[t][point] = sum of the four bilinear corner terms; `pad` is
-// the receiver's shot (its pair is pad / 2, its lane pad % 2).
 // A receiver with Hicks interpolation: 8 x 8 support from (row, col), weights wx[i] * wy[j].
 struct HicksGather {
     int row, col, point, shot;
     float wx[8], wy[8];
 };
 
+// One point of a gather: rec[t][point] = sum of the four bilinear corner terms; `pad` is the
+// point's shot (its pair is pad / 2, its lane pad % 2).
 struct Gather {
     int row, col, point, pad;
     float w00, w01, w10, w11;
@@ -72,16 +62,7 @@ struct Step2D {
     const float* C3;
     float hx, hy;             // spacing
     float dt;
-    // sparse points (CSR over CTAs in launch order: shot-major, then chunk, then strip)
-    const Inject* inj;
-    const int* inj_off;
-    const float* inj_amp;     // [nt][n_inj_points] time-major amplitudes
-    int inj_ld;
-    const Gather* gat;
-    const int* gat_off;
-    float* gat_out;           // [nt][n_gather_points]
-    int gat_ld;
-    // wavefield save (forward) / imaging condition (adjoint)
+    // wavefield save (forward); sources, receivers and the imaging condition are separate kernels
     int f;                    // undersampling factor
     int save;                 // forward: store p.dt2 on t % f == 0
     float* snaps;             // [pairs][n_snap][nx][pitch][2]

@@ -12,9 +12,10 @@
 //  * the sponge damping (boundaries/devito.py:49-67) is evaluated on the fly from two 1D
 //    ramps, attenuation (devito.py:1536-1548) from alpha, the update solves
 //    p.dt2 - Lt + 2 a vp p.dt + vp^2 (2 d p.dtc + d^2 p) = 0 (devito.py:1575-1581);
-//  * source injection (devito.py:357-363), receiver interpolation (:364), the undersampled
-//    p.dt2 save (:398-418) and the adjoint receiver injection / vp imaging condition
-//    (:748-753, :1000-1024) are fused epilogues with per-CTA point lists (no atomics).
+//  * the undersampled p.dt2 save (:398-418) is a fused epilogue; source injection (:357-363),
+//    receiver interpolation (:364), the adjoint receiver injection (:748-753) and the vp imaging
+//    condition (:1000-1024) run as their own kernels after the step (helpers.cu), which kept
+//    their irregular loads out of the stencil's loop.
 //
 // The new level is written in place of the older one (each point's p[t-1] is read only by
 // the thread that writes p[t+1] there), so a shot needs two field buffers.
@@ -159,9 +160,6 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
     const float2* __restrict__ cur = reinterpret_cast<const float2*>(a.cur);
     float2* __restrict__ prev = reinterpret_cast<float2*>(a.prev) + poff;
 
-    const int cta = (pair * gridDim.y + chunk) * gridDim.x + strip;
-    const int inj_b = a.inj ? a.inj_off[cta] : 0, inj_e = a.inj ? a.inj_off[cta + 1] : 0;
-    const int gat_b = a.gat ? a.gat_off[cta] : 0, gat_e = a.gat ? a.gat_off[cta + 1] : 0;
 
     const float2 ihx = f2(1.f / a.hx), ihy = f2(1.f / a.hy);
     const float2 ihx2 = f2(1.f / (a.hx * a.hx)), ihy2 = f2(1.f / (a.hy * a.hy));
@@ -213,7 +211,6 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
             if constexpr (STAG) f2q[k] = f2(0.f);
         }
     }
-    int inj_ptr = inj_b, gat_ptr = gat_b;
     const bool do_save = a.save && (a.t % a.f == 0);
 
 #pragma unroll 1
@@ -283,20 +280,6 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
         cp_async_wait<PF - 1>();
         __syncthreads();  // rows i..i+RB-1 and this iteration's fluxes visible; last iteration done
         prefetch(i + PF * RB, sI + PF * RB >= QU ? sI + PF * RB - QU : sI + PF * RB);
-
-        // ---- receiver interpolation of p[t] -> rec[t-1]: base rows i-1 .. i+RB-2 ----------
-        while (gat_ptr < gat_e && a.gat[gat_ptr].row + 1 < i) gat_ptr++;
-        for (int e = gat_ptr + tid; e < gat_e; e += NT) {
-            const Gather G = a.gat[e];
-            if (G.row + 1 >= i + RB) break;
-            const float2* s0 = rowU(wrapU(sI + G.row - i));
-            const float2* s1 = rowU(wrapU(sI + G.row + 1 - i));
-            const bool hi = G.pad & 1;
-            const float2 a00 = s0[G.col], a01 = s0[G.col + 1], a10 = s1[G.col], a11 = s1[G.col + 1];
-            const float v = G.w00 * (hi ? a00.y : a00.x) + G.w01 * (hi ? a01.y : a01.x) +
-                            G.w10 * (hi ? a10.y : a10.x) + G.w11 * (hi ? a11.y : a11.x);
-            a.gat_out[(long long)(a.t - 1) * a.gat_ld + G.point] = v;
-        }
 
         // stage-2 and update medium of this iteration
         float Wo[RB], bxj[RB], c1[RB], c2[RB], c3[RB];
@@ -397,17 +380,6 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
                 const float2 u_o = rowU(wrapU(sI - S * R + r))[c];
                 const float2 pm = pmo[r];
                 float2 pn = fma2(f2(c1[r]), Lt[r], fma2(f2(c2[r]), u_o, mul2(f2(-c3[r]), pm)));
-                // injection into the new level (sources forward, receivers adjoint)
-                while (inj_ptr < inj_e && a.inj[inj_ptr].row < orow) inj_ptr++;
-                for (int q = inj_ptr; q < inj_e; q++) {
-                    const Inject E = a.inj[q];
-                    if (E.row != orow) break;
-                    if (E.col == c) {
-                        const float amp = E.coef * a.inj_amp[(long long)a.t * a.inj_ld + E.point];
-                        if (E.lane) pn.y = pn.y + amp;
-                        else pn.x = pn.x + amp;
-                    }
-                }
                 if (do_save) {
                     float2* snap = reinterpret_cast<float2*>(a.snaps) + (long long)pair * a.snap_shot_stride +
                                    (long long)(a.t / a.f) * a.snap_stride + idx;

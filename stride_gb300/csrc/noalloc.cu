@@ -181,10 +181,11 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
     const size_t med_bytes = (size_t)(reinterpret_cast<unsigned char*>(als + pe) - reinterpret_cast<unsigned char*>(med_begin));
     float* src_amp = cv.take<float>((size_t)nt * (n_src ? n_src : 1));
     float* rec_amp = cv.take<float>((size_t)nt * (n_rec ? n_rec : 1));
-    sa::Inject* inj = cv.take<sa::Inject>((size_t)4 * kMaxSrc);
-    int* inj_off = cv.take<int>(ncta + 1);
+    long long* tidx = cv.take<long long>((size_t)4 * kMaxSrc);  // source corners grouped by target point
+    int* toff = cv.take<int>((size_t)4 * kMaxSrc + 1);
+    float* tcoef = cv.take<float>((size_t)4 * kMaxSrc);
+    int* tpoint = cv.take<int>((size_t)4 * kMaxSrc);
     sa::Gather* gat = cv.take<sa::Gather>(kMaxRec);
-    int* gat_off = cv.take<int>(ncta + 1);
     if (cv.used > kScratchBytes) return err(SA_E_INVALID, "grid, traces and lists exceed the 32 MiB scratch array");
 
     // ---- zero what must start at zero, then the medium ---------------------------------
@@ -213,8 +214,6 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
     const double h = std::max(d.spacing[0], d.spacing[1]);
     int sbx[kMaxSrc], sby[kMaxSrc];
     double sfx[kMaxSrc], sfy[kMaxSrc];
-    sa::Inject hinj[4 * kMaxSrc];
-    int hinj_off[kMaxCta + 1] = {0};
     auto locate = [&](const float* xyz, int i, int* bx, int* byy, double* fx, double* fy) -> bool {
         double rel[2];
         int base[2];
@@ -241,66 +240,53 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
                 return err(SA_E_CUDA, "reading vp at the source corners failed");
         }
     if (cudaStreamSynchronize(s) != cudaSuccess) return err(SA_E_CUDA, "stream synchronisation failed");
-    int ninj = 0;
-    int counts[kMaxCta + 1] = {0};
+    // source corners ordered by target point (insertion sort of at most 64 entries), grouped so
+    // one thread sums each point's entries in a fixed order
     struct E {
-        int cta;
-        sa::Inject e;
+        long long key;
+        float coef;
+        int point;
     } tmp[4 * kMaxSrc];
+    int ninj = 0;
     for (int i = 0; i < n_src; i++)
         for (int k = 0; k < 4; k++) {
             const int cx = k >> 1, cy = k & 1, x = sbx[i] + cx, y = sby[i] + cy;
             const double w = (cx ? sfx[i] : 1 - sfx[i]) * (cy ? sfy[i] : 1 - sfy[i]);
-            const int cta = (x / chunk_rows) * nstrips + y / by;
-            tmp[ninj++] = {cta, {x, y, i, (float)(w * 2.0 * d.dt / h * (double)vpc[4 * i + k]), 0, {0, 0, 0}}};
-            counts[cta + 1]++;
+            E v{2 * ((long long)x * pitch + y), (float)(w * 2.0 * d.dt / h * (double)vpc[4 * i + k]), i};
+            int b = ninj - 1;
+            while (b >= 0 && tmp[b].key > v.key) {
+                tmp[b + 1] = tmp[b];
+                b--;
+            }
+            tmp[b + 1] = v;
+            ninj++;
         }
-    // order by (cta, row): insertion sort of at most 64 entries
-    for (int a = 1; a < ninj; a++) {
-        E v = tmp[a];
-        int b = a - 1;
-        while (b >= 0 && (tmp[b].cta > v.cta || (tmp[b].cta == v.cta && tmp[b].e.row > v.e.row))) {
-            tmp[b + 1] = tmp[b];
-            b--;
+    long long htidx[4 * kMaxSrc];
+    int htoff[4 * kMaxSrc + 1], htpoint[4 * kMaxSrc];
+    float htcoef[4 * kMaxSrc];
+    int ntgt = 0;
+    for (int e = 0; e < ninj; e++) {
+        if (e == 0 || tmp[e].key != tmp[e - 1].key) {
+            htidx[ntgt] = tmp[e].key;
+            htoff[ntgt++] = e;
         }
-        tmp[b + 1] = v;
+        htcoef[e] = tmp[e].coef;
+        htpoint[e] = tmp[e].point;
     }
-    for (int a = 0; a < ninj; a++) hinj[a] = tmp[a].e;
-    for (int c = 0; c < ncta; c++) hinj_off[c + 1] = hinj_off[c] + counts[c + 1];
+    htoff[ntgt] = ninj;
     static thread_local sa::Gather hg[kMaxRec];
-    static thread_local int hg_cta[kMaxRec];
-    int gcount[kMaxCta + 1] = {0};
-    int hgat_off[kMaxCta + 1] = {0};
     for (int r = 0; r < n_rec; r++) {
         int bx, byy;
         double fx, fy;
         if (!locate(rec_xyz, r, &bx, &byy, &fx, &fy)) return err(SA_E_INVALID, "receiver outside the grid");
         hg[r] = {bx, byy, r, 0, (float)((1 - fx) * (1 - fy)), (float)((1 - fx) * fy), (float)(fx * (1 - fy)),
                  (float)(fx * fy)};
-        hg_cta[r] = (bx / chunk_rows) * nstrips + byy / by;
-        gcount[hg_cta[r] + 1]++;
     }
-    for (int c = 0; c < ncta; c++) hgat_off[c + 1] = hgat_off[c] + gcount[c + 1];
-    static thread_local sa::Gather hgs[kMaxRec];
-    {
-        int fill[kMaxCta + 1];
-        for (int c = 0; c <= ncta; c++) fill[c] = hgat_off[c];
-        for (int r = 0; r < n_rec; r++) hgs[fill[hg_cta[r]]++] = hg[r];
-        for (int c = 0; c < ncta; c++)  // rows ascending within a CTA
-            for (int a = hgat_off[c] + 1; a < hgat_off[c + 1]; a++) {
-                sa::Gather v = hgs[a];
-                int b = a - 1;
-                while (b >= hgat_off[c] && hgs[b].row > v.row) {
-                    hgs[b + 1] = hgs[b];
-                    b--;
-                }
-                hgs[b + 1] = v;
-            }
-    }
-    if ((ninj && cudaMemcpyAsync(inj, hinj, ninj * sizeof(sa::Inject), cudaMemcpyHostToDevice, s) != cudaSuccess) ||
-        cudaMemcpyAsync(inj_off, hinj_off, (ncta + 1) * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        (n_rec && cudaMemcpyAsync(gat, hgs, n_rec * sizeof(sa::Gather), cudaMemcpyHostToDevice, s) != cudaSuccess) ||
-        cudaMemcpyAsync(gat_off, hgat_off, (ncta + 1) * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+    if ((ntgt && (cudaMemcpyAsync(tidx, htidx, ntgt * sizeof(long long), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+                  cudaMemcpyAsync(toff, htoff, (ntgt + 1) * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+                  cudaMemcpyAsync(tcoef, htcoef, ninj * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+                  cudaMemcpyAsync(tpoint, htpoint, ninj * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess)) ||
+        (n_rec && cudaMemcpyAsync(gat, hg, n_rec * sizeof(sa::Gather), cudaMemcpyHostToDevice, s) != cudaSuccess) ||
         cudaStreamSynchronize(s) != cudaSuccess)
         return err(SA_E_CUDA, "copying the point lists failed");
 
@@ -324,27 +310,19 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
     a.hx = (float)d.spacing[0];
     a.hy = (float)d.spacing[1];
     a.dt = (float)d.dt;
-    a.inj = n_src ? inj : nullptr;
-    a.inj_off = inj_off;
-    a.inj_amp = src_amp;
-    a.inj_ld = n_src;
-    a.gat_off = gat_off;
-    a.gat_out = rec_amp;
-    a.gat_ld = n_rec;
     a.f = d.undersampling > 0 ? d.undersampling : 4;
     const dim3 grid(nstrips, nchunks, 1);
     for (int t = 1; t <= nt - 2; t++) {
         a.t = t;
         a.cur = (t & 1) ? field[1] : field[0];
         a.prev = (t & 1) ? field[0] : field[1];
-        a.gat = (t >= 2 && n_rec) ? gat : nullptr;
         if (sa::launch_step2d(kind, ot4, NT, grid, s, a) != cudaSuccess) return err(SA_E_CUDA, "step kernel launch failed");
+        // p[t+1] += sources at t; rec[t] = interp(p[t+1])
+        if (sa::inject_targets2d(a.prev, tidx, toff, tcoef, tpoint, ntgt, src_amp, n_src, t, nullptr, 0, 0, 0, 0.f, s) !=
+                cudaSuccess ||
+            (n_rec && sa::final_gather2d(a.prev, pe, pitch, gat, n_rec, rec_amp, n_rec, t, s) != cudaSuccess))
+            return err(SA_E_CUDA, "source or receiver kernel launch failed");
     }
-    if (n_rec) {
-        const float* last = ((nt - 1) & 1) ? field[1] : field[0];
-        if (sa::final_gather2d(last, pe, pitch, gat, n_rec, rec_amp, n_rec, nt - 2, s) != cudaSuccess ||
-            sa::transpose(rec_amp, nt, n_rec, traces, s) != cudaSuccess)
-            return err(SA_E_CUDA, "trace gather failed");
-    }
+    if (n_rec && sa::transpose(rec_amp, nt, n_rec, traces, s) != cudaSuccess) return err(SA_E_CUDA, "trace transpose failed");
     return SA_OK;
 }

@@ -116,12 +116,9 @@ struct sa_plan {
     std::vector<int> src_bx, src_by, rec_bx, rec_by;
     std::vector<double> src_fx, src_fy, rec_fx, rec_fy;
     bool geometry_set = false;
-    // per-CTA lists for the current layout
-    sa::Inject *inj_src = nullptr, *inj_rec = nullptr;
-    int *inj_src_off = nullptr, *inj_rec_off = nullptr, *gat_off = nullptr;
-    sa::Gather *gat = nullptr, *gat_flat = nullptr;
-    size_t cap_inj_src = 0, cap_inj_rec = 0, cap_inj_src_off = 0, cap_inj_rec_off = 0, cap_gat_off = 0, cap_gat = 0,
-           cap_gat_flat = 0;
+    // receiver gathers (one per receiver, applied by their own kernel after each step)
+    sa::Gather* gat_flat = nullptr;
+    size_t cap_gat_flat = 0;
     // sparse traces, time-major
     float *src_amp = nullptr, *rec_amp = nullptr, *stage = nullptr;
     size_t cap_src_amp = 0, cap_rec_amp = 0, cap_stage = 0;
@@ -148,21 +145,18 @@ struct sa_plan {
            cap_ones = 0, cap_zeros = 0;
     bool exact_coef_valid = false;
     std::vector<float> c1w_host;
-    sa::Inject* inj_recx = nullptr;
-    int* inj_recx_off = nullptr;
     sa::Gather* src_flat = nullptr;
-    size_t cap_inj_recx = 0, cap_inj_recx_off = 0, cap_src_flat = 0;
-    // wavelet gradient: per-CTA source gathers (negated weights) and its time-major buffer
+    size_t cap_src_flat = 0;
+    // wavelet gradient: source gathers with negated weights and its time-major buffer
     sa::Gather* gat_src = nullptr;
-    int* gat_src_off = nullptr;
     float* wgrad = nullptr;
-    size_t cap_gat_src = 0, cap_gat_src_off = 0, cap_wgrad = 0;
+    size_t cap_gat_src = 0, cap_wgrad = 0;
     // Hicks interpolation: receiver gathers run as their own kernel after each step
     sa::HicksGather* hgat = nullptr;
     size_t cap_hgat = 0;
-    // source (forward) and receiver (adjoint) injection grouped by target point, each applied by
-    // its own kernel after the step
-    Targets stgt, rtgt;
+    // source (forward), receiver (adjoint) and exact-gradient receiver injection grouped by target
+    // point, each applied by its own kernel after the step
+    Targets stgt, rtgt, xtgt;
     // layout
     int NT = 128, by = 110, chunk_rows = 1, nstrips = 1, nchunks = 1;
     bool layout_fixed = false;
@@ -278,17 +272,16 @@ struct HostInject {
 // list pointers (not their contents): they are dropped only when a list moves.
 int build_lists_impl(sa_plan* p);
 int build_lists(sa_plan* p) {
-    const void* before[] = {p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
-                            p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off, p->hgat,
-                            p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx, p->stgt.off,
-                            p->stgt.point, p->stgt.coef};
-    const int n_before = p->rtgt.n + 7919 * p->stgt.n;
+    const void* before[] = {p->gat_flat, p->src_flat, p->gat_src, p->hgat, p->rtgt.idx, p->rtgt.off, p->rtgt.point,
+                            p->rtgt.coef, p->stgt.idx, p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx,
+                            p->xtgt.off, p->xtgt.point, p->xtgt.coef};
+    const int counts_before[3] = {p->stgt.n, p->rtgt.n, p->xtgt.n};
     const int rc = build_lists_impl(p);
-    const void* after[] = {p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
-                           p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off, p->hgat,
-                           p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx, p->stgt.off,
-                           p->stgt.point, p->stgt.coef};
-    if (n_before != p->rtgt.n + 7919 * p->stgt.n) drop_graphs(p);  // injection launch sizes are captured
+    const void* after[] = {p->gat_flat, p->src_flat, p->gat_src, p->hgat, p->rtgt.idx, p->rtgt.off, p->rtgt.point,
+                           p->rtgt.coef, p->stgt.idx, p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx,
+                           p->xtgt.off, p->xtgt.point, p->xtgt.coef};
+    if (counts_before[0] != p->stgt.n || counts_before[1] != p->rtgt.n || counts_before[2] != p->xtgt.n)
+        drop_graphs(p);  // the injection kernels' launch sizes are captured
     for (size_t k = 0; k < sizeof(before) / sizeof(before[0]); k++)
         if (before[k] != after[k]) {
             drop_graphs(p);
@@ -299,7 +292,6 @@ int build_lists(sa_plan* p) {
 
 int build_lists_impl(sa_plan* p) {
     const int nc = p->nchunks, ns = p->nstrips;
-    const int ncta = npairs(p) * nc * ns;
     const double h = std::max(p->d.spacing[0], p->d.spacing[1]);
     const double dt = p->d.dt;
     // shots advance in pairs (the two lanes of a float2); CTA index of (pair, chunk, strip)
@@ -371,21 +363,6 @@ int build_lists_impl(sa_plan* p) {
         CK(cudaMemcpy(T.off, toff.data(), toff.size() * sizeof(int), cudaMemcpyHostToDevice));
         return SA_OK;
     };
-    auto upload_inj = [&](const std::vector<HostInject>& in, sa::Inject** dl, size_t* capl, int** doff,
-                          size_t* capo) -> int {
-        std::vector<sa::Inject> l(in.size());
-        std::vector<int> off(ncta + 1, 0);
-        for (size_t k = 0; k < in.size(); k++) {
-            l[k] = {in[k].row, in[k].col, in[k].point, in[k].coef, in[k].lane, {0, 0, 0}};
-            off[in[k].cta + 1]++;
-        }
-        for (int c = 0; c < ncta; c++) off[c + 1] += off[c];
-        CKR(ensure(dl, capl, l.size()));
-        CKR(ensure(doff, capo, off.size()));
-        if (!l.empty()) CK(cudaMemcpy(*dl, l.data(), l.size() * sizeof(sa::Inject), cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(*doff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
-        return SA_OK;
-    };
     std::vector<HostInject> tmp;
     // forward source: src * 2 dt^2 vp / h / dt (iso_acoustic/devito.py:349-363), vp at the corner
     auto vp_at = [&](int x, int y) { return p->vp_host.empty() ? 0.0 : (double)p->vp_host[(size_t)x * p->ny + y]; };
@@ -395,15 +372,13 @@ int build_lists_impl(sa_plan* p) {
     };
     auto c1w_at = [&](int x, int y) { return p->c1w_host.empty() ? 0.0 : (double)p->c1w_host[(size_t)x * p->ny + y]; };
     make_inj(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, 2.0 * dt / h, vp_at, tmp, true);
-    CKR(upload_inj(tmp, &p->inj_src, &p->cap_inj_src, &p->inj_src_off, &p->cap_inj_src_off));
     CKR(make_targets(tmp, p->stgt));
     // adjoint receiver: -rec * dt^2 * vp^2 (devito.py:748-753), vp^2 at the corner
     make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, -dt * dt, vp2_at, tmp, false);
-    CKR(upload_inj(tmp, &p->inj_rec, &p->cap_inj_rec, &p->inj_rec_off, &p->cap_inj_rec_off));
     CKR(make_targets(tmp, p->rtgt));
     // exact-gradient adjoint: dL/drec injected with the update's own C1 W at the corner
     make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, 1.0, c1w_at, tmp, false);
-    CKR(upload_inj(tmp, &p->inj_recx, &p->cap_inj_recx, &p->inj_recx_off, &p->cap_inj_recx_off));
+    CKR(make_targets(tmp, p->xtgt));
     {  // flat source list (pad = shot) for the exact gradient's source term
         std::vector<sa::Gather> sf;
         for (int s = 0; s < p->n_shots; s++)
@@ -420,9 +395,7 @@ int build_lists_impl(sa_plan* p) {
     // and sources with negated weights (the adjoint's wavelet gradient, -interp(p_a))
     auto make_gathers = [&](const std::vector<int>& off, const std::vector<int>& bx, const std::vector<int>& by,
                             const std::vector<double>& fx, const std::vector<double>& fy, float sign,
-                            sa::Gather** dl, size_t* capl, int** doff, size_t* capo, sa::Gather** dflat,
-                            size_t* capf) -> int {
-        std::vector<std::pair<int, sa::Gather>> g;
+                            sa::Gather** dflat, size_t* capf) -> int {
         std::vector<sa::Gather> flat;
         for (int s = 0; s < p->n_shots; s++)
             for (int r = off[s]; r < off[s + 1]; r++) {
@@ -435,34 +408,15 @@ int build_lists_impl(sa_plan* p) {
                 G.w01 = sign * (float)((1 - fx[r]) * fy[r]);
                 G.w10 = sign * (float)(fx[r] * (1 - fy[r]));
                 G.w11 = sign * (float)(fx[r] * fy[r]);
-                g.push_back({cta_of(s, G.row, G.col), G});
                 flat.push_back(G);
             }
-        std::stable_sort(g.begin(), g.end(), [](const auto& a, const auto& b) {
-            return a.first != b.first ? a.first < b.first : a.second.row < b.second.row;
-        });
-        std::vector<sa::Gather> gl(g.size());
-        std::vector<int> goff(ncta + 1, 0);
-        for (size_t k = 0; k < g.size(); k++) {
-            gl[k] = g[k].second;
-            goff[g[k].first + 1]++;
-        }
-        for (int c = 0; c < ncta; c++) goff[c + 1] += goff[c];
-        CKR(ensure(dl, capl, gl.size()));
-        CKR(ensure(doff, capo, goff.size()));
-        if (!gl.empty()) CK(cudaMemcpy(*dl, gl.data(), gl.size() * sizeof(sa::Gather), cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(*doff, goff.data(), goff.size() * sizeof(int), cudaMemcpyHostToDevice));
-        if (dflat) {
-            CKR(ensure(dflat, capf, flat.size()));
-            if (!flat.empty())
-                CK(cudaMemcpy(*dflat, flat.data(), flat.size() * sizeof(sa::Gather), cudaMemcpyHostToDevice));
-        }
+        CKR(ensure(dflat, capf, flat.size()));
+        if (!flat.empty())
+            CK(cudaMemcpy(*dflat, flat.data(), flat.size() * sizeof(sa::Gather), cudaMemcpyHostToDevice));
         return SA_OK;
     };
-    CKR(make_gathers(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, 1.f, &p->gat, &p->cap_gat, &p->gat_off,
-                     &p->cap_gat_off, &p->gat_flat, &p->cap_gat_flat));
-    CKR(make_gathers(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, -1.f, &p->gat_src, &p->cap_gat_src,
-                     &p->gat_src_off, &p->cap_gat_src_off, nullptr, nullptr));
+    CKR(make_gathers(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, 1.f, &p->gat_flat, &p->cap_gat_flat));
+    CKR(make_gathers(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, -1.f, &p->gat_src, &p->cap_gat_src));
     if (hicks) {  // receivers gathered by their own kernel over the 8 x 8 support
         std::vector<sa::HicksGather> hg;
         for (int s = 0; s < p->n_shots; s++)
@@ -563,11 +517,7 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
     CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
     CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
     CK(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * p->n_rec * sizeof(float), s));
-    sa::Step2D a = base_args(p);
-    a.inj = nullptr;  // sources are injected by inject_targets2d after the step
-    a.gat_off = p->gat_off;
-    a.gat_out = p->rec_amp;
-    a.gat_ld = p->n_rec;
+    sa::Step2D a = base_args(p);  // sources and receivers are handled by their own kernels after the step
     a.save = save ? 1 : 0;
     const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     long long n = 0;
@@ -575,7 +525,6 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
         a.t = t;
         a.cur = (t & 1) ? p->field[1] : p->field[0];
         a.prev = (t & 1) ? p->field[0] : p->field[1];
-        a.gat = nullptr;  // receivers are gathered by their own kernel after the step
         CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
         n++;
         CKR(inject_sources(p, a.prev, t, p->snaps, p->snap_shot_stride, save && t % p->d.undersampling == 0, s, n));
@@ -599,14 +548,12 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
 }
 
 // Issues the reverse-time adjoint loop t = nt-1-f .. 1 (devito.py:915-920).
-// The adjoint's source gathers write -interp(p_a[t]) into wgrad[t] (the kernel writes row t-1 at
-// step t, so the output base is one row ahead) when the wavelet gradient is requested.
-void wavelet_gather(const sa_plan* p, sa::Step2D& a, bool wav) {
-    if (!wav || !p->n_src) return;
-    a.gat = p->gat_src;
-    a.gat_off = p->gat_src_off;
-    a.gat_out = p->wgrad + p->n_src;
-    a.gat_ld = p->n_src;
+// The wavelet gradient: -interp(p_a[t]) at the sources into wgrad row t (negated gather weights).
+int wavelet_gather(const sa_plan* p, const float* q, int t, bool wav, cudaStream_t s, long long& n) {
+    if (!wav || !p->n_src) return SA_OK;
+    CK(sa::final_gather2d(q, p->shot_stride, p->pitch, p->gat_src, p->n_src, p->wgrad, p->n_src, t, s));
+    n++;
+    return SA_OK;
 }
 
 // The imaging condition (grad += snap q, prec += snap^2, interior, t % f == 0) runs as its own
@@ -619,12 +566,9 @@ int issue_adjoint(sa_plan* p, bool wav, cudaStream_t s) {
     CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
     CK(cudaMemsetAsync(p->gradb, 0, gbytes, s));
     CK(cudaMemsetAsync(p->precb, 0, gbytes, s));
-    sa::Step2D a = base_args(p);
-    a.inj = nullptr;  // receivers are injected by inject_targets2d after the step
-    a.gat = nullptr;
+    sa::Step2D a = base_args(p);  // receivers are injected by inject_targets2d after the step
     a.save = 0;
     if (wav) CK(cudaMemsetAsync(p->wgrad, 0, (size_t)p->d.nt * p->n_src * sizeof(float), s));
-    wavelet_gather(p, a, wav);
     const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     const int T0 = p->d.nt - 1 - p->d.undersampling;
     long long n = 0;
@@ -637,6 +581,7 @@ int issue_adjoint(sa_plan* p, bool wav, cudaStream_t s) {
         n++;
         CKR(inject_receivers(p, a.prev, t, s, n));
         CKR(image_step(p, a.cur, p->snaps, p->snap_shot_stride, t, s, n));
+        CKR(wavelet_gather(p, a.cur, t, wav, s, n));
     }
     p->adj_launches[0] = n;
     return SA_OK;
@@ -659,18 +604,13 @@ int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
     CK(cudaMemsetAsync(p->precb, 0, gbytes, s));
     const int f = p->d.undersampling, K = p->ck_K;
     const int T0 = p->d.nt - 1 - f;
-    sa::Step2D fa = base_args(p);
-    fa.inj = nullptr;  // sources are injected by inject_targets2d after the step
-    fa.gat = nullptr;
+    sa::Step2D fa = base_args(p);  // sources are injected by inject_targets2d after the step
     fa.save = 1;
     fa.snap_shot_stride = (long long)(K / f) * p->shot_stride;
-    sa::Step2D aa = base_args(p);
-    aa.inj = nullptr;  // receivers are injected by inject_targets2d after the step
-    aa.gat = nullptr;
+    sa::Step2D aa = base_args(p);  // receivers are injected by inject_targets2d after the step
     aa.save = 0;
     aa.snap_shot_stride = fa.snap_shot_stride;
     if (wav) CK(cudaMemsetAsync(p->wgrad, 0, (size_t)p->d.nt * p->n_src * sizeof(float), s));
-    wavelet_gather(p, aa, wav);
     const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     long long n = 0;
     for (int k = T0 >= 1 ? (T0 - 1) / K : -1; k >= 0; k--) {
@@ -705,6 +645,7 @@ int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
             n++;
             CKR(inject_receivers(p, aa.prev, t, s, n));
             CKR(image_step(p, aa.cur, base, aa.snap_shot_stride, t, s, n));
+            CKR(wavelet_gather(p, aa.cur, t, wav, s, n));
         }
     }
     p->adj_launches[1] = n;
@@ -732,16 +673,9 @@ int issue_adjoint_exact(sa_plan* p, cudaStream_t s) {
     CK(cudaMemsetAsync(p->gradb, 0, gbytes, s));
     CK(cudaMemsetAsync(p->precb, 0, gbytes, s));
     sa::Step2D fa = base_args(p);  // forward recompute (sources injected after each step)
-    fa.inj = nullptr;
-    fa.gat = nullptr;
     fa.save = 0;
-    sa::Step2D aa = fa;  // adjoint: dL/drec[t-2] at step t
-    aa.inj = p->n_rec ? p->inj_recx : nullptr;
-    aa.inj_off = p->inj_recx_off;
-    aa.inj_amp = p->rec_amp - 2 * (long long)p->n_rec;  // read at t >= 2 only
-    aa.inj_ld = p->n_rec;
+    sa::Step2D aa = fa;  // adjoint (dL/drec[t-2] injected after step t)
     sa::Step2D la = fa;  // W G(cur) into prev
-    la.inj = nullptr;
     la.C1 = row0(p, p->ones_g, p->pitch);
     la.C2 = la.C3 = row0(p, p->zeros_g, p->pitch);
     const dim3 grid(p->nstrips, p->nchunks, npairs(p));
@@ -779,6 +713,11 @@ int issue_adjoint_exact(sa_plan* p, cudaStream_t s) {
             aa.prev = p->afield[(t + 1) & 1];
             CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, aa));
             n++;
+            if (p->xtgt.n) {  // z[t-1] += C1 W dL/drec[t-2] (rows read only for t >= 2)
+                CK(sa::inject_targets2d(aa.prev, p->xtgt.idx, p->xtgt.off, p->xtgt.coef, p->xtgt.point, p->xtgt.n,
+                                        p->rec_amp, p->n_rec, t - 2, nullptr, 0, 0, 0, 0.f, s));
+                n++;
+            }
             if (t > nt - 1) continue;  // z[nt] = 0
             const float *Lu = nullptr, *Lz = nullptr;
             if (p->ot4) {
@@ -987,12 +926,12 @@ int sa_plan_destroy(sa_plan* p) {
     drop_graphs(p);
     void* bufs[] = {p->field[0], p->field[1], p->W, p->vp, p->alpha, p->buoy, p->bxh, p->byh, p->C1, p->C2, p->C3,
                     p->medium_stage,
-                    p->inj_src, p->inj_rec, p->inj_src_off, p->inj_rec_off, p->gat_off, p->gat, p->gat_flat,
+                    p->gat_flat,
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
-                    p->ones_g, p->zeros_g, p->inj_recx, p->inj_recx_off, p->src_flat, p->gat_src, p->gat_src_off,
+                    p->ones_g, p->zeros_g, p->src_flat, p->gat_src,
                     p->wgrad, p->hgat, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
-                    p->stgt.off, p->stgt.point, p->stgt.coef};
+                    p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx, p->xtgt.off, p->xtgt.point, p->xtgt.coef};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (p->cap) cudaStreamDestroy(p->cap);
@@ -1260,8 +1199,6 @@ int sa_autotune(sa_plan* p, void* stream) {
         p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
         CKR(build_lists(p));
         sa::Step2D a = base_args(p);
-        a.inj = nullptr;
-        a.gat = nullptr;
         a.cur = p->field[0];
         a.prev = p->field[1];
         const dim3 grid(p->nstrips, p->nchunks, npairs(p));
