@@ -23,6 +23,7 @@ oracle/, because the reference's Devito operator cannot be installed here).
 import argparse
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -39,7 +40,7 @@ HBM_FALLBACK_GBS = 6800.0
 # dram__bytes_read.sum + dram__bytes_write.sum of one fdtd2d_step launch on this workload's
 # batch (64 shots of 552^2, forward step with wavefield save), from the ncu capture summarised
 # in profiles/fdtd2d_step_fwdadj_552sq_64shots.md.
-NCU_TRAFFIC_PER_LAUNCH = 180.294656e6 + 102.961664e6
+NCU_TRAFFIC_PER_LAUNCH = 179.700992e6 + 102.897664e6
 
 
 WORKLOADS = {
@@ -79,6 +80,11 @@ WORKLOAD_NAMES = {
            '500 kHz, f_max 0.5 MHz: plain (reference loop, GPU pipelines) vs U-Net-preconditioned (BF16 tcgen05, '
            'trained on plain-FWI paths of held-out seeds), wall time to the target relative vp error',
 }
+
+
+def workload_name(name, nt):
+    """The workload's description with its actual number of time steps."""
+    return re.sub(r'\d+ steps', '%d steps' % nt, WORKLOAD_NAMES[name])
 
 
 def workload_config(name='fwdadj64', nt=None, n_shots=None, rank=0):
@@ -203,10 +209,10 @@ def cpu_arm(w, target_s=15.0, threads=None, calib=True, mode='fwdadj'):
         dt = time.perf_counter() - t0
         return pts / dt / 1e9, dt
 
-    nt = 24
+    nt = min(24, w['nt'])
     rate, dt = run(nt)
     if calib:
-        nt = int(min(w['nt'], max(24, nt * target_s / max(dt, 1e-3))))
+        nt = int(min(w['nt'], max(nt, nt * target_s / max(dt, 1e-3))))
         rate, dt = run(nt)
     sample = '1 shot of the workload, %s, %d of %d steps, %.1f s' % (
         'forward (save) + adjoint' if grad else 'forward', nt, w['nt'], dt)
@@ -332,7 +338,7 @@ def reference_arm(args):
         'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': _points(w, args.workload) / (value * 1e9) * 1e3, 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded phantoms)',
-        'config': {'workload': WORKLOAD_NAMES[args.workload], 'grid': list(w['shape']), 'shots': len(w['shots']),
+        'config': {'workload': workload_name(args.workload, w['nt']), 'grid': list(w['shape']), 'shots': len(w['shots']),
                    'nt': w['nt'], 'kernel': 'OT4', 'l2_flush': 'inputs larger than L2'},
         'cpu_baseline': {'value': value, 'unit': 'GPts/s', 'cores': threads, 'kind': 'port',
                          'sample': samples[-1] + ' per step (the reference Devito operator cannot be installed here; '
@@ -502,7 +508,7 @@ def gb300_arm(args):
             'metric': METRIC[mode], 'value': value, 'unit': 'GPts/s', 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_step, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded phantoms)',
-            'config': {'workload': WORKLOAD_NAMES[args.workload], 'grid': list(w['shape']),
+            'config': {'workload': workload_name(args.workload, nt), 'grid': list(w['shape']),
                        'shots_per_gpu': n_shots, 'nt': nt, 'kernel': 'OT4',
                        'gradient': (method + (' (adjoint time includes the forward recompute from checkpoints)'
                                               if method != 'snapshots' else '')) if grad_mode else None,
