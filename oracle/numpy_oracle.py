@@ -25,7 +25,7 @@ import scipy.signal
 __all__ = [
     'second_derivative_weights', 'staggered_weights', 'damping_profile',
     'linear_stencil', 'select_kernel', 'select_undersampling', 'bandwidth',
-    'tone_burst', 'tukey', 'forward', 'adjoint', 'grad_vp_chain', 'adjoint_exact',
+    'tone_burst', 'tukey', 'forward', 'adjoint', 'grad_vp_chain', 'adjoint_exact', 'rho_term',
     'DB_TO_NEPER',
 ]
 
@@ -382,7 +382,8 @@ def forward(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, or
     Arrays are on the extended grid. ``wavelets`` [n_src, nt] raw (the Tukey window
     of :505-509 is applied here). Returns traces [n_rec, nt] (float32) and, when
     ``save``, the undersampled second time derivative snapshots [n_snap, *shape]
-    (:398-418, common/devito.py:492-578).
+    (:398-418, common/devito.py:492-578); ``save='raw'`` stores p[t] itself instead, as the
+    reference does when the rho or wavelet gradient is needed (:410-413).
     """
     dim = vp.ndim
     shape = vp.shape
@@ -419,21 +420,61 @@ def forward(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, or
             np.add.at(pn, idx, (sw[:, c] * amp).astype(dtype))
         rec[t] = _gather(pn, rb, rw, dim, roffs)
         if save and t % f == 0:
-            snaps[t // f] = (pn - 2 * p + pm) / dtype(dt * dt)
+            snaps[t // f] = p if save == 'raw' else (pn - 2 * p + pm) / dtype(dt * dt)
         pm, p = p, pn
     return rec.T.astype(np.float32 if dtype == np.float32 else np.float64), snaps
 
 
+def _edge(a, d, idx):
+    return np.take(a, np.clip(idx, 0, a.shape[d] - 1), axis=d)
+
+
+def _zero(a, d, idx):
+    n = a.shape[d]
+    out = np.take(a, np.clip(idx, 0, n - 1), axis=d)
+    bad = (idx < 0) | (idx >= n)
+    shape = [1] * a.ndim
+    shape[d] = n
+    return np.where(bad.reshape(shape), 0, out)
+
+
+def rho_term(s, buoy, spacing):
+    """The rho imaging term of a raw snapshot s (iso_acoustic/devito.py:1137-1138):
+    -grad(b, shift=-1/2) . grad(s, shift=-1/2) - b laplace(s), FP64. The shifted gradients are
+    10th-order staggered first derivatives at i-1/2 from the nodes i+m, i-1-m (m = 0..4); b takes
+    the edge value beyond the grid (edge-padded material halo), s is zero there."""
+    ws = staggered_weights()
+    w2 = second_derivative_weights()
+    s = s.astype(np.float64)
+    b = buoy.astype(np.float64)
+    out = -b * _laplace(s, spacing, w2)
+    for d in range(s.ndim):
+        i = np.arange(s.shape[d])
+        db = sum(ws[m] * (_edge(b, d, i + m) - _edge(b, d, i - 1 - m)) for m in range(len(ws))) / spacing[d]
+        ds = sum(ws[m] * (_zero(s, d, i + m) - _zero(s, d, i - 1 - m)) for m in range(len(ws))) / spacing[d]
+        out = out - db * ds
+    return out
+
+
 def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
             rho=None, alpha=None, kernel=None, undersampling=4, dtype=np.float32, src_coords=None,
-            interpolation='linear'):
+            interpolation='linear', raw=False, rho_grad=False):
     """Reverse-time adjoint and vp imaging condition of the reference
     (iso_acoustic/devito.py:689-920, 985-1043): backward update of p_a[t-1],
     injection of -res[t] dt^2 vp^2 at the receivers (fw3d_mode, :725,748-753), and on
     t % f == 0 in the interior: grad += snap[t/f] p_a[t], prec += snap[t/f]^2.
     Returns raw (grad, prec) on the extended grid (zero outside the interior); with src_coords
     also the wavelet gradient [n_src, nt], src[t] = -interp(p_a[t]) (src.interpolate(expr=-p_a),
-    :755-756)."""
+    :755-756).
+
+    ``raw``: the snapshots hold p[n f] (forward ``save='raw'``) and the gradients follow the
+    reference's raw-wavefield path (:1003-1024, 1133-1150): on t = n f the held terms
+    p_dt = (s[n+1] - 2 s[n] + s[n-1]) / (f dt)^2 and, with ``rho_grad``, the rho term
+    (``rho_term``) are recomputed (the Eqs under the undersampling condition), and on every step
+    grad += held p_a[t], prec += held^2 (the Incs, which no conditional dimension guards). The
+    time spacing f dt of the undersampled derivative is the physical one (unpinned: Devito
+    is not available to confirm it). Returns (grad, prec, grad_rho, prec_rho[, gsrc]) with
+    ``rho_grad``."""
     dim = vp.ndim
     shape = vp.shape
     h = max(spacing)
@@ -458,6 +499,14 @@ def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
         sb, sw, soffs = sparse_stencil(interpolation, np.asarray(src_coords, np.float32) + eps, origin, spacing,
                                        True)
         gsrc = np.zeros((nt, sb.shape[0]))
+    if rho_grad:
+        if rho is None:
+            raise ValueError('the rho gradient needs rho')
+        buoy = (1 / rho.astype(np.float32)).astype(np.float32)
+        grad_rho = np.zeros(shape, dtype=np.float64)
+        prec_rho = np.zeros(shape, dtype=np.float64)
+    hold_vp = np.zeros(shape)
+    hold_rho = np.zeros(shape)
     for t in range(nt - 1 - f, 0, -1):
         if gsrc is not None:
             gsrc[t] = -_gather(q, sb, sw, dim, soffs)
@@ -467,14 +516,30 @@ def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
             idx = tuple(rb[:, d] + off[d] for d in range(dim))
             amp = -res[t].astype(np.float64) * dt * dt * med.vp2[idx].astype(np.float64)
             np.add.at(qn, idx, (rw[:, c] * amp).astype(dtype))
-        if t % f == 0:
+        if raw:
+            if t % f == 0:
+                n = t // f
+                sn = [snaps[n + k].astype(np.float64) for k in (-1, 0, 1)]
+                hold_vp = (sn[2] - 2 * sn[1] + sn[0]) / (f * dt) ** 2
+                if rho_grad:
+                    hold_rho = rho_term(snaps[n], buoy, spacing)
+            qd = q.astype(np.float64)
+            grad[interior] += (hold_vp * qd)[interior]
+            prec[interior] += (hold_vp * hold_vp)[interior]
+            if rho_grad:
+                grad_rho[interior] += (hold_rho * qd)[interior]
+                prec_rho[interior] += (hold_rho * hold_rho)[interior]
+        elif t % f == 0:
             s = snaps[t // f].astype(np.float64)
             grad[interior] += (s * q.astype(np.float64))[interior]
             prec[interior] += (s * s)[interior]
         qp, q = q, qn
+    out = (grad.astype(np.float32), prec.astype(np.float32))
+    if rho_grad:
+        out = out + (grad_rho.astype(np.float32), prec_rho.astype(np.float32))
     if gsrc is not None:
-        return grad.astype(np.float32), prec.astype(np.float32), gsrc.T.astype(np.float32)
-    return grad.astype(np.float32), prec.astype(np.float32)
+        out = out + (gsrc.T.astype(np.float32),)
+    return out
 
 
 def grad_vp_chain(grad, prec, vp_inner, slowness=True):

@@ -27,6 +27,7 @@ SA_DENSITY_CONSTANT = 2
 SA_SAVE_NONE = 0
 SA_SAVE_SNAPSHOTS = 1
 SA_SAVE_CHECKPOINTS = 2
+SA_SAVE_RAW = 3
 SA_GRAD_PARITY = 0
 SA_INTERP_LINEAR = 0
 SA_INTERP_HICKS = 1
@@ -34,7 +35,7 @@ SA_GRAD_EXACT = 1
 
 # every symbol include/strideacc.h declares
 EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometry', 'sa_forward',
-           'sa_adjoint', 'sa_adjoint_wavelets', 'sa_autotune', 'sa_last_error', 'sa_launch_count',
+           'sa_adjoint', 'sa_adjoint_wavelets', 'sa_adjoint_grads', 'sa_autotune', 'sa_last_error', 'sa_launch_count',
            'sa_forward_2d_noalloc',
            'sa_traces_sosfilt', 'sa_traces_fir', 'sa_traces_check', 'sa_traces_norm_per_shot', 'sa_traces_mute',
            'sa_field_mul', 'sa_field_clip', 'sa_field_axpy', 'sa_field_slowness_step', 'sa_field_stats',
@@ -79,6 +80,7 @@ def load():
     lib.sa_forward.argtypes = [P, P, P, I, P]
     lib.sa_adjoint.argtypes = [P, P, P, P, I, P]
     lib.sa_adjoint_wavelets.argtypes = [P, P, P, P, P, I, P]
+    lib.sa_adjoint_grads.argtypes = [P, P, P, P, P, P, P, P]
     lib.sa_autotune.argtypes = [P, P]
     lib.sa_last_error.argtypes = [ctypes.c_char_p, I]
     lib.sa_launch_count.argtypes = [P]
@@ -212,15 +214,24 @@ class Plan:
         self.n_rec = int(ro[-1])
 
     def forward(self, wavelets, traces, save=False, stream=None):
-        """save: False, True / 'snapshots' (p.dt2 every f steps) or 'checkpoints'."""
+        """save: False, True / 'snapshots' (p.dt2 every f steps), 'raw' (p itself every f steps,
+        for the rho and wavelet gradients of the reference) or 'checkpoints'."""
         mode = {False: SA_SAVE_NONE, None: SA_SAVE_NONE, True: SA_SAVE_SNAPSHOTS, 'snapshots': SA_SAVE_SNAPSHOTS,
-                'checkpoints': SA_SAVE_CHECKPOINTS}[save]
+                'checkpoints': SA_SAVE_CHECKPOINTS, 'raw': SA_SAVE_RAW}[save]
         check(load().sa_forward(self._h, _ptr(wavelets), _ptr(traces), mode, _stream(stream)))
 
-    def adjoint(self, residuals, grad, prec, stream=None, exact=False, grad_wavelets=None):
+    def adjoint(self, residuals, grad, prec, stream=None, exact=False, grad_wavelets=None, grad_rho=None,
+                prec_rho=None):
         """exact=False: the reference's imaging condition; exact=True: dL/dvp of the discrete forward
         map for residuals = dL/dtraces (needs a forward with save='checkpoints'). grad_wavelets
-        [n_src, nt]: also the reference's wavelet gradient -interp(p_a) (parity mode)."""
+        [n_src, nt]: also the reference's wavelet gradient -interp(p_a) (parity mode).
+        grad_rho/prec_rho [shape]: also the rho gradient (needs a forward with save='raw')."""
+        if grad_rho is not None or prec_rho is not None:
+            if exact:
+                raise ValueError('the rho gradient is the reference imaging condition (exact=False)')
+            check(load().sa_adjoint_grads(self._h, _ptr(residuals), _ptr(grad), _ptr(prec), _ptr(grad_rho),
+                                          _ptr(prec_rho), _ptr(grad_wavelets), _stream(stream)))
+            return
         check(load().sa_adjoint_wavelets(self._h, _ptr(residuals), _ptr(grad), _ptr(prec), _ptr(grad_wavelets),
                                          SA_GRAD_EXACT if exact else SA_GRAD_PARITY, _stream(stream)))
 

@@ -64,7 +64,7 @@ struct Step2D {
     float dt;
     // wavefield save (forward); sources, receivers and the imaging condition are separate kernels
     int f;                    // undersampling factor
-    int save;                 // forward: store p.dt2 on t % f == 0
+    int save;                 // forward, on t % f == 0: 1 stores p.dt2, 2 stores p[t] itself
     float* snaps;             // [pairs][n_snap][nx][pitch][2]
     long long snap_shot_stride, snap_stride;  // in float2 elements: per pair, per snapshot
 };

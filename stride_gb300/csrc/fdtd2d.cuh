@@ -12,7 +12,7 @@
 //  * the sponge damping (boundaries/devito.py:49-67) is evaluated on the fly from two 1D
 //    ramps, attenuation (devito.py:1536-1548) from alpha, the update solves
 //    p.dt2 - Lt + 2 a vp p.dt + vp^2 (2 d p.dtc + d^2 p) = 0 (devito.py:1575-1581);
-//  * the undersampled p.dt2 save (:398-418) is a fused epilogue; source injection (:357-363),
+//  * the undersampled save of p.dt2 or of p itself (:398-418) is a fused epilogue; source injection (:357-363),
 //    receiver interpolation (:364), the adjoint receiver injection (:748-753) and the vp imaging
 //    condition (:1000-1024) run as their own kernels after the step (helpers.cu), which kept
 //    their irregular loads out of the stencil's loop.
@@ -383,7 +383,8 @@ __global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_con
                 if (do_save) {
                     float2* snap = reinterpret_cast<float2*>(a.snaps) + (long long)pair * a.snap_shot_stride +
                                    (long long)(a.t / a.f) * a.snap_stride + idx;
-                    *snap = make_float2((pn.x - 2.f * u_o.x + pm.x) / dt2, (pn.y - 2.f * u_o.y + pm.y) / dt2);
+                    *snap = a.save == 2 ? u_o  // raw p[t] (rho / wavelet gradients)
+                                        : make_float2((pn.x - 2.f * u_o.x + pm.x) / dt2, (pn.y - 2.f * u_o.y + pm.y) / dt2);
                 }
                 prev[idx] = pn;
             }

@@ -19,9 +19,9 @@ __global__ void k_medium2d(const float* __restrict__ vp_in, const float* __restr
         const float v = vp_in[q];
         vp[p] = v;
         float w = v * v;
-        if (density == 1) {
+        if (density >= 1) {  // 1: variable density (W = vp^2 rho), 2: constant (b kept for the rho gradient)
             const float r = rho_in[q];
-            w = w * r;
+            if (density == 1) w = w * r;
             buoy[p] = 1.f / r;
         }
         W[p] = w;
@@ -168,6 +168,120 @@ cudaError_t image2d(const float* q, const float* snap, float* gradb, float* prec
     const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 8);
     k_image2d<<<blocks, 256, 0, s>>>(reinterpret_cast<const float2*>(q), reinterpret_cast<const float2*>(snap), gradb,
                                      precb, ix0, ix1, iy0, iy1, pitch, npairs, shot_stride, snap_shot_stride);
+    return cudaGetLastError();
+}
+
+// D-_x b and D-_y b at every node: the staggered first derivatives at x-1/2 and y-1/2 of the
+// buoyancy, nodes beyond the grid taking the edge value (the reference's edge-padded material
+// halo). They are the grad(buoy, shift=-0.5) factor of the rho imaging term
+// (iso_acoustic/devito.py:1137).
+__global__ void k_rho_terms2d(const float* __restrict__ buoy, int nx, int ny, int pitch, float ihx, float ihy,
+                              float* dbx, float* dby) {
+    const long long n = (long long)nx * ny;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(e / ny), y = (int)(e % ny);
+        float ax = 0.f, ay = 0.f;
+#pragma unroll
+        for (int m = 0; m < 5; m++) {
+            const int xh = min(x + m, nx - 1), xl = max(x - 1 - m, 0);
+            const int yh = min(y + m, ny - 1), yl = max(y - 1 - m, 0);
+            ax += kWS(m) * (buoy[(long long)xh * pitch + y] - buoy[(long long)xl * pitch + y]);
+            ay += kWS(m) * (buoy[(long long)x * pitch + yh] - buoy[(long long)x * pitch + yl]);
+        }
+        dbx[(long long)x * pitch + y] = ax * ihx;
+        dby[(long long)x * pitch + y] = ay * ihy;
+    }
+}
+
+cudaError_t rho_terms2d(const float* buoy, int nx, int ny, int pitch, float hx, float hy, float* dbx, float* dby,
+                        cudaStream_t s) {
+    k_rho_terms2d<<<1024, 256, 0, s>>>(buoy, nx, ny, pitch, 1.f / hx, 1.f / hy, dbx, dby);
+    return cudaGetLastError();
+}
+
+// Imaging from the raw saved wavefield s[n] = p[n f] (the reference's gradients when rho or the
+// wavelets need one, iso_acoustic/devito.py:1003-1024, 1133-1150). On a refresh step (t = n f)
+// the held terms of every interior point are recomputed from the snapshots:
+//   vp:  (s[n+1] - 2 s[n] + s[n-1]) * inv_fdt2,
+//   rho: -(D-_x b D-_x s[n] + D-_y b D-_y s[n]) - b laplace(s[n])  (zero halo for s),
+// and every step accumulates grad += held q, prec += held^2 over the pair's two lanes.
+// snap addresses slot n of pair 0 (float2 units for the strides); hold_rho null: vp only.
+__global__ void k_image_raw2d(const float2* __restrict__ q, const float2* __restrict__ snap, long long snap_stride,
+                              long long snap_shot_stride, int refresh, float inv_fdt2, float2* hold_vp,
+                              float2* hold_rho, const float* __restrict__ buoy, const float* __restrict__ dbx,
+                              const float* __restrict__ dby, float ihx, float ihy, int nx, int ny, float* gradb,
+                              float* precb, float* gradrb, float* precrb, int ix0, int ix1, int iy0, int iy1,
+                              int pitch, int npairs, long long shot_stride) {
+    const int w = iy1 - iy0;
+    const long long per = (long long)(ix1 - ix0) * w;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < per * npairs;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int pair = (int)(e / per);
+        const long long r = e - (long long)pair * per;
+        const int x = ix0 + (int)(r / w), y = iy0 + (int)(r % w);
+        const long long idx = (long long)x * pitch + y;
+        const long long gi = (long long)pair * shot_stride + idx;
+        float2 hv, hr = make_float2(0.f, 0.f);
+        if (refresh) {
+            const float2* sp = snap + (long long)pair * snap_shot_stride;
+            const float2 s0 = sp[idx], sn = sp[idx + snap_stride], so = sp[idx - snap_stride];
+            hv = make_float2(((sn.x - 2.f * s0.x) + so.x) * inv_fdt2, ((sn.y - 2.f * s0.y) + so.y) * inv_fdt2);
+            hold_vp[gi] = hv;
+            if (hold_rho) {
+                float2 gx = make_float2(0.f, 0.f), gy = gx;
+                float2 lx = make_float2(kW2(0) * s0.x, kW2(0) * s0.y), ly = lx;
+#pragma unroll
+                for (int m = 0; m < 5; m++) {
+                    const float2 xh = x + m < nx ? sp[idx + (long long)m * pitch] : make_float2(0.f, 0.f);
+                    const float2 xl = x - 1 - m >= 0 ? sp[idx - (long long)(m + 1) * pitch] : make_float2(0.f, 0.f);
+                    const float2 yh = y + m < ny ? sp[idx + m] : make_float2(0.f, 0.f);
+                    const float2 yl = y - 1 - m >= 0 ? sp[idx - (m + 1)] : make_float2(0.f, 0.f);
+                    gx.x += kWS(m) * (xh.x - xl.x);
+                    gx.y += kWS(m) * (xh.y - xl.y);
+                    gy.x += kWS(m) * (yh.x - yl.x);
+                    gy.y += kWS(m) * (yh.y - yl.y);
+                    const int k = m + 1;
+                    const float2 xp = x + k < nx ? sp[idx + (long long)k * pitch] : make_float2(0.f, 0.f);
+                    const float2 xm = x - k >= 0 ? sp[idx - (long long)k * pitch] : make_float2(0.f, 0.f);
+                    const float2 yp = y + k < ny ? sp[idx + k] : make_float2(0.f, 0.f);
+                    const float2 ym = y - k >= 0 ? sp[idx - k] : make_float2(0.f, 0.f);
+                    lx.x += kW2(k) * (xp.x + xm.x);
+                    lx.y += kW2(k) * (xp.y + xm.y);
+                    ly.x += kW2(k) * (yp.x + ym.x);
+                    ly.y += kW2(k) * (yp.y + ym.y);
+                }
+                const float bx = dbx[idx], by = dby[idx], b = buoy[idx];
+                const float ihx2 = ihx * ihx, ihy2 = ihy * ihy;
+                hr.x = -(bx * (gx.x * ihx) + by * (gy.x * ihy)) - b * (lx.x * ihx2 + ly.x * ihy2);
+                hr.y = -(bx * (gx.y * ihx) + by * (gy.y * ihy)) - b * (lx.y * ihx2 + ly.y * ihy2);
+                hold_rho[gi] = hr;
+            }
+        } else {
+            hv = hold_vp[gi];
+            if (hold_rho) hr = hold_rho[gi];
+        }
+        const float2 u = q[gi];
+        gradb[gi] += hv.x * u.x + hv.y * u.y;
+        precb[gi] += hv.x * hv.x + hv.y * hv.y;
+        if (hold_rho) {
+            gradrb[gi] += hr.x * u.x + hr.y * u.y;
+            precrb[gi] += hr.x * hr.x + hr.y * hr.y;
+        }
+    }
+}
+
+cudaError_t image_raw2d(const float* q, const float* snap, long long snap_stride, long long snap_shot_stride,
+                        int refresh, float inv_fdt2, float* hold_vp, float* hold_rho, const float* buoy,
+                        const float* dbx, const float* dby, float hx, float hy, int nx, int ny, float* gradb,
+                        float* precb, float* gradrb, float* precrb, int ix0, int ix1, int iy0, int iy1, int pitch,
+                        int npairs, long long shot_stride, cudaStream_t s) {
+    const long long n = (long long)(ix1 - ix0) * (iy1 - iy0) * npairs;
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 8);
+    k_image_raw2d<<<blocks, 256, 0, s>>>(
+        reinterpret_cast<const float2*>(q), reinterpret_cast<const float2*>(snap), snap_stride, snap_shot_stride,
+        refresh, inv_fdt2, reinterpret_cast<float2*>(hold_vp), reinterpret_cast<float2*>(hold_rho), buoy, dbx, dby,
+        1.f / hx, 1.f / hy, nx, ny, gradb, precb, gradrb, precrb, ix0, ix1, iy0, iy1, pitch, npairs, shot_stride);
     return cudaGetLastError();
 }
 

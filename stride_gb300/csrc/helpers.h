@@ -49,6 +49,15 @@ cudaError_t inject_targets2d(float* field, const long long* idx, const int* off,
                              long long snap_shot_stride, int unused, float inv_dt2, cudaStream_t s);
 cudaError_t image2d(const float* q, const float* snap, float* gradb, float* precb, int ix0, int ix1, int iy0, int iy1,
                     int pitch, int npairs, long long shot_stride, long long snap_shot_stride, cudaStream_t s);
+// D-_x b and D-_y b at every node (edge-padded b), for the rho imaging term.
+cudaError_t rho_terms2d(const float* buoy, int nx, int ny, int pitch, float hx, float hy, float* dbx, float* dby,
+                        cudaStream_t s);
+// Raw-snapshot imaging: held vp (and rho) terms refreshed on t = n f, accumulated every step.
+cudaError_t image_raw2d(const float* q, const float* snap, long long snap_stride, long long snap_shot_stride,
+                        int refresh, float inv_fdt2, float* hold_vp, float* hold_rho, const float* buoy,
+                        const float* dbx, const float* dby, float hx, float hy, int nx, int ny, float* gradb,
+                        float* precb, float* gradrb, float* precrb, int ix0, int ix1, int iy0, int iy1, int pitch,
+                        int npairs, long long shot_stride, cudaStream_t s);
 cudaError_t hicks_gather2d(const float* field, long long shot_stride, int pitch, const HicksGather* g, int n, float* out,
                            int ld, int trow, cudaStream_t s);
 cudaError_t final_gather2d(const float* field, long long shot_stride, int pitch, const Gather* g, int n, float* out,

@@ -128,8 +128,14 @@ struct sa_plan {
     int n_snap = 0;
     long long snap_stride = 0, snap_shot_stride = 0;
     bool snaps_valid = false;
+    bool snaps_raw = false;  // the snapshots hold p[t] (SA_SAVE_RAW), not p.dt2
     float *gradb = nullptr, *precb = nullptr;
     size_t cap_gradb = 0, cap_precb = 0;
+    // raw-snapshot gradients: held vp/rho terms per shot pair, rho accumulators, D-b per node
+    float *hold_vp = nullptr, *hold_rho = nullptr, *gradrb = nullptr, *precrb = nullptr, *dbx = nullptr,
+          *dby = nullptr;
+    size_t cap_hold_vp = 0, cap_hold_rho = 0, cap_gradrb = 0, cap_precrb = 0, cap_dbx = 0, cap_dby = 0;
+    bool rho_terms_valid = false;
     // checkpoints (SA_SAVE_CHECKPOINTS): both levels after every ck_K-th forward step, the
     // recomputed snapshots of one segment, and the adjoint's own two levels
     float *ckpt = nullptr, *segsnaps = nullptr, *afield[2] = {nullptr, nullptr};
@@ -163,10 +169,11 @@ struct sa_plan {
     sa::Sponge sponge{};
     // graphs
     cudaStream_t cap = nullptr;
-    cudaGraphExec_t g_fwd[3] = {nullptr, nullptr, nullptr};  // by save mode
-    cudaGraphExec_t g_adj[3][2] = {};  // [from snapshots, from checkpoints, exact][wavelet gradient]
-    long long fwd_launches[3] = {0, 0, 0};                   // kernels in each forward loop (by save mode)
-    long long adj_launches[3] = {0, 0, 0};                   // kernels in each adjoint loop
+    cudaGraphExec_t g_fwd[4] = {nullptr, nullptr, nullptr, nullptr};  // by save mode
+    // [from snapshots, from checkpoints, exact, raw vp, raw vp + rho][wavelet gradient]
+    cudaGraphExec_t g_adj[5][2] = {};
+    long long fwd_launches[4] = {0, 0, 0, 0};  // kernels in each forward loop (by save mode)
+    long long adj_launches[5] = {0, 0, 0, 0, 0};  // kernels in each adjoint loop
     bool use_graphs = true;
     long long launches = 0;                   // kernels launched by the last sa_forward / sa_adjoint
 };
@@ -507,20 +514,50 @@ int image_step(const sa_plan* p, const float* q, const float* snaps_base, long l
     return SA_OK;
 }
 
+// Imaging from raw snapshots (SA_SAVE_RAW): on t % f == 0 the held vp (and rho) terms are
+// recomputed from slots t/f - 1 .. t/f + 1, and every step accumulates them against q = p_a[t]
+// (the reference's unconditioned Inc of a Function written under the undersampling condition,
+// iso_acoustic/devito.py:1007-1024, 1133-1150).
+int image_raw_step(const sa_plan* p, const float* q, int t, bool rho, cudaStream_t s, long long& n) {
+    const int f = p->d.undersampling;
+    const bool refresh = t % f == 0;
+    const float* snap = p->snaps + (long long)(refresh ? t / f : 0) * p->snap_stride * 2;
+    const double fdt = (double)f * p->d.dt;
+    CK(sa::image_raw2d(q, snap, p->snap_stride, p->snap_shot_stride, refresh ? 1 : 0, (float)(1.0 / (fdt * fdt)),
+                       p->hold_vp, rho ? p->hold_rho : nullptr, p->buoy, p->dbx, p->dby, (float)p->d.spacing[0],
+                       (float)p->d.spacing[1], p->nx, p->ny, p->gradb, p->precb, p->gradrb, p->precrb,
+                       p->d.absorbing[0], p->nx - p->d.absorbing[0], p->d.absorbing[1], p->ny - p->d.absorbing[1],
+                       p->pitch, npairs(p), p->shot_stride, s));
+    n++;
+    return SA_OK;
+}
+
 // Issues the forward time loop t = 1..nt-2 (iso_acoustic/devito.py:575-581) on stream s.
-// SA_SAVE_SNAPSHOTS saves p.dt2 every f steps; SA_SAVE_CHECKPOINTS copies both levels
-// (p[t+1], p[t]) after every step t = kK, k = 1..ck_n, into checkpoint slot k-1.
+// SA_SAVE_SNAPSHOTS saves p.dt2 every f steps, SA_SAVE_RAW p[t] itself (its slots the loop does
+// not write, n = 0 and n f > nt-2, are zeroed as the reference's fresh buffer);
+// SA_SAVE_CHECKPOINTS copies both levels (p[t+1], p[t]) after every step t = kK, k = 1..ck_n,
+// into checkpoint slot k-1.
 int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
     const bool save = mode == SA_SAVE_SNAPSHOTS;
+    const bool raw = mode == SA_SAVE_RAW;
     const bool hicks = p->d.interpolation == SA_INTERP_HICKS;
     const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
     CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
     CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
     CK(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * p->n_rec * sizeof(float), s));
     sa::Step2D a = base_args(p);  // sources and receivers are handled by their own kernels after the step
-    a.save = save ? 1 : 0;
+    a.save = save ? 1 : (raw ? 2 : 0);
     const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     long long n = 0;
+    if (raw) {
+        const int f = p->d.undersampling, last = (p->d.nt - 2) / f;  // slots 1..last are written
+        const size_t slot = (size_t)p->snap_stride * 2 * sizeof(float);
+        const size_t pitchb = (size_t)p->snap_shot_stride * 2 * sizeof(float);
+        CK(cudaMemset2DAsync(p->snaps, pitchb, 0, slot, npairs(p), s));
+        if (last + 1 < p->n_snap)
+            CK(cudaMemset2DAsync(p->snaps + (size_t)(last + 1) * p->snap_stride * 2, pitchb, 0,
+                                 (size_t)(p->n_snap - last - 1) * slot, npairs(p), s));
+    }
     for (int t = 1; t <= p->d.nt - 2; t++) {
         a.t = t;
         a.cur = (t & 1) ? p->field[1] : p->field[0];
@@ -559,13 +596,21 @@ int wavelet_gather(const sa_plan* p, const float* q, int t, bool wav, cudaStream
 // The imaging condition (grad += snap q, prec += snap^2, interior, t % f == 0) runs as its own
 // streaming kernel after the step of level t: in the step kernel's epilogue its dependent loads
 // stalled the adjoint (6 % slower overall).
-int issue_adjoint(sa_plan* p, bool wav, cudaStream_t s) {
+int issue_adjoint(sa_plan* p, bool wav, bool raw, bool rho, cudaStream_t s) {
     const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
     const size_t gbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float);
     CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
     CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
     CK(cudaMemsetAsync(p->gradb, 0, gbytes, s));
     CK(cudaMemsetAsync(p->precb, 0, gbytes, s));
+    if (raw) {  // held terms start at zero (a fresh Function)
+        CK(cudaMemsetAsync(p->hold_vp, 0, fbytes, s));
+        if (rho) {
+            CK(cudaMemsetAsync(p->hold_rho, 0, fbytes, s));
+            CK(cudaMemsetAsync(p->gradrb, 0, gbytes, s));
+            CK(cudaMemsetAsync(p->precrb, 0, gbytes, s));
+        }
+    }
     sa::Step2D a = base_args(p);  // receivers are injected by inject_targets2d after the step
     a.save = 0;
     if (wav) CK(cudaMemsetAsync(p->wgrad, 0, (size_t)p->d.nt * p->n_src * sizeof(float), s));
@@ -580,10 +625,13 @@ int issue_adjoint(sa_plan* p, bool wav, cudaStream_t s) {
         CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
         n++;
         CKR(inject_receivers(p, a.prev, t, s, n));
-        CKR(image_step(p, a.cur, p->snaps, p->snap_shot_stride, t, s, n));
+        if (raw)
+            CKR(image_raw_step(p, a.cur, t, rho, s, n));
+        else
+            CKR(image_step(p, a.cur, p->snaps, p->snap_shot_stride, t, s, n));
         CKR(wavelet_gather(p, a.cur, t, wav, s, n));
     }
-    p->adj_launches[0] = n;
+    p->adj_launches[raw ? (rho ? 4 : 3) : 0] = n;
     return SA_OK;
 }
 
@@ -892,8 +940,8 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
     if (rc == SA_OK) rc = ensure(&p->C3, &p->cap_C3, NG);
     if (rc == SA_OK) rc = ensure(&p->vp, &p->cap_vp, N);
     if (rc == SA_OK) rc = ensure(&p->alpha, &p->cap_alpha, N);
+    if (rc == SA_OK && p->kind >= 1) rc = ensure(&p->buoy, &p->cap_buoy, N);  // b = 1/rho (rho gradient)
     if (rc == SA_OK && p->kind == 1) {
-        rc = ensure(&p->buoy, &p->cap_buoy, N);
         if (rc == SA_OK) rc = ensure(&p->bxh, &p->cap_bxh, (size_t)(p->nx + 9 + 2 * sa::GUARD) * p->pitch);
         if (rc == SA_OK) rc = ensure(&p->byh, &p->cap_byh, (size_t)(p->nx + 2 * sa::GUARD) * p->pitch_b);
     }
@@ -929,7 +977,8 @@ int sa_plan_destroy(sa_plan* p) {
                     p->gat_flat,
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
-                    p->ones_g, p->zeros_g, p->src_flat, p->gat_src,
+                    p->ones_g, p->zeros_g, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
+                    p->dbx, p->dby,
                     p->wgrad, p->hgat, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
                     p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx, p->xtgt.off, p->xtgt.point, p->xtgt.coef};
     for (void* b : bufs)
@@ -945,7 +994,7 @@ int sa_set_medium(sa_plan* p, const float* vp, const float* rho, const float* al
     if (p->d.attenuation && !alpha) return fail(SA_E_INVALID, "alpha required by the plan");
     if (p->p3) return sa::plan3d_set_medium(p->p3, vp, rho, alpha);
     const size_t N = (size_t)p->nx * p->ny;
-    const float* in[3] = {vp, p->d.density == SA_DENSITY_VARIABLE ? rho : nullptr, p->d.attenuation ? alpha : nullptr};
+    const float* in[3] = {vp, p->d.density != SA_DENSITY_NONE ? rho : nullptr, p->d.attenuation ? alpha : nullptr};
     const float* dev[3] = {nullptr, nullptr, nullptr};
     const bool any_host = (in[0] && !is_device(in[0])) || (in[1] && !is_device(in[1])) || (in[2] && !is_device(in[2]));
     if (any_host) CKR(ensure(&p->medium_stage, &p->cap_medium_stage, 3 * N));
@@ -958,7 +1007,7 @@ int sa_set_medium(sa_plan* p, const float* vp, const float* rho, const float* al
             dev[k] = p->medium_stage + k * N;
         }
     }
-    CK(sa::medium2d(dev[0], dev[1], dev[2], p->nx, p->ny, p->pitch, p->pitch_b, p->kind == 1 ? 1 : 0, kDbToNeper,
+    CK(sa::medium2d(dev[0], dev[1], dev[2], p->nx, p->ny, p->pitch, p->pitch_b, p->kind, kDbToNeper,
                     p->sponge, (float)p->d.dt, const_cast<float*>(row0(p, p->W, p->pitch)), p->vp, p->alpha, p->buoy,
                     p->bxh ? const_cast<float*>(row0(p, p->bxh, p->pitch, 5)) : nullptr,
                     p->byh ? const_cast<float*>(row0(p, p->byh, p->pitch_b)) : nullptr,
@@ -977,6 +1026,7 @@ int sa_set_medium(sa_plan* p, const float* vp, const float* rho, const float* al
                 p->c1w_host[(size_t)x * p->ny + y] = c1[(size_t)x * p->pitch + y] * w[(size_t)x * p->pitch + y];
     }
     p->exact_coef_valid = false;
+    p->rho_terms_valid = false;
     p->medium_set = true;
     if (p->geometry_set) CKR(build_lists(p));
     p->snaps_valid = false;
@@ -1042,15 +1092,19 @@ int sa_set_geometry(sa_plan* p, int n_shots, const int* src_offsets, const float
 
 int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, void* stream) {
     if (!p) return fail(SA_E_INVALID, "null plan");
-    if (save_mode != SA_SAVE_NONE && save_mode != SA_SAVE_SNAPSHOTS && save_mode != SA_SAVE_CHECKPOINTS)
+    if (save_mode != SA_SAVE_NONE && save_mode != SA_SAVE_SNAPSHOTS && save_mode != SA_SAVE_CHECKPOINTS &&
+        save_mode != SA_SAVE_RAW)
         return fail(SA_E_INVALID, "save_mode %d", save_mode);
-    if (p->p3) return sa::plan3d_forward(p->p3, wavelets, traces, save_mode, (cudaStream_t)stream);
+    if (p->p3) {
+        if (save_mode == SA_SAVE_RAW) return fail(SA_E_UNSUPPORTED, "SA_SAVE_RAW is implemented for 2D plans");
+        return sa::plan3d_forward(p->p3, wavelets, traces, save_mode, (cudaStream_t)stream);
+    }
     if (!p->medium_set || !p->geometry_set) return fail(SA_E_INVALID, "medium and geometry must be set first");
     if ((p->n_src && !wavelets) || (p->n_rec && !traces)) return fail(SA_E_INVALID, "null wavelets or traces");
     cudaStream_t s = (cudaStream_t)stream;
     // a forward replaces the plan's wavelets, which the checkpointed adjoint re-injects
     p->ckpt_valid = false;
-    if (save_mode == SA_SAVE_SNAPSHOTS) {
+    if (save_mode == SA_SAVE_SNAPSHOTS || save_mode == SA_SAVE_RAW) {
         const size_t n = (size_t)npairs(p) * p->snap_shot_stride * 2;
         float* old = p->snaps;
         CKR(ensure(&p->snaps, &p->cap_snaps, n));
@@ -1069,7 +1123,10 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
     CKR(run_loop(p, &p->g_fwd[save_mode], s, [&](cudaStream_t cs) { return issue_forward(p, save_mode, cs); }));
     CKR(store_transposed(p, p->rec_amp, p->d.nt, p->n_rec, traces, s));
     p->launches = (p->n_src ? 1 : 0) + p->fwd_launches[save_mode] + (p->n_rec ? 1 : 0);
-    if (save_mode == SA_SAVE_SNAPSHOTS) p->snaps_valid = true;
+    if (save_mode == SA_SAVE_SNAPSHOTS || save_mode == SA_SAVE_RAW) {
+        p->snaps_valid = true;
+        p->snaps_raw = save_mode == SA_SAVE_RAW;
+    }
     if (save_mode == SA_SAVE_CHECKPOINTS) p->ckpt_valid = true;
     return SA_OK;
 }
@@ -1078,8 +1135,29 @@ int sa_adjoint(sa_plan* p, const float* residuals, float* grad_vp, float* prec_v
     return sa_adjoint_wavelets(p, residuals, grad_vp, prec_vp, nullptr, grad_mode, stream);
 }
 
+namespace {
+int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec_vp, float* grad_rho,
+                 float* prec_rho, float* grad_wavelets, int grad_mode, void* stream);
+}
+
 int sa_adjoint_wavelets(sa_plan* p, const float* residuals, float* grad_vp, float* prec_vp, float* grad_wavelets,
                         int grad_mode, void* stream) {
+    return adjoint_impl(p, residuals, grad_vp, prec_vp, nullptr, nullptr, grad_wavelets, grad_mode, stream);
+}
+
+int sa_adjoint_grads(sa_plan* p, const float* residuals, float* grad_vp, float* prec_vp, float* grad_rho,
+                     float* prec_rho, float* grad_wavelets, void* stream) {
+    if (!p) return fail(SA_E_INVALID, "null plan");
+    if (p->p3) return fail(SA_E_UNSUPPORTED, "sa_adjoint_grads is implemented for 2D plans");
+    if (!p->snaps_valid || !p->snaps_raw) return fail(SA_E_INVALID, "sa_adjoint_grads needs a prior sa_forward with SA_SAVE_RAW");
+    if ((grad_rho == nullptr) != (prec_rho == nullptr)) return fail(SA_E_INVALID, "grad_rho and prec_rho go together");
+    if (grad_rho && p->kind == 0) return fail(SA_E_INVALID, "the rho gradient needs a plan with rho");
+    return adjoint_impl(p, residuals, grad_vp, prec_vp, grad_rho, prec_rho, grad_wavelets, SA_GRAD_PARITY, stream);
+}
+
+namespace {
+int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec_vp, float* grad_rho,
+                 float* prec_rho, float* grad_wavelets, int grad_mode, void* stream) {
     if (!p) return fail(SA_E_INVALID, "null plan");
     if (grad_mode != SA_GRAD_PARITY && grad_mode != SA_GRAD_EXACT) return fail(SA_E_INVALID, "grad_mode %d", grad_mode);
     const bool exact = grad_mode == SA_GRAD_EXACT;
@@ -1094,6 +1172,8 @@ int sa_adjoint_wavelets(sa_plan* p, const float* residuals, float* grad_vp, floa
         return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream);
     }
     const bool ck = p->ckpt_valid;
+    const bool raw = !ck && p->snaps_valid && p->snaps_raw;  // imaging from raw snapshots
+    const bool rho = grad_rho != nullptr;
     if (exact && !ck) return fail(SA_E_INVALID, "SA_GRAD_EXACT needs a prior sa_forward with SA_SAVE_CHECKPOINTS");
     if (!p->snaps_valid && !ck)
         return fail(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS or SA_SAVE_CHECKPOINTS");
@@ -1144,16 +1224,39 @@ int sa_adjoint_wavelets(sa_plan* p, const float* residuals, float* grad_vp, floa
         CKR(ensure(&p->wgrad, &p->cap_wgrad, (size_t)p->d.nt * std::max(1, p->n_src)));
         if (ow != p->wgrad) drop_graphs(p);
     }
+    if (raw) {
+        float* old[] = {p->hold_vp, p->hold_rho, p->gradrb, p->precrb, p->dbx, p->dby};
+        CKR(ensure(&p->hold_vp, &p->cap_hold_vp, 2 * fe));
+        if (rho) {
+            CKR(ensure(&p->hold_rho, &p->cap_hold_rho, 2 * fe));
+            CKR(ensure(&p->gradrb, &p->cap_gradrb, fe));
+            CKR(ensure(&p->precrb, &p->cap_precrb, fe));
+            CKR(ensure(&p->dbx, &p->cap_dbx, (size_t)p->shot_stride));
+            CKR(ensure(&p->dby, &p->cap_dby, (size_t)p->shot_stride));
+        }
+        float* now[] = {p->hold_vp, p->hold_rho, p->gradrb, p->precrb, p->dbx, p->dby};
+        if (!std::equal(std::begin(old), std::end(old), std::begin(now))) {
+            drop_graphs(p);
+            p->rho_terms_valid = false;
+        }
+        if (rho && !p->rho_terms_valid) {
+            CK(sa::rho_terms2d(p->buoy, p->nx, p->ny, p->pitch, (float)p->d.spacing[0], (float)p->d.spacing[1],
+                               p->dbx, p->dby, 0));
+            CK(cudaDeviceSynchronize());
+            p->rho_terms_valid = true;
+        }
+    }
     CKR(load_transposed(p, residuals, p->n_rec, p->d.nt, p->rec_amp, s));
-    const int am = exact ? 2 : (ck ? 1 : 0);
+    const int am = exact ? 2 : (ck ? 1 : (raw ? (rho ? 4 : 3) : 0));
     CKR(run_loop(p, &p->g_adj[am][wav ? 1 : 0], s, [&](cudaStream_t cs) {
-        return exact ? issue_adjoint_exact(p, cs) : (ck ? issue_adjoint_ckpt(p, wav, cs) : issue_adjoint(p, wav, cs));
+        return exact ? issue_adjoint_exact(p, cs)
+                     : (ck ? issue_adjoint_ckpt(p, wav, cs) : issue_adjoint(p, wav, raw, rho, cs));
     }));
     if (wav) CKR(store_transposed(p, p->wgrad, p->d.nt, p->n_src, grad_wavelets, s));
     const size_t N = (size_t)p->nx * p->ny;
-    for (int k = 0; k < 2; k++) {
-        float* user = k == 0 ? grad_vp : prec_vp;
-        const float* buf = k == 0 ? p->gradb : p->precb;
+    for (int k = 0; k < (rho ? 4 : 2); k++) {
+        float* user = k == 0 ? grad_vp : (k == 1 ? prec_vp : (k == 2 ? grad_rho : prec_rho));
+        const float* buf = k == 0 ? p->gradb : (k == 1 ? p->precb : (k == 2 ? p->gradrb : p->precrb));
         if (is_device(user)) {
             CK(sa::reduce_shots(buf, p->shot_stride, npairs(p), p->nx, p->ny, p->pitch, user, s));
         } else {
@@ -1163,9 +1266,10 @@ int sa_adjoint_wavelets(sa_plan* p, const float* residuals, float* grad_vp, floa
             CK(cudaStreamSynchronize(s));
         }
     }
-    p->launches = (p->n_rec ? 1 : 0) + p->adj_launches[am] + 2;
+    p->launches = (p->n_rec ? 1 : 0) + p->adj_launches[am] + (rho ? 4 : 2);
     return SA_OK;
 }
+}  // namespace
 
 int sa_autotune(sa_plan* p, void* stream) {
     if (p && p->p3) return SA_OK;  // 3D plans use a fixed tile (kTile3dY x kTile3dZ columns per CTA)

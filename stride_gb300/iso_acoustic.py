@@ -121,9 +121,11 @@ class IsoAcousticGB300(ProblemTypeBase):
     ``boundary_type='sponge_boundary_2'``, ``interpolation_type='linear'``,
     ``attenuation_power=0``, ``diff_source``, ``save_undersampling``, ``save_wavefield``.
     ``platform``, ``devito_config`` and ``devito_args`` are accepted and ignored (the time
-    loop always runs on the GPU). Options the reference supports but this build does not
-    (CFS-PML boundary, Hicks interpolation, attenuation power 2, rho/alpha gradients)
-    raise NotImplementedError; unknown values raise ValueError as in the reference.
+    loop always runs on the GPU). Gradients: vp, rho (2D) and the wavelets; alpha raises
+    ValueError('Variable alpha not implemented') as in the reference, which has no alpha
+    gradient. Options the reference supports but this build does not (CFS-PML boundary, sinc
+    interpolation, attenuation power 2) raise NotImplementedError; unknown values raise
+    ValueError as in the reference.
     """
 
     space_order = 10
@@ -171,9 +173,8 @@ class IsoAcousticGB300(ProblemTypeBase):
         if kwargs.get('drp', False):
             self.logger.warning('DRP weights are not implemented in this version of stride')
         self.drp = False
-        for v in (rho, alpha):
-            if v is not None and getattr(v, 'needs_grad', False):
-                raise NotImplementedError('rho/alpha gradients are not implemented in this build')
+        if rho is not None and getattr(rho, 'needs_grad', False) and self.space.dim != 2:
+            raise NotImplementedError('the rho gradient is implemented for 2D problems')
         self._check_conditions(wavelets, vp, rho, alpha, kwargs.get('kernel', None),
                                kwargs.get('save_undersampling', None), **kwargs)
 
@@ -270,10 +271,13 @@ class IsoAcousticGB300(ProblemTypeBase):
 
     @staticmethod
     def _save_wavefield(vp, rho, alpha, kwargs, wavelets=None):
-        save = kwargs.get('save_wavefield', False)
-        if save is False:
-            save = bool(getattr(vp, 'needs_grad', False)) or bool(getattr(wavelets, 'needs_grad', False))
-        return bool(save)
+        """False, 'snapshots' (p.dt2 every f steps) or 'raw' (p itself, which the reference
+        saves when the wavelets, rho or alpha need a gradient, devito.py:319,410-413)."""
+        raw = any(v is not None and getattr(v, 'needs_grad', False) for v in (wavelets, rho, alpha))
+        save = kwargs.get('save_wavefield', False) or bool(getattr(vp, 'needs_grad', False)) or raw
+        if not save:
+            return False
+        return 'raw' if raw else 'snapshots'
 
     # ---------------------------------------------------------------------------- forward
 
@@ -322,10 +326,15 @@ class IsoAcousticGB300(ProblemTypeBase):
         self._wgrad = None
         if getattr(wavelets, 'needs_grad', False):
             self._wgrad = np.zeros((self._plan.n_src, self.time.extended_num), np.float32)
+        self._grad_rho = self._prec_rho = None
+        if rho is not None and getattr(rho, 'needs_grad', False):
+            self._grad_rho = np.zeros(shape, np.float32)
+            self._prec_rho = np.zeros(shape, np.float32)
         if np.linalg.norm(np.asarray(adjoint_source.data)) < 1e-31:
             self.logger.warning('(ShotID %d) Empty adjoint source, not running adjoint', problem.shot.id)
             return
-        self._plan.adjoint(self._res, self._grad, self._prec, grad_wavelets=self._wgrad)
+        self._plan.adjoint(self._res, self._grad, self._prec, grad_wavelets=self._wgrad, grad_rho=self._grad_rho,
+                           prec_rho=self._prec_rho)
 
     def after_adjoint(self, adjoint_source, wavelets, vp, rho=None, alpha=None, **kwargs):
         """Retrieve the gradients (devito.py:922-981)."""
@@ -366,6 +375,29 @@ class IsoAcousticGB300(ProblemTypeBase):
         grad.prec = vp.alike(name='vp_prec', data=p, shape=p.shape, extended_shape=p.shape, inner=None)
         return grad
 
+    def prepare_grad_rho(self, rho, **kwargs):
+        """The rho imaging condition, -grad(b, shift=-1/2) . grad(p, shift=-1/2) - b laplace(p)
+        from the raw saved wavefield times p_a, runs after each adjoint step (devito.py:1115-1150)."""
+        return ()
+
+    def init_grad_rho(self, rho, **kwargs):
+        """Gradient buffers start at zero (devito.py:1152-1169)."""
+        self._grad_rho = None
+        self._prec_rho = None
+
+    def get_grad_rho(self, rho, **kwargs):
+        """The raw rho gradient on the inner grid (no chain rule), with its preconditioner in
+        ``.prec`` (devito.py:1171-1208)."""
+        inner = self.space.inner
+        shape = self.space.extended_shape
+        gr = self._grad_rho if self._grad_rho is not None else np.zeros(shape, np.float32)
+        pr = self._prec_rho if self._prec_rho is not None else np.zeros(shape, np.float32)
+        g = np.asarray(gr[inner], dtype=np.float32).copy()
+        p = np.asarray(pr[inner], dtype=np.float32).copy()
+        grad = rho.alike(name='rho_grad', data=g, shape=g.shape, extended_shape=g.shape, inner=None)
+        grad.prec = rho.alike(name='rho_prec', data=p, shape=g.shape, extended_shape=g.shape, inner=None)
+        return grad
+
     def prepare_grad_wavelets(self, wavelets, **kwargs):
         """The wavelet gradient is gathered inside the adjoint kernel (devito.py:755-756, 1189-1203)."""
         return ()
@@ -400,12 +432,18 @@ class IsoAcousticGB300(ProblemTypeBase):
             k += s.num_points_receivers
         return out
 
-    def gradient_batch(self, residuals, vp):
+    def gradient_batch(self, residuals, vp, rho_grad=False):
         """Adjoint of the last ``forward_batch(save_wavefield=True)``: residuals per shot,
-        returns the summed raw (grad, prec) on the extended grid."""
+        returns the summed raw (grad, prec) on the extended grid. ``rho_grad`` (after
+        ``forward_batch(save_wavefield='raw')``): returns (grad, prec, grad_rho, prec_rho)."""
         res = np.concatenate([np.atleast_2d(r) for r in residuals]).astype(np.float64)
         res = np.ascontiguousarray((res * self._window()[None, :]).astype(np.float32))
         grad = np.zeros(self.space.extended_shape, np.float32)
         prec = np.zeros(self.space.extended_shape, np.float32)
+        if rho_grad:
+            gr = np.zeros(self.space.extended_shape, np.float32)
+            pr = np.zeros(self.space.extended_shape, np.float32)
+            self._plan.adjoint(res, grad, prec, grad_rho=gr, prec_rho=pr)
+            return grad, prec, gr, pr
         self._plan.adjoint(res, grad, prec)
         return grad, prec

@@ -91,3 +91,45 @@ def test_pde_wavelet_gradient():
     _, _, gw = O.adjoint(vp.extended_data, space.spacing, time.step, time.num, space.absorbing, geo,
                          traces.data * np.float32(0.7), space.pml_origin, snaps, kernel='OT4', src_coords=geo[:1], **kw)
     assert C.rel_l2(grads[0].data, gw) <= 1e-4
+    # with the wavelets needing a gradient the reference saves the raw wavefield, and so does the
+    # drop-in: its vp gradient follows the raw-wavefield path
+    _, raw = O.forward(vp.extended_data, space.spacing, time.step, time.num, space.absorbing, geo[:1], geo, w[None],
+                       space.pml_origin, kernel='OT4', save='raw', **kw)
+    g_ref, _ = O.adjoint(vp.extended_data, space.spacing, time.step, time.num, space.absorbing, geo,
+                         traces.data * np.float32(0.7), space.pml_origin, raw, kernel='OT4', raw=True, **kw)
+    g_ref, _ = O.grad_vp_chain(g_ref[space.inner], g_ref[space.inner], vp.data, slowness=True)
+    assert C.cosine(grads[1].extended_data, g_ref) >= 0.999
+
+
+def test_pde_rho_gradient():
+    """rho.needs_grad (positional rho, as the reference's adjoint graph needs): the adjoint returns
+    (None, vp_grad, rho_grad, None); rho_grad is the raw imaging term on the inner grid."""
+    space, time, vp, rho, al, shot, sub, geo, w = _setup(True, True)
+    rho.needs_grad = True
+    pde = iso_acoustic.IsoAcousticGB300(space=space, time=time)
+    traces = pde(shot.wavelets, vp, rho, al, problem=sub)
+    residual = shot.observed.alike(name='residual', data=traces.data * np.float32(0.7))
+    grads = pde.adjoint(residual, shot.wavelets, vp, rho, al, problem=sub)
+    assert grads[0] is None and grads[3] is None
+    assert grads[2].name == 'rho_grad' and grads[2].prec.name == 'rho_prec'
+    kw = dict(rho=rho.extended_data, alpha=al.extended_data)
+    _, raw = O.forward(vp.extended_data, space.spacing, time.step, time.num, space.absorbing, geo[:1], geo, w[None],
+                       space.pml_origin, kernel='OT4', save='raw', **kw)
+    g, _, g_rho, p_rho = O.adjoint(vp.extended_data, space.spacing, time.step, time.num, space.absorbing, geo,
+                                   traces.data * np.float32(0.7), space.pml_origin, raw, kernel='OT4', raw=True,
+                                   rho_grad=True, **kw)
+    assert C.cosine(grads[2].extended_data, g_rho[space.inner]) >= 0.999
+    assert C.rel_l2(grads[2].prec.extended_data, p_rho[space.inner]) <= 1e-3
+    g_ref, _ = O.grad_vp_chain(g[space.inner], g[space.inner], vp.data, slowness=True)
+    assert C.cosine(grads[1].extended_data, g_ref) >= 0.999
+
+
+def test_pde_alpha_gradient_is_not_implemented():
+    """The reference has no alpha gradient: its prepare_grad raises ValueError."""
+    space, time, vp, rho, al, shot, sub, geo, w = _setup(True, True)
+    al.needs_grad = True
+    pde = iso_acoustic.IsoAcousticGB300(space=space, time=time)
+    traces = pde(shot.wavelets, vp, rho, al, problem=sub)
+    residual = shot.observed.alike(name='residual', data=traces.data)
+    with pytest.raises(ValueError, match='alpha not implemented'):
+        pde.adjoint(residual, shot.wavelets, vp, rho, al, problem=sub)
