@@ -45,6 +45,11 @@ extern "C" {
 #define SA_INTERP_HICKS 1     /* Kaiser-windowed sinc, 8 points per axis (common/devito.py:640-648,843-885);
                                  2D, sources smoothed as the reference's src, receivers not */
 
+#define SA_BOUNDARY_SPONGE 0  /* SpongeBoundary2 (boundaries/devito.py:37-69), the reference's default */
+#define SA_BOUNDARY_CFS_PML 1 /* ComplexFrequencyShiftPML2 (boundaries/devito.py:72-191): auxiliary fields on
+                                 the absorbing slabs instead of the sponge; 2D with OT2 (the combination the
+                                 reference's own example runs), snapshot and raw saves */
+
 #define SA_GRAD_PARITY 0      /* reference imaging condition: sum_{t%f==0} p_tt * p_a, interior only */
 #define SA_GRAD_EXACT 1       /* gradient of the discrete forward map (its exact transpose), every grid
                                  point; needs SA_SAVE_CHECKPOINTS; 2D plans. No counterpart in the
@@ -68,6 +73,9 @@ typedef struct sa_desc {
     int checkpoint_interval;   /* steps between checkpoints for SA_SAVE_CHECKPOINTS (0: 50) */
     double checkpoint_budget;  /* bytes the checkpoints may use (0: no limit); widens the interval */
     int interpolation;         /* SA_INTERP_LINEAR or SA_INTERP_HICKS (2D): sparse-point interpolation */
+    int boundary;              /* SA_BOUNDARY_SPONGE or SA_BOUNDARY_CFS_PML */
+    double f_centre;           /* Hz, centre of the propagated band (IsoAcousticDevito._bandwidth[1]): the
+                                  CFS-PML's alpha = 0.01 pi f_centre; unused by the sponge */
 } sa_desc;
 
 typedef struct sa_plan sa_plan;

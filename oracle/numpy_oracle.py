@@ -102,6 +102,81 @@ def damping_profile(shape, spacing, absorbing, vp_ext, dt):
     return damp.astype(np.float32)
 
 
+def first_derivative_weights(order=10):
+    """Centred 1st-derivative weights c_1..c_{order/2} (c_{-k} = -c_k) for Devito's
+    Derivative(f, (d, 1)) at space order 10 (boundaries/devito.py:131)."""
+    r = order // 2
+    w = _fornberg(1, Fraction(0), [Fraction(i) for i in range(-r, r + 1)])
+    return [float(w[r + k]) for k in range(1, r + 1)]
+
+
+def pml_profiles(shape, spacing, absorbing, vp_max, f_centre):
+    """CFS-PML profiles of ComplexFrequencyShiftPML2 (stride/physics/boundaries/devito.py:72-127),
+    one 1D FP32 array per axis, built with Boundary.damping (boundaries/boundary.py:59-170):
+    sigma 'power' degree 3 with the coefficient from the reflection coefficient, times max(vp)
+    (the 1D profile does not match the velocity's shape); alpha 'power' degree 2 with
+    coefficient 0.01 pi f_centre as a mask (interior = the coefficient, layer = -coefficient
+    pos^2); their derivatives are 2nd-order centred differences over an edge-padded halo of 2.
+    Returns [(sigma, alpha, dsigma, dalpha)] per axis."""
+    refl = 10 ** (-(np.log10(max(*absorbing)) - 1) / np.log10(2) - 3)
+    out = []
+    for d, n in enumerate(shape):
+        A, h = absorbing[d], spacing[d]
+        cs = (3 + 1) / 2 * np.log(1.0 / refl)
+        cs = cs / (A * h) if A > 15 else 0.67 / h
+        ca = 0.01 * np.pi * f_centre
+        sig = np.zeros(n, np.float32)
+        alp = np.ones(n, np.float32)
+        alp *= ca
+        for index in range(A):
+            pos = np.abs((A - index - 1) / float(A - 1))
+            sig[index] = sig[n - index - 1] = cs * pos ** 3
+            alp[index] = alp[n - index - 1] = ca * -(pos ** 2)
+        sig *= np.float32(vp_max)
+        sp = np.pad(sig, 2, mode='edge')
+        ap = np.pad(alp, 2, mode='edge')
+        dsig = ((sp[3:-1] - sp[1:-3]) / np.float32(2 * h)).astype(np.float32)
+        dalp = ((ap[3:-1] - ap[1:-3]) / np.float32(2 * h)).astype(np.float32)
+        out.append((sig, alp, dsig, dalp))
+    return out
+
+
+def _pml_aux(aux, f, prof, spacing, absorbing, dt, adjoint):
+    """One update of the CFS-PML auxiliary fields u_3, u_2, u_1 of every axis d on its two
+    slabs (PMLSide subdomains: the absorbing cells of axis d, every cell of the others), from
+    the boundary field f (ComplexFrequencyShiftPML2.apply, boundaries/devito.py:129-160):
+        u3' = u3 - dt ((a + s) u3 - s^2 (s' + a') f_d)
+        u2' = u2 - dt ((a + s) u2 - s (2 s' f_d + a' f_d + s f_dd) + u3')
+        u1' = u1 - dt ((a + s) u1 - (s' f_d + 2 s f_dd) + u2')
+    f_d, f_dd the 10th-order centred derivatives along d (zero halo); the adjoint uses the
+    transposed first derivative, -f_d. Returns sum_d u1' (zero outside the slabs)."""
+    t = f.dtype.type
+    c1 = first_derivative_weights()
+    w2 = second_derivative_weights()
+    dt_ = t(dt)
+    B = np.zeros_like(f)
+    for d in range(f.ndim):
+        n = f.shape[d]
+        h = t(spacing[d])
+        bs = [1] * f.ndim
+        bs[d] = n
+        sg, al, dsg, dal = (x.astype(f.dtype).reshape(bs) for x in prof[d])
+        fd = sum(t(c1[k - 1]) * (_shift(f, d, k) - _shift(f, d, -k)) for k in range(1, 6)) / h
+        fdd = (t(w2[0]) * f + sum(t(w2[k]) * (_shift(f, d, k) + _shift(f, d, -k)) for k in range(1, 6))) / (h * h)
+        if adjoint:
+            fd = -fd
+        i = np.arange(n)
+        slab = ((i < absorbing[d]) | (i >= n - absorbing[d])).reshape(bs)
+        u3, u2, u1 = aux[d]
+        a_s = al + sg
+        n3 = u3 - dt_ * (a_s * u3 - sg * sg * (dsg + dal) * fd)
+        n2 = u2 - dt_ * (a_s * u2 - sg * (t(2) * dsg * fd + dal * fd + sg * fdd) + n3)
+        n1 = u1 - dt_ * (a_s * u1 - (dsg * fd + t(2) * sg * fdd) + n2)
+        aux[d] = [np.where(slab, n3, u3), np.where(slab, n2, u2), np.where(slab, n1, u1)]
+        B = B + np.where(slab, n1, t(0))
+    return B
+
+
 def linear_stencil(coords, origin, spacing):
     """Bi/trilinear corner indices and weights of Devito's linear SparseTimeFunction
     (stride/physics/common/devito.py:580-653). ``coords`` are the float32 point
@@ -374,16 +449,43 @@ def _gather(field, base, w, dim, offs=None):
     return out
 
 
+def _pml_state(boundary, vp, spacing, absorbing, f_centre, dtype):
+    """Profiles and zero auxiliary fields of the CFS-PML (None for the sponge)."""
+    if boundary == 'sponge':
+        return None
+    if boundary != 'pml':
+        raise ValueError('boundary %r' % boundary)
+    prof = pml_profiles(vp.shape, spacing, absorbing, np.max(vp.astype(np.float32)), f_centre)
+    aux = [[np.zeros(vp.shape, dtype) for _ in range(3)] for _ in range(vp.ndim)]
+    return dict(prof=prof, aux=aux, lap=np.zeros(vp.shape, dtype))
+
+
+def _pml_Lt(pml, med, u, kernel, dt, w2, ws, spacing, absorbing, adjoint):
+    """Lt - vp^2 sum_d u_1,d for the CFS-PML update (iso_acoustic/devito.py:1552-1582): the
+    auxiliary equations run before the step's first Laplacian, so under OT4 they see the
+    boundary field `laplacian` of the previous step (zero on the first), under OT2 the field."""
+    f = pml['lap'] if kernel != 'OT2' else u
+    B = _pml_aux(pml['aux'], f, pml['prof'], spacing, absorbing, dt, adjoint)
+    lap = med.L(u, w2, ws)
+    if kernel == 'OT2':
+        Lt = lap
+    else:
+        Lt = lap + u.dtype.type(dt * dt / 12) * med.L(lap, w2, ws)
+        pml['lap'] = lap
+    return Lt - med.vp2 * B
+
+
 def forward(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, origin,
             rho=None, alpha=None, kernel=None, save=False, undersampling=4,
-            dtype=np.float32, diff_source=False, interpolation='linear'):
+            dtype=np.float32, diff_source=False, interpolation='linear', boundary='sponge', f_centre=None):
     """Forward modelling of one shot (iso_acoustic/devito.py:220-581).
 
     Arrays are on the extended grid. ``wavelets`` [n_src, nt] raw (the Tukey window
     of :505-509 is applied here). Returns traces [n_rec, nt] (float32) and, when
     ``save``, the undersampled second time derivative snapshots [n_snap, *shape]
     (:398-418, common/devito.py:492-578); ``save='raw'`` stores p[t] itself instead, as the
-    reference does when the rho or wavelet gradient is needed (:410-413).
+    reference does when the rho or wavelet gradient is needed (:410-413). ``boundary='pml'``:
+    ComplexFrequencyShiftPML2 with centre frequency ``f_centre`` instead of the sponge.
     """
     dim = vp.ndim
     shape = vp.shape
@@ -410,8 +512,14 @@ def forward(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, or
     snaps = np.zeros((n_snap,) + shape, dtype=np.float32) if save else None
     pm = np.zeros(shape, dtype=dtype)
     p = np.zeros(shape, dtype=dtype)
+    pml = _pml_state(boundary, vp, spacing, absorbing, f_centre, dtype)
+    if pml is not None:
+        damp = np.zeros_like(damp)
     for t in range(1, nt - 1):
-        Lt = _Lt(med, p, kernel, dt, w2, ws)
+        if pml is None:
+            Lt = _Lt(med, p, kernel, dt, w2, ws)
+        else:
+            Lt = _pml_Lt(pml, med, p, kernel, dt, w2, ws, spacing, absorbing, False)
         pn = _update(med, damp, Lt, p, pm, dt)
         # src.inject(p.forward, src * 2 dt^2 vp / h / dt): vp at each support point (H1 reading)
         for c, off in enumerate(soffs):
@@ -458,7 +566,7 @@ def rho_term(s, buoy, spacing):
 
 def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
             rho=None, alpha=None, kernel=None, undersampling=4, dtype=np.float32, src_coords=None,
-            interpolation='linear', raw=False, rho_grad=False):
+            interpolation='linear', raw=False, rho_grad=False, boundary='sponge', f_centre=None):
     """Reverse-time adjoint and vp imaging condition of the reference
     (iso_acoustic/devito.py:689-920, 985-1043): backward update of p_a[t-1],
     injection of -res[t] dt^2 vp^2 at the receivers (fw3d_mode, :725,748-753), and on
@@ -474,7 +582,8 @@ def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
     grad += held p_a[t], prec += held^2 (the Incs, which no conditional dimension guards). The
     time spacing f dt of the undersampled derivative is the physical one (unpinned: Devito
     is not available to confirm it). Returns (grad, prec, grad_rho, prec_rho[, gsrc]) with
-    ``rho_grad``."""
+    ``rho_grad``. ``boundary='pml'``: the CFS-PML's adjoint as Devito forms it (time derivative
+    and first space derivative transposed, boundaries/devito.py:135-149)."""
     dim = vp.ndim
     shape = vp.shape
     h = max(spacing)
@@ -507,10 +616,16 @@ def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
         prec_rho = np.zeros(shape, dtype=np.float64)
     hold_vp = np.zeros(shape)
     hold_rho = np.zeros(shape)
+    pml = _pml_state(boundary, vp, spacing, absorbing, f_centre, dtype)
+    if pml is not None:
+        damp = np.zeros_like(damp)
     for t in range(nt - 1 - f, 0, -1):
         if gsrc is not None:
             gsrc[t] = -_gather(q, sb, sw, dim, soffs)
-        Lt = _Lt(med, q, kernel, dt, w2, ws)
+        if pml is None:
+            Lt = _Lt(med, q, kernel, dt, w2, ws)
+        else:
+            Lt = _pml_Lt(pml, med, q, kernel, dt, w2, ws, spacing, absorbing, True)
         qn = _update(med, damp, Lt, q, qp, dt)
         for c, off in enumerate(offs):
             idx = tuple(rb[:, d] + off[d] for d in range(dim))

@@ -29,6 +29,8 @@ SA_SAVE_SNAPSHOTS = 1
 SA_SAVE_CHECKPOINTS = 2
 SA_SAVE_RAW = 3
 SA_GRAD_PARITY = 0
+SA_BOUNDARY_SPONGE = 0
+SA_BOUNDARY_CFS_PML = 1
 SA_INTERP_LINEAR = 0
 SA_INTERP_HICKS = 1
 SA_GRAD_EXACT = 1
@@ -51,7 +53,7 @@ class SaDesc(ctypes.Structure):
                 ('nt', ctypes.c_int), ('kernel', ctypes.c_int), ('density', ctypes.c_int),
                 ('attenuation', ctypes.c_int), ('undersampling', ctypes.c_int), ('max_shots', ctypes.c_int),
                 ('checkpoint_interval', ctypes.c_int), ('checkpoint_budget', ctypes.c_double),
-                ('interpolation', ctypes.c_int)]
+                ('interpolation', ctypes.c_int), ('boundary', ctypes.c_int), ('f_centre', ctypes.c_double)]
 
 
 class StrideAccError(RuntimeError):
@@ -162,7 +164,9 @@ class Plan:
 
     def __init__(self, dim, shape, spacing, extra, absorbing, dt, nt, kernel='OT4', density=SA_DENSITY_NONE,
                  attenuation=False, undersampling=4, max_shots=1, checkpoint_interval=0, checkpoint_budget=0.0,
-                 interpolation='linear'):
+                 interpolation='linear', boundary='sponge', f_centre=0.0):
+        """boundary: 'sponge' (SpongeBoundary2) or 'pml' (ComplexFrequencyShiftPML2, 2D OT2, with the
+        band centre f_centre in Hz)."""
         lib = load()
         d = SaDesc()
         d.dim = dim
@@ -181,6 +185,8 @@ class Plan:
         d.checkpoint_interval = int(checkpoint_interval)
         d.checkpoint_budget = float(checkpoint_budget)
         d.interpolation = {'linear': SA_INTERP_LINEAR, 'hicks': SA_INTERP_HICKS}[interpolation]
+        d.boundary = {'sponge': SA_BOUNDARY_SPONGE, 'pml': SA_BOUNDARY_CFS_PML}[boundary]
+        d.f_centre = float(f_centre)
         self.desc = d
         h = ctypes.c_void_p()
         check(lib.sa_plan_create(ctypes.byref(d), ctypes.byref(h)))

@@ -285,6 +285,126 @@ cudaError_t image_raw2d(const float* q, const float* snap, long long snap_stride
     return cudaGetLastError();
 }
 
+// 10th-order centred first-derivative weights c_1..c_5 (c_-k = -c_k): Devito's Derivative(f, (d, 1))
+// at space order 10, the CFS-PML's u_di (stride/physics/boundaries/devito.py:131).
+__host__ __device__ constexpr float kW1(int k) {
+    return k == 1 ? (float)(5.0 / 6.0)
+         : k == 2 ? (float)(-5.0 / 21.0)
+         : k == 3 ? (float)(5.0 / 84.0)
+         : k == 4 ? (float)(-5.0 / 504.0)
+                  : (float)(1.0 / 1260.0);
+}
+
+// CFS-PML (ComplexFrequencyShiftPML2, boundaries/devito.py:72-191) after a step of the OT2
+// operator: on every point of the absorbing frame, for each axis d whose slab holds the point,
+// the auxiliary fields advance with the derivatives of the current level f = p[t] along d
+// (zero halo; the adjoint transposes the first derivative, -f_d):
+//   u3' = u3 - dt ((a + s) u3 - s^2 (s' + a') f_d)
+//   u2' = u2 - dt ((a + s) u2 - s (2 s' f_d + a' f_d + s f_dd) + u3')
+//   u1' = u1 - dt ((a + s) u1 - (s' f_d + 2 s f_dd) + u2')
+// and the new level, computed by the step kernel without the boundary term, takes it:
+// p[t+1] -= C1 vp^2 sum_d u1' (the term vp^2 u_1 of the boundary equation, iso_acoustic/devito.py:
+// 1575-1582). On a p.dt2 save step the snapshot takes the same correction / dt^2.
+// prof: sigma, alpha, sigma', alpha' of the x axis (nx each), then of the y axis (ny each).
+// aux: 6 fields (u3, u2, u1 of x, then of y), each npairs * shot_stride float2.
+__global__ void k_pml2d(const float2* __restrict__ cur, float2* nxt, float2* aux, const float* __restrict__ prof,
+                        const float* __restrict__ C1, const float* __restrict__ vp, int nx, int ny, int pitch,
+                        long long shot_stride, int npairs, int ax, int ay, float ihx, float ihy, float dt, int adjoint,
+                        float2* snap, long long snap_shot_stride, float inv_dt2) {
+    const long long band = (long long)ax * ny;             // points of one x slab
+    const long long side = (long long)(nx - 2 * ax) * ay;  // points of one y slab between the x slabs
+    const long long per = 2 * band + 2 * side;
+    const long long fs = (long long)npairs * shot_stride;  // float2 per auxiliary field
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < per * npairs;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int pair = (int)(e / per);
+        long long r = e - (long long)pair * per;
+        int x, y;
+        if (r < 2 * band) {
+            const long long q = r < band ? r : r - band;
+            x = (int)(q / ny) + (r < band ? 0 : nx - ax);
+            y = (int)(q % ny);
+        } else {
+            r -= 2 * band;
+            const long long q = r < side ? r : r - side;
+            x = ax + (int)(q / ay);
+            y = (int)(q % ay) + (r < side ? 0 : ny - ay);
+        }
+        const long long idx = (long long)x * pitch + y;
+        const long long base = (long long)pair * shot_stride;
+        const float2* f = cur + base;
+        float bx = 0.f, by = 0.f;  // sum of u1' over the axes, per lane
+#pragma unroll
+        for (int d = 0; d < 2; d++) {
+            const int i = d == 0 ? x : y, n = d == 0 ? nx : ny, a = d == 0 ? ax : ay;
+            if (!(i < a || i >= n - a)) continue;
+            const long long st = d == 0 ? pitch : 1;
+            const float ih = d == 0 ? ihx : ihy;
+            const float2 f0 = f[idx];
+            float2 g = make_float2(0.f, 0.f), l = make_float2(kW2(0) * f0.x, kW2(0) * f0.y);
+#pragma unroll
+            for (int k = 1; k <= 5; k++) {
+                const float2 fp = i + k < n ? f[idx + k * st] : make_float2(0.f, 0.f);
+                const float2 fm = i - k >= 0 ? f[idx - k * st] : make_float2(0.f, 0.f);
+                g.x += kW1(k) * (fp.x - fm.x);
+                g.y += kW1(k) * (fp.y - fm.y);
+                l.x += kW2(k) * (fp.x + fm.x);
+                l.y += kW2(k) * (fp.y + fm.y);
+            }
+            const float sgn = adjoint ? -ih : ih;
+            g.x *= sgn;
+            g.y *= sgn;
+            l.x *= ih * ih;
+            l.y *= ih * ih;
+            const float* pr = prof + (d == 0 ? 0 : 4 * nx);
+            const float s = pr[i], al = pr[n + i], ds = pr[2 * n + i], da = pr[3 * n + i];
+            float2* u3 = aux + (3 * d) * fs + base + idx;
+            float2* u2 = aux + (3 * d + 1) * fs + base + idx;
+            float2* u1 = aux + (3 * d + 2) * fs + base + idx;
+            float2 v3 = *u3, v2 = *u2, v1 = *u1;
+            const float as = al + s;
+            v3.x = v3.x - dt * (as * v3.x - s * s * (ds + da) * g.x);
+            v3.y = v3.y - dt * (as * v3.y - s * s * (ds + da) * g.y);
+            v2.x = v2.x - dt * (as * v2.x - s * (2.f * ds * g.x + da * g.x + s * l.x) + v3.x);
+            v2.y = v2.y - dt * (as * v2.y - s * (2.f * ds * g.y + da * g.y + s * l.y) + v3.y);
+            v1.x = v1.x - dt * (as * v1.x - (ds * g.x + 2.f * s * l.x) + v2.x);
+            v1.y = v1.y - dt * (as * v1.y - (ds * g.y + 2.f * s * l.y) + v2.y);
+            *u3 = v3;
+            *u2 = v2;
+            *u1 = v1;
+            bx += v1.x;
+            by += v1.y;
+        }
+        const float v = vp[idx];
+        const float k = C1[idx] * (v * v);
+        float2* pn = nxt + base + idx;
+        float2 o = *pn;
+        o.x -= k * bx;
+        o.y -= k * by;
+        *pn = o;
+        if (snap) {
+            float2* sp = snap + (long long)pair * snap_shot_stride + idx;
+            float2 w = *sp;
+            w.x -= k * bx * inv_dt2;
+            w.y -= k * by * inv_dt2;
+            *sp = w;
+        }
+    }
+}
+
+cudaError_t pml2d(const float* cur, float* nxt, float* aux, const float* prof, const float* C1, const float* vp, int nx,
+                  int ny, int pitch, long long shot_stride, int npairs, int ax, int ay, float hx, float hy, float dt,
+                  int adjoint, float* snap, long long snap_shot_stride, float inv_dt2, cudaStream_t s) {
+    const long long n = (2LL * ax * ny + 2LL * (nx - 2 * ax) * ay) * npairs;
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 8);
+    k_pml2d<<<blocks, 256, 0, s>>>(reinterpret_cast<const float2*>(cur), reinterpret_cast<float2*>(nxt),
+                                   reinterpret_cast<float2*>(aux), prof, C1, vp, nx, ny, pitch, shot_stride, npairs,
+                                   ax, ay, 1.f / hx, 1.f / hy, dt, adjoint, reinterpret_cast<float2*>(snap),
+                                   snap_shot_stride, inv_dt2);
+    return cudaGetLastError();
+}
+
 // field[idx[k]] += sum over the target's entries of coef[e] * amp[t][point[e]] (one thread per
 // target point; entries in a fixed order). With snap, the same sum times inv_dt2 also enters the
 // pair-interleaved snapshot level (shot-pair stride snap_shot_stride instead of shot_stride).

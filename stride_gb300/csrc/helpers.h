@@ -58,6 +58,10 @@ cudaError_t image_raw2d(const float* q, const float* snap, long long snap_stride
                         const float* dbx, const float* dby, float hx, float hy, int nx, int ny, float* gradb,
                         float* precb, float* gradrb, float* precrb, int ix0, int ix1, int iy0, int iy1, int pitch,
                         int npairs, long long shot_stride, cudaStream_t s);
+// CFS-PML auxiliary update on the absorbing frame and the boundary term of the new level (OT2).
+cudaError_t pml2d(const float* cur, float* nxt, float* aux, const float* prof, const float* C1, const float* vp, int nx,
+                  int ny, int pitch, long long shot_stride, int npairs, int ax, int ay, float hx, float hy, float dt,
+                  int adjoint, float* snap, long long snap_shot_stride, float inv_dt2, cudaStream_t s);
 cudaError_t hicks_gather2d(const float* field, long long shot_stride, int pitch, const HicksGather* g, int n, float* out,
                            int ld, int trow, cudaStream_t s);
 cudaError_t final_gather2d(const float* field, long long shot_stride, int pitch, const Gather* g, int n, float* out,

@@ -120,6 +120,7 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
     if (d.kernel != SA_KERNEL_OT2 && d.kernel != SA_KERNEL_OT4) return err(SA_E_INVALID, "kernel must be OT2 or OT4");
     if (d.density < 0 || d.density > 2) return err(SA_E_INVALID, "density mode");
     if (d.interpolation != SA_INTERP_LINEAR) return err(SA_E_UNSUPPORTED, "linear interpolation only");
+    if (d.boundary != SA_BOUNDARY_SPONGE) return err(SA_E_UNSUPPORTED, "sponge boundary only");
     if (!(d.dt > 0) || !(d.spacing[0] > 0) || !(d.spacing[1] > 0)) return err(SA_E_INVALID, "dt and spacing");
     for (int a = 0; a < 2; a++)
         if (d.absorbing[a] < 0 || d.absorbing[a] > sa::MAX_ABS || d.absorbing[a] == 1 || d.absorbing[a] > d.extra[a] ||

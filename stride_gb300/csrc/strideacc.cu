@@ -136,6 +136,11 @@ struct sa_plan {
           *dby = nullptr;
     size_t cap_hold_vp = 0, cap_hold_rho = 0, cap_gradrb = 0, cap_precrb = 0, cap_dbx = 0, cap_dby = 0;
     bool rho_terms_valid = false;
+    // CFS-PML (SA_BOUNDARY_CFS_PML): sigma/alpha profiles and their derivatives per axis, and the
+    // six auxiliary fields (u3, u2, u1 of each axis) per shot pair
+    bool pml = false;
+    float *pml_prof = nullptr, *pml_aux = nullptr;
+    size_t cap_pml_prof = 0, cap_pml_aux = 0;
     // checkpoints (SA_SAVE_CHECKPOINTS): both levels after every ck_K-th forward step, the
     // recomputed snapshots of one segment, and the adjoint's own two levels
     float *ckpt = nullptr, *segsnaps = nullptr, *afield[2] = {nullptr, nullptr};
@@ -514,6 +519,24 @@ int image_step(const sa_plan* p, const float* q, const float* snaps_base, long l
     return SA_OK;
 }
 
+// The CFS-PML after the step of level cur (new level nxt, its p.dt2 snapshot slot snap or null):
+// auxiliary fields of the absorbing slabs and the boundary term of the new level.
+int pml_step(const sa_plan* p, const float* cur, float* nxt, bool adjoint, float* snap, cudaStream_t s,
+             long long& n) {
+    if (!p->pml) return SA_OK;
+    CK(sa::pml2d(cur, nxt, p->pml_aux, p->pml_prof, row0(p, p->C1, p->pitch), p->vp, p->nx, p->ny, p->pitch,
+                 p->shot_stride, npairs(p), p->d.absorbing[0], p->d.absorbing[1], (float)p->d.spacing[0],
+                 (float)p->d.spacing[1], (float)p->d.dt, adjoint ? 1 : 0, snap, p->snap_shot_stride,
+                 (float)(1.0 / (p->d.dt * p->d.dt)), s));
+    n++;
+    return SA_OK;
+}
+
+int pml_clear(const sa_plan* p, cudaStream_t s) {
+    if (p->pml) CK(cudaMemsetAsync(p->pml_aux, 0, 6 * 2 * (size_t)npairs(p) * p->shot_stride * sizeof(float), s));
+    return SA_OK;
+}
+
 // Imaging from raw snapshots (SA_SAVE_RAW): on t % f == 0 the held vp (and rho) terms are
 // recomputed from slots t/f - 1 .. t/f + 1, and every step accumulates them against q = p_a[t]
 // (the reference's unconditioned Inc of a Function written under the undersampling condition,
@@ -549,6 +572,7 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
     a.save = save ? 1 : (raw ? 2 : 0);
     const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     long long n = 0;
+    CKR(pml_clear(p, s));
     if (raw) {
         const int f = p->d.undersampling, last = (p->d.nt - 2) / f;  // slots 1..last are written
         const size_t slot = (size_t)p->snap_stride * 2 * sizeof(float);
@@ -564,7 +588,10 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
         a.prev = (t & 1) ? p->field[0] : p->field[1];
         CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
         n++;
-        CKR(inject_sources(p, a.prev, t, p->snaps, p->snap_shot_stride, save && t % p->d.undersampling == 0, s, n));
+        const bool save_now = save && t % p->d.undersampling == 0;
+        CKR(pml_step(p, a.cur, a.prev, false,
+                     save_now ? p->snaps + 2 * (long long)(t / p->d.undersampling) * p->snap_stride : nullptr, s, n));
+        CKR(inject_sources(p, a.prev, t, p->snaps, p->snap_shot_stride, save_now, s, n));
         if (p->n_rec) {  // rec[t] = interp(p[t+1]) (linear or over the Hicks support)
             if (hicks)
                 CK(sa::hicks_gather2d(a.prev, p->shot_stride, p->pitch, p->hgat, p->n_rec, p->rec_amp, p->n_rec, t,
@@ -617,6 +644,7 @@ int issue_adjoint(sa_plan* p, bool wav, bool raw, bool rho, cudaStream_t s) {
     const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     const int T0 = p->d.nt - 1 - p->d.undersampling;
     long long n = 0;
+    CKR(pml_clear(p, s));
     for (int t = T0; t >= 1; t--) {
         a.t = t;
         const bool even = ((T0 - t) & 1) == 0;
@@ -624,6 +652,7 @@ int issue_adjoint(sa_plan* p, bool wav, bool raw, bool rho, cudaStream_t s) {
         a.prev = even ? p->field[0] : p->field[1];
         CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
         n++;
+        CKR(pml_step(p, a.cur, a.prev, true, nullptr, s, n));
         CKR(inject_receivers(p, a.prev, t, s, n));
         if (raw)
             CKR(image_raw_step(p, a.cur, t, rho, s, n));
@@ -872,6 +901,44 @@ long long sa_launch_count(const sa_plan* p) {
     return p->p3 ? sa::plan3d_launches(p->p3) : p->launches;
 }
 
+namespace {
+// CFS-PML profiles per axis (ComplexFrequencyShiftPML2.apply, stride/physics/boundaries/devito.py:
+// 96-127, with Boundary.damping, boundaries/boundary.py:59-170), FP32 as the reference stores them:
+// sigma 'power' degree 3 with the coefficient 2 ln(1/R) / (absorbing h) (0.67 / h for layers of 15
+// cells or fewer), times max(vp); alpha a 'power' degree 2 mask, 0.01 pi f_centre in the interior
+// and -0.01 pi f_centre pos^2 in the layer; sigma' and alpha' 2nd-order centred differences over an
+// edge-padded halo. Layout: sigma, alpha, sigma', alpha' of x (nx each), then of y (ny each).
+int pml_profiles(sa_plan* p) {
+    const sa_desc& d = p->d;
+    const int amax = std::max(d.absorbing[0], d.absorbing[1]);
+    const double refl = std::pow(10.0, -(std::log10((double)std::max(amax, 2)) - 1) / std::log10(2.0) - 3);
+    float vmax = 0.f;
+    for (float v : p->vp_host) vmax = std::max(vmax, v);
+    std::vector<float> out;
+    for (int a = 0; a < 2; a++) {
+        const int n = a == 0 ? p->nx : p->ny, A = d.absorbing[a];
+        const double h = d.spacing[a];
+        const double cs = A > 15 ? (3 + 1) / 2.0 * std::log(1.0 / refl) / (A * h) : 0.67 / h;
+        const double ca = 0.01 * M_PI * d.f_centre;
+        std::vector<float> sg(n, 0.f), al(n, (float)ca), dsg(n), dal(n);
+        for (int index = 0; index < A; index++) {
+            const double pos = std::fabs((A - index - 1) / (double)(A - 1));
+            sg[index] = sg[n - index - 1] = (float)(cs * pos * pos * pos);
+            al[index] = al[n - index - 1] = (float)(ca * -(pos * pos));
+        }
+        for (float& v : sg) v *= vmax;
+        for (int i = 0; i < n; i++) {
+            const int ip = std::min(i + 1, n - 1), im = std::max(i - 1, 0);
+            dsg[i] = (sg[ip] - sg[im]) / (float)(2 * h);
+            dal[i] = (al[ip] - al[im]) / (float)(2 * h);
+        }
+        for (auto* v : {&sg, &al, &dsg, &dal}) out.insert(out.end(), v->begin(), v->end());
+    }
+    CK(cudaMemcpy(p->pml_prof, out.data(), out.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return SA_OK;
+}
+}  // namespace
+
 int sa_plan_create(const sa_desc* desc, sa_plan** out) {
     if (!desc || !out) return fail(SA_E_INVALID, "null argument");
     *out = nullptr;
@@ -884,6 +951,11 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
         return fail(SA_E_INVALID, "interpolation %d", d.interpolation);
     if (d.interpolation == SA_INTERP_HICKS && d.dim != 2)
         return fail(SA_E_UNSUPPORTED, "Hicks interpolation is implemented for 2D plans");
+    if (d.boundary != SA_BOUNDARY_SPONGE && d.boundary != SA_BOUNDARY_CFS_PML)
+        return fail(SA_E_INVALID, "boundary %d", d.boundary);
+    if (d.boundary == SA_BOUNDARY_CFS_PML && (d.dim != 2 || d.kernel != SA_KERNEL_OT2))
+        return fail(SA_E_UNSUPPORTED, "the CFS-PML is implemented for 2D plans with OT2");
+    if (d.boundary == SA_BOUNDARY_CFS_PML && !(d.f_centre > 0)) return fail(SA_E_INVALID, "f_centre");
     if (d.nt < 3 || d.undersampling < 1 || d.max_shots < 1) return fail(SA_E_INVALID, "nt/undersampling/max_shots");
     for (int a = 0; a < d.dim; a++) {
         if (d.shape[a] < 24) return fail(SA_E_INVALID, "shape[%d] = %d is below 24 cells", a, d.shape[a]);
@@ -926,7 +998,8 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
     p->sponge.a[1] = d.absorbing[1];
     int amax = 0;
     for (int a = 0; a < d.dim; a++) amax = std::max(amax, d.absorbing[a]);
-    if (amax > 1) {
+    p->pml = d.boundary == SA_BOUNDARY_CFS_PML;
+    if (amax > 1 && !p->pml) {  // the CFS-PML replaces the sponge: no damping in the update
         const double refl = std::pow(10.0, -(std::log10((double)amax) - 1) / std::log10(2.0) - 3);
         damping_table(d.absorbing[0], d.spacing[0], refl, p->sponge.s[0]);
         damping_table(d.absorbing[1], d.spacing[1], refl, p->sponge.s[1]);
@@ -941,6 +1014,9 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
     if (rc == SA_OK) rc = ensure(&p->vp, &p->cap_vp, N);
     if (rc == SA_OK) rc = ensure(&p->alpha, &p->cap_alpha, N);
     if (rc == SA_OK && p->kind >= 1) rc = ensure(&p->buoy, &p->cap_buoy, N);  // b = 1/rho (rho gradient)
+    if (rc == SA_OK && p->pml) rc = ensure(&p->pml_prof, &p->cap_pml_prof, 4 * (size_t)(p->nx + p->ny));
+    if (rc == SA_OK && p->pml)  // six auxiliary fields for every shot pair the plan can hold
+        rc = ensure(&p->pml_aux, &p->cap_pml_aux, 6 * 2 * (size_t)((std::max(1, d.max_shots) + 1) / 2) * N);
     if (rc == SA_OK && p->kind == 1) {
         if (rc == SA_OK) rc = ensure(&p->bxh, &p->cap_bxh, (size_t)(p->nx + 9 + 2 * sa::GUARD) * p->pitch);
         if (rc == SA_OK) rc = ensure(&p->byh, &p->cap_byh, (size_t)(p->nx + 2 * sa::GUARD) * p->pitch_b);
@@ -978,7 +1054,7 @@ int sa_plan_destroy(sa_plan* p) {
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
                     p->ones_g, p->zeros_g, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
-                    p->dbx, p->dby,
+                    p->dbx, p->dby, p->pml_prof, p->pml_aux,
                     p->wgrad, p->hgat, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
                     p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx, p->xtgt.off, p->xtgt.point, p->xtgt.coef};
     for (void* b : bufs)
@@ -1025,6 +1101,7 @@ int sa_set_medium(sa_plan* p, const float* vp, const float* rho, const float* al
             for (int y = 0; y < p->ny; y++)
                 p->c1w_host[(size_t)x * p->ny + y] = c1[(size_t)x * p->pitch + y] * w[(size_t)x * p->pitch + y];
     }
+    if (p->pml) CKR(pml_profiles(p));
     p->exact_coef_valid = false;
     p->rho_terms_valid = false;
     p->medium_set = true;
@@ -1095,6 +1172,8 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
     if (save_mode != SA_SAVE_NONE && save_mode != SA_SAVE_SNAPSHOTS && save_mode != SA_SAVE_CHECKPOINTS &&
         save_mode != SA_SAVE_RAW)
         return fail(SA_E_INVALID, "save_mode %d", save_mode);
+    if (p->pml && save_mode == SA_SAVE_CHECKPOINTS)
+        return fail(SA_E_UNSUPPORTED, "checkpoints are implemented for the sponge boundary");
     if (p->p3) {
         if (save_mode == SA_SAVE_RAW) return fail(SA_E_UNSUPPORTED, "SA_SAVE_RAW is implemented for 2D plans");
         return sa::plan3d_forward(p->p3, wavelets, traces, save_mode, (cudaStream_t)stream);

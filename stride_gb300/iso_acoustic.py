@@ -30,7 +30,7 @@ except Exception:  # noqa: BLE001
     _mosaic = None
 
 DB_TO_NEPER = 100 * (1e-6 / (2 * np.pi)) ** 0 / (20 * np.log10(np.exp(1)))
-SUPPORTED_BOUNDARIES = ('sponge_boundary_2',)
+SUPPORTED_BOUNDARIES = ('sponge_boundary_2', 'complex_frequency_shift_PML_2')
 KNOWN_BOUNDARIES = ('sponge_boundary_2', 'complex_frequency_shift_PML_2', 'sponge_boundary_1')
 SUPPORTED_INTERPOLATION = ('linear', 'hicks')
 KNOWN_INTERPOLATION = ('linear', 'hicks', 'sinc')
@@ -121,11 +121,12 @@ class IsoAcousticGB300(ProblemTypeBase):
     ``boundary_type='sponge_boundary_2'``, ``interpolation_type='linear'``,
     ``attenuation_power=0``, ``diff_source``, ``save_undersampling``, ``save_wavefield``.
     ``platform``, ``devito_config`` and ``devito_args`` are accepted and ignored (the time
-    loop always runs on the GPU). Gradients: vp, rho (2D) and the wavelets; alpha raises
-    ValueError('Variable alpha not implemented') as in the reference, which has no alpha
-    gradient. Options the reference supports but this build does not (CFS-PML boundary, sinc
-    interpolation, attenuation power 2) raise NotImplementedError; unknown values raise
-    ValueError as in the reference.
+    loop always runs on the GPU). ``boundary_type='complex_frequency_shift_PML_2'`` runs in 2D
+    with kernel OT2 (the combination the reference's own example runs). Gradients: vp, rho (2D)
+    and the wavelets; alpha raises ValueError('Variable alpha not implemented') as in the
+    reference, which has no alpha gradient. Options the reference supports but this build does
+    not (the CFS-PML with OT4 or in 3D, sinc interpolation, attenuation power 2) raise
+    NotImplementedError; unknown values raise ValueError as in the reference.
     """
 
     space_order = 10
@@ -177,6 +178,8 @@ class IsoAcousticGB300(ProblemTypeBase):
             raise NotImplementedError('the rho gradient is implemented for 2D problems')
         self._check_conditions(wavelets, vp, rho, alpha, kwargs.get('kernel', None),
                                kwargs.get('save_undersampling', None), **kwargs)
+        if self.boundary_type == 'complex_frequency_shift_PML_2' and (self.kernel != 'OT2' or self.space.dim != 2):
+            raise NotImplementedError('complex_frequency_shift_PML_2 is implemented for 2D problems with kernel OT2')
 
     def _check_conditions(self, wavelets, vp, rho=None, alpha=None, preferred_kernel=None,
                           preferred_undersampling=None, **kwargs):
@@ -233,13 +236,15 @@ class IsoAcousticGB300(ProblemTypeBase):
         space, time = self.space, self.time
         key = (space.extended_shape, space.spacing, space.extra, space.absorbing, time.step, time.extended_num,
                self.kernel, self._density_mode(rho), alpha is not None, self.undersampling_factor, n_shots,
-               self.interpolation_type)
+               self.interpolation_type, self.boundary_type, float(self._bandwidth[1]))
         plan = self._plans.get(key)
         if plan is None:
             plan = _lib.Plan(space.dim, space.extended_shape, space.spacing, space.extra, space.absorbing,
                              time.step, time.extended_num, kernel=self.kernel, density=key[7],
                              attenuation=alpha is not None, undersampling=self.undersampling_factor,
-                             max_shots=n_shots, interpolation=self.interpolation_type)
+                             max_shots=n_shots, interpolation=self.interpolation_type,
+                             boundary='pml' if self.boundary_type == 'complex_frequency_shift_PML_2' else 'sponge',
+                             f_centre=float(self._bandwidth[1]))
             self._plans = {key: plan}  # one live plan: the previous one's device memory is released
         self._plan = plan
         return plan

@@ -8,10 +8,9 @@ from oracle import numpy_oracle as npo
 from stride_gb300 import phantoms
 
 
-def small_case(kernel='OT4', density='none', alpha=False, inner=64, nt=300, seed=0, n_shots=1, uneven=False):
+def small_case(kernel='OT4', density='none', alpha=False, inner=64, nt=300, seed=0, n_shots=1, uneven=False, extra=12):
     """A reduced 2D case with the structure of the benchmark workloads."""
     rng = np.random.default_rng(seed)
-    extra = 12
     h = 0.5e-3
     shape_i = (inner, inner + 7)  # non-square on purpose
     vpi, rhoi, ali = phantoms.ellipse_phantom(shape_i, (h, h), 4, rng, rho_range=(950., 1100.),

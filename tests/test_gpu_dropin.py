@@ -13,11 +13,11 @@ from tests import _cases as C
 pytestmark = pytest.mark.gpu
 
 
-def _setup(density=True, alpha=True, nt=300, n=60):
+def _setup(density=True, alpha=True, nt=300, n=60, cfl=0.6):
     rng = np.random.default_rng(5)
     h = 0.5e-3
     space = problem.Space((n, n + 4), h, extra=(12, 12), absorbing=(12, 12))
-    time = problem.Time(0., 0.6 * h / 1650, nt)
+    time = problem.Time(0., cfl * h / 1650, nt)
     grid = problem.Grid(space, time)
     vpi, rhoi, ali = phantoms.ellipse_phantom(space.shape, space.spacing, 3, rng, rho_range=(950., 1100.),
                                               alpha_range=(0., 1.), disk_radius=8e-3, axes=(2e-3, 6e-3))
@@ -133,3 +133,17 @@ def test_pde_alpha_gradient_is_not_implemented():
     residual = shot.observed.alike(name='residual', data=traces.data)
     with pytest.raises(ValueError, match='alpha not implemented'):
         pde.adjoint(residual, shot.wavelets, vp, rho, al, problem=sub)
+
+
+def test_pde_cfs_pml():
+    """boundary_type='complex_frequency_shift_PML_2' with kernel OT2: traces against the oracle's
+    CFS-PML with the band centre the drop-in estimated (IsoAcousticDevito._bandwidth[1])."""
+    space, time, vp, rho, al, shot, sub, geo, w = _setup(True, True, cfl=0.4)
+    pde = iso_acoustic.IsoAcousticGB300(space=space, time=time)
+    traces = pde(shot.wavelets, vp, rho=rho, alpha=al, problem=sub, boundary_type='complex_frequency_shift_PML_2',
+                 kernel='OT2')
+    ref, _ = O.forward(vp.extended_data, space.spacing, time.step, time.num, space.absorbing, geo[:1], geo, w[None],
+                       space.pml_origin, rho=rho.extended_data, alpha=al.extended_data, kernel='OT2',
+                       boundary='pml', f_centre=pde._bandwidth[1])
+    assert np.abs(ref).max() > 0
+    assert C.rel_l2(traces.data, ref) <= 1e-4

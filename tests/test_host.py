@@ -42,6 +42,16 @@ def test_option_errors(kw, exc):
         pde._check_problem(shot.wavelets, vp, problem=sub, **kw)
 
 
+def test_cfs_pml_runs_with_ot2_in_2d():
+    """The CFS-PML is accepted with OT2 (the reference example's combination) and refused with OT4."""
+    pde, shot, sub, vp, grid = _setup()
+    pde._check_problem(shot.wavelets, vp, problem=sub, boundary_type='complex_frequency_shift_PML_2', kernel='OT2')
+    assert pde.boundary_type == 'complex_frequency_shift_PML_2' and pde.kernel == 'OT2'
+    with pytest.raises(NotImplementedError):
+        pde._check_problem(shot.wavelets, vp, problem=sub, boundary_type='complex_frequency_shift_PML_2',
+                           kernel='OT4')
+
+
 def test_attenuation_power_errors():
     pde, shot, sub, vp, grid = _setup()
     alpha = problem.ScalarField('alpha', grid)

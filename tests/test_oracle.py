@@ -223,3 +223,20 @@ def test_raw_vp_gradient_matches_snapshot_path_at_f1():
                                        raw, raw=True, rho_grad=True, **kw)
     assert np.abs(g).max() > 0 and np.abs(g_rho).max() > 0 and p_rho.min() >= 0
     assert np.linalg.norm(g_raw - g) <= 1e-6 * np.linalg.norm(g)  # FP32 snapshots and outputs
+
+
+def test_cfs_pml_absorbs_better_than_the_sponge():
+    """The CFS-PML restatement (OT2) against a domain large enough that nothing returns from its
+    edges: its traces stay within 3 % where the 20-cell sponge is off by several per cent."""
+    h, e, n, nt = 0.5e-3, 20, 40, 700
+    dt = 0.4 * h / 1650
+    src = np.array([[10 * h, 20 * h]])
+    rec = np.array([[30 * h, 20 * h], [20 * h, 38 * h]])
+    w = O.tone_burst(0.5e6, 3, nt, dt)[None]
+    run = lambda E, **kw: O.forward(np.full((n + 2 * E,) * 2, 1500., np.float32), (h, h), dt, nt, (E, E), src, rec,
+                                    w, (-E * h, -E * h), kernel='OT2', **kw)[0]
+    big = run(120)
+    pml = run(e, boundary='pml', f_centre=0.5e6)
+    sponge = run(e)
+    err = lambda tr: np.linalg.norm(tr - big) / np.linalg.norm(big)
+    assert err(pml) < 0.03 and err(pml) < err(sponge) / 3
