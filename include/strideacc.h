@@ -39,7 +39,7 @@ extern "C" {
 #define SA_SAVE_CHECKPOINTS 2 /* store the state every checkpoint interval; the adjoint recomputes each
                                  segment's p.dt2 from its checkpoint (same gradient, less memory) */
 #define SA_SAVE_RAW 3         /* store p[t] itself every f steps, as the reference does when the rho or
-                                 wavelet gradient is needed (iso_acoustic/devito.py:410-413); 2D */
+                                 wavelet gradient is needed (iso_acoustic/devito.py:410-413) */
 
 #define SA_INTERP_LINEAR 0    /* bilinear / trilinear SparseTimeFunction (common/devito.py:580-653) */
 #define SA_INTERP_HICKS 1     /* Kaiser-windowed sinc, 8 points per axis (common/devito.py:640-648,843-885);
@@ -131,7 +131,7 @@ int sa_adjoint(sa_plan* plan, const float* residuals, float* grad_vp, float* pre
 int sa_adjoint_wavelets(sa_plan* plan, const float* residuals, float* grad_vp, float* prec_vp, float* grad_wavelets,
                         int grad_mode, void* stream);
 
-/* The adjoint after a forward with SA_SAVE_RAW (2D), with the gradients the reference forms from
+/* The adjoint after a forward with SA_SAVE_RAW (2D and 3D), with the gradients the reference forms from
  * the raw saved wavefield p_s[n] = p[n f] (iso_acoustic/devito.py:985-1024, 1115-1150):
  *   vp:  p_dt = (p_s[n+1] - 2 p_s[n] + p_s[n-1]) / (f dt)^2,
  *   rho: g = -grad(b, shift=-1/2) . grad(p_s[n], shift=-1/2) - b laplace(p_s[n]), b = 1/rho,
@@ -140,7 +140,7 @@ int sa_adjoint_wavelets(sa_plan* plan, const float* residuals, float* grad_vp, f
  * step: grad += held * p_a, prec += held^2, interior points, summed over the shots.
  * grad_vp/prec_vp [N] are required; grad_rho/prec_rho [N] (both or neither; the plan needs
  * rho, SA_DENSITY_VARIABLE or SA_DENSITY_CONSTANT) and grad_wavelets [n_src_total, nt]
- * (as sa_adjoint_wavelets) are optional. Host or device pointers. Replaces run_adjoint with
+ * (as sa_adjoint_wavelets, 2D) are optional. Host or device pointers. Replaces run_adjoint with
  * rho.needs_grad and/or wavelets.needs_grad, and get_grad_rho (:1171-1208). */
 int sa_adjoint_grads(sa_plan* plan, const float* residuals, float* grad_vp, float* prec_vp, float* grad_rho,
                      float* prec_rho, float* grad_wavelets, void* stream);

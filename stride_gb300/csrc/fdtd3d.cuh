@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
                 const float pn = c1v[r] * res[r] + c2v[r] * u_o - c3v[r] * pm;
                 if (do_save) {
                     a.snaps[(long long)shot * a.snap_shot_stride + (long long)(a.t / a.f) * a.snap_stride + idx] =
-                        (pn - 2.f * u_o + pm) / dt2;
+                        a.save == 2 ? u_o : (pn - 2.f * u_o + pm) / dt2;  // 2: raw p[t] (rho gradient)
                 }
                 a.prev[soff + idx] = pn;
             }

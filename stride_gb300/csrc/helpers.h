@@ -41,6 +41,14 @@ cudaError_t sparse3d_gather(const Sparse3D& sp, int n, const float* field, long 
                             float* out, int ld, int trow, cudaStream_t s);
 cudaError_t image3d(const float* q, const float* snap, float* gradb, float* precb, const int* lo, const int* hi,
                     int ny, int zp, int nshots, long long field, long long snap_shot_stride, cudaStream_t s);
+// 3D rho-gradient medium terms (D-b per axis) and raw-snapshot imaging (held terms, every step).
+cudaError_t rho_terms3d(const float* b, int nx, int ny, int nz, int zp, const double* h, float* dbx, float* dby,
+                        float* dbz, cudaStream_t s);
+cudaError_t image_raw3d(const float* q, const float* snap, long long snap_stride, long long snap_shot_stride,
+                        int refresh, float inv_fdt2, float* hold_vp, float* hold_rho, const float* buoy,
+                        const float* dbx, const float* dby, const float* dbz, const double* h, int nx, int ny, int nz,
+                        int zp, float* gradb, float* precb, float* gradrb, float* precrb, const int* lo,
+                        const int* hi, int nshots, long long field, cudaStream_t s);
 cudaError_t reduce3d(const float* buf, long long shot_stride, int nshots, int nx, int ny, int nz, int zp, float* out,
                      cudaStream_t s);
 cudaError_t transpose(const float* in, int rows, int cols, float* out, cudaStream_t s);

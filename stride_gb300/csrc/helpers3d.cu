@@ -19,9 +19,9 @@ __global__ void k_medium3d(const float* __restrict__ vp_in, const float* __restr
         const float v = vp_in[q];
         vp[p] = v;
         float w = v * v;
-        if (density == 1) {
+        if (density >= 1) {  // 1: variable density (W = vp^2 rho), 2: constant (b kept for the rho gradient)
             const float r = rho_in[q];
-            w = w * r;
+            if (density == 1) w = w * r;
             buoy[p] = 1.f / r;
         }
         W[p] = w;
@@ -187,6 +187,118 @@ cudaError_t image3d(const float* q, const float* snap, float* gradb, float* prec
     const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 16);
     k_image3d<<<blocks, 256, 0, s>>>(q, snap, gradb, precb, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], ny, zp, nshots,
                                      field, snap_shot_stride);
+    return cudaGetLastError();
+}
+
+// D-_x b, D-_y b, D-_z b at every node (staggered first derivatives at i-1/2 of the edge-padded
+// buoyancy), the grad(buoy, shift=-0.5) factor of the rho imaging term (iso_acoustic/devito.py:1137).
+__global__ void k_rho_terms3d(const float* __restrict__ b, int nx, int ny, int nz, int zp, float ihx, float ihy,
+                              float ihz, float* dbx, float* dby, float* dbz) {
+    const long long n = (long long)nx * ny * nz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(q % nz);
+        const int y = (int)((q / nz) % ny);
+        const int x = (int)(q / ((long long)nz * ny));
+        auto at = [&](int xx, int yy, int zz) { return b[((long long)xx * ny + yy) * zp + zz]; };
+        float ax = 0.f, ay = 0.f, az = 0.f;
+#pragma unroll
+        for (int m = 0; m < 5; m++) {
+            ax += kWS(m) * (at(min(x + m, nx - 1), y, z) - at(max(x - 1 - m, 0), y, z));
+            ay += kWS(m) * (at(x, min(y + m, ny - 1), z) - at(x, max(y - 1 - m, 0), z));
+            az += kWS(m) * (at(x, y, min(z + m, nz - 1)) - at(x, y, max(z - 1 - m, 0)));
+        }
+        const long long i = ((long long)x * ny + y) * zp + z;
+        dbx[i] = ax * ihx;
+        dby[i] = ay * ihy;
+        dbz[i] = az * ihz;
+    }
+}
+
+cudaError_t rho_terms3d(const float* b, int nx, int ny, int nz, int zp, const double* h, float* dbx, float* dby,
+                        float* dbz, cudaStream_t s) {
+    k_rho_terms3d<<<2048, 256, 0, s>>>(b, nx, ny, nz, zp, (float)(1.0 / h[0]), (float)(1.0 / h[1]),
+                                       (float)(1.0 / h[2]), dbx, dby, dbz);
+    return cudaGetLastError();
+}
+
+// Imaging from the raw saved wavefield s[n] = p[n f] in 3D (the 2D k_image_raw2d per shot): on a
+// refresh step the held vp term (s[n+1] - 2 s[n] + s[n-1]) inv_fdt2 and, with hold_rho, the rho
+// term -(grad(b, -1/2) . grad(s[n], -1/2)) - b laplace(s[n]) (zero halo for s) are recomputed at
+// every interior point; every step accumulates grad += held q, prec += held^2.
+// snap addresses slot n of shot 0.
+__global__ void k_image_raw3d(const float* __restrict__ q, const float* __restrict__ snap, long long snap_stride,
+                              long long snap_shot_stride, int refresh, float inv_fdt2, float* hold_vp,
+                              float* hold_rho, const float* __restrict__ buoy, const float* __restrict__ dbx,
+                              const float* __restrict__ dby, const float* __restrict__ dbz, float ihx, float ihy,
+                              float ihz, int nx, int ny, int nz, int zp, float* gradb, float* precb, float* gradrb,
+                              float* precrb, int ix0, int ix1, int iy0, int iy1, int iz0, int iz1, int nshots,
+                              long long field) {
+    const int wz = iz1 - iz0, wy = iy1 - iy0;
+    const long long per = (long long)(ix1 - ix0) * wy * wz;
+    const long long sx = (long long)ny * zp, sy = zp;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < per * nshots;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int shot = (int)(e / per);
+        long long r = e - (long long)shot * per;
+        const int z = iz0 + (int)(r % wz);
+        r /= wz;
+        const int y = iy0 + (int)(r % wy);
+        const int x = ix0 + (int)(r / wy);
+        const long long idx = ((long long)x * ny + y) * zp + z;
+        const long long gi = (long long)shot * field + idx;
+        float hv, hr = 0.f;
+        if (refresh) {
+            const float* sp = snap + (long long)shot * snap_shot_stride;
+            const float s0 = sp[idx];
+            hv = ((sp[idx + snap_stride] - 2.f * s0) + sp[idx - snap_stride]) * inv_fdt2;
+            hold_vp[gi] = hv;
+            if (hold_rho) {
+                float g[3] = {0.f, 0.f, 0.f}, l[3] = {kW2(0) * s0, kW2(0) * s0, kW2(0) * s0};
+                const int pos[3] = {x, y, z}, n[3] = {nx, ny, nz};
+                const long long st[3] = {sx, sy, 1};
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+#pragma unroll
+                    for (int m = 0; m < 5; m++) {
+                        const float hi = pos[d] + m < n[d] ? sp[idx + m * st[d]] : 0.f;
+                        const float lo = pos[d] - 1 - m >= 0 ? sp[idx - (m + 1) * st[d]] : 0.f;
+                        g[d] += kWS(m) * (hi - lo);
+                        const int k = m + 1;
+                        const float fp = pos[d] + k < n[d] ? sp[idx + k * st[d]] : 0.f;
+                        const float fm = pos[d] - k >= 0 ? sp[idx - k * st[d]] : 0.f;
+                        l[d] += kW2(k) * (fp + fm);
+                    }
+                }
+                hr = -(dbx[idx] * (g[0] * ihx) + dby[idx] * (g[1] * ihy) + dbz[idx] * (g[2] * ihz)) -
+                     buoy[idx] * (l[0] * (ihx * ihx) + l[1] * (ihy * ihy) + l[2] * (ihz * ihz));
+                hold_rho[gi] = hr;
+            }
+        } else {
+            hv = hold_vp[gi];
+            if (hold_rho) hr = hold_rho[gi];
+        }
+        const float u = q[gi];
+        gradb[gi] += hv * u;
+        precb[gi] += hv * hv;
+        if (hold_rho) {
+            gradrb[gi] += hr * u;
+            precrb[gi] += hr * hr;
+        }
+    }
+}
+
+cudaError_t image_raw3d(const float* q, const float* snap, long long snap_stride, long long snap_shot_stride,
+                        int refresh, float inv_fdt2, float* hold_vp, float* hold_rho, const float* buoy,
+                        const float* dbx, const float* dby, const float* dbz, const double* h, int nx, int ny, int nz,
+                        int zp, float* gradb, float* precb, float* gradrb, float* precrb, const int* lo,
+                        const int* hi, int nshots, long long field, cudaStream_t s) {
+    const long long n = (long long)(hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]) * nshots;
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 16);
+    k_image_raw3d<<<blocks, 256, 0, s>>>(q, snap, snap_stride, snap_shot_stride, refresh, inv_fdt2, hold_vp, hold_rho,
+                                         buoy, dbx, dby, dbz, (float)(1.0 / h[0]), (float)(1.0 / h[1]),
+                                         (float)(1.0 / h[2]), nx, ny, nz, zp, gradb, precb, gradrb, precrb, lo[0],
+                                         hi[0], lo[1], hi[1], lo[2], hi[2], nshots, field);
     return cudaGetLastError();
 }
 

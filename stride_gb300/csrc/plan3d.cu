@@ -129,6 +129,9 @@ struct Plan3D {
     int ck_K = 0, ck_n = 0;
     bool ckpt_valid = false;
     float *gradb = nullptr, *precb = nullptr;
+    // raw snapshots (SA_SAVE_RAW): held vp/rho terms per shot, rho accumulators, D-b per axis
+    bool snaps_raw = false, rho_valid = false;
+    float *hold_vp = nullptr, *hold_rho = nullptr, *gradrb = nullptr, *precrb = nullptr, *db[3] = {};
     long long launches = 0;
     int chunk_rows = 0, nchunks = 1, ty0n = 1, tz0n = 1;
 };
@@ -171,8 +174,8 @@ int plan3d_create(const sa_desc& d, Plan3D** out) {
     if (rc == SA_OK) rc = alloc3(&p->C3, guarded);
     if (rc == SA_OK) rc = alloc3(&p->vp, (size_t)p->field);
     if (rc == SA_OK) rc = alloc3(&p->alpha, (size_t)p->field);
+    if (rc == SA_OK && p->kind >= 1) rc = alloc3(&p->buoy, (size_t)p->field);  // b = 1/rho (rho gradient)
     if (rc == SA_OK && p->kind == 1) {
-        rc = alloc3(&p->buoy, (size_t)p->field);
         if (rc == SA_OK) rc = alloc3(&p->bxh, (size_t)(p->nx + 9 + 2 * G) * p->plane);
         if (rc == SA_OK) rc = alloc3(&p->byh, (size_t)(p->nx + 2 * G) * (p->ny + 12) * p->zp);
         if (rc == SA_OK) rc = alloc3(&p->bzh, (size_t)(p->nx + 2 * G) * p->ny * p->zpb);
@@ -191,7 +194,8 @@ void plan3d_destroy(Plan3D* p) {
     if (!p) return;
     float* fb[] = {p->F[0], p->F[1], p->Lbuf, p->W, p->C1, p->C2, p->C3, p->bxh, p->byh, p->bzh, p->vp, p->alpha,
                    p->buoy, p->stage, p->s_w, p->s_coef, p->r_w, p->r_coef, p->src_amp, p->rec_amp, p->tstage,
-                   p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps, p->A[0], p->A[1]};
+                   p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps, p->A[0], p->A[1], p->hold_vp, p->hold_rho,
+                   p->gradrb, p->precrb, p->db[0], p->db[1], p->db[2]};
     for (float* b : fb)
         if (b) cudaFree(b);
     int* ib[] = {p->s_shot, p->s_base, p->r_shot, p->r_base};
@@ -202,7 +206,7 @@ void plan3d_destroy(Plan3D* p) {
 
 int plan3d_set_medium(Plan3D* p, const float* vp, const float* rho, const float* alpha) {
     const size_t N = (size_t)p->nx * p->ny * p->nz;
-    const float* in[3] = {vp, p->kind == 1 ? rho : nullptr, p->d.attenuation ? alpha : nullptr};
+    const float* in[3] = {vp, p->kind >= 1 ? rho : nullptr, p->d.attenuation ? alpha : nullptr};
     const float* dv[3] = {nullptr, nullptr, nullptr};
     for (int k = 0; k < 3; k++) {
         if (!in[k]) continue;
@@ -218,7 +222,7 @@ int plan3d_set_medium(Plan3D* p, const float* vp, const float* rho, const float*
         }
     }
     const long long g0 = (long long)GUARD * p->plane;
-    CK3(medium3d(dv[0], dv[1], dv[2], p->nx, p->ny, p->nz, p->zp, p->zpb, p->kind == 1 ? 1 : 0,
+    CK3(medium3d(dv[0], dv[1], dv[2], p->nx, p->ny, p->nz, p->zp, p->zpb, p->kind,
                  100.0 / (20.0 * 0.43429448190325176), p->sponge, (float)p->d.dt, p->W + g0, p->vp, p->alpha, p->buoy,
                  p->bxh ? p->bxh + (long long)(GUARD + 5) * p->plane : nullptr,
                  p->byh ? p->byh + (long long)GUARD * (p->ny + 12) * p->zp : nullptr,
@@ -229,6 +233,7 @@ int plan3d_set_medium(Plan3D* p, const float* vp, const float* rho, const float*
     p->medium_set = true;
     p->snaps_valid = false;
     p->ckpt_valid = false;
+    p->rho_valid = false;
     if (p->geometry_set) return plan3d_set_geometry(p, p->n_shots, p->so.data(), p->sx.data(), p->ro.data(), p->rx.data());
     return SA_OK;
 }
@@ -364,6 +369,21 @@ static int image_level(Plan3D* p, const Step3D& a, const float* q, cudaStream_t 
     return SA_OK;
 }
 
+// Imaging from raw snapshots of adjoint level t, q = p_a[t]: held terms refreshed on t % f == 0,
+// accumulated every step (the 2D image_raw_step).
+static int image_raw_level(Plan3D* p, const Step3D& a, const float* q, bool rho, cudaStream_t s, long long& n) {
+    const bool refresh = a.t % a.f == 0;
+    const int lo[3] = {p->d.absorbing[0], p->d.absorbing[1], p->d.absorbing[2]};
+    const int hi[3] = {p->nx - p->d.absorbing[0], p->ny - p->d.absorbing[1], p->nz - p->d.absorbing[2]};
+    const double fdt = (double)a.f * p->d.dt;
+    CK3(image_raw3d(q, a.snaps + (long long)(refresh ? a.t / a.f : 0) * a.snap_stride, a.snap_stride,
+                    a.snap_shot_stride, refresh ? 1 : 0, (float)(1.0 / (fdt * fdt)), p->hold_vp,
+                    rho ? p->hold_rho : nullptr, p->buoy, p->db[0], p->db[1], p->db[2], p->d.spacing, p->nx, p->ny,
+                    p->nz, p->zp, p->gradb, p->precb, p->gradrb, p->precrb, lo, hi, p->n_shots, p->field, s));
+    n++;
+    return SA_OK;
+}
+
 // One time level: [pass A] + pass B, then injection into the new level (and its snapshot).
 static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, const Sparse3D& inj, int n_inj,
                  const float* amp, bool save_now, cudaStream_t s, long long& n) {
@@ -390,7 +410,8 @@ static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, const Spar
 
 int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mode, cudaStream_t s) {
     if (!p->medium_set || !p->geometry_set) return fail3(SA_E_INVALID, "medium and geometry must be set first");
-    const bool save = save_mode == SA_SAVE_SNAPSHOTS;
+    const bool raw = save_mode == SA_SAVE_RAW;
+    const bool save = save_mode == SA_SAVE_SNAPSHOTS || raw;
     const bool ckpt = save_mode == SA_SAVE_CHECKPOINTS;
     p->ckpt_valid = false;  // the wavelets the checkpointed adjoint re-injects are replaced
     if (save && (size_t)p->n_shots * p->n_snap * p->snap_stride > p->cap_snaps) {
@@ -416,7 +437,15 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
     CK3(cudaMemsetAsync(p->F[1], 0, fb, s));
     CK3(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * std::max(1, p->n_rec) * sizeof(float), s));
     Step3D a = args3(p);
-    a.save = save ? 1 : 0;
+    a.save = raw ? 2 : (save ? 1 : 0);
+    if (raw) {  // slots the loop does not write (n = 0, n f > nt-2) read as zero, the reference's fresh buffer
+        const int last = (p->d.nt - 2) / a.f;
+        const size_t slot = (size_t)p->snap_stride * sizeof(float), pitch = (size_t)a.snap_shot_stride * sizeof(float);
+        CK3(cudaMemset2DAsync(p->snaps, pitch, 0, slot, p->n_shots, s));
+        if (last + 1 < p->n_snap)
+            CK3(cudaMemset2DAsync(p->snaps + (size_t)(last + 1) * p->snap_stride, pitch, 0,
+                                  (size_t)(p->n_snap - last - 1) * slot, p->n_shots, s));
+    }
     const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
     const Sparse3D rec{p->r_shot, p->r_base, p->r_w, p->r_coef};
     long long n = p->n_src ? 1 : 0;
@@ -424,7 +453,7 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
         a.t = t;
         float* cur = (t & 1) ? p->F[1] : p->F[0];
         float* prev = (t & 1) ? p->F[0] : p->F[1];
-        rc = step3(p, a, cur, prev, src, p->n_src, p->src_amp, save && t % a.f == 0, s, n);
+        rc = step3(p, a, cur, prev, src, p->n_src, p->src_amp, save && !raw && t % a.f == 0, s, n);
         if (rc != SA_OK) return rc;
         if (p->n_rec) {  // rec[t] = interp(p[t+1])
             CK3(sparse3d_gather(rec, p->n_rec, prev, p->field, p->ny, p->zp, p->rec_amp, p->n_rec, t, s));
@@ -452,7 +481,10 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
         n++;
     }
     p->launches = n;
-    if (save) p->snaps_valid = true;
+    if (save) {
+        p->snaps_valid = true;
+        p->snaps_raw = raw;
+    }
     if (ckpt) p->ckpt_valid = true;
     return SA_OK;
 }
@@ -505,11 +537,33 @@ static int adjoint_segments(Plan3D* p, Step3D& aa, const Sparse3D& rec, cudaStre
     return SA_OK;
 }
 
-int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s) {
+int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s, float* grad_rho,
+                   float* prec_rho) {
     const bool ck = p->ckpt_valid;
     if (!p->snaps_valid && !ck)
         return fail3(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS or SA_SAVE_CHECKPOINTS");
+    const bool raw = !ck && p->snaps_raw;
+    const bool rho = grad_rho != nullptr;
+    if ((grad_rho == nullptr) != (prec_rho == nullptr)) return fail3(SA_E_INVALID, "grad_rho and prec_rho go together");
+    if (rho && !raw) return fail3(SA_E_INVALID, "the rho gradient needs a prior sa_forward with SA_SAVE_RAW");
+    if (rho && p->kind == 0) return fail3(SA_E_INVALID, "the rho gradient needs a plan with rho");
     int rc = SA_OK;
+    const size_t fl = (size_t)std::max(1, p->d.max_shots) * p->field;
+    if (raw) {
+        if (!p->hold_vp && (rc = alloc3(&p->hold_vp, fl)) != SA_OK) return rc;
+        if (rho) {
+            float** bufs[] = {&p->hold_rho, &p->gradrb, &p->precrb};
+            for (float** b : bufs)
+                if (!*b && (rc = alloc3(b, fl)) != SA_OK) return rc;
+            for (int k = 0; k < 3; k++)
+                if (!p->db[k] && (rc = alloc3(&p->db[k], (size_t)p->field)) != SA_OK) return rc;
+            if (!p->rho_valid) {
+                CK3(rho_terms3d(p->buoy, p->nx, p->ny, p->nz, p->zp, p->d.spacing, p->db[0], p->db[1], p->db[2], 0));
+                CK3(cudaDeviceSynchronize());
+                p->rho_valid = true;
+            }
+        }
+    }
     if (ck) {
         const size_t level = (size_t)std::max(1, p->d.max_shots) * p->field;
         for (int k = 0; k < 2; k++)
@@ -520,14 +574,20 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
             p->cap_segsnaps = need;
         }
     }
-    if (!p->gradb && (rc = alloc3(&p->gradb, (size_t)p->n_shots * p->field)) != SA_OK) return rc;
-    if (!p->precb && (rc = alloc3(&p->precb, (size_t)p->n_shots * p->field)) != SA_OK) return rc;
+    if (!p->gradb && (rc = alloc3(&p->gradb, fl)) != SA_OK) return rc;
+    if (!p->precb && (rc = alloc3(&p->precb, fl)) != SA_OK) return rc;
     if ((rc = load_tm(p, residuals, p->n_rec, p->d.nt, p->rec_amp, s)) != SA_OK) return rc;
     const size_t fb = (size_t)p->n_shots * p->field * sizeof(float);
     CK3(cudaMemsetAsync(p->F[0], 0, fb, s));
     CK3(cudaMemsetAsync(p->F[1], 0, fb, s));
     CK3(cudaMemsetAsync(p->gradb, 0, fb, s));
     CK3(cudaMemsetAsync(p->precb, 0, fb, s));
+    if (raw) CK3(cudaMemsetAsync(p->hold_vp, 0, fb, s));  // held terms start at zero
+    if (rho) {
+        CK3(cudaMemsetAsync(p->hold_rho, 0, fb, s));
+        CK3(cudaMemsetAsync(p->gradrb, 0, fb, s));
+        CK3(cudaMemsetAsync(p->precrb, 0, fb, s));
+    }
     Step3D a = args3(p);
     a.save = 0;
     const Sparse3D rec{p->r_shot, p->r_base, p->r_w, p->r_coef};
@@ -541,12 +601,13 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
         float* prev = even ? p->F[0] : p->F[1];
         rc = step3(p, a, cur, prev, rec, p->n_rec, p->rec_amp, false, s, n);
         if (rc != SA_OK) return rc;
-        if ((rc = image_level(p, a, cur, s, n)) != SA_OK) return rc;
+        rc = raw ? image_raw_level(p, a, cur, rho, s, n) : image_level(p, a, cur, s, n);
+        if (rc != SA_OK) return rc;
     }
     const size_t N = (size_t)p->nx * p->ny * p->nz;
-    for (int k = 0; k < 2; k++) {
-        float* user = k == 0 ? grad : prec;
-        const float* buf = k == 0 ? p->gradb : p->precb;
+    for (int k = 0; k < (rho ? 4 : 2); k++) {
+        float* user = k == 0 ? grad : (k == 1 ? prec : (k == 2 ? grad_rho : prec_rho));
+        const float* buf = k == 0 ? p->gradb : (k == 1 ? p->precb : (k == 2 ? p->gradrb : p->precrb));
         if (dev_ptr(user)) {
             CK3(reduce3d(buf, p->field, p->n_shots, p->nx, p->ny, p->nz, p->zp, user, s));
         } else {

@@ -11,7 +11,10 @@ void plan3d_destroy(Plan3D* p);
 int plan3d_set_medium(Plan3D* p, const float* vp, const float* rho, const float* alpha);
 int plan3d_set_geometry(Plan3D* p, int n_shots, const int* so, const float* sx, const int* ro, const float* rx);
 int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mode, cudaStream_t s);
-int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s);
+// grad_rho/prec_rho (both or neither) need a prior forward with SA_SAVE_RAW; after such a forward
+// the vp gradient follows the raw-wavefield path too.
+int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s,
+                   float* grad_rho = nullptr, float* prec_rho = nullptr);
 long long plan3d_launches(const Plan3D* p);
 // Checkpoint interval K (a multiple of f) and the number of stored checkpoints for a plan whose
 // two state levels take `level_bytes` (SA_SAVE_CHECKPOINTS, both dimensions).

@@ -1174,10 +1174,7 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
         return fail(SA_E_INVALID, "save_mode %d", save_mode);
     if (p->pml && save_mode == SA_SAVE_CHECKPOINTS)
         return fail(SA_E_UNSUPPORTED, "checkpoints are implemented for the sponge boundary");
-    if (p->p3) {
-        if (save_mode == SA_SAVE_RAW) return fail(SA_E_UNSUPPORTED, "SA_SAVE_RAW is implemented for 2D plans");
-        return sa::plan3d_forward(p->p3, wavelets, traces, save_mode, (cudaStream_t)stream);
-    }
+    if (p->p3) return sa::plan3d_forward(p->p3, wavelets, traces, save_mode, (cudaStream_t)stream);
     if (!p->medium_set || !p->geometry_set) return fail(SA_E_INVALID, "medium and geometry must be set first");
     if ((p->n_src && !wavelets) || (p->n_rec && !traces)) return fail(SA_E_INVALID, "null wavelets or traces");
     cudaStream_t s = (cudaStream_t)stream;
@@ -1227,8 +1224,13 @@ int sa_adjoint_wavelets(sa_plan* p, const float* residuals, float* grad_vp, floa
 int sa_adjoint_grads(sa_plan* p, const float* residuals, float* grad_vp, float* prec_vp, float* grad_rho,
                      float* prec_rho, float* grad_wavelets, void* stream) {
     if (!p) return fail(SA_E_INVALID, "null plan");
-    if (p->p3) return fail(SA_E_UNSUPPORTED, "sa_adjoint_grads is implemented for 2D plans");
-    if (!p->snaps_valid || !p->snaps_raw) return fail(SA_E_INVALID, "sa_adjoint_grads needs a prior sa_forward with SA_SAVE_RAW");
+    if (p->p3) {
+        if (grad_wavelets) return fail(SA_E_UNSUPPORTED, "the wavelet gradient is implemented for 2D plans");
+        if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
+        return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream, grad_rho, prec_rho);
+    }
+    if (!p->snaps_valid || !p->snaps_raw)
+        return fail(SA_E_INVALID, "sa_adjoint_grads needs a prior sa_forward with SA_SAVE_RAW");
     if ((grad_rho == nullptr) != (prec_rho == nullptr)) return fail(SA_E_INVALID, "grad_rho and prec_rho go together");
     if (grad_rho && p->kind == 0) return fail(SA_E_INVALID, "the rho gradient needs a plan with rho");
     return adjoint_impl(p, residuals, grad_vp, prec_vp, grad_rho, prec_rho, grad_wavelets, SA_GRAD_PARITY, stream);

@@ -122,8 +122,8 @@ class IsoAcousticGB300(ProblemTypeBase):
     ``attenuation_power=0``, ``diff_source``, ``save_undersampling``, ``save_wavefield``.
     ``platform``, ``devito_config`` and ``devito_args`` are accepted and ignored (the time
     loop always runs on the GPU). ``boundary_type='complex_frequency_shift_PML_2'`` runs in 2D
-    with kernel OT2 (the combination the reference's own example runs). Gradients: vp, rho (2D)
-    and the wavelets; alpha raises ValueError('Variable alpha not implemented') as in the
+    with kernel OT2 (the combination the reference's own example runs). Gradients: vp, rho and
+    the wavelets (2D); alpha raises ValueError('Variable alpha not implemented') as in the
     reference, which has no alpha gradient. Options the reference supports but this build does
     not (the CFS-PML with OT4 or in 3D, sinc interpolation, attenuation power 2) raise
     NotImplementedError; unknown values raise ValueError as in the reference.
@@ -174,8 +174,6 @@ class IsoAcousticGB300(ProblemTypeBase):
         if kwargs.get('drp', False):
             self.logger.warning('DRP weights are not implemented in this version of stride')
         self.drp = False
-        if rho is not None and getattr(rho, 'needs_grad', False) and self.space.dim != 2:
-            raise NotImplementedError('the rho gradient is implemented for 2D problems')
         self._check_conditions(wavelets, vp, rho, alpha, kwargs.get('kernel', None),
                                kwargs.get('save_undersampling', None), **kwargs)
         if self.boundary_type == 'complex_frequency_shift_PML_2' and (self.kernel != 'OT2' or self.space.dim != 2):
