@@ -127,7 +127,7 @@ int sa_adjoint(sa_plan* plan, const float* residuals, float* grad_vp, float* pre
 /* sa_adjoint plus the gradient with respect to the wavelets: grad_wavelets [n_src_total, nt]
  * (host or device) receives -interp(p_a[t]) at the sources for t = 1 .. nt-1-f and zero
  * elsewhere, the reference's src.interpolate(expr=-p_a) (iso_acoustic/devito.py:755-756) read back
- * by get_grad_wavelets (:1226-1262). 2D, grad_mode SA_GRAD_PARITY. */
+ * by get_grad_wavelets (:1226-1262). grad_mode SA_GRAD_PARITY; linear interpolation. */
 int sa_adjoint_wavelets(sa_plan* plan, const float* residuals, float* grad_vp, float* prec_vp, float* grad_wavelets,
                         int grad_mode, void* stream);
 
@@ -140,7 +140,7 @@ int sa_adjoint_wavelets(sa_plan* plan, const float* residuals, float* grad_vp, f
  * step: grad += held * p_a, prec += held^2, interior points, summed over the shots.
  * grad_vp/prec_vp [N] are required; grad_rho/prec_rho [N] (both or neither; the plan needs
  * rho, SA_DENSITY_VARIABLE or SA_DENSITY_CONSTANT) and grad_wavelets [n_src_total, nt]
- * (as sa_adjoint_wavelets, 2D) are optional. Host or device pointers. Replaces run_adjoint with
+ * (as sa_adjoint_wavelets) are optional. Host or device pointers. Replaces run_adjoint with
  * rho.needs_grad and/or wavelets.needs_grad, and get_grad_rho (:1171-1208). */
 int sa_adjoint_grads(sa_plan* plan, const float* residuals, float* grad_vp, float* prec_vp, float* grad_rho,
                      float* prec_rho, float* grad_wavelets, void* stream);

@@ -298,6 +298,6 @@ struct Sparse3D {
 __global__ void inject3d(const Sparse3D s, int n, const float* amp, int ld, int t, float* field, long long shot_stride,
                          int ny, int zp, float* snap, long long snap_shot_stride, long long snap_off, float inv_dt2);
 __global__ void gather3d(const Sparse3D s, int n, const float* field, long long shot_stride, int ny, int zp, float* out,
-                         int ld, int trow);
+                         int ld, int trow, float scale);
 
 }  // namespace sa

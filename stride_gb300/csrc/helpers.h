@@ -37,8 +37,9 @@ cudaError_t medium3d(const float* vp_in, const float* rho_in, const float* alpha
 cudaError_t sparse3d_inject(const Sparse3D& sp, int n, const float* amp, int ld, int t, float* field,
                             long long shot_stride, int ny, int zp, float* snap, long long snap_shot_stride,
                             long long snap_off, float inv_dt2, cudaStream_t s);
+// out[trow][k] = scale * trilinear interpolation of the field at point k
 cudaError_t sparse3d_gather(const Sparse3D& sp, int n, const float* field, long long shot_stride, int ny, int zp,
-                            float* out, int ld, int trow, cudaStream_t s);
+                            float* out, int ld, int trow, cudaStream_t s, float scale = 1.f);
 cudaError_t image3d(const float* q, const float* snap, float* gradb, float* precb, const int* lo, const int* hi,
                     int ny, int zp, int nshots, long long field, long long snap_shot_stride, cudaStream_t s);
 // 3D rho-gradient medium terms (D-b per axis) and raw-snapshot imaging (held terms, every step).

@@ -107,7 +107,7 @@ __global__ void inject3d(const Sparse3D s, int n, const float* amp, int ld, int 
 }
 
 __global__ void gather3d(const Sparse3D s, int n, const float* field, long long shot_stride, int ny, int zp, float* out,
-                         int ld, int trow) {
+                         int ld, int trow, float scale) {
     const int pnt = blockIdx.x * blockDim.x + threadIdx.x;
     if (pnt >= n) return;
     const int* b = s.base + 3 * pnt;
@@ -117,7 +117,7 @@ __global__ void gather3d(const Sparse3D s, int n, const float* field, long long 
         const int x = b[0] + ((c >> 2) & 1), y = b[1] + ((c >> 1) & 1), z = b[2] + (c & 1);
         acc += s.w[8 * pnt + c] * f[((long long)x * ny + y) * zp + z];
     }
-    out[(long long)trow * ld + pnt] = acc;
+    out[(long long)trow * ld + pnt] = scale * acc;
 }
 
 __global__ void k_reduce3d(const float* __restrict__ buf, long long shot_stride, int nshots, int nx, int ny, int nz,
@@ -151,9 +151,9 @@ cudaError_t sparse3d_inject(const Sparse3D& sp, int n, const float* amp, int ld,
 }
 
 cudaError_t sparse3d_gather(const Sparse3D& sp, int n, const float* field, long long shot_stride, int ny, int zp,
-                            float* out, int ld, int trow, cudaStream_t s) {
+                            float* out, int ld, int trow, cudaStream_t s, float scale) {
     if (n == 0) return cudaSuccess;
-    gather3d<<<(n + 127) / 128, 128, 0, s>>>(sp, n, field, shot_stride, ny, zp, out, ld, trow);
+    gather3d<<<(n + 127) / 128, 128, 0, s>>>(sp, n, field, shot_stride, ny, zp, out, ld, trow, scale);
     return cudaGetLastError();
 }
 

@@ -132,6 +132,9 @@ struct Plan3D {
     // raw snapshots (SA_SAVE_RAW): held vp/rho terms per shot, rho accumulators, D-b per axis
     bool snaps_raw = false, rho_valid = false;
     float *hold_vp = nullptr, *hold_rho = nullptr, *gradrb = nullptr, *precrb = nullptr, *db[3] = {};
+    // wavelet gradient, time-major [nt][n_src]
+    float* wgrad = nullptr;
+    size_t cap_wgrad = 0;
     long long launches = 0;
     int chunk_rows = 0, nchunks = 1, ty0n = 1, tz0n = 1;
 };
@@ -195,7 +198,7 @@ void plan3d_destroy(Plan3D* p) {
     float* fb[] = {p->F[0], p->F[1], p->Lbuf, p->W, p->C1, p->C2, p->C3, p->bxh, p->byh, p->bzh, p->vp, p->alpha,
                    p->buoy, p->stage, p->s_w, p->s_coef, p->r_w, p->r_coef, p->src_amp, p->rec_amp, p->tstage,
                    p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps, p->A[0], p->A[1], p->hold_vp, p->hold_rho,
-                   p->gradrb, p->precrb, p->db[0], p->db[1], p->db[2]};
+                   p->gradrb, p->precrb, p->db[0], p->db[1], p->db[2], p->wgrad};
     for (float* b : fb)
         if (b) cudaFree(b);
     int* ib[] = {p->s_shot, p->s_base, p->r_shot, p->r_base};
@@ -493,7 +496,17 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
 // last to first its start state is restored (zero for k = 0), its forward steps are re-run
 // with p.dt2 saved into a K/f-slot segment buffer, and the adjoint steps run back through it
 // on their own two levels. The recomputed snapshots are bitwise the stored ones.
-static int adjoint_segments(Plan3D* p, Step3D& aa, const Sparse3D& rec, cudaStream_t s, long long& n) {
+// The wavelet gradient of adjoint level t: -interp(p_a[t]) at the sources into row t
+// (src.interpolate(expr=-p_a), iso_acoustic/devito.py:755-756).
+static int wavelet_level(Plan3D* p, const float* q, int t, bool wav, cudaStream_t s, long long& n) {
+    if (!wav || !p->n_src) return SA_OK;
+    const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
+    CK3(sparse3d_gather(src, p->n_src, q, p->field, p->ny, p->zp, p->wgrad, p->n_src, t, s, -1.f));
+    n++;
+    return SA_OK;
+}
+
+static int adjoint_segments(Plan3D* p, Step3D& aa, const Sparse3D& rec, bool wav, cudaStream_t s, long long& n) {
     const size_t level = (size_t)p->n_shots * p->field;
     const size_t lb = level * sizeof(float);
     const int f = p->d.undersampling, K = p->ck_K;
@@ -532,13 +545,15 @@ static int adjoint_segments(Plan3D* p, Step3D& aa, const Sparse3D& rec, cudaStre
                            false, s, n);
             if (rc != SA_OK) return rc;
             if ((rc = image_level(p, aa, even ? p->A[1] : p->A[0], s, n)) != SA_OK) return rc;
+            if ((rc = wavelet_level(p, even ? p->A[1] : p->A[0], t, wav, s, n)) != SA_OK) return rc;
         }
     }
     return SA_OK;
 }
 
 int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s, float* grad_rho,
-                   float* prec_rho) {
+                   float* prec_rho, float* grad_wavelets) {
+    const bool wav = grad_wavelets != nullptr;
     const bool ck = p->ckpt_valid;
     if (!p->snaps_valid && !ck)
         return fail3(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS or SA_SAVE_CHECKPOINTS");
@@ -577,6 +592,12 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
     if (!p->gradb && (rc = alloc3(&p->gradb, fl)) != SA_OK) return rc;
     if (!p->precb && (rc = alloc3(&p->precb, fl)) != SA_OK) return rc;
     if ((rc = load_tm(p, residuals, p->n_rec, p->d.nt, p->rec_amp, s)) != SA_OK) return rc;
+    const size_t wn = (size_t)p->d.nt * std::max(1, p->n_src);
+    if (wav && wn > p->cap_wgrad) {
+        if ((rc = alloc3(&p->wgrad, wn)) != SA_OK) return rc;
+        p->cap_wgrad = wn;
+    }
+    if (wav) CK3(cudaMemsetAsync(p->wgrad, 0, wn * sizeof(float), s));
     const size_t fb = (size_t)p->n_shots * p->field * sizeof(float);
     CK3(cudaMemsetAsync(p->F[0], 0, fb, s));
     CK3(cudaMemsetAsync(p->F[1], 0, fb, s));
@@ -593,7 +614,7 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
     const Sparse3D rec{p->r_shot, p->r_base, p->r_w, p->r_coef};
     const int T0 = p->d.nt - 1 - p->d.undersampling;
     long long n = p->n_rec ? 1 : 0;
-    if (ck && (rc = adjoint_segments(p, a, rec, s, n)) != SA_OK) return rc;
+    if (ck && (rc = adjoint_segments(p, a, rec, wav, s, n)) != SA_OK) return rc;
     for (int t = ck ? 0 : T0; t >= 1; t--) {
         a.t = t;
         const bool even = ((T0 - t) & 1) == 0;
@@ -603,6 +624,21 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
         if (rc != SA_OK) return rc;
         rc = raw ? image_raw_level(p, a, cur, rho, s, n) : image_level(p, a, cur, s, n);
         if (rc != SA_OK) return rc;
+        if ((rc = wavelet_level(p, cur, t, wav, s, n)) != SA_OK) return rc;
+    }
+    if (wav && p->n_src) {  // time-major -> [n_src, nt]
+        if (dev_ptr(grad_wavelets)) {
+            CK3(transpose(p->wgrad, p->d.nt, p->n_src, grad_wavelets, s));
+        } else {
+            if (wn > p->cap_tstage) {
+                if ((rc = alloc3(&p->tstage, wn)) != SA_OK) return rc;
+                p->cap_tstage = wn;
+            }
+            CK3(transpose(p->wgrad, p->d.nt, p->n_src, p->tstage, s));
+            CK3(cudaMemcpyAsync(grad_wavelets, p->tstage, wn * sizeof(float), cudaMemcpyDeviceToHost, s));
+            CK3(cudaStreamSynchronize(s));
+        }
+        n++;
     }
     const size_t N = (size_t)p->nx * p->ny * p->nz;
     for (int k = 0; k < (rho ? 4 : 2); k++) {

@@ -13,8 +13,9 @@ int plan3d_set_geometry(Plan3D* p, int n_shots, const int* so, const float* sx, 
 int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mode, cudaStream_t s);
 // grad_rho/prec_rho (both or neither) need a prior forward with SA_SAVE_RAW; after such a forward
 // the vp gradient follows the raw-wavefield path too.
+// grad_wavelets [n_src, nt] (host or device, optional): -interp(p_a[t]) at the sources.
 int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s,
-                   float* grad_rho = nullptr, float* prec_rho = nullptr);
+                   float* grad_rho = nullptr, float* prec_rho = nullptr, float* grad_wavelets = nullptr);
 long long plan3d_launches(const Plan3D* p);
 // Checkpoint interval K (a multiple of f) and the number of stored checkpoints for a plan whose
 // two state levels take `level_bytes` (SA_SAVE_CHECKPOINTS, both dimensions).

@@ -1225,9 +1225,9 @@ int sa_adjoint_grads(sa_plan* p, const float* residuals, float* grad_vp, float* 
                      float* prec_rho, float* grad_wavelets, void* stream) {
     if (!p) return fail(SA_E_INVALID, "null plan");
     if (p->p3) {
-        if (grad_wavelets) return fail(SA_E_UNSUPPORTED, "the wavelet gradient is implemented for 2D plans");
         if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
-        return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream, grad_rho, prec_rho);
+        return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream, grad_rho, prec_rho,
+                                  grad_wavelets);
     }
     if (!p->snaps_valid || !p->snaps_raw)
         return fail(SA_E_INVALID, "sa_adjoint_grads needs a prior sa_forward with SA_SAVE_RAW");
@@ -1247,10 +1247,10 @@ int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec
     if ((wav || exact) && p->d.interpolation == SA_INTERP_HICKS)
         return fail(SA_E_UNSUPPORTED, "wavelet and exact gradients use linear interpolation");
     if (p->p3) {
-        if (wav) return fail(SA_E_UNSUPPORTED, "the wavelet gradient is implemented for 2D plans");
         if (exact) return fail(SA_E_UNSUPPORTED, "SA_GRAD_EXACT is implemented for 2D plans");
         if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
-        return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream);
+        return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream, grad_rho, prec_rho,
+                                  grad_wavelets);
     }
     const bool ck = p->ckpt_valid;
     const bool raw = !ck && p->snaps_valid && p->snaps_raw;  // imaging from raw snapshots

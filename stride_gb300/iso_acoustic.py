@@ -123,7 +123,7 @@ class IsoAcousticGB300(ProblemTypeBase):
     ``platform``, ``devito_config`` and ``devito_args`` are accepted and ignored (the time
     loop always runs on the GPU). ``boundary_type='complex_frequency_shift_PML_2'`` runs in 2D
     with kernel OT2 (the combination the reference's own example runs). Gradients: vp, rho and
-    the wavelets (2D); alpha raises ValueError('Variable alpha not implemented') as in the
+    the wavelets; alpha raises ValueError('Variable alpha not implemented') as in the
     reference, which has no alpha gradient. Options the reference supports but this build does
     not (the CFS-PML with OT4 or in 3D, sinc interpolation, attenuation power 2) raise
     NotImplementedError; unknown values raise ValueError as in the reference.
