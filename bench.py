@@ -53,6 +53,8 @@ WORKLOADS = {
     'exact64': ('batched', 64, 'fwdadj'),   # exact gradient (autograd backward), checkpoints every 50 steps
     '3dgrad8': ('3d', 8, 'fwdadj'),         # 3D gradient of 8 shots, checkpoints under a 150 GB budget
     'fwi': ('single', 32, 'fwi'),           # plain vs learned-preconditioned FWI, wall time to a vp error
+    'rho64': ('batched', 64, 'fwdadj'),     # vp and rho gradients from the raw saved wavefield
+    'pml64': ('batched', 64, 'fwdadj'),     # vp gradient with the CFS-PML boundary (OT2)
 }
 # gradient method per workload: the reference imaging condition from snapshots (default), the
 # same from checkpoints with recompute, or the exact discrete adjoint from checkpoints
@@ -60,7 +62,11 @@ WORKLOADS = {
 GRADIENT = {
     'exact64': ('exact', dict(undersampling=1, checkpoint_interval=50)),
     '3dgrad8': ('checkpoints', dict(undersampling=4, checkpoint_budget=150e9)),
+    'rho64': ('raw', dict(undersampling=4)),
+    'pml64': ('snapshots', dict(undersampling=4, kernel='OT2', boundary='pml', f_centre=1.0e6)),
 }
+# time step of the workload's grid as a CFL number (OT2 needs one below its stability limit)
+CFL = {'pml64': 0.4}
 WORKLOAD_NAMES = {
     'fwdadj64': '2D fwd+adj vp gradient: 552^2 extended (512^2 at 0.25 mm + 20 sponge), vp/rho/alpha phantom, '
                 '64 shots x 256 receivers, 4000 steps, OT4, f=4',
@@ -76,6 +82,10 @@ WORKLOAD_NAMES = {
                'recompute',
     '3dgrad8': '3D fwd+adj vp gradient: 296^3 extended, vp/rho/alpha phantom, 8 shots per launch x 512 receivers, '
                '3000 steps, OT4, f=4, checkpoints under a 150 GB budget with recompute',
+    'rho64': '2D fwd+adj vp and rho gradients (raw saved wavefield, held imaging terms every step): 552^2 extended, '
+             'vp/rho/alpha phantom, 64 shots x 256 receivers, 4000 steps, OT4, f=4',
+    'pml64': '2D fwd+adj vp gradient with the CFS-PML boundary: 552^2 extended (20-cell PML), vp/rho/alpha phantom, '
+             '64 shots x 256 receivers, 4000 steps, OT2 at CFL 0.4, f=4',
     'fwi': 'FWI of seeded 256^2 ellipse phantoms at 0.5 mm (296^2 extended), 32 shots x 128 receivers, 2000 steps, '
            '500 kHz, f_max 0.5 MHz: plain (reference loop, GPU pipelines) vs U-Net-preconditioned (BF16 tcgen05, '
            'trained on plain-FWI paths of held-out seeds), wall time to the target relative vp error',
@@ -94,7 +104,7 @@ def workload_config(name='fwdadj64', nt=None, n_shots=None, rank=0):
     if gen == '3d':
         w = phantoms.workload3d(seed=0, nt=nt, n_shots=n_shots)
     else:
-        w = phantoms.workload(gen, seed=0, nt=nt)
+        w = phantoms.workload(gen, seed=0, nt=nt, cfl=CFL.get(name, 0.6))
     ntr = len(w['geometry'])
     stride = max(1, ntr // n_shots)
     first = rank % stride
@@ -379,9 +389,13 @@ def gb300_arm(args):
     win = scipy.signal.get_window(('tukey', 0.001), nt, False).astype(np.float32)
 
     method, plan_kw = GRADIENT.get(args.workload, ('snapshots', dict(undersampling=4)))
-    save = {'snapshots': True, 'checkpoints': 'checkpoints', 'exact': 'checkpoints'}[method] if grad_mode else False
+    save = {'snapshots': True, 'checkpoints': 'checkpoints', 'exact': 'checkpoints', 'raw': 'raw'}[method] \
+        if grad_mode else False
     exact = method == 'exact'
-    plan = _lib.Plan(dim, w['shape'], w['spacing'], w['extra'], w['absorbing'], w['dt'], nt, kernel='OT4',
+    rho_grad = method == 'raw'
+    plan_kw = dict(plan_kw)
+    kernel = plan_kw.pop('kernel', 'OT4')
+    plan = _lib.Plan(dim, w['shape'], w['spacing'], w['extra'], w['absorbing'], w['dt'], nt, kernel=kernel,
                      density=_density(w), attenuation=w['alpha'] is not None, max_shots=n_shots, **plan_kw)
     plan.set_geometry(so, sx, ro, rx)
     wav = torch.from_numpy(np.tile((w['wavelet'] * win)[None].astype(np.float32), (plan.n_src, 1))).to(dev)
@@ -397,6 +411,8 @@ def gb300_arm(args):
     traces = torch.zeros((plan.n_rec, nt), device=dev)
     grad = torch.zeros(w['shape'], device=dev)
     prec = torch.zeros(w['shape'], device=dev)
+    rho_out = dict(grad_rho=torch.zeros(w['shape'], device=dev), prec_rho=torch.zeros(w['shape'], device=dev)) \
+        if rho_grad else {}
 
     ev = lambda: torch.cuda.Event(enable_timing=True)
     fwd_ms, adj_ms = [], []
@@ -410,7 +426,7 @@ def gb300_arm(args):
         e1.record(stream)
         if grad_mode:
             res = (traces - observed) * win_d[None, :]  # L2 residual, adjoint-source window
-            plan.adjoint(res, grad, prec, stream=stream, exact=exact)
+            plan.adjoint(res, grad, prec, stream=stream, exact=exact, **rho_out)
             launches['n'] += plan.launches
         e2.record(stream)
         if world > 1 and grad_mode:
@@ -471,13 +487,15 @@ def gb300_arm(args):
         res_h = torch.zeros((plan.n_rec, nt)).pin_memory()
         g_h = torch.zeros(w['shape']).pin_memory()
         p_h = torch.zeros(w['shape']).pin_memory()
+        rho_h = dict(grad_rho=torch.zeros(w['shape']).pin_memory(), prec_rho=torch.zeros(w['shape']).pin_memory()) \
+            if rho_grad else {}
         tr_n, res_n, win_n = tr_h.numpy(), res_h.numpy(), win[None, :]
 
         def e2e_step():
             plan.forward(wav_h, tr_h, save=save, stream=stream)
             if grad_mode:
                 np.multiply(np.subtract(tr_n, obs_h, out=res_n), win_n, out=res_n)
-                plan.adjoint(res_h, g_h, p_h, stream=stream, exact=exact)
+                plan.adjoint(res_h, g_h, p_h, stream=stream, exact=exact, **rho_h)
 
         e2e_step()
         torch.cuda.synchronize()
@@ -493,12 +511,13 @@ def gb300_arm(args):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             es = float(t.item())
         h2d = wav_h.numel() * 4 + (res_h.numel() * 4 if grad_mode else 0)
-        d2h = tr_h.numel() * 4 + (2 * g_h.numel() * 4 if grad_mode else 0)
+        d2h = tr_h.numel() * 4 + ((2 + 2 * rho_grad) * g_h.numel() * 4 if grad_mode else 0)
         e2e = {'value': pts_step * world / es / 1e9, 'unit': 'GPts/s', 'h2d_bytes_per_step': int(h2d),
                'd2h_bytes_per_step': int(d2h)}
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    # the C port restates the sponge / p.dt2 path only: no CPU line for the raw-save and CFS-PML workloads
+    if rank == 0 and world == 1 and not args.no_cpu and args.workload not in ('rho64', 'pml64'):
         rate, cores, sample, _ = cpu_arm(w, target_s=args.cpu_seconds, mode=mode)
         cpu = {'value': rate, 'unit': 'GPts/s', 'cores': cores, 'kind': 'port', 'sample': sample}
 

@@ -88,13 +88,14 @@ def hemisphere_geometry(num, radius, centre):
     return np.asarray(pts[:num])
 
 
-def workload(name, seed=0, nt=None, n_shots=None, inner=None):
+def workload(name, seed=0, nt=None, n_shots=None, inner=None, cfl=0.6):
     """Synthetic 2D workload.
 
     name: 'single' (256^2 at 0.5 mm, vp only, 128 transducers, 500 kHz, shot 0, 2000 steps)
           or 'batched' (512^2 at 0.25 mm, vp/rho/alpha, 256 jittered transducers, 1 MHz,
           one shot per transducer, 4000 steps).
-    ``nt``, ``n_shots`` and ``inner`` override the size for reduced test cases.
+    ``nt``, ``n_shots`` and ``inner`` override the size for reduced test cases; ``cfl`` sets
+    dt = cfl h / 1650 m/s (0.6 for OT4, 0.4 within the OT2 limit).
     Returns a dict with extended-grid materials, geometry per shot and wavelets.
     """
     rng = np.random.default_rng(seed)
@@ -117,7 +118,7 @@ def workload(name, seed=0, nt=None, n_shots=None, inner=None):
     centre = ((n - 1) * h / 2, (n - 1) * h / 2)
     radius = min(55e-3, 0.45 * (n - 1) * h)  # 55 mm, or less on reduced test grids
     geo = circle_geometry(ntr, radius, centre, jitter=0.5 if name == 'batched' else 0.0, spacing=spacing, rng=rng)
-    dt = 0.6 * h / 1650.
+    dt = cfl * h / 1650.
     nt = steps if nt is None else nt
     n_tone = int((3 / f0) // dt + 1)
     wav = _wavelets.tone_burst(f0, 3, max(nt, n_tone), dt)[:nt]
