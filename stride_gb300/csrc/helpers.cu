@@ -106,14 +106,18 @@ __global__ void k_transpose(const float* __restrict__ in, int rows, int cols, fl
     }
 }
 
-__global__ void gather_final2d(const float* __restrict__ field, long long shot_stride, int pitch,
-                               const Gather* __restrict__ g, int n, float* out, int ld, int trow) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n) return;
+__device__ __forceinline__ void gather_point(const float* __restrict__ field, long long shot_stride, int pitch,
+                                             const Gather* __restrict__ g, int e, float* out, int ld, int trow) {
     const Gather G = g[e];  // pad = shot: pair pad / 2, lane pad % 2 of the interleaved field
     const float* f = field + (long long)(G.pad / 2) * shot_stride * 2 + (G.pad & 1);
     const long long i0 = 2 * ((long long)G.row * pitch + G.col), i1 = i0 + 2 * (long long)pitch;
     out[(long long)trow * ld + G.point] = G.w00 * f[i0] + G.w01 * f[i0 + 2] + G.w10 * f[i1] + G.w11 * f[i1 + 2];
+}
+
+__global__ void gather_final2d(const float* __restrict__ field, long long shot_stride, int pitch,
+                               const Gather* __restrict__ g, int n, float* out, int ld, int trow) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) gather_point(field, shot_stride, pitch, g, e, out, ld, trow);
 }
 
 // rec[trow][point] = sum over the 8 x 8 Hicks support of wx[i] wy[j] field(row + i, col + j).
@@ -408,12 +412,11 @@ cudaError_t pml2d(const float* cur, float* nxt, float* aux, const float* prof, c
 // field[idx[k]] += sum over the target's entries of coef[e] * amp[t][point[e]] (one thread per
 // target point; entries in a fixed order). With snap, the same sum times inv_dt2 also enters the
 // pair-interleaved snapshot level (shot-pair stride snap_shot_stride instead of shot_stride).
-__global__ void k_inject_targets2d(float* field, const long long* __restrict__ idx, const int* __restrict__ off,
-                                   const float* __restrict__ coef, const int* __restrict__ point, int n,
-                                   const float* __restrict__ amp, int ld, int t, float* snap, long long shot_stride,
-                                   long long snap_shot_stride, float inv_dt2) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+__device__ __forceinline__ void inject_target(float* field, const long long* __restrict__ idx,
+                                              const int* __restrict__ off, const float* __restrict__ coef,
+                                              const int* __restrict__ point, int k, const float* __restrict__ amp,
+                                              int ld, int t, float* snap, long long shot_stride,
+                                              long long snap_shot_stride, float inv_dt2) {
     float v = 0.f;
     const float* a = amp + (long long)t * ld;
     for (int e = off[k]; e < off[k + 1]; e++) v += coef[e] * a[point[e]];
@@ -423,6 +426,43 @@ __global__ void k_inject_targets2d(float* field, const long long* __restrict__ i
         const long long pair = i / (2 * shot_stride);
         snap[pair * 2 * snap_shot_stride + (i - pair * 2 * shot_stride)] += v * inv_dt2;
     }
+}
+
+__global__ void k_inject_targets2d(float* field, const long long* __restrict__ idx, const int* __restrict__ off,
+                                   const float* __restrict__ coef, const int* __restrict__ point, int n,
+                                   const float* __restrict__ amp, int ld, int t, float* snap, long long shot_stride,
+                                   long long snap_shot_stride, float inv_dt2) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) inject_target(field, idx, off, coef, point, k, amp, ld, t, snap, shot_stride, snap_shot_stride, inv_dt2);
+}
+
+// The sparse work between two forward steps in one launch: blocks [0, nbi) inject the sources of
+// step t into the new level (as k_inject_targets2d), the other blocks gather the receivers of the
+// previous step, rec[trow] = interp(gfield), from the current level. The two touch different
+// levels, so their order does not matter; one launch instead of two per step.
+__global__ void k_inject_gather2d(float* field, const long long* __restrict__ idx, const int* __restrict__ off,
+                                  const float* __restrict__ coef, const int* __restrict__ point, int n,
+                                  const float* __restrict__ amp, int ld, int t, float* snap, long long shot_stride,
+                                  long long snap_shot_stride, float inv_dt2, int nbi, const float* __restrict__ gfield,
+                                  int pitch, const Gather* __restrict__ g, int ng, float* out, int gld, int trow) {
+    if ((int)blockIdx.x < nbi) {
+        const int k = blockIdx.x * blockDim.x + threadIdx.x;
+        if (k < n) inject_target(field, idx, off, coef, point, k, amp, ld, t, snap, shot_stride, snap_shot_stride, inv_dt2);
+    } else {
+        const int e = (blockIdx.x - nbi) * blockDim.x + threadIdx.x;
+        if (e < ng) gather_point(gfield, shot_stride, pitch, g, e, out, gld, trow);
+    }
+}
+
+cudaError_t inject_gather2d(float* field, const long long* idx, const int* off, const float* coef, const int* point,
+                            int n, const float* amp, int ld, int t, float* snap, long long shot_stride,
+                            long long snap_shot_stride, float inv_dt2, const float* gfield, int pitch,
+                            const Gather* g, int ng, float* out, int gld, int trow, cudaStream_t s) {
+    const int nbi = (n + 255) / 256, nbg = (ng + 255) / 256;
+    if (nbi + nbg == 0) return cudaSuccess;
+    k_inject_gather2d<<<nbi + nbg, 256, 0, s>>>(field, idx, off, coef, point, n, amp, ld, t, snap, shot_stride,
+                                                snap_shot_stride, inv_dt2, nbi, gfield, pitch, g, ng, out, gld, trow);
+    return cudaGetLastError();
 }
 
 cudaError_t inject_targets2d(float* field, const long long* idx, const int* off, const float* coef, const int* point,

@@ -56,6 +56,12 @@ cudaError_t transpose(const float* in, int rows, int cols, float* out, cudaStrea
 cudaError_t inject_targets2d(float* field, const long long* idx, const int* off, const float* coef, const int* point,
                              int n, const float* amp, int ld, int t, float* snap, long long shot_stride,
                              long long snap_shot_stride, int unused, float inv_dt2, cudaStream_t s);
+// Source injection of step t into `field` and the receiver gather rec[trow] = interp(gfield) in one
+// launch (the two levels differ).
+cudaError_t inject_gather2d(float* field, const long long* idx, const int* off, const float* coef, const int* point,
+                            int n, const float* amp, int ld, int t, float* snap, long long shot_stride,
+                            long long snap_shot_stride, float inv_dt2, const float* gfield, int pitch,
+                            const Gather* g, int ng, float* out, int gld, int trow, cudaStream_t s);
 cudaError_t image2d(const float* q, const float* snap, float* gradb, float* precb, int ix0, int ix1, int iy0, int iy1,
                     int pitch, int npairs, long long shot_stride, long long snap_shot_stride, cudaStream_t s);
 // D-_x b and D-_y b at every node (edge-padded b), for the rho imaging term.

@@ -589,16 +589,24 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
         CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
         n++;
         const bool save_now = save && t % p->d.undersampling == 0;
-        CKR(pml_step(p, a.cur, a.prev, false,
-                     save_now ? p->snaps + 2 * (long long)(t / p->d.undersampling) * p->snap_stride : nullptr, s, n));
-        CKR(inject_sources(p, a.prev, t, p->snaps, p->snap_shot_stride, save_now, s, n));
-        if (p->n_rec) {  // rec[t] = interp(p[t+1]) (linear or over the Hicks support)
-            if (hicks)
-                CK(sa::hicks_gather2d(a.prev, p->shot_stride, p->pitch, p->hgat, p->n_rec, p->rec_amp, p->n_rec, t,
-                                      s));
-            else
-                CK(sa::final_gather2d(a.prev, p->shot_stride, p->pitch, p->gat_flat, p->n_rec, p->rec_amp, p->n_rec,
-                                      t, s));
+        float* snap_now = save_now ? p->snaps + 2 * (long long)(t / p->d.undersampling) * p->snap_stride : nullptr;
+        CKR(pml_step(p, a.cur, a.prev, false, snap_now, s, n));
+        if (hicks || !p->n_rec || t == 1) {
+            CKR(inject_sources(p, a.prev, t, p->snaps, p->snap_shot_stride, save_now, s, n));
+        } else {  // this step's sources into p[t+1] and the previous step's rec[t-1] = interp(p[t]), one launch
+            CK(sa::inject_gather2d(a.prev, p->stgt.idx, p->stgt.off, p->stgt.coef, p->stgt.point, p->stgt.n,
+                                   p->src_amp, p->n_src, t, snap_now, p->shot_stride, p->snap_shot_stride,
+                                   (float)(1.0 / (p->d.dt * p->d.dt)), a.cur, p->pitch, p->gat_flat, p->n_rec,
+                                   p->rec_amp, p->n_rec, t - 1, s));
+            n++;
+        }
+        if (p->n_rec && hicks) {  // rec[t] = interp(p[t+1]) over the Hicks support
+            CK(sa::hicks_gather2d(a.prev, p->shot_stride, p->pitch, p->hgat, p->n_rec, p->rec_amp, p->n_rec, t, s));
+            n++;
+        }
+        if (p->n_rec && !hicks && t == p->d.nt - 2) {  // the last step's receivers
+            CK(sa::final_gather2d(a.prev, p->shot_stride, p->pitch, p->gat_flat, p->n_rec, p->rec_amp, p->n_rec, t,
+                                  s));
             n++;
         }
         if (mode == SA_SAVE_CHECKPOINTS && t % p->ck_K == 0 && t / p->ck_K <= p->ck_n) {
