@@ -346,7 +346,7 @@ class IsoAcousticGB300(ProblemTypeBase):
     # ---------------------------------------------------------------------------- gradients
 
     def prepare_grad_vp(self, vp, **kwargs):
-        """The vp imaging condition runs inside the adjoint kernel (devito.py:985-1024)."""
+        """The vp imaging condition runs as its own kernel after each adjoint step (devito.py:985-1024)."""
         return ()
 
     def init_grad_vp(self, vp, **kwargs):
@@ -402,7 +402,7 @@ class IsoAcousticGB300(ProblemTypeBase):
         return grad
 
     def prepare_grad_wavelets(self, wavelets, **kwargs):
-        """The wavelet gradient is gathered inside the adjoint kernel (devito.py:755-756, 1189-1203)."""
+        """The wavelet gradient is gathered after each adjoint step (devito.py:755-756, 1189-1203)."""
         return ()
 
     def init_grad_wavelets(self, wavelets, **kwargs):
