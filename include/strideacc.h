@@ -52,7 +52,7 @@ extern "C" {
 
 #define SA_GRAD_PARITY 0      /* reference imaging condition: sum_{t%f==0} p_tt * p_a, interior only */
 #define SA_GRAD_EXACT 1       /* gradient of the discrete forward map (its exact transpose), every grid
-                                 point; needs SA_SAVE_CHECKPOINTS; 2D plans. No counterpart in the
+                                 point; needs SA_SAVE_CHECKPOINTS; 2D and 3D plans. No counterpart in the
                                  reference (whose gradient is SA_GRAD_PARITY) */
 
 /* Plan description (stride/physics/iso_acoustic/devito.py:119-183 defaults; shapes are the

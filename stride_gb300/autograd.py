@@ -1,4 +1,4 @@
-"""PyTorch autograd around the batched 2D forward map vp -> traces.
+"""PyTorch autograd around the batched forward map vp -> traces (2D and 3D).
 
 ``WaveOperator`` binds one plan (grid, time axis, physics options, geometry of all shots and
 their wavelets); ``op(vp)`` returns the traces of every shot as a CUDA tensor whose backward
@@ -41,7 +41,7 @@ class _ForwardMap(torch.autograd.Function):
 
 
 class WaveOperator:
-    """Forward map of a batch of 2D shots on one GPU, differentiable in vp.
+    """Forward map of a batch of 2D or 3D shots on one GPU, differentiable in vp.
 
     shape/spacing/extra/absorbing describe the extended grid as the plan does; src_offsets /
     rec_offsets are CSR offsets of each shot's points, src_xyz / rec_xyz their coordinates
@@ -52,8 +52,6 @@ class WaveOperator:
     def __init__(self, shape, spacing, extra, absorbing, dt, nt, src_offsets, src_xyz, rec_offsets, rec_xyz,
                  wavelets, rho=None, alpha=None, kernel='OT4', checkpoint_interval=50, checkpoint_budget=0.0,
                  device=None):
-        if len(shape) != 2:
-            raise ValueError('WaveOperator is 2D (the exact gradient mode is implemented for 2D plans)')
         self.device = torch.device(device) if device is not None else torch.device('cuda', torch.cuda.current_device())
         n_shots = len(src_offsets) - 1
         if rho is None:
@@ -62,7 +60,7 @@ class WaveOperator:
             r = np.asarray(rho, np.float32)
             density = _lib.SA_DENSITY_CONSTANT if np.isclose(r.min(), r.max()) else _lib.SA_DENSITY_VARIABLE
         with torch.cuda.device(self.device):
-            self.plan = _lib.Plan(2, shape, spacing, extra, absorbing, dt, nt, kernel=kernel, density=density,
+            self.plan = _lib.Plan(len(shape), shape, spacing, extra, absorbing, dt, nt, kernel=kernel, density=density,
                                   attenuation=alpha is not None, undersampling=1, max_shots=n_shots,
                                   checkpoint_interval=checkpoint_interval, checkpoint_budget=checkpoint_budget)
         self.shape = tuple(int(s) for s in shape)

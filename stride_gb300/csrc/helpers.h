@@ -50,6 +50,18 @@ cudaError_t image_raw3d(const float* q, const float* snap, long long snap_stride
                         const float* dbx, const float* dby, const float* dbz, const double* h, int nx, int ny, int nz,
                         int zp, float* gradb, float* precb, float* gradrb, float* precrb, const int* lo,
                         const int* hi, int nshots, long long field, cudaStream_t s);
+// Exact-gradient helpers of 3D plans (the 3D counterparts of exact2d.cu).
+cudaError_t exact_coef3d(const float* vp, const float* alpha, const float* W, int nx, int ny, int nz, int zp,
+                         const Sponge3& sp, float dt, float* EA, float* EB, float* EC, float* EG4, float* ES,
+                         cudaStream_t s);
+cudaError_t exact_grad3d(const float* z, const float* u0, const float* u1, const float* u2, const float* Lu,
+                         const float* Lz, const float* EA, const float* EB, const float* EC, const float* EG4, int nx,
+                         int ny, int nz, int zp, int nshots, long long field, float inv_dt2, float* gradb,
+                         float* precb, cudaStream_t s);
+cudaError_t exact_src3d(const float* z, const Sparse3D& sp, int n, const float* amp, int ld, int trow, float scale,
+                        const float* ES, int ny, int zp, long long field, float* gradb, cudaStream_t s);
+cudaError_t xcoef3d(const Sparse3D& sp, int n, const float* C1, const float* W, int ny, int zp, float* out,
+                    cudaStream_t s);
 cudaError_t reduce3d(const float* buf, long long shot_stride, int nshots, int nx, int ny, int nz, int zp, float* out,
                      cudaStream_t s);
 cudaError_t transpose(const float* in, int rows, int cols, float* out, cudaStream_t s);

@@ -302,6 +302,130 @@ cudaError_t image_raw3d(const float* q, const float* snap, long long snap_stride
     return cudaGetLastError();
 }
 
+// Exact-gradient helpers of 3D plans (SA_GRAD_EXACT), the 3D counterparts of exact2d.cu: the
+// per-point coefficients of the vp derivative of the update (with the damping and coefficients
+// exactly as k_coef3d forms them), the per-step accumulation and the source term.
+__global__ void k_exact_coef3d(const float* __restrict__ vp, const float* __restrict__ alpha,
+                               const float* __restrict__ W, int nx, int ny, int nz, int zp, Sponge3 sp, float dt,
+                               float* EA, float* EB, float* EC, float* EG4, float* ES) {
+    const long long n = (long long)nx * ny * nz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(q % nz), y = (int)((q / nz) % ny), x = (int)(q / ((long long)nz * ny));
+        const long long p = ((long long)x * ny + y) * zp + z;
+        const int e[3] = {min(x, nx - 1 - x), min(y, ny - 1 - y), min(z, nz - 1 - z)};
+        float s = 0.f;
+        for (int a = 0; a < 3; a++) {
+            bool ok = e[a] < sp.a[a];
+            for (int b2 = 0; b2 < 3; b2++)
+                if (b2 != a && e[b2] < e[a]) ok = false;
+            if (ok) s += sp.s[a][e[a]];
+        }
+        const float v = vp[p], v2 = v * v;
+        const float d = 7.f * (s * v) * dt;
+        float beta = v2 * d;
+        beta = beta + alpha[p] * v;
+        beta = dt * beta;
+        const float den = 1.f + beta;
+        const float C1 = (dt * dt) / den;
+        const float C2 = (2.f - dt * dt * v2 * d * d) / den;
+        const float C3 = (1.f - beta) / den;
+        const double Dt = dt, V = v, Dd = d, Q = 1.0 + (double)beta;
+        const double dbeta = Dt * (3.0 * V * Dd + (double)alpha[p]);
+        const double dC1 = -Dt * Dt * dbeta / (Q * Q);
+        const double dC2 = (-Dt * Dt * 4.0 * V * Dd * Dd * Q - (2.0 - Dt * Dt * V * V * Dd * Dd) * dbeta) / (Q * Q);
+        const double dC3 = -2.0 * dbeta / (Q * Q);
+        const double w = W[p], c1 = C1, c1w = c1 * w;
+        const double G1 = (dC1 + 2.0 * c1 / V) / (c1 * c1w);
+        EA[p] = (float)G1;
+        EB[p] = (float)(-G1 * (double)C2 + dC2 / c1w);
+        EC[p] = (float)(G1 * (double)C3 - dC3 / c1w);
+        EG4[p] = (float)(Dt * Dt / (6.0 * V * w));
+        ES[p] = (float)(1.0 / c1w - G1 * V);
+    }
+}
+
+// grad[shot] += z (a u0 + b u1 + c u2) [+ g4 Lu Lz]; prec[shot] += ((u0 - 2 u1 + u2) / dt^2)^2
+__global__ void k_exact_grad3d(const float* __restrict__ z, const float* __restrict__ u0,
+                               const float* __restrict__ u1, const float* __restrict__ u2,
+                               const float* __restrict__ Lu, const float* __restrict__ Lz,
+                               const float* __restrict__ EA, const float* __restrict__ EB,
+                               const float* __restrict__ EC, const float* __restrict__ EG4, int nx, int ny, int nz,
+                               int zp, int nshots, long long field, float inv_dt2, float* gradb, float* precb) {
+    const long long n = (long long)nx * ny * nz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n * nshots;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int shot = (int)(q / n);
+        const long long r = q - (long long)shot * n;
+        const int zz = (int)(r % nz), y = (int)((r / nz) % ny), x = (int)(r / ((long long)nz * ny));
+        const long long p = ((long long)x * ny + y) * zp + zz;
+        const long long i = (long long)shot * field + p;
+        const float a0 = u0[i], a1 = u1[i], a2 = u2[i];
+        float g = z[i] * (EA[p] * a0 + EB[p] * a1 + EC[p] * a2);
+        if (Lu) g += EG4[p] * (Lu[i] * Lz[i]);
+        const float dd = (a0 - 2.f * a1 + a2) * inv_dt2;
+        gradb[i] += g;
+        precb[i] += dd * dd;
+    }
+}
+
+// Source term at the 8 corners of each source point: z w src[trow] scale ES.
+__global__ void k_exact_src3d(const float* __restrict__ z, const Sparse3D s, int n, const float* __restrict__ amp,
+                              int ld, int trow, float scale, const float* __restrict__ ES, int ny, int zp,
+                              long long field, float* gradb) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 8 * n) return;
+    const int pnt = k >> 3, c = k & 7;
+    const int* b = s.base + 3 * pnt;
+    const int x = b[0] + ((c >> 2) & 1), y = b[1] + ((c >> 1) & 1), zz = b[2] + (c & 1);
+    const long long p = ((long long)x * ny + y) * zp + zz;
+    const long long i = (long long)s.shot[pnt] * field + p;
+    atomicAdd(gradb + i, z[i] * s.w[8 * pnt + c] * amp[(long long)trow * ld + pnt] * scale * ES[p]);
+}
+
+cudaError_t exact_coef3d(const float* vp, const float* alpha, const float* W, int nx, int ny, int nz, int zp,
+                         const Sponge3& sp, float dt, float* EA, float* EB, float* EC, float* EG4, float* ES,
+                         cudaStream_t s) {
+    k_exact_coef3d<<<2048, 256, 0, s>>>(vp, alpha, W, nx, ny, nz, zp, sp, dt, EA, EB, EC, EG4, ES);
+    return cudaGetLastError();
+}
+
+cudaError_t exact_grad3d(const float* z, const float* u0, const float* u1, const float* u2, const float* Lu,
+                         const float* Lz, const float* EA, const float* EB, const float* EC, const float* EG4, int nx,
+                         int ny, int nz, int zp, int nshots, long long field, float inv_dt2, float* gradb,
+                         float* precb, cudaStream_t s) {
+    const long long n = (long long)nx * ny * nz * nshots;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 16);
+    k_exact_grad3d<<<blocks, 256, 0, s>>>(z, u0, u1, u2, Lu, Lz, EA, EB, EC, EG4, nx, ny, nz, zp, nshots, field,
+                                          inv_dt2, gradb, precb);
+    return cudaGetLastError();
+}
+
+cudaError_t exact_src3d(const float* z, const Sparse3D& sp, int n, const float* amp, int ld, int trow, float scale,
+                        const float* ES, int ny, int zp, long long field, float* gradb, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_exact_src3d<<<(8 * n + 127) / 128, 128, 0, s>>>(z, sp, n, amp, ld, trow, scale, ES, ny, zp, field, gradb);
+    return cudaGetLastError();
+}
+
+// Receiver injection coefficients of the exact adjoint: w C1 W at each corner.
+__global__ void k_xcoef3d(const Sparse3D s, int n, const float* __restrict__ C1, const float* __restrict__ W, int ny,
+                          int zp, float* out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 8 * n) return;
+    const int pnt = k >> 3, c = k & 7;
+    const int* b = s.base + 3 * pnt;
+    const int x = b[0] + ((c >> 2) & 1), y = b[1] + ((c >> 1) & 1), z = b[2] + (c & 1);
+    const long long p = ((long long)x * ny + y) * zp + z;
+    out[k] = s.w[k] * (C1[p] * W[p]);
+}
+
+cudaError_t xcoef3d(const Sparse3D& sp, int n, const float* C1, const float* W, int ny, int zp, float* out,
+                    cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_xcoef3d<<<(8 * n + 127) / 128, 128, 0, s>>>(sp, n, C1, W, ny, zp, out);
+    return cudaGetLastError();
+}
+
 cudaError_t reduce3d(const float* buf, long long shot_stride, int nshots, int nx, int ny, int nz, int zp, float* out,
                      cudaStream_t s) {
     k_reduce3d<<<2048, 256, 0, s>>>(buf, shot_stride, nshots, nx, ny, nz, zp, out);

@@ -135,6 +135,13 @@ struct Plan3D {
     // wavelet gradient, time-major [nt][n_src]
     float* wgrad = nullptr;
     size_t cap_wgrad = 0;
+    // exact gradient (SA_GRAD_EXACT): vp-derivative coefficients of the update, every level of a
+    // segment, the W G(.) of a forward and an adjoint level, unit / zero update coefficients
+    // (guarded), receiver injection coefficients w C1 W
+    float *EA = nullptr, *EB = nullptr, *EC = nullptr, *EG4 = nullptr, *ES = nullptr, *levels = nullptr;
+    float *Lu = nullptr, *Lz = nullptr, *ones = nullptr, *zeros = nullptr, *r_xcoef = nullptr;
+    size_t cap_levels = 0;
+    bool exact_valid = false;
     long long launches = 0;
     int chunk_rows = 0, nchunks = 1, ty0n = 1, tz0n = 1;
 };
@@ -198,7 +205,8 @@ void plan3d_destroy(Plan3D* p) {
     float* fb[] = {p->F[0], p->F[1], p->Lbuf, p->W, p->C1, p->C2, p->C3, p->bxh, p->byh, p->bzh, p->vp, p->alpha,
                    p->buoy, p->stage, p->s_w, p->s_coef, p->r_w, p->r_coef, p->src_amp, p->rec_amp, p->tstage,
                    p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps, p->A[0], p->A[1], p->hold_vp, p->hold_rho,
-                   p->gradrb, p->precrb, p->db[0], p->db[1], p->db[2], p->wgrad};
+                   p->gradrb, p->precrb, p->db[0], p->db[1], p->db[2], p->wgrad, p->EA, p->EB, p->EC, p->EG4,
+                   p->ES, p->levels, p->Lu, p->Lz, p->ones, p->zeros, p->r_xcoef};
     for (float* b : fb)
         if (b) cudaFree(b);
     int* ib[] = {p->s_shot, p->s_base, p->r_shot, p->r_base};
@@ -237,6 +245,7 @@ int plan3d_set_medium(Plan3D* p, const float* vp, const float* rho, const float*
     p->snaps_valid = false;
     p->ckpt_valid = false;
     p->rho_valid = false;
+    p->exact_valid = false;
     if (p->geometry_set) return plan3d_set_geometry(p, p->n_shots, p->so.data(), p->sx.data(), p->ro.data(), p->rx.data());
     return SA_OK;
 }
@@ -284,6 +293,7 @@ static int build_points(Plan3D* p, int n_shots, const int* off, const float* xyz
 }
 
 int plan3d_set_geometry(Plan3D* p, int n_shots, const int* so, const float* sx, const int* ro, const float* rx) {
+    p->exact_valid = false;  // the receivers' C1 W coefficients follow the geometry
     std::vector<int> so_(so, so + n_shots + 1), ro_(ro, ro + n_shots + 1);
     std::vector<float> sx_(sx ? sx : nullptr, sx ? sx + 3 * (size_t)so[n_shots] : nullptr);
     std::vector<float> rx_(rx ? rx : nullptr, rx ? rx + 3 * (size_t)ro[n_shots] : nullptr);
@@ -644,6 +654,149 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
     for (int k = 0; k < (rho ? 4 : 2); k++) {
         float* user = k == 0 ? grad : (k == 1 ? prec : (k == 2 ? grad_rho : prec_rho));
         const float* buf = k == 0 ? p->gradb : (k == 1 ? p->precb : (k == 2 ? p->gradrb : p->precrb));
+        if (dev_ptr(user)) {
+            CK3(reduce3d(buf, p->field, p->n_shots, p->nx, p->ny, p->nz, p->zp, user, s));
+        } else {
+            if (N > p->cap_tstage) {
+                if ((rc = alloc3(&p->tstage, N)) != SA_OK) return rc;
+                p->cap_tstage = N;
+            }
+            CK3(reduce3d(buf, p->field, p->n_shots, p->nx, p->ny, p->nz, p->zp, p->tstage, s));
+            CK3(cudaMemcpyAsync(user, p->tstage, N * sizeof(float), cudaMemcpyDeviceToHost, s));
+            CK3(cudaStreamSynchronize(s));
+        }
+        n++;
+    }
+    p->launches = n;
+    return SA_OK;
+}
+
+}  // namespace sa
+
+namespace sa {
+
+// Exact adjoint of the discrete 3D forward map (SA_GRAD_EXACT), the 3D form of the 2D plan's
+// issue_adjoint_exact: with z = C1 W mu obeying the forward recursion, segment k of K steps is
+// recomputed from checkpoint k with every level kept (K + 2 levels), then the adjoint steps run
+// back through it: z[t-1] from z[t], z[t+1] (no receiver term inside the step), plus
+// w C1 W dL/drec[t-2] at the receivers; the vp gradient of step t-1 from three stored levels,
+// W G(u[t-1]) and W G(z[t]) (OT4, unit-coefficient OT2 passes) and the source term.
+int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s) {
+    if (!p->ckpt_valid)
+        return fail3(SA_E_INVALID, "SA_GRAD_EXACT needs a prior sa_forward with SA_SAVE_CHECKPOINTS");
+    const int nt = p->d.nt, K = p->ck_K;
+    const size_t fl = (size_t)std::max(1, p->d.max_shots) * p->field;  // floats of one level (capacity)
+    const size_t level = (size_t)p->n_shots * p->field;                  // floats of one level (in use)
+    const size_t lb = level * sizeof(float);
+    const long long G = GUARD;
+    const size_t guarded = (size_t)(p->nx + 2 * G) * p->plane;
+    int rc = SA_OK;
+    for (int k = 0; k < 2; k++)
+        if (!p->A[k] && (rc = alloc3(&p->A[k], fl)) != SA_OK) return rc;
+    if (!p->gradb && (rc = alloc3(&p->gradb, fl)) != SA_OK) return rc;
+    if (!p->precb && (rc = alloc3(&p->precb, fl)) != SA_OK) return rc;
+    const size_t need = (size_t)(K + 2) * level;
+    if (need > p->cap_levels) {
+        if ((rc = alloc3(&p->levels, need)) != SA_OK) return rc;
+        p->cap_levels = need;
+    }
+    if (!p->EA) {
+        float** per_point[] = {&p->EA, &p->EB, &p->EC, &p->EG4, &p->ES};
+        for (float** b : per_point)
+            if ((rc = alloc3(b, (size_t)p->field)) != SA_OK) return rc;
+        if ((rc = alloc3(&p->Lu, fl)) != SA_OK || (rc = alloc3(&p->Lz, fl)) != SA_OK) return rc;  // zeroed: finite
+        if ((rc = alloc3(&p->zeros, guarded)) != SA_OK || (rc = alloc3(&p->ones, guarded)) != SA_OK) return rc;
+        std::vector<float> one(guarded, 1.f);
+        CK3(cudaMemcpy(p->ones, one.data(), guarded * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    if (!p->exact_valid) {
+        CK3(exact_coef3d(p->vp, p->alpha, p->W + G * p->plane, p->nx, p->ny, p->nz, p->zp, p->sponge, (float)p->d.dt,
+                         p->EA, p->EB, p->EC, p->EG4, p->ES, 0));
+        if ((rc = alloc3(&p->r_xcoef, 8 * (size_t)std::max(1, p->n_rec))) != SA_OK) return rc;
+        const Sparse3D rec{p->r_shot, p->r_base, p->r_w, p->r_coef};
+        CK3(xcoef3d(rec, p->n_rec, p->C1 + G * p->plane, p->W + G * p->plane, p->ny, p->zp, p->r_xcoef, 0));
+        CK3(cudaDeviceSynchronize());
+        p->exact_valid = true;
+    }
+    if ((rc = load_tm(p, residuals, p->n_rec, nt, p->rec_amp, s)) != SA_OK) return rc;
+    CK3(cudaMemsetAsync(p->A[0], 0, lb, s));
+    CK3(cudaMemsetAsync(p->A[1], 0, lb, s));
+    CK3(cudaMemsetAsync(p->gradb, 0, lb, s));
+    CK3(cudaMemsetAsync(p->precb, 0, lb, s));
+    Step3D fa = args3(p);  // forward recompute, sources injected after each step
+    fa.save = 0;
+    Step3D aa = fa;        // adjoint steps, the receiver term injected separately
+    Step3D la = fa;        // W G(.) with unit / zero update coefficients
+    la.C1 = p->ones + G * p->plane;
+    la.C2 = la.C3 = p->zeros + G * p->plane;
+    const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
+    const Sparse3D none{p->r_shot, p->r_base, p->r_w, p->r_coef};
+    const Sparse3D recx{p->r_shot, p->r_base, p->r_w, p->r_xcoef};
+    const dim3 grid(p->ty0n * p->tz0n * p->n_shots, p->nchunks, 1);
+    const float inv_dt2 = (float)(1.0 / (p->d.dt * p->d.dt));
+    const double h = std::max(p->d.spacing[0], std::max(p->d.spacing[1], p->d.spacing[2]));
+    const float src_scale = (float)(2.0 * p->d.dt / h);
+    auto lvl = [&](int k, int m) { return p->levels + (size_t)(m - k * K) * level; };
+    long long n = p->n_rec ? 1 : 0;
+    for (int k = (nt - 2) / K; k >= 0; k--) {
+        const int t_lo = std::max(2, k * K + 2), t_hi = std::min((k + 1) * K + 1, nt);
+        if (t_lo > t_hi) continue;
+        if (k == 0) {
+            CK3(cudaMemsetAsync(p->F[0], 0, lb, s));
+            CK3(cudaMemsetAsync(p->F[1], 0, lb, s));
+        } else {
+            const float* slot = p->ckpt + (size_t)(k - 1) * 2 * level;
+            CK3(cudaMemcpyAsync(p->F[0], slot, lb, cudaMemcpyDeviceToDevice, s));
+            CK3(cudaMemcpyAsync(p->F[1], slot + level, lb, cudaMemcpyDeviceToDevice, s));
+        }
+        // u[kK] lives in F[kK & 1], u[kK+1] in the other
+        CK3(cudaMemcpyAsync(lvl(k, k * K), p->F[(k * K) & 1], lb, cudaMemcpyDeviceToDevice, s));
+        CK3(cudaMemcpyAsync(lvl(k, k * K + 1), p->F[(k * K + 1) & 1], lb, cudaMemcpyDeviceToDevice, s));
+        for (int m = k * K + 1; m <= std::min((k + 1) * K, nt - 2); m++) {  // forward step m -> u[m+1]
+            fa.t = m;
+            if ((rc = step3(p, fa, p->F[m & 1], p->F[(m + 1) & 1], src, p->n_src, p->src_amp, false, s, n)) != SA_OK)
+                return rc;
+            CK3(cudaMemcpyAsync(lvl(k, m + 1), p->F[(m + 1) & 1], lb, cudaMemcpyDeviceToDevice, s));
+        }
+        for (int t = t_hi; t >= t_lo; t--) {
+            float* zt = p->A[t & 1];
+            float* znext = p->A[(t + 1) & 1];
+            aa.t = t;
+            if ((rc = step3(p, aa, zt, znext, none, 0, p->rec_amp, false, s, n)) != SA_OK) return rc;
+            if (p->n_rec) {  // z[t-1] += w C1 W dL/drec[t-2]
+                CK3(sparse3d_inject(recx, p->n_rec, p->rec_amp, p->n_rec, t - 2, znext, p->field, p->ny, p->zp,
+                                    nullptr, 0, 0, 0.f, s));
+                n++;
+            }
+            if (t > nt - 1) continue;  // z[nt] = 0
+            const float *Lu = nullptr, *Lz = nullptr;
+            if (p->ot4) {
+                la.t = t - 1;
+                la.cur = la.in = lvl(k, t - 1);
+                la.prev = p->Lu;
+                CK3(launch_step3d(p->kind, true, false, grid, s, la));
+                la.t = t;
+                la.cur = la.in = zt;
+                la.prev = p->Lz;
+                CK3(launch_step3d(p->kind, true, false, grid, s, la));
+                Lu = p->Lu;
+                Lz = p->Lz;
+                n += 2;
+            }
+            CK3(exact_grad3d(zt, lvl(k, t), lvl(k, t - 1), lvl(k, t - 2), Lu, Lz, p->EA, p->EB, p->EC, p->EG4, p->nx,
+                             p->ny, p->nz, p->zp, p->n_shots, p->field, inv_dt2, p->gradb, p->precb, s));
+            n++;
+            if (p->n_src) {
+                CK3(exact_src3d(zt, src, p->n_src, p->src_amp, p->n_src, t - 1, src_scale, p->ES, p->ny, p->zp,
+                                p->field, p->gradb, s));
+                n++;
+            }
+        }
+    }
+    const size_t N = (size_t)p->nx * p->ny * p->nz;
+    for (int k = 0; k < 2; k++) {
+        float* user = k == 0 ? grad : prec;
+        const float* buf = k == 0 ? p->gradb : p->precb;
         if (dev_ptr(user)) {
             CK3(reduce3d(buf, p->field, p->n_shots, p->nx, p->ny, p->nz, p->zp, user, s));
         } else {

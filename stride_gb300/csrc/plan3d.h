@@ -16,6 +16,9 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
 // grad_wavelets [n_src, nt] (host or device, optional): -interp(p_a[t]) at the sources.
 int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s,
                    float* grad_rho = nullptr, float* prec_rho = nullptr, float* grad_wavelets = nullptr);
+// SA_GRAD_EXACT after a forward with SA_SAVE_CHECKPOINTS: residuals are dL/dtraces, grad receives
+// dL/dvp of the discrete forward map at every point, prec the sum over all steps of p.dt2^2.
+int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s);
 long long plan3d_launches(const Plan3D* p);
 // Checkpoint interval K (a multiple of f) and the number of stored checkpoints for a plan whose
 // two state levels take `level_bytes` (SA_SAVE_CHECKPOINTS, both dimensions).

@@ -1255,8 +1255,8 @@ int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec
     if ((wav || exact) && p->d.interpolation == SA_INTERP_HICKS)
         return fail(SA_E_UNSUPPORTED, "wavelet and exact gradients use linear interpolation");
     if (p->p3) {
-        if (exact) return fail(SA_E_UNSUPPORTED, "SA_GRAD_EXACT is implemented for 2D plans");
         if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
+        if (exact) return sa::plan3d_adjoint_exact(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream);
         return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream, grad_rho, prec_rho,
                                   grad_wavelets);
     }

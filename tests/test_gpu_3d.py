@@ -153,3 +153,47 @@ def test_wavelet_gradient_3d():
     gw2 = np.zeros_like(gw)
     ck.adjoint(resw, np.zeros(shape, np.float32), np.zeros(shape, np.float32), grad_wavelets=gw2)
     assert np.array_equal(gw, gw2)
+
+
+@pytest.mark.parametrize('kernel,density,alpha,interval', [('OT4', 'variable', True, 16), ('OT2', 'constant', False, 12)])
+def test_exact_gradient_3d(kernel, density, alpha, interval):
+    """SA_GRAD_EXACT on a 3D plan (checkpoints, segment recompute) against the FP64 exact-adjoint
+    oracle, and through torch.autograd (WaveOperator) the same gradient."""
+    import torch
+    from stride_gb300.autograd import WaveOperator
+    c = case3d(kernel=kernel, density=density, alpha=alpha, inner=16, nt=90, n_shots=2)
+    plan = make_plan3(c, checkpoint_interval=interval)
+    C.gpu_forward(c, plan=plan, save='checkpoints')
+    n_rec = sum(len(r) for r in c['recs'])
+    weights = np.random.default_rng(5).standard_normal((n_rec, c['nt']))
+    g = np.zeros(c['vp'].shape, np.float32)
+    plan.adjoint(np.ascontiguousarray(weights.astype(np.float32)), g, np.zeros_like(g), exact=True)
+    origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
+    ref = np.zeros(c['vp'].shape)
+    k = 0
+    for s in range(2):
+        nr = len(c['recs'][s])
+        wav = np.tile(c['wav'][None], (len(c['srcs'][s]), 1))
+        gs, _ = npo.adjoint_exact(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][s],
+                                  c['recs'][s], wav, weights[k:k + nr], origin, rho=c['rho'], alpha=c['alpha'],
+                                  kernel=kernel)
+        ref += gs
+        k += nr
+    assert np.abs(ref).max() > 0
+    assert C.cosine(g, ref) >= 0.9999
+    assert C.rel_l2(g, ref) <= 2e-3
+    # the same gradient through torch.autograd
+    so = np.cumsum([0] + [len(x) for x in c['srcs']])
+    ro = np.cumsum([0] + [len(x) for x in c['recs']])
+    eps = 1e-3 * np.asarray(c['spacing'])
+    sx = (np.concatenate(c['srcs']) + eps).astype(np.float32)
+    rx = (np.concatenate(c['recs']) + eps).astype(np.float32)
+    wav = np.concatenate([np.tile(c['wav'][None], (len(x), 1)) for x in c['srcs']]).astype(np.float64)
+    wav = (wav * C.window(c['nt'])[None, :]).astype(np.float32)
+    op = WaveOperator(c['vp'].shape, c['spacing'], c['extra'], c['absorbing'], c['dt'], c['nt'], so, sx, ro, rx, wav,
+                      rho=c['rho'], alpha=c['alpha'], kernel=kernel, checkpoint_interval=interval)
+    vp = torch.tensor(c['vp'], device='cuda', requires_grad=True)
+    w = torch.tensor(weights.astype(np.float32), device='cuda')
+    (op(vp) * w).sum().backward()
+    assert C.rel_l2(vp.grad.cpu().numpy(), g) <= 1e-5
+    op.close()
