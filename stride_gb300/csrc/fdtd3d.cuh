@@ -46,6 +46,8 @@ struct Step3D {
     long long snap_shot_stride, snap_stride;
 };
 
+__host__ __device__ constexpr int pow2_at_least(int x) { return x <= 1 ? 1 : 2 * pow2_at_least((x + 1) / 2); }
+
 template <int KIND, int TY, int TZ, int RB, int PF>
 struct Smem3D {
     static constexpr bool STAG = KIND != 0;
@@ -55,7 +57,10 @@ struct Smem3D {
     static constexpr int PLANE = PY * PZ;
     static constexpr int QU = R + RB * (PF + 1);            // planes kept: o .. i + RB*(PF+1) - 1
     static constexpr int FY = (TY + 9) * TZ;                // y fluxes of one row
-    static constexpr int FZ = TY * (TZ + 9);                // z fluxes of one row
+    // z fluxes of one row: TZ + 9 per y row, stored at a power-of-two stride so that a flat index
+    // splits into (y, z) with a shift and a mask
+    static constexpr int WZF = pow2_at_least(TZ + 9);
+    static constexpr int FZ = TY * WZF;
     static constexpr int oU = 0;
     static constexpr int oFY = QU * PLANE;
     static constexpr int oFZ = oFY + (STAG ? RB * FY : 0);
@@ -91,7 +96,7 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
     using L = Smem3D<KIND, TY, TZ, RB, PF>;
     constexpr int NT = TY * TZ;
     constexpr bool STAG = L::STAG, VARB = KIND == 1;
-    constexpr int R = L::R, QU = L::QU, PY = L::PY, PZ = L::PZ;
+    constexpr int R = L::R, QU = L::QU, PY = L::PY, PZ = L::PZ, WZF = L::WZF;
     constexpr int QB = STAG ? 9 : 10;
     constexpr int QL = QB + RB;
 
@@ -120,15 +125,17 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
     const float dt2 = a.dt * a.dt;
     const float k12 = (float)((double)a.dt * (double)a.dt / 12.0);
 
-    // plane ring: x row r in slot (r - i0) mod QU; element (yy, zz) at [(yy-y0+R)*PZ + zz - Z0]
-    auto slot = [&](int r) { return sU + (((r - i0) % QU + QU) % QU) * L::PLANE; };
+    // plane ring: x row r in slot (r - i0) mod QU, kept as a running slot index (sI: row i);
+    // element (yy, zz) at [(yy-y0+R)*PZ + zz - Z0]
+    auto wrap = [](int s) { return s < 0 ? s + QU : (s >= QU ? s - QU : s); };
+    auto slotp = [&](int s) { return sU + s * L::PLANE; };
     constexpr int NQ = PY * (PZ / 4);
-    auto prefetch = [&](int ii) {
+    auto prefetch = [&](int ii, int si) {  // rows ii, ii+1, ... into slots si, si+1, ...
 #pragma unroll
         for (int rr = 0; rr < RB; rr++) {
             const int r = ii + rr;
             if (r < i1) {
-                float* dst = slot(r);
+                float* dst = slotp(wrap(si + rr));
                 const bool row_ok = r >= 0 && r < a.nx;
                 for (int k = tid; k < NQ; k += NT) {
                     const int py = k / (PZ / 4), q = Z0 + 4 * (k % (PZ / 4));
@@ -152,12 +159,13 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
     const bool do_save = FINAL && a.save && (a.t % a.f == 0);
 
 #pragma unroll 1
-    for (int k = 0; k < PF; k++) prefetch(i0 + k * RB);
+    for (int k = 0; k < PF; k++) prefetch(i0 + k * RB, k * RB);
 
+    int sI = 0;  // ring slot of row i
 #pragma unroll 1
     for (int i = i0; i < i1; i += RB) {
         const int j = i - R;  // output row of this iteration's first input row
-        constexpr int KY = ((TY + 9) * TZ + NT - 1) / NT, KZ = (TY * (TZ + 9) + NT - 1) / NT;
+        constexpr int KY = ((TY + 9) * TZ + NT - 1) / NT, KZ = (TY * WZF + NT - 1) / NT;
         float Wj[RB], bxi[RB], byv[RB][VARB ? KY : 1], bzv[RB][VARB ? KZ : 1];
         float c1v[RB], c2v[RB], c3v[RB], uov[RB], pmv[RB];
 #pragma unroll
@@ -176,7 +184,7 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
 #pragma unroll
                 for (int q = 0; q < KZ; q++) {
                     const int k = tid + q * NT;
-                    const int ky = min(k / (TZ + 9), TY - 1), kz = k % (TZ + 9);
+                    const int ky = min(k / WZF, TY - 1), kz = k % WZF;
                     const int yy = min(y0 + ky, a.ny - 1), zz = min(max(z0 - 5 + kz + 6, 0), a.zpb - 1);
                     bzv[r][q] = __ldg(a.bzh + (long long)xx * a.ny * a.zpb + (long long)yy * a.zpb + zz);
                 }
@@ -195,12 +203,12 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
         (void)byv; (void)bzv; (void)c1v; (void)c2v; (void)c3v; (void)uov; (void)pmv;
         cp_async_wait<PF - 1>();
         __syncthreads();
-        prefetch(i + PF * RB);
+        prefetch(i + PF * RB, sI + PF * RB);
         // y/z fluxes of rows j..j+RB-1 (staggered): F_y at half-rows y0-5+k, F_z at z0-5+k
         if constexpr (STAG) {
 #pragma unroll
             for (int r = 0; r < RB; r++) {
-                const float* pl = slot(j + r);
+                const float* pl = slotp(wrap(sI - R + r));
 #pragma unroll
                 for (int q = 0; q < KY; q++) {
                     const int k = tid + q * NT;
@@ -216,20 +224,20 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
 #pragma unroll
                 for (int q = 0; q < KZ; q++) {
                     const int k = tid + q * NT;
-                    if (k < TY * (TZ + 9)) {
-                        const int ky = k / (TZ + 9), kz = k % (TZ + 9);
+                    const int ky = k / WZF, kz = k % WZF;
+                    if (ky < TY && kz < TZ + 9) {
                         const int hz = z0 - 5 + kz;  // half column hz + 1/2
                         const int base = (ky + R) * PZ + (hz - Z0);
                         float v = dstag_1(pl, base + 1, base, 1) * ihz;
                         if constexpr (VARB) v *= bzv[r][q];
-                        sFZ[r * (TY * (TZ + 9)) + k] = v;
+                        sFZ[r * L::FZ + k] = v;
                     }
                 }
             }
             __syncthreads();
         }
 #pragma unroll
-        for (int r = 0; r < RB; r++) uq[QB + r] = slot(i + r)[me];
+        for (int r = 0; r < RB; r++) uq[QB + r] = slotp(wrap(sI + r))[me];
         float res[RB];
 #pragma unroll
         for (int r = 0; r < RB; r++) {
@@ -240,14 +248,14 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
                 fq[QB + r] = v;
                 gx = dstag_1(fq, r + 5, r + 4, 1) * ihx;
                 const float* Fy = sFY + r * ((TY + 9) * TZ);
-                const float* Fz = sFZ + r * (TY * (TZ + 9));
+                const float* Fz = sFZ + r * L::FZ;
                 // D- along y at row ty: fluxes at half rows ty-5 .. ty+4 (index ky = half - y0 + 5)
                 const float gy = dstag_1(Fy, (ty + 5) * TZ + tz, (ty + 4) * TZ + tz, TZ) * ihy;
-                const float gz = dstag_1(Fz, ty * (TZ + 9) + tz + 5, ty * (TZ + 9) + tz + 4, 1) * ihz;
+                const float gz = dstag_1(Fz, ty * WZF + tz + 5, ty * WZF + tz + 4, 1) * ihz;
                 gyz = gy + gz;
             } else {
                 gx = dcent_1(uq, r + 5, 1) * ihx2;
-                const float* pl = slot(j + r);
+                const float* pl = slotp(wrap(sI - R + r));
                 gyz = dcent_1(pl, me, PZ) * ihy2 + dcent_1(pl, me, 1) * ihz2;
             }
             const float g = gx + gyz;
@@ -281,6 +289,7 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
                 a.prev[soff + idx] = pn;
             }
         }
+        sI = sI + RB >= QU ? sI + RB - QU : sI + RB;
     }
     cp_async_wait<0>();
 }
