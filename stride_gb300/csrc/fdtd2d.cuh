@@ -121,9 +121,12 @@ __device__ __forceinline__ void qshift(float2 (&q)[QL]) {
 #ifndef SA_MINBLOCKS
 #define SA_MINBLOCKS 3  // CTAs per SM the register allocation must allow (latency hiding)
 #endif
+// CTAs per SM the register budget is sized for: SA_MINBLOCKS for narrow CTAs, two for CTAs of
+// more than 170 threads (whose three would leave under 128 registers a thread)
+__host__ __device__ constexpr int step_min_blocks(int nt) { return nt * SA_MINBLOCKS <= 512 ? SA_MINBLOCKS : 2; }
 
 template <int KIND, bool OT4, int NT, int RB, int PF>
-__global__ void __launch_bounds__(NT, SA_MINBLOCKS) fdtd2d_step(const __grid_constant__ Step2D a) {
+__global__ void __launch_bounds__(NT, step_min_blocks(NT)) fdtd2d_step(const __grid_constant__ Step2D a) {
     using L = Smem2D<KIND, OT4, NT, RB, PF>;
     using CL = Cols2D<KIND, OT4, NT>;
     constexpr bool STAG = CL::STAG;           // staggered div(b grad) operator

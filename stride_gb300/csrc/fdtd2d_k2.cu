@@ -37,6 +37,7 @@ cudaError_t launch_step2d_k2(bool ot4, int nt_threads, dim3 grid, cudaStream_t s
         case 128: return ot4 ? go<true, 128>(grid, s, a) : go<false, 128>(grid, s, a);
         case 160: return ot4 ? go<true, 160>(grid, s, a) : go<false, 160>(grid, s, a);
         case 192: return ot4 ? go<true, 192>(grid, s, a) : go<false, 192>(grid, s, a);
+        case 256: return ot4 ? go<true, 256>(grid, s, a) : go<false, 256>(grid, s, a);
         default: return cudaErrorInvalidValue;
     }
 }

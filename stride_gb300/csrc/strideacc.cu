@@ -190,7 +190,7 @@ int halo1(const sa_plan* p) { return p->ot4 ? (p->kind == 0 ? 5 : 9) : 0; }
 int radius(const sa_plan* p) { return p->kind == 0 ? 5 : 9; }
 // output columns of a CTA of `nt` threads (one column per thread, halo H1 on both sides)
 int bymax(const sa_plan* p, int nt) { return nt - 2 * halo1(p); }
-const int kThreads[] = {96, 128, 160, 192};
+const int kThreads[] = {96, 128, 160, 192, 256};
 void set_strips(sa_plan* p, int nt) {
     p->NT = nt;
     const int bm = bymax(p, nt);
