@@ -1,10 +1,35 @@
 #include <algorithm>
+#include <cmath>
 // Small device helpers of the plan: medium preparation, sparse-trace transposes, the final
 // receiver gather and the reduction of per-shot gradients.
 #include "fdtd2d.cuh"
 #include "helpers.h"
 
 namespace sa {
+
+// Hicks coefficients of one axis (GridDevito._calculate_hicks, common/devito.py:843-885): Kaiser-
+// windowed sinc at offsets -3..3 from the base point (index 3 + offset; index 7 is zero), with the
+// reference's smoothing of the central coefficients for sources.
+void hicks_coefs(double frac, bool smooth, double c[8]) {
+    const double kb = 4.14, half = 3.0, ext = half / 0.99, den = std::cyl_bessel_i(0.0, kb);
+    for (int k = 0; k < 8; k++) c[k] = 0.0;
+    for (int gp = -3; gp <= 3; gp++) {
+        const double x = frac - gp;
+        double w = (x / ext) * (x / ext);
+        if (w > 1) w = 1;
+        const double sinc = x == 0.0 ? 1.0 : std::sin(M_PI * x) / (M_PI * x);
+        c[3 + gp] = sinc * std::cyl_bessel_i(0.0, kb * std::sqrt(1 - w)) / den;
+    }
+    if (smooth) {
+        const int m = 2;
+        const double a = c[m], b = c[m + 1], cc = c[m + 2];
+        c[m - 1] = c[m - 1] + a * 0.01;
+        c[m] = a * 0.98 + b * 0.03;
+        c[m + 1] = b * 0.94 + (a + cc) * 0.01;
+        c[m + 2] = cc * 0.98 + b * 0.03;
+        c[m + 3] = c[m + 3] + cc * 0.01;
+    }
+}
 
 // vp, rho, alpha (dB/cm) on the unpadded extended grid -> pitched W (guarded layout, pointer
 // at row 0), vp, alpha (Np/m) and buoyancy b = 1/rho scratch (iso_acoustic/devito.py:476-497).

@@ -25,11 +25,22 @@ cudaError_t exact_src2d(const float* z, const Gather* g, int n, const float* amp
                         const float* ES, int pitch, long long shot_stride, float* gradb, cudaStream_t s);
 
 // 3D plans
+// Hicks coefficients of one axis at the fractional offset frac (index 3 + grid offset, -3..4).
+void hicks_coefs(double frac, bool smooth, double c[8]);
+
 struct Sponge3 {
     int a[3];
     float s[3][MAX_ABS];
 };
 struct Sparse3D;
+struct Entries3D;
+struct HicksGather3D;
+// Hicks injection (flat support entries) and gather (8^3 support) of 3D plans.
+cudaError_t inject_entries3d(const Entries3D& e, int n, const float* amp, int ld, int t, float* field,
+                             long long shot_stride, float* snap, long long snap_shot_stride, long long snap_off,
+                             float inv_dt2, cudaStream_t s);
+cudaError_t hicks_gather3d(const HicksGather3D* g, int n, const float* field, long long shot_stride, int ny, int zp,
+                           float* out, int ld, int trow, float scale, cudaStream_t s);
 cudaError_t medium3d(const float* vp_in, const float* rho_in, const float* alpha_in, int nx, int ny, int nz, int zp,
                      int zpb, int density, double db_to_np, const Sponge3& sp, float dt, float* W, float* vp,
                      float* alpha, float* buoy, float* bxh, float* byh, float* bzh, float* C1, float* C2, float* C3,

@@ -426,6 +426,55 @@ cudaError_t xcoef3d(const Sparse3D& sp, int n, const float* C1, const float* W, 
     return cudaGetLastError();
 }
 
+// Hicks injection: field[shot][idx[e]] += coef[e] amp[t][point[e]] (and its snapshot / dt^2).
+__global__ void k_inject_entries3d(const Entries3D e, int n, const float* __restrict__ amp, int ld, int t, float* field,
+                                   long long shot_stride, float* snap, long long snap_shot_stride, long long snap_off,
+                                   float inv_dt2) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float v = e.coef[k] * amp[(long long)t * ld + e.point[k]];
+    const int sh = e.shot[k];
+    atomicAdd(field + (long long)sh * shot_stride + e.idx[k], v);
+    if (snap) atomicAdd(snap + (long long)sh * snap_shot_stride + snap_off + e.idx[k], v * inv_dt2);
+}
+
+// Hicks gather: out[trow][point] = scale * sum over the 8^3 support of wx wy wz field.
+__global__ void k_hicks_gather3d(const HicksGather3D* __restrict__ g, int n, const float* __restrict__ field,
+                                 long long shot_stride, int ny, int zp, float* out, int ld, int trow, float scale) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const HicksGather3D G = g[k];
+    const float* f = field + (long long)G.shot * shot_stride;
+    float v = 0.f;
+    for (int a = 0; a < 8; a++) {
+        float va = 0.f;
+        for (int b = 0; b < 8; b++) {
+            const float* row = f + ((long long)(G.x + a) * ny + (G.y + b)) * zp + G.z;
+            float vb = 0.f;
+            for (int c = 0; c < 8; c++) vb += G.wz[c] * row[c];
+            va += G.wy[b] * vb;
+        }
+        v += G.wx[a] * va;
+    }
+    out[(long long)trow * ld + G.point] = scale * v;
+}
+
+cudaError_t inject_entries3d(const Entries3D& e, int n, const float* amp, int ld, int t, float* field,
+                             long long shot_stride, float* snap, long long snap_shot_stride, long long snap_off,
+                             float inv_dt2, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_inject_entries3d<<<(n + 255) / 256, 256, 0, s>>>(e, n, amp, ld, t, field, shot_stride, snap, snap_shot_stride,
+                                                       snap_off, inv_dt2);
+    return cudaGetLastError();
+}
+
+cudaError_t hicks_gather3d(const HicksGather3D* g, int n, const float* field, long long shot_stride, int ny, int zp,
+                           float* out, int ld, int trow, float scale, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_hicks_gather3d<<<(n + 127) / 128, 128, 0, s>>>(g, n, field, shot_stride, ny, zp, out, ld, trow, scale);
+    return cudaGetLastError();
+}
+
 cudaError_t reduce3d(const float* buf, long long shot_stride, int nshots, int nx, int ny, int nz, int zp, float* out,
                      cudaStream_t s) {
     k_reduce3d<<<2048, 256, 0, s>>>(buf, shot_stride, nshots, nx, ny, nz, zp, out);

@@ -142,6 +142,13 @@ struct Plan3D {
     float *Lu = nullptr, *Lz = nullptr, *ones = nullptr, *zeros = nullptr, *r_xcoef = nullptr;
     size_t cap_levels = 0;
     bool exact_valid = false;
+    // Hicks interpolation: injection entries of the sources [0] and receivers [1], receiver gathers
+    bool hicks = false;
+    int *e_shot[2] = {}, *e_point[2] = {};
+    long long* e_idx[2] = {};
+    float* e_coef[2] = {};
+    int n_ent[2] = {0, 0};
+    HicksGather3D* hgat = nullptr;
     long long launches = 0;
     int chunk_rows = 0, nchunks = 1, ty0n = 1, tz0n = 1;
 };
@@ -159,6 +166,7 @@ int plan3d_create(const sa_desc& d, Plan3D** out) {
     p->zpb = (p->nz + 12 + 31) / 32 * 32;
     p->kind = d.density == SA_DENSITY_NONE ? 0 : (d.density == SA_DENSITY_VARIABLE ? 1 : 2);
     p->ot4 = d.kernel == SA_KERNEL_OT4;
+    p->hicks = d.interpolation == SA_INTERP_HICKS;
     p->plane = (long long)p->ny * p->zp;
     p->field = (long long)p->nx * p->plane;
     p->n_snap = (d.nt + d.undersampling) / d.undersampling + 1;
@@ -206,8 +214,11 @@ void plan3d_destroy(Plan3D* p) {
                    p->buoy, p->stage, p->s_w, p->s_coef, p->r_w, p->r_coef, p->src_amp, p->rec_amp, p->tstage,
                    p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps, p->A[0], p->A[1], p->hold_vp, p->hold_rho,
                    p->gradrb, p->precrb, p->db[0], p->db[1], p->db[2], p->wgrad, p->EA, p->EB, p->EC, p->EG4,
-                   p->ES, p->levels, p->Lu, p->Lz, p->ones, p->zeros, p->r_xcoef};
+                   p->ES, p->levels, p->Lu, p->Lz, p->ones, p->zeros, p->r_xcoef, p->e_coef[0], p->e_coef[1]};
     for (float* b : fb)
+        if (b) cudaFree(b);
+    void* vb[] = {p->e_shot[0], p->e_shot[1], p->e_point[0], p->e_point[1], p->e_idx[0], p->e_idx[1], p->hgat};
+    for (void* b : vb)
         if (b) cudaFree(b);
     int* ib[] = {p->s_shot, p->s_base, p->r_shot, p->r_base};
     for (int* b : ib)
@@ -292,6 +303,76 @@ static int build_points(Plan3D* p, int n_shots, const int* off, const float* xyz
     return SA_OK;
 }
 
+// Hicks support of every point (8 per axis from base - 3, within the grid): injection entries
+// (weight * scale * vp^k at the support point; sources smoothed as the reference's src) and, for
+// the receivers, the gathers of the 8^3 support.
+static int build_hicks(Plan3D* p, int n_shots, const int* off, const float* xyz, bool smooth, double scale,
+                       int vp_power, int which) {
+    const int n = off[n_shots];
+    std::vector<int> shot, point;
+    std::vector<long long> idx;
+    std::vector<float> coef;
+    std::vector<HicksGather3D> hg;
+    for (int s = 0; s < n_shots; s++)
+        for (int i = off[s]; i < off[s + 1]; i++) {
+            int base[3];
+            double c[3][8];
+            for (int a = 0; a < 3; a++) {
+                const double rel = ((double)xyz[3 * i + a] + p->d.extra[a] * p->d.spacing[a]) / p->d.spacing[a];
+                base[a] = (int)std::floor(rel);
+                if (!(base[a] - 3 >= 0 && base[a] + 4 <= p->d.shape[a] - 1))
+                    return fail3(SA_E_INVALID, "point's Hicks support lies outside the 3D grid");
+                hicks_coefs(rel - base[a], smooth, c[a]);
+            }
+            for (int u = 0; u < 8; u++)
+                for (int v = 0; v < 8; v++)
+                    for (int w = 0; w < 8; w++) {
+                        const double ww = c[0][u] * c[1][v] * c[2][w];
+                        if (ww == 0.0) continue;
+                        const int x = base[0] - 3 + u, y = base[1] - 3 + v, z = base[2] - 3 + w;
+                        const float vv = p->vp_host.empty() ? 0.f : p->vp_host[((size_t)x * p->ny + y) * p->nz + z];
+                        const double vpow = vp_power == 2 ? (double)(vv * vv) : (double)vv;
+                        shot.push_back(s);
+                        point.push_back(i);
+                        idx.push_back(((long long)x * p->ny + y) * p->zp + z);
+                        coef.push_back((float)(ww * scale * vpow));
+                    }
+            if (which == 1) {
+                HicksGather3D G;
+                G.x = base[0] - 3;
+                G.y = base[1] - 3;
+                G.z = base[2] - 3;
+                G.point = i;
+                G.shot = s;
+                for (int k = 0; k < 8; k++) {
+                    G.wx[k] = (float)c[0][k];
+                    G.wy[k] = (float)c[1][k];
+                    G.wz[k] = (float)c[2][k];
+                }
+                hg.push_back(G);
+            }
+        }
+    const size_t m = coef.size();
+    int rc = SA_OK;
+    if ((rc = alloc3(&p->e_shot[which], m)) != SA_OK || (rc = alloc3(&p->e_point[which], m)) != SA_OK ||
+        (rc = alloc3(&p->e_idx[which], m)) != SA_OK || (rc = alloc3(&p->e_coef[which], m)) != SA_OK)
+        return rc;
+    if (m) {
+        CK3(cudaMemcpy(p->e_shot[which], shot.data(), m * sizeof(int), cudaMemcpyHostToDevice));
+        CK3(cudaMemcpy(p->e_point[which], point.data(), m * sizeof(int), cudaMemcpyHostToDevice));
+        CK3(cudaMemcpy(p->e_idx[which], idx.data(), m * sizeof(long long), cudaMemcpyHostToDevice));
+        CK3(cudaMemcpy(p->e_coef[which], coef.data(), m * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    p->n_ent[which] = (int)m;
+    if (which == 1) {
+        if ((rc = alloc3(&p->hgat, std::max<size_t>(1, hg.size()))) != SA_OK) return rc;
+        if (!hg.empty())
+            CK3(cudaMemcpy(p->hgat, hg.data(), hg.size() * sizeof(HicksGather3D), cudaMemcpyHostToDevice));
+    }
+    (void)n;
+    return SA_OK;
+}
+
 int plan3d_set_geometry(Plan3D* p, int n_shots, const int* so, const float* sx, const int* ro, const float* rx) {
     p->exact_valid = false;  // the receivers' C1 W coefficients follow the geometry
     std::vector<int> so_(so, so + n_shots + 1), ro_(ro, ro + n_shots + 1);
@@ -303,6 +384,10 @@ int plan3d_set_geometry(Plan3D* p, int n_shots, const int* so, const float* sx, 
     if (rc == SA_OK)
         rc = build_points(p, n_shots, ro_.data(), rx_.data(), -p->d.dt * p->d.dt, 2, &p->r_shot, &p->r_base, &p->r_w,
                           &p->r_coef);
+    if (rc == SA_OK && p->hicks)
+        rc = build_hicks(p, n_shots, so_.data(), sx_.data(), true, 2.0 * p->d.dt / h, 1, 0);
+    if (rc == SA_OK && p->hicks)
+        rc = build_hicks(p, n_shots, ro_.data(), rx_.data(), false, -p->d.dt * p->d.dt, 2, 1);
     if (rc != SA_OK) return rc;
     p->so = so_;
     p->ro = ro_;
@@ -398,8 +483,10 @@ static int image_raw_level(Plan3D* p, const Step3D& a, const float* q, bool rho,
 }
 
 // One time level: [pass A] + pass B, then injection into the new level (and its snapshot).
-static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, const Sparse3D& inj, int n_inj,
-                 const float* amp, bool save_now, cudaStream_t s, long long& n) {
+// which: 0 injects the sources (amp = their samples), 1 the receivers, -1 nothing; linear or Hicks
+// as the plan's interpolation.
+static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, int which, const float* amp, bool save_now,
+                 cudaStream_t s, long long& n) {
     const dim3 grid(p->ty0n * p->tz0n * p->n_shots, p->nchunks, 1);
     a.cur = cur;
     a.prev = prev;
@@ -414,10 +501,22 @@ static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, const Spar
     }
     CK3(launch_step3d(p->kind, true, p->ot4, grid, s, a));
     n++;
+    if (which < 0) return SA_OK;
     const float inv_dt2 = (float)(1.0 / ((double)a.dt * (double)a.dt));
-    CK3(sparse3d_inject(inj, n_inj, amp, n_inj, a.t, prev, p->field, p->ny, p->zp, save_now ? a.snaps : nullptr,
-                        a.snap_shot_stride, (long long)(a.t / a.f) * a.snap_stride, inv_dt2, s));
-    if (n_inj) n++;
+    const int npts = which == 0 ? p->n_src : p->n_rec;
+    float* snap = save_now ? a.snaps : nullptr;
+    const long long soff = (long long)(a.t / a.f) * a.snap_stride;
+    if (p->hicks) {
+        const Entries3D e{p->e_shot[which], p->e_point[which], p->e_idx[which], p->e_coef[which]};
+        CK3(inject_entries3d(e, p->n_ent[which], amp, npts, a.t, prev, p->field, snap, a.snap_shot_stride, soff,
+                             inv_dt2, s));
+    } else {
+        const Sparse3D inj = which == 0 ? Sparse3D{p->s_shot, p->s_base, p->s_w, p->s_coef}
+                                        : Sparse3D{p->r_shot, p->r_base, p->r_w, p->r_coef};
+        CK3(sparse3d_inject(inj, npts, amp, npts, a.t, prev, p->field, p->ny, p->zp, snap, a.snap_shot_stride, soff,
+                            inv_dt2, s));
+    }
+    if (npts) n++;
     return SA_OK;
 }
 
@@ -459,17 +558,19 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
             CK3(cudaMemset2DAsync(p->snaps + (size_t)(last + 1) * p->snap_stride, pitch, 0,
                                   (size_t)(p->n_snap - last - 1) * slot, p->n_shots, s));
     }
-    const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
     const Sparse3D rec{p->r_shot, p->r_base, p->r_w, p->r_coef};
     long long n = p->n_src ? 1 : 0;
     for (int t = 1; t <= p->d.nt - 2; t++) {
         a.t = t;
         float* cur = (t & 1) ? p->F[1] : p->F[0];
         float* prev = (t & 1) ? p->F[0] : p->F[1];
-        rc = step3(p, a, cur, prev, src, p->n_src, p->src_amp, save && !raw && t % a.f == 0, s, n);
+        rc = step3(p, a, cur, prev, 0, p->src_amp, save && !raw && t % a.f == 0, s, n);
         if (rc != SA_OK) return rc;
         if (p->n_rec) {  // rec[t] = interp(p[t+1])
-            CK3(sparse3d_gather(rec, p->n_rec, prev, p->field, p->ny, p->zp, p->rec_amp, p->n_rec, t, s));
+            if (p->hicks)
+                CK3(hicks_gather3d(p->hgat, p->n_rec, prev, p->field, p->ny, p->zp, p->rec_amp, p->n_rec, t, 1.f, s));
+            else
+                CK3(sparse3d_gather(rec, p->n_rec, prev, p->field, p->ny, p->zp, p->rec_amp, p->n_rec, t, s));
             n++;
         }
         if (ckpt && t % p->ck_K == 0 && t / p->ck_K <= p->ck_n) {  // (p[t+1], p[t]) into slot t/K - 1
@@ -526,7 +627,6 @@ static int adjoint_segments(Plan3D* p, Step3D& aa, const Sparse3D& rec, bool wav
     Step3D fa = args3(p);
     fa.save = 1;
     fa.snap_shot_stride = aa.snap_shot_stride = (long long)(K / f) * p->snap_stride;
-    const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
     for (int k = T0 >= 1 ? (T0 - 1) / K : -1; k >= 0; k--) {
         const int t_lo = k * K + 1, t_hi = std::min((k + 1) * K, T0);
         if (k == 0) {
@@ -544,14 +644,14 @@ static int adjoint_segments(Plan3D* p, Step3D& aa, const Sparse3D& rec, bool wav
         fa.snaps = aa.snaps = base;
         for (int t = t_lo; t <= t_hi; t++) {
             fa.t = t;
-            int rc = step3(p, fa, (t & 1) ? p->F[1] : p->F[0], (t & 1) ? p->F[0] : p->F[1], src, p->n_src,
+            int rc = step3(p, fa, (t & 1) ? p->F[1] : p->F[0], (t & 1) ? p->F[0] : p->F[1], 0,
                            p->src_amp, t % f == 0, s, n);
             if (rc != SA_OK) return rc;
         }
         for (int t = t_hi; t >= t_lo; t--) {
             aa.t = t;
             const bool even = ((T0 - t) & 1) == 0;
-            int rc = step3(p, aa, even ? p->A[1] : p->A[0], even ? p->A[0] : p->A[1], rec, p->n_rec, p->rec_amp,
+            int rc = step3(p, aa, even ? p->A[1] : p->A[0], even ? p->A[0] : p->A[1], 1, p->rec_amp,
                            false, s, n);
             if (rc != SA_OK) return rc;
             if ((rc = image_level(p, aa, even ? p->A[1] : p->A[0], s, n)) != SA_OK) return rc;
@@ -630,7 +730,7 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
         const bool even = ((T0 - t) & 1) == 0;
         float* cur = even ? p->F[1] : p->F[0];
         float* prev = even ? p->F[0] : p->F[1];
-        rc = step3(p, a, cur, prev, rec, p->n_rec, p->rec_amp, false, s, n);
+        rc = step3(p, a, cur, prev, 1, p->rec_amp, false, s, n);
         if (rc != SA_OK) return rc;
         rc = raw ? image_raw_level(p, a, cur, rho, s, n) : image_level(p, a, cur, s, n);
         if (rc != SA_OK) return rc;
@@ -730,7 +830,6 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
     la.C1 = p->ones + G * p->plane;
     la.C2 = la.C3 = p->zeros + G * p->plane;
     const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
-    const Sparse3D none{p->r_shot, p->r_base, p->r_w, p->r_coef};
     const Sparse3D recx{p->r_shot, p->r_base, p->r_w, p->r_xcoef};
     const dim3 grid(p->ty0n * p->tz0n * p->n_shots, p->nchunks, 1);
     const float inv_dt2 = (float)(1.0 / (p->d.dt * p->d.dt));
@@ -754,7 +853,7 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
         CK3(cudaMemcpyAsync(lvl(k, k * K + 1), p->F[(k * K + 1) & 1], lb, cudaMemcpyDeviceToDevice, s));
         for (int m = k * K + 1; m <= std::min((k + 1) * K, nt - 2); m++) {  // forward step m -> u[m+1]
             fa.t = m;
-            if ((rc = step3(p, fa, p->F[m & 1], p->F[(m + 1) & 1], src, p->n_src, p->src_amp, false, s, n)) != SA_OK)
+            if ((rc = step3(p, fa, p->F[m & 1], p->F[(m + 1) & 1], 0, p->src_amp, false, s, n)) != SA_OK)
                 return rc;
             CK3(cudaMemcpyAsync(lvl(k, m + 1), p->F[(m + 1) & 1], lb, cudaMemcpyDeviceToDevice, s));
         }
@@ -762,7 +861,7 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
             float* zt = p->A[t & 1];
             float* znext = p->A[(t + 1) & 1];
             aa.t = t;
-            if ((rc = step3(p, aa, zt, znext, none, 0, p->rec_amp, false, s, n)) != SA_OK) return rc;
+            if ((rc = step3(p, aa, zt, znext, -1, p->rec_amp, false, s, n)) != SA_OK) return rc;
             if (p->n_rec) {  // z[t-1] += w C1 W dL/drec[t-2]
                 CK3(sparse3d_inject(recx, p->n_rec, p->rec_amp, p->n_rec, t - 2, znext, p->field, p->ny, p->zp,
                                     nullptr, 0, 0, 0.f, s));

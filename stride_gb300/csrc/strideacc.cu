@@ -226,30 +226,6 @@ void damping_table(int A, double h, double refl, float* out) {  // out: MAX_ABS 
     }
 }
 
-// Hicks coefficients of one axis (GridDevito._calculate_hicks, common/devito.py:843-885): Kaiser-
-// windowed sinc at offsets -3..3 from the base point (index 3 + offset; index 7 is zero), with the
-// reference's smoothing of the central coefficients for sources.
-void hicks_coefs(double frac, bool smooth, double c[8]) {
-    const double kb = 4.14, half = 3.0, ext = half / 0.99, den = std::cyl_bessel_i(0.0, kb);
-    for (int k = 0; k < 8; k++) c[k] = 0.0;
-    for (int gp = -3; gp <= 3; gp++) {
-        const double x = frac - gp;
-        double w = (x / ext) * (x / ext);
-        if (w > 1) w = 1;
-        const double sinc = x == 0.0 ? 1.0 : std::sin(M_PI * x) / (M_PI * x);
-        c[3 + gp] = sinc * std::cyl_bessel_i(0.0, kb * std::sqrt(1 - w)) / den;
-    }
-    if (smooth) {
-        const int m = 2;
-        const double a = c[m], b = c[m + 1], cc = c[m + 2];
-        c[m - 1] = c[m - 1] + a * 0.01;
-        c[m] = a * 0.98 + b * 0.03;
-        c[m + 1] = b * 0.94 + (a + cc) * 0.01;
-        c[m + 2] = cc * 0.98 + b * 0.03;
-        c[m + 3] = c[m + 3] + cc * 0.01;
-    }
-}
-
 void default_layout(sa_plan* p) {
     if (p->layout_fixed) return;
     int best_nt = 128, best_cost = 1 << 30;
@@ -319,8 +295,8 @@ int build_lists_impl(sa_plan* p) {
             for (int i = off[s]; i < off[s + 1]; i++) {
                 if (hicks) {
                     double cxs[8], cys[8];
-                    hicks_coefs(fx[i], smooth, cxs);
-                    hicks_coefs(fy[i], smooth, cys);
+                    sa::hicks_coefs(fx[i], smooth, cxs);
+                    sa::hicks_coefs(fy[i], smooth, cys);
                     for (int a = 0; a < 8; a++)
                         for (int b = 0; b < 8; b++) {
                             const double w = cxs[a] * cys[b];
@@ -439,8 +415,8 @@ int build_lists_impl(sa_plan* p) {
                 G.point = r;
                 G.shot = s;
                 double cx[8], cy[8];
-                hicks_coefs(p->rec_fx[r], false, cx);
-                hicks_coefs(p->rec_fy[r], false, cy);
+                sa::hicks_coefs(p->rec_fx[r], false, cx);
+                sa::hicks_coefs(p->rec_fy[r], false, cy);
                 for (int k = 0; k < 8; k++) {
                     G.wx[k] = (float)cx[k];
                     G.wy[k] = (float)cy[k];
@@ -957,8 +933,6 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
     if (d.density < 0 || d.density > 2) return fail(SA_E_INVALID, "density mode %d", d.density);
     if (d.interpolation != SA_INTERP_LINEAR && d.interpolation != SA_INTERP_HICKS)
         return fail(SA_E_INVALID, "interpolation %d", d.interpolation);
-    if (d.interpolation == SA_INTERP_HICKS && d.dim != 2)
-        return fail(SA_E_UNSUPPORTED, "Hicks interpolation is implemented for 2D plans");
     if (d.boundary != SA_BOUNDARY_SPONGE && d.boundary != SA_BOUNDARY_CFS_PML)
         return fail(SA_E_INVALID, "boundary %d", d.boundary);
     if (d.boundary == SA_BOUNDARY_CFS_PML && (d.dim != 2 || d.kernel != SA_KERNEL_OT2))
@@ -1234,6 +1208,8 @@ int sa_adjoint_grads(sa_plan* p, const float* residuals, float* grad_vp, float* 
     if (!p) return fail(SA_E_INVALID, "null plan");
     if (p->p3) {
         if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
+        if (grad_wavelets && p->d.interpolation == SA_INTERP_HICKS)
+            return fail(SA_E_UNSUPPORTED, "the wavelet gradient uses linear interpolation");
         return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream, grad_rho, prec_rho,
                                   grad_wavelets);
     }

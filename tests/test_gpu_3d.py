@@ -197,3 +197,36 @@ def test_exact_gradient_3d(kernel, density, alpha, interval):
     (op(vp) * w).sum().backward()
     assert C.rel_l2(vp.grad.cpu().numpy(), g) <= 1e-5
     op.close()
+
+
+@pytest.mark.parametrize('density', ['none', 'variable'])
+def test_hicks_3d(density):
+    """Hicks (Kaiser-windowed sinc) sources and receivers on a 3D plan: traces and the vp gradient
+    against the NumPy oracle with the same interpolation (common/devito.py:640-648,843-885)."""
+    c = case3d(kernel='OT4', density=density, alpha=True, n_shots=2, nt=120)
+    plan = make_plan3(c, interpolation='hicks')
+    got, plan = C.gpu_forward(c, plan=plan, save=True)
+    origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
+    kw = dict(rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation='hicks')
+    snaps = []
+    for s in range(2):
+        wav = np.tile(c['wav'][None], (len(c['srcs'][s]), 1))
+        ref, sn = npo.forward(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][s], c['recs'][s],
+                              wav, origin, save=True, **kw)
+        assert np.abs(ref).max() > 0
+        assert C.rel_l2(got[s], ref) <= 1e-4
+        snaps.append(sn)
+    lin, _ = C.gpu_forward(c, plan=make_plan3(c))
+    assert C.rel_l2(got[0], lin[0]) > 1e-3  # the interpolation is not the linear one
+    res = [g * np.float32(0.8) for g in got]
+    resw = np.ascontiguousarray((np.concatenate(res).astype(np.float64) * C.window(c['nt'])[None, :]).astype(np.float32))
+    grad = np.zeros(c['vp'].shape, np.float32)
+    prec = np.zeros(c['vp'].shape, np.float32)
+    plan.adjoint(resw, grad, prec)
+    g_ref = np.zeros(c['vp'].shape)
+    for s in range(2):
+        g, _ = npo.adjoint(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['recs'][s], res[s], origin,
+                           snaps[s], **kw)
+        g_ref += g
+    assert C.cosine(grad, g_ref) >= 0.999
+    assert C.rel_l2(grad, g_ref) <= 1e-3
