@@ -47,7 +47,7 @@ extern "C" {
 
 #define SA_BOUNDARY_SPONGE 0  /* SpongeBoundary2 (boundaries/devito.py:37-69), the reference's default */
 #define SA_BOUNDARY_CFS_PML 1 /* ComplexFrequencyShiftPML2 (boundaries/devito.py:72-191): auxiliary fields on
-                                 the absorbing slabs instead of the sponge; 2D with OT2 (the combination the
+                                 the absorbing slabs instead of the sponge; with OT2 (the combination the
                                  reference's own example runs), snapshot and raw saves */
 
 #define SA_GRAD_PARITY 0      /* reference imaging condition: sum_{t%f==0} p_tt * p_a, interior only */

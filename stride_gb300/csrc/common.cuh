@@ -28,6 +28,16 @@ __host__ __device__ constexpr float kWS(int k) {
                   : (float)(35.0 / 294912.0);
 }
 
+// 10th-order centred first-derivative weights c_1..c_5 (c_-k = -c_k): Devito's Derivative(f, (d, 1))
+// at space order 10, the CFS-PML's u_di (stride/physics/boundaries/devito.py:131).
+__host__ __device__ constexpr float kW1(int k) {
+    return k == 1 ? (float)(5.0 / 6.0)
+         : k == 2 ? (float)(-5.0 / 21.0)
+         : k == 3 ? (float)(5.0 / 84.0)
+         : k == 4 ? (float)(-5.0 / 504.0)
+                  : (float)(1.0 / 1260.0);
+}
+
 constexpr int GUARD = 40;  // zero rows above and below every pitched medium array (>= 3R + RB + 5)
 
 // A receiver with Hicks interpolation: 8 x 8 support from (row, col), weights wx[i] * wy[j].

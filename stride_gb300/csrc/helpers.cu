@@ -1,5 +1,6 @@
 #include <algorithm>
 #include <cmath>
+#include <vector>
 // Small device helpers of the plan: medium preparation, sparse-trace transposes, the final
 // receiver gather and the reduction of per-shot gradients.
 #include "fdtd2d.cuh"
@@ -29,6 +30,39 @@ void hicks_coefs(double frac, bool smooth, double c[8]) {
         c[m + 2] = cc * 0.98 + b * 0.03;
         c[m + 3] = c[m + 3] + cc * 0.01;
     }
+}
+
+// CFS-PML profiles per axis (ComplexFrequencyShiftPML2.apply, stride/physics/boundaries/devito.py:
+// 96-127, with Boundary.damping, boundaries/boundary.py:59-170), FP32 as the reference stores them:
+// sigma 'power' degree 3 with the coefficient 2 ln(1/R) / (absorbing h) (0.67 / h for layers of 15
+// cells or fewer), times max(vp); alpha a 'power' degree 2 mask, 0.01 pi f_centre in the interior
+// and -0.01 pi f_centre pos^2 in the layer; sigma' and alpha' 2nd-order centred differences over an
+// edge-padded halo. Layout: sigma, alpha, sigma', alpha' of axis 0 (shape[0] each), then axis 1, ...
+std::vector<float> pml_profile_tables(const sa_desc& d, float vmax) {
+    int amax = 0;
+    for (int a = 0; a < d.dim; a++) amax = std::max(amax, d.absorbing[a]);
+    const double refl = std::pow(10.0, -(std::log10((double)std::max(amax, 2)) - 1) / std::log10(2.0) - 3);
+    std::vector<float> out;
+    for (int a = 0; a < d.dim; a++) {
+        const int n = d.shape[a], A = d.absorbing[a];
+        const double h = d.spacing[a];
+        const double cs = A > 15 ? (3 + 1) / 2.0 * std::log(1.0 / refl) / (A * h) : 0.67 / h;
+        const double ca = 0.01 * M_PI * d.f_centre;
+        std::vector<float> sg(n, 0.f), al(n, (float)ca), dsg(n), dal(n);
+        for (int index = 0; index < A; index++) {
+            const double pos = std::fabs((A - index - 1) / (double)(A - 1));
+            sg[index] = sg[n - index - 1] = (float)(cs * pos * pos * pos);
+            al[index] = al[n - index - 1] = (float)(ca * -(pos * pos));
+        }
+        for (float& v : sg) v *= vmax;
+        for (int i = 0; i < n; i++) {
+            const int ip = std::min(i + 1, n - 1), im = std::max(i - 1, 0);
+            dsg[i] = (sg[ip] - sg[im]) / (float)(2 * h);
+            dal[i] = (al[ip] - al[im]) / (float)(2 * h);
+        }
+        for (auto* v : {&sg, &al, &dsg, &dal}) out.insert(out.end(), v->begin(), v->end());
+    }
+    return out;
 }
 
 // vp, rho, alpha (dB/cm) on the unpadded extended grid -> pitched W (guarded layout, pointer
@@ -314,15 +348,6 @@ cudaError_t image_raw2d(const float* q, const float* snap, long long snap_stride
     return cudaGetLastError();
 }
 
-// 10th-order centred first-derivative weights c_1..c_5 (c_-k = -c_k): Devito's Derivative(f, (d, 1))
-// at space order 10, the CFS-PML's u_di (stride/physics/boundaries/devito.py:131).
-__host__ __device__ constexpr float kW1(int k) {
-    return k == 1 ? (float)(5.0 / 6.0)
-         : k == 2 ? (float)(-5.0 / 21.0)
-         : k == 3 ? (float)(5.0 / 84.0)
-         : k == 4 ? (float)(-5.0 / 504.0)
-                  : (float)(1.0 / 1260.0);
-}
 
 // CFS-PML (ComplexFrequencyShiftPML2, boundaries/devito.py:72-191) after a step of the OT2
 // operator: on every point of the absorbing frame, for each axis d whose slab holds the point,

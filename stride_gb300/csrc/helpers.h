@@ -1,5 +1,8 @@
 // Host launchers of the plan's helper kernels (helpers.cu).
 #pragma once
+#include <vector>
+
+#include "../../include/strideacc.h"
 #include "common.cuh"
 
 namespace sa {
@@ -27,6 +30,8 @@ cudaError_t exact_src2d(const float* z, const Gather* g, int n, const float* amp
 // 3D plans
 // Hicks coefficients of one axis at the fractional offset frac (index 3 + grid offset, -3..4).
 void hicks_coefs(double frac, bool smooth, double c[8]);
+// CFS-PML profile tables (sigma, alpha, sigma', alpha' per axis) of a plan description.
+std::vector<float> pml_profile_tables(const sa_desc& d, float vmax);
 
 struct Sponge3 {
     int a[3];
@@ -35,6 +40,10 @@ struct Sponge3 {
 struct Sparse3D;
 struct Entries3D;
 struct HicksGather3D;
+// CFS-PML auxiliary update and boundary term after a 3D OT2 step.
+cudaError_t pml3d(const float* cur, float* nxt, float* aux, const float* prof, const float* C1, const float* vp,
+                  int nx, int ny, int nz, int zp, int nshots, long long field, const int* a, const double* h, float dt,
+                  int adjoint, float* snap, long long snap_shot_stride, float inv_dt2, cudaStream_t s);
 // Hicks injection (flat support entries) and gather (8^3 support) of 3D plans.
 cudaError_t inject_entries3d(const Entries3D& e, int n, const float* amp, int ld, int t, float* field,
                              long long shot_stride, float* snap, long long snap_shot_stride, long long snap_off,

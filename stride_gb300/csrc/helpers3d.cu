@@ -475,6 +475,82 @@ cudaError_t hicks_gather3d(const HicksGather3D* g, int n, const float* field, lo
     return cudaGetLastError();
 }
 
+// CFS-PML after a 3D OT2 step (the 3D form of k_pml2d): at every point of the absorbing frame, for
+// each axis whose slab holds it, the auxiliary fields u3, u2, u1 advance with the 10th-order
+// derivatives of p[t] along that axis (adjoint: -f_d), and the new level takes -C1 vp^2 sum u1
+// (its p.dt2 snapshot too on a save step). Interior points exit at once.
+// prof: sigma, alpha, sigma', alpha' per axis (n_a each, axes in order); aux: 9 fields (u3, u2, u1
+// of x, y, z), each nshots * field floats.
+__global__ void k_pml3d(const float* __restrict__ cur, float* nxt, float* aux, const float* __restrict__ prof,
+                        const float* __restrict__ C1, const float* __restrict__ vp, int nx, int ny, int nz, int zp,
+                        int nshots, long long field, int ax, int ay, int az, float ihx, float ihy, float ihz, float dt,
+                        int adjoint, float* snap, long long snap_shot_stride, float inv_dt2) {
+    const long long n = (long long)nx * ny * nz;
+    const long long fs = (long long)nshots * field;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n * nshots;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int shot = (int)(q / n);
+        const long long r = q - (long long)shot * n;
+        const int z = (int)(r % nz), y = (int)((r / nz) % ny), x = (int)(r / ((long long)nz * ny));
+        const int pos[3] = {x, y, z}, len[3] = {nx, ny, nz}, thick[3] = {ax, ay, az};
+        bool any = false;
+#pragma unroll
+        for (int d = 0; d < 3; d++) any |= pos[d] < thick[d] || pos[d] >= len[d] - thick[d];
+        if (!any) continue;
+        const long long idx = ((long long)x * ny + y) * zp + z;
+        const long long base = (long long)shot * field;
+        const float* f = cur + base;
+        const long long st[3] = {(long long)ny * zp, zp, 1};
+        const float ihs[3] = {ihx, ihy, ihz};
+        const int poff[3] = {0, 4 * nx, 4 * (nx + ny)};
+        float B = 0.f;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const int i = pos[d], nn = len[d], a = thick[d];
+            if (!(i < a || i >= nn - a)) continue;
+            const float f0 = f[idx];
+            float g = 0.f, l = kW2(0) * f0;
+#pragma unroll
+            for (int k = 1; k <= 5; k++) {
+                const float fp = i + k < nn ? f[idx + k * st[d]] : 0.f;
+                const float fm = i - k >= 0 ? f[idx - k * st[d]] : 0.f;
+                g += kW1(k) * (fp - fm);
+                l += kW2(k) * (fp + fm);
+            }
+            g *= adjoint ? -ihs[d] : ihs[d];
+            l *= ihs[d] * ihs[d];
+            const float* pr = prof + poff[d];
+            const float s = pr[i], al = pr[nn + i], ds = pr[2 * nn + i], da = pr[3 * nn + i];
+            float* u3 = aux + (3 * d) * fs + base + idx;
+            float* u2 = aux + (3 * d + 1) * fs + base + idx;
+            float* u1 = aux + (3 * d + 2) * fs + base + idx;
+            const float as = al + s;
+            const float v3 = *u3 - dt * (as * *u3 - s * s * (ds + da) * g);
+            const float v2 = *u2 - dt * (as * *u2 - s * (2.f * ds * g + da * g + s * l) + v3);
+            const float v1 = *u1 - dt * (as * *u1 - (ds * g + 2.f * s * l) + v2);
+            *u3 = v3;
+            *u2 = v2;
+            *u1 = v1;
+            B += v1;
+        }
+        const float v = vp[idx];
+        const float k = C1[idx] * (v * v) * B;
+        nxt[base + idx] -= k;
+        if (snap) snap[(long long)shot * snap_shot_stride + idx] -= k * inv_dt2;
+    }
+}
+
+cudaError_t pml3d(const float* cur, float* nxt, float* aux, const float* prof, const float* C1, const float* vp,
+                  int nx, int ny, int nz, int zp, int nshots, long long field, const int* a, const double* h, float dt,
+                  int adjoint, float* snap, long long snap_shot_stride, float inv_dt2, cudaStream_t s) {
+    const long long n = (long long)nx * ny * nz * nshots;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 16);
+    k_pml3d<<<blocks, 256, 0, s>>>(cur, nxt, aux, prof, C1, vp, nx, ny, nz, zp, nshots, field, a[0], a[1], a[2],
+                                   (float)(1.0 / h[0]), (float)(1.0 / h[1]), (float)(1.0 / h[2]), dt, adjoint, snap,
+                                   snap_shot_stride, inv_dt2);
+    return cudaGetLastError();
+}
+
 cudaError_t reduce3d(const float* buf, long long shot_stride, int nshots, int nx, int ny, int nz, int zp, float* out,
                      cudaStream_t s) {
     k_reduce3d<<<2048, 256, 0, s>>>(buf, shot_stride, nshots, nx, ny, nz, zp, out);

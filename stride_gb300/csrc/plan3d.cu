@@ -149,6 +149,9 @@ struct Plan3D {
     float* e_coef[2] = {};
     int n_ent[2] = {0, 0};
     HicksGather3D* hgat = nullptr;
+    // CFS-PML (SA_BOUNDARY_CFS_PML, OT2): profiles per axis and nine auxiliary fields per shot
+    bool pml = false;
+    float *pml_prof = nullptr, *pml_aux = nullptr;
     long long launches = 0;
     int chunk_rows = 0, nchunks = 1, ty0n = 1, tz0n = 1;
 };
@@ -167,6 +170,7 @@ int plan3d_create(const sa_desc& d, Plan3D** out) {
     p->kind = d.density == SA_DENSITY_NONE ? 0 : (d.density == SA_DENSITY_VARIABLE ? 1 : 2);
     p->ot4 = d.kernel == SA_KERNEL_OT4;
     p->hicks = d.interpolation == SA_INTERP_HICKS;
+    p->pml = d.boundary == SA_BOUNDARY_CFS_PML;
     p->plane = (long long)p->ny * p->zp;
     p->field = (long long)p->nx * p->plane;
     p->n_snap = (d.nt + d.undersampling) / d.undersampling + 1;
@@ -176,7 +180,7 @@ int plan3d_create(const sa_desc& d, Plan3D** out) {
         p->sponge.a[a] = d.absorbing[a];
         amax = std::max(amax, d.absorbing[a]);
     }
-    if (amax > 1) {
+    if (amax > 1 && !p->pml) {  // the CFS-PML replaces the sponge: no damping in the update
         const double refl = std::pow(10.0, -(std::log10((double)amax) - 1) / std::log10(2.0) - 3);
         for (int a = 0; a < 3; a++) ramp(d.absorbing[a], d.spacing[a], refl, p->sponge.s[a]);
     }
@@ -185,6 +189,8 @@ int plan3d_create(const sa_desc& d, Plan3D** out) {
     int rc = SA_OK;
     for (int k = 0; k < 2 && rc == SA_OK; k++) rc = alloc3(&p->F[k], shots * p->field);
     if (rc == SA_OK && p->ot4) rc = alloc3(&p->Lbuf, shots * p->field);
+    if (rc == SA_OK && p->pml) rc = alloc3(&p->pml_prof, 4 * (size_t)(p->nx + p->ny + p->nz));
+    if (rc == SA_OK && p->pml) rc = alloc3(&p->pml_aux, 9 * shots * p->field);
     const size_t guarded = (size_t)(p->nx + 2 * G) * p->plane;
     if (rc == SA_OK) rc = alloc3(&p->W, guarded);
     if (rc == SA_OK) rc = alloc3(&p->C1, guarded);
@@ -214,7 +220,8 @@ void plan3d_destroy(Plan3D* p) {
                    p->buoy, p->stage, p->s_w, p->s_coef, p->r_w, p->r_coef, p->src_amp, p->rec_amp, p->tstage,
                    p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps, p->A[0], p->A[1], p->hold_vp, p->hold_rho,
                    p->gradrb, p->precrb, p->db[0], p->db[1], p->db[2], p->wgrad, p->EA, p->EB, p->EC, p->EG4,
-                   p->ES, p->levels, p->Lu, p->Lz, p->ones, p->zeros, p->r_xcoef, p->e_coef[0], p->e_coef[1]};
+                   p->ES, p->levels, p->Lu, p->Lz, p->ones, p->zeros, p->r_xcoef, p->e_coef[0], p->e_coef[1],
+                   p->pml_prof, p->pml_aux};
     for (float* b : fb)
         if (b) cudaFree(b);
     void* vb[] = {p->e_shot[0], p->e_shot[1], p->e_point[0], p->e_point[1], p->e_idx[0], p->e_idx[1], p->hgat};
@@ -252,6 +259,12 @@ int plan3d_set_medium(Plan3D* p, const float* vp, const float* rho, const float*
     CK3(cudaDeviceSynchronize());
     p->vp_host.resize(N);
     CK3(cudaMemcpy(p->vp_host.data(), dv[0], N * sizeof(float), cudaMemcpyDeviceToHost));
+    if (p->pml) {
+        float vmax = 0.f;
+        for (float v : p->vp_host) vmax = std::max(vmax, v);
+        const std::vector<float> prof = pml_profile_tables(p->d, vmax);
+        CK3(cudaMemcpy(p->pml_prof, prof.data(), prof.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
     p->medium_set = true;
     p->snaps_valid = false;
     p->ckpt_valid = false;
@@ -501,8 +514,15 @@ static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, int which,
     }
     CK3(launch_step3d(p->kind, true, p->ot4, grid, s, a));
     n++;
-    if (which < 0) return SA_OK;
     const float inv_dt2 = (float)(1.0 / ((double)a.dt * (double)a.dt));
+    if (p->pml) {  // auxiliary fields and the boundary term of the new level (which 1: the adjoint)
+        CK3(pml3d(cur, prev, p->pml_aux, p->pml_prof, p->C1 + (long long)GUARD * p->plane, p->vp, p->nx, p->ny, p->nz,
+                  p->zp, p->n_shots, p->field, p->d.absorbing, p->d.spacing, a.dt, which == 1 ? 1 : 0,
+                  save_now ? a.snaps + (long long)(a.t / a.f) * a.snap_stride : nullptr, a.snap_shot_stride, inv_dt2,
+                  s));
+        n++;
+    }
+    if (which < 0) return SA_OK;
     const int npts = which == 0 ? p->n_src : p->n_rec;
     float* snap = save_now ? a.snaps : nullptr;
     const long long soff = (long long)(a.t / a.f) * a.snap_stride;
@@ -525,6 +545,7 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
     const bool raw = save_mode == SA_SAVE_RAW;
     const bool save = save_mode == SA_SAVE_SNAPSHOTS || raw;
     const bool ckpt = save_mode == SA_SAVE_CHECKPOINTS;
+    if (ckpt && p->pml) return fail3(SA_E_UNSUPPORTED, "checkpoints are implemented for the sponge boundary");
     p->ckpt_valid = false;  // the wavelets the checkpointed adjoint re-injects are replaced
     if (save && (size_t)p->n_shots * p->n_snap * p->snap_stride > p->cap_snaps) {
         p->cap_snaps = (size_t)p->n_shots * p->n_snap * p->snap_stride;
@@ -548,6 +569,7 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
     CK3(cudaMemsetAsync(p->F[0], 0, fb, s));
     CK3(cudaMemsetAsync(p->F[1], 0, fb, s));
     CK3(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * std::max(1, p->n_rec) * sizeof(float), s));
+    if (p->pml) CK3(cudaMemsetAsync(p->pml_aux, 0, 9 * (size_t)p->n_shots * p->field * sizeof(float), s));
     Step3D a = args3(p);
     a.save = raw ? 2 : (save ? 1 : 0);
     if (raw) {  // slots the loop does not write (n = 0, n f > nt-2) read as zero, the reference's fresh buffer
@@ -714,6 +736,7 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
     CK3(cudaMemsetAsync(p->gradb, 0, fb, s));
     CK3(cudaMemsetAsync(p->precb, 0, fb, s));
     if (raw) CK3(cudaMemsetAsync(p->hold_vp, 0, fb, s));  // held terms start at zero
+    if (p->pml) CK3(cudaMemsetAsync(p->pml_aux, 0, 9 * fb, s));
     if (rho) {
         CK3(cudaMemsetAsync(p->hold_rho, 0, fb, s));
         CK3(cudaMemsetAsync(p->gradrb, 0, fb, s));

@@ -886,38 +886,10 @@ long long sa_launch_count(const sa_plan* p) {
 }
 
 namespace {
-// CFS-PML profiles per axis (ComplexFrequencyShiftPML2.apply, stride/physics/boundaries/devito.py:
-// 96-127, with Boundary.damping, boundaries/boundary.py:59-170), FP32 as the reference stores them:
-// sigma 'power' degree 3 with the coefficient 2 ln(1/R) / (absorbing h) (0.67 / h for layers of 15
-// cells or fewer), times max(vp); alpha a 'power' degree 2 mask, 0.01 pi f_centre in the interior
-// and -0.01 pi f_centre pos^2 in the layer; sigma' and alpha' 2nd-order centred differences over an
-// edge-padded halo. Layout: sigma, alpha, sigma', alpha' of x (nx each), then of y (ny each).
 int pml_profiles(sa_plan* p) {
-    const sa_desc& d = p->d;
-    const int amax = std::max(d.absorbing[0], d.absorbing[1]);
-    const double refl = std::pow(10.0, -(std::log10((double)std::max(amax, 2)) - 1) / std::log10(2.0) - 3);
     float vmax = 0.f;
     for (float v : p->vp_host) vmax = std::max(vmax, v);
-    std::vector<float> out;
-    for (int a = 0; a < 2; a++) {
-        const int n = a == 0 ? p->nx : p->ny, A = d.absorbing[a];
-        const double h = d.spacing[a];
-        const double cs = A > 15 ? (3 + 1) / 2.0 * std::log(1.0 / refl) / (A * h) : 0.67 / h;
-        const double ca = 0.01 * M_PI * d.f_centre;
-        std::vector<float> sg(n, 0.f), al(n, (float)ca), dsg(n), dal(n);
-        for (int index = 0; index < A; index++) {
-            const double pos = std::fabs((A - index - 1) / (double)(A - 1));
-            sg[index] = sg[n - index - 1] = (float)(cs * pos * pos * pos);
-            al[index] = al[n - index - 1] = (float)(ca * -(pos * pos));
-        }
-        for (float& v : sg) v *= vmax;
-        for (int i = 0; i < n; i++) {
-            const int ip = std::min(i + 1, n - 1), im = std::max(i - 1, 0);
-            dsg[i] = (sg[ip] - sg[im]) / (float)(2 * h);
-            dal[i] = (al[ip] - al[im]) / (float)(2 * h);
-        }
-        for (auto* v : {&sg, &al, &dsg, &dal}) out.insert(out.end(), v->begin(), v->end());
-    }
+    const std::vector<float> out = sa::pml_profile_tables(p->d, vmax);
     CK(cudaMemcpy(p->pml_prof, out.data(), out.size() * sizeof(float), cudaMemcpyHostToDevice));
     return SA_OK;
 }
@@ -935,8 +907,8 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
         return fail(SA_E_INVALID, "interpolation %d", d.interpolation);
     if (d.boundary != SA_BOUNDARY_SPONGE && d.boundary != SA_BOUNDARY_CFS_PML)
         return fail(SA_E_INVALID, "boundary %d", d.boundary);
-    if (d.boundary == SA_BOUNDARY_CFS_PML && (d.dim != 2 || d.kernel != SA_KERNEL_OT2))
-        return fail(SA_E_UNSUPPORTED, "the CFS-PML is implemented for 2D plans with OT2");
+    if (d.boundary == SA_BOUNDARY_CFS_PML && d.kernel != SA_KERNEL_OT2)
+        return fail(SA_E_UNSUPPORTED, "the CFS-PML is implemented with OT2");
     if (d.boundary == SA_BOUNDARY_CFS_PML && !(d.f_centre > 0)) return fail(SA_E_INVALID, "f_centre");
     if (d.nt < 3 || d.undersampling < 1 || d.max_shots < 1) return fail(SA_E_INVALID, "nt/undersampling/max_shots");
     for (int a = 0; a < d.dim; a++) {

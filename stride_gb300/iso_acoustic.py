@@ -121,11 +121,11 @@ class IsoAcousticGB300(ProblemTypeBase):
     ``boundary_type='sponge_boundary_2'``, ``interpolation_type='linear'``,
     ``attenuation_power=0``, ``diff_source``, ``save_undersampling``, ``save_wavefield``.
     ``platform``, ``devito_config`` and ``devito_args`` are accepted and ignored (the time
-    loop always runs on the GPU). ``boundary_type='complex_frequency_shift_PML_2'`` runs in 2D
-    with kernel OT2 (the combination the reference's own example runs). Gradients: vp, rho and
+    loop always runs on the GPU). ``boundary_type='complex_frequency_shift_PML_2'`` runs with
+    kernel OT2 (the combination the reference's own example runs). Gradients: vp, rho and
     the wavelets; alpha raises ValueError('Variable alpha not implemented') as in the
     reference, which has no alpha gradient. Options the reference supports but this build does
-    not (the CFS-PML with OT4 or in 3D, sinc interpolation, attenuation power 2) raise
+    not (the CFS-PML with OT4, sinc interpolation, attenuation power 2) raise
     NotImplementedError; unknown values raise ValueError as in the reference.
     """
 
@@ -176,8 +176,8 @@ class IsoAcousticGB300(ProblemTypeBase):
         self.drp = False
         self._check_conditions(wavelets, vp, rho, alpha, kwargs.get('kernel', None),
                                kwargs.get('save_undersampling', None), **kwargs)
-        if self.boundary_type == 'complex_frequency_shift_PML_2' and (self.kernel != 'OT2' or self.space.dim != 2):
-            raise NotImplementedError('complex_frequency_shift_PML_2 is implemented for 2D problems with kernel OT2')
+        if self.boundary_type == 'complex_frequency_shift_PML_2' and self.kernel != 'OT2':
+            raise NotImplementedError('complex_frequency_shift_PML_2 is implemented with kernel OT2')
 
     def _check_conditions(self, wavelets, vp, rho=None, alpha=None, preferred_kernel=None,
                           preferred_undersampling=None, **kwargs):

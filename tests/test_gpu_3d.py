@@ -230,3 +230,35 @@ def test_hicks_3d(density):
         g_ref += g
     assert C.cosine(grad, g_ref) >= 0.999
     assert C.rel_l2(grad, g_ref) <= 1e-3
+
+
+def test_cfs_pml_3d():
+    """The CFS-PML (OT2) on a 3D plan: traces and the vp gradient against the NumPy restatement
+    (ComplexFrequencyShiftPML2, stride/physics/boundaries/devito.py:72-191)."""
+    c = case3d(kernel='OT2', density='variable', alpha=True, n_shots=2, nt=140)
+    plan = make_plan3(c, boundary='pml', f_centre=1.0e6)
+    got, plan = C.gpu_forward(c, plan=plan, save=True)
+    sponge, _ = C.gpu_forward(c, plan=make_plan3(c))
+    origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
+    kw = dict(rho=c['rho'], alpha=c['alpha'], kernel='OT2', boundary='pml', f_centre=1.0e6)
+    snaps = []
+    for s in range(2):
+        wav = np.tile(c['wav'][None], (len(c['srcs'][s]), 1))
+        ref, sn = npo.forward(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][s], c['recs'][s],
+                              wav, origin, save=True, **kw)
+        assert np.abs(ref).max() > 0
+        assert C.rel_l2(got[s], ref) <= 1e-4
+        assert C.rel_l2(got[s], sponge[s]) > 1e-3
+        snaps.append(sn)
+    res = [g * np.float32(0.8) for g in got]
+    resw = np.ascontiguousarray((np.concatenate(res).astype(np.float64) * C.window(c['nt'])[None, :]).astype(np.float32))
+    grad = np.zeros(c['vp'].shape, np.float32)
+    prec = np.zeros(c['vp'].shape, np.float32)
+    plan.adjoint(resw, grad, prec)
+    g_ref = np.zeros(c['vp'].shape)
+    for s in range(2):
+        g, _ = npo.adjoint(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['recs'][s], res[s], origin,
+                           snaps[s], **kw)
+        g_ref += g
+    assert C.cosine(grad, g_ref) >= 0.999
+    assert C.rel_l2(grad, g_ref) <= 1e-3
