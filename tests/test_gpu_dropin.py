@@ -147,3 +147,40 @@ def test_pde_cfs_pml():
                        boundary='pml', f_centre=pde._bandwidth[1])
     assert np.abs(ref).max() > 0
     assert C.rel_l2(traces.data, ref) <= 1e-4
+
+
+def test_pde_3d_forward_and_gradient():
+    """The drop-in on a 3D problem: pde(...) traces and the adjoint's vp gradient against the C
+    oracle (3D extended grid, variable density and attenuation)."""
+    rng = np.random.default_rng(9)
+    h = 0.5e-3
+    n = 24
+    space = problem.Space((n, n + 2, n + 4), h, extra=(8, 8, 8), absorbing=(8, 8, 8))
+    time = problem.Time(0., 0.6 * h / 1650, 140)
+    grid = problem.Grid(space, time)
+    vpi, rhoi, ali = phantoms.ellipse_phantom(space.shape, space.spacing, 3, rng, rho_range=(950., 1100.),
+                                              alpha_range=(0., 1.), disk_radius=3e-3, axes=(1.5e-3, 4e-3))
+    vp = problem.ScalarField('vp', grid, data=phantoms.extend(vpi, space.extra), needs_grad=True)
+    rho = problem.ScalarField('rho', grid, data=phantoms.extend(rhoi, space.extra))
+    al = problem.ScalarField('alpha', grid, data=phantoms.extend(ali, space.extra))
+    c = np.array([(s - 1) * h / 2 for s in space.shape])
+    geo = c + 4e-3 * np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [-1, 0, 0], [0, -1, 0.3], [0.5, 0.5, -0.6]])
+    w = wavelets.tone_burst(1e6, 3, time.num, time.step)
+    shot = problem.Shot(0, geo[:1], geo, w[None], grid=grid)
+    sub = problem.SubProblem(shot, space, time)
+    pde = iso_acoustic.IsoAcousticGB300(space=space, time=time)
+    traces = pde(shot.wavelets, vp, rho=rho, alpha=al, problem=sub)
+    kw = dict(rho=rho.extended_data, alpha=al.extended_data)
+    ref, snaps = c_oracle.forward(vp.extended_data, space.spacing, time.step, time.num, space.absorbing, geo[:1], geo,
+                                  w[None], space.pml_origin, kernel=pde.kernel, save=True,
+                                  undersampling=pde.undersampling_factor, **kw)
+    assert np.abs(ref).max() > 0
+    assert C.rel_l2(traces.data, ref) <= 1e-4
+    residual = shot.observed.alike(name='residual', data=traces.data * np.float32(0.7))
+    grads = pde.adjoint(residual, shot.wavelets, vp, rho, al, problem=sub)
+    g_ref, _ = c_oracle.adjoint(vp.extended_data, space.spacing, time.step, time.num, space.absorbing, geo,
+                                traces.data * np.float32(0.7), space.pml_origin, snaps, kernel=pde.kernel,
+                                undersampling=pde.undersampling_factor, **kw)
+    g_ref, _ = O.grad_vp_chain(g_ref[space.inner], g_ref[space.inner], vp.data, slowness=True)
+    assert grads[1].extended_data.shape == space.shape
+    assert C.cosine(grads[1].extended_data, g_ref) >= 0.999
