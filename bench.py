@@ -482,19 +482,20 @@ def gb300_arm(args):
     e2e = None
     if not args.no_e2e:
         wav_h = wav.cpu().pin_memory()
-        obs_h = observed.cpu().numpy()
+        obs_h = observed.cpu()
         tr_h = torch.zeros((plan.n_rec, nt)).pin_memory()
         res_h = torch.zeros((plan.n_rec, nt)).pin_memory()
         g_h = torch.zeros(w['shape']).pin_memory()
         p_h = torch.zeros(w['shape']).pin_memory()
         rho_h = dict(grad_rho=torch.zeros(w['shape']).pin_memory(), prec_rho=torch.zeros(w['shape']).pin_memory()) \
             if rho_grad else {}
-        tr_n, res_n, win_n = tr_h.numpy(), res_h.numpy(), win[None, :]
+        win_h = torch.from_numpy(win)[None, :]
 
         def e2e_step():
             plan.forward(wav_h, tr_h, save=save, stream=stream)
             if grad_mode:
-                np.multiply(np.subtract(tr_n, obs_h, out=res_n), win_n, out=res_n)
+                # the residual on the host, with PyTorch's multithreaded CPU kernels
+                torch.mul(torch.sub(tr_h, obs_h, out=res_h), win_h, out=res_h)
                 plan.adjoint(res_h, g_h, p_h, stream=stream, exact=exact, **rho_h)
 
         e2e_step()
