@@ -121,9 +121,9 @@ __device__ __forceinline__ void qshift(float2 (&q)[QL]) {
 #ifndef SA_MINBLOCKS
 #define SA_MINBLOCKS 3  // CTAs per SM the register allocation must allow (latency hiding)
 #endif
-// CTAs per SM the register budget is sized for: SA_MINBLOCKS for narrow CTAs, two for CTAs of
-// more than 170 threads (whose three would leave under 128 registers a thread)
-__host__ __device__ constexpr int step_min_blocks(int nt) { return nt * SA_MINBLOCKS <= 512 ? SA_MINBLOCKS : 2; }
+// CTAs per SM the register budget is sized for: SA_MINBLOCKS up to 192 threads (the OT2 kernels
+// fit three CTAs of 192), two for the 256-thread CTA (whose three would leave 85 registers)
+__host__ __device__ constexpr int step_min_blocks(int nt) { return nt <= 192 ? SA_MINBLOCKS : 2; }
 
 template <int KIND, bool OT4, int NT, int RB, int PF>
 __global__ void __launch_bounds__(NT, step_min_blocks(NT)) fdtd2d_step(const __grid_constant__ Step2D a) {
