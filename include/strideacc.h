@@ -127,7 +127,8 @@ int sa_adjoint(sa_plan* plan, const float* residuals, float* grad_vp, float* pre
 /* sa_adjoint plus the gradient with respect to the wavelets: grad_wavelets [n_src_total, nt]
  * (host or device) receives -interp(p_a[t]) at the sources for t = 1 .. nt-1-f and zero
  * elsewhere, the reference's src.interpolate(expr=-p_a) (iso_acoustic/devito.py:755-756) read back
- * by get_grad_wavelets (:1226-1262). grad_mode SA_GRAD_PARITY; linear interpolation. */
+ * by get_grad_wavelets (:1226-1262). grad_mode SA_GRAD_PARITY; linear or Hicks interpolation (the
+ * sources' smoothed support). */
 int sa_adjoint_wavelets(sa_plan* plan, const float* residuals, float* grad_vp, float* prec_vp, float* grad_wavelets,
                         int grad_mode, void* stream);
 

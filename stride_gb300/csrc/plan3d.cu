@@ -149,6 +149,7 @@ struct Plan3D {
     float* e_coef[2] = {};
     int n_ent[2] = {0, 0};
     HicksGather3D* hgat = nullptr;
+    HicksGather3D* hgat_src = nullptr;  // sources (smoothed): the wavelet gradient's gathers
     // CFS-PML (SA_BOUNDARY_CFS_PML, OT2): profiles per axis and nine auxiliary fields per shot
     bool pml = false;
     float *pml_prof = nullptr, *pml_aux = nullptr;
@@ -224,7 +225,8 @@ void plan3d_destroy(Plan3D* p) {
                    p->pml_prof, p->pml_aux};
     for (float* b : fb)
         if (b) cudaFree(b);
-    void* vb[] = {p->e_shot[0], p->e_shot[1], p->e_point[0], p->e_point[1], p->e_idx[0], p->e_idx[1], p->hgat};
+    void* vb[] = {p->e_shot[0], p->e_shot[1], p->e_point[0], p->e_point[1], p->e_idx[0], p->e_idx[1], p->hgat,
+                  p->hgat_src};
     for (void* b : vb)
         if (b) cudaFree(b);
     int* ib[] = {p->s_shot, p->s_base, p->r_shot, p->r_base};
@@ -317,8 +319,8 @@ static int build_points(Plan3D* p, int n_shots, const int* off, const float* xyz
 }
 
 // Hicks support of every point (8 per axis from base - 3, within the grid): injection entries
-// (weight * scale * vp^k at the support point; sources smoothed as the reference's src) and, for
-// the receivers, the gathers of the 8^3 support.
+// (weight * scale * vp^k at the support point; sources smoothed as the reference's src) and the
+// gathers of the 8^3 support (receivers: the traces; sources: the wavelet gradient).
 static int build_hicks(Plan3D* p, int n_shots, const int* off, const float* xyz, bool smooth, double scale,
                        int vp_power, int which) {
     const int n = off[n_shots];
@@ -350,7 +352,7 @@ static int build_hicks(Plan3D* p, int n_shots, const int* off, const float* xyz,
                         idx.push_back(((long long)x * p->ny + y) * p->zp + z);
                         coef.push_back((float)(ww * scale * vpow));
                     }
-            if (which == 1) {
+            {
                 HicksGather3D G;
                 G.x = base[0] - 3;
                 G.y = base[1] - 3;
@@ -377,11 +379,9 @@ static int build_hicks(Plan3D* p, int n_shots, const int* off, const float* xyz,
         CK3(cudaMemcpy(p->e_coef[which], coef.data(), m * sizeof(float), cudaMemcpyHostToDevice));
     }
     p->n_ent[which] = (int)m;
-    if (which == 1) {
-        if ((rc = alloc3(&p->hgat, std::max<size_t>(1, hg.size()))) != SA_OK) return rc;
-        if (!hg.empty())
-            CK3(cudaMemcpy(p->hgat, hg.data(), hg.size() * sizeof(HicksGather3D), cudaMemcpyHostToDevice));
-    }
+    HicksGather3D** dst = which == 1 ? &p->hgat : &p->hgat_src;
+    if ((rc = alloc3(dst, std::max<size_t>(1, hg.size()))) != SA_OK) return rc;
+    if (!hg.empty()) CK3(cudaMemcpy(*dst, hg.data(), hg.size() * sizeof(HicksGather3D), cudaMemcpyHostToDevice));
     (void)n;
     return SA_OK;
 }
@@ -634,7 +634,10 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
 static int wavelet_level(Plan3D* p, const float* q, int t, bool wav, cudaStream_t s, long long& n) {
     if (!wav || !p->n_src) return SA_OK;
     const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
-    CK3(sparse3d_gather(src, p->n_src, q, p->field, p->ny, p->zp, p->wgrad, p->n_src, t, s, -1.f));
+    if (p->hicks)
+        CK3(hicks_gather3d(p->hgat_src, p->n_src, q, p->field, p->ny, p->zp, p->wgrad, p->n_src, t, -1.f, s));
+    else
+        CK3(sparse3d_gather(src, p->n_src, q, p->field, p->ny, p->zp, p->wgrad, p->n_src, t, s, -1.f));
     n++;
     return SA_OK;
 }

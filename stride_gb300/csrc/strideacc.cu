@@ -165,6 +165,8 @@ struct sa_plan {
     // Hicks interpolation: receiver gathers run as their own kernel after each step
     sa::HicksGather* hgat = nullptr;
     size_t cap_hgat = 0;
+    sa::HicksGather* hgat_src = nullptr;  // sources, smoothed and negated: the wavelet gradient
+    size_t cap_hgat_src = 0;
     // source (forward), receiver (adjoint) and exact-gradient receiver injection grouped by target
     // point, each applied by its own kernel after the step
     Targets stgt, rtgt, xtgt;
@@ -260,12 +262,12 @@ struct HostInject {
 // list pointers (not their contents): they are dropped only when a list moves.
 int build_lists_impl(sa_plan* p);
 int build_lists(sa_plan* p) {
-    const void* before[] = {p->gat_flat, p->src_flat, p->gat_src, p->hgat, p->rtgt.idx, p->rtgt.off, p->rtgt.point,
+    const void* before[] = {p->gat_flat, p->src_flat, p->gat_src, p->hgat, p->hgat_src, p->rtgt.idx, p->rtgt.off, p->rtgt.point,
                             p->rtgt.coef, p->stgt.idx, p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx,
                             p->xtgt.off, p->xtgt.point, p->xtgt.coef};
     const int counts_before[3] = {p->stgt.n, p->rtgt.n, p->xtgt.n};
     const int rc = build_lists_impl(p);
-    const void* after[] = {p->gat_flat, p->src_flat, p->gat_src, p->hgat, p->rtgt.idx, p->rtgt.off, p->rtgt.point,
+    const void* after[] = {p->gat_flat, p->src_flat, p->gat_src, p->hgat, p->hgat_src, p->rtgt.idx, p->rtgt.off, p->rtgt.point,
                            p->rtgt.coef, p->stgt.idx, p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx,
                            p->xtgt.off, p->xtgt.point, p->xtgt.coef};
     if (counts_before[0] != p->stgt.n || counts_before[1] != p->rtgt.n || counts_before[2] != p->xtgt.n)
@@ -405,27 +407,36 @@ int build_lists_impl(sa_plan* p) {
     };
     CKR(make_gathers(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, 1.f, &p->gat_flat, &p->cap_gat_flat));
     CKR(make_gathers(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, -1.f, &p->gat_src, &p->cap_gat_src));
-    if (hicks) {  // receivers gathered by their own kernel over the 8 x 8 support
+    // Hicks gathers over the 8 x 8 support: receivers (the forward's traces) and, smoothed as the
+    // sources are and negated, the sources (the adjoint's wavelet gradient, -interp(p_a))
+    auto make_hicks = [&](const std::vector<int>& off, const std::vector<int>& bx, const std::vector<int>& by,
+                          const std::vector<double>& fx, const std::vector<double>& fy, bool smooth, float sign,
+                          sa::HicksGather** dst, size_t* cap) -> int {
         std::vector<sa::HicksGather> hg;
         for (int s = 0; s < p->n_shots; s++)
-            for (int r = p->rec_off[s]; r < p->rec_off[s + 1]; r++) {
+            for (int r = off[s]; r < off[s + 1]; r++) {
                 sa::HicksGather G;
-                G.row = p->rec_bx[r] - 3;
-                G.col = p->rec_by[r] - 3;
+                G.row = bx[r] - 3;
+                G.col = by[r] - 3;
                 G.point = r;
                 G.shot = s;
                 double cx[8], cy[8];
-                sa::hicks_coefs(p->rec_fx[r], false, cx);
-                sa::hicks_coefs(p->rec_fy[r], false, cy);
+                sa::hicks_coefs(fx[r], smooth, cx);
+                sa::hicks_coefs(fy[r], smooth, cy);
                 for (int k = 0; k < 8; k++) {
-                    G.wx[k] = (float)cx[k];
+                    G.wx[k] = sign * (float)cx[k];
                     G.wy[k] = (float)cy[k];
                 }
                 hg.push_back(G);
             }
-        CKR(ensure(&p->hgat, &p->cap_hgat, hg.size()));
-        if (!hg.empty())
-            CK(cudaMemcpy(p->hgat, hg.data(), hg.size() * sizeof(sa::HicksGather), cudaMemcpyHostToDevice));
+        CKR(ensure(dst, cap, hg.size()));
+        if (!hg.empty()) CK(cudaMemcpy(*dst, hg.data(), hg.size() * sizeof(sa::HicksGather), cudaMemcpyHostToDevice));
+        return SA_OK;
+    };
+    if (hicks) {
+        CKR(make_hicks(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, false, 1.f, &p->hgat, &p->cap_hgat));
+        CKR(make_hicks(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, true, -1.f, &p->hgat_src,
+                       &p->cap_hgat_src));
     }
     return SA_OK;
 }
@@ -599,7 +610,10 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
 // The wavelet gradient: -interp(p_a[t]) at the sources into wgrad row t (negated gather weights).
 int wavelet_gather(const sa_plan* p, const float* q, int t, bool wav, cudaStream_t s, long long& n) {
     if (!wav || !p->n_src) return SA_OK;
-    CK(sa::final_gather2d(q, p->shot_stride, p->pitch, p->gat_src, p->n_src, p->wgrad, p->n_src, t, s));
+    if (p->d.interpolation == SA_INTERP_HICKS)
+        CK(sa::hicks_gather2d(q, p->shot_stride, p->pitch, p->hgat_src, p->n_src, p->wgrad, p->n_src, t, s));
+    else
+        CK(sa::final_gather2d(q, p->shot_stride, p->pitch, p->gat_src, p->n_src, p->wgrad, p->n_src, t, s));
     n++;
     return SA_OK;
 }
@@ -1009,7 +1023,7 @@ int sa_plan_destroy(sa_plan* p) {
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
                     p->ones_g, p->zeros_g, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
                     p->dbx, p->dby, p->pml_prof, p->pml_aux,
-                    p->wgrad, p->hgat, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
+                    p->wgrad, p->hgat, p->hgat_src, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
                     p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx, p->xtgt.off, p->xtgt.point, p->xtgt.coef};
     for (void* b : bufs)
         if (b) cudaFree(b);
@@ -1180,8 +1194,6 @@ int sa_adjoint_grads(sa_plan* p, const float* residuals, float* grad_vp, float* 
     if (!p) return fail(SA_E_INVALID, "null plan");
     if (p->p3) {
         if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
-        if (grad_wavelets && p->d.interpolation == SA_INTERP_HICKS)
-            return fail(SA_E_UNSUPPORTED, "the wavelet gradient uses linear interpolation");
         return sa::plan3d_adjoint(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream, grad_rho, prec_rho,
                                   grad_wavelets);
     }
@@ -1200,8 +1212,8 @@ int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec
     const bool exact = grad_mode == SA_GRAD_EXACT;
     const bool wav = grad_wavelets != nullptr;
     if (wav && exact) return fail(SA_E_UNSUPPORTED, "the wavelet gradient is the parity mode's (src.interpolate(-p_a))");
-    if ((wav || exact) && p->d.interpolation == SA_INTERP_HICKS)
-        return fail(SA_E_UNSUPPORTED, "wavelet and exact gradients use linear interpolation");
+    if (exact && p->d.interpolation == SA_INTERP_HICKS)
+        return fail(SA_E_UNSUPPORTED, "the exact gradient uses linear interpolation");
     if (p->p3) {
         if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
         if (exact) return sa::plan3d_adjoint_exact(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream);

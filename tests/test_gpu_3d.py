@@ -262,3 +262,28 @@ def test_cfs_pml_3d():
         g_ref += g
     assert C.cosine(grad, g_ref) >= 0.999
     assert C.rel_l2(grad, g_ref) <= 1e-3
+
+
+def test_wavelet_gradient_hicks_3d():
+    """The wavelet gradient with Hicks interpolation on a 3D plan against the NumPy oracle."""
+    c = case3d(kernel='OT4', density='variable', alpha=False, n_shots=2, nt=110)
+    plan = make_plan3(c, interpolation='hicks')
+    got, plan = C.gpu_forward(c, plan=plan, save=True)
+    res = [g * np.float32(0.8) for g in got]
+    resw = np.ascontiguousarray((np.concatenate(res).astype(np.float64) * C.window(c['nt'])[None, :]).astype(np.float32))
+    shape = c['vp'].shape
+    gw = np.zeros((plan.n_src, c['nt']), np.float32)
+    plan.adjoint(resw, np.zeros(shape, np.float32), np.zeros(shape, np.float32), grad_wavelets=gw)
+    origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
+    kw = dict(rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation='hicks')
+    k = 0
+    for s in range(2):
+        wav = np.tile(c['wav'][None], (len(c['srcs'][s]), 1))
+        _, snaps = npo.forward(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][s], c['recs'][s],
+                               wav, origin, save=True, **kw)
+        _, _, g_ref = npo.adjoint(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['recs'][s], res[s],
+                                  origin, snaps, src_coords=c['srcs'][s], **kw)
+        ns = len(c['srcs'][s])
+        assert np.abs(g_ref).max() > 0
+        assert C.rel_l2(gw[k:k + ns], g_ref) <= 1e-4
+        k += ns

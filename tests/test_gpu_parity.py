@@ -134,3 +134,31 @@ def test_hicks_interpolation_parity(density):
         g_ref += g
     assert C.cosine(grad, g_ref) >= 0.999
     assert C.rel_l2(grad, g_ref) <= 1e-3
+
+
+def test_wavelet_gradient_hicks():
+    """The wavelet gradient with Hicks interpolation: -interp(p_a) over the sources' smoothed 8 x 8
+    support, against the NumPy oracle."""
+    from oracle import numpy_oracle as npo
+    c = C.small_case(kernel='OT4', density='variable', alpha=True, n_shots=2, uneven=True, nt=200, inner=48)
+    plan = C.make_plan(c, interpolation='hicks')
+    got, plan = C.gpu_forward(c, plan=plan, save=True)
+    rng = np.random.default_rng(6)
+    res = [rng.standard_normal(g.shape).astype(np.float32) * np.abs(g).max() for g in got]
+    resw = np.ascontiguousarray((np.concatenate(res).astype(np.float64) * C.window(c['nt'])[None, :]).astype(np.float32))
+    gw = np.zeros((plan.n_src, c['nt']), np.float32)
+    plan.adjoint(resw, np.zeros(c['vp'].shape, np.float32), np.zeros(c['vp'].shape, np.float32), grad_wavelets=gw)
+    origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
+    k = 0
+    for s in range(2):
+        wav = np.tile(c['wav'][None], (len(c['srcs'][s]), 1))
+        _, snaps = npo.forward(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][s], c['recs'][s],
+                               wav, origin, rho=c['rho'], alpha=c['alpha'], kernel='OT4', save=True,
+                               interpolation='hicks')
+        _, _, g_ref = npo.adjoint(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['recs'][s], res[s], origin,
+                                  snaps, rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation='hicks',
+                                  src_coords=c['srcs'][s])
+        ns = len(c['srcs'][s])
+        assert np.abs(g_ref).max() > 0
+        assert C.rel_l2(gw[k:k + ns], g_ref) <= 1e-4
+        k += ns
