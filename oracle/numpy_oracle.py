@@ -693,7 +693,7 @@ def _coefficient_derivatives(med, damp, dt):
 
 
 def adjoint_exact(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavelets, rec_weights, origin,
-                  rho=None, alpha=None, kernel=None):
+                  rho=None, alpha=None, kernel=None, interpolation='linear'):
     """Exact discrete adjoint of ``forward`` (FP64): the gradient of L = sum(rec_weights * traces)
     with respect to vp at every grid point and to the raw wavelets, i.e. the transpose of the
     linearised forward map applied to ``rec_weights`` [n_rec, nt] (dL/dtraces).
@@ -706,7 +706,8 @@ def adjoint_exact(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavele
     derivative of the update: the coefficients (attenuation and damping included), W inside Lt
     (dW/dvp = 2 W / vp), the OT4 term's inner W (dt^2/12 dW (G u)(G z)) and the source
     injection's vp factor. This is the ``exact`` gradient mode (no counterpart in the
-    reference, whose imaging condition is iso_acoustic/devito.py:985-1043)."""
+    reference, whose imaging condition is iso_acoustic/devito.py:985-1043). ``interpolation``:
+    'linear' or 'hicks' (sources smoothed, receivers not) for both the forward and its transpose."""
     dim = vp.ndim
     shape = vp.shape
     h = max(spacing)
@@ -718,12 +719,11 @@ def adjoint_exact(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavele
     med = _Medium(vp, rho, alpha, spacing, t64)
     damp = damping_profile(shape, spacing, absorbing, vp, dt).astype(t64)
     eps = 1e-3 * np.asarray(spacing)
-    sb, sw = linear_stencil(np.asarray(src_coords, np.float32) + eps, origin, spacing)
-    rb, rw = linear_stencil(np.asarray(rec_coords, np.float32) + eps, origin, spacing)
+    sb, sw, offs = sparse_stencil(interpolation, np.asarray(src_coords, np.float32) + eps, origin, spacing, True)
+    rb, rw, roffs = sparse_stencil(interpolation, np.asarray(rec_coords, np.float32) + eps, origin, spacing, False)
     win = tukey(nt)
     src = np.asarray(wavelets, np.float64).T * win[:, None]
     scale = 2 * dt / h
-    offs = _corner_offsets(dim)
     # forward levels u[0..nt-1]
     u = np.zeros((nt,) + shape)
     for n in range(1, nt - 1):
@@ -743,7 +743,7 @@ def adjoint_exact(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavele
     for n in range(nt - 1, 1, -1):
         zn = _update(med, damp, _Lt(med, z1, kernel, dt, w2, ws), z1, z2, dt) if n < nt - 1 else np.zeros(shape)
         if 1 <= n - 1 <= nt - 2:
-            for c, off in enumerate(offs):
+            for c, off in enumerate(roffs):
                 idx = tuple(rb[:, d] + off[d] for d in range(dim))
                 np.add.at(zn, idx, rw[:, c] * r[n - 1] * (C1 * W)[idx])
         # contributions of step m = n-1 (u[n] = RHS(u[n-1], u[n-2])) with mu[n] = z[n] / (C1 W)

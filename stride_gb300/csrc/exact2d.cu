@@ -86,21 +86,16 @@ __global__ void k_exact_grad2d(const float2* __restrict__ z, const float2* __res
     }
 }
 
-// Source term at the corners of each source point: z w src[trow] (2 dt / h) ES.
-__global__ void k_exact_src2d(const float* __restrict__ z, const Gather* __restrict__ g, int n,
+// Source term at each support point of each source (linear corners or the smoothed Hicks
+// support): z w src[trow] (2 dt / h) ES.
+__global__ void k_exact_src2d(const float* __restrict__ z, const ExactSrc2D* __restrict__ e, int n,
                               const float* __restrict__ amp, int ld, int trow, float scale,
-                              const float* __restrict__ ES, int pitch, long long shot_stride, float* gradb) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n) return;
-    const Gather G = g[e];  // pad = shot
-    const int pair = G.pad / 2, lane = G.pad & 1;
-    const float a = amp[(long long)trow * ld + G.point] * scale;
-    const float w[4] = {G.w00, G.w01, G.w10, G.w11};
-    for (int c = 0; c < 4; c++) {
-        const long long p = (long long)(G.row + (c >> 1)) * pitch + G.col + (c & 1);
-        const long long i = (long long)pair * shot_stride + p;
-        atomicAdd(gradb + i, z[2 * i + lane] * w[c] * a * ES[p]);
-    }
+                              const float* __restrict__ ES, float* gradb) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const ExactSrc2D E = e[k];
+    const float a = amp[(long long)trow * ld + E.point] * scale;
+    atomicAdd(gradb + E.i, z[2 * E.i + E.lane] * E.w * a * ES[E.p]);
 }
 
 }  // namespace
@@ -125,10 +120,10 @@ cudaError_t exact_grad2d(const float* z, const float* u0, const float* u1, const
     return cudaGetLastError();
 }
 
-cudaError_t exact_src2d(const float* z, const Gather* g, int n, const float* amp, int ld, int trow, float scale,
-                        const float* ES, int pitch, long long shot_stride, float* gradb, cudaStream_t s) {
+cudaError_t exact_src2d(const float* z, const ExactSrc2D* e, int n, const float* amp, int ld, int trow, float scale,
+                        const float* ES, float* gradb, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_exact_src2d<<<(n + 127) / 128, 128, 0, s>>>(z, g, n, amp, ld, trow, scale, ES, pitch, shot_stride, gradb);
+    k_exact_src2d<<<(n + 127) / 128, 128, 0, s>>>(z, e, n, amp, ld, trow, scale, ES, gradb);
     return cudaGetLastError();
 }
 

@@ -24,8 +24,15 @@ cudaError_t exact_grad2d(const float* z, const float* u0, const float* u1, const
                          const float* Lz, const float* EA, const float* EB, const float* EC, const float* EG4, int nx,
                          int ny, int pitch, int npairs, long long shot_stride, float inv_dt2, float* gradb,
                          float* precb, cudaStream_t s);
-cudaError_t exact_src2d(const float* z, const Gather* g, int n, const float* amp, int ld, int trow, float scale,
-                        const float* ES, int pitch, long long shot_stride, float* gradb, cudaStream_t s);
+// One support point of a source for the exact gradient's source term: plane index within the
+// pair's gradient buffer (i) and within a plane (p), lane of the pair, source row, raw weight.
+struct ExactSrc2D {
+    long long i;
+    int p, lane, point;
+    float w;
+};
+cudaError_t exact_src2d(const float* z, const ExactSrc2D* e, int n, const float* amp, int ld, int trow, float scale,
+                        const float* ES, float* gradb, cudaStream_t s);
 
 // 3D plans
 // Hicks coefficients of one axis at the fractional offset frac (index 3 + grid offset, -3..4).
@@ -44,6 +51,11 @@ struct HicksGather3D;
 cudaError_t pml3d(const float* cur, float* nxt, float* aux, const float* prof, const float* C1, const float* vp,
                   int nx, int ny, int nz, int zp, int nshots, long long field, const int* a, const double* h, float dt,
                   int adjoint, float* snap, long long snap_shot_stride, float inv_dt2, cudaStream_t s);
+// Hicks forms of the 3D exact gradient's receiver coefficients and source term.
+cudaError_t xcoef_entries3d(const long long* idx, const float* w, int n, const float* C1, const float* W, float* out,
+                            cudaStream_t s);
+cudaError_t exact_src_entries3d(const float* z, const Entries3D& e, const float* w, int n, const float* amp, int ld,
+                                int trow, float scale, const float* ES, long long field, float* gradb, cudaStream_t s);
 // Hicks injection (flat support entries) and gather (8^3 support) of 3D plans.
 cudaError_t inject_entries3d(const Entries3D& e, int n, const float* amp, int ld, int t, float* field,
                              long long shot_stride, float* snap, long long snap_shot_stride, long long snap_off,

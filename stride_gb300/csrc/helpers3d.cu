@@ -551,6 +551,37 @@ cudaError_t pml3d(const float* cur, float* nxt, float* aux, const float* prof, c
     return cudaGetLastError();
 }
 
+// Hicks forms of the 3D exact gradient's point terms: receiver coefficients w C1 W at each
+// support entry, and the source term z w src[trow] scale ES at each source support entry.
+__global__ void k_xcoef_entries3d(const long long* __restrict__ idx, const float* __restrict__ w, int n,
+                                  const float* __restrict__ C1, const float* __restrict__ W, float* out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] = w[k] * (C1[idx[k]] * W[idx[k]]);
+}
+
+__global__ void k_exact_src_entries3d(const float* __restrict__ z, const Entries3D e, const float* __restrict__ w,
+                                      int n, const float* __restrict__ amp, int ld, int trow, float scale,
+                                      const float* __restrict__ ES, long long field, float* gradb) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const long long p = e.idx[k], i = (long long)e.shot[k] * field + p;
+    atomicAdd(gradb + i, z[i] * w[k] * amp[(long long)trow * ld + e.point[k]] * scale * ES[p]);
+}
+
+cudaError_t xcoef_entries3d(const long long* idx, const float* w, int n, const float* C1, const float* W, float* out,
+                            cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_xcoef_entries3d<<<(n + 255) / 256, 256, 0, s>>>(idx, w, n, C1, W, out);
+    return cudaGetLastError();
+}
+
+cudaError_t exact_src_entries3d(const float* z, const Entries3D& e, const float* w, int n, const float* amp, int ld,
+                                int trow, float scale, const float* ES, long long field, float* gradb, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_exact_src_entries3d<<<(n + 255) / 256, 256, 0, s>>>(z, e, w, n, amp, ld, trow, scale, ES, field, gradb);
+    return cudaGetLastError();
+}
+
 cudaError_t reduce3d(const float* buf, long long shot_stride, int nshots, int nx, int ny, int nz, int zp, float* out,
                      cudaStream_t s) {
     k_reduce3d<<<2048, 256, 0, s>>>(buf, shot_stride, nshots, nx, ny, nz, zp, out);

@@ -147,6 +147,8 @@ struct Plan3D {
     int *e_shot[2] = {}, *e_point[2] = {};
     long long* e_idx[2] = {};
     float* e_coef[2] = {};
+    float* e_w[2] = {};  // raw support weights (the exact gradient's point terms)
+    float* e_xcoef = nullptr;  // receivers' w C1 W (exact gradient)
     int n_ent[2] = {0, 0};
     HicksGather3D* hgat = nullptr;
     HicksGather3D* hgat_src = nullptr;  // sources (smoothed): the wavelet gradient's gathers
@@ -222,7 +224,7 @@ void plan3d_destroy(Plan3D* p) {
                    p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps, p->A[0], p->A[1], p->hold_vp, p->hold_rho,
                    p->gradrb, p->precrb, p->db[0], p->db[1], p->db[2], p->wgrad, p->EA, p->EB, p->EC, p->EG4,
                    p->ES, p->levels, p->Lu, p->Lz, p->ones, p->zeros, p->r_xcoef, p->e_coef[0], p->e_coef[1],
-                   p->pml_prof, p->pml_aux};
+                   p->pml_prof, p->pml_aux, p->e_w[0], p->e_w[1], p->e_xcoef};
     for (float* b : fb)
         if (b) cudaFree(b);
     void* vb[] = {p->e_shot[0], p->e_shot[1], p->e_point[0], p->e_point[1], p->e_idx[0], p->e_idx[1], p->hgat,
@@ -326,7 +328,7 @@ static int build_hicks(Plan3D* p, int n_shots, const int* off, const float* xyz,
     const int n = off[n_shots];
     std::vector<int> shot, point;
     std::vector<long long> idx;
-    std::vector<float> coef;
+    std::vector<float> coef, wraw;
     std::vector<HicksGather3D> hg;
     for (int s = 0; s < n_shots; s++)
         for (int i = off[s]; i < off[s + 1]; i++) {
@@ -351,6 +353,7 @@ static int build_hicks(Plan3D* p, int n_shots, const int* off, const float* xyz,
                         point.push_back(i);
                         idx.push_back(((long long)x * p->ny + y) * p->zp + z);
                         coef.push_back((float)(ww * scale * vpow));
+                        wraw.push_back((float)ww);
                     }
             {
                 HicksGather3D G;
@@ -370,13 +373,15 @@ static int build_hicks(Plan3D* p, int n_shots, const int* off, const float* xyz,
     const size_t m = coef.size();
     int rc = SA_OK;
     if ((rc = alloc3(&p->e_shot[which], m)) != SA_OK || (rc = alloc3(&p->e_point[which], m)) != SA_OK ||
-        (rc = alloc3(&p->e_idx[which], m)) != SA_OK || (rc = alloc3(&p->e_coef[which], m)) != SA_OK)
+        (rc = alloc3(&p->e_idx[which], m)) != SA_OK || (rc = alloc3(&p->e_coef[which], m)) != SA_OK ||
+        (rc = alloc3(&p->e_w[which], m)) != SA_OK)
         return rc;
     if (m) {
         CK3(cudaMemcpy(p->e_shot[which], shot.data(), m * sizeof(int), cudaMemcpyHostToDevice));
         CK3(cudaMemcpy(p->e_point[which], point.data(), m * sizeof(int), cudaMemcpyHostToDevice));
         CK3(cudaMemcpy(p->e_idx[which], idx.data(), m * sizeof(long long), cudaMemcpyHostToDevice));
         CK3(cudaMemcpy(p->e_coef[which], coef.data(), m * sizeof(float), cudaMemcpyHostToDevice));
+        CK3(cudaMemcpy(p->e_w[which], wraw.data(), m * sizeof(float), cudaMemcpyHostToDevice));
     }
     p->n_ent[which] = (int)m;
     HicksGather3D** dst = which == 1 ? &p->hgat : &p->hgat_src;
@@ -841,6 +846,11 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
         if ((rc = alloc3(&p->r_xcoef, 8 * (size_t)std::max(1, p->n_rec))) != SA_OK) return rc;
         const Sparse3D rec{p->r_shot, p->r_base, p->r_w, p->r_coef};
         CK3(xcoef3d(rec, p->n_rec, p->C1 + G * p->plane, p->W + G * p->plane, p->ny, p->zp, p->r_xcoef, 0));
+        if (p->hicks) {
+            if ((rc = alloc3(&p->e_xcoef, std::max<size_t>(1, p->n_ent[1]))) != SA_OK) return rc;
+            CK3(xcoef_entries3d(p->e_idx[1], p->e_w[1], p->n_ent[1], p->C1 + G * p->plane, p->W + G * p->plane,
+                                p->e_xcoef, 0));
+        }
         CK3(cudaDeviceSynchronize());
         p->exact_valid = true;
     }
@@ -889,8 +899,14 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
             aa.t = t;
             if ((rc = step3(p, aa, zt, znext, -1, p->rec_amp, false, s, n)) != SA_OK) return rc;
             if (p->n_rec) {  // z[t-1] += w C1 W dL/drec[t-2]
-                CK3(sparse3d_inject(recx, p->n_rec, p->rec_amp, p->n_rec, t - 2, znext, p->field, p->ny, p->zp,
-                                    nullptr, 0, 0, 0.f, s));
+                if (p->hicks) {
+                    const Entries3D e{p->e_shot[1], p->e_point[1], p->e_idx[1], p->e_xcoef};
+                    CK3(inject_entries3d(e, p->n_ent[1], p->rec_amp, p->n_rec, t - 2, znext, p->field, nullptr, 0, 0,
+                                         0.f, s));
+                } else {
+                    CK3(sparse3d_inject(recx, p->n_rec, p->rec_amp, p->n_rec, t - 2, znext, p->field, p->ny, p->zp,
+                                        nullptr, 0, 0, 0.f, s));
+                }
                 n++;
             }
             if (t > nt - 1) continue;  // z[nt] = 0
@@ -912,8 +928,14 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
                              p->ny, p->nz, p->zp, p->n_shots, p->field, inv_dt2, p->gradb, p->precb, s));
             n++;
             if (p->n_src) {
-                CK3(exact_src3d(zt, src, p->n_src, p->src_amp, p->n_src, t - 1, src_scale, p->ES, p->ny, p->zp,
-                                p->field, p->gradb, s));
+                if (p->hicks) {
+                    const Entries3D e{p->e_shot[0], p->e_point[0], p->e_idx[0], p->e_coef[0]};
+                    CK3(exact_src_entries3d(zt, e, p->e_w[0], p->n_ent[0], p->src_amp, p->n_src, t - 1, src_scale,
+                                            p->ES, p->field, p->gradb, s));
+                } else {
+                    CK3(exact_src3d(zt, src, p->n_src, p->src_amp, p->n_src, t - 1, src_scale, p->ES, p->ny, p->zp,
+                                    p->field, p->gradb, s));
+                }
                 n++;
             }
         }

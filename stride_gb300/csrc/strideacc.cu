@@ -156,8 +156,9 @@ struct sa_plan {
            cap_ones = 0, cap_zeros = 0;
     bool exact_coef_valid = false;
     std::vector<float> c1w_host;
-    sa::Gather* src_flat = nullptr;
+    sa::ExactSrc2D* src_flat = nullptr;  // support points of the sources (exact gradient's source term)
     size_t cap_src_flat = 0;
+    int n_src_flat = 0;
     // wavelet gradient: source gathers with negated weights and its time-major buffer
     sa::Gather* gat_src = nullptr;
     float* wgrad = nullptr;
@@ -369,17 +370,17 @@ int build_lists_impl(sa_plan* p) {
     // exact-gradient adjoint: dL/drec injected with the update's own C1 W at the corner
     make_inj(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, 1.0, c1w_at, tmp, false);
     CKR(make_targets(tmp, p->xtgt));
-    {  // flat source list (pad = shot) for the exact gradient's source term
-        std::vector<sa::Gather> sf;
-        for (int s = 0; s < p->n_shots; s++)
-            for (int i = p->src_off[s]; i < p->src_off[s + 1]; i++) {
-                const double fx = p->src_fx[i], fy = p->src_fy[i];
-                sf.push_back({p->src_bx[i], p->src_by[i], i, s, (float)((1 - fx) * (1 - fy)), (float)((1 - fx) * fy),
-                              (float)(fx * (1 - fy)), (float)(fx * fy)});
-            }
-        CKR(ensure(&p->src_flat, &p->cap_src_flat, sf.size()));
+    {  // the sources' support points with their raw weights, for the exact gradient's source term
+        make_inj(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, 1.0, [](int, int) { return 1.0; }, tmp, true);
+        std::vector<sa::ExactSrc2D> sf;
+        for (const HostInject& e : tmp) {
+            const long long pair = e.cta / (nc * ns), pl = (long long)e.row * p->pitch + e.col;
+            sf.push_back({pair * p->shot_stride + pl, (int)pl, e.lane, e.point, e.coef});
+        }
+        CKR(ensure(&p->src_flat, &p->cap_src_flat, std::max<size_t>(1, sf.size())));
         if (!sf.empty())
-            CK(cudaMemcpy(p->src_flat, sf.data(), sf.size() * sizeof(sa::Gather), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(p->src_flat, sf.data(), sf.size() * sizeof(sa::ExactSrc2D), cudaMemcpyHostToDevice));
+        p->n_src_flat = (int)sf.size();
     }
     // gathers, one per point, owned by the CTA of its base corner: receivers (the forward's traces)
     // and sources with negated weights (the adjoint's wavelet gradient, -interp(p_a))
@@ -812,8 +813,8 @@ int issue_adjoint_exact(sa_plan* p, cudaStream_t s) {
                                 p->nx, p->ny, p->pitch, npairs(p), p->shot_stride, inv_dt2, p->gradb, p->precb, s));
             n++;
             if (p->n_src) {
-                CK(sa::exact_src2d(zt, p->src_flat, p->n_src, p->src_amp, p->n_src, t - 1, src_scale, p->ES, p->pitch,
-                                   p->shot_stride, p->gradb, s));
+                CK(sa::exact_src2d(zt, p->src_flat, p->n_src_flat, p->src_amp, p->n_src, t - 1, src_scale, p->ES,
+                                   p->gradb, s));
                 n++;
             }
         }
@@ -1212,8 +1213,6 @@ int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec
     const bool exact = grad_mode == SA_GRAD_EXACT;
     const bool wav = grad_wavelets != nullptr;
     if (wav && exact) return fail(SA_E_UNSUPPORTED, "the wavelet gradient is the parity mode's (src.interpolate(-p_a))");
-    if (exact && p->d.interpolation == SA_INTERP_HICKS)
-        return fail(SA_E_UNSUPPORTED, "the exact gradient uses linear interpolation");
     if (p->p3) {
         if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
         if (exact) return sa::plan3d_adjoint_exact(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream);

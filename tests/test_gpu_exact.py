@@ -99,3 +99,27 @@ def test_exact_mode_needs_checkpoints():
     with pytest.raises(_lib.StrideAccError):
         plan.adjoint(np.zeros((plan.n_rec, c['nt']), np.float32), np.zeros(c['vp'].shape, np.float32),
                      np.zeros(c['vp'].shape, np.float32), exact=True)
+
+
+def test_exact_gradient_hicks():
+    """SA_GRAD_EXACT with Hicks sources and receivers (the forward's support in its transpose)
+    against the FP64 exact-adjoint oracle with the same interpolation."""
+    c = C.small_case(kernel='OT4', density='variable', alpha=True, inner=40, nt=160, n_shots=2, uneven=True)
+    plan = C.make_plan(c, checkpoint_interval=16, interpolation='hicks')
+    n_rec = sum(len(r) for r in c['recs'])
+    weights = np.random.default_rng(8).standard_normal((n_rec, c['nt']))
+    _, g = _exact(c, plan, weights)
+    origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
+    ref = np.zeros(c['vp'].shape)
+    k = 0
+    for s in range(2):
+        nr = len(c['recs'][s])
+        wav = np.tile(c['wav'][None], (len(c['srcs'][s]), 1))
+        gs, _ = npo.adjoint_exact(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][s],
+                                  c['recs'][s], wav, weights[k:k + nr], origin, rho=c['rho'], alpha=c['alpha'],
+                                  kernel='OT4', interpolation='hicks')
+        ref += gs
+        k += nr
+    assert np.abs(ref).max() > 0
+    assert C.cosine(g, ref) >= 0.99999
+    assert C.rel_l2(g, ref) <= 2e-3

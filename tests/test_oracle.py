@@ -240,3 +240,17 @@ def test_cfs_pml_absorbs_better_than_the_sponge():
     sponge = run(e)
     err = lambda tr: np.linalg.norm(tr - big) / np.linalg.norm(big)
     assert err(pml) < 0.03 and err(pml) < err(sponge) / 3
+
+
+def test_exact_adjoint_dot_product_hicks():
+    """The exact adjoint with Hicks sources (smoothed) and receivers: <F w, r> = <w, F^T r>."""
+    c = _exact_case('OT4', 'variable', True)
+    r = c['rng'].standard_normal((len(c['rec']), c['nt']))
+    w = c['rng'].standard_normal(c['wav'].shape).astype(np.float32).astype(np.float64)
+    _, gw = O.adjoint_exact(c['vp'], c['spacing'], c['dt'], c['nt'], c['ab'], c['src'], c['rec'], w, r, c['origin'],
+                            rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation='hicks')
+    tr = O.forward(c['vp'], c['spacing'], c['dt'], c['nt'], c['ab'], c['src'], c['rec'], w, c['origin'], rho=c['rho'],
+                   alpha=c['alpha'], kernel='OT4', dtype=np.float64, interpolation='hicks')[0]
+    lhs = float(np.sum(tr * r))
+    rhs = float(np.sum(gw * w))
+    assert abs(lhs - rhs) <= 1e-6 * abs(lhs)
