@@ -69,16 +69,16 @@ void ramp(int A, double h, double refl, float* out) {
 
 }  // namespace
 
-// The requested interval (50 by default), unless the checkpoints and one segment's snapshots
-// exceed the byte budget; then the multiple of f nearest to it that fits.
-int choose_checkpoints(const sa_desc& d, double level, int* K_out, int* n_out) {
+// The requested interval (50 by default), unless the checkpoints (ck_levels levels each) and one
+// segment's snapshots exceed the byte budget; then the multiple of f nearest to it that fits.
+int choose_checkpoints(const sa_desc& d, double level, int* K_out, int* n_out, double ck_levels) {
     const int f = d.undersampling;
     const int T0 = d.nt - 1 - f;
     int K = d.checkpoint_interval > 0 ? d.checkpoint_interval : 50;
     K = (K + f - 1) / f * f;
     // checkpoints after steps K, 2K, .. <= nt-2 (the exact adjoint's segments reach that far) and
     // one segment's K/f snapshots
-    auto bytes = [&](int k) { return ((d.nt - 2) / k) * 2 * level + (k / f) * level; };
+    auto bytes = [&](int k) { return ((d.nt - 2) / k) * ck_levels * level + (k / f) * level; };
     if (d.checkpoint_budget > 0 && bytes(K) > d.checkpoint_budget) {
         int best = -1;
         double least = 1e300;
@@ -155,6 +155,10 @@ struct Plan3D {
     // CFS-PML (SA_BOUNDARY_CFS_PML, OT2): profiles per axis and nine auxiliary fields per shot
     bool pml = false;
     float *pml_prof = nullptr, *pml_aux = nullptr;
+    // with checkpoints: the forward's auxiliary fields at every checkpoint, and the set the forward
+    // recompute advances (the adjoint keeps its own in pml_aux)
+    float *pml_ck = nullptr, *pml_aux_f = nullptr;
+    size_t cap_pml_ck = 0;
     long long launches = 0;
     int chunk_rows = 0, nchunks = 1, ty0n = 1, tz0n = 1;
 };
@@ -224,7 +228,7 @@ void plan3d_destroy(Plan3D* p) {
                    p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps, p->A[0], p->A[1], p->hold_vp, p->hold_rho,
                    p->gradrb, p->precrb, p->db[0], p->db[1], p->db[2], p->wgrad, p->EA, p->EB, p->EC, p->EG4,
                    p->ES, p->levels, p->Lu, p->Lz, p->ones, p->zeros, p->r_xcoef, p->e_coef[0], p->e_coef[1],
-                   p->pml_prof, p->pml_aux, p->e_w[0], p->e_w[1], p->e_xcoef};
+                   p->pml_prof, p->pml_aux, p->pml_ck, p->pml_aux_f, p->e_w[0], p->e_w[1], p->e_xcoef};
     for (float* b : fb)
         if (b) cudaFree(b);
     void* vb[] = {p->e_shot[0], p->e_shot[1], p->e_point[0], p->e_point[1], p->e_idx[0], p->e_idx[1], p->hgat,
@@ -502,9 +506,9 @@ static int image_raw_level(Plan3D* p, const Step3D& a, const float* q, bool rho,
 
 // One time level: [pass A] + pass B, then injection into the new level (and its snapshot).
 // which: 0 injects the sources (amp = their samples), 1 the receivers, -1 nothing; linear or Hicks
-// as the plan's interpolation.
+// as the plan's interpolation. aux: the CFS-PML auxiliary fields advanced (default: the plan's).
 static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, int which, const float* amp, bool save_now,
-                 cudaStream_t s, long long& n) {
+                 cudaStream_t s, long long& n, float* aux = nullptr) {
     const dim3 grid(p->ty0n * p->tz0n * p->n_shots, p->nchunks, 1);
     a.cur = cur;
     a.prev = prev;
@@ -521,7 +525,7 @@ static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, int which,
     n++;
     const float inv_dt2 = (float)(1.0 / ((double)a.dt * (double)a.dt));
     if (p->pml) {  // auxiliary fields and the boundary term of the new level (which 1: the adjoint)
-        CK3(pml3d(cur, prev, p->pml_aux, p->pml_prof, p->C1 + (long long)GUARD * p->plane, p->vp, p->nx, p->ny, p->nz,
+        CK3(pml3d(cur, prev, aux ? aux : p->pml_aux, p->pml_prof, p->C1 + (long long)GUARD * p->plane, p->vp, p->nx, p->ny, p->nz,
                   p->zp, p->n_shots, p->field, p->d.absorbing, p->d.spacing, a.dt, which == 1 ? 1 : 0,
                   save_now ? a.snaps + (long long)(a.t / a.f) * a.snap_stride : nullptr, a.snap_shot_stride, inv_dt2,
                   s));
@@ -550,7 +554,6 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
     const bool raw = save_mode == SA_SAVE_RAW;
     const bool save = save_mode == SA_SAVE_SNAPSHOTS || raw;
     const bool ckpt = save_mode == SA_SAVE_CHECKPOINTS;
-    if (ckpt && p->pml) return fail3(SA_E_UNSUPPORTED, "checkpoints are implemented for the sponge boundary");
     p->ckpt_valid = false;  // the wavelets the checkpointed adjoint re-injects are replaced
     if (save && (size_t)p->n_shots * p->n_snap * p->snap_stride > p->cap_snaps) {
         p->cap_snaps = (size_t)p->n_shots * p->n_snap * p->snap_stride;
@@ -559,13 +562,21 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
     }
     const size_t level = (size_t)p->n_shots * p->field;  // floats of one level of every shot
     if (ckpt) {
-        int rc = choose_checkpoints(p->d, (double)level * sizeof(float), &p->ck_K, &p->ck_n);
+        // a checkpoint holds both levels and, with the CFS-PML, its nine auxiliary fields
+        int rc = choose_checkpoints(p->d, (double)level * sizeof(float), &p->ck_K, &p->ck_n, p->pml ? 11 : 2);
         if (rc != SA_OK) return rc;
         const size_t need = std::max<size_t>(1, (size_t)p->ck_n * 2 * level);
         if (need > p->cap_ckpt) {
             if ((rc = alloc3(&p->ckpt, need)) != SA_OK) return rc;
             p->cap_ckpt = need;
         }
+        const size_t need_pml = std::max<size_t>(1, (size_t)p->ck_n * 9 * level);
+        if (p->pml && need_pml > p->cap_pml_ck) {
+            if ((rc = alloc3(&p->pml_ck, need_pml)) != SA_OK) return rc;
+            p->cap_pml_ck = need_pml;
+        }
+        if (p->pml && !p->pml_aux_f && (rc = alloc3(&p->pml_aux_f, 9 * std::max(1, p->d.max_shots) * (size_t)p->field)))
+            return rc;
         p->snaps_valid = false;
     }
     int rc = load_tm(p, wavelets, p->n_src, p->d.nt, p->src_amp, s);
@@ -604,6 +615,9 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
             float* slot = p->ckpt + (size_t)(t / p->ck_K - 1) * 2 * level;
             CK3(cudaMemcpyAsync(slot, p->F[0], level * sizeof(float), cudaMemcpyDeviceToDevice, s));
             CK3(cudaMemcpyAsync(slot + level, p->F[1], level * sizeof(float), cudaMemcpyDeviceToDevice, s));
+            if (p->pml)  // the CFS-PML's auxiliary fields after step t
+                CK3(cudaMemcpyAsync(p->pml_ck + (size_t)(t / p->ck_K - 1) * 9 * level, p->pml_aux,
+                                    9 * level * sizeof(float), cudaMemcpyDeviceToDevice, s));
         }
     }
     if (p->n_rec) {
@@ -662,10 +676,14 @@ static int adjoint_segments(Plan3D* p, Step3D& aa, const Sparse3D& rec, bool wav
         if (k == 0) {
             CK3(cudaMemsetAsync(p->F[0], 0, lb, s));
             CK3(cudaMemsetAsync(p->F[1], 0, lb, s));
+            if (p->pml) CK3(cudaMemsetAsync(p->pml_aux_f, 0, 9 * lb, s));
         } else {
             const float* slot = p->ckpt + (size_t)(k - 1) * 2 * level;
             CK3(cudaMemcpyAsync(p->F[0], slot, lb, cudaMemcpyDeviceToDevice, s));
             CK3(cudaMemcpyAsync(p->F[1], slot + level, lb, cudaMemcpyDeviceToDevice, s));
+            if (p->pml)
+                CK3(cudaMemcpyAsync(p->pml_aux_f, p->pml_ck + (size_t)(k - 1) * 9 * level, 9 * lb,
+                                    cudaMemcpyDeviceToDevice, s));
         }
         // the kernels address snapshot t/f; slot t/f - (kK/f + 1) of the segment buffer is meant
         const long long first = (long long)k * K / f + 1;
@@ -675,7 +693,7 @@ static int adjoint_segments(Plan3D* p, Step3D& aa, const Sparse3D& rec, bool wav
         for (int t = t_lo; t <= t_hi; t++) {
             fa.t = t;
             int rc = step3(p, fa, (t & 1) ? p->F[1] : p->F[0], (t & 1) ? p->F[0] : p->F[1], 0,
-                           p->src_amp, t % f == 0, s, n);
+                           p->src_amp, t % f == 0, s, n, p->pml_aux_f);
             if (rc != SA_OK) return rc;
         }
         for (int t = t_hi; t >= t_lo; t--) {

@@ -141,6 +141,10 @@ struct sa_plan {
     bool pml = false;
     float *pml_prof = nullptr, *pml_aux = nullptr;
     size_t cap_pml_prof = 0, cap_pml_aux = 0;
+    // with checkpoints: the forward's auxiliary fields at every checkpoint, and a second set for the
+    // forward recompute (the adjoint keeps its own in pml_aux)
+    float *pml_ck = nullptr, *pml_aux_f = nullptr;
+    size_t cap_pml_ck = 0, cap_pml_aux_f = 0;
     // checkpoints (SA_SAVE_CHECKPOINTS): both levels after every ck_K-th forward step, the
     // recomputed snapshots of one segment, and the adjoint's own two levels
     float *ckpt = nullptr, *segsnaps = nullptr, *afield[2] = {nullptr, nullptr};
@@ -509,19 +513,22 @@ int image_step(const sa_plan* p, const float* q, const float* snaps_base, long l
 
 // The CFS-PML after the step of level cur (new level nxt, its p.dt2 snapshot slot snap or null):
 // auxiliary fields of the absorbing slabs and the boundary term of the new level.
+// aux: the auxiliary fields advanced (default: the plan's), snap_pair: snapshot stride per pair.
 int pml_step(const sa_plan* p, const float* cur, float* nxt, bool adjoint, float* snap, cudaStream_t s,
-             long long& n) {
+             long long& n, float* aux = nullptr, long long snap_pair = -1) {
     if (!p->pml) return SA_OK;
-    CK(sa::pml2d(cur, nxt, p->pml_aux, p->pml_prof, row0(p, p->C1, p->pitch), p->vp, p->nx, p->ny, p->pitch,
-                 p->shot_stride, npairs(p), p->d.absorbing[0], p->d.absorbing[1], (float)p->d.spacing[0],
-                 (float)p->d.spacing[1], (float)p->d.dt, adjoint ? 1 : 0, snap, p->snap_shot_stride,
-                 (float)(1.0 / (p->d.dt * p->d.dt)), s));
+    CK(sa::pml2d(cur, nxt, aux ? aux : p->pml_aux, p->pml_prof, row0(p, p->C1, p->pitch), p->vp, p->nx, p->ny,
+                 p->pitch, p->shot_stride, npairs(p), p->d.absorbing[0], p->d.absorbing[1], (float)p->d.spacing[0],
+                 (float)p->d.spacing[1], (float)p->d.dt, adjoint ? 1 : 0, snap,
+                 snap_pair >= 0 ? snap_pair : p->snap_shot_stride, (float)(1.0 / (p->d.dt * p->d.dt)), s));
     n++;
     return SA_OK;
 }
 
-int pml_clear(const sa_plan* p, cudaStream_t s) {
-    if (p->pml) CK(cudaMemsetAsync(p->pml_aux, 0, 6 * 2 * (size_t)npairs(p) * p->shot_stride * sizeof(float), s));
+size_t pml_aux_bytes(const sa_plan* p) { return 6 * 2 * (size_t)npairs(p) * p->shot_stride * sizeof(float); }
+
+int pml_clear(const sa_plan* p, cudaStream_t s, float* aux = nullptr) {
+    if (p->pml) CK(cudaMemsetAsync(aux ? aux : p->pml_aux, 0, pml_aux_bytes(p), s));
     return SA_OK;
 }
 
@@ -601,6 +608,9 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
             float* slot = p->ckpt + (size_t)(t / p->ck_K - 1) * 2 * (fbytes / sizeof(float));
             CK(cudaMemcpyAsync(slot, p->field[0], fbytes, cudaMemcpyDeviceToDevice, s));
             CK(cudaMemcpyAsync(slot + fbytes / sizeof(float), p->field[1], fbytes, cudaMemcpyDeviceToDevice, s));
+            if (p->pml)  // the CFS-PML's auxiliary fields after step t
+                CK(cudaMemcpyAsync(p->pml_ck + (size_t)(t / p->ck_K - 1) * (pml_aux_bytes(p) / sizeof(float)),
+                                   p->pml_aux, pml_aux_bytes(p), cudaMemcpyDeviceToDevice, s));
         }
     }
     p->fwd_launches[mode] = n;
@@ -689,15 +699,20 @@ int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
     if (wav) CK(cudaMemsetAsync(p->wgrad, 0, (size_t)p->d.nt * p->n_src * sizeof(float), s));
     const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     long long n = 0;
+    CKR(pml_clear(p, s));  // the adjoint's own auxiliary fields
     for (int k = T0 >= 1 ? (T0 - 1) / K : -1; k >= 0; k--) {
         const int t_lo = k * K + 1, t_hi = std::min((k + 1) * K, T0);
         if (k == 0) {
             CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
             CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
+            CKR(pml_clear(p, s, p->pml_aux_f));
         } else {
             const float* slot = p->ckpt + (size_t)(k - 1) * 2 * ffloats;
             CK(cudaMemcpyAsync(p->field[0], slot, fbytes, cudaMemcpyDeviceToDevice, s));
             CK(cudaMemcpyAsync(p->field[1], slot + ffloats, fbytes, cudaMemcpyDeviceToDevice, s));
+            if (p->pml)
+                CK(cudaMemcpyAsync(p->pml_aux_f, p->pml_ck + (size_t)(k - 1) * (pml_aux_bytes(p) / sizeof(float)),
+                                   pml_aux_bytes(p), cudaMemcpyDeviceToDevice, s));
         }
         // the kernels address snapshot t/f; slot t/f - (kK/f + 1) of the segment buffer is meant
         const long long first = (long long)k * K / f + 1;
@@ -710,6 +725,8 @@ int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
             fa.prev = (t & 1) ? p->field[0] : p->field[1];
             CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, fa));
             n++;
+            CKR(pml_step(p, fa.cur, fa.prev, false, t % f == 0 ? base + 2 * (long long)(t / f) * p->snap_stride : nullptr,
+                         s, n, p->pml_aux_f, fa.snap_shot_stride));
             CKR(inject_sources(p, fa.prev, t, base, fa.snap_shot_stride, t % f == 0, s, n));
         }
         for (int t = t_hi; t >= t_lo; t--) {
@@ -719,6 +736,7 @@ int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
             aa.prev = even ? p->afield[0] : p->afield[1];
             CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, aa));
             n++;
+            CKR(pml_step(p, aa.cur, aa.prev, true, nullptr, s, n));
             CKR(inject_receivers(p, aa.prev, t, s, n));
             CKR(image_step(p, aa.cur, base, aa.snap_shot_stride, t, s, n));
             CKR(wavelet_gather(p, aa.cur, t, wav, s, n));
@@ -729,7 +747,9 @@ int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
 }
 
 int plan_checkpoints(sa_plan* p) {
-    return sa::choose_checkpoints(p->d, (double)npairs(p) * p->shot_stride * sizeof(float2), &p->ck_K, &p->ck_n);
+    // a checkpoint holds both levels and, with the CFS-PML, its six auxiliary fields (six more levels)
+    return sa::choose_checkpoints(p->d, (double)npairs(p) * p->shot_stride * sizeof(float2), &p->ck_K, &p->ck_n,
+                                  p->pml ? 8 : 2);
 }
 
 // Exact gradient of the discrete forward map (SA_GRAD_EXACT) from checkpoints. With z = C1 W mu
@@ -1023,7 +1043,7 @@ int sa_plan_destroy(sa_plan* p) {
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
                     p->ones_g, p->zeros_g, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
-                    p->dbx, p->dby, p->pml_prof, p->pml_aux,
+                    p->dbx, p->dby, p->pml_prof, p->pml_aux, p->pml_ck, p->pml_aux_f,
                     p->wgrad, p->hgat, p->hgat_src, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
                     p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx, p->xtgt.off, p->xtgt.point, p->xtgt.coef};
     for (void* b : bufs)
@@ -1141,8 +1161,6 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
     if (save_mode != SA_SAVE_NONE && save_mode != SA_SAVE_SNAPSHOTS && save_mode != SA_SAVE_CHECKPOINTS &&
         save_mode != SA_SAVE_RAW)
         return fail(SA_E_INVALID, "save_mode %d", save_mode);
-    if (p->pml && save_mode == SA_SAVE_CHECKPOINTS)
-        return fail(SA_E_UNSUPPORTED, "checkpoints are implemented for the sponge boundary");
     if (p->p3) return sa::plan3d_forward(p->p3, wavelets, traces, save_mode, (cudaStream_t)stream);
     if (!p->medium_set || !p->geometry_set) return fail(SA_E_INVALID, "medium and geometry must be set first");
     if ((p->n_src && !wavelets) || (p->n_rec && !traces)) return fail(SA_E_INVALID, "null wavelets or traces");
@@ -1159,9 +1177,14 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
         const int oldK = p->ck_K;
         CKR(plan_checkpoints(p));
         const size_t n = std::max<size_t>(1, (size_t)p->ck_n * 2 * npairs(p) * p->shot_stride * 2);
-        float* old = p->ckpt;
+        float *old = p->ckpt, *old_ck = p->pml_ck, *old_f = p->pml_aux_f;
         CKR(ensure(&p->ckpt, &p->cap_ckpt, n));
-        if (old != p->ckpt || oldK != p->ck_K) drop_graphs(p);
+        if (p->pml) {
+            const size_t na = pml_aux_bytes(p) / sizeof(float);
+            CKR(ensure(&p->pml_ck, &p->cap_pml_ck, std::max<size_t>(1, (size_t)p->ck_n * na)));
+            CKR(ensure(&p->pml_aux_f, &p->cap_pml_aux_f, na));
+        }
+        if (old != p->ckpt || old_ck != p->pml_ck || old_f != p->pml_aux_f || oldK != p->ck_K) drop_graphs(p);
         p->snaps_valid = false;
     }
     CKR(load_transposed(p, wavelets, p->n_src, p->d.nt, p->src_amp, s));
@@ -1213,6 +1236,8 @@ int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec
     const bool exact = grad_mode == SA_GRAD_EXACT;
     const bool wav = grad_wavelets != nullptr;
     if (wav && exact) return fail(SA_E_UNSUPPORTED, "the wavelet gradient is the parity mode's (src.interpolate(-p_a))");
+    if (exact && p->d.boundary != SA_BOUNDARY_SPONGE)
+        return fail(SA_E_UNSUPPORTED, "the exact gradient is implemented for the sponge boundary");
     if (p->p3) {
         if (!grad_vp || !prec_vp) return fail(SA_E_INVALID, "null outputs");
         if (exact) return sa::plan3d_adjoint_exact(p->p3, residuals, grad_vp, prec_vp, (cudaStream_t)stream);

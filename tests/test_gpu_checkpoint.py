@@ -1,8 +1,8 @@
 """Wavefield checkpointing (SA_SAVE_CHECKPOINTS): the adjoint that recomputes each segment's
 snapshots from stored checkpoints returns the same gradient and preconditioner, bit for bit,
 as the adjoint from the full undersampled wavefield, in 2D and 3D, for intervals that divide
-the adjoint's time range, that do not, that cover it in one segment, and for an interval
-chosen from a byte budget."""
+the adjoint's time range, that do not, that cover it in one segment, for an interval chosen
+from a byte budget, and with the CFS-PML (its auxiliary fields checkpointed with the levels)."""
 
 import numpy as np
 import pytest
@@ -79,6 +79,32 @@ def test_checkpointed_gradient_3d_bitwise(interval):
     tr0, g0, p0, resw = _gradient(c, make_plan3(c), True)
     assert np.abs(g0).max() > 0
     tr1, g1, p1, _ = _gradient(c, make_plan3(c, checkpoint_interval=interval), 'checkpoints', resw)
+    assert np.array_equal(tr0, tr1)
+    assert np.array_equal(g0, g1)
+    assert np.array_equal(p0, p1)
+
+
+@pytest.mark.parametrize('interval', [12, 40])
+def test_checkpointed_gradient_pml_2d_bitwise(interval):
+    c = C.small_case(kernel='OT2', density='variable', alpha=True, n_shots=3, uneven=True, nt=220, inner=40)
+    kw = dict(boundary='pml', f_centre=1.0e6)
+    tr0, g0, p0, resw = _gradient(c, C.make_plan(c, **kw), True)
+    assert np.abs(g0).max() > 0
+    plan = C.make_plan(c, checkpoint_interval=interval, **kw)
+    tr1, g1, p1, _ = _gradient(c, plan, 'checkpoints', resw)
+    assert np.array_equal(tr0, tr1)
+    assert np.array_equal(g0, g1)
+    assert np.array_equal(p0, p1)
+    _, g2, _, _ = _gradient(c, plan, 'checkpoints', resw)
+    assert np.array_equal(g0, g2)
+
+
+def test_checkpointed_gradient_pml_3d_bitwise():
+    c = case3d(kernel='OT2', density='variable', alpha=True, n_shots=2, nt=120)
+    kw = dict(boundary='pml', f_centre=1.0e6)
+    tr0, g0, p0, resw = _gradient(c, make_plan3(c, **kw), True)
+    assert np.abs(g0).max() > 0
+    tr1, g1, p1, _ = _gradient(c, make_plan3(c, checkpoint_interval=16, **kw), 'checkpoints', resw)
     assert np.array_equal(tr0, tr1)
     assert np.array_equal(g0, g1)
     assert np.array_equal(p0, p1)

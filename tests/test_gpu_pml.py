@@ -87,5 +87,9 @@ def test_pml_plan_limits():
     assert e.value.code == _lib.SA_E_UNSUPPORTED
     c = C.small_case(kernel='OT2', n_shots=1, nt=60, inner=32)
     plan = C.make_plan(c, boundary='pml', f_centre=F_CENTRE)
-    with pytest.raises(_lib.StrideAccError):
-        C.gpu_forward(c, plan=plan, save='checkpoints')
+    C.gpu_forward(c, plan=plan, save='checkpoints')
+    shape = c['vp'].shape
+    res = np.zeros((plan.n_rec, c['nt']), np.float32)
+    with pytest.raises(_lib.StrideAccError) as e:  # the exact adjoint holds no CFS-PML terms
+        plan.adjoint(res, np.zeros(shape, np.float32), np.zeros(shape, np.float32), exact=True)
+    assert e.value.code == _lib.SA_E_UNSUPPORTED
