@@ -165,8 +165,8 @@ class Plan:
     def __init__(self, dim, shape, spacing, extra, absorbing, dt, nt, kernel='OT4', density=SA_DENSITY_NONE,
                  attenuation=False, undersampling=4, max_shots=1, checkpoint_interval=0, checkpoint_budget=0.0,
                  interpolation='linear', boundary='sponge', f_centre=0.0):
-        """boundary: 'sponge' (SpongeBoundary2) or 'pml' (ComplexFrequencyShiftPML2, 2D OT2, with the
-        band centre f_centre in Hz)."""
+        """boundary: 'sponge' (SpongeBoundary2) or 'pml' (ComplexFrequencyShiftPML2, OT2, 2D and 3D, with
+        the band centre f_centre in Hz)."""
         lib = load()
         d = SaDesc()
         d.dim = dim

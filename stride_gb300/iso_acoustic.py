@@ -127,6 +127,12 @@ class IsoAcousticGB300(ProblemTypeBase):
     reference, which has no alpha gradient. Options the reference supports but this build does
     not (the CFS-PML with OT4, sinc interpolation, attenuation power 2) raise
     NotImplementedError; unknown values raise ValueError as in the reference.
+
+    Memory: ``checkpoint_interval=K`` (steps) or ``checkpoint_budget`` (bytes) keeps the wavefield
+    every K steps instead of every undersampled ``p.dt2`` and recomputes each segment in the
+    adjoint; the vp gradient is the same, bit for bit. This stands where the reference reduces
+    the saved wavefield with ``save_compression`` (devito.py:331-332), which is accepted and
+    ignored. The raw-wavefield path (wavelet or rho gradients) always saves snapshots.
     """
 
     space_order = 10
@@ -140,6 +146,8 @@ class IsoAcousticGB300(ProblemTypeBase):
         self.boundary_type = 'sponge_boundary_2'
         self.interpolation_type = 'linear'
         self.attenuation_power = 0
+        self.checkpoint_interval = 0
+        self.checkpoint_budget = 0.0
         self._bandwidth = (0., 0., 0.)
         self._plans = {}
         self._plan = None
@@ -171,6 +179,11 @@ class IsoAcousticGB300(ProblemTypeBase):
             if attenuation_power != 0:
                 raise NotImplementedError('attenuation_power %r is not implemented in this build' % attenuation_power)
         self.attenuation_power = attenuation_power
+        interval = kwargs.get('checkpoint_interval', 0) or 0
+        budget = kwargs.get('checkpoint_budget', 0.0) or 0.0
+        if int(interval) != interval or interval < 0 or budget < 0:
+            raise ValueError('checkpoint_interval must be a non-negative integer and checkpoint_budget >= 0')
+        self.checkpoint_interval, self.checkpoint_budget = int(interval), float(budget)
         if kwargs.get('drp', False):
             self.logger.warning('DRP weights are not implemented in this version of stride')
         self.drp = False
@@ -234,7 +247,8 @@ class IsoAcousticGB300(ProblemTypeBase):
         space, time = self.space, self.time
         key = (space.extended_shape, space.spacing, space.extra, space.absorbing, time.step, time.extended_num,
                self.kernel, self._density_mode(rho), alpha is not None, self.undersampling_factor, n_shots,
-               self.interpolation_type, self.boundary_type, float(self._bandwidth[1]))
+               self.interpolation_type, self.boundary_type, float(self._bandwidth[1]), self.checkpoint_interval,
+               self.checkpoint_budget)
         plan = self._plans.get(key)
         if plan is None:
             plan = _lib.Plan(space.dim, space.extended_shape, space.spacing, space.extra, space.absorbing,
@@ -242,7 +256,8 @@ class IsoAcousticGB300(ProblemTypeBase):
                              attenuation=alpha is not None, undersampling=self.undersampling_factor,
                              max_shots=n_shots, interpolation=self.interpolation_type,
                              boundary='pml' if self.boundary_type == 'complex_frequency_shift_PML_2' else 'sponge',
-                             f_centre=float(self._bandwidth[1]))
+                             f_centre=float(self._bandwidth[1]), checkpoint_interval=self.checkpoint_interval,
+                             checkpoint_budget=self.checkpoint_budget)
             self._plans = {key: plan}  # one live plan: the previous one's device memory is released
         self._plan = plan
         return plan
@@ -272,15 +287,17 @@ class IsoAcousticGB300(ProblemTypeBase):
             data = np.gradient(data, self.time.step, axis=-1) * self.time.step
         return np.ascontiguousarray((data * self._window()[None, :]).astype(np.float32))
 
-    @staticmethod
-    def _save_wavefield(vp, rho, alpha, kwargs, wavelets=None):
-        """False, 'snapshots' (p.dt2 every f steps) or 'raw' (p itself, which the reference
-        saves when the wavelets, rho or alpha need a gradient, devito.py:319,410-413)."""
+    def _save_wavefield(self, vp, rho, alpha, kwargs, wavelets=None):
+        """False, 'snapshots' (p.dt2 every f steps), 'checkpoints' (both levels every K steps,
+        with a checkpoint interval or budget) or 'raw' (p itself, which the reference saves when
+        the wavelets, rho or alpha need a gradient, devito.py:319,410-413)."""
         raw = any(v is not None and getattr(v, 'needs_grad', False) for v in (wavelets, rho, alpha))
         save = kwargs.get('save_wavefield', False) or bool(getattr(vp, 'needs_grad', False)) or raw
         if not save:
             return False
-        return 'raw' if raw else 'snapshots'
+        if raw:
+            return 'raw'
+        return 'checkpoints' if self.checkpoint_interval > 0 or self.checkpoint_budget > 0 else 'snapshots'
 
     # ---------------------------------------------------------------------------- forward
 

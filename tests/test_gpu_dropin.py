@@ -149,6 +149,24 @@ def test_pde_cfs_pml():
     assert C.rel_l2(traces.data, ref) <= 1e-4
 
 
+def test_pde_checkpointed_gradient_is_bitwise_equal():
+    """checkpoint_interval / checkpoint_budget: the adjoint recomputes segments from checkpoints
+    and returns the snapshot path's vp gradient bit for bit."""
+    space, time, vp, rho, al, shot, sub, geo, w = _setup(True, True)
+    out = []
+    for kw in (dict(), dict(checkpoint_interval=24), dict(checkpoint_budget=2e9)):
+        pde = iso_acoustic.IsoAcousticGB300(space=space, time=time)
+        traces = pde(shot.wavelets, vp, rho=rho, alpha=al, problem=sub, **kw)
+        assert pde._saved == ('checkpoints' if kw else 'snapshots')
+        residual = shot.observed.alike(name='residual', data=traces.data * np.float32(0.7))
+        g = pde.adjoint(residual, shot.wavelets, vp, rho, al, problem=sub, **kw)[1]
+        out.append((traces.data.copy(), g.extended_data.copy(), g.prec.extended_data.copy()))
+    assert np.abs(out[0][1]).max() > 0
+    for o in out[1:]:
+        for a, b in zip(out[0], o):
+            assert np.array_equal(a, b)
+
+
 def test_pde_3d_forward_and_gradient():
     """The drop-in on a 3D problem: pde(...) traces and the adjoint's vp gradient against the C
     oracle (3D extended grid, variable density and attenuation)."""

@@ -35,6 +35,9 @@ def test_kernel_selection_matches_reference_rule():
     (dict(interpolation_type='cubic'), ValueError),
     (dict(interpolation_type='sinc'), NotImplementedError),
     (dict(kernel='OT6'), ValueError),
+    (dict(checkpoint_interval=-4), ValueError),
+    (dict(checkpoint_interval=2.5), ValueError),
+    (dict(checkpoint_budget=-1.0), ValueError),
 ])
 def test_option_errors(kw, exc):
     pde, shot, sub, vp, grid = _setup()
