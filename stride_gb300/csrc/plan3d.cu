@@ -70,12 +70,18 @@ void ramp(int A, double h, double refl, float* out) {
 }  // namespace
 
 // The requested interval (50 by default), unless the checkpoints (ck_levels levels each) and one
-// segment's snapshots exceed the byte budget; then the multiple of f nearest to it that fits.
-int choose_checkpoints(const sa_desc& d, double level, int* K_out, int* n_out, double ck_levels) {
+// segment's snapshots exceed the byte budget; then the multiple of f nearest to it that fits. When
+// no one-level interval fits, two levels (*K2_out > 0): the forward keeps coarse checkpoints every
+// K steps, and the adjoint re-runs each coarse segment once to place fine checkpoints every K2
+// steps in it (K a multiple of K2), then each fine segment once more for its snapshots. Every
+// step is then recomputed at most twice; memory is (nt-2)/K + K/K2 - 1 checkpoints and K2/f
+// snapshots. Of the pairs that fit, the largest K2 (fewest restores), then the least memory.
+int choose_checkpoints(const sa_desc& d, double level, int* K_out, int* n_out, double ck_levels, int* K2_out) {
     const int f = d.undersampling;
     const int T0 = d.nt - 1 - f;
     int K = d.checkpoint_interval > 0 ? d.checkpoint_interval : 50;
     K = (K + f - 1) / f * f;
+    int K2 = 0;
     // checkpoints after steps K, 2K, .. <= nt-2 (the exact adjoint's segments reach that far) and
     // one segment's K/f snapshots
     auto bytes = [&](int k) { return ((d.nt - 2) / k) * ck_levels * level + (k / f) * level; };
@@ -87,15 +93,33 @@ int choose_checkpoints(const sa_desc& d, double level, int* K_out, int* n_out, d
             if (bytes(k) <= d.checkpoint_budget && (best < 0 || std::abs(k - K) < std::abs(best - K))) best = k;
         }
         if (best < 0) {
-            char b[256];
-            snprintf(b, sizeof(b), "no checkpoint interval fits %.0f bytes (at least %.0f needed)",
-                     d.checkpoint_budget, least);
-            return fail3(SA_E_NOMEM, b);
+            auto bytes2 = [&](int k1, int k2) {
+                return ((d.nt - 2) / k1) * ck_levels * level + (k1 / k2 - 1) * ck_levels * level + (k2 / f) * level;
+            };
+            int b1 = -1, b2 = -1;
+            for (int k2 = f; k2 <= std::max(f, T0); k2 += f)
+                for (int k1 = 2 * k2; k1 <= std::max(2 * k2, T0 + k2 - 1); k1 += k2) {
+                    const double b = bytes2(k1, k2);
+                    least = std::min(least, b);
+                    if (b <= d.checkpoint_budget && (k2 > b2 || (k2 == b2 && b < bytes2(b1, b2)))) {
+                        b1 = k1;
+                        b2 = k2;
+                    }
+                }
+            if (b1 < 0) {
+                char b[256];
+                snprintf(b, sizeof(b), "no checkpoint schedule fits %.0f bytes (at least %.0f needed)",
+                         d.checkpoint_budget, least);
+                return fail3(SA_E_NOMEM, b);
+            }
+            best = b1;
+            K2 = b2;
         }
         K = best;
     }
     *K_out = K;
     *n_out = (d.nt - 2) / K;
+    if (K2_out) *K2_out = K2;
     return SA_OK;
 }
 
@@ -127,6 +151,10 @@ struct Plan3D {
     float *ckpt = nullptr, *segsnaps = nullptr, *A[2] = {nullptr, nullptr};
     size_t cap_ckpt = 0, cap_segsnaps = 0;
     int ck_K = 0, ck_n = 0;
+    // two-level schedule (ck_K2 > 0): fine checkpoints every ck_K2 steps of one coarse segment
+    int ck_K2 = 0;
+    float *ckpt2 = nullptr, *pml_ck2 = nullptr;
+    size_t cap_ckpt2 = 0, cap_pml_ck2 = 0;
     bool ckpt_valid = false;
     float *gradb = nullptr, *precb = nullptr;
     // raw snapshots (SA_SAVE_RAW): held vp/rho terms per shot, rho accumulators, D-b per axis
@@ -228,7 +256,7 @@ void plan3d_destroy(Plan3D* p) {
                    p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps, p->A[0], p->A[1], p->hold_vp, p->hold_rho,
                    p->gradrb, p->precrb, p->db[0], p->db[1], p->db[2], p->wgrad, p->EA, p->EB, p->EC, p->EG4,
                    p->ES, p->levels, p->Lu, p->Lz, p->ones, p->zeros, p->r_xcoef, p->e_coef[0], p->e_coef[1],
-                   p->pml_prof, p->pml_aux, p->pml_ck, p->pml_aux_f, p->e_w[0], p->e_w[1], p->e_xcoef};
+                   p->pml_prof, p->pml_aux, p->pml_ck, p->pml_aux_f, p->ckpt2, p->pml_ck2, p->e_w[0], p->e_w[1], p->e_xcoef};
     for (float* b : fb)
         if (b) cudaFree(b);
     void* vb[] = {p->e_shot[0], p->e_shot[1], p->e_point[0], p->e_point[1], p->e_idx[0], p->e_idx[1], p->hgat,
@@ -563,7 +591,8 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
     const size_t level = (size_t)p->n_shots * p->field;  // floats of one level of every shot
     if (ckpt) {
         // a checkpoint holds both levels and, with the CFS-PML, its nine auxiliary fields
-        int rc = choose_checkpoints(p->d, (double)level * sizeof(float), &p->ck_K, &p->ck_n, p->pml ? 11 : 2);
+        int rc = choose_checkpoints(p->d, (double)level * sizeof(float), &p->ck_K, &p->ck_n, p->pml ? 11 : 2,
+                                    &p->ck_K2);
         if (rc != SA_OK) return rc;
         const size_t need = std::max<size_t>(1, (size_t)p->ck_n * 2 * level);
         if (need > p->cap_ckpt) {
@@ -661,49 +690,83 @@ static int wavelet_level(Plan3D* p, const float* q, int t, bool wav, cudaStream_
     return SA_OK;
 }
 
+// Checkpointed imaging condition: coarse segments from last to first; with two levels (ck_K2 > 0)
+// each coarse segment is first re-run without snapshots to place fine checkpoints, then each fine
+// segment restores its start, re-runs its forward steps with p.dt2 saved, and runs the adjoint
+// back through it (the 2D plan's issue_adjoint_ckpt does the same).
 static int adjoint_segments(Plan3D* p, Step3D& aa, const Sparse3D& rec, bool wav, cudaStream_t s, long long& n) {
     const size_t level = (size_t)p->n_shots * p->field;
     const size_t lb = level * sizeof(float);
     const int f = p->d.undersampling, K = p->ck_K;
+    const int K2 = p->ck_K2 > 0 ? p->ck_K2 : K;  // fine interval (one level: the coarse one)
     const int T0 = p->d.nt - 1 - f;
     CK3(cudaMemsetAsync(p->A[0], 0, lb, s));
     CK3(cudaMemsetAsync(p->A[1], 0, lb, s));
     Step3D fa = args3(p);
     fa.save = 1;
-    fa.snap_shot_stride = aa.snap_shot_stride = (long long)(K / f) * p->snap_stride;
-    for (int k = T0 >= 1 ? (T0 - 1) / K : -1; k >= 0; k--) {
-        const int t_lo = k * K + 1, t_hi = std::min((k + 1) * K, T0);
-        if (k == 0) {
+    fa.snap_shot_stride = aa.snap_shot_stride = (long long)(K2 / f) * p->snap_stride;
+    Step3D fr = args3(p);  // the recompute that places fine checkpoints saves nothing
+    fr.save = 0;
+    // forward state <- coarse checkpoint k (fine < 0) or fine checkpoint `fine`; zero for coarse 0
+    auto restore = [&](int k, int fine) -> int {
+        if (fine < 0 && k == 0) {
             CK3(cudaMemsetAsync(p->F[0], 0, lb, s));
             CK3(cudaMemsetAsync(p->F[1], 0, lb, s));
             if (p->pml) CK3(cudaMemsetAsync(p->pml_aux_f, 0, 9 * lb, s));
-        } else {
-            const float* slot = p->ckpt + (size_t)(k - 1) * 2 * level;
-            CK3(cudaMemcpyAsync(p->F[0], slot, lb, cudaMemcpyDeviceToDevice, s));
-            CK3(cudaMemcpyAsync(p->F[1], slot + level, lb, cudaMemcpyDeviceToDevice, s));
-            if (p->pml)
-                CK3(cudaMemcpyAsync(p->pml_aux_f, p->pml_ck + (size_t)(k - 1) * 9 * level, 9 * lb,
-                                    cudaMemcpyDeviceToDevice, s));
+            return SA_OK;
         }
-        // the kernels address snapshot t/f; slot t/f - (kK/f + 1) of the segment buffer is meant
-        const long long first = (long long)k * K / f + 1;
-        float* base = reinterpret_cast<float*>(reinterpret_cast<uintptr_t>(p->segsnaps) -
-                                               (uintptr_t)(first * p->snap_stride * (long long)sizeof(float)));
-        fa.snaps = aa.snaps = base;
-        for (int t = t_lo; t <= t_hi; t++) {
-            fa.t = t;
-            int rc = step3(p, fa, (t & 1) ? p->F[1] : p->F[0], (t & 1) ? p->F[0] : p->F[1], 0,
-                           p->src_amp, t % f == 0, s, n, p->pml_aux_f);
-            if (rc != SA_OK) return rc;
+        const float* lv = fine < 0 ? p->ckpt + (size_t)(k - 1) * 2 * level : p->ckpt2 + (size_t)fine * 2 * level;
+        CK3(cudaMemcpyAsync(p->F[0], lv, lb, cudaMemcpyDeviceToDevice, s));
+        CK3(cudaMemcpyAsync(p->F[1], lv + level, lb, cudaMemcpyDeviceToDevice, s));
+        if (p->pml) {
+            const float* ax = fine < 0 ? p->pml_ck + (size_t)(k - 1) * 9 * level : p->pml_ck2 + (size_t)fine * 9 * level;
+            CK3(cudaMemcpyAsync(p->pml_aux_f, ax, 9 * lb, cudaMemcpyDeviceToDevice, s));
         }
-        for (int t = t_hi; t >= t_lo; t--) {
-            aa.t = t;
-            const bool even = ((T0 - t) & 1) == 0;
-            int rc = step3(p, aa, even ? p->A[1] : p->A[0], even ? p->A[0] : p->A[1], 1, p->rec_amp,
-                           false, s, n);
-            if (rc != SA_OK) return rc;
-            if ((rc = image_level(p, aa, even ? p->A[1] : p->A[0], s, n)) != SA_OK) return rc;
-            if ((rc = wavelet_level(p, even ? p->A[1] : p->A[0], t, wav, s, n)) != SA_OK) return rc;
+        return SA_OK;
+    };
+    for (int k = T0 >= 1 ? (T0 - 1) / K : -1; k >= 0; k--) {
+        const int c0 = k * K, c_hi = std::min((k + 1) * K, T0);
+        const int nf = (c_hi - c0 + K2 - 1) / K2;  // fine segments
+        int rc = SA_OK;
+        if (nf > 1) {  // fine checkpoints j = 1 .. nf-1 into slots j-1
+            if ((rc = restore(k, -1)) != SA_OK) return rc;
+            for (int t = c0 + 1; t <= c0 + (nf - 1) * K2; t++) {
+                fr.t = t;
+                rc = step3(p, fr, (t & 1) ? p->F[1] : p->F[0], (t & 1) ? p->F[0] : p->F[1], 0, p->src_amp, false, s,
+                           n, p->pml_aux_f);
+                if (rc != SA_OK) return rc;
+                if ((t - c0) % K2 == 0) {
+                    const size_t j = (size_t)((t - c0) / K2 - 1);
+                    CK3(cudaMemcpyAsync(p->ckpt2 + j * 2 * level, p->F[0], lb, cudaMemcpyDeviceToDevice, s));
+                    CK3(cudaMemcpyAsync(p->ckpt2 + j * 2 * level + level, p->F[1], lb, cudaMemcpyDeviceToDevice, s));
+                    if (p->pml)
+                        CK3(cudaMemcpyAsync(p->pml_ck2 + j * 9 * level, p->pml_aux_f, 9 * lb, cudaMemcpyDeviceToDevice,
+                                            s));
+                }
+            }
+        }
+        for (int j = nf - 1; j >= 0; j--) {
+            const int t_lo = c0 + j * K2 + 1, t_hi = std::min(c0 + (j + 1) * K2, c_hi);
+            if ((rc = restore(k, j - 1)) != SA_OK) return rc;
+            // the kernels address snapshot t/f; slot t/f - ((c0 + jK2)/f + 1) of the segment buffer is meant
+            const long long first = (long long)(c0 + j * K2) / f + 1;
+            float* base = reinterpret_cast<float*>(reinterpret_cast<uintptr_t>(p->segsnaps) -
+                                                   (uintptr_t)(first * p->snap_stride * (long long)sizeof(float)));
+            fa.snaps = aa.snaps = base;
+            for (int t = t_lo; t <= t_hi; t++) {
+                fa.t = t;
+                rc = step3(p, fa, (t & 1) ? p->F[1] : p->F[0], (t & 1) ? p->F[0] : p->F[1], 0, p->src_amp, t % f == 0,
+                           s, n, p->pml_aux_f);
+                if (rc != SA_OK) return rc;
+            }
+            for (int t = t_hi; t >= t_lo; t--) {
+                aa.t = t;
+                const bool even = ((T0 - t) & 1) == 0;
+                rc = step3(p, aa, even ? p->A[1] : p->A[0], even ? p->A[0] : p->A[1], 1, p->rec_amp, false, s, n);
+                if (rc != SA_OK) return rc;
+                if ((rc = image_level(p, aa, even ? p->A[1] : p->A[0], s, n)) != SA_OK) return rc;
+                if ((rc = wavelet_level(p, even ? p->A[1] : p->A[0], t, wav, s, n)) != SA_OK) return rc;
+            }
         }
     }
     return SA_OK;
@@ -741,10 +804,24 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
         const size_t level = (size_t)std::max(1, p->d.max_shots) * p->field;
         for (int k = 0; k < 2; k++)
             if (!p->A[k] && (rc = alloc3(&p->A[k], level)) != SA_OK) return rc;
-        const size_t need = (size_t)(p->ck_K / p->d.undersampling) * p->n_shots * p->field;
+        const int K2 = p->ck_K2 > 0 ? p->ck_K2 : p->ck_K;
+        const size_t need = (size_t)(K2 / p->d.undersampling) * p->n_shots * p->field;
         if (need > p->cap_segsnaps) {
             if ((rc = alloc3(&p->segsnaps, need)) != SA_OK) return rc;
             p->cap_segsnaps = need;
+        }
+        if (p->ck_K2 > 0) {  // fine checkpoints of one coarse segment
+            const size_t nf = (size_t)std::max(1, p->ck_K / p->ck_K2 - 1);
+            const size_t need2 = nf * 2 * (size_t)p->n_shots * p->field;
+            if (need2 > p->cap_ckpt2) {
+                if ((rc = alloc3(&p->ckpt2, need2)) != SA_OK) return rc;
+                p->cap_ckpt2 = need2;
+            }
+            const size_t need_pml = nf * 9 * (size_t)p->n_shots * p->field;
+            if (p->pml && need_pml > p->cap_pml_ck2) {
+                if ((rc = alloc3(&p->pml_ck2, need_pml)) != SA_OK) return rc;
+                p->cap_pml_ck2 = need_pml;
+            }
         }
     }
     if (!p->gradb && (rc = alloc3(&p->gradb, fl)) != SA_OK) return rc;
@@ -833,6 +910,8 @@ namespace sa {
 int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s) {
     if (!p->ckpt_valid)
         return fail3(SA_E_INVALID, "SA_GRAD_EXACT needs a prior sa_forward with SA_SAVE_CHECKPOINTS");
+    if (p->ck_K2 > 0)
+        return fail3(SA_E_NOMEM, "SA_GRAD_EXACT needs a one-level checkpoint schedule: checkpoint_budget is too small");
     const int nt = p->d.nt, K = p->ck_K;
     const size_t fl = (size_t)std::max(1, p->d.max_shots) * p->field;  // floats of one level (capacity)
     const size_t level = (size_t)p->n_shots * p->field;                  // floats of one level (in use)

@@ -22,5 +22,6 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
 long long plan3d_launches(const Plan3D* p);
 // Checkpoint interval K (a multiple of f) and the number of stored checkpoints for a plan whose
 // two state levels take `level_bytes` (SA_SAVE_CHECKPOINTS, both dimensions).
-int choose_checkpoints(const sa_desc& d, double level_bytes, int* K, int* n_ckpt, double ck_levels = 2);
+int choose_checkpoints(const sa_desc& d, double level_bytes, int* K, int* n_ckpt, double ck_levels = 2,
+                       int* K2 = nullptr);
 }  // namespace sa

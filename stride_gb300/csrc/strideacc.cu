@@ -150,6 +150,11 @@ struct sa_plan {
     float *ckpt = nullptr, *segsnaps = nullptr, *afield[2] = {nullptr, nullptr};
     size_t cap_ckpt = 0, cap_segsnaps = 0, afield_cap[2] = {0, 0};
     int ck_K = 0, ck_n = 0;
+    // two-level schedule (ck_K2 > 0): fine checkpoints every ck_K2 steps of one coarse segment,
+    // placed by the adjoint's recompute (levels, and the CFS-PML's auxiliary fields)
+    int ck_K2 = 0;
+    float *ckpt2 = nullptr, *pml_ck2 = nullptr;
+    size_t cap_ckpt2 = 0, cap_pml_ck2 = 0;
     bool ckpt_valid = false;
     // exact-gradient mode: per-point derivative coefficients, every level of a segment, the
     // W G(.) of a forward and an adjoint level, unit/zero update coefficients (guarded), the
@@ -674,25 +679,31 @@ int issue_adjoint(sa_plan* p, bool wav, bool raw, bool rho, cudaStream_t s) {
 }
 
 // Reverse-time adjoint from checkpoints: the same steps and gradient as issue_adjoint, with
-// the snapshots recomputed per segment. Segment k covers t = kK+1 .. min((k+1)K, T0); from
-// last to first, its start state (checkpoint k, zero for k = 0) is restored, the forward
-// steps of the segment are re-run with p.dt2 saved into a segment buffer of K/f slots, and
-// the adjoint steps run back through the segment on their own two levels. The recomputed
-// steps are the forward's own launches (no receiver gather), so the snapshots are bitwise
-// the ones SA_SAVE_SNAPSHOTS stores.
+// the snapshots recomputed per segment. Coarse segment k covers t = kK+1 .. min((k+1)K, T0);
+// from last to first, its start state (checkpoint k, zero for k = 0) is restored. With two
+// levels (ck_K2 > 0) the coarse segment's forward steps are first re-run without snapshots to
+// place fine checkpoints after steps kK + jK2. Each fine segment (the whole coarse one with one
+// level), last to first, then restores its start state, re-runs its forward steps with p.dt2
+// saved into a segment buffer of K2/f slots, and runs the adjoint steps back through it on
+// their own two levels. The recomputed steps are the forward's own launches (no receiver
+// gather), so the snapshots are bitwise the ones SA_SAVE_SNAPSHOTS stores.
 int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
     const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
     const size_t ffloats = fbytes / sizeof(float);
     const size_t gbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float);
+    const size_t abytes = p->pml ? pml_aux_bytes(p) : 0, afloats = abytes / sizeof(float);
     CK(cudaMemsetAsync(p->afield[0], 0, fbytes, s));
     CK(cudaMemsetAsync(p->afield[1], 0, fbytes, s));
     CK(cudaMemsetAsync(p->gradb, 0, gbytes, s));
     CK(cudaMemsetAsync(p->precb, 0, gbytes, s));
     const int f = p->d.undersampling, K = p->ck_K;
+    const int K2 = p->ck_K2 > 0 ? p->ck_K2 : K;  // fine interval (one level: the coarse one)
     const int T0 = p->d.nt - 1 - f;
     sa::Step2D fa = base_args(p);  // sources are injected by inject_targets2d after the step
     fa.save = 1;
-    fa.snap_shot_stride = (long long)(K / f) * p->shot_stride;
+    fa.snap_shot_stride = (long long)(K2 / f) * p->shot_stride;
+    sa::Step2D fr = base_args(p);  // the recompute that places fine checkpoints saves nothing
+    fr.save = 0;
     sa::Step2D aa = base_args(p);  // receivers are injected by inject_targets2d after the step
     aa.save = 0;
     aa.snap_shot_stride = fa.snap_shot_stride;
@@ -700,46 +711,72 @@ int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
     const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     long long n = 0;
     CKR(pml_clear(p, s));  // the adjoint's own auxiliary fields
-    for (int k = T0 >= 1 ? (T0 - 1) / K : -1; k >= 0; k--) {
-        const int t_lo = k * K + 1, t_hi = std::min((k + 1) * K, T0);
-        if (k == 0) {
+    // forward state <- coarse checkpoint k (fine < 0) or fine checkpoint `fine`; zero for coarse 0
+    auto restore = [&](int k, int fine) -> int {
+        if (fine < 0 && k == 0) {
             CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
             CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
-            CKR(pml_clear(p, s, p->pml_aux_f));
-        } else {
-            const float* slot = p->ckpt + (size_t)(k - 1) * 2 * ffloats;
-            CK(cudaMemcpyAsync(p->field[0], slot, fbytes, cudaMemcpyDeviceToDevice, s));
-            CK(cudaMemcpyAsync(p->field[1], slot + ffloats, fbytes, cudaMemcpyDeviceToDevice, s));
-            if (p->pml)
-                CK(cudaMemcpyAsync(p->pml_aux_f, p->pml_ck + (size_t)(k - 1) * (pml_aux_bytes(p) / sizeof(float)),
-                                   pml_aux_bytes(p), cudaMemcpyDeviceToDevice, s));
+            return pml_clear(p, s, p->pml_aux_f);
         }
-        // the kernels address snapshot t/f; slot t/f - (kK/f + 1) of the segment buffer is meant
-        const long long first = (long long)k * K / f + 1;
-        float* base = reinterpret_cast<float*>(reinterpret_cast<uintptr_t>(p->segsnaps) -
-                                               (uintptr_t)(first * p->shot_stride * (long long)sizeof(float2)));
-        fa.snaps = aa.snaps = base;
-        for (int t = t_lo; t <= t_hi; t++) {
-            fa.t = t;
-            fa.cur = (t & 1) ? p->field[1] : p->field[0];
-            fa.prev = (t & 1) ? p->field[0] : p->field[1];
-            CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, fa));
-            n++;
-            CKR(pml_step(p, fa.cur, fa.prev, false, t % f == 0 ? base + 2 * (long long)(t / f) * p->snap_stride : nullptr,
-                         s, n, p->pml_aux_f, fa.snap_shot_stride));
-            CKR(inject_sources(p, fa.prev, t, base, fa.snap_shot_stride, t % f == 0, s, n));
+        const float* lv = fine < 0 ? p->ckpt + (size_t)(k - 1) * 2 * ffloats : p->ckpt2 + (size_t)fine * 2 * ffloats;
+        CK(cudaMemcpyAsync(p->field[0], lv, fbytes, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(p->field[1], lv + ffloats, fbytes, cudaMemcpyDeviceToDevice, s));
+        if (p->pml) {
+            const float* ax = fine < 0 ? p->pml_ck + (size_t)(k - 1) * afloats : p->pml_ck2 + (size_t)fine * afloats;
+            CK(cudaMemcpyAsync(p->pml_aux_f, ax, abytes, cudaMemcpyDeviceToDevice, s));
         }
-        for (int t = t_hi; t >= t_lo; t--) {
-            aa.t = t;
-            const bool even = ((T0 - t) & 1) == 0;
-            aa.cur = even ? p->afield[1] : p->afield[0];
-            aa.prev = even ? p->afield[0] : p->afield[1];
-            CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, aa));
-            n++;
-            CKR(pml_step(p, aa.cur, aa.prev, true, nullptr, s, n));
-            CKR(inject_receivers(p, aa.prev, t, s, n));
-            CKR(image_step(p, aa.cur, base, aa.snap_shot_stride, t, s, n));
-            CKR(wavelet_gather(p, aa.cur, t, wav, s, n));
+        return SA_OK;
+    };
+    auto forward_step = [&](sa::Step2D& a, int t, float* base) -> int {
+        const bool save_now = base != nullptr && t % f == 0;
+        a.t = t;
+        a.cur = (t & 1) ? p->field[1] : p->field[0];
+        a.prev = (t & 1) ? p->field[0] : p->field[1];
+        CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, a));
+        n++;
+        CKR(pml_step(p, a.cur, a.prev, false, save_now ? base + 2 * (long long)(t / f) * p->snap_stride : nullptr, s,
+                     n, p->pml_aux_f, fa.snap_shot_stride));
+        return inject_sources(p, a.prev, t, base, fa.snap_shot_stride, save_now, s, n);
+    };
+    for (int k = T0 >= 1 ? (T0 - 1) / K : -1; k >= 0; k--) {
+        const int c0 = k * K, c_hi = std::min((k + 1) * K, T0);
+        const int nf = (c_hi - c0 + K2 - 1) / K2;  // fine segments
+        if (nf > 1) {  // fine checkpoints j = 1 .. nf-1 into slots j-1
+            CKR(restore(k, -1));
+            for (int t = c0 + 1; t <= c0 + (nf - 1) * K2; t++) {
+                CKR(forward_step(fr, t, nullptr));
+                if ((t - c0) % K2 == 0) {
+                    const size_t j = (size_t)((t - c0) / K2 - 1);
+                    CK(cudaMemcpyAsync(p->ckpt2 + j * 2 * ffloats, p->field[0], fbytes, cudaMemcpyDeviceToDevice, s));
+                    CK(cudaMemcpyAsync(p->ckpt2 + j * 2 * ffloats + ffloats, p->field[1], fbytes,
+                                       cudaMemcpyDeviceToDevice, s));
+                    if (p->pml)
+                        CK(cudaMemcpyAsync(p->pml_ck2 + j * afloats, p->pml_aux_f, abytes, cudaMemcpyDeviceToDevice,
+                                           s));
+                }
+            }
+        }
+        for (int j = nf - 1; j >= 0; j--) {
+            const int t_lo = c0 + j * K2 + 1, t_hi = std::min(c0 + (j + 1) * K2, c_hi);
+            CKR(restore(k, j - 1));
+            // the kernels address snapshot t/f; slot t/f - ((c0 + jK2)/f + 1) of the segment buffer is meant
+            const long long first = (long long)(c0 + j * K2) / f + 1;
+            float* base = reinterpret_cast<float*>(reinterpret_cast<uintptr_t>(p->segsnaps) -
+                                                   (uintptr_t)(first * p->shot_stride * (long long)sizeof(float2)));
+            fa.snaps = aa.snaps = base;
+            for (int t = t_lo; t <= t_hi; t++) CKR(forward_step(fa, t, base));
+            for (int t = t_hi; t >= t_lo; t--) {
+                aa.t = t;
+                const bool even = ((T0 - t) & 1) == 0;
+                aa.cur = even ? p->afield[1] : p->afield[0];
+                aa.prev = even ? p->afield[0] : p->afield[1];
+                CK(sa::launch_step2d(p->kind, p->ot4, p->NT, grid, s, aa));
+                n++;
+                CKR(pml_step(p, aa.cur, aa.prev, true, nullptr, s, n));
+                CKR(inject_receivers(p, aa.prev, t, s, n));
+                CKR(image_step(p, aa.cur, base, aa.snap_shot_stride, t, s, n));
+                CKR(wavelet_gather(p, aa.cur, t, wav, s, n));
+            }
         }
     }
     p->adj_launches[1] = n;
@@ -749,7 +786,7 @@ int issue_adjoint_ckpt(sa_plan* p, bool wav, cudaStream_t s) {
 int plan_checkpoints(sa_plan* p) {
     // a checkpoint holds both levels and, with the CFS-PML, its six auxiliary fields (six more levels)
     return sa::choose_checkpoints(p->d, (double)npairs(p) * p->shot_stride * sizeof(float2), &p->ck_K, &p->ck_n,
-                                  p->pml ? 8 : 2);
+                                  p->pml ? 8 : 2, &p->ck_K2);
 }
 
 // Exact gradient of the discrete forward map (SA_GRAD_EXACT) from checkpoints. With z = C1 W mu
@@ -1043,7 +1080,7 @@ int sa_plan_destroy(sa_plan* p) {
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
                     p->ones_g, p->zeros_g, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
-                    p->dbx, p->dby, p->pml_prof, p->pml_aux, p->pml_ck, p->pml_aux_f,
+                    p->dbx, p->dby, p->pml_prof, p->pml_aux, p->pml_ck, p->pml_aux_f, p->ckpt2, p->pml_ck2,
                     p->wgrad, p->hgat, p->hgat_src, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
                     p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx, p->xtgt.off, p->xtgt.point, p->xtgt.coef};
     for (void* b : bufs)
@@ -1174,7 +1211,7 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
         if (old != p->snaps) drop_graphs(p);
         // every slot the adjoint reads (t % f == 0, f <= t <= nt-1-f) is written by this forward
     } else if (save_mode == SA_SAVE_CHECKPOINTS) {
-        const int oldK = p->ck_K;
+        const int oldK = p->ck_K, oldK2 = p->ck_K2;
         CKR(plan_checkpoints(p));
         const size_t n = std::max<size_t>(1, (size_t)p->ck_n * 2 * npairs(p) * p->shot_stride * 2);
         float *old = p->ckpt, *old_ck = p->pml_ck, *old_f = p->pml_aux_f;
@@ -1184,7 +1221,8 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
             CKR(ensure(&p->pml_ck, &p->cap_pml_ck, std::max<size_t>(1, (size_t)p->ck_n * na)));
             CKR(ensure(&p->pml_aux_f, &p->cap_pml_aux_f, na));
         }
-        if (old != p->ckpt || old_ck != p->pml_ck || old_f != p->pml_aux_f || oldK != p->ck_K) drop_graphs(p);
+        if (old != p->ckpt || old_ck != p->pml_ck || old_f != p->pml_aux_f || oldK != p->ck_K || oldK2 != p->ck_K2)
+            drop_graphs(p);
         p->snaps_valid = false;
     }
     CKR(load_transposed(p, wavelets, p->n_src, p->d.nt, p->src_amp, s));
@@ -1248,6 +1286,8 @@ int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec
     const bool raw = !ck && p->snaps_valid && p->snaps_raw;  // imaging from raw snapshots
     const bool rho = grad_rho != nullptr;
     if (exact && !ck) return fail(SA_E_INVALID, "SA_GRAD_EXACT needs a prior sa_forward with SA_SAVE_CHECKPOINTS");
+    if (exact && p->ck_K2 > 0)
+        return fail(SA_E_NOMEM, "SA_GRAD_EXACT needs a one-level checkpoint schedule: checkpoint_budget is too small");
     if (!p->snaps_valid && !ck)
         return fail(SA_E_INVALID, "sa_adjoint needs a prior sa_forward with SA_SAVE_SNAPSHOTS or SA_SAVE_CHECKPOINTS");
     if ((p->n_rec && !residuals) || !grad_vp || !prec_vp) return fail(SA_E_INVALID, "null residuals or outputs");
@@ -1261,8 +1301,16 @@ int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec
         float *o0 = p->afield[0], *o1 = p->afield[1], *os = p->segsnaps;
         CKR(ensure(&p->afield[0], &p->afield_cap[0], 2 * fe));
         CKR(ensure(&p->afield[1], &p->afield_cap[1], 2 * fe));
-        if (!exact) CKR(ensure(&p->segsnaps, &p->cap_segsnaps, (size_t)(p->ck_K / p->d.undersampling) * 2 * fe));
-        if (o0 != p->afield[0] || o1 != p->afield[1] || os != p->segsnaps) drop_graphs(p);
+        float *oc2 = p->ckpt2, *oa2 = p->pml_ck2;
+        const int K2 = p->ck_K2 > 0 ? p->ck_K2 : p->ck_K;
+        if (!exact) CKR(ensure(&p->segsnaps, &p->cap_segsnaps, (size_t)(K2 / p->d.undersampling) * 2 * fe));
+        if (!exact && p->ck_K2 > 0) {  // fine checkpoints of one coarse segment
+            const size_t nf = (size_t)std::max(1, p->ck_K / p->ck_K2 - 1);
+            CKR(ensure(&p->ckpt2, &p->cap_ckpt2, nf * 2 * 2 * fe));
+            if (p->pml) CKR(ensure(&p->pml_ck2, &p->cap_pml_ck2, nf * (pml_aux_bytes(p) / sizeof(float))));
+        }
+        if (o0 != p->afield[0] || o1 != p->afield[1] || os != p->segsnaps || oc2 != p->ckpt2 || oa2 != p->pml_ck2)
+            drop_graphs(p);
     }
     if (exact) {
         const size_t NG = (size_t)(p->nx + 2 * sa::GUARD) * p->pitch;
