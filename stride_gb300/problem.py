@@ -8,7 +8,54 @@ installed, its own objects are passed to the operator instead and these are not 
 
 import numpy as np
 
+from . import h5
+
 __all__ = ['Space', 'Time', 'Grid', 'ScalarField', 'Traces', 'Shot', 'SubProblem', 'inv_transform']
+
+
+def _grid_description(space, time):
+    """GriddedSaved.grid_description (stride/problem/base.py:268-314)."""
+    d = {}
+    if space is not None:
+        d['space'] = {'shape': space.shape, 'spacing': space.spacing, 'extra': space.extra,
+                      'absorbing': space.absorbing}
+    if time is not None:
+        d['time'] = {'start': time.start, 'stop': time.stop, 'step': time.step, 'num': time.num}
+    return d
+
+
+def _pad_edge(data, extended_shape):
+    """StructuredData.pad_data without smoothing (stride/problem/data.py:513-536): edge padding
+    of half the size difference on each side."""
+    widths = [(e - s) // 2 for e, s in zip(extended_shape, data.shape)]
+    if sum(widths) > 0:
+        data = np.pad(data, [(w, w) for w in widths], mode='edge')
+    return data
+
+
+class _Saved:
+    """dump / append / load through the mosaic HDF5 layer (stride/problem/base.py:102-249):
+    the file name is given (``filename``, ``path``) or formed from ``project_name``, the object's
+    name as ``parameter`` and ``version``."""
+
+    def dump(self, *args, **kwargs):
+        kwargs['parameter'] = kwargs.get('parameter', self.name)
+        desc = _grid_description(*self._grid_parts())
+        desc.update(self.__get_desc__())
+        with h5.HDF5(*args, **kwargs, mode='w') as f:
+            f.dump(desc)
+
+    def append(self, *args, **kwargs):
+        kwargs['parameter'] = kwargs.get('parameter', self.name)
+        desc = _grid_description(*self._grid_parts())
+        desc.update(self.__get_desc__())
+        with h5.HDF5(*args, **kwargs, mode='a') as f:
+            f.append(desc)
+
+    def load(self, *args, **kwargs):
+        kwargs['parameter'] = self.name
+        with h5.HDF5(*args, **kwargs, mode='r') as f:
+            self.__set_desc__(f.load(lazy=False))
 
 
 class Space:
@@ -61,8 +108,11 @@ def inv_transform(x):
     return 1 / x
 
 
-class ScalarField:
-    """Scalar field on the extended grid; ``data`` is the inner view (data.py:98-446)."""
+class ScalarField(_Saved):
+    """Scalar field on the extended grid; ``data`` is the inner view (data.py:98-446).
+    ``dump``/``load`` write and read the reference's description (StructuredData and
+    ScalarField, data.py:725-780,1163-1187) as HDF5; loading pads the stored inner data to
+    the extended grid with edge values."""
 
     def __init__(self, name, grid, data=None, needs_grad=False, transform=None):
         self.name = name
@@ -84,6 +134,24 @@ class ScalarField:
     def fill(self, value):
         self.extended_data.fill(value)
 
+    def _grid_parts(self):
+        return self.grid.space, getattr(self.grid, 'time', None)
+
+    def __get_desc__(self):
+        space = self.grid.space
+        return {'shape': space.shape, 'extended_shape': space.extended_shape,
+                'inner': [[str(s.start), str(s.stop), str(s.step)] for s in space.inner],
+                'dtype': 'float32', 'data': np.ascontiguousarray(self.data), 'compression': False,
+                'step_size': None, 'time_dependent': False, 'slow_time_dependent': False}
+
+    def __set_desc__(self, desc):
+        if getattr(desc, 'compression', False):
+            raise NotImplementedError('compressed field data')
+        data = np.asarray(desc.data, dtype=np.float32)
+        if tuple(data.shape) != tuple(self.grid.space.shape):
+            raise ValueError('stored field of shape %s on a grid of shape %s' % (data.shape, self.grid.space.shape))
+        self.extended_data = np.ascontiguousarray(_pad_edge(data, self.grid.space.extended_shape))
+
     def alike(self, name=None, data=None, **kwargs):
         out = ScalarField.__new__(ScalarField)
         out.name = name or self.name
@@ -95,8 +163,10 @@ class ScalarField:
         return out
 
 
-class Traces:
-    """Time traces [n_points, nt] (data.py:1100-1645)."""
+class Traces(_Saved):
+    """Time traces [n_points, nt] (data.py:1100-1645). ``dump``/``load`` write and read the
+    reference's description (data.py:1631-1641: the structured data plus ``num_transducers``
+    and ``transducer_ids``) as HDF5."""
 
     def __init__(self, name, data, grid=None):
         self.name = name
@@ -107,6 +177,21 @@ class Traces:
     def alike(self, name=None, data=None, **kwargs):
         t = Traces(name or self.name, self.data if data is None else data, self.grid)
         return t
+
+    def _grid_parts(self):
+        return None, getattr(self.grid, 'time', None) if self.grid is not None else None
+
+    def __get_desc__(self):
+        shape = tuple(self.data.shape)
+        return {'shape': shape, 'extended_shape': shape, 'inner': [['None', 'None', 'None']] * len(shape),
+                'dtype': 'float32', 'data': np.ascontiguousarray(self.data), 'compression': False,
+                'step_size': None, 'time_dependent': True, 'slow_time_dependent': False,
+                'num_transducers': shape[0], 'transducer_ids': list(range(shape[0]))}
+
+    def __set_desc__(self, desc):
+        if getattr(desc, 'compression', False):
+            raise NotImplementedError('compressed trace data')
+        self.data = np.ascontiguousarray(np.asarray(desc.data, dtype=np.float32))
 
 
 class Shot:
