@@ -7,10 +7,12 @@ specification) that those files use:
 
 * reading: superblocks v0 (libhdf5 defaults) and v2/v3 (``libver='latest'``, which mosaic opens
   with); object headers v1 and v2 with continuation blocks; groups as symbol tables (v1 B-tree,
-  symbol-table nodes, local heap) or compact link messages; contiguous and compact dataset
+  symbol-table nodes, local heap), compact link messages or dense links (fractal heap and v2
+  B-tree name index, which ``libver='latest'`` uses past eight links); contiguous and compact dataset
   layouts; fixed-point, floating-point, fixed and variable-length strings (global heap), enums
   (h5py's booleans) and opaque types (mosaic's ``bytes``); attribute messages v1-v3. Dense
-  (fractal-heap) link or attribute storage and chunked layouts raise NotImplementedError;
+  attribute storage, multi-level heaps or name indexes and chunked layouts raise
+  NotImplementedError;
 * writing: superblock v0 with v1 object headers, symbol-table groups, contiguous datasets and
   attributes, strings as fixed-length UTF-8, booleans as h5py's FALSE/TRUE enum.
 
@@ -217,9 +219,12 @@ class File:
                     if target is not None:
                         g[lname] = self._object(lname, target, g)
                 elif t == 0x02:
-                    fh = self._u(d + 2 + (8 if self._b[d + 1] & 1 else 0), self.O)
-                    if fh != _UNDEF:
-                        raise NotImplementedError('HDF5 dense link storage (more links than the compact limit)')
+                    q = d + 2 + (8 if self._b[d + 1] & 1 else 0)
+                    heap, index = self._addr(q), self._addr(q + self.O)
+                    if heap != _UNDEF:  # dense storage: link messages in a fractal heap, by name index
+                        for lname, target in self._dense_links(self._abs(heap), self._abs(index)):
+                            if target is not None:
+                                g[lname] = self._object(lname, target, g)
             return g
         if 0x08 in types:
             return self._dataset(name, msgs, attrs)
@@ -245,6 +250,73 @@ class File:
                     g[lname] = self._object(lname, self._abs(self._addr(e + self.O)), g)
 
         walk(btree)
+
+    def _dense_links(self, heap, index):
+        """Links of a group with dense storage: the records of its v2 B-tree name index (type 5:
+        name hash, heap ID) point at link messages stored as managed objects of its fractal heap.
+        Handles a root direct block or a root indirect block of direct blocks, and a name index
+        whose root is a leaf (the shape of every group short of thousands of links)."""
+        self._need(heap, b'FRHP')
+        flags = self._b[heap + 9]
+        max_managed = self._u(heap + 10, 4)
+        L, O = self.L, self.O
+        if self._u(heap + 7, 2):
+            raise NotImplementedError('HDF5 fractal heap with I/O filters')
+        q = heap + 14 + 10 * L + 2 * O  # table width, past the object counters
+        width = self._u(q, 2)
+        start_block, max_direct = self._u(q + 2, L), self._u(q + 2 + L, L)
+        max_heap_bits = self._u(q + 2 + 2 * L, 2)
+        root = self._addr(q + 2 + 2 * L + 4)
+        rows = self._u(q + 2 + 2 * L + 4 + O, 2)
+        off_bytes = (max_heap_bits + 7) // 8
+        len_bytes = min((max_direct.bit_length() - 1 + 7) // 8, (max_managed.bit_length() - 1) // 8 + 1)
+        hdr = 5 + O + off_bytes + (4 if flags & 2 else 0)  # direct block header
+
+        blocks = []  # (heap offset, address, size) of every direct block
+        if rows == 0:
+            blocks.append((0, self._abs(root), start_block))
+        else:
+            r = self._abs(root)
+            self._need(r, b'FHIB')
+            direct_rows = (max_direct.bit_length() - 1) - (start_block.bit_length() - 1) + 2
+            if rows > direct_rows:
+                raise NotImplementedError('HDF5 fractal heap with indirect child blocks')
+            e, off = r + 5 + O + off_bytes, 0
+            for row in range(rows):
+                size = start_block if row < 2 else start_block << (row - 1)
+                for _ in range(width):
+                    a = self._addr(e)
+                    e += O
+                    if a != _UNDEF:
+                        blocks.append((off, self._abs(a), size))
+                    off += size
+
+        def managed(hid):
+            if (hid[0] >> 4) & 3 != 0:
+                raise NotImplementedError('HDF5 huge or tiny fractal heap objects')
+            off = int.from_bytes(hid[1:1 + off_bytes], 'little')
+            n = int.from_bytes(hid[1 + off_bytes:1 + off_bytes + len_bytes], 'little')
+            for boff, a, size in blocks:
+                if boff <= off < boff + size:
+                    self._need(a, b'FHDB')
+                    if off - boff < hdr:
+                        break
+                    return a + (off - boff)
+            raise ValueError('HDF5: fractal heap offset %d outside its blocks' % off)
+
+        self._need(index, b'BTHD')
+        rec_size, depth = self._u(index + 10, 2), self._u(index + 12, 2)
+        node, nrec = self._abs(self._addr(index + 16)), self._u(index + 16 + O, 2)
+        if depth != 0:
+            raise NotImplementedError('HDF5 link name index deeper than one leaf')
+        if nrec == 0:
+            return []
+        self._need(node, b'BTLF')
+        out = []
+        for i in range(nrec):
+            rec = node + 6 + i * rec_size
+            out.append(self._link(managed(self._b[rec + 4:rec + rec_size])))
+        return out
 
     def _link(self, d):
         flags = self._b[d + 1]

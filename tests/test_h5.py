@@ -162,6 +162,58 @@ def test_superblock_v3_object_header_v2_paths(tmp_path):
     assert ds.attrs['unit'] == 'café'
 
 
+def _dense_file(n):
+    """A superblock-v3 file by hand whose root group keeps n links in dense storage: a link info
+    message pointing at a fractal heap (root direct block of link messages) and at its v2 B-tree
+    name index (one leaf of type-5 records: name hash, 7-byte managed heap ID)."""
+    U = 0xFFFFFFFFFFFFFFFF
+    buf = bytearray(8192)
+
+    def ohdr(msgs):
+        body = b''.join(struct.pack('<BHB', t, len(d), 0) + d for t, d in msgs)
+        return b'OHDR' + bytes([2, 1]) + struct.pack('<H', len(body)) + body + b'\0' * 4
+
+    f32 = struct.pack('<B3sIHHBBBBI', 0x11, bytes([0x20, 31, 0]), 4, 0, 32, 23, 8, 0, 23, 127)
+    at, targets = 4096, []
+    for k in range(n):  # scalar datasets holding k, compact layout
+        ds = ohdr([(0x01, bytes([2, 0, 0, 0])), (0x03, f32), (0x08, struct.pack('<BBH', 3, 0, 4) +
+                                                              np.float32(k).tobytes())])
+        buf[at:at + len(ds)] = ds
+        targets.append(at)
+        at += (len(ds) + 7) // 8 * 8
+    heap_at, block_at, tree_at, leaf_at = 1024, 1536, 2560, 3072
+    objs, ids, off = b'', [], 17  # direct block header: 4 + 1 + 8 + 4 (offset bytes)
+    for k in range(n):
+        name = ('key%02d' % k).encode()
+        link = bytes([1, 0, len(name)]) + name + struct.pack('<Q', targets[k])
+        ids.append(bytes([0]) + struct.pack('<I', off) + struct.pack('<H', len(link)))
+        objs += link
+        off += len(link)
+    block = b'FHDB' + bytes([0]) + struct.pack('<Q', heap_at) + struct.pack('<I', 0) + objs
+    buf[block_at:block_at + len(block)] = block
+    frhp = b'FRHP' + bytes([0]) + struct.pack('<HHBI', 7, 0, 0, 65536) + struct.pack('<QQQQ', 0, U, 0, U) + \
+        struct.pack('<8Q', 512, 512, off, n, 0, 0, 0, 0) + struct.pack('<HQQHH', 4, 512, 65536, 32, 1) + \
+        struct.pack('<QH', block_at, 0) + b'\0' * 4
+    buf[heap_at:heap_at + len(frhp)] = frhp
+    leaf = b'BTLF' + bytes([0, 5]) + b''.join(struct.pack('<I', 0) + i for i in ids) + b'\0' * 4
+    buf[leaf_at:leaf_at + len(leaf)] = leaf
+    bthd = b'BTHD' + bytes([0, 5]) + struct.pack('<IHHBB', 512, 11, 0, 100, 40) + struct.pack('<QHQ', leaf_at, n, n)
+    buf[tree_at:tree_at + len(bthd) + 4] = bthd + b'\0' * 4
+    root = ohdr([(0x02, bytes([0, 0]) + struct.pack('<QQ', heap_at, tree_at))])
+    buf[64:64 + len(root)] = root
+    buf[0:48] = b'\x89HDF\r\n\x1a\n' + bytes([3, 8, 8, 0]) + struct.pack('<QQQQ', 0, U, len(buf), 64) + b'\0' * 4
+    return bytes(buf)
+
+
+def test_dense_link_storage(tmp_path):
+    path = str(tmp_path / 'dense.h5')
+    with open(path, 'wb') as fh:
+        fh.write(_dense_file(11))
+    root = h5.read_file(path)
+    assert sorted(root.keys()) == ['key%02d' % k for k in range(11)]
+    assert all(root['key%02d' % k][()] == np.float32(k) for k in range(11))
+
+
 def test_mosaic_file_naming_and_versions(tmp_path):
     p = str(tmp_path)
     kw = dict(project_name='breast', parameter='vp_model', path=p)
