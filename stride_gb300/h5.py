@@ -299,7 +299,7 @@ class File:
             for boff, a, size in blocks:
                 if boff <= off < boff + size:
                     self._need(a, b'FHDB')
-                    if off - boff < hdr:
+                    if off - boff < hdr or off + n > boff + size:
                         break
                     return a + (off - boff)
             raise ValueError('HDF5: fractal heap offset %d outside its blocks' % off)
@@ -376,7 +376,7 @@ class File:
         raise NotImplementedError('HDF5 datatype class %d' % cls)
 
     def _dataspace(self, d):
-        ver, rank, flags = self._b[d], self._b[d + 1], self._b[d + 2]
+        ver, rank = self._b[d], self._b[d + 1]
         if ver == 1:
             q = d + 8
         else:

@@ -101,10 +101,10 @@ def test_writer_structures_match_libhdf5_encodings(tmp_path):
     assert (leaf_k, internal_k, flags) == (4, 16, 0)
     base, free, eof, driver = struct.unpack('<QQQQ', b[24:56])
     assert base == 0 and free == driver == 0xFFFFFFFFFFFFFFFF and eof == len(b)
-    name_off, root, cache, _, btree, heap = struct.unpack('<QQIIQQ', b[56:96])
+    name_off, _, cache, _, btree, heap = struct.unpack('<QQIIQQ', b[56:96])
     assert name_off == 0 and cache == 1
     assert b[btree:btree + 4] == b'TREE' and b[heap:heap + 4] == b'HEAP'
-    seg, free_head, data = struct.unpack('<QQQ', b[heap + 8:heap + 32])
+    _, free_head, data = struct.unpack('<QQQ', b[heap + 8:heap + 32])
     assert free_head == 1 and b[data] == 0  # end-of-list marker; empty name at offset 0
     used = struct.unpack('<H', b[btree + 6:btree + 8])[0]
     snod = struct.unpack('<Q', b[btree + 32:btree + 40])[0]
