@@ -1094,6 +1094,9 @@ int sa_set_medium(sa_plan* p, const float* vp, const float* rho, const float* al
     if (!p || !vp) return fail(SA_E_INVALID, "null plan or vp");
     if (p->d.density != SA_DENSITY_NONE && !rho) return fail(SA_E_INVALID, "rho required by the plan's density mode");
     if (p->d.attenuation && !alpha) return fail(SA_E_INVALID, "alpha required by the plan");
+    // work still queued on the caller's streams reads the medium being replaced; the upload below runs on
+    // the legacy default stream, which does not wait for non-blocking streams
+    CK(cudaDeviceSynchronize());
     if (p->p3) return sa::plan3d_set_medium(p->p3, vp, rho, alpha);
     const size_t N = (size_t)p->nx * p->ny;
     const float* in[3] = {vp, p->d.density != SA_DENSITY_NONE ? rho : nullptr, p->d.attenuation ? alpha : nullptr};
@@ -1145,6 +1148,7 @@ int sa_set_geometry(sa_plan* p, int n_shots, const int* src_offsets, const float
         if (src_offsets[s + 1] < src_offsets[s] || rec_offsets[s + 1] < rec_offsets[s])
             return fail(SA_E_INVALID, "offsets must be non-decreasing");
     if (src_offsets[0] != 0 || rec_offsets[0] != 0) return fail(SA_E_INVALID, "offsets must start at 0");
+    CK(cudaDeviceSynchronize());  // queued work on any stream reads the point lists being replaced
     const int ns = src_offsets[n_shots], nr = rec_offsets[n_shots];
     if ((ns && !src_xyz) || (nr && !rec_xyz)) return fail(SA_E_INVALID, "missing coordinates");
     if (p->p3) return sa::plan3d_set_geometry(p->p3, n_shots, src_offsets, src_xyz, rec_offsets, rec_xyz);
