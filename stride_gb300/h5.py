@@ -105,6 +105,7 @@ class File:
             self._b = fh.read()
         self.filename = filename
         self._gheaps = {}
+        self._path = set()  # object headers on the path from the root (hard links may form cycles)
         self._superblock()
         self.root = self._object('/', self._root_addr, None)
 
@@ -168,6 +169,7 @@ class File:
             size0 = self._u(q, nsz)
             q += nsz
             blocks = [(q, q + size0)]
+            seen = set()
             hdr = 6 if flags & 0x04 else 4
             while blocks:
                 q, end = blocks.pop(0)
@@ -177,6 +179,9 @@ class File:
                     if mtype == 0x10:
                         c = self._abs(self._addr(d))
                         self._need(c, b'OCHK')
+                        if c in seen:
+                            raise ValueError('HDF5: object header continuation loop at %d' % c)
+                        seen.add(c)
                         blocks.append((c + 4, c + self._u(d + self.O, self.L) - 4))
                     elif mtype != 0:
                         out.append((mtype, d, msize))
@@ -186,20 +191,33 @@ class File:
             raise NotImplementedError('HDF5 object header version %d' % self._b[addr])
         nmsg = self._u(addr + 2, 2)
         blocks = [(addr + 16, addr + 16 + self._u(addr + 8, 4))]
+        seen = set()
         while blocks and len(out) < nmsg:
             q, end = blocks.pop(0)
             while q + 8 <= end:
                 mtype, msize = self._u(q, 2), self._u(q + 2, 2)
                 d = q + 8
                 if mtype == 0x10:
-                    blocks.append((self._abs(self._addr(d)),
-                                   self._abs(self._addr(d)) + self._u(d + self.O, self.L)))
+                    c = self._abs(self._addr(d))
+                    if c in seen:
+                        raise ValueError('HDF5: object header continuation loop at %d' % c)
+                    seen.add(c)
+                    blocks.append((c, c + self._u(d + self.O, self.L)))
                 elif mtype != 0:
                     out.append((mtype, d, msize))
                 q = d + msize
         return out
 
     def _object(self, name, addr, parent):
+        if addr in self._path:
+            raise ValueError('HDF5: hard link cycle at %r' % name)
+        self._path.add(addr)
+        try:
+            return self._object_at(name, addr)
+        finally:
+            self._path.discard(addr)
+
+    def _object_at(self, name, addr):
         msgs = self._messages(addr)
         attrs = {}
         for t, d, _ in msgs:
@@ -234,14 +252,16 @@ class File:
         self._need(heap, b'HEAP')
         data = self._abs(self._addr(heap + 8 + 2 * self.L))
 
-        def walk(node):
+        def walk(node, above=256):
             self._need(node, b'TREE')
             level, used = self._b[node + 5], self._u(node + 6, 2)
+            if level >= above:
+                raise ValueError('HDF5: group B-tree levels do not decrease at %d' % node)
             q = node + 8 + 2 * self.O
             for i in range(used):
                 child = self._abs(self._addr(q + self.L + i * (self.L + self.O)))
                 if level > 0:
-                    walk(child)
+                    walk(child, level)
                     continue
                 self._need(child, b'SNOD')
                 for k in range(self._u(child + 6, 2)):

@@ -214,6 +214,22 @@ def test_dense_link_storage(tmp_path):
     assert all(root['key%02d' % k][()] == np.float32(k) for k in range(11))
 
 
+def test_hard_link_cycle_is_an_error(tmp_path):
+    """A group that links to itself (legal in HDF5) ends in ValueError, not unbounded recursion."""
+    U = 0xFFFFFFFFFFFFFFFF
+    link = bytes([1, 0, 4]) + b'self' + struct.pack('<Q', 64)
+    body = struct.pack('<BHB', 0x06, len(link), 0) + link
+    root = b'OHDR' + bytes([2, 0, len(body)]) + body + b'\0' * 4
+    buf = bytearray(256)
+    buf[0:48] = b'\x89HDF\r\n\x1a\n' + bytes([3, 8, 8, 0]) + struct.pack('<QQQQ', 0, U, 256, 64) + b'\0' * 4
+    buf[64:64 + len(root)] = root
+    path = str(tmp_path / 'cycle.h5')
+    with open(path, 'wb') as fh:
+        fh.write(bytes(buf))
+    with pytest.raises(ValueError):
+        h5.read_file(path)
+
+
 def test_mosaic_file_naming_and_versions(tmp_path):
     p = str(tmp_path)
     kw = dict(project_name='breast', parameter='vp_model', path=p)
