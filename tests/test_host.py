@@ -55,6 +55,26 @@ def test_cfs_pml_runs_with_ot2_in_2d():
                            kernel='OT4')
 
 
+def test_saved_wavefield_choice():
+    """Snapshots for the vp gradient, checkpoints when an interval or budget is given, the raw
+    wavefield whenever rho or the wavelets need a gradient (devito.py:319,410-413)."""
+    pde, shot, sub, vp, grid = _setup()
+    rho = problem.ScalarField('rho', grid, needs_grad=True)
+    pde._check_problem(shot.wavelets, vp, problem=sub)
+    assert pde._save_wavefield(vp, None, None, {}) is False
+    vp.needs_grad = True
+    assert pde._save_wavefield(vp, None, None, {}) == 'snapshots'
+    assert pde._save_wavefield(vp, rho, None, {}) == 'raw'
+    pde._check_problem(shot.wavelets, vp, problem=sub, checkpoint_interval=40)
+    assert pde.checkpoint_interval == 40
+    assert pde._save_wavefield(vp, None, None, {}) == 'checkpoints'
+    assert pde._save_wavefield(vp, rho, None, {}) == 'raw'
+    pde._check_problem(shot.wavelets, vp, problem=sub, checkpoint_budget=1e9)
+    assert pde.checkpoint_interval == 0 and pde._save_wavefield(vp, None, None, {}) == 'checkpoints'
+    pde._check_problem(shot.wavelets, vp, problem=sub)
+    assert pde._save_wavefield(vp, None, None, {}) == 'snapshots'
+
+
 def test_attenuation_power_errors():
     pde, shot, sub, vp, grid = _setup()
     alpha = problem.ScalarField('alpha', grid)
