@@ -21,11 +21,52 @@ import numpy as np
 import scipy.signal
 import torch
 
-from . import _lib
+from . import _lib, h5
 from .pipelines import (CheckTraces, Clip, FilterTraces, GradientDescent, MaskField, MuteTraces, NormField,
                         NormPerShot, SmoothField, apply_prec)
 
-__all__ = ['PlainFWI', 'LearnedFWI', 'relative_error', 'features', 'generate_pairs', 'train_unet', 'run_to_error']
+__all__ = ['PlainFWI', 'LearnedFWI', 'relative_error', 'features', 'generate_pairs', 'train_unet', 'run_to_error',
+           'dump_state', 'load_state']
+
+
+def dump_state(vp, history, inner, spacing, path, project_name='fwi'):
+    """Per-iteration dump for restarts, as the reference's inversion loop keeps them
+    (stride/__init__.py:281-297, optimisation_loop.py:475-530): the model as a vp field file
+    ``<project>-Vp[-%05d].h5`` whose version is the number of completed iterations (the
+    reference's ScalarField description: inner ``data`` and its grid, plus ``extended_data`` so
+    that the absorbing frame is restored exactly), and the loop's per-iteration records in
+    ``<project>-OptimisationLoop.h5``."""
+    vp = np.ascontiguousarray(vp, dtype=np.float32)
+    inner_shape = tuple(s.stop - s.start for s in inner)
+    extra = tuple(s.start for s in inner)
+    desc = {'space': {'shape': inner_shape, 'spacing': tuple(float(h) for h in spacing), 'extra': extra,
+                      'absorbing': extra},
+            'shape': inner_shape, 'extended_shape': vp.shape,
+            'inner': [[str(s.start), str(s.stop), 'None'] for s in inner], 'dtype': 'float32',
+            'data': np.ascontiguousarray(vp[inner]), 'extended_data': vp, 'time_dependent': False}
+    version = len(history)
+    with h5.HDF5(project_name=project_name, parameter='vp', path=path, version=version, mode='w') as f:
+        f.dump(desc)
+    loop = {'num_iterations': version,
+            'iterations': [dict({'id': k}, **{key: rec[key] for key in ('misfit', 'error', 'seconds', 'f_max')})
+                           for k, rec in enumerate(history)]}
+    with h5.HDF5(project_name=project_name, parameter='optimisation_loop', path=path, version=0, mode='w') as f:
+        f.dump(loop)
+    return version
+
+
+def load_state(path, project_name='fwi', version=None):
+    """(extended vp, history records, version) of a dump: the latest model version unless one is
+    given, and the loop records up to it."""
+    with h5.HDF5(project_name=project_name, parameter='vp', path=path, version=version, mode='r') as f:
+        d = f.load(lazy=False)
+    vp = np.asarray(d['extended_data'] if 'extended_data' in d else d['data'], dtype=np.float32)
+    with h5.HDF5(project_name=project_name, parameter='optimisation_loop', path=path, version=0, mode='r') as f:
+        loop = f.load(lazy=False)
+    recs = loop['iterations'] if loop.get('num_iterations', 0) > 0 else []
+    done = len(recs) if version is None else int(version)
+    history = [{key: r[key] for key in ('misfit', 'error', 'seconds', 'f_max')} for r in recs[:done]]
+    return vp, history, len(history)
 
 
 def relative_error(vp, vp_true, inner):
@@ -103,6 +144,20 @@ class PlainFWI:
 
     def close(self):
         self.plan.close()
+
+    def dump(self, path, project_name='fwi'):
+        """Writes the current model and loop records (``dump_state``); returns the version."""
+        return dump_state(self.vp.cpu().numpy(), self.history, self.inner, self.w['spacing'], path, project_name)
+
+    def resume(self, path, project_name='fwi', version=None):
+        """Restores the model and loop records of a dump (the latest unless ``version``); returns the
+        number of completed iterations, from which ``iterate`` continues."""
+        vp, history, done = load_state(path, project_name, version)
+        if tuple(vp.shape) != tuple(self.vp.shape):
+            raise ValueError('dumped model of shape %s on a grid of shape %s' % (vp.shape, tuple(self.vp.shape)))
+        self.vp.copy_(torch.as_tensor(vp, device=self.device))
+        self.history = history
+        return done
 
     def error(self):
         return relative_error(self.vp, self.vp_true, self.inner)

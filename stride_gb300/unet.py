@@ -16,7 +16,7 @@ import ctypes
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, h5
 
 __all__ = ['UNet']
 
@@ -249,3 +249,11 @@ class UNet:
             layer.w.copy_(torch.as_tensor(sd['%d_w' % i]))
             layer.b.copy_(torch.as_tensor(sd['%d_b' % i]))
             layer.pack()
+
+    def dump(self, filename):
+        """The weights as an HDF5 file: one dataset per layer weight and bias (state_dict names)."""
+        h5.write_file(filename, self.state_dict())
+
+    def load(self, filename):
+        """Weights from a file written by ``dump``."""
+        self.load_state_dict(h5.HDF5(filename, mode='r').load(lazy=False))

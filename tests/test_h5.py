@@ -11,7 +11,7 @@ import struct
 import numpy as np
 import pytest
 
-from stride_gb300 import h5, problem
+from stride_gb300 import fwi, h5, problem
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, 'golden', 'anastasio2d_truemodel.json')
@@ -286,3 +286,26 @@ def test_unsupported_structures_raise(tmp_path):
         h5.read_file(path)
     with pytest.raises(TypeError):
         h5.write_file(str(tmp_path / 'x.h5'), {'z': np.ones(2, np.complex64)})
+
+
+def test_fwi_state_dump_and_restart(tmp_path):
+    """The inversion's per-iteration dumps (model versions and loop records) and the restart
+    from the latest or a chosen version, as the reference's optimisation loop keeps them."""
+    rng = np.random.default_rng(4)
+    vp = rng.uniform(1400, 1600, (40, 44)).astype(np.float32)
+    inner = (slice(6, 34), slice(6, 38))
+    hist = []
+    models = []
+    for k in range(3):
+        models.append(vp + k)
+        assert fwi.dump_state(models[-1], hist, inner, (5e-4, 5e-4), str(tmp_path), 'inv') == k
+        hist.append({'misfit': 10.0 - k, 'error': 0.03 - 0.01 * k, 'seconds': 0.5, 'f_max': None if k else 3e5})
+    assert sorted(os.listdir(tmp_path)) == ['inv-OptimisationLoop.h5', 'inv-Vp-00001.h5', 'inv-Vp-00002.h5',
+                                            'inv-Vp.h5']
+    v, h, done = fwi.load_state(str(tmp_path), 'inv')
+    assert done == 2 and np.array_equal(v, models[2]) and h == hist[:2]
+    v, h, done = fwi.load_state(str(tmp_path), 'inv', version=1)
+    assert done == 1 and np.array_equal(v, models[1]) and h == hist[:1]
+    # the model file is the reference's vp field description: inner data and grid
+    d = h5.HDF5(project_name='inv', parameter='vp', path=str(tmp_path), version=2, mode='r').load(lazy=False)
+    assert np.array_equal(d.data, models[2][inner]) and d.space.extra == (6, 6) and d.extended_shape == (40, 44)
