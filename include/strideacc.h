@@ -280,6 +280,13 @@ int sa_last_error(char* buf, int len);
 /* Kernel launches the last sa_forward/sa_adjoint issued (for throughput accounting). */
 long long sa_launch_count(const sa_plan* plan);
 
+/* The checkpoint schedule sa_forward(SA_SAVE_CHECKPOINTS) takes for n_shots shots of a plan with
+   description d (its checkpoint_interval, checkpoint_budget, grid, nt, undersampling, boundary):
+   coarse interval *K and *n_ckpt checkpoints, and *K2 the fine interval of a two-level schedule (0:
+   one level). SA_E_NOMEM when no schedule fits the budget. Host only: no device work. Replaces the
+   memory planning the reference leaves to Devito's save options (iso_acoustic/devito.py:325-403). */
+int sa_checkpoint_schedule(const sa_desc* d, int n_shots, int* K, int* n_ckpt, int* K2);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,6 +38,7 @@ SA_GRAD_EXACT = 1
 # every symbol include/strideacc.h declares
 EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometry', 'sa_forward',
            'sa_adjoint', 'sa_adjoint_wavelets', 'sa_adjoint_grads', 'sa_autotune', 'sa_last_error', 'sa_launch_count',
+           'sa_checkpoint_schedule',
            'sa_forward_2d_noalloc',
            'sa_traces_sosfilt', 'sa_traces_fir', 'sa_traces_check', 'sa_traces_norm_per_shot', 'sa_traces_mute',
            'sa_field_mul', 'sa_field_clip', 'sa_field_axpy', 'sa_field_slowness_step', 'sa_field_stats',
@@ -87,6 +88,8 @@ def load():
     lib.sa_last_error.argtypes = [ctypes.c_char_p, I]
     lib.sa_launch_count.argtypes = [P]
     lib.sa_launch_count.restype = ctypes.c_longlong
+    IP = ctypes.POINTER(I)
+    lib.sa_checkpoint_schedule.argtypes = [ctypes.POINTER(SaDesc), I, IP, IP, IP]
     L = ctypes.c_longlong
     F = ctypes.c_float
     D = ctypes.c_double
@@ -123,6 +126,26 @@ def load():
             getattr(lib, name).restype = I
     _lib = lib
     return lib
+
+
+def checkpoint_schedule(dim, shape, nt, n_shots=1, undersampling=4, checkpoint_interval=0, checkpoint_budget=0.0,
+                        boundary='sponge'):
+    """(K, n_checkpoints, K2) that sa_forward(SA_SAVE_CHECKPOINTS) takes for n_shots shots: the
+    coarse interval and count and the fine interval of a two-level schedule (0: one level). Host
+    only; raises StrideAccError(SA_E_NOMEM) when nothing fits checkpoint_budget bytes."""
+    d = SaDesc()
+    d.dim = dim
+    for i in range(3):
+        d.shape[i] = int(shape[i]) if i < dim else 1
+    d.nt = int(nt)
+    d.undersampling = int(undersampling)
+    d.checkpoint_interval = int(checkpoint_interval)
+    d.checkpoint_budget = float(checkpoint_budget)
+    d.boundary = {'sponge': SA_BOUNDARY_SPONGE, 'pml': SA_BOUNDARY_CFS_PML}[boundary]
+    K, n, K2 = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    check(load().sa_checkpoint_schedule(ctypes.byref(d), int(n_shots), ctypes.byref(K), ctypes.byref(n),
+                                        ctypes.byref(K2)))
+    return K.value, n.value, K2.value
 
 
 def last_error():

@@ -957,6 +957,26 @@ long long sa_launch_count(const sa_plan* p) {
     return p->p3 ? sa::plan3d_launches(p->p3) : p->launches;
 }
 
+int sa_checkpoint_schedule(const sa_desc* d, int n_shots, int* K, int* n_ckpt, int* K2) {
+    if (!d || !K || !n_ckpt || !K2 || n_shots < 1) return fail(SA_E_INVALID, "null argument or n_shots < 1");
+    if (d->dim != 2 && d->dim != 3) return fail(SA_E_INVALID, "dim %d", d->dim);
+    for (int a = 0; a < d->dim; a++)
+        if (d->shape[a] < 1) return fail(SA_E_INVALID, "shape");
+    if (d->nt < 3 || d->undersampling < 1) return fail(SA_E_INVALID, "nt or undersampling");
+    const bool pml = d->boundary == SA_BOUNDARY_CFS_PML;
+    double level;  // bytes of one wavefield level of every shot, as the plans lay it out
+    if (d->dim == 2) {
+        const long long pitch = (d->shape[1] + 2 + 31) / 32 * 32;
+        level = (double)((n_shots + 1) / 2) * d->shape[0] * pitch * 2 * sizeof(float);
+    } else {
+        const long long zp = (d->shape[2] + 2 + 31) / 32 * 32;
+        level = (double)n_shots * d->shape[0] * d->shape[1] * zp * sizeof(float);
+    }
+    // a checkpoint: both levels, plus the CFS-PML's auxiliary fields (six levels in 2D, nine in 3D)
+    const double ck_levels = d->dim == 2 ? (pml ? 8 : 2) : (pml ? 11 : 2);
+    return sa::choose_checkpoints(*d, level, K, n_ckpt, ck_levels, K2);
+}
+
 namespace {
 int pml_profiles(sa_plan* p) {
     float vmax = 0.f;
