@@ -13,6 +13,7 @@ otherwise a local mirror of the base class is used.
 """
 
 import logging
+import time
 
 import numpy as np
 import scipy.signal
@@ -30,6 +31,9 @@ except Exception:  # noqa: BLE001
     _mosaic = None
 
 DB_TO_NEPER = 100 * (1e-6 / (2 * np.pi)) ** 0 / (20 * np.log10(np.exp(1)))
+PERF = 19  # the level of Devito's and Mosaic's 'perf' lines, between DEBUG and INFO
+logging.addLevelName(PERF, 'PERF')
+
 SUPPORTED_BOUNDARIES = ('sponge_boundary_2', 'complex_frequency_shift_PML_2')
 KNOWN_BOUNDARIES = ('sponge_boundary_2', 'complex_frequency_shift_PML_2', 'sponge_boundary_1')
 SUPPORTED_INTERPOLATION = ('linear', 'hicks')
@@ -158,6 +162,14 @@ class IsoAcousticGB300(ProblemTypeBase):
 
     # ---------------------------------------------------------------------------- checks
 
+    def _perf(self, msg, *args):
+        """A 'perf' line: Mosaic's logger level when the host logger has one, else PERF."""
+        perf = getattr(self.logger, 'perf', None)
+        if perf is not None:
+            perf(msg % args if args else msg)
+        else:
+            self.logger.log(PERF, msg, *args)
+
     def _check_problem(self, wavelets, vp, rho=None, alpha=None, **kwargs):
         """Option validation and scheme selection (devito.py:1266-1352)."""
         boundary_type = kwargs.get('boundary_type', 'sponge_boundary_2')
@@ -166,6 +178,9 @@ class IsoAcousticGB300(ProblemTypeBase):
         if boundary_type not in SUPPORTED_BOUNDARIES:
             raise NotImplementedError('boundary_type %s is not implemented in this build' % boundary_type)
         self.boundary_type = boundary_type
+        problem = kwargs.get('problem')
+        self._perf('(ShotID %d) Selected boundary type %s', problem.shot.id if problem is not None else -1,
+                   boundary_type)
         interpolation_type = kwargs.get('interpolation_type', self.interpolation_type)
         if interpolation_type not in KNOWN_INTERPOLATION:
             raise ValueError('Only "linear" and "hicks" interpolations are allowed.')
@@ -213,6 +228,8 @@ class IsoAcousticGB300(ProblemTypeBase):
         f_max = np.max(f_maxs) if f_maxs else 0.05 / dt
         f_centre = np.median(f_centres) if f_centres else 0.05 / dt
         self._bandwidth = (f_min, f_centre, f_max)
+        self._perf('(ShotID %d) Estimated bandwidth for the propagated wavelet %.3f-%.3f MHz', shot_id, f_min / 1e6,
+                   f_max / 1e6)
         h = max(*self.space.spacing)
         ppw = vp_min / f_max / h if f_max > 0 else np.inf
         if ppw < 5:
@@ -231,9 +248,11 @@ class IsoAcousticGB300(ProblemTypeBase):
         self.kernel = selected if preferred_kernel is None else preferred_kernel
         if self.kernel not in ('OT2', 'OT4'):
             raise ValueError('Unrecognized kernel')
+        self._perf('(ShotID %d) Selected time stepping scheme %s', shot_id, self.kernel)
         dt_max = 1 / (4 * f_max)
         self.undersampling_factor = min(max(4, int(dt_max / dt)), 10) \
             if preferred_undersampling is None else int(preferred_undersampling)
+        self._perf('(ShotID %d) Selected undersampling level %d', shot_id, self.undersampling_factor)
 
     # ---------------------------------------------------------------------------- plans
 
@@ -319,8 +338,17 @@ class IsoAcousticGB300(ProblemTypeBase):
             self._saved = False
             return
         save = self._save_wavefield(vp, rho, alpha, kwargs, wavelets)
+        shot_id = problem.shot.id if problem is not None else -1
+        points = float(np.prod(self.space.extended_shape))
+        if save in ('snapshots', 'raw'):
+            n_snap = (self.time.extended_num + self.undersampling_factor) // self.undersampling_factor + 1
+            self._perf('(ShotID %d) Expected wavefield size %.4f GB', shot_id, n_snap * points * 4 / 1024 ** 3)
+        t0 = time.perf_counter()
         self._plan.forward(self._src, self._traces, save=save)
         self._saved = save
+        secs = time.perf_counter() - t0
+        self._perf('(ShotID %d) Forward ran in %.3f s (%.2f GPts/s)', shot_id, secs,
+                   points * (self.time.extended_num - 2) / max(secs, 1e-9) / 1e9)
 
     def after_forward(self, wavelets, vp, rho=None, alpha=None, **kwargs):
         """Return the modelled traces (devito.py:583-685)."""
@@ -353,8 +381,13 @@ class IsoAcousticGB300(ProblemTypeBase):
         if np.linalg.norm(np.asarray(adjoint_source.data)) < 1e-31:
             self.logger.warning('(ShotID %d) Empty adjoint source, not running adjoint', problem.shot.id)
             return
+        t0 = time.perf_counter()
         self._plan.adjoint(self._res, self._grad, self._prec, grad_wavelets=self._wgrad, grad_rho=self._grad_rho,
                            prec_rho=self._prec_rho)
+        secs = time.perf_counter() - t0
+        steps = self.time.extended_num - 1 - self.undersampling_factor
+        self._perf('(ShotID %d) Adjoint ran in %.3f s (%.2f GPts/s)', problem.shot.id if problem is not None else -1,
+                   secs, float(np.prod(self.space.extended_shape)) * steps / max(secs, 1e-9) / 1e9)
 
     def after_adjoint(self, adjoint_source, wavelets, vp, rho=None, alpha=None, **kwargs):
         """Retrieve the gradients (devito.py:922-981)."""

@@ -75,6 +75,38 @@ def test_saved_wavefield_choice():
     assert pde._save_wavefield(vp, None, None, {}) == 'snapshots'
 
 
+def test_perf_lines(caplog):
+    """The reference's per-shot 'perf' lines (devito.py:406,1289,1347,1382,1458) and the run times,
+    with the forward and adjoint driven through a stub plan (no GPU)."""
+    pde, shot, sub, vp, grid = _setup()
+    vp.needs_grad = True
+
+    class StubPlan:
+        n_src = 1
+        save = adj = None
+
+        def forward(self, src, traces, save=False):
+            self.save = save
+
+        def adjoint(self, res, grad, prec, **kw):
+            self.adj = True
+
+    with caplog.at_level(iso_acoustic.PERF, logger='stride_gb300'):
+        pde._check_problem(shot.wavelets, vp, problem=sub)
+        pde._plan = StubPlan()
+        pde._src = np.zeros((1, 400), np.float32)
+        pde._traces = np.zeros((2, 400), np.float32)
+        pde.run_forward(shot.wavelets, vp, problem=sub)
+        pde._res = np.zeros((2, 400), np.float32)
+        pde.run_adjoint(shot.observed.alike(name='residual', data=np.ones((2, 400), np.float32)), shot.wavelets, vp,
+                        problem=sub)
+    for m in ('(ShotID 0) Selected boundary type sponge_boundary_2', 'Estimated bandwidth for the propagated wavelet',
+              'Selected time stepping scheme OT4', 'Selected undersampling level 4', 'Expected wavefield size',
+              'Forward ran in', 'Adjoint ran in'):
+        assert m in caplog.text
+    assert pde._plan.save == 'snapshots' and pde._plan.adj
+
+
 def test_attenuation_power_errors():
     pde, shot, sub, vp, grid = _setup()
     alpha = problem.ScalarField('alpha', grid)
