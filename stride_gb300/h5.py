@@ -23,6 +23,7 @@ Checksums of v2 structures are not verified.
 """
 
 import datetime
+import mmap
 import os
 import re
 import struct
@@ -98,11 +99,13 @@ class _Type:
 
 
 class File:
-    """Read-only view of an HDF5 file held in memory; ``root`` is the root Group."""
+    """Read-only view of an HDF5 file, memory-mapped (datasets are read when loaded); ``root`` is
+    the root Group."""
 
     def __init__(self, filename):
         with open(filename, 'rb') as fh:
-            self._b = fh.read()
+            size = os.fstat(fh.fileno()).st_size
+            self._b = mmap.mmap(fh.fileno(), 0, access=mmap.ACCESS_READ) if size else b''
         self.filename = filename
         self._gheaps = {}
         self._path = set()  # object headers on the path from the root (hard links may form cycles)
@@ -116,7 +119,9 @@ class File:
         return node
 
     def close(self):
-        pass
+        """Unmaps the file; datasets not yet loaded can no longer be read."""
+        if isinstance(self._b, mmap.mmap):
+            self._b.close()
 
     # ---- primitives
     def _u(self, pos, n):
@@ -133,7 +138,9 @@ class File:
             raise ValueError('HDF5: expected %r at %d' % (sig, pos))
 
     def _cstr(self, pos):
-        end = self._b.index(b'\0', pos)
+        end = self._b.find(b'\0', pos)
+        if end < 0:
+            raise ValueError('HDF5: unterminated string at %d' % pos)
         return self._b[pos:end]
 
     # ---- superblock
@@ -478,15 +485,21 @@ class File:
         n = int(np.prod(shape)) if shape else (0 if shape is None else 1)
         nbytes = n * t.size
         if cls == 0:
-            raw = self._b[layout + 4:layout + 4 + nbytes]
+            start = layout + 4
         elif cls == 1:
             a = self._addr(layout + 2)
-            raw = b'\0' * nbytes if a == _UNDEF else self._b[self._abs(a):self._abs(a) + nbytes]
+            start = None if a == _UNDEF else self._abs(a)
         else:
             raise NotImplementedError('HDF5 chunked or virtual datasets')
+
+        def read():  # the data are sliced out of the mapping only when the dataset is loaded
+            if shape is None:
+                return None
+            raw = b'\0' * nbytes if start is None else self._b[start:start + nbytes]
+            return self._values(t, shape, raw, as_str=False)
+
         dt = np.dtype(object) if t.kind == 'vstr' else (np.dtype(np.bool_) if t.kind == 'enum' else t.dtype)
-        return Dataset(name, attrs, shape if shape is not None else (), dt,
-                       lambda: None if shape is None else self._values(t, shape, raw, as_str=False))
+        return Dataset(name, attrs, shape if shape is not None else (), dt, read)
 
 
 def read_file(filename):
@@ -797,6 +810,9 @@ class HDF5:
         return self._file
 
     def close(self):
+        """Closes the file: lazily returned datasets not yet loaded become unreadable, as with h5py."""
+        if self._file is not None:
+            self._file.close()
         self._file = None
 
     def load(self, lazy=True, filter=None, only=None):
@@ -812,7 +828,11 @@ class HDF5:
     def append(self, description):
         old = {}
         if os.path.exists(self._filename):
-            old = _read(File(self._filename).root, lazy=False)
+            f = File(self._filename)
+            try:  # everything read into memory, and the mapping closed, before the file is rewritten
+                old = _read(f.root, lazy=False)
+            finally:
+                f.close()
         write_file(self._filename, _merge(old, description))
 
     def __enter__(self):
