@@ -38,8 +38,8 @@ if ROOT not in sys.path:
 
 HBM_FALLBACK_GBS = 6800.0
 # dram__bytes_read.sum + dram__bytes_write.sum of one fdtd2d_step launch on this workload's
-# batch (64 shots of 552^2, forward step with wavefield save), from the ncu capture summarised
-# in profiles/fdtd2d_step_fwdadj_552sq_64shots.md.
+# batch (64 shots of 552^2, forward step with wavefield save), from an ncu capture of that
+# launch: a fixed figure of the kernel, not measured by this run.
 NCU_TRAFFIC_PER_LAUNCH = 179.700992e6 + 102.897664e6
 
 
@@ -196,9 +196,10 @@ def measured_hbm():
         return HBM_FALLBACK_GBS, 'fallback'
 
 
-def cpu_arm(w, target_s=15.0, threads=None, calib=True, mode='fwdadj'):
+def cpu_arm(w, target_s=15.0, threads=None, calib=True, mode='fwdadj', full=False):
     """Times the oracle's C restatement of the reference operator (one shot: forward, plus
-    the adjoint for mode 'fwdadj') on the host cores; returns GPts/s and the sample description."""
+    the adjoint for mode 'fwdadj') on the host cores; returns GPts/s and the sample description.
+    full: every time step of the shot, no calibration run."""
     from oracle import c_oracle
     threads = threads or os.cpu_count()
     origin = tuple(-e * h for e, h in zip(w['extra'], w['spacing']))
@@ -219,6 +220,11 @@ def cpu_arm(w, target_s=15.0, threads=None, calib=True, mode='fwdadj'):
         dt = time.perf_counter() - t0
         return pts / dt / 1e9, dt
 
+    if full:
+        nt = w['nt']
+        rate, dt = run(nt)
+        return rate, threads, '1 shot of the workload, %s, %d of %d steps, %.1f s' % (
+            'forward (save) + adjoint' if grad else 'forward', nt, w['nt'], dt), dt
     nt = min(24, w['nt'])
     rate, dt = run(nt)
     if calib:
@@ -335,30 +341,39 @@ def fwi_arm(args):
 
 
 def reference_arm(args):
+    """The reference algorithm's CPU implementation on all host cores. One step is one whole shot
+    of the workload (every time step of the forward with save and, for gradient workloads, of the
+    adjoint), the unit the reference's own worker processes at a time; `value` is that shot's
+    points over its measured time, and `ms_per_step` the measured time of one such step."""
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
         return 0
     w = workload_config(args.workload, nt=args.nt, n_shots=args.shots)
     mode = WORKLOADS[args.workload][2]
     threads = os.cpu_count()
-    rates, samples = [], []
     for _ in range(args.warmup):
-        cpu_arm(w, target_s=1.0, threads=threads, calib=False, mode=mode)
+        cpu_arm(w, threads=threads, calib=False, mode=mode, full=True)
+    rates, times, sample = [], [], ''
     for _ in range(args.steps):
-        r, _, sample, dt = cpu_arm(w, target_s=args.cpu_seconds / max(1, args.steps), threads=threads, mode=mode)
+        r, _, sample, dt = cpu_arm(w, threads=threads, calib=False, mode=mode, full=True)
         rates.append(r)
-        samples.append(sample)
-    value = statistics.median(rates)
+        times.append(dt)
+    ms_step = 1e3 * sum(times) / len(times)
+    N = int(np.prod(w['shape']))
+    shot_pts = N * (w['nt'] - 2) + (N * (w['nt'] - 1 - 4) if mode == 'fwdadj' else 0)
+    value = shot_pts / (ms_step * 1e-3) / 1e9
     line = {
         'impl': 'reference', 'metric': METRIC[mode], 'value': value, 'unit': 'GPts/s',
         'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': _points(w, args.workload) / (value * 1e9) * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+        'ms_per_step': ms_step, 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded phantoms)',
         'config': {'workload': workload_name(args.workload, w['nt']), 'grid': list(w['shape']), 'shots': len(w['shots']),
-                   'nt': w['nt'], 'kernel': 'OT4', 'l2_flush': 'inputs larger than L2'},
+                   'nt': w['nt'], 'kernel': 'OT4', 'l2_flush': 'inputs larger than L2',
+                   'step': 'one whole shot of the workload per step (%s); the %d-shot batch is %d such steps'
+                           % (sample, len(w['shots']), len(w['shots']))},
         'cpu_baseline': {'value': value, 'unit': 'GPts/s', 'cores': threads, 'kind': 'port',
-                         'sample': samples[-1] + ' per step (the reference Devito operator cannot be installed here; '
-                                                 'this is the oracle C/OpenMP restatement of it)'},
+                         'sample': sample + ' per step, %d steps (the reference Devito operator cannot be installed '
+                                            'here; this is the oracle C/OpenMP restatement of it)' % args.steps},
         'e2e': {'value': value, 'unit': 'GPts/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
     }
     print(json.dumps(line))
@@ -369,11 +384,13 @@ def gb300_arm(args):
     import torch
     import torch.distributed as dist
     import scipy.signal
-    from stride_gb300 import _lib
+    from stride_gb300 import _lib, shards
 
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
     local = int(os.environ.get('LOCAL_RANK', '0'))
+    if world != args.gpus:
+        raise SystemExit('bench.py: %d rank(s) running for --gpus %d' % (world, args.gpus))
     if world > 1:
         dist.init_process_group('nccl')
     torch.cuda.set_device(local)
@@ -436,8 +453,7 @@ def gb300_arm(args):
             launches['n'] += plan.launches
         e2.record(stream)
         if world > 1 and grad_mode:
-            dist.all_reduce(grad)
-            dist.all_reduce(prec)
+            shards.allreduce_sum(grad, prec)  # the one exchange step: per-rank sums over every shot
         if timed:
             fwd_ms.append((e0, e1))
             adj_ms.append((e1, e2))
@@ -525,7 +541,8 @@ def gb300_arm(args):
     cpu = None
     # the C port restates the sponge / p.dt2 path only: no CPU line for the raw-save and CFS-PML workloads
     if rank == 0 and world == 1 and not args.no_cpu and args.workload not in ('rho64', 'pml64'):
-        rate, cores, sample, _ = cpu_arm(w, target_s=args.cpu_seconds, mode=mode)
+        # 2D: one whole shot, as the reference arm times it; 3D: a calibrated sample of one shot
+        rate, cores, sample, _ = cpu_arm(w, target_s=args.cpu_seconds, mode=mode, full=dim == 2)
         cpu = {'value': rate, 'unit': 'GPts/s', 'cores': cores, 'kind': 'port', 'sample': sample}
 
     if rank == 0:
@@ -544,6 +561,9 @@ def gb300_arm(args):
             'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                          'frac': achieved / peak, 'peak_source': peak_kind,
                          'traffic': NCU_TRAFFIC_PER_LAUNCH if args.workload == 'fwdadj64' else None,
+                         'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one forward step '
+                                           'launch of this workload (a profile figure, not measured in this run)'
+                                           if args.workload == 'fwdadj64' else None,
                          'alg_bytes_per_point': {'forward': b_fwd, 'adjoint': b_adj if grad_mode else None},
                          'kernel': 'fdtd2d_step' if dim == 2 else 'fdtd3d_pass',
                          'step_ms': per_step_s * 1e3},
@@ -555,6 +575,25 @@ def gb300_arm(args):
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def _free_port():
+    import socket
+    with socket.socket() as so:
+        so.bind(('127.0.0.1', 0))
+        return so.getsockname()[1]
+
+
+def launch_ranks(n, argv, port=None, capture=False):
+    """Runs the script argv[0] (with argv[1:]) as n ranks of one node under torch.distributed.run,
+    rendezvous on 127.0.0.1; returns the exit status (and the ranks' stdout when capture)."""
+    cmd = [sys.executable, '-m', 'torch.distributed.run', '--nnodes=1', '--nproc-per-node', str(n),
+           '--master-addr', '127.0.0.1', '--master-port', str(port or _free_port())] + list(argv)
+    env = dict(os.environ, OMP_NUM_THREADS=os.environ.get('OMP_NUM_THREADS', '1'))
+    if capture:
+        r = subprocess.run(cmd, env=env, stdout=subprocess.PIPE, text=True)
+        return r.returncode, r.stdout
+    return subprocess.call(cmd, env=env)
 
 
 def main():
@@ -576,6 +615,9 @@ def main():
     ap.add_argument('--fwi-target', type=float, default=0.01)
     ap.add_argument('--fwi-iters', type=int, default=25)
     args = ap.parse_args()
+    if args.gpus > 1 and 'WORLD_SIZE' not in os.environ:
+        # one process per GPU: this script again as --gpus ranks under torch.distributed.run
+        return launch_ranks(args.gpus, [os.path.abspath(__file__)] + sys.argv[1:])
     if args.workload == 'fwi':
         if args.impl == 'reference':
             print(json.dumps({'impl': 'reference', 'unavailable': 'the fwi workload compares two GPU methods; its '

@@ -147,7 +147,9 @@ int sa_adjoint_grads(sa_plan* plan, const float* residuals, float* grad_vp, floa
                      float* prec_rho, float* grad_wavelets, void* stream);
 
 /* Picks the CTA width and row chunking for the current geometry by timing the candidates
- * (no counterpart in the reference, whose Devito autotuner is optional: common/devito.py:1043). */
+ * (no counterpart in the reference, whose Devito autotuner is optional: common/devito.py:1043).
+ * It steps the plan's wavefield buffers, so it returns SA_E_INVALID while a saved wavefield
+ * (snapshots or checkpoints of a forward with save) waits for its adjoint. */
 int sa_autotune(sa_plan* plan, void* stream);
 
 /* Single-shot 2D forward modelling that allocates no device memory (no counterpart in the
@@ -161,7 +163,10 @@ int sa_autotune(sa_plan* plan, void* stream);
  * (unpadded extended grid), wavelets [n_src, nt] (as src.data) and traces [n_rec, nt] are
  * device pointers; src_xyz/rec_xyz are host [n, 2] coordinates, already shifted by +1e-3*h.
  * The first call on a device looks up the array's address with that device current: make it
- * before any stream capture. Calls share the array, so calls that overlap on the GPU race. */
+ * before any stream capture. Calls share the array, so calls that overlap on the GPU race.
+ * Every call synchronises `stream` twice while it prepares the point lists (it reads vp at the
+ * source corners back to the host), so it blocks the calling host thread; host src_xyz/rec_xyz
+ * are required (device pointers there return SA_E_INVALID). */
 int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const float* rho, const float* alpha, int n_src,
                           const float* src_xyz, const float* wavelets, int n_rec, const float* rec_xyz, float* traces,
                           void* stream);

@@ -133,6 +133,8 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
                              n_src ? wavelets : nullptr, n_rec ? traces : nullptr};
     for (const float* q : dev_in)
         if (q && !on_device(q)) return err(SA_E_INVALID, "medium, wavelets and traces must be device pointers");
+    if ((n_src && on_device(src_xyz)) || (n_rec && on_device(rec_xyz)))
+        return err(SA_E_INVALID, "src_xyz and rec_xyz must be host pointers (they are read on the host)");
 
     void* sbase = nullptr;
     int rc = scratch_address(&sbase);

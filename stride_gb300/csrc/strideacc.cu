@@ -128,6 +128,7 @@ struct sa_plan {
     int n_snap = 0;
     long long snap_stride = 0, snap_shot_stride = 0;
     bool snaps_valid = false;
+    bool adjoint_pending = false;  // a forward with save ran and no adjoint has used it yet
     bool snaps_raw = false;  // the snapshots hold p[t] (SA_SAVE_RAW), not p.dt2
     float *gradb = nullptr, *precb = nullptr;
     size_t cap_gradb = 0, cap_precb = 0;
@@ -1258,6 +1259,7 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
         p->snaps_raw = save_mode == SA_SAVE_RAW;
     }
     if (save_mode == SA_SAVE_CHECKPOINTS) p->ckpt_valid = true;
+    p->adjoint_pending = save_mode != SA_SAVE_NONE;
     return SA_OK;
 }
 
@@ -1412,6 +1414,7 @@ int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec
         }
     }
     p->launches = (p->n_rec ? 1 : 0) + p->adj_launches[am] + (rho ? 4 : 2);
+    p->adjoint_pending = false;
     return SA_OK;
 }
 }  // namespace
@@ -1419,6 +1422,9 @@ int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec
 int sa_autotune(sa_plan* p, void* stream) {
     if (p && p->p3) return SA_OK;  // 3D plans use a fixed tile (kTile3dY x kTile3dZ columns per CTA)
     if (!p || !p->geometry_set || !p->medium_set) return fail(SA_E_INVALID, "autotune needs medium and geometry");
+    if (p->adjoint_pending && (p->snaps_valid || p->ckpt_valid))
+        return fail(SA_E_INVALID, "autotune between a saving forward and its adjoint would discard the saved "
+                                  "wavefield: run the adjoint first");
     cudaStream_t s = (cudaStream_t)stream;
     const int S = p->ot4 ? 2 : 1;
     struct Cand {

@@ -25,6 +25,7 @@ Checksums of v2 structures are not verified.
 import datetime
 import mmap
 import os
+import tempfile
 import re
 import struct
 
@@ -98,6 +99,19 @@ class _Type:
         self.kind, self.size, self.dtype, self.members, self.charset = kind, size, dtype, members, charset
 
 
+class _Closed:
+    """The bytes of a closed File: any read raises a ValueError naming the file."""
+
+    def __init__(self, filename):
+        self.filename = filename
+
+    def __getitem__(self, key):
+        raise ValueError('HDF5 file %s is closed: load its datasets before closing it' % self.filename)
+
+    def __len__(self):
+        return 0
+
+
 class File:
     """Read-only view of an HDF5 file, memory-mapped (datasets are read when loaded); ``root`` is
     the root Group."""
@@ -119,9 +133,10 @@ class File:
         return node
 
     def close(self):
-        """Unmaps the file; datasets not yet loaded can no longer be read."""
+        """Unmaps the file; datasets not yet loaded can no longer be read (ValueError)."""
         if isinstance(self._b, mmap.mmap):
             self._b.close()
+        self._b = _Closed(self.filename)
 
     # ---- primitives
     def _u(self, pos, n):
@@ -503,7 +518,7 @@ class File:
 
 
 def read_file(filename):
-    """The root Group of an HDF5 file."""
+    """The root Group of an HDF5 file (its datasets read when loaded, from the file's mapping)."""
     return File(filename).root
 
 
@@ -679,8 +694,21 @@ def write_file(filename, description):
 
     oh, (btree, heap) = emit(tree)
     data = w.finish(oh, btree, heap)
-    with open(filename, 'wb') as fh:
-        fh.write(data)
+    # written beside the target and renamed over it: a File still mapping the old file keeps its
+    # inode, so its lazy datasets stay readable (truncating in place would fault their pages)
+    folder = os.path.dirname(os.path.abspath(filename))
+    fd, tmp = tempfile.mkstemp(prefix='.' + os.path.basename(filename) + '.', suffix='.tmp', dir=folder)
+    try:
+        with os.fdopen(fd, 'wb') as fh:
+            fh.write(data)
+        umask = os.umask(0)
+        os.umask(umask)
+        os.chmod(tmp, 0o666 & ~umask)  # the permissions open(filename, 'wb') would give
+        os.replace(tmp, filename)
+    except BaseException:
+        if os.path.exists(tmp):
+            os.unlink(tmp)
+        raise
 
 
 # ------------------------------------------------------------------------------------- mosaic's layer
@@ -819,8 +847,15 @@ class HDF5:
         if filter is not None:
             filter = {k: [v_ if isinstance(v_, str) else str(v_) for v_ in (v if isinstance(v, list) else [v])]
                       for k, v in filter.items()}
-        root = (self._file or File(self._filename)).root
-        return Struct(_read(root, lazy=lazy, filter=filter, only=only))
+        if self._file is not None:
+            return Struct(_read(self._file.root, lazy=lazy, filter=filter, only=only))
+        f = File(self._filename)  # mode 'w' / 'a': a view of the file as it is now
+        if lazy:
+            return Struct(_read(f.root, lazy=True, filter=filter, only=only))
+        try:  # everything read into memory: the mapping is not needed afterwards
+            return Struct(_read(f.root, lazy=False, filter=filter, only=only))
+        finally:
+            f.close()
 
     def dump(self, description):
         write_file(self._filename, description)

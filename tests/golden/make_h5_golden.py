@@ -21,7 +21,10 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from stride_gb300 import h5  # noqa: E402
 
-FIXTURE = '/root/reference/stride_examples/examples/breast2D/data/anastasio2D-TrueModel.h5'
+# the reference checkout's root: STRIDE_REFERENCE_ROOT, else a `reference` folder beside this repository
+REFERENCE_ROOT = os.environ.get('STRIDE_REFERENCE_ROOT',
+                                os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(HERE))), 'reference'))
+FIXTURE = os.path.join(REFERENCE_ROOT, 'stride_examples', 'examples', 'breast2D', 'data', 'anastasio2D-TrueModel.h5')
 OUT = os.path.join(HERE, 'anastasio2d_truemodel.json')
 
 

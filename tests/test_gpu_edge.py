@@ -89,3 +89,24 @@ def test_new_geometry_and_layout_independence():
     for a, b, d in zip(fresh, again, tuned):
         assert np.array_equal(a, b)
         assert np.array_equal(a, d)  # every point's arithmetic is the same in any launch shape
+
+
+def test_autotune_refuses_to_discard_a_saved_wavefield():
+    """sa_autotune steps the plan's wavefield buffers: between a saving forward and its adjoint it
+    returns SA_E_INVALID and the saved wavefield still gives the untuned gradient."""
+    c = C.small_case(kernel='OT4', density='none', n_shots=2, nt=160)
+    plan = C.make_plan(c)
+    got, plan = C.gpu_forward(c, plan=plan, save=True)
+    with pytest.raises(_lib.StrideAccError) as e:
+        plan.autotune()
+    assert e.value.code == _lib.SA_E_INVALID
+    res = np.ascontiguousarray(np.concatenate(got) * np.float32(0.5))
+    g1 = np.zeros(c['vp'].shape, np.float32)
+    p1 = np.zeros(c['vp'].shape, np.float32)
+    plan.adjoint(res, g1, p1)
+    plan.autotune()  # the saved wavefield has been used: allowed again
+    C.gpu_forward(c, plan=plan, save=True)
+    g2 = np.zeros(c['vp'].shape, np.float32)
+    p2 = np.zeros(c['vp'].shape, np.float32)
+    plan.adjoint(res, g2, p2)
+    assert np.array_equal(g1, g2) and np.array_equal(p1, p2)

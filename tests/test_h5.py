@@ -309,3 +309,47 @@ def test_fwi_state_dump_and_restart(tmp_path):
     # the model file is the reference's vp field description: inner data and grid
     d = h5.HDF5(project_name='inv', parameter='vp', path=str(tmp_path), version=2, mode='r').load(lazy=False)
     assert np.array_equal(d.data, models[2][inner]) and d.space.extra == (6, 6) and d.extended_shape == (40, 44)
+
+
+def test_rewrite_keeps_a_live_mapping_readable(tmp_path):
+    """A lazy dataset of an open file stays readable after the same file is appended to or dumped
+    over: the writer replaces the file instead of truncating the mapped one."""
+    fn = str(tmp_path / 'm.h5')
+    data = np.arange(4096, dtype=np.float32).reshape(64, 64)
+    h5.HDF5(fn, mode='w').dump({'data': data, 'name': 'a'})
+    reader = h5.HDF5(fn, mode='r')
+    lazy = reader.load(lazy=True)
+    h5.HDF5(fn, mode='a').append({'extra': np.ones(3)})
+    h5.HDF5(fn, mode='w').dump({'other': np.zeros(2)})
+    np.testing.assert_array_equal(lazy['data'][()], data)  # the old file's contents
+    reader.close()
+    assert list(h5.HDF5(fn, mode='r').load(lazy=False).keys()) == ['other']
+    assert oct(os.stat(fn).st_mode & 0o777) == oct(0o666 & ~_umask())
+
+
+def _umask():
+    m = os.umask(0)
+    os.umask(m)
+    return m
+
+
+def test_close_behaviour(tmp_path):
+    fn = str(tmp_path / 'c.h5')
+    h5.HDF5(fn, mode='w').dump({'data': np.arange(10.)})
+    f = h5.HDF5(fn, mode='r')
+    lazy = f.load(lazy=True)
+    f.close()
+    with pytest.raises(ValueError, match='closed'):
+        lazy['data'][()]
+    f.close()  # a second close is a no-op
+    # a non-lazy load through a writing handle reads everything and releases its mapping
+    got = h5.HDF5(fn, mode='a').load(lazy=False)
+    np.testing.assert_array_equal(got['data'], np.arange(10.))
+    # an empty file: opening fails on the superblock, closing a File over no bytes is a no-op
+    empty = str(tmp_path / 'empty.h5')
+    open(empty, 'wb').close()
+    with pytest.raises(Exception):
+        h5.File(empty)
+    obj = h5.File.__new__(h5.File)
+    obj._b, obj.filename = b'', empty
+    obj.close()

@@ -46,3 +46,37 @@ def test_shard_assignment_covers_all_shots_once():
     parts = [shards.shard_shots(ids, r, 3) for r in range(3)]
     assert sorted(sum(parts, [])) == ids
     assert parts[0] == [0, 3, 6, 9]
+
+
+def test_bench_launcher_starts_the_ranks():
+    """bench.launch_ranks (what `bench.py --gpus N` does when started without torchrun) runs N
+    ranks; their all-reduced per-shot sums equal the single-process sum over all shots."""
+    import json
+    import bench
+    from tests import _rank_sum
+    script = os.path.join(os.path.dirname(os.path.abspath(__file__)), '_rank_sum.py')
+    rc, out = bench.launch_ranks(2, [script], capture=True)
+    assert rc == 0
+    lines = [l for l in out.splitlines() if l.startswith('{')]
+    assert len(lines) == 1
+    got = json.loads(lines[0])
+    assert got['world'] == 2
+    full = sum(_rank_sum.per_shot(s) for s in range(7))
+    np.testing.assert_allclose(np.array(got['sum']), full, rtol=1e-5, atol=1e-5)
+
+
+def test_bench_reference_arm_under_two_ranks():
+    """`bench.py --impl reference --gpus 2` relaunches itself as two ranks; rank 0 alone prints the
+    reference arm's line, with n_gpus 2."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, 'bench.py'), '--impl', 'reference', '--gpus', '2',
+                        '--workload', 'single', '--nt', '40', '--steps', '1', '--warmup', '0'],
+                       stdout=subprocess.PIPE, text=True, timeout=600)
+    assert r.returncode == 0
+    lines = [l for l in r.stdout.splitlines() if l.startswith('{')]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line['impl'] == 'reference' and line['n_gpus'] == 2 and line['steps'] == 1
