@@ -458,20 +458,24 @@ def gb300_arm(args):
             fwd_ms.append((e0, e1))
             adj_ms.append((e1, e2))
 
+    torch.cuda.nvtx.range_push('warmup')
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
     launches['n'] = 0
     with ClockSampler(local) as clk:
         t0, t1 = ev(), ev()
+        torch.cuda.nvtx.range_push('timed')  # a profiler can restrict its capture to this range
         t0.record(stream)
         for _ in range(args.steps):
             step(timed=True)
         t1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
     if world > 1:
         dist.barrier()
     ms = t0.elapsed_time(t1)
@@ -553,6 +557,7 @@ def gb300_arm(args):
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded phantoms)',
             'config': {'workload': workload_name(args.workload, nt), 'grid': list(w['shape']),
                        'shots_per_gpu': n_shots, 'nt': nt, 'kernel': 'OT4',
+                       'layout': dict(zip(('threads', 'strips', 'chunks'), plan.layout)),
                        'gradient': (method + (' (adjoint time includes the forward recompute from checkpoints)'
                                               if method != 'snapshots' else '')) if grad_mode else None,
                        'parallelism': 'shots sharded over %d GPU(s)%s' % (world, ', gradient all-reduce' if grad_mode else ''),

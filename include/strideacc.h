@@ -155,8 +155,8 @@ int sa_autotune(sa_plan* plan, void* stream);
 /* Single-shot 2D forward modelling that allocates no device memory (no counterpart in the
  * reference). For callers that cannot let a library allocate GPU memory, e.g. an application
  * whose memory pool owns the whole device, or a loop that must not pay the device-wide
- * synchronisation of cudaFree. It runs the same time-step kernel as sa_forward with every
- * scratch buffer in one 32 MiB __device__ array of the library (held by each GPU that loads the
+ * synchronisation of cudaFree. It runs the same time-step kernels as sa_forward with every
+ * scratch buffer in one 64 MiB __device__ array of the library (held by each GPU that loads the
  * library until exit). Limits: extended grid at most 640 x 640, 16 sources, 1024 receivers,
  * and everything must fit the array (else SA_E_INVALID). desc gives the grid, dt, nt, kernel,
  * density and attenuation modes (max_shots and undersampling are not used). vp/rho/alpha
@@ -284,6 +284,11 @@ int sa_last_error(char* buf, int len);
 
 /* Kernel launches the last sa_forward/sa_adjoint issued (for throughput accounting). */
 long long sa_launch_count(const sa_plan* plan);
+
+/* The launch layout of a 2D plan's time-step passes (after sa_autotune, the tuned one): threads
+ * per CTA (two grid columns each), column strips and row chunks of the grid; 3D plans report
+ * their fixed tile as threads and 0 strips and chunks. No counterpart in the reference. */
+int sa_plan_layout(const sa_plan* plan, int* threads, int* strips, int* chunks);
 
 /* The checkpoint schedule sa_forward(SA_SAVE_CHECKPOINTS) takes for n_shots shots of a plan with
    description d (its checkpoint_interval, checkpoint_budget, grid, nt, undersampling, boundary):

@@ -38,7 +38,7 @@ SA_GRAD_EXACT = 1
 # every symbol include/strideacc.h declares
 EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometry', 'sa_forward',
            'sa_adjoint', 'sa_adjoint_wavelets', 'sa_adjoint_grads', 'sa_autotune', 'sa_last_error', 'sa_launch_count',
-           'sa_checkpoint_schedule',
+           'sa_plan_layout', 'sa_checkpoint_schedule',
            'sa_forward_2d_noalloc',
            'sa_traces_sosfilt', 'sa_traces_fir', 'sa_traces_check', 'sa_traces_norm_per_shot', 'sa_traces_mute',
            'sa_field_mul', 'sa_field_clip', 'sa_field_axpy', 'sa_field_slowness_step', 'sa_field_stats',
@@ -89,6 +89,7 @@ def load():
     lib.sa_launch_count.argtypes = [P]
     lib.sa_launch_count.restype = ctypes.c_longlong
     IP = ctypes.POINTER(I)
+    lib.sa_plan_layout.argtypes = [P, IP, IP, IP]
     lib.sa_checkpoint_schedule.argtypes = [ctypes.POINTER(SaDesc), I, IP, IP, IP]
     L = ctypes.c_longlong
     F = ctypes.c_float
@@ -270,3 +271,10 @@ class Plan:
     @property
     def launches(self):
         return int(load().sa_launch_count(self._h))
+
+    @property
+    def layout(self):
+        """(threads per CTA, column strips, row chunks) of the time-step launches."""
+        t, s, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(load().sa_plan_layout(self._h, ctypes.byref(t), ctypes.byref(s), ctypes.byref(c)))
+        return t.value, s.value, c.value

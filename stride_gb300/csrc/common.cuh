@@ -53,30 +53,39 @@ struct Gather {
     float w00, w01, w10, w11;
 };
 
-// Arguments of one 2D time step over a batch of shots.
+// Arguments of one 2D time step over a batch of shots (the passes of fdtd2d.cuh).
 struct Step2D {
-    int nx, ny, pitch;        // extended grid, row pitch (columns)
-    long long shot_stride;    // float2 elements per shot pair in a field buffer (nx * pitch)
-    int chunk_rows;           // output rows per CTA
-    int by;                   // output columns per CTA (even, <= Cols2D::BYMAX)
-    int t;                    // time index of the current level (cur = p[t])
-    const float* cur;         // p[t] of shot pairs, interleaved: [pairs][nx][pitch][2]
-    float* prev;              // other level in, new level out (in place)
-    // medium (shared by all shots); pointers address row 0, GUARD zero rows on both sides
-    const float* W;           // node coefficient: vp^2 (density none/constant) or vp^2 rho
-    const float* bxh;         // buoyancy at (x+1/2, y), half-rows -5..nx+3 valid
-    const float* byh;         // buoyancy at (x, y+1/2): column y+6 holds y = -6..ny+3
-    int pitch_b;
-    const float* C1;          // update p_new = C1 Lt + C2 p - C3 p_other (damping, attenuation)
-    const float* C2;
-    const float* C3;
-    float hx, hy;             // spacing
-    float dt;
-    // wavefield save (forward); sources, receivers and the imaging condition are separate kernels
-    int f;                    // undersampling factor
-    int save;                 // forward, on t % f == 0: 1 stores p.dt2, 2 stores p[t] itself
-    float* snaps;             // [pairs][n_snap][nx][pitch][2]
+    int nx, ny, pitch;         // extended grid, field row pitch (columns)
+    long long shot_stride;     // float2 elements per shot pair in a field buffer (nx * pitch)
+    int chunk_rows;            // output rows per CTA
+    int by;                    // output columns per CTA (even, at most twice the threads)
+    int t;                     // time index of the current level (cur = p[t])
+    const float* cur;          // p[t] of shot pairs, interleaved: [pairs][nx][pitch][2]
+    float* prev;               // other level in, new level out (in place)
+    float* lbuf;               // OT4: l = W G(p[t]) of the first pass (same layout; zero beyond ny)
+    // medium duplicated per pair: point (x, y) of array m is the float2 {v, v} at m[x * mpitch + y]
+    // (pointers at row 0, column 0; DUP_GUARD rows above and below, DUP_MARGIN columns left and right)
+    const float2* Wd;          // vp^2 (density none or constant) or vp^2 rho
+    const float2* bxd;         // buoyancy at (x + 1/2, y)
+    const float2* byd;         // buoyancy at (x, y + 1/2)
+    const float2* C1d;         // new = C1 Lt + C2 p + NC3 p_other, NC3 = -C3 (damping, attenuation)
+    const float2* C2d;
+    const float2* NC3d;
+    int mpitch;                // float2 per medium row
+    int ymax;                  // largest (even) medium column a thread may address
+    float2 wx[6], wy[6];       // FD weights over h (staggered: 5) or over h^2 (laplace: 6), {w, w}
+    float k12;                 // dt^2 / 12
+    int wg_only;               // 1: new level = W G(p[t]) (OT2; the exact adjoint's W G pass)
+    int f;                     // undersampling factor
+    int save;                  // forward, on t % f == 0: 1 stores p.dt2, 2 stores p[t] itself
+    float inv_dt2;
+    float* snaps;              // [pairs][n_snap][nx][pitch][2]
     long long snap_shot_stride, snap_stride;  // in float2 elements: per pair, per snapshot
 };
+
+constexpr int DUP_GUARD = 40;   // rows of the duplicated medium beyond the grid, each side
+constexpr int DUP_MARGIN = 32;  // columns of the duplicated medium beyond the grid, each side
+constexpr int STEP_MAX_THREADS = 128;  // threads per CTA of the 2D passes (two columns each), at most
+constexpr int STEP_MIN_THREADS = 16;   // and at least
 
 }  // namespace sa

@@ -1,25 +1,37 @@
-// 2D iso-acoustic FDTD time step for sm_103a: one launch advances every shot of a batch by one
-// time level. Restates the Devito operator that IsoAcousticDevito builds
-// (stride/physics/iso_acoustic/devito.py:1466-1608) as a streaming kernel:
+// 2D iso-acoustic FDTD time step for sm_103a: two streaming passes advance every shot pair of a
+// batch by one time level.
 //
-//  * a CTA owns a strip of `by` output columns (the contiguous y axis) and a chunk of rows of
-//    one shot, and streams the rows of the current level p[t] through shared memory one row
-//    per iteration (coalesced row loads, zero halo beyond the grid as Devito's p halo);
-//  * derivatives along the streamed x axis come from per-thread register queues (2.5D
-//    streaming), derivatives along y from the shared row;
-//  * OT4 (L + dt^2/12 L(L p)) is fused: the first application's rows feed a second pipeline
-//    stage `R` rows behind, so the intermediate never touches memory;
-//  * the sponge damping (boundaries/devito.py:49-67) is evaluated on the fly from two 1D
-//    ramps, attenuation (devito.py:1536-1548) from alpha, the update solves
-//    p.dt2 - Lt + 2 a vp p.dt + vp^2 (2 d p.dtc + d^2 p) = 0 (devito.py:1575-1581);
-//  * the undersampled save of p.dt2 or of p itself (:398-418) is a fused epilogue; source injection (:357-363),
-//    receiver interpolation (:364), the adjoint receiver injection (:748-753) and the vp imaging
-//    condition (:1000-1024) run as their own kernels after the step (helpers.cu), which kept
-//    their irregular loads out of the stencil's loop.
+// Restates the Devito operator that IsoAcousticDevito builds (stride/physics/iso_acoustic/
+// devito.py:1466-1608): p.dt2 - Lt + 2 a vp p.dt + vp^2 (2 d p.dtc + d^2 p) = 0 solved for the new
+// level (:1575-1581), Lt = W G(p) (OT2) or l + dt^2/12 W G(l) with l = W G(p) (OT4, :1503-1534),
+// G the 10th-order Laplacian (rho absent) or the staggered div(b grad) (:1655-1665), W = vp^2 or
+// vp^2 rho. As Devito materialises its `laplacian` Function, OT4 runs two passes: pass L writes
+// l (zero beyond the grid) and pass U applies G to l and updates the level; OT2 runs pass U on
+// p itself. Sources, receivers and the imaging condition run as their own kernels after a step.
 //
-// The new level is written in place of the older one (each point's p[t-1] is read only by
-// the thread that writes p[t+1] there), so a shot needs two field buffers.
+// Work assignment of a pass. A CTA owns a strip of output columns, a chunk of rows and one shot
+// pair; each thread owns two adjacent columns (c, c + 1, c even), so every value it handles is a
+// float4 {col c shot 0, col c shot 1, col c+1 shot 0, col c+1 shot 1} of the pair-interleaved
+// field layout and all arithmetic is the packed FP32 pairs of the sm_100 family. Rows of the
+// pass input stream through the CTA (2.5D):
+//   * derivatives along the streamed x axis come from per-thread register queues whose slots
+//     rotate by compile-time index: the row loop is unrolled over the queue period P, so a new
+//     row costs no register moves;
+//   * derivatives along y read 12-column windows of the shared input row as six 16-byte loads
+//     (the windows of a thread's two columns overlap in 11 columns); the staggered operator's
+//     y-fluxes are computed once per half-column and exchanged through a double-buffered shared
+//     row, with one barrier per row;
+//   * input rows arrive by cp.async (zero-fill beyond the grid: Devito's zero halo of p and of
+//     `laplacian`) PF rows ahead; the update's p[t] / p[t-1] values by per-thread cp.async PF2
+//     rows ahead; each medium value is loaded one row ahead of its use;
+//   * the medium is pre-duplicated per pair ({v, v} per point), so one 16-byte load gives the
+//     packed operand of both columns.
+// The new level is written in place of p[t-1] (each point's old value is read only by the
+// thread that writes its new value). The undersampled save of p.dt2 or of p (:398-418) is a
+// fused epilogue of pass U.
 #pragma once
+#include <utility>
+
 #include "common.cuh"
 
 namespace sa {
@@ -35,366 +47,394 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 
 __host__ __device__ constexpr int round4(int x) { return (x + 3) / 4 * 4; }
 
-// ---- arithmetic on the two lanes of a shot pair ---------------------------------------------
-// SA_PACKED=1 issues the sm_100-family f32x2 instructions (one instruction for both shots;
-// 4 % faster on the 64-shot gradient); 0 issues two scalar FP32 instructions, which take
-// immediate operands (the FD weights) without register pairs. Both round identically.
-#ifndef SA_PACKED
-#define SA_PACKED 1
-#endif
+// ---- packed FP32 arithmetic on the two shots of a pair (one sm_100-family f32x2 instruction) --
 __device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
-#if SA_PACKED
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
-#else
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-    return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
-}
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return make_float2(a.x * b.x, a.y * b.y); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-#endif
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }  // exact a - b
 
-// Staggered first derivative sum_m w_m (v[hi+m] - v[lo-m]) over float2 values (queue or shared).
-template <class A>
-__device__ __forceinline__ float2 dstag2(const A& v, int hi, int lo) {
-    float2 a = mul2(f2(kWS(0)), v[hi]);
-    float2 b = mul2(f2(kWS(0)), v[lo]);
+// Two columns (c, c + 1) of a shot pair.
+struct Col2 {
+    float2 a, b;
+};
+__device__ __forceinline__ Col2 as_col2(float4 v) { return {make_float2(v.x, v.y), make_float2(v.z, v.w)}; }
+__device__ __forceinline__ float4 as_f4(Col2 v) { return make_float4(v.a.x, v.a.y, v.b.x, v.b.y); }
+__device__ __forceinline__ Col2 ld_c2(const float4* p) { return as_col2(*p); }
+__device__ __forceinline__ Col2 zero_c2() { return {f2(0.f), f2(0.f)}; }
+__device__ __forceinline__ Col2 add_c2(Col2 x, Col2 y) { return {add2(x.a, y.a), add2(x.b, y.b)}; }
+__device__ __forceinline__ Col2 mul_c2(Col2 x, Col2 y) { return {mul2(x.a, y.a), mul2(x.b, y.b)}; }
+__device__ __forceinline__ Col2 fma_c2(Col2 x, Col2 y, Col2 z) { return {fma2(x.a, y.a, z.a), fma2(x.b, y.b, z.b)}; }
+
+// Staggered first derivative along a queue: sum_m w[m] (q[(K + HI + m) % P] - q[(K + LO - m) % P]).
+template <int P, int K, int HI, int LO>
+__device__ __forceinline__ Col2 qstag(const Col2 (&q)[P], const float2 (&w)[6]) {
+    constexpr int h0 = ((K + HI) % P + P) % P, l0 = ((K + LO) % P + P) % P;
+    Col2 acc;
+    acc.a = mul2(w[0], sub2(q[h0].a, q[l0].a));
+    acc.b = mul2(w[0], sub2(q[h0].b, q[l0].b));
 #pragma unroll
     for (int m = 1; m < 5; m++) {
-        a = fma2(f2(kWS(m)), v[hi + m], a);
-        b = fma2(f2(kWS(m)), v[lo - m], b);
+        const int h = ((K + HI + m) % P + P) % P, l = ((K + LO - m) % P + P) % P;
+        acc.a = fma2(w[m], sub2(q[h].a, q[l].a), acc.a);
+        acc.b = fma2(w[m], sub2(q[h].b, q[l].b), acc.b);
     }
-    return sub2(a, b);
+    return acc;
 }
-// Centred second derivative sum_k w_k (v[c+k] + v[c-k]) + w_0 v[c].
-template <class A>
-__device__ __forceinline__ float2 dcent2(const A& v, int cidx) {
-    float2 a = mul2(f2(kW2(0)), v[cidx]);
+// Centred second derivative along a queue about slot (K + C) % P.
+template <int P, int K, int C>
+__device__ __forceinline__ Col2 qcent(const Col2 (&q)[P], const float2 (&w)[6]) {
+    constexpr int c0 = ((K + C) % P + P) % P;
+    Col2 acc;
+    acc.a = mul2(w[0], q[c0].a);
+    acc.b = mul2(w[0], q[c0].b);
 #pragma unroll
-    for (int k = 1; k <= 5; k++) a = fma2(f2(kW2(k)), add2(v[cidx + k], v[cidx - k]), a);
-    return a;
+    for (int k = 1; k <= 5; k++) {
+        const int h = ((K + C + k) % P + P) % P, l = ((K + C - k) % P + P) % P;
+        acc.a = fma2(w[k], add2(q[h].a, q[l].a), acc.a);
+        acc.b = fma2(w[k], add2(q[h].b, q[l].b), acc.b);
+    }
+    return acc;
 }
 
-// Column layout of one CTA: thread t owns column c = L1 + t; every value is a float2 holding
-// the same grid point of the two shots of a shot pair.
-template <int KIND, bool OT4, int NT>
-struct Cols2D {
-    static constexpr bool STAG = KIND != 0;
-    static constexpr int R = STAG ? 9 : 5;            // radius of one operator application
-    static constexpr int S = OT4 ? 2 : 1;             // pipeline stages
-    static constexpr int H1 = (S - 1) * R;            // halo of the stage-1 output columns
-    static constexpr int BYMAX = NT - 2 * H1;         // output columns
+// Staggered y-fluxes at half-columns 4 and 5 of a 12-column window of a shared row (float2 per
+// column, window start at float4 index k): F(h) = sum_m w[m] (v[h + 1 + m] - v[h - m]).
+__device__ __forceinline__ Col2 yflux_pair(const float4* row, int k, const float2 (&w)[6]) {
+    float2 v[12];
+#pragma unroll
+    for (int e = 0; e < 6; e++) {
+        const float4 q = row[k + e];
+        v[2 * e] = make_float2(q.x, q.y);
+        v[2 * e + 1] = make_float2(q.z, q.w);
+    }
+    Col2 acc;
+    acc.a = mul2(w[0], sub2(v[5], v[4]));
+    acc.b = mul2(w[0], sub2(v[6], v[5]));
+#pragma unroll
+    for (int m = 1; m < 5; m++) {
+        acc.a = fma2(w[m], sub2(v[5 + m], v[4 - m]), acc.a);
+        acc.b = fma2(w[m], sub2(v[6 + m], v[5 - m]), acc.b);
+    }
+    return acc;
+}
+// D- along y at window columns 6 and 7 from a 12-entry flux window f starting at float4 index k0:
+// D = sum_m w[m] (f[6 + m] - f[5 - m]) (flux f[e] at the half-column after window column e).
+__device__ __forceinline__ Col2 ydiv_pair(const float4* frow, int k0, const float2 (&w)[6]) {
+    float2 v[12];
+#pragma unroll
+    for (int e = 0; e < 6; e++) {
+        const float4 q = frow[k0 + e];
+        v[2 * e] = make_float2(q.x, q.y);
+        v[2 * e + 1] = make_float2(q.z, q.w);
+    }
+    Col2 acc;
+    acc.a = mul2(w[0], sub2(v[6], v[5]));
+    acc.b = mul2(w[0], sub2(v[7], v[6]));
+#pragma unroll
+    for (int m = 1; m < 5; m++) {
+        acc.a = fma2(w[m], sub2(v[6 + m], v[5 - m]), acc.a);
+        acc.b = fma2(w[m], sub2(v[7 + m], v[6 - m]), acc.b);
+    }
+    return acc;
+}
+// Centred second derivative along y at window columns 6 and 7 of a 14-column window starting at
+// float4 index k0.
+__device__ __forceinline__ Col2 ycent_pair(const float4* row, int k0, const float2 (&w)[6]) {
+    float2 v[14];
+#pragma unroll
+    for (int e = 0; e < 7; e++) {
+        const float4 q = row[k0 + e];
+        v[2 * e] = make_float2(q.x, q.y);
+        v[2 * e + 1] = make_float2(q.z, q.w);
+    }
+    Col2 acc;
+    acc.a = mul2(w[0], v[6]);
+    acc.b = mul2(w[0], v[7]);
+#pragma unroll
+    for (int k = 1; k <= 5; k++) {
+        acc.a = fma2(w[k], add2(v[6 + k], v[6 - k]), acc.a);
+        acc.b = fma2(w[k], add2(v[7 + k], v[7 - k]), acc.b);
+    }
+    return acc;
+}
+
+template <int... K, class F>
+__device__ __forceinline__ void unroll_period(std::integer_sequence<int, K...>, F&& f) {
+    (f(std::integral_constant<int, K>{}), ...);
+}
+
+// What a pass computes.
+enum PassMode : int {
+    PASS_L = 0,   // l = W G(p[t]) into Step2D::lbuf (OT4's first pass)
+    PASS_U4 = 1,  // new = C1 (l + dt^2/12 W G(l)) + C2 p[t] - C3 p[t-1] (OT4's second pass)
+    PASS_U2 = 2,  // new = C1 W G(p[t]) + C2 p[t] - C3 p[t-1], or W G(p[t]) with wg_only (OT2)
 };
 
-// Shared-memory layout of one CTA, in float2 units.
-template <int KIND, bool OT4, int NT, int RB, int PF>
-struct Smem2D {
-    using C = Cols2D<KIND, OT4, NT>;
-    static constexpr bool STAG = C::STAG;
-    static constexpr int R = C::R, S = C::S;
-    static constexpr int C0 = NT + 2 * R;                 // u columns [L0, L0 + C0)
-    static constexpr int WU = ((C0 + 1 + 1) & ~1) + 2;    // u row from floor2(L0), even
-    static constexpr int QU = S * R + RB * (PF + 1);      // u rows kept: o .. i + RB*(PF+1) - 1
-    static constexpr int QLR = R + RB;                    // rows of the intermediate kept (OT4)
-    static constexpr int WL = NT + 2;
-    static constexpr int WF = NT + 10;
-    static constexpr int oU = 0;
-    static constexpr int oL = oU + QU * WU;
-    // y-flux rows of both stages, double-buffered by iteration parity (written before the
-    // iteration's barrier, read after it)
-    static constexpr int oF = oL + (OT4 ? QLR * WL : 0);
-    static constexpr int oF2 = oF + (STAG ? 2 * RB * WF : 0);
-    static constexpr int total = oF2 + ((OT4 && STAG) ? 2 * RB * WF : 0);
-    static constexpr size_t bytes = (size_t)total * sizeof(float2);
-};
-
-// Register queue shift by RB (the oldest RB entries leave).
-template <int QL, int RB>
-__device__ __forceinline__ void qshift(float2 (&q)[QL]) {
-#pragma unroll
-    for (int k = 0; k + RB < QL; k++) q[k] = q[k + RB];
-}
-
-#ifndef SA_MINBLOCKS
-#define SA_MINBLOCKS 3  // CTAs per SM the register allocation must allow (latency hiding)
+#ifndef SA_PASS_MINB
+#define SA_PASS_MINB 3
 #endif
-// CTAs per SM the register budget is sized for: SA_MINBLOCKS up to 192 threads (the OT2 kernels
-// fit three CTAs of 192), two for the 256-thread CTA (whose three would leave 85 registers)
-__host__ __device__ constexpr int step_min_blocks(int nt) { return nt <= 192 ? SA_MINBLOCKS : 2; }
 
-template <int KIND, bool OT4, int NT, int RB, int PF>
-__global__ void __launch_bounds__(NT, step_min_blocks(NT)) fdtd2d_step(const __grid_constant__ Step2D a) {
-    using L = Smem2D<KIND, OT4, NT, RB, PF>;
-    using CL = Cols2D<KIND, OT4, NT>;
-    constexpr bool STAG = CL::STAG;           // staggered div(b grad) operator
-    constexpr bool VARB = KIND == 1;          // variable buoyancy
-    constexpr int R = CL::R, S = CL::S, H1 = CL::H1;
-    constexpr int QU = L::QU, QLR = L::QLR;
-    // register queues along x: u rows i-QB..i+RB-1; fluxes at half-rows i-QB-5..i-6+RB (STAG)
-    constexpr int QB = STAG ? 9 : 10;
-    constexpr int QL = QB + RB;
+// Geometry of a pass CTA of nt threads (nt <= STEP_MAX_THREADS, runtime): operator kind fixes
+// the reach, the mode which per-thread update rings exist. Shared memory in float4 units.
+template <int KIND, int MODE>
+struct PassCfg {
+    static constexpr bool STAG = KIND != 0;    // staggered div(b grad) operator
+    static constexpr bool VARB = KIND == 1;    // variable buoyancy
+    static constexpr int R = STAG ? 9 : 5;     // rows / columns of one operator application
+    static constexpr int P = STAG ? 10 : 11;   // rows per period of the register queues
+    static constexpr int UL = STAG ? 10 : 6;   // input columns left of the thread columns
+    static constexpr int UX = STAG ? 10 : 7;   // float4 of an input row beyond the threads'
+    static constexpr int QU = 16;              // shared input rows (ring)
+    static constexpr int PF = 3;               // input rows prefetched ahead (QU >= R + PF + 1)
+    static constexpr int QC = 4;               // rows of the update's p[t] / p[t-1] ring
+    static constexpr int PF2 = 3;              // update rows prefetched ahead (PF <= PF2 < QC)
+    static constexpr bool HAS_C = MODE == PASS_U4;  // p[t] ring (U2 takes p[t] from its input queue)
+    static constexpr bool HAS_P = MODE != PASS_L;   // p[t-1] ring
+    __host__ __device__ static constexpr int WU(int nt) { return nt + UX; }
+    __host__ __device__ static constexpr int NF(int nt) { return STAG ? nt + 5 : 0; }
+    __host__ __device__ static constexpr int oF(int nt) { return QU * WU(nt); }
+    __host__ __device__ static constexpr int oC(int nt) { return oF(nt) + 2 * NF(nt); }
+    __host__ __device__ static constexpr int oP(int nt) { return oC(nt) + (HAS_C ? QC * nt : 0); }
+    __host__ __device__ static constexpr int total(int nt) { return oP(nt) + (HAS_P ? QC * nt : 0); }
+    __host__ __device__ static constexpr size_t bytes(int nt) { return (size_t)total(nt) * sizeof(float4); }
+    static_assert(QU >= R + PF + 1 && (QU & (QU - 1)) == 0, "input ring");
+    static_assert(PF2 >= PF && PF2 < QC && (QC & (QC - 1)) == 0, "update ring");
+    static_assert(P % 2 == 0 || !STAG, "flux buffers alternate by the parity of the period slot");
+};
 
-    extern __shared__ __align__(16) float2 smem2[];
-    float2* const sU = smem2 + L::oU;
-    float2* const sLr = smem2 + L::oL;
-    float2* const sF = smem2 + L::oF;
-    float2* const sF2 = smem2 + L::oF2;
+// The medium values one iteration of a pass uses: each is reloaded for the next iteration right
+// after its last use, so the loads are in flight for a whole row.
+struct PassMedium {
+    Col2 by, byb;      // buoyancy at the y-flux half-columns of the thread's pair (and its extra pair)
+    Col2 bx;           // buoyancy at the x-flux half-row
+    Col2 W;            // W at the output row
+    Col2 c1, c2, nc3;  // update coefficients at the output row
+};
+
+template <int KIND, int MODE>
+__global__ void __launch_bounds__(STEP_MAX_THREADS, SA_PASS_MINB) fdtd2d_pass(const __grid_constant__ Step2D a) {
+    using CF = PassCfg<KIND, MODE>;
+    constexpr bool STAG = CF::STAG, VARB = CF::VARB;
+    constexpr int R = CF::R, UL = CF::UL, P = CF::P, QU = CF::QU, PF = CF::PF, QC = CF::QC, PF2 = CF::PF2;
+
+    const int NT = blockDim.x;
+    const int WU = CF::WU(NT), NF = CF::NF(NT);
+    extern __shared__ __align__(16) float4 smem4[];
+    float4* const sU = smem4;
+    float4* const sF = smem4 + CF::oF(NT);
+    float4* const sC = smem4 + CF::oC(NT);
+    float4* const sP = smem4 + CF::oP(NT);
 
     const int tid = threadIdx.x;
     const int strip = blockIdx.x, chunk = blockIdx.y, pair = blockIdx.z;
-    const int BY = a.by;
-    const int y0 = strip * BY;
-    const int L1 = y0 - H1;                   // first stage-1 output column
-    const int L0 = L1 - R;                    // first stage-1 input column
-    const int QU0 = L0 & ~1;                  // u rows start at an even column (16-byte copies)
-    const int c = L1 + tid;                   // this thread's column
-    const bool c_in = (c >= 0) && (c < a.ny);
-    const bool out_col = (tid >= H1) && (tid < H1 + BY) && c_in;
-    const int cc = min(max(c, 0), a.ny - 1);
+    const int y0 = strip * a.by;
+    const int BY = min(a.by, a.ny - y0);       // output columns of this strip
+    const int L0 = y0 - UL;                    // column of shared input index 0 (even)
+    const int c = y0 + 2 * tid;                // this thread's columns c, c + 1
     const int xo0 = chunk * a.chunk_rows;
     const int xo1 = min(a.nx, xo0 + a.chunk_rows);
-    const int i0 = xo0 - S * R, i1 = xo1 + S * R;
-    const int pitch = a.pitch, pitch_b = a.pitch_b;
+    const int i0 = xo0 - R;                    // first input row streamed
+    const int niter = (xo1 - xo0) + 2 * R;     // rows streamed; row i0 + n - R is output from n = 2R
+    const int pitch = a.pitch;
 
-    const long long poff = (long long)pair * a.shot_stride;  // float2 elements per pair: nx*pitch
-    const float2* __restrict__ cur = reinterpret_cast<const float2*>(a.cur);
-    float2* __restrict__ prev = reinterpret_cast<float2*>(a.prev) + poff;
+    const bool out_t = 2 * tid < BY;           // output columns of this thread
+    const bool out1 = out_t && c + 1 < a.ny;
+    const int cm = min(c, a.ymax);             // medium column (clamped beyond the grid)
 
+    const long long poff = (long long)pair * a.shot_stride * 2;  // floats per pair
+    const float* __restrict__ in = (MODE == PASS_U4 ? a.lbuf : a.cur) + poff;
+    const float* __restrict__ cur = a.cur + poff;
+    float* __restrict__ prev = a.prev + poff;
+    float* __restrict__ outp = (MODE == PASS_L ? a.lbuf : a.prev) + poff;
 
-    const float2 ihx = f2(1.f / a.hx), ihy = f2(1.f / a.hy);
-    const float2 ihx2 = f2(1.f / (a.hx * a.hx)), ihy2 = f2(1.f / (a.hy * a.hy));
-    const float dt2 = a.dt * a.dt;
-    const float2 k12 = f2((float)((double)a.dt * (double)a.dt / 12.0));
-
-    // per-thread medium pointers at row 0 of this thread's column (GUARD zero rows make rows
-    // beyond the grid addressable; their values only reach discarded lanes)
-    const float* __restrict__ pW = a.W + cc;
-    const float* __restrict__ pBX = a.bxh + cc;
-    // byh storage column of half-col h is h + 6
-    const int kb1 = min(max(L1 + 1 + tid, 0), pitch_b - 1);        // stage-1 flux k = tid
-    const int kb1b = min(max(L1 + 1 + NT + tid, 0), pitch_b - 1);  // stage-1 flux k = NT + tid
-    const int kb2 = min(max(y0 + 1 + tid, 0), pitch_b - 1);        // stage-2 flux k = tid
-    const float* __restrict__ pC1 = a.C1 + cc;
-    const float* __restrict__ pC2 = a.C2 + cc;
-    const float* __restrict__ pC3 = a.C3 + cc;
-
-    // u ring: row r in slot (r - i0) mod QU
-    constexpr int NQU = L::WU / 2;  // 16-byte copies (2 columns x 2 shots)
-    auto wrapU = [](int sl) { return sl < 0 ? sl + QU : (sl >= QU ? sl - QU : sl); };
-    auto rowU = [&](int sl) { return sU + sl * L::WU - QU0; };  // rowU(s)[col] = u(row, col)
-    int sI = 0;  // slot of row i
-    auto prefetch = [&](int ii, int slot) {
+    float2 wx[6], wy[6];
 #pragma unroll
-        for (int rr = 0; rr < RB; rr++) {
-            const int r = ii + rr;
-            if (r < i1) {
-                float2* dst = sU + wrapU(slot + rr) * L::WU;
-                const bool row_ok = r >= 0 && r < a.nx;
-                const float2* rowp = cur + poff + (long long)r * pitch;
-                for (int k = tid; k < NQU; k += NT) {
-                    const int q = QU0 + 2 * k;
-                    const bool ok = row_ok && q >= 0 && q + 2 <= pitch;
-                    cp_async16(dst + 2 * k, ok ? rowp + q : cur, ok);
-                }
-            }
-        }
-        cp_async_commit();
-    };
-
-    float2 uq[QL], fq[STAG ? QL : 1], lq[OT4 ? QL : 1], f2q[(OT4 && STAG) ? QL : 1];
-#pragma unroll
-    for (int k = 0; k < QL; k++) {
-        uq[k] = f2(0.f);
-        if constexpr (STAG) fq[k] = f2(0.f);
-        if constexpr (OT4) {
-            lq[k] = f2(0.f);
-            if constexpr (STAG) f2q[k] = f2(0.f);
-        }
+    for (int m = 0; m < 6; m++) {
+        wx[m] = a.wx[m];
+        wy[m] = a.wy[m];
     }
-    const bool do_save = a.save && (a.t % a.f == 0);
+    const bool do_save = MODE != PASS_L && a.save && (a.t % a.f == 0);
 
-#pragma unroll 1
-    for (int k = 0; k < PF; k++) prefetch(i0 + k * RB, wrapU(k * RB % QU));
-
-    int sJ = 0;  // ring slot of intermediate row j (slot of row x is (x - (i0 - R)) mod QLR)
-    auto wrapL = [](int sl) { return sl < 0 ? sl + QLR : (sl >= QLR ? sl - QLR : sl); };
-    int par = 0;  // flux buffer of this iteration
-    // One barrier per iteration. Before it, the y-fluxes of both stages are computed from rows
-    // that became visible in earlier iterations (u rows j.., intermediate rows o..) into this
-    // iteration's flux buffers; after it, the rows that just landed (cp.async) and the fluxes
-    // are read. Ring slots written after the barrier (new intermediate rows, prefetched u rows)
-    // hold rows no thread reads before the next barrier.
-#pragma unroll 1
-    for (int i = i0; i < i1; i += RB) {
-        const int j = i - R;        // first stage-1 output row of this iteration
-        const int o = i - S * R;    // first output row of this iteration
-        // ---- stage-1 medium, stage-2 y medium -----------------------------------------
-        float Wj[RB], bxi[RB], by1[RB], by1b[RB], by2[RB];
-#pragma unroll
-        for (int r = 0; r < RB; r++) {
-            Wj[r] = __ldg(pW + (long long)(j + r) * pitch);
-            if constexpr (VARB) {
-                bxi[r] = __ldg(pBX + (long long)(i - 5 + r) * pitch);
-                const float* byr = a.byh + (long long)(j + r) * pitch_b;
-                by1[r] = __ldg(byr + kb1);
-                by1b[r] = tid < 9 ? __ldg(byr + kb1b) : 0.f;
-                if constexpr (OT4) by2[r] = __ldg(a.byh + (long long)(o + r) * pitch_b + kb2);
-            }
+    // ---- prefetch of input rows (whole CTA) and of the update's p[t] / p[t-1] (own columns) ---
+    // input-row copies of this thread: float4 k = tid and k = tid + NT (< WU), columns L0 + 2k,
+    // L0 + 2k + 1, zero-filled outside the row's pitch
+    const bool has2 = tid + NT < WU;
+    const int q1 = L0 + 2 * tid, q2 = L0 + 2 * (tid + NT);
+    const bool ok1 = q1 >= 0 && q1 + 2 <= pitch, ok2 = has2 && q2 >= 0 && q2 + 2 <= pitch;
+    const int so1 = ok1 ? 2 * q1 : 0, so2 = ok2 ? 2 * q2 : 0;
+    auto prefetch_in = [&](int n) {  // input row i0 + n into ring slot n % QU
+        const int r = i0 + n;
+        float4* dst = sU + (n & (QU - 1)) * WU + tid;
+        const bool row_ok = r >= 0 && r < a.nx;
+        const float* rowp = row_ok ? in + (long long)r * pitch * 2 : in;
+        cp_async16(dst, rowp + so1, row_ok && ok1);
+        if (has2) cp_async16(dst + NT, rowp + so2, row_ok && ok2);
+    };
+    auto out_row = [&](int n) { return i0 + n - R; };  // output row of iteration n (stored from n = 2R)
+    auto prefetch_upd = [&](int n) {                   // p[t], p[t-1] at the output row of iteration n
+        if constexpr (MODE != PASS_L) {
+            const int ro = out_row(n);
+            if (ro < xo0 || ro >= xo1 || !out_t) return;
+            const long long off = (long long)ro * pitch * 2 + 2 * c;
+            if constexpr (CF::HAS_C) cp_async16(sC + (n & (QC - 1)) * NT + tid, cur + off, true);
+            cp_async16(sP + (n & (QC - 1)) * NT + tid, prev + off, true);
         }
-        (void)bxi; (void)by1; (void)by1b; (void)by2;
-        float2* const F = sF + par * RB * L::WF;
-        float2* const F2 = sF2 + par * RB * L::WF;
-        if constexpr (STAG) {
-            // stage-1 y-fluxes at half-cols L1-5+k from u rows j+r (F[k])
+    };
+    for (int n = 0; n < PF; n++) {
+        prefetch_in(n);
+        if (n == 0)
+            for (int m = 0; m < PF2; m++) prefetch_upd(m);
+        cp_async_commit();
+    }
+
+    // ---- medium: pointers at this thread's (clamped) columns, rows added per iteration --------
+    const int mp = a.mpitch;
+    const float2* __restrict__ mW = a.Wd + cm;
+    const float2* __restrict__ mBX = a.bxd + cm;
+    const float2* __restrict__ mC1 = a.C1d + cm;
+    const float2* __restrict__ mC2 = a.C2d + cm;
+    const float2* __restrict__ mC3 = a.NC3d + cm;
+    // y-flux pair k = tid at half-columns y0 - 6 + 2k (and k = tid + NT for tid < 5)
+    const float2* __restrict__ mBY = a.byd + min(max(y0 - 6 + 2 * tid, -DUP_MARGIN), a.ymax);
+    const float2* __restrict__ mBYb = a.byd + min(max(y0 - 6 + 2 * (tid + NT), -DUP_MARGIN), a.ymax);
+    auto ldm = [](const float2* p) { return as_col2(__ldg(reinterpret_cast<const float4*>(p))); };
+    PassMedium md;
+    md.byb = zero_c2();
+    auto ld_by = [&](int n) {  // output row
+        const long long r = (long long)out_row(n) * mp;
+        md.by = ldm(mBY + r);
+        if (tid < 5) md.byb = ldm(mBYb + r);
+    };
+    auto ld_bx = [&](int n) { md.bx = ldm(mBX + (long long)(i0 + n - 5) * mp); };  // x-flux half-row
+    auto ld_W = [&](int n) { md.W = ldm(mW + (long long)out_row(n) * mp); };
+    auto ld_upd = [&](int n) {
+        if constexpr (MODE != PASS_L) {
+            const int ro = out_row(n);
+            if (ro < xo0 || ro >= xo1 || !out_t || a.wg_only) return;
+            const long long r = (long long)ro * mp;
+            md.c1 = ldm(mC1 + r);
+            md.c2 = ldm(mC2 + r);
+            md.nc3 = ldm(mC3 + r);
+        }
+    };
+    if constexpr (VARB) {
+        ld_by(0);
+        ld_bx(0);
+    }
+    ld_W(0);
+    ld_upd(0);
+
+    // ---- register queues (slot = iteration number mod P): input rows, staggered x-fluxes -------
+    Col2 uq[P], fq[STAG ? P : 1];
 #pragma unroll
-            for (int r = 0; r < RB; r++) {
-                const float2* su = rowU(wrapU(sI - R + r)) + L0;  // su[k] = u(j+r, L0 + k)
-                {
-                    const int k = tid;
-                    float2 v = mul2(dstag2(su, k + 5, k + 4), ihy);
-                    if constexpr (VARB) v = mul2(v, f2(by1[r]));
-                    F[r * L::WF + k] = v;
-                }
-                if (tid < 9) {
-                    const int k = NT + tid;
-                    float2 v = mul2(dstag2(su, k + 5, k + 4), ihy);
-                    if constexpr (VARB) v = mul2(v, f2(by1b[r]));
-                    F[r * L::WF + k] = v;
-                }
-            }
-            if constexpr (OT4) {
-                // stage-2 y-fluxes at half-cols y0-5+k from intermediate rows o+r (F2[k])
-#pragma unroll
-                for (int r = 0; r < RB; r++) {
-                    const float2* sl = sLr + wrapL(sJ - R + r) * L::WL;  // l(o+r, L1 + k)
-                    if (tid < BY + 9) {
-                        const int k = tid;
-                        float2 v = mul2(dstag2(sl, k + 5, k + 4), ihy);
-                        if constexpr (VARB) v = mul2(v, f2(by2[r]));
-                        F2[r * L::WF + k] = v;
+    for (int k = 0; k < P; k++) {
+        uq[k] = zero_c2();
+        if constexpr (STAG) fq[k] = zero_c2();
+    }
+    // Warm-up: iteration n feeds the x-fluxes from n >= R (staggered) and outputs from n >= 2R;
+    // earlier work would only reach rows that are not stored.
+#pragma unroll 1
+    for (int base = 0; base < niter; base += P) {
+        unroll_period(std::make_integer_sequence<int, P>{}, [&](auto KC) {
+            constexpr int K = decltype(KC)::value;
+            const int n = base + K;
+            if (n >= niter) return;  // uniform: the barrier below is reached by all or none
+            const int par = K & 1;
+            const bool outn = n >= 2 * R;
+
+            // ---- phase A: y-fluxes of the output row (its input row is visible since earlier
+            // barriers) into this iteration's flux buffer ----------------------------------------
+            if constexpr (STAG) {
+                if (outn) {
+                    // input row r = i - R: index e <-> column L0 + e; pair k at half-columns y0 - 6 + 2k
+                    const float4* urow = sU + ((n - R) & (QU - 1)) * WU;
+                    Col2 F = yflux_pair(urow, tid, wy);
+                    if constexpr (VARB) F = mul_c2(F, md.by);
+                    sF[par * NF + tid] = as_f4(F);
+                    if (tid < 5) {
+                        Col2 Fb = yflux_pair(urow, tid + NT, wy);
+                        if constexpr (VARB) Fb = mul_c2(Fb, md.byb);
+                        sF[par * NF + tid + NT] = as_f4(Fb);
                     }
                 }
+                if constexpr (VARB) ld_by(n + 1);
             }
-        }
+            cp_async_wait<PF - 1>();
+            __syncthreads();  // input row i, this iteration's fluxes visible; the previous iteration done
+            prefetch_in(n + PF);
+            prefetch_upd(n + PF2);
+            cp_async_commit();
 
-        cp_async_wait<PF - 1>();
-        __syncthreads();  // rows i..i+RB-1 and this iteration's fluxes visible; last iteration done
-        prefetch(i + PF * RB, sI + PF * RB >= QU ? sI + PF * RB - QU : sI + PF * RB);
-
-        // stage-2 and update medium of this iteration
-        float Wo[RB], bxj[RB], c1[RB], c2[RB], c3[RB];
-        float2 pmo[RB];
-#pragma unroll
-        for (int r = 0; r < RB; r++) {
-            if constexpr (OT4) {
-                Wo[r] = __ldg(pW + (long long)(o + r) * pitch);
-                if constexpr (VARB) bxj[r] = __ldg(pBX + (long long)(j - 5 + r) * pitch);
-            }
-            const bool o_ok = (o + r >= xo0) && (o + r < xo1) && out_col;
-            const long long orow = (long long)(o + r) * pitch;
-            c1[r] = o_ok ? __ldg(pC1 + orow) : 0.f;
-            c2[r] = o_ok ? __ldg(pC2 + orow) : 0.f;
-            c3[r] = o_ok ? __ldg(pC3 + orow) : 0.f;
-            pmo[r] = o_ok ? prev[orow + c] : f2(0.f);
-        }
-        (void)Wo; (void)bxj;
-
-        // ---- stage 1: l = W * G(u) at rows j .. j+RB-1 ----------------------------------
-#pragma unroll
-        for (int r = 0; r < RB; r++) uq[QB + r] = rowU(wrapU(sI + r))[c];
-        float2 gy[RB];
-        if constexpr (STAG) {
-#pragma unroll
-            for (int r = 0; r < RB; r++) gy[r] = mul2(dstag2(F + r * L::WF, tid + 5, tid + 4), ihy);
-        } else {
-#pragma unroll
-            for (int r = 0; r < RB; r++) gy[r] = mul2(dcent2(rowU(wrapU(sI - R + r)), c), ihy2);
-        }
-        float2 lj[RB];
-#pragma unroll
-        for (int r = 0; r < RB; r++) {
-            float2 gx;
+            // ---- G(in) at the output row r = i - R ----------------------------------------------
+            uq[K] = ld_c2(sU + (n & (QU - 1)) * WU + tid + UL / 2);  // input row i, own columns
             if constexpr (STAG) {
-                // flux at half-row (i-5+r)+1/2 from u rows i-9+r .. i+r (queue index r .. r+9)
-                float2 v = mul2(dstag2(uq, r + 5, r + 4), ihx);
-                if constexpr (VARB) v = mul2(v, f2(bxi[r]));
-                fq[QB + r] = v;
-                // D- at row j+r from fluxes at half-rows j+r-5 .. j+r+4 (queue index r .. r+9)
-                gx = mul2(dstag2(fq, r + 5, r + 4), ihx);
-            } else {
-                gx = mul2(dcent2(uq, r + 5), ihx2);  // rows i+r-10 .. i+r
+                if (n >= R) {  // x-flux at half-row i - 5 from input rows i - 9 .. i
+                    Col2 fx = qstag<P, K, -4, -5>(uq, wx);
+                    if constexpr (VARB) fx = mul_c2(fx, md.bx);
+                    fq[K] = fx;
+                }
+                if constexpr (VARB) ld_bx(n + 1);
             }
-            const bool keep = j + r >= 0 && j + r < a.nx && c_in;  // zero halo of the intermediate
-            lj[r] = keep ? mul2(f2(Wj[r]), add2(gx, gy[r])) : f2(0.f);
-        }
-        qshift<QL, RB>(uq);
-        if constexpr (STAG) qshift<QL, RB>(fq);
-
-        // ---- stage 2 (OT4): Lt = l + dt^2/12 W G(l) at rows o .. o+RB-1 ------------------
-        float2 Lt[RB];
-        if constexpr (OT4) {
-#pragma unroll
-            for (int r = 0; r < RB; r++) {
-                sLr[wrapL(sJ + r) * L::WL + tid] = lj[r];  // l(j+r, L1 + k), read R rows later
-                lq[QB + r] = lj[r];
-            }
-            float2 gy2[RB];
-            const bool s2 = (tid >= H1) && (tid < H1 + BY);
-            if constexpr (STAG) {
-#pragma unroll
-                for (int r = 0; r < RB; r++)
-                    gy2[r] = s2 ? mul2(dstag2(F2 + r * L::WF, tid - H1 + 5, tid - H1 + 4), ihy) : f2(0.f);
-            } else {
-#pragma unroll
-                for (int r = 0; r < RB; r++)
-                    gy2[r] = s2 ? mul2(dcent2(sLr + wrapL(sJ - R + r) * L::WL, tid), ihy2) : f2(0.f);
-            }
-#pragma unroll
-            for (int r = 0; r < RB; r++) {
-                float2 gx2;
+            if (outn) {
+                Col2 g;
                 if constexpr (STAG) {
-                    float2 v = mul2(dstag2(lq, r + 5, r + 4), ihx);
-                    if constexpr (VARB) v = mul2(v, f2(bxj[r]));
-                    f2q[QB + r] = v;
-                    gx2 = mul2(dstag2(f2q, r + 5, r + 4), ihx);
+                    // D- along x at row r from fluxes at half-rows r - 5 .. r + 4 (iterations K - 9 .. K)
+                    const Col2 gx = qstag<P, K, -4, -5>(fq, wx);
+                    // D- along y at (c, c + 1) from flux pairs tid .. tid + 5
+                    const Col2 gy = ydiv_pair(sF + par * NF, tid, wy);
+                    g = add_c2(gx, gy);
                 } else {
-                    gx2 = mul2(dcent2(lq, r + 5), ihx2);
+                    const Col2 gx = qcent<P, K, -5>(uq, wx);  // input rows i - 10 .. i about r = i - 5
+                    const Col2 gy = ycent_pair(sU + ((n - R) & (QU - 1)) * WU, tid, wy);
+                    g = add_c2(gx, gy);
                 }
-                // l(o+r): queue index r (STAG, rows j-9..) or r+5 (laplace, rows j-10..)
-                const float2 lo = STAG ? lq[r] : lq[r + 5];
-                Lt[r] = fma2(k12, mul2(f2(Wo[r]), add2(gx2, gy2[r])), lo);
-            }
-            qshift<QL, RB>(lq);
-            if constexpr (STAG) qshift<QL, RB>(f2q);
-        } else {
-#pragma unroll
-            for (int r = 0; r < RB; r++) Lt[r] = lj[r];
-        }
-
-        // ---- update of rows o .. o+RB-1, fused epilogues ------------------------------
-#pragma unroll
-        for (int r = 0; r < RB; r++) {
-            const int orow = o + r;
-            if (orow >= xo0 && orow < xo1 && out_col) {
-                const long long idx = (long long)orow * pitch + c;  // float2 index within the pair
-                const float2 u_o = rowU(wrapU(sI - S * R + r))[c];
-                const float2 pm = pmo[r];
-                float2 pn = fma2(f2(c1[r]), Lt[r], fma2(f2(c2[r]), u_o, mul2(f2(-c3[r]), pm)));
-                if (do_save) {
-                    float2* snap = reinterpret_cast<float2*>(a.snaps) + (long long)pair * a.snap_shot_stride +
-                                   (long long)(a.t / a.f) * a.snap_stride + idx;
-                    *snap = a.save == 2 ? u_o  // raw p[t] (rho / wavelet gradients)
-                                        : make_float2((pn.x - 2.f * u_o.x + pm.x) / dt2, (pn.y - 2.f * u_o.y + pm.y) / dt2);
+                const Col2 in_r = uq[((K - R) % P + P) % P];  // the input at the output row
+                const int r = out_row(n);
+                const long long idx = (long long)r * pitch + c;  // float2 index within the pair
+                Col2 res;
+                if constexpr (MODE == PASS_L) {
+                    res = mul_c2(md.W, g);  // l; rows and columns beyond the grid are never stored (zero)
+                } else {
+                    Col2 Lt;
+                    if constexpr (MODE == PASS_U4) {
+                        Lt = fma_c2(mul_c2(md.W, {f2(a.k12), f2(a.k12)}), g, in_r);
+                    } else {
+                        Lt = mul_c2(md.W, g);
+                    }
+                    if (out_t) {
+                        const Col2 u_o = CF::HAS_C ? ld_c2(sC + (n & (QC - 1)) * NT + tid) : in_r;
+                        const Col2 pm = ld_c2(sP + (n & (QC - 1)) * NT + tid);
+                        if (a.wg_only) {
+                            res = Lt;
+                        } else {
+                            res.a = fma2(md.c1.a, Lt.a, fma2(md.c2.a, u_o.a, mul2(md.nc3.a, pm.a)));
+                            res.b = fma2(md.c1.b, Lt.b, fma2(md.c2.b, u_o.b, mul2(md.nc3.b, pm.b)));
+                        }
+                        if (do_save) {
+                            float2* snap = reinterpret_cast<float2*>(a.snaps) + (long long)pair * a.snap_shot_stride +
+                                           (long long)(a.t / a.f) * a.snap_stride + idx;
+                            Col2 sv;
+                            if (a.save == 2) {
+                                sv = u_o;  // raw p[t] (rho / wavelet gradients)
+                            } else {
+                                const float2 id = f2(a.inv_dt2);
+                                sv.a = mul2(add2(sub2(res.a, add2(u_o.a, u_o.a)), pm.a), id);
+                                sv.b = mul2(add2(sub2(res.b, add2(u_o.b, u_o.b)), pm.b), id);
+                            }
+                            if (out1) *reinterpret_cast<float4*>(snap) = as_f4(sv);
+                            else *snap = sv.a;
+                        }
+                    }
                 }
-                prev[idx] = pn;
+                if (out_t) {
+                    float2* dst = reinterpret_cast<float2*>(outp) + idx;
+                    if (out1) *reinterpret_cast<float4*>(dst) = as_f4(res);
+                    else *dst = res.a;
+                }
             }
-        }
-        sI = sI + RB >= QU ? sI + RB - QU : sI + RB;
-        if constexpr (OT4) sJ = sJ + RB >= QLR ? sJ + RB - QLR : sJ + RB;
-        par ^= 1;
+            ld_W(n + 1);
+            ld_upd(n + 1);
+        });
     }
     cp_async_wait<0>();
 }

@@ -1,5 +1,6 @@
 // Host launchers of the plan's helper kernels (helpers.cu).
 #pragma once
+#include <algorithm>
 #include <vector>
 
 #include "../../include/strideacc.h"
@@ -15,6 +16,57 @@ cudaError_t medium2d(const float* vp_in, const float* rho_in, const float* alpha
                      int pitch_b, int density, double db_to_np, const Sponge& sp, float dt, float* W, float* vp,
                      float* alpha, float* buoy, float* bxh, float* byh, float* C1, float* C2, float* C3,
                      cudaStream_t s);
+// Row pitch (float2) of the duplicated medium of an ny-column grid, and the largest even column a
+// step thread may address in it.
+inline int dup_pitch(int ny) { return (ny + 2 * DUP_MARGIN + 15) / 16 * 16; }
+inline int dup_ymax(int ny) { return (ny + DUP_MARGIN - 2) & ~1; }
+// Float2 elements of the six duplicated medium arrays of an nx x ny grid.
+inline size_t dup_medium_size(int nx, int ny) { return (size_t)6 * (nx + 2 * DUP_GUARD) * dup_pitch(ny); }
+// The step passes' duplicated medium (helpers.cu k_dup_medium2d), dup_medium_size(nx, ny) float2.
+cudaError_t dup_medium2d(const float* W, const float* bxh, const float* byh, const float* C1, const float* C2,
+                         const float* C3, int nx, int ny, int pitch, int pitch_b, float2* out, cudaStream_t s);
+// Points a step's medium fields at a duplicated-medium allocation of an nx x ny grid.
+inline void step_medium(Step2D& a, const float2* dmed, int nx, int ny) {
+    const int mp = dup_pitch(ny);
+    const long long astride = (long long)(nx + 2 * DUP_GUARD) * mp;
+    const float2* at0 = dmed + (long long)DUP_GUARD * mp + DUP_MARGIN;
+    a.Wd = at0;
+    a.bxd = at0 + astride;
+    a.byd = at0 + 2 * astride;
+    a.C1d = at0 + 3 * astride;
+    a.C2d = at0 + 4 * astride;
+    a.NC3d = at0 + 5 * astride;
+    a.mpitch = mp;
+    a.ymax = dup_ymax(ny);
+}
+// The step's FD weights over the spacing (kind 0: the 10th-order Laplacian's over h^2; else the
+// staggered first derivative's over h), dt^2 / 12 and 1 / dt^2.
+inline void step_weights(Step2D& a, int kind, double hx, double hy, double dt) {
+    for (int m = 0; m < 6; m++) {
+        float wx, wy;
+        if (kind == 0) {
+            wx = (float)((double)kW2(m) / (hx * hx));
+            wy = (float)((double)kW2(m) / (hy * hy));
+        } else {
+            wx = m < 5 ? (float)((double)kWS(m) / hx) : 0.f;
+            wy = m < 5 ? (float)((double)kWS(m) / hy) : 0.f;
+        }
+        a.wx[m] = make_float2(wx, wx);
+        a.wy[m] = make_float2(wy, wy);
+    }
+    a.k12 = (float)(dt * dt / 12.0);
+    a.inv_dt2 = (float)(1.0 / (dt * dt));
+}
+// Launch layout of the step passes for a ny-column grid split into `strips` column strips: output
+// columns per strip (even) and threads per CTA (two columns each, at least STEP_MIN_THREADS);
+// false when a strip needs more than STEP_MAX_THREADS threads.
+inline bool step_strips(int ny, int strips, int* by, int* threads) {
+    const int b = ((ny + strips - 1) / strips + 1) & ~1;
+    const int t = std::max(STEP_MIN_THREADS, b / 2);
+    *by = b;
+    *threads = t;
+    return t <= STEP_MAX_THREADS && strips >= 1;
+}
 void set_last_error(const char* msg);
 // exact-gradient mode (exact2d.cu)
 cudaError_t exact_coef2d(const float* vp, const float* alpha, const float* W, int nx, int ny, int pitch,

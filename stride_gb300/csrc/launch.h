@@ -27,6 +27,8 @@ inline cudaError_t launch_step3d(int kind, bool final_pass, bool ot4, dim3 grid,
     }
 }
 
+// One 2D time step of a batch: OT4 launches pass L then pass U, OT2 pass U (fdtd2d.cuh);
+// nt_threads in [STEP_MIN_THREADS, STEP_MAX_THREADS], two grid columns per thread.
 inline cudaError_t launch_step2d(int kind, bool ot4, int nt_threads, dim3 grid, cudaStream_t s, const Step2D& a) {
     switch (kind) {
         case 0: return launch_step2d_k0(ot4, nt_threads, grid, s, a);

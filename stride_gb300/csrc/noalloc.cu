@@ -3,9 +3,10 @@
 // Some callers cannot let a library allocate GPU memory: a host application that hands the
 // whole device to a memory pool it manages and forbids allocations outside it, or a loop that
 // must not pay for cudaMalloc/cudaFree (cudaFree synchronises the device). For them this entry
-// point runs the same time-step kernel as sa_forward, but keeps every scratch buffer (the two
-// wavefield levels, the medium copies, the point lists and the time-major traces) in one
-// file-scope __device__ array of kScratchBytes. The caller passes the inputs and the output.
+// point runs the same time-step kernels as sa_forward, but keeps every scratch buffer (the two
+// wavefield levels, the intermediate level of OT4, the medium copies and their pair-duplicated
+// form, the point lists and the time-major traces) in one file-scope __device__ array of
+// kScratchBytes. The caller passes the inputs and the output.
 //
 // Limits and behaviour:
 //  * one shot, 2D, extended grid at most kMaxSide x kMaxSide, at most kMaxSrc sources and
@@ -30,7 +31,7 @@
 
 namespace {
 
-constexpr size_t kScratchBytes = 32u << 20;  // 32 MiB per device
+constexpr size_t kScratchBytes = 64u << 20;  // 64 MiB per device
 constexpr int kMaxSide = 640;                // extended grid side
 constexpr int kMaxSrc = 16;
 constexpr int kMaxRec = 1024;
@@ -145,22 +146,12 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
     const int kind = d.density == SA_DENSITY_NONE ? 0 : (d.density == SA_DENSITY_VARIABLE ? 1 : 2);
     const bool ot4 = d.kernel == SA_KERNEL_OT4;
     const int R = kind == 0 ? 5 : 9;
-    const int H1 = ot4 ? R : 0;
-    const int S = ot4 ? 2 : 1;
     const int pitch = (ny + 2 + 31) / 32 * 32, pitch_b = (ny + 12 + 31) / 32 * 32;
-    int NT = 96, best = 1 << 30;
-    for (int nt_ : {96, 128, 160, 192}) {
-        const int bm = nt_ - 2 * H1;
-        const int cost = ((ny + bm - 1) / bm) * nt_;
-        if (cost < best) {
-            best = cost;
-            NT = nt_;
-        }
-    }
-    const int bymax = NT - 2 * H1;
-    const int nstrips = (ny + bymax - 1) / bymax;
-    const int by = (ny + nstrips - 1) / nstrips;
-    int nchunks = std::max(1, std::min((152 * 6 + nstrips - 1) / nstrips, nx / (4 * S * R)));
+    int by = 0, NT = 0;  // the fewest column strips (two columns a thread)
+    sa::step_strips(ny, (ny + 2 * sa::STEP_MAX_THREADS - 1) / (2 * sa::STEP_MAX_THREADS), &by, &NT);
+    const int nstrips = (ny + by - 1) / by;
+    const int warps = (NT + 31) / 32;
+    int nchunks = std::max(1, std::min((152 * 12 / warps + nstrips - 1) / nstrips, nx / (4 * R)));
     const int chunk_rows = (nx + nchunks - 1) / nchunks;
     nchunks = (nx + chunk_rows - 1) / chunk_rows;
     const int ncta = nchunks * nstrips;
@@ -189,13 +180,16 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
     float* tcoef = cv.take<float>((size_t)4 * kMaxSrc);
     int* tpoint = cv.take<int>((size_t)4 * kMaxSrc);
     sa::Gather* gat = cv.take<sa::Gather>(kMaxRec);
-    if (cv.used > kScratchBytes) return err(SA_E_INVALID, "grid, traces and lists exceed the 32 MiB scratch array");
+    float2* dmed = cv.take<float2>(sa::dup_medium_size(nx, ny));  // the step passes' pair-duplicated medium
+    float* lbuf = ot4 ? cv.take<float>(2 * pe) : nullptr;          // OT4's intermediate level
+    if (cv.used > kScratchBytes) return err(SA_E_INVALID, "grid, traces and lists exceed the 64 MiB scratch array");
 
     // ---- zero what must start at zero, then the medium ---------------------------------
     if (cudaMemsetAsync(field[0], 0, 2 * pe * sizeof(float), s) != cudaSuccess ||
         cudaMemsetAsync(field[1], 0, 2 * pe * sizeof(float), s) != cudaSuccess ||
         cudaMemsetAsync(med_begin, 0, med_bytes, s) != cudaSuccess ||
-        (n_rec && cudaMemsetAsync(rec_amp, 0, (size_t)nt * n_rec * sizeof(float), s) != cudaSuccess))
+        (n_rec && cudaMemsetAsync(rec_amp, 0, (size_t)nt * n_rec * sizeof(float), s) != cudaSuccess) ||
+        (lbuf && cudaMemsetAsync(lbuf, 0, 2 * pe * sizeof(float), s) != cudaSuccess))
         return err(SA_E_CUDA, "cudaMemsetAsync on the scratch array failed");
     sa::Sponge sp{};
     sp.a[0] = d.absorbing[0];
@@ -212,6 +206,10 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
                      W + g0, vps, als, buoy, bxh ? bxh + (long long)(sa::GUARD + 5) * pitch : nullptr,
                      byh ? byh + (long long)sa::GUARD * pitch_b : nullptr, C1 + g0, C2 + g0, C3 + g0, s) != cudaSuccess)
         return err(SA_E_CUDA, "medium preparation kernel failed");
+    if (sa::dup_medium2d(W + g0, bxh ? bxh + (long long)(sa::GUARD + 5) * pitch : nullptr,
+                         byh ? byh + (long long)sa::GUARD * pitch_b : nullptr, C1 + g0, C2 + g0, C3 + g0, nx, ny, pitch,
+                         pitch_b, dmed, s) != cudaSuccess)
+        return err(SA_E_CUDA, "medium duplication kernel failed");
 
     // ---- point lists (host arrays on the stack, copied into the scratch array) -----------
     const double h = std::max(d.spacing[0], d.spacing[1]);
@@ -303,16 +301,9 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
     a.shot_stride = pe;
     a.chunk_rows = chunk_rows;
     a.by = by;
-    a.W = W + g0;
-    a.bxh = bxh ? bxh + (long long)(sa::GUARD + 5) * pitch : nullptr;
-    a.byh = byh ? byh + (long long)sa::GUARD * pitch_b : nullptr;
-    a.pitch_b = pitch_b;
-    a.C1 = C1 + g0;
-    a.C2 = C2 + g0;
-    a.C3 = C3 + g0;
-    a.hx = (float)d.spacing[0];
-    a.hy = (float)d.spacing[1];
-    a.dt = (float)d.dt;
+    a.lbuf = lbuf;
+    sa::step_medium(a, dmed, nx, ny);
+    sa::step_weights(a, kind, d.spacing[0], d.spacing[1], d.dt);
     a.f = d.undersampling > 0 ? d.undersampling : 4;
     const dim3 grid(nstrips, nchunks, 1);
     for (int t = 1; t <= nt - 2; t++) {

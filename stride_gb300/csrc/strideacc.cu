@@ -100,10 +100,15 @@ struct sa_plan {
     bool ot4 = true;
     float* field[2] = {nullptr, nullptr};
     size_t field_cap[2] = {0, 0};
+    float* lbuf = nullptr;  // OT4: l = W G(p[t]) between the step's two passes (zero beyond the grid)
+    size_t lbuf_cap = 0;
     // medium: W, bxh, byh, C1..C3 have GUARD zero rows on both sides (the *_0 pointers address
     // row 0 / half-row 0); vp, alpha, buoy are unguarded scratch of the preparation kernels
     float *W = nullptr, *vp = nullptr, *alpha = nullptr, *buoy = nullptr, *bxh = nullptr, *byh = nullptr;
     float *C1 = nullptr, *C2 = nullptr, *C3 = nullptr;
+    // the step passes' pair-duplicated copies of W, bxh, byh, C1, C2, -C3 (dup_medium2d)
+    float2* dmed = nullptr;
+    size_t cap_dmed = 0;
     size_t cap_W = 0, cap_vp = 0, cap_alpha = 0, cap_buoy = 0, cap_bxh = 0, cap_byh = 0, cap_C1 = 0, cap_C2 = 0,
            cap_C3 = 0;
     std::vector<float> vp_host;  // for the injection coefficients (vp at the corners)
@@ -158,12 +163,11 @@ struct sa_plan {
     size_t cap_ckpt2 = 0, cap_pml_ck2 = 0;
     bool ckpt_valid = false;
     // exact-gradient mode: per-point derivative coefficients, every level of a segment, the
-    // W G(.) of a forward and an adjoint level, unit/zero update coefficients (guarded), the
-    // receiver injection with coefficient C1 W, flat source list
+    // W G(.) of a forward and an adjoint level (the step pass's wg_only mode), the receiver
+    // injection with coefficient C1 W, flat source list
     float *EA = nullptr, *EB = nullptr, *EC = nullptr, *EG4 = nullptr, *ES = nullptr, *levels = nullptr;
-    float *Lu = nullptr, *Lz = nullptr, *ones_g = nullptr, *zeros_g = nullptr;
-    size_t cap_EA = 0, cap_EB = 0, cap_EC = 0, cap_EG4 = 0, cap_ES = 0, cap_levels = 0, cap_Lu = 0, cap_Lz = 0,
-           cap_ones = 0, cap_zeros = 0;
+    float *Lu = nullptr, *Lz = nullptr;
+    size_t cap_EA = 0, cap_EB = 0, cap_EC = 0, cap_EG4 = 0, cap_ES = 0, cap_levels = 0, cap_Lu = 0, cap_Lz = 0;
     bool exact_coef_valid = false;
     std::vector<float> c1w_host;
     sa::ExactSrc2D* src_flat = nullptr;  // support points of the sources (exact gradient's source term)
@@ -199,16 +203,15 @@ struct sa_plan {
 namespace {
 
 int npairs(const sa_plan* p) { return (p->n_shots + 1) / 2; }
-int halo1(const sa_plan* p) { return p->ot4 ? (p->kind == 0 ? 5 : 9) : 0; }
 int radius(const sa_plan* p) { return p->kind == 0 ? 5 : 9; }
-// output columns of a CTA of `nt` threads (one column per thread, halo H1 on both sides)
-int bymax(const sa_plan* p, int nt) { return nt - 2 * halo1(p); }
-const int kThreads[] = {96, 128, 160, 192, 256};
-void set_strips(sa_plan* p, int nt) {
+// fewest column strips of the step passes (a CTA thread owns two columns)
+int min_strips(const sa_plan* p) { return (p->ny + 2 * sa::STEP_MAX_THREADS - 1) / (2 * sa::STEP_MAX_THREADS); }
+void set_strips(sa_plan* p, int strips) {
+    int by = 0, nt = 0;
+    sa::step_strips(p->ny, strips, &by, &nt);
+    p->by = by;
     p->NT = nt;
-    const int bm = bymax(p, nt);
-    p->nstrips = (p->ny + bm - 1) / bm;
-    p->by = (p->ny + p->nstrips - 1) / p->nstrips;
+    p->nstrips = (p->ny + by - 1) / by;
 }
 
 void drop_graphs(sa_plan* p) {
@@ -241,23 +244,13 @@ void damping_table(int A, double h, double refl, float* out) {  // out: MAX_ABS 
 
 void default_layout(sa_plan* p) {
     if (p->layout_fixed) return;
-    int best_nt = 128, best_cost = 1 << 30;
-    for (int nt : kThreads) {
-        const int bm = bymax(p, nt);
-        const int strips = (p->ny + bm - 1) / bm;
-        const int cost = strips * nt;
-        if (cost < best_cost) {
-            best_cost = cost;
-            best_nt = nt;
-        }
-    }
-    set_strips(p, best_nt);
-    // enough CTAs to fill 152 SMs several times; each chunk keeps >= 4 pipeline depths of rows
-    const int S = p->ot4 ? 2 : 1;
-    const int minrows = 4 * S * radius(p);
+    set_strips(p, min_strips(p));
+    // about one wave of 12 warps on each of the 152 SMs; each chunk keeps >= 2 pipeline depths of rows
+    const int minrows = 4 * radius(p);
     const int shots = std::max(1, npairs(p));
-    const int target = 152 * 6;
-    int nchunks = (target + p->nstrips * shots - 1) / (p->nstrips * shots);
+    const int warps_per_chunk = p->nstrips * shots * ((p->NT + 31) / 32);
+    const int target = 152 * 12;
+    int nchunks = (target + warps_per_chunk - 1) / warps_per_chunk;
     nchunks = std::max(1, std::min(nchunks, p->nx / minrows));
     p->chunk_rows = (p->nx + nchunks - 1) / nchunks;
     p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
@@ -464,16 +457,9 @@ sa::Step2D base_args(const sa_plan* p) {
     a.shot_stride = p->shot_stride;
     a.chunk_rows = p->chunk_rows;
     a.by = p->by;
-    a.W = row0(p, p->W, p->pitch);
-    a.bxh = p->bxh ? row0(p, p->bxh, p->pitch, 5) : nullptr;
-    a.byh = p->byh ? row0(p, p->byh, p->pitch_b) : nullptr;
-    a.pitch_b = p->pitch_b;
-    a.C1 = row0(p, p->C1, p->pitch);
-    a.C2 = row0(p, p->C2, p->pitch);
-    a.C3 = row0(p, p->C3, p->pitch);
-    a.hx = (float)p->d.spacing[0];
-    a.hy = (float)p->d.spacing[1];
-    a.dt = (float)p->d.dt;
+    a.lbuf = p->lbuf;
+    sa::step_medium(a, p->dmed, p->nx, p->ny);
+    sa::step_weights(a, p->kind, p->d.spacing[0], p->d.spacing[1], p->d.dt);
     a.f = p->d.undersampling;
     a.snaps = p->snaps;
     a.snap_stride = p->snap_stride;
@@ -810,8 +796,7 @@ int issue_adjoint_exact(sa_plan* p, cudaStream_t s) {
     fa.save = 0;
     sa::Step2D aa = fa;  // adjoint (dL/drec[t-2] injected after step t)
     sa::Step2D la = fa;  // W G(cur) into prev
-    la.C1 = row0(p, p->ones_g, p->pitch);
-    la.C2 = la.C3 = row0(p, p->zeros_g, p->pitch);
+    la.wg_only = 1;
     const dim3 grid(p->nstrips, p->nchunks, npairs(p));
     const float inv_dt2 = (float)(1.0 / (p->d.dt * p->d.dt));
     const float src_scale = (float)(2.0 * p->d.dt / std::max(p->d.spacing[0], p->d.spacing[1]));
@@ -940,6 +925,10 @@ int ensure_fields(sa_plan* p) {
     const size_t n = (size_t)((std::max(1, p->d.max_shots) + 1) / 2) * p->shot_stride * 2;
     CKR(ensure(&p->field[0], &p->field_cap[0], n));
     CKR(ensure(&p->field[1], &p->field_cap[1], n));
+    if (p->ot4) {  // pass L writes grid columns only: the pitch columns beyond ny stay zero (the halo)
+        CKR(ensure(&p->lbuf, &p->lbuf_cap, n));
+        CK(cudaMemset(p->lbuf, 0, n * sizeof(float)));
+    }
     return SA_OK;
 }
 
@@ -956,6 +945,19 @@ int sa_last_error(char* buf, int len) {
 long long sa_launch_count(const sa_plan* p) {
     if (!p) return -1;
     return p->p3 ? sa::plan3d_launches(p->p3) : p->launches;
+}
+
+int sa_plan_layout(const sa_plan* p, int* threads, int* strips, int* chunks) {
+    if (!p || !threads || !strips || !chunks) return fail(SA_E_INVALID, "null argument");
+    if (p->p3) {
+        *threads = sa::kTile3dY * sa::kTile3dZ;
+        *strips = *chunks = 0;
+        return SA_OK;
+    }
+    *threads = p->NT;
+    *strips = p->nstrips;
+    *chunks = p->nchunks;
+    return SA_OK;
 }
 
 int sa_checkpoint_schedule(const sa_desc* d, int n_shots, int* K, int* n_ckpt, int* K2) {
@@ -1100,7 +1102,7 @@ int sa_plan_destroy(sa_plan* p) {
                     p->gat_flat,
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
-                    p->ones_g, p->zeros_g, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
+                    p->dmed, p->lbuf, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
                     p->dbx, p->dby, p->pml_prof, p->pml_aux, p->pml_ck, p->pml_aux_f, p->ckpt2, p->pml_ck2,
                     p->wgrad, p->hgat, p->hgat_src, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
                     p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx, p->xtgt.off, p->xtgt.point, p->xtgt.coef};
@@ -1139,6 +1141,15 @@ int sa_set_medium(sa_plan* p, const float* vp, const float* rho, const float* al
                     p->byh ? const_cast<float*>(row0(p, p->byh, p->pitch_b)) : nullptr,
                     const_cast<float*>(row0(p, p->C1, p->pitch)), const_cast<float*>(row0(p, p->C2, p->pitch)),
                     const_cast<float*>(row0(p, p->C3, p->pitch)), 0));
+    {
+        float2* old = p->dmed;
+        CKR(ensure(&p->dmed, &p->cap_dmed, sa::dup_medium_size(p->nx, p->ny)));
+        if (old != p->dmed) drop_graphs(p);  // the captured step launches hold the medium pointers
+        CK(sa::dup_medium2d(row0(p, p->W, p->pitch), p->bxh ? row0(p, p->bxh, p->pitch, 5) : nullptr,
+                            p->byh ? row0(p, p->byh, p->pitch_b) : nullptr, row0(p, p->C1, p->pitch),
+                            row0(p, p->C2, p->pitch), row0(p, p->C3, p->pitch), p->nx, p->ny, p->pitch, p->pitch_b,
+                            p->dmed, 0));
+    }
     CK(cudaDeviceSynchronize());
     p->vp_host.resize(N);
     CK(cudaMemcpy(p->vp_host.data(), dev[0], N * sizeof(float), cudaMemcpyDeviceToHost));
@@ -1339,8 +1350,7 @@ int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec
             drop_graphs(p);
     }
     if (exact) {
-        const size_t NG = (size_t)(p->nx + 2 * sa::GUARD) * p->pitch;
-        float* old[] = {p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz, p->ones_g, p->zeros_g};
+        float* old[] = {p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz};
         CKR(ensure(&p->EA, &p->cap_EA, (size_t)p->shot_stride));
         CKR(ensure(&p->EB, &p->cap_EB, (size_t)p->shot_stride));
         CKR(ensure(&p->EC, &p->cap_EC, (size_t)p->shot_stride));
@@ -1349,17 +1359,11 @@ int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec
         CKR(ensure(&p->levels, &p->cap_levels, (size_t)(p->ck_K + 2) * 2 * fe));
         CKR(ensure(&p->Lu, &p->cap_Lu, 2 * fe));
         CKR(ensure(&p->Lz, &p->cap_Lz, 2 * fe));
-        CKR(ensure(&p->ones_g, &p->cap_ones, NG));
-        CKR(ensure(&p->zeros_g, &p->cap_zeros, NG));
-        float* now[] = {p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz, p->ones_g, p->zeros_g};
+        float* now[] = {p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz};
         if (!std::equal(std::begin(old), std::end(old), std::begin(now)) || !p->exact_coef_valid) {
             drop_graphs(p);
-            // W G(.) outputs start finite (their kernel multiplies the old value by C3 = 0)
             CK(cudaMemset(p->Lu, 0, 2 * fe * sizeof(float)));
             CK(cudaMemset(p->Lz, 0, 2 * fe * sizeof(float)));
-            CK(cudaMemset(p->zeros_g, 0, NG * sizeof(float)));
-            std::vector<float> ones(NG, 1.f);
-            CK(cudaMemcpy(p->ones_g, ones.data(), NG * sizeof(float), cudaMemcpyHostToDevice));
             CK(sa::exact_coef2d(p->vp, p->alpha, row0(p, p->W, p->pitch), p->nx, p->ny, p->pitch, p->sponge,
                                 (float)p->d.dt, p->EA, p->EB, p->EC, p->EG4, p->ES, 0));
             CK(cudaDeviceSynchronize());
@@ -1426,30 +1430,33 @@ int sa_autotune(sa_plan* p, void* stream) {
         return fail(SA_E_INVALID, "autotune between a saving forward and its adjoint would discard the saved "
                                   "wavefield: run the adjoint first");
     cudaStream_t s = (cudaStream_t)stream;
-    const int S = p->ot4 ? 2 : 1;
     struct Cand {
-        int nt, nchunks;
+        int strips, nchunks;
     };
     std::vector<Cand> cands;
-    // row chunks: short chunks (more CTAs, more pipeline warm-up rows) only pay off when the
-    // batch alone cannot fill the GPU
-    const int ctas1 = npairs(p) * ((p->ny + bymax(p, 128) - 1) / bymax(p, 128));
-    for (int nt : kThreads)
+    // column strips from the fewest (widest CTAs) to four more; row chunks: short chunks (more
+    // CTAs, more pipeline warm-up rows) only pay off when the batch alone cannot fill the GPU
+    const int s0 = min_strips(p);
+    const int ctas1 = npairs(p) * s0;
+    for (int st = s0; st <= s0 + 4; st++) {
+        int by = 0, nt = 0;
+        if (!sa::step_strips(p->ny, st, &by, &nt) || (st > s0 && by < 16)) continue;
         for (int nc : {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48}) {
-            const int min_rows = ctas1 >= 456 ? 4 * S * radius(p) : 8;
+            const int min_rows = ctas1 >= 456 ? 4 * radius(p) : 8;
             if (p->nx / nc < min_rows) continue;
-            cands.push_back({nt, nc});
+            cands.push_back({st, nc});
         }
+    }
     const int steps = std::min(24, p->d.nt - 2);
     float best = 1e30f;
-    Cand bc = {p->NT, p->nchunks};
+    Cand bc = {p->nstrips, p->nchunks};
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     p->layout_fixed = true;
     drop_graphs(p);  // the launch shape is baked into the captured loops
     for (const Cand& c : cands) {
-        set_strips(p, c.nt);
+        set_strips(p, c.strips);
         p->chunk_rows = (p->nx + c.nchunks - 1) / c.nchunks;
         p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
         CKR(build_lists(p));
@@ -1480,7 +1487,7 @@ int sa_autotune(sa_plan* p, void* stream) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    set_strips(p, bc.nt);
+    set_strips(p, bc.strips);
     p->chunk_rows = (p->nx + bc.nchunks - 1) / bc.nchunks;
     p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
     CKR(build_lists(p));
