@@ -63,15 +63,16 @@ struct Step2D {
     const float* cur;          // p[t] of shot pairs, interleaved: [pairs][nx][pitch][2]
     float* prev;               // other level in, new level out (in place)
     float* lbuf;               // OT4: l = W G(p[t]) of the first pass (same layout; zero beyond ny)
-    // medium duplicated per pair: point (x, y) of array m is the float2 {v, v} at m[x * mpitch + y]
-    // (pointers at row 0, column 0; DUP_GUARD rows above and below, DUP_MARGIN columns left and right)
-    const float2* Wd;          // vp^2 (density none or constant) or vp^2 rho
-    const float2* bxd;         // buoyancy at (x + 1/2, y)
-    const float2* byd;         // buoyancy at (x, y + 1/2)
-    const float2* C1d;         // new = C1 Lt + C2 p + NC3 p_other, NC3 = -C3 (damping, attenuation)
-    const float2* C2d;
-    const float2* NC3d;
-    int mpitch;                // float2 per medium row
+    // medium: point (x, y) of array m at m[x * mpitch + y] (pointers at row 0, column 0; MED_GUARD
+    // rows above and below, MED_MARGIN columns left and right); a thread loads columns (c, c + 1)
+    // of a field as one float2 and uses each value for both shots of its pair
+    const float* Wm;           // vp^2 (density none or constant) or vp^2 rho
+    const float* bxm;          // buoyancy at (x + 1/2, y)
+    const float* bym;          // buoyancy at (x, y + 1/2)
+    const float* C1m;          // new = C1 Lt + C2 p + NC3 p_other, NC3 = -C3 (damping, attenuation)
+    const float* C2m;
+    const float* NC3m;
+    int mpitch;                // floats per medium row
     int ymax;                  // largest (even) medium column a thread may address
     float2 wx[6], wy[6];       // FD weights over h (staggered: 5) or over h^2 (laplace: 6), {w, w}
     float k12;                 // dt^2 / 12
@@ -83,8 +84,8 @@ struct Step2D {
     long long snap_shot_stride, snap_stride;  // in float2 elements: per pair, per snapshot
 };
 
-constexpr int DUP_GUARD = 40;   // rows of the duplicated medium beyond the grid, each side
-constexpr int DUP_MARGIN = 32;  // columns of the duplicated medium beyond the grid, each side
+constexpr int MED_GUARD = 40;   // rows of the step passes' medium beyond the grid, each side
+constexpr int MED_MARGIN = 32;  // columns of the step passes' medium beyond the grid, each side
 constexpr int STEP_MAX_THREADS = 128;  // threads per CTA of the 2D passes (two columns each), at most
 constexpr int STEP_MIN_THREADS = 16;   // and at least
 

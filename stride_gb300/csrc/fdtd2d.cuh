@@ -23,9 +23,9 @@
 //     row, with one barrier per row;
 //   * input rows arrive by cp.async (zero-fill beyond the grid: Devito's zero halo of p and of
 //     `laplacian`) PF rows ahead; the update's p[t] / p[t-1] values by per-thread cp.async PF2
-//     rows ahead; each medium value is loaded one row ahead of its use;
-//   * the medium is pre-duplicated per pair ({v, v} per point), so one 16-byte load gives the
-//     packed operand of both columns.
+//     rows ahead;
+//   * the medium (one float per point and field) is loaded as the thread's two columns in one
+//     8-byte load, AHEAD rows before its use, each value serving both shots of the pair.
 // The new level is written in place of p[t-1] (each point's old value is read only by the
 // thread that writes its new value). The undersampled save of p.dt2 or of p (:398-418) is a
 // fused epilogue of pass U.
@@ -173,6 +173,15 @@ enum PassMode : int {
 #ifndef SA_PASS_MINB
 #define SA_PASS_MINB 3
 #endif
+#ifndef SA_PASS_PF
+#define SA_PASS_PF 3
+#endif
+#ifndef SA_PASS_QC
+#define SA_PASS_QC 4
+#endif
+#ifndef SA_PASS_AHEAD
+#define SA_PASS_AHEAD 2
+#endif
 
 // Geometry of a pass CTA of nt threads (nt <= STEP_MAX_THREADS, runtime): operator kind fixes
 // the reach, the mode which per-thread update rings exist. Shared memory in float4 units.
@@ -185,9 +194,9 @@ struct PassCfg {
     static constexpr int UL = STAG ? 10 : 6;   // input columns left of the thread columns
     static constexpr int UX = STAG ? 10 : 7;   // float4 of an input row beyond the threads'
     static constexpr int QU = 16;              // shared input rows (ring)
-    static constexpr int PF = 3;               // input rows prefetched ahead (QU >= R + PF + 1)
-    static constexpr int QC = 4;               // rows of the update's p[t] / p[t-1] ring
-    static constexpr int PF2 = 3;              // update rows prefetched ahead (PF <= PF2 < QC)
+    static constexpr int PF = SA_PASS_PF;      // input rows prefetched ahead (QU >= R + PF + 1)
+    static constexpr int QC = SA_PASS_QC;      // rows of the update's p[t] / p[t-1] ring
+    static constexpr int PF2 = SA_PASS_PF;     // update rows prefetched ahead (PF <= PF2 < QC)
     static constexpr bool HAS_C = MODE == PASS_U4;  // p[t] ring (U2 takes p[t] from its input queue)
     static constexpr bool HAS_P = MODE != PASS_L;   // p[t-1] ring
     __host__ __device__ static constexpr int WU(int nt) { return nt + UX; }
@@ -202,14 +211,16 @@ struct PassCfg {
     static_assert(P % 2 == 0 || !STAG, "flux buffers alternate by the parity of the period slot");
 };
 
-// The medium values one iteration of a pass uses: each is reloaded for the next iteration right
-// after its last use, so the loads are in flight for a whole row.
+// The medium values one iteration of a pass uses, each as the two values of the thread's columns
+// (c, c + 1) (used for both shots of the pair). Each is reloaded AHEAD iterations further right
+// after its last use, so the loads are in flight for AHEAD rows.
 struct PassMedium {
-    Col2 by, byb;      // buoyancy at the y-flux half-columns of the thread's pair (and its extra pair)
-    Col2 bx;           // buoyancy at the x-flux half-row
-    Col2 W;            // W at the output row
-    Col2 c1, c2, nc3;  // update coefficients at the output row
+    float2 by, byb;     // buoyancy at the y-flux half-columns of the thread's pair (and its extra pair)
+    float2 bx;          // buoyancy at the x-flux half-row
+    float2 W;           // W at the output row
+    float2 c1, c2, nc3; // update coefficients at the output row
 };
+__device__ __forceinline__ Col2 dup_c2(float2 v) { return {f2(v.x), f2(v.y)}; }
 
 template <int KIND, int MODE>
 __global__ void __launch_bounds__(STEP_MAX_THREADS, SA_PASS_MINB) fdtd2d_pass(const __grid_constant__ Step2D a) {
@@ -288,41 +299,46 @@ __global__ void __launch_bounds__(STEP_MAX_THREADS, SA_PASS_MINB) fdtd2d_pass(co
     }
 
     // ---- medium: pointers at this thread's (clamped) columns, rows added per iteration --------
+    // AHEAD sets of values rotate with the iteration (slot n % AHEAD; AHEAD divides P)
+    constexpr int AHEAD = (P % SA_PASS_AHEAD == 0) ? SA_PASS_AHEAD : 1;
     const int mp = a.mpitch;
-    const float2* __restrict__ mW = a.Wd + cm;
-    const float2* __restrict__ mBX = a.bxd + cm;
-    const float2* __restrict__ mC1 = a.C1d + cm;
-    const float2* __restrict__ mC2 = a.C2d + cm;
-    const float2* __restrict__ mC3 = a.NC3d + cm;
+    const float* __restrict__ mW = a.Wm + cm;
+    const float* __restrict__ mBX = a.bxm + cm;
+    const float* __restrict__ mC1 = a.C1m + cm;
+    const float* __restrict__ mC2 = a.C2m + cm;
+    const float* __restrict__ mC3 = a.NC3m + cm;
     // y-flux pair k = tid at half-columns y0 - 6 + 2k (and k = tid + NT for tid < 5)
-    const float2* __restrict__ mBY = a.byd + min(max(y0 - 6 + 2 * tid, -DUP_MARGIN), a.ymax);
-    const float2* __restrict__ mBYb = a.byd + min(max(y0 - 6 + 2 * (tid + NT), -DUP_MARGIN), a.ymax);
-    auto ldm = [](const float2* p) { return as_col2(__ldg(reinterpret_cast<const float4*>(p))); };
-    PassMedium md;
-    md.byb = zero_c2();
-    auto ld_by = [&](int n) {  // output row
+    const float* __restrict__ mBY = a.bym + min(max(y0 - 6 + 2 * tid, -MED_MARGIN), a.ymax);
+    const float* __restrict__ mBYb = a.bym + min(max(y0 - 6 + 2 * (tid + NT), -MED_MARGIN), a.ymax);
+    auto ldm = [](const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); };
+    PassMedium md[AHEAD];
+    auto ld_by = [&](PassMedium& m, int n) {  // output row
         const long long r = (long long)out_row(n) * mp;
-        md.by = ldm(mBY + r);
-        if (tid < 5) md.byb = ldm(mBYb + r);
+        m.by = ldm(mBY + r);
+        if (tid < 5) m.byb = ldm(mBYb + r);
     };
-    auto ld_bx = [&](int n) { md.bx = ldm(mBX + (long long)(i0 + n - 5) * mp); };  // x-flux half-row
-    auto ld_W = [&](int n) { md.W = ldm(mW + (long long)out_row(n) * mp); };
-    auto ld_upd = [&](int n) {
+    auto ld_bx = [&](PassMedium& m, int n) { m.bx = ldm(mBX + (long long)(i0 + n - 5) * mp); };  // x-flux half-row
+    auto ld_W = [&](PassMedium& m, int n) { m.W = ldm(mW + (long long)out_row(n) * mp); };
+    auto ld_upd = [&](PassMedium& m, int n) {
         if constexpr (MODE != PASS_L) {
             const int ro = out_row(n);
             if (ro < xo0 || ro >= xo1 || !out_t || a.wg_only) return;
             const long long r = (long long)ro * mp;
-            md.c1 = ldm(mC1 + r);
-            md.c2 = ldm(mC2 + r);
-            md.nc3 = ldm(mC3 + r);
+            m.c1 = ldm(mC1 + r);
+            m.c2 = ldm(mC2 + r);
+            m.nc3 = ldm(mC3 + r);
         }
     };
-    if constexpr (VARB) {
-        ld_by(0);
-        ld_bx(0);
+#pragma unroll
+    for (int k = 0; k < AHEAD; k++) {
+        md[k].byb = make_float2(0.f, 0.f);
+        if constexpr (VARB) {
+            ld_by(md[k], k);
+            ld_bx(md[k], k);
+        }
+        ld_W(md[k], k);
+        ld_upd(md[k], k);
     }
-    ld_W(0);
-    ld_upd(0);
 
     // ---- register queues (slot = iteration number mod P): input rows, staggered x-fluxes -------
     Col2 uq[P], fq[STAG ? P : 1];
@@ -341,6 +357,7 @@ __global__ void __launch_bounds__(STEP_MAX_THREADS, SA_PASS_MINB) fdtd2d_pass(co
             if (n >= niter) return;  // uniform: the barrier below is reached by all or none
             const int par = K & 1;
             const bool outn = n >= 2 * R;
+            PassMedium& m = md[K % AHEAD];
 
             // ---- phase A: y-fluxes of the output row (its input row is visible since earlier
             // barriers) into this iteration's flux buffer ----------------------------------------
@@ -349,15 +366,15 @@ __global__ void __launch_bounds__(STEP_MAX_THREADS, SA_PASS_MINB) fdtd2d_pass(co
                     // input row r = i - R: index e <-> column L0 + e; pair k at half-columns y0 - 6 + 2k
                     const float4* urow = sU + ((n - R) & (QU - 1)) * WU;
                     Col2 F = yflux_pair(urow, tid, wy);
-                    if constexpr (VARB) F = mul_c2(F, md.by);
+                    if constexpr (VARB) F = mul_c2(F, dup_c2(m.by));
                     sF[par * NF + tid] = as_f4(F);
                     if (tid < 5) {
                         Col2 Fb = yflux_pair(urow, tid + NT, wy);
-                        if constexpr (VARB) Fb = mul_c2(Fb, md.byb);
+                        if constexpr (VARB) Fb = mul_c2(Fb, dup_c2(m.byb));
                         sF[par * NF + tid + NT] = as_f4(Fb);
                     }
                 }
-                if constexpr (VARB) ld_by(n + 1);
+                if constexpr (VARB) ld_by(m, n + AHEAD);
             }
             cp_async_wait<PF - 1>();
             __syncthreads();  // input row i, this iteration's fluxes visible; the previous iteration done
@@ -370,10 +387,10 @@ __global__ void __launch_bounds__(STEP_MAX_THREADS, SA_PASS_MINB) fdtd2d_pass(co
             if constexpr (STAG) {
                 if (n >= R) {  // x-flux at half-row i - 5 from input rows i - 9 .. i
                     Col2 fx = qstag<P, K, -4, -5>(uq, wx);
-                    if constexpr (VARB) fx = mul_c2(fx, md.bx);
+                    if constexpr (VARB) fx = mul_c2(fx, dup_c2(m.bx));
                     fq[K] = fx;
                 }
-                if constexpr (VARB) ld_bx(n + 1);
+                if constexpr (VARB) ld_bx(m, n + AHEAD);
             }
             if (outn) {
                 Col2 g;
@@ -393,13 +410,13 @@ __global__ void __launch_bounds__(STEP_MAX_THREADS, SA_PASS_MINB) fdtd2d_pass(co
                 const long long idx = (long long)r * pitch + c;  // float2 index within the pair
                 Col2 res;
                 if constexpr (MODE == PASS_L) {
-                    res = mul_c2(md.W, g);  // l; rows and columns beyond the grid are never stored (zero)
+                    res = mul_c2(dup_c2(m.W), g);  // l; rows and columns beyond the grid are never stored (zero)
                 } else {
                     Col2 Lt;
                     if constexpr (MODE == PASS_U4) {
-                        Lt = fma_c2(mul_c2(md.W, {f2(a.k12), f2(a.k12)}), g, in_r);
+                        Lt = fma_c2(dup_c2(make_float2(m.W.x * a.k12, m.W.y * a.k12)), g, in_r);
                     } else {
-                        Lt = mul_c2(md.W, g);
+                        Lt = mul_c2(dup_c2(m.W), g);
                     }
                     if (out_t) {
                         const Col2 u_o = CF::HAS_C ? ld_c2(sC + (n & (QC - 1)) * NT + tid) : in_r;
@@ -407,8 +424,8 @@ __global__ void __launch_bounds__(STEP_MAX_THREADS, SA_PASS_MINB) fdtd2d_pass(co
                         if (a.wg_only) {
                             res = Lt;
                         } else {
-                            res.a = fma2(md.c1.a, Lt.a, fma2(md.c2.a, u_o.a, mul2(md.nc3.a, pm.a)));
-                            res.b = fma2(md.c1.b, Lt.b, fma2(md.c2.b, u_o.b, mul2(md.nc3.b, pm.b)));
+                            res.a = fma2(f2(m.c1.x), Lt.a, fma2(f2(m.c2.x), u_o.a, mul2(f2(m.nc3.x), pm.a)));
+                            res.b = fma2(f2(m.c1.y), Lt.b, fma2(f2(m.c2.y), u_o.b, mul2(f2(m.nc3.y), pm.b)));
                         }
                         if (do_save) {
                             float2* snap = reinterpret_cast<float2*>(a.snaps) + (long long)pair * a.snap_shot_stride +
@@ -432,8 +449,8 @@ __global__ void __launch_bounds__(STEP_MAX_THREADS, SA_PASS_MINB) fdtd2d_pass(co
                     else *dst = res.a;
                 }
             }
-            ld_W(n + 1);
-            ld_upd(n + 1);
+            ld_W(m, n + AHEAD);
+            ld_upd(m, n + AHEAD);
         });
     }
     cp_async_wait<0>();

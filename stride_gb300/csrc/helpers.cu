@@ -150,43 +150,39 @@ cudaError_t medium2d(const float* vp_in, const float* rho_in, const float* alpha
     return cudaGetLastError();
 }
 
-// Pair-duplicated medium of the 2D step passes: six arrays (W, bx, by, C1, C2, -C3), each
-// [nx + 2 DUP_GUARD][mpitch] float2 {v, v}, `astride` float2 apart, column y at index
-// y + DUP_MARGIN (one array per field: a warp's 16-byte loads of one field are contiguous).
-// Beyond what the source arrays hold, a value is the nearest held one: the edge-padded halo of
-// the materials (stride/physics/common/devito.py:805-841) for the half-point buoyancy, any
-// finite value elsewhere (it only reaches lanes the kernel discards). W, C1..C3 address row 0
-// (columns 0..ny-1); bxh half-row 0 (half-rows -5..nx+3); byh row 0 with half-column y at
-// column y + 6 (y = -6..ny+3). bxh/byh may be null (no buoyancy).
-__global__ void k_dup_medium2d(const float* __restrict__ W, const float* __restrict__ bxh,
-                               const float* __restrict__ byh, const float* __restrict__ C1,
-                               const float* __restrict__ C2, const float* __restrict__ C3, int nx, int ny, int pitch,
-                               int pitch_b, int mpitch, long long astride, float2* __restrict__ out) {
-    const int rows = nx + 2 * DUP_GUARD;
+// Medium of the 2D step passes: six arrays (W, bx, by, C1, C2, -C3), each
+// [nx + 2 MED_GUARD][mpitch] floats, `astride` floats apart, column y at index y + MED_MARGIN
+// (one array per field: a warp's loads of one field are contiguous). Beyond what the source
+// arrays hold, a value is the nearest held one: the edge-padded halo of the materials
+// (stride/physics/common/devito.py:805-841) for the half-point buoyancy, any finite value
+// elsewhere (it only reaches lanes the kernel discards). W, C1..C3 address row 0 (columns
+// 0..ny-1); bxh half-row 0 (half-rows -5..nx+3); byh row 0 with half-column y at column y + 6
+// (y = -6..ny+3). bxh/byh may be null (no buoyancy).
+__global__ void k_step_medium2d(const float* __restrict__ W, const float* __restrict__ bxh,
+                                const float* __restrict__ byh, const float* __restrict__ C1,
+                                const float* __restrict__ C2, const float* __restrict__ C3, int nx, int ny, int pitch,
+                                int pitch_b, int mpitch, long long astride, float* __restrict__ out) {
+    const int rows = nx + 2 * MED_GUARD;
     const long long n = (long long)rows * mpitch;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
          q += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(q / mpitch) - DUP_GUARD, y = (int)(q % mpitch) - DUP_MARGIN;
+        const int x = (int)(q / mpitch) - MED_GUARD, y = (int)(q % mpitch) - MED_MARGIN;
         const int xn = min(max(x, 0), nx - 1), yn = min(max(y, 0), ny - 1);
         const long long node = (long long)xn * pitch + yn;
-        const float vals[6] = {
-            W[node],
-            bxh ? bxh[(long long)min(max(x, -5), nx + 3) * pitch + yn] : 1.f,
-            byh ? byh[(long long)xn * pitch_b + min(max(y, -6), ny + 3) + 6] : 1.f,
-            C1[node],
-            C2[node],
-            -C3[node],
-        };
-#pragma unroll
-        for (int k = 0; k < 6; k++) out[k * astride + q] = make_float2(vals[k], vals[k]);
+        out[q] = W[node];
+        out[astride + q] = bxh ? bxh[(long long)min(max(x, -5), nx + 3) * pitch + yn] : 1.f;
+        out[2 * astride + q] = byh ? byh[(long long)xn * pitch_b + min(max(y, -6), ny + 3) + 6] : 1.f;
+        out[3 * astride + q] = C1[node];
+        out[4 * astride + q] = C2[node];
+        out[5 * astride + q] = -C3[node];
     }
 }
 
-cudaError_t dup_medium2d(const float* W, const float* bxh, const float* byh, const float* C1, const float* C2,
-                         const float* C3, int nx, int ny, int pitch, int pitch_b, float2* out, cudaStream_t s) {
-    const int mp = dup_pitch(ny);
-    k_dup_medium2d<<<1024, 256, 0, s>>>(W, bxh, byh, C1, C2, C3, nx, ny, pitch, pitch_b, mp,
-                                        (long long)(nx + 2 * DUP_GUARD) * mp, out);
+cudaError_t step_medium2d(const float* W, const float* bxh, const float* byh, const float* C1, const float* C2,
+                          const float* C3, int nx, int ny, int pitch, int pitch_b, float* out, cudaStream_t s) {
+    const int mp = med_pitch(ny);
+    k_step_medium2d<<<1024, 256, 0, s>>>(W, bxh, byh, C1, C2, C3, nx, ny, pitch, pitch_b, mp,
+                                         (long long)(nx + 2 * MED_GUARD) * mp, out);
     return cudaGetLastError();
 }
 

@@ -16,28 +16,28 @@ cudaError_t medium2d(const float* vp_in, const float* rho_in, const float* alpha
                      int pitch_b, int density, double db_to_np, const Sponge& sp, float dt, float* W, float* vp,
                      float* alpha, float* buoy, float* bxh, float* byh, float* C1, float* C2, float* C3,
                      cudaStream_t s);
-// Row pitch (float2) of the duplicated medium of an ny-column grid, and the largest even column a
-// step thread may address in it.
-inline int dup_pitch(int ny) { return (ny + 2 * DUP_MARGIN + 15) / 16 * 16; }
-inline int dup_ymax(int ny) { return (ny + DUP_MARGIN - 2) & ~1; }
-// Float2 elements of the six duplicated medium arrays of an nx x ny grid.
-inline size_t dup_medium_size(int nx, int ny) { return (size_t)6 * (nx + 2 * DUP_GUARD) * dup_pitch(ny); }
-// The step passes' duplicated medium (helpers.cu k_dup_medium2d), dup_medium_size(nx, ny) float2.
-cudaError_t dup_medium2d(const float* W, const float* bxh, const float* byh, const float* C1, const float* C2,
-                         const float* C3, int nx, int ny, int pitch, int pitch_b, float2* out, cudaStream_t s);
-// Points a step's medium fields at a duplicated-medium allocation of an nx x ny grid.
-inline void step_medium(Step2D& a, const float2* dmed, int nx, int ny) {
-    const int mp = dup_pitch(ny);
-    const long long astride = (long long)(nx + 2 * DUP_GUARD) * mp;
-    const float2* at0 = dmed + (long long)DUP_GUARD * mp + DUP_MARGIN;
-    a.Wd = at0;
-    a.bxd = at0 + astride;
-    a.byd = at0 + 2 * astride;
-    a.C1d = at0 + 3 * astride;
-    a.C2d = at0 + 4 * astride;
-    a.NC3d = at0 + 5 * astride;
+// Row pitch (floats, even) of the step passes' medium for an ny-column grid, and the largest even
+// column a step thread may address in it.
+inline int med_pitch(int ny) { return (ny + 2 * MED_MARGIN + 15) / 16 * 16; }
+inline int med_ymax(int ny) { return (ny + MED_MARGIN - 2) & ~1; }
+// Floats of the six medium arrays of an nx x ny grid.
+inline size_t step_medium_size(int nx, int ny) { return (size_t)6 * (nx + 2 * MED_GUARD) * med_pitch(ny); }
+// The step passes' medium (helpers.cu k_step_medium2d), step_medium_size(nx, ny) floats.
+cudaError_t step_medium2d(const float* W, const float* bxh, const float* byh, const float* C1, const float* C2,
+                          const float* C3, int nx, int ny, int pitch, int pitch_b, float* out, cudaStream_t s);
+// Points a step's medium fields at a step-medium allocation of an nx x ny grid.
+inline void step_medium(Step2D& a, const float* med, int nx, int ny) {
+    const int mp = med_pitch(ny);
+    const long long astride = (long long)(nx + 2 * MED_GUARD) * mp;
+    const float* at0 = med + (long long)MED_GUARD * mp + MED_MARGIN;
+    a.Wm = at0;
+    a.bxm = at0 + astride;
+    a.bym = at0 + 2 * astride;
+    a.C1m = at0 + 3 * astride;
+    a.C2m = at0 + 4 * astride;
+    a.NC3m = at0 + 5 * astride;
     a.mpitch = mp;
-    a.ymax = dup_ymax(ny);
+    a.ymax = med_ymax(ny);
 }
 // The step's FD weights over the spacing (kind 0: the 10th-order Laplacian's over h^2; else the
 // staggered first derivative's over h), dt^2 / 12 and 1 / dt^2.

@@ -4,8 +4,8 @@
 // whole device to a memory pool it manages and forbids allocations outside it, or a loop that
 // must not pay for cudaMalloc/cudaFree (cudaFree synchronises the device). For them this entry
 // point runs the same time-step kernels as sa_forward, but keeps every scratch buffer (the two
-// wavefield levels, the intermediate level of OT4, the medium copies and their pair-duplicated
-// form, the point lists and the time-major traces) in one file-scope __device__ array of
+// wavefield levels, the intermediate level of OT4, the medium copies and the step passes' form
+// of them, the point lists and the time-major traces) in one file-scope __device__ array of
 // kScratchBytes. The caller passes the inputs and the output.
 //
 // Limits and behaviour:
@@ -180,7 +180,7 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
     float* tcoef = cv.take<float>((size_t)4 * kMaxSrc);
     int* tpoint = cv.take<int>((size_t)4 * kMaxSrc);
     sa::Gather* gat = cv.take<sa::Gather>(kMaxRec);
-    float2* dmed = cv.take<float2>(sa::dup_medium_size(nx, ny));  // the step passes' pair-duplicated medium
+    float* smed = cv.take<float>(sa::step_medium_size(nx, ny));  // the step passes' medium
     float* lbuf = ot4 ? cv.take<float>(2 * pe) : nullptr;          // OT4's intermediate level
     if (cv.used > kScratchBytes) return err(SA_E_INVALID, "grid, traces and lists exceed the 64 MiB scratch array");
 
@@ -206,10 +206,10 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
                      W + g0, vps, als, buoy, bxh ? bxh + (long long)(sa::GUARD + 5) * pitch : nullptr,
                      byh ? byh + (long long)sa::GUARD * pitch_b : nullptr, C1 + g0, C2 + g0, C3 + g0, s) != cudaSuccess)
         return err(SA_E_CUDA, "medium preparation kernel failed");
-    if (sa::dup_medium2d(W + g0, bxh ? bxh + (long long)(sa::GUARD + 5) * pitch : nullptr,
-                         byh ? byh + (long long)sa::GUARD * pitch_b : nullptr, C1 + g0, C2 + g0, C3 + g0, nx, ny, pitch,
-                         pitch_b, dmed, s) != cudaSuccess)
-        return err(SA_E_CUDA, "medium duplication kernel failed");
+    if (sa::step_medium2d(W + g0, bxh ? bxh + (long long)(sa::GUARD + 5) * pitch : nullptr,
+                          byh ? byh + (long long)sa::GUARD * pitch_b : nullptr, C1 + g0, C2 + g0, C3 + g0, nx, ny, pitch,
+                          pitch_b, smed, s) != cudaSuccess)
+        return err(SA_E_CUDA, "step medium kernel failed");
 
     // ---- point lists (host arrays on the stack, copied into the scratch array) -----------
     const double h = std::max(d.spacing[0], d.spacing[1]);
@@ -302,7 +302,7 @@ extern "C" int sa_forward_2d_noalloc(const sa_desc* desc, const float* vp, const
     a.chunk_rows = chunk_rows;
     a.by = by;
     a.lbuf = lbuf;
-    sa::step_medium(a, dmed, nx, ny);
+    sa::step_medium(a, smed, nx, ny);
     sa::step_weights(a, kind, d.spacing[0], d.spacing[1], d.dt);
     a.f = d.undersampling > 0 ? d.undersampling : 4;
     const dim3 grid(nstrips, nchunks, 1);

@@ -106,9 +106,9 @@ struct sa_plan {
     // row 0 / half-row 0); vp, alpha, buoy are unguarded scratch of the preparation kernels
     float *W = nullptr, *vp = nullptr, *alpha = nullptr, *buoy = nullptr, *bxh = nullptr, *byh = nullptr;
     float *C1 = nullptr, *C2 = nullptr, *C3 = nullptr;
-    // the step passes' pair-duplicated copies of W, bxh, byh, C1, C2, -C3 (dup_medium2d)
-    float2* dmed = nullptr;
-    size_t cap_dmed = 0;
+    // the step passes' copies of W, bxh, byh, C1, C2, -C3 (step_medium2d)
+    float* smed = nullptr;
+    size_t cap_smed = 0;
     size_t cap_W = 0, cap_vp = 0, cap_alpha = 0, cap_buoy = 0, cap_bxh = 0, cap_byh = 0, cap_C1 = 0, cap_C2 = 0,
            cap_C3 = 0;
     std::vector<float> vp_host;  // for the injection coefficients (vp at the corners)
@@ -197,6 +197,10 @@ struct sa_plan {
     long long fwd_launches[4] = {0, 0, 0, 0};  // kernels in each forward loop (by save mode)
     long long adj_launches[5] = {0, 0, 0, 0, 0};  // kernels in each adjoint loop
     bool use_graphs = true;
+    // L2 residency of the duplicated medium: every shot pair's CTAs read each of its rows once per
+    // pass, just after the previous pass streamed the wavefields through L2; the captured step
+    // kernels carry this persisting window
+    cudaAccessPolicyWindow l2win{};
     long long launches = 0;                   // kernels launched by the last sa_forward / sa_adjoint
 };
 
@@ -458,7 +462,7 @@ sa::Step2D base_args(const sa_plan* p) {
     a.chunk_rows = p->chunk_rows;
     a.by = p->by;
     a.lbuf = p->lbuf;
-    sa::step_medium(a, p->dmed, p->nx, p->ny);
+    sa::step_medium(a, p->smed, p->nx, p->ny);
     sa::step_weights(a, p->kind, p->d.spacing[0], p->d.spacing[1], p->d.dt);
     a.f = p->d.undersampling;
     a.snaps = p->snaps;
@@ -867,6 +871,47 @@ int issue_adjoint_exact(sa_plan* p, cudaStream_t s) {
 }
 
 // Runs `issue` through a cached CUDA graph (captured on the plan's own stream) or directly.
+int medium_l2_window(sa_plan* p) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    int max_persist = 0, max_window = 0;
+    CK(cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev));
+    CK(cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, dev));
+    const size_t bytes = std::min(sa::step_medium_size(p->nx, p->ny) * sizeof(float), (size_t)std::max(0, max_window));
+    p->l2win = cudaAccessPolicyWindow{};
+    if (max_persist <= 0 || bytes == 0) return SA_OK;  // no persisting L2 on this device
+    size_t limit = 0;
+    CK(cudaDeviceGetLimit(&limit, cudaLimitPersistingL2CacheSize));
+    const size_t want = std::min(bytes, (size_t)max_persist);
+    if (limit < want) {  // a limit of this process's context: raised, never lowered
+        CK(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want));
+        limit = want;
+    }
+    p->l2win.base_ptr = p->smed;
+    p->l2win.num_bytes = bytes;
+    p->l2win.hitRatio = (float)std::min(1.0, (double)limit / (double)bytes);
+    p->l2win.hitProp = cudaAccessPropertyPersisting;
+    p->l2win.missProp = cudaAccessPropertyStreaming;
+    return SA_OK;
+}
+
+// Gives every kernel node of a captured loop the medium's persisting L2 window.
+int apply_l2_window(const sa_plan* p, cudaGraph_t graph) {
+    if (!p->l2win.num_bytes) return SA_OK;
+    size_t n = 0;
+    CK(cudaGraphGetNodes(graph, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    CK(cudaGraphGetNodes(graph, nodes.data(), &n));
+    cudaKernelNodeAttrValue v{};
+    v.accessPolicyWindow = p->l2win;
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType t;
+        CK(cudaGraphNodeGetType(nd, &t));
+        if (t == cudaGraphNodeTypeKernel) CK(cudaGraphKernelNodeSetAttribute(nd, cudaKernelNodeAttributeAccessPolicyWindow, &v));
+    }
+    return SA_OK;
+}
+
 template <class F>
 int run_loop(sa_plan* p, cudaGraphExec_t* slot, cudaStream_t s, F issue) {
     if (!p->use_graphs) return issue(s);
@@ -881,6 +926,11 @@ int run_loop(sa_plan* p, cudaGraphExec_t* slot, cudaStream_t s, F issue) {
             return rc;
         }
         if (ce != cudaSuccess) return fail(SA_E_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+        const int wr = apply_l2_window(p, graph);
+        if (wr != SA_OK) {
+            cudaGraphDestroy(graph);
+            return wr;
+        }
         const cudaError_t ie = cudaGraphInstantiate(slot, graph, 0);
         cudaGraphDestroy(graph);
         if (ie != cudaSuccess) {
@@ -1097,12 +1147,13 @@ int sa_plan_destroy(sa_plan* p) {
         return SA_OK;
     }
     drop_graphs(p);
+    if (p->l2win.num_bytes) cudaCtxResetPersistingL2Cache();  // its lines go back to normal eviction
     void* bufs[] = {p->field[0], p->field[1], p->W, p->vp, p->alpha, p->buoy, p->bxh, p->byh, p->C1, p->C2, p->C3,
                     p->medium_stage,
                     p->gat_flat,
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
-                    p->dmed, p->lbuf, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
+                    p->smed, p->lbuf, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
                     p->dbx, p->dby, p->pml_prof, p->pml_aux, p->pml_ck, p->pml_aux_f, p->ckpt2, p->pml_ck2,
                     p->wgrad, p->hgat, p->hgat_src, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
                     p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx, p->xtgt.off, p->xtgt.point, p->xtgt.coef};
@@ -1142,13 +1193,14 @@ int sa_set_medium(sa_plan* p, const float* vp, const float* rho, const float* al
                     const_cast<float*>(row0(p, p->C1, p->pitch)), const_cast<float*>(row0(p, p->C2, p->pitch)),
                     const_cast<float*>(row0(p, p->C3, p->pitch)), 0));
     {
-        float2* old = p->dmed;
-        CKR(ensure(&p->dmed, &p->cap_dmed, sa::dup_medium_size(p->nx, p->ny)));
-        if (old != p->dmed) drop_graphs(p);  // the captured step launches hold the medium pointers
-        CK(sa::dup_medium2d(row0(p, p->W, p->pitch), p->bxh ? row0(p, p->bxh, p->pitch, 5) : nullptr,
-                            p->byh ? row0(p, p->byh, p->pitch_b) : nullptr, row0(p, p->C1, p->pitch),
-                            row0(p, p->C2, p->pitch), row0(p, p->C3, p->pitch), p->nx, p->ny, p->pitch, p->pitch_b,
-                            p->dmed, 0));
+        float* old = p->smed;
+        CKR(ensure(&p->smed, &p->cap_smed, sa::step_medium_size(p->nx, p->ny)));
+        if (old != p->smed) drop_graphs(p);  // the captured step launches hold the medium pointers
+        CK(sa::step_medium2d(row0(p, p->W, p->pitch), p->bxh ? row0(p, p->bxh, p->pitch, 5) : nullptr,
+                             p->byh ? row0(p, p->byh, p->pitch_b) : nullptr, row0(p, p->C1, p->pitch),
+                             row0(p, p->C2, p->pitch), row0(p, p->C3, p->pitch), p->nx, p->ny, p->pitch, p->pitch_b,
+                             p->smed, 0));
+        CKR(medium_l2_window(p));
     }
     CK(cudaDeviceSynchronize());
     p->vp_host.resize(N);
