@@ -37,10 +37,10 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 HBM_FALLBACK_GBS = 6800.0
-# dram__bytes_read.sum + dram__bytes_write.sum of one fdtd2d_step launch on this workload's
-# batch (64 shots of 552^2, forward step with wavefield save), from an ncu capture of that
-# launch: a fixed figure of the kernel, not measured by this run.
-NCU_TRAFFIC_PER_LAUNCH = 179.700992e6 + 102.897664e6
+# dram__bytes_read.sum + dram__bytes_write.sum of one time step of this workload's batch (64 shots
+# of 552^2: one launch each of the two step passes, a forward step), from an ncu capture of those
+# launches: a fixed figure of the kernels, not measured by this run.
+NCU_TRAFFIC_PER_STEP = (101.428224e6 + 37.445120e6) + (263.725312e6 + 52.639232e6)
 
 
 WORKLOADS = {
@@ -565,12 +565,12 @@ def gb300_arm(args):
                                    % (2 * N * n_shots * 4 / 1e9 + snap_gb)},
             'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                          'frac': achieved / peak, 'peak_source': peak_kind,
-                         'traffic': NCU_TRAFFIC_PER_LAUNCH if args.workload == 'fwdadj64' else None,
-                         'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one forward step '
-                                           'launch of this workload (a profile figure, not measured in this run)'
-                                           if args.workload == 'fwdadj64' else None,
+                         'traffic': NCU_TRAFFIC_PER_STEP if args.workload == 'fwdadj64' else None,
+                         'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one forward time '
+                                           'step (passes L and U) of this workload (a profile figure, not measured '
+                                           'in this run)' if args.workload == 'fwdadj64' else None,
                          'alg_bytes_per_point': {'forward': b_fwd, 'adjoint': b_adj if grad_mode else None},
-                         'kernel': 'fdtd2d_step' if dim == 2 else 'fdtd3d_pass',
+                         'kernel': 'fdtd2d_pass (L + U per time step)' if dim == 2 else 'fdtd3d_pass',
                          'step_ms': per_step_s * 1e3},
             'cpu_baseline': cpu, 'e2e': e2e, 'gpu_launches': launches['n'], 'clocks': clk.summary(),
             'forward_ms': t_fwd, 'adjoint_ms': t_adj if grad_mode else None,
