@@ -55,6 +55,7 @@ WORKLOADS = {
     'fwi': ('single', 32, 'fwi'),           # plain vs learned-preconditioned FWI, wall time to a vp error
     'rho64': ('batched', 64, 'fwdadj'),     # vp and rho gradients from the raw saved wavefield
     'pml64': ('batched', 64, 'fwdadj'),     # vp gradient with the CFS-PML boundary (OT2)
+    'ckpt64': ('batched', 64, 'fwdadj'),    # the default gradient from checkpoints every 50 steps with recompute
 }
 # gradient method per workload: the reference imaging condition from snapshots (default), the
 # same from checkpoints with recompute, or the exact discrete adjoint from checkpoints
@@ -64,6 +65,7 @@ GRADIENT = {
     '3dgrad8': ('checkpoints', dict(undersampling=4, checkpoint_budget=150e9)),
     'rho64': ('raw', dict(undersampling=4)),
     'pml64': ('snapshots', dict(undersampling=4, kernel='OT2', boundary='pml', f_centre=1.0e6)),
+    'ckpt64': ('checkpoints', dict(undersampling=4, checkpoint_interval=50)),
 }
 # time step of the workload's grid as a CFL number (OT2 needs one below its stability limit)
 CFL = {'pml64': 0.4}
@@ -86,6 +88,8 @@ WORKLOAD_NAMES = {
              'vp/rho/alpha phantom, 64 shots x 256 receivers, 4000 steps, OT4, f=4',
     'pml64': '2D fwd+adj vp gradient with the CFS-PML boundary: 552^2 extended (20-cell PML), vp/rho/alpha phantom, '
              '64 shots x 256 receivers, 4000 steps, OT2 at CFL 0.4, f=4',
+    'ckpt64': '2D fwd+adj vp gradient: 552^2 extended, vp/rho/alpha phantom, 64 shots x 256 receivers, 4000 steps, '
+              'OT4, f=4, forward wavefield checkpointed every 50 steps and recomputed for the imaging condition',
     'fwi': 'FWI of seeded 256^2 ellipse phantoms at 0.5 mm (296^2 extended), 32 shots x 128 receivers, 2000 steps, '
            '500 kHz, f_max 0.5 MHz: plain (reference loop, GPU pipelines) vs U-Net-preconditioned (BF16 tcgen05, '
            'trained on plain-FWI paths of held-out seeds), wall time to the target relative vp error',
