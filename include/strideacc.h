@@ -55,6 +55,17 @@ extern "C" {
                                  point; needs SA_SAVE_CHECKPOINTS; 2D and 3D plans. No counterpart in the
                                  reference (whose gradient is SA_GRAD_PARITY) */
 
+/* Options of sa_plan_option (no counterpart in the reference). */
+#define SA_OPT_PERSISTENT 1     /* 2D forward without a saved wavefield as one persistent cooperative launch
+                                   (linear interpolation, sponge): -1 never, 0 when the batch is small
+                                   (default), 1 whenever eligible; the traces equal the step passes' bit for
+                                   bit, and the call synchronises its stream to check the barrier status */
+#define SA_OPT_BARRIER_EXTRA 2  /* for tests of the timeout path: the persistent launch's grid barrier waits
+                                   for this many CTAs more than it launches, so its first wait gives up and
+                                   sa_forward returns SA_E_TIMEOUT (default 0) */
+#define SA_OPT_BARRIER_SPIN 3   /* polls (about 0.1 us each) before a persistent barrier wait gives up and sets
+                                   the kernel's error flag (default 10^7, about a second) */
+
 /* Plan description (stride/physics/iso_acoustic/devito.py:119-183 defaults; shapes are the
  * extended grid of stride/problem/domain.py:48-74). */
 typedef struct sa_desc {
@@ -284,6 +295,9 @@ int sa_last_error(char* buf, int len);
 
 /* Kernel launches the last sa_forward/sa_adjoint issued (for throughput accounting). */
 long long sa_launch_count(const sa_plan* plan);
+
+/* Sets a plan option (SA_OPT_*). No counterpart in the reference. */
+int sa_plan_option(sa_plan* plan, int option, long long value);
 
 /* The launch layout of a 2D plan's time-step passes (after sa_autotune, the tuned one): threads
  * per CTA (two grid columns each), column strips and row chunks of the grid; 3D plans report

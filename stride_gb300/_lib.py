@@ -18,6 +18,9 @@ SA_E_UNSUPPORTED = -2
 SA_E_CUDA = -3
 SA_E_NOMEM = -4
 SA_E_TIMEOUT = -5
+SA_OPT_PERSISTENT = 1
+SA_OPT_BARRIER_EXTRA = 2
+SA_OPT_BARRIER_SPIN = 3
 
 SA_KERNEL_OT2 = 2
 SA_KERNEL_OT4 = 4
@@ -38,7 +41,7 @@ SA_GRAD_EXACT = 1
 # every symbol include/strideacc.h declares
 EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometry', 'sa_forward',
            'sa_adjoint', 'sa_adjoint_wavelets', 'sa_adjoint_grads', 'sa_autotune', 'sa_last_error', 'sa_launch_count',
-           'sa_plan_layout', 'sa_checkpoint_schedule',
+           'sa_plan_layout', 'sa_plan_option', 'sa_checkpoint_schedule',
            'sa_forward_2d_noalloc',
            'sa_traces_sosfilt', 'sa_traces_fir', 'sa_traces_check', 'sa_traces_norm_per_shot', 'sa_traces_mute',
            'sa_field_mul', 'sa_field_clip', 'sa_field_axpy', 'sa_field_slowness_step', 'sa_field_stats',
@@ -90,6 +93,7 @@ def load():
     lib.sa_launch_count.restype = ctypes.c_longlong
     IP = ctypes.POINTER(I)
     lib.sa_plan_layout.argtypes = [P, IP, IP, IP]
+    lib.sa_plan_option.argtypes = [P, I, ctypes.c_longlong]
     lib.sa_checkpoint_schedule.argtypes = [ctypes.POINTER(SaDesc), I, IP, IP, IP]
     L = ctypes.c_longlong
     F = ctypes.c_float
@@ -271,6 +275,10 @@ class Plan:
     @property
     def launches(self):
         return int(load().sa_launch_count(self._h))
+
+    def set_option(self, option, value):
+        """sa_plan_option: SA_OPT_PERSISTENT, SA_OPT_BARRIER_EXTRA or SA_OPT_BARRIER_SPIN."""
+        check(load().sa_plan_option(self._h, int(option), int(value)))
 
     @property
     def layout(self):

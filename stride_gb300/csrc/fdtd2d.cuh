@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(STEP_MAX_THREADS, SA_PASS_MINB) fdtd2d_pass(co
             constexpr int K = decltype(KC)::value;
             const int n = base + K;
             if (n >= niter) return;  // uniform: the barrier below is reached by all or none
-            const int par = K & 1;
+            [[maybe_unused]] const int par = K & 1;
             const bool outn = n >= 2 * R;
             PassMedium& m = md[K % AHEAD];
 
@@ -405,7 +405,7 @@ __global__ void __launch_bounds__(STEP_MAX_THREADS, SA_PASS_MINB) fdtd2d_pass(co
                     const Col2 gy = ycent_pair(sU + ((n - R) & (QU - 1)) * WU, tid, wy);
                     g = add_c2(gx, gy);
                 }
-                const Col2 in_r = uq[((K - R) % P + P) % P];  // the input at the output row
+                [[maybe_unused]] const Col2 in_r = uq[((K - R) % P + P) % P];  // the input at the output row
                 const int r = out_row(n);
                 const long long idx = (long long)r * pitch + c;  // float2 index within the pair
                 Col2 res;

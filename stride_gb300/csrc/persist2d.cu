@@ -1,0 +1,281 @@
+// Persistent 2D forward for batches too small to fill the GPU with the streaming step passes.
+//
+// One cooperative launch runs every time step of the forward (the loop OperatorDevito.run drives,
+// stride/physics/common/devito.py:1025-1070): each CTA owns a tile of one shot pair, keeps the tile
+// and its halo in shared memory for the step, and CTAs meet at one grid-wide barrier per step.
+// A step of a CTA:
+//   1. p[t] over the tile and a halo of 2R (OT4) or R (OT2) points into shared memory (zero beyond
+//      the grid, Devito's halo of p);
+//   2. OT4: l = W G(p[t]) over the tile and R more (zero beyond the grid, as Devito's `laplacian`),
+//      recomputed by each CTA for its halo so that no second barrier is needed;
+//   3. the update of the tile, p[t+1] = C1 Lt + C2 p[t] - C3 p[t-1], in place of p[t-1];
+//   4. the sources of step t at the tile's points (iso_acoustic/devito.py:357-363), each target
+//      point's entries summed in a fixed order;
+//   5. the barrier, then the receivers of step t, rec[t] = interp(p[t+1]) (:364), spread over CTAs.
+// Every point's arithmetic is the step passes' (fdtd2d.cuh) operation for operation, so the traces
+// equal the streaming forward's bit for bit.
+//
+// The barrier waits are bounded: a wait that gives up sets an error flag, and every CTA leaves the
+// time loop at its next barrier; the host reports SA_E_TIMEOUT.
+#include <cooperative_groups.h>
+
+#include "fdtd2d.cuh"
+#include "persist2d.h"
+
+namespace sa {
+
+namespace {
+
+// Grid-wide barrier of a cooperative launch with a bounded wait. Returns false when this CTA's
+// wait gave up or another CTA's did (the error flag); the caller then leaves its time loop.
+__device__ bool grid_barrier(unsigned* bar, int* err, int expected, long long spin_limit) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = bar + 1;
+        volatile int* verr = err;
+        const unsigned g = *gen;
+        __threadfence();  // this CTA's writes of the step before its arrival
+        const unsigned arrived = atomicAdd(bar, 1u) + 1u;
+        int ok = 1;
+        if (arrived == (unsigned)expected) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);  // release the others
+        } else {
+            long long k = 0;
+            while (*gen == g) {
+                if (*verr || ++k > spin_limit) {
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(100);
+            }
+            if (!ok) atomicExch(err, 1);
+        }
+        __threadfence();
+        ok_s = ok && !*verr;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+__device__ __forceinline__ float2 ld_cg2(const float* p) { return __ldcg(reinterpret_cast<const float2*>(p)); }
+
+// G(in) over the output region [ox0, ox1) x [oy0, oy1) of shared array `in` (origin (ix0, iy0),
+// row stride iw; it covers the region and R more on every side); epi(x, y, g) per output point.
+// Staggered kinds stage the x- and y-fluxes in sFX / sFY first. Operation for operation the
+// arithmetic of the step passes' queues and windows.
+template <int KIND, class Epi>
+__device__ __forceinline__ void stencil_region(const Step2D& a, const float2* in, int ix0, int iy0, int iw, int ox0,
+                                               int ox1, int oy0, int oy1, float2* sFX, float2* sFY, Epi epi) {
+    constexpr bool STAG = KIND != 0, VARB = KIND == 1;
+    const int NTH = blockDim.x, tid = threadIdx.x;
+    const int ow = oy1 - oy0, oh = ox1 - ox0;
+    const int mp = a.mpitch;
+    auto at = [&](int x, int y) { return in[(x - ix0) * iw + (y - iy0)]; };
+    if constexpr (STAG) {
+        // x-fluxes at half-rows ox0 - 5 .. ox1 + 3 (flux h at h + 1/2), columns of the region
+        for (int e = tid; e < (oh + 9) * ow; e += NTH) {
+            const int h = ox0 - 5 + e / ow, y = oy0 + e % ow;
+            float2 acc = mul2(a.wx[0], sub2(at(h + 1, y), at(h, y)));
+#pragma unroll
+            for (int m = 1; m < 5; m++) acc = fma2(a.wx[m], sub2(at(h + 1 + m, y), at(h - m, y)), acc);
+            if constexpr (VARB) acc = mul2(acc, f2(__ldg(a.bxm + (long long)h * mp + y)));
+            sFX[e] = acc;
+        }
+        // y-fluxes at half-columns oy0 - 5 .. oy1 + 3, rows of the region
+        for (int e = tid; e < oh * (ow + 9); e += NTH) {
+            const int x = ox0 + e / (ow + 9), hc = oy0 - 5 + e % (ow + 9);
+            float2 acc = mul2(a.wy[0], sub2(at(x, hc + 1), at(x, hc)));
+#pragma unroll
+            for (int m = 1; m < 5; m++) acc = fma2(a.wy[m], sub2(at(x, hc + 1 + m), at(x, hc - m)), acc);
+            if constexpr (VARB) acc = mul2(acc, f2(__ldg(a.bym + (long long)x * mp + hc)));
+            sFY[e] = acc;
+        }
+        __syncthreads();
+        for (int e = tid; e < oh * ow; e += NTH) {
+            const int xr = e / ow, yr = e % ow;
+            const float2* fx = sFX + (xr + 5) * ow + yr;     // flux at half-row x (x + 1/2)
+            const float2* fy = sFY + xr * (ow + 9) + yr + 5;  // flux at half-column y
+            float2 gx = mul2(a.wx[0], sub2(fx[0], fx[-ow]));
+            float2 gy = mul2(a.wy[0], sub2(fy[0], fy[-1]));
+#pragma unroll
+            for (int m = 1; m < 5; m++) {
+                gx = fma2(a.wx[m], sub2(fx[m * ow], fx[-(1 + m) * ow]), gx);
+                gy = fma2(a.wy[m], sub2(fy[m], fy[-1 - m]), gy);
+            }
+            epi(ox0 + xr, oy0 + yr, add2(gx, gy));
+        }
+        __syncthreads();  // the flux rows are reused
+    } else {
+        for (int e = tid; e < oh * ow; e += NTH) {
+            const int x = ox0 + e / ow, y = oy0 + e % ow;
+            float2 gx = mul2(a.wx[0], at(x, y));
+            float2 gy = mul2(a.wy[0], at(x, y));
+#pragma unroll
+            for (int k = 1; k <= 5; k++) {
+                gx = fma2(a.wx[k], add2(at(x + k, y), at(x - k, y)), gx);
+                gy = fma2(a.wy[k], add2(at(x, y + k), at(x, y - k)), gy);
+            }
+            epi(x, y, add2(gx, gy));
+        }
+    }
+}
+
+template <int KIND, bool OT4>
+struct PersistCfg {
+    static constexpr int R = KIND != 0 ? 9 : 5;
+    static constexpr int HU = OT4 ? 2 * R : R;  // p[t] halo
+    static constexpr int HL = OT4 ? R : 0;      // stage-1 region beyond the tile
+    // shared memory (float2): p[t] region, l region (OT4), flux rows of the larger stage (staggered)
+    __host__ __device__ static constexpr size_t nU(int tx, int ty) { return (size_t)(tx + 2 * HU) * (ty + 2 * HU); }
+    __host__ __device__ static constexpr size_t nL(int tx, int ty) { return OT4 ? (size_t)(tx + 2 * HL) * (ty + 2 * HL) : 0; }
+    __host__ __device__ static constexpr size_t nF(int tx, int ty) {
+        return KIND != 0 ? (size_t)(tx + 2 * HL + 9) * (ty + 2 * HL) : 0;
+    }
+    __host__ __device__ static constexpr size_t nG(int tx, int ty) {
+        return KIND != 0 ? (size_t)(tx + 2 * HL) * (ty + 2 * HL + 9) : 0;
+    }
+    __host__ __device__ static constexpr size_t bytes(int tx, int ty) {
+        return (nU(tx, ty) + nL(tx, ty) + nF(tx, ty) + nG(tx, ty)) * sizeof(float2);
+    }
+};
+
+template <int KIND, bool OT4>
+__global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_constant__ Persist2D P) {
+    using CF = PersistCfg<KIND, OT4>;
+    constexpr int HU = CF::HU, HL = CF::HL;
+    const Step2D& a = P.s;
+    extern __shared__ __align__(16) float2 psm[];
+    float2* const sU = psm;
+    float2* const sL = sU + CF::nU(P.tx, P.ty);
+    float2* const sFX = sL + CF::nL(P.tx, P.ty);
+    float2* const sFY = sFX + CF::nF(P.tx, P.ty);
+
+    const int tid = threadIdx.x, NTH = blockDim.x, b = blockIdx.x;
+    const int ntile = P.tiles_x * P.tiles_y;
+    const int pair = b / ntile, tile = b % ntile;
+    const int x0 = (tile / P.tiles_y) * P.tx, y0 = (tile % P.tiles_y) * P.ty;
+    const int x1 = min(x0 + P.tx, a.nx), y1 = min(y0 + P.ty, a.ny);
+    const int uw = P.ty + 2 * HU, lw = P.ty + 2 * HL;
+    const int mp = a.mpitch, pitch = a.pitch;
+    const long long poff = (long long)pair * a.shot_stride * 2;  // floats per pair
+
+    for (int t = 1; t <= P.nt - 2; t++) {
+        const float* cur = ((t & 1) ? P.f1 : P.f0) + poff;
+        float* nxt = ((t & 1) ? P.f0 : P.f1) + poff;  // p[t-1] in, p[t+1] out
+        // 1. p[t] over the tile and its halo
+        const int ux0 = x0 - HU, uy0 = y0 - HU, uh = (x1 - x0) + 2 * HU, uwr = (y1 - y0) + 2 * HU;
+        for (int e = tid; e < uh * uwr; e += NTH) {
+            const int x = ux0 + e / uwr, y = uy0 + e % uwr;
+            const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
+            sU[(x - ux0) * uw + (y - uy0)] = in ? ld_cg2(cur + 2 * ((long long)x * pitch + y)) : f2(0.f);
+        }
+        __syncthreads();
+        // 2-3. the update of the tile (OT4: after l over the tile and R more)
+        auto update = [&](int x, int y, float2 Lt) {
+            const long long q = (long long)x * mp + y, idx = 2 * ((long long)x * pitch + y);
+            const float2 u = sU[(x - ux0) * uw + (y - uy0)];
+            const float2 pm = ld_cg2(nxt + idx);
+            const float2 res = fma2(f2(__ldg(a.C1m + q)), Lt, fma2(f2(__ldg(a.C2m + q)), u, mul2(f2(__ldg(a.NC3m + q)), pm)));
+            __stcg(reinterpret_cast<float2*>(nxt + idx), res);
+        };
+        if constexpr (OT4) {
+            const int lx0 = x0 - HL, ly0 = y0 - HL;
+            stencil_region<KIND>(a, sU, ux0, uy0, uw, lx0, x1 + HL, ly0, y1 + HL, sFX, sFY,
+                                 [&](int x, int y, float2 g) {
+                                     const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
+                                     const float W = __ldg(a.Wm + (long long)x * mp + y);
+                                     sL[(x - lx0) * lw + (y - ly0)] = in ? mul2(f2(W), g) : f2(0.f);
+                                 });
+            __syncthreads();
+            stencil_region<KIND>(a, sL, lx0, ly0, lw, x0, x1, y0, y1, sFX, sFY, [&](int x, int y, float2 g) {
+                const float Wk = __ldg(a.Wm + (long long)x * mp + y) * a.k12;
+                update(x, y, fma2(f2(Wk), g, sL[(x - lx0) * lw + (y - ly0)]));
+            });
+        } else {
+            stencil_region<KIND>(a, sU, ux0, uy0, uw, x0, x1, y0, y1, sFX, sFY, [&](int x, int y, float2 g) {
+                update(x, y, mul2(f2(__ldg(a.Wm + (long long)x * mp + y)), g));
+            });
+        }
+        __syncthreads();  // the tile's new level is written
+        // 4. this step's sources at the tile's points
+        for (int k = P.cta_off[b] + tid; k < P.cta_off[b + 1]; k += NTH) {
+            const int tg = P.cta_tgt[k];
+            float v = 0.f;
+            const float* amp = P.src_amp + (long long)t * P.n_src;
+            for (int e = P.toff[tg]; e < P.toff[tg + 1]; e++) v += P.tcoef[e] * amp[P.tpoint[e]];
+            float* f = ((t & 1) ? P.f0 : P.f1) + P.tidx[tg];
+            __stcg(f, __ldcg(f) + v);
+        }
+        // 5. every tile of p[t+1] complete, then the receivers of step t
+        if (!grid_barrier(P.bar, P.err, P.expected, P.spin_limit)) return;
+        const float* level = (t & 1) ? P.f0 : P.f1;
+        for (int e = b * NTH + tid; e < P.n_rec; e += gridDim.x * NTH) {
+            const Gather G = P.gat[e];  // pad = shot: pair pad / 2, lane pad % 2
+            const float* f = level + (long long)(G.pad / 2) * a.shot_stride * 2 + (G.pad & 1);
+            const long long i0 = 2 * ((long long)G.row * pitch + G.col), i1 = i0 + 2 * (long long)pitch;
+            P.rec_amp[(long long)t * P.n_rec + G.point] =
+                G.w00 * __ldcg(f + i0) + G.w01 * __ldcg(f + i0 + 2) + G.w10 * __ldcg(f + i1) + G.w11 * __ldcg(f + i1 + 2);
+        }
+    }
+}
+
+template <int KIND, bool OT4>
+cudaError_t launch_one(int nblocks, size_t smem, cudaStream_t s, const Persist2D& a) {
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(fdtd2d_persist<KIND, OT4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             227 * 1024);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    void* args[] = {const_cast<Persist2D*>(&a)};
+    return cudaLaunchCooperativeKernel((const void*)fdtd2d_persist<KIND, OT4>, dim3(nblocks), dim3(PERSIST_THREADS),
+                                       args, smem, s);
+}
+
+template <int KIND, bool OT4>
+int blocks_one(size_t smem) {
+    static bool configured = false;
+    if (!configured) {
+        if (cudaFuncSetAttribute(fdtd2d_persist<KIND, OT4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
+            cudaSuccess)
+            return 0;
+        configured = true;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fdtd2d_persist<KIND, OT4>, PERSIST_THREADS, smem) !=
+        cudaSuccess)
+        return 0;
+    return n;
+}
+
+}  // namespace
+
+size_t persist2d_smem(int kind, bool ot4, int tx, int ty) {
+    switch (kind) {
+        case 0: return ot4 ? PersistCfg<0, true>::bytes(tx, ty) : PersistCfg<0, false>::bytes(tx, ty);
+        case 1: return ot4 ? PersistCfg<1, true>::bytes(tx, ty) : PersistCfg<1, false>::bytes(tx, ty);
+        default: return ot4 ? PersistCfg<2, true>::bytes(tx, ty) : PersistCfg<2, false>::bytes(tx, ty);
+    }
+}
+
+int persist2d_blocks_per_sm(int kind, bool ot4, size_t smem) {
+    switch (kind) {
+        case 0: return ot4 ? blocks_one<0, true>(smem) : blocks_one<0, false>(smem);
+        case 1: return ot4 ? blocks_one<1, true>(smem) : blocks_one<1, false>(smem);
+        default: return ot4 ? blocks_one<2, true>(smem) : blocks_one<2, false>(smem);
+    }
+}
+
+cudaError_t launch_persist2d(int kind, bool ot4, int nblocks, size_t smem, cudaStream_t s, const Persist2D& a) {
+    switch (kind) {
+        case 0: return ot4 ? launch_one<0, true>(nblocks, smem, s, a) : launch_one<0, false>(nblocks, smem, s, a);
+        case 1: return ot4 ? launch_one<1, true>(nblocks, smem, s, a) : launch_one<1, false>(nblocks, smem, s, a);
+        default: return ot4 ? launch_one<2, true>(nblocks, smem, s, a) : launch_one<2, false>(nblocks, smem, s, a);
+    }
+}
+
+}  // namespace sa

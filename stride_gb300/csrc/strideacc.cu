@@ -18,6 +18,7 @@
 #include "common.cuh"
 #include "helpers.h"
 #include "launch.h"
+#include "persist2d.h"
 #include "plan3d.h"
 
 namespace {
@@ -89,6 +90,7 @@ struct Targets {
     float* coef = nullptr;
     size_t cap_idx = 0, cap_off = 0, cap_point = 0, cap_coef = 0;
     int n = 0;
+    std::vector<long long> hidx;  // host copy of idx (the persistent forward's owner of each target)
 };
 
 struct sa_plan {
@@ -197,6 +199,17 @@ struct sa_plan {
     long long fwd_launches[4] = {0, 0, 0, 0};  // kernels in each forward loop (by save mode)
     long long adj_launches[5] = {0, 0, 0, 0, 0};  // kernels in each adjoint loop
     bool use_graphs = true;
+    // persistent forward of small batches (persist2d.cu): mode (-1 never, 0 automatic, 1 whenever
+    // eligible), the tests' barrier knobs, its tile layout and device state
+    int persist_mode = 0;
+    int persist_extra = 0;
+    long long persist_spin = 10000000;
+    int ptx = 0, pty = 0, ptiles_x = 0, ptiles_y = 0, pblocks = 0;
+    size_t psmem = 0;
+    unsigned* pbar = nullptr;  // [0] arrivals, [1] generation, [2] error flag
+    size_t cap_pbar = 0;
+    int *pcta_off = nullptr, *pcta_tgt = nullptr;
+    size_t cap_pcta_off = 0, cap_pcta_tgt = 0;
     // L2 residency of the duplicated medium: every shot pair's CTAs read each of its rows once per
     // pass, just after the previous pass streamed the wavefields through L2; the captured step
     // kernels carry this persisting window
@@ -349,6 +362,7 @@ int build_lists_impl(sa_plan* p) {
         }
         toff.push_back((int)keyed.size());
         T.n = (int)tidx.size();
+        T.hidx = tidx;
         CKR(ensure(&T.idx, &T.cap_idx, tidx.size()));
         CKR(ensure(&T.off, &T.cap_off, toff.size()));
         CKR(ensure(&T.coef, &T.cap_coef, tcoef.size()));
@@ -971,6 +985,108 @@ int store_transposed(sa_plan* p, const float* tm, int rows, int cols, float* use
     return SA_OK;
 }
 
+// The persistent forward: eligible for a plan with linear interpolation, the sponge and no saved
+// wavefield; automatic when the whole batch is small (the streaming passes could not fill the
+// GPU); its tiles are the smallest whose CTAs (one per tile and shot pair) are co-resident.
+bool persist_layout(sa_plan* p) {
+    const int kind = p->kind;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    const int pairs = npairs(p);
+    long long best = -1;
+    for (int ty = 16; ty <= 96; ty += 8)
+        for (int tx = 8; tx <= 96; tx += 4) {
+            const int tiles_x = (p->nx + tx - 1) / tx, tiles_y = (p->ny + ty - 1) / ty;
+            const long long blocks = (long long)tiles_x * tiles_y * pairs;
+            const size_t smem = sa::persist2d_smem(kind, p->ot4, tx, ty);
+            if (smem > 227 * 1024) continue;
+            const int per_sm = sa::persist2d_blocks_per_sm(kind, p->ot4, smem);
+            if (per_sm < 1 || blocks > (long long)per_sm * sms) continue;
+            const int H = (kind == 0 ? 5 : 9) * (p->ot4 ? 2 : 1);
+            const long long cost = (long long)(tx + 2 * H) * (ty + 2 * H);  // points a CTA loads per step
+            if (best < 0 || cost < best) {
+                best = cost;
+                p->ptx = tx;
+                p->pty = ty;
+                p->ptiles_x = tiles_x;
+                p->ptiles_y = tiles_y;
+                p->pblocks = (int)blocks;
+                p->psmem = smem;
+            }
+        }
+    return best >= 0;
+}
+
+bool use_persistent(sa_plan* p, int save_mode) {
+    if (p->persist_mode < 0 || save_mode != SA_SAVE_NONE || p->d.interpolation != SA_INTERP_LINEAR ||
+        p->d.boundary != SA_BOUNDARY_SPONGE)
+        return false;
+    if (p->persist_mode == 0 && (long long)npairs(p) * p->nx * p->ny > 152LL * 4096) return false;
+    return persist_layout(p);
+}
+
+int forward_persistent(sa_plan* p, cudaStream_t s) {
+    const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
+    // the sources' targets by owning CTA (tile and shot pair of the target point), in target order
+    const int ntile = p->ptiles_x * p->ptiles_y;
+    std::vector<int> cnt(p->pblocks + 1, 0), tgt(p->stgt.n);
+    std::vector<int> owner(p->stgt.n);
+    for (int k = 0; k < p->stgt.n; k++) {
+        const long long i = p->stgt.hidx[k];
+        const long long pair = i / (2 * p->shot_stride), rem = (i % (2 * p->shot_stride)) / 2;
+        const int x = (int)(rem / p->pitch), y = (int)(rem % p->pitch);
+        owner[k] = (int)pair * ntile + (x / p->ptx) * p->ptiles_y + y / p->pty;
+        cnt[owner[k] + 1]++;
+    }
+    for (int b = 0; b < p->pblocks; b++) cnt[b + 1] += cnt[b];
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int k = 0; k < p->stgt.n; k++) tgt[fill[owner[k]]++] = k;
+    CKR(ensure(&p->pcta_off, &p->cap_pcta_off, cnt.size()));
+    CKR(ensure(&p->pcta_tgt, &p->cap_pcta_tgt, std::max<size_t>(1, tgt.size())));
+    CKR(ensure(&p->pbar, &p->cap_pbar, 4));
+    CK(cudaMemcpyAsync(p->pcta_off, cnt.data(), cnt.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (!tgt.empty()) CK(cudaMemcpyAsync(p->pcta_tgt, tgt.data(), tgt.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(p->pbar, 0, 4 * sizeof(unsigned), s));
+    CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
+    CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
+    CK(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * p->n_rec * sizeof(float), s));
+    sa::Persist2D a{};
+    a.s = base_args(p);
+    a.f0 = p->field[0];
+    a.f1 = p->field[1];
+    a.nt = p->d.nt;
+    a.tx = p->ptx;
+    a.ty = p->pty;
+    a.tiles_x = p->ptiles_x;
+    a.tiles_y = p->ptiles_y;
+    a.cta_off = p->pcta_off;
+    a.cta_tgt = p->pcta_tgt;
+    a.tidx = p->stgt.idx;
+    a.toff = p->stgt.off;
+    a.tcoef = p->stgt.coef;
+    a.tpoint = p->stgt.point;
+    a.src_amp = p->src_amp;
+    a.n_src = p->n_src;
+    a.gat = p->gat_flat;
+    a.n_rec = p->n_rec;
+    a.rec_amp = p->rec_amp;
+    a.bar = p->pbar;
+    a.err = reinterpret_cast<int*>(p->pbar + 2);
+    a.expected = p->pblocks + p->persist_extra;
+    a.spin_limit = p->persist_spin;
+    CK(sa::launch_persist2d(p->kind, p->ot4, p->pblocks, p->psmem, s, a));
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, p->pbar + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (err) return fail(SA_E_TIMEOUT, "persistent forward: a grid barrier wait gave up (%d CTAs expected, %d launched)",
+                         a.expected, p->pblocks);
+    p->launches = 1;
+    return SA_OK;
+}
+
 int ensure_fields(sa_plan* p) {
     const size_t n = (size_t)((std::max(1, p->d.max_shots) + 1) / 2) * p->shot_stride * 2;
     CKR(ensure(&p->field[0], &p->field_cap[0], n));
@@ -995,6 +1111,25 @@ int sa_last_error(char* buf, int len) {
 long long sa_launch_count(const sa_plan* p) {
     if (!p) return -1;
     return p->p3 ? sa::plan3d_launches(p->p3) : p->launches;
+}
+
+int sa_plan_option(sa_plan* p, int option, long long value) {
+    if (!p) return fail(SA_E_INVALID, "null plan");
+    switch (option) {
+        case SA_OPT_PERSISTENT:
+            if (value < -1 || value > 1) return fail(SA_E_INVALID, "SA_OPT_PERSISTENT takes -1, 0 or 1");
+            p->persist_mode = (int)value;
+            return SA_OK;
+        case SA_OPT_BARRIER_EXTRA:
+            if (value < 0 || value > 1024) return fail(SA_E_INVALID, "SA_OPT_BARRIER_EXTRA takes 0..1024");
+            p->persist_extra = (int)value;
+            return SA_OK;
+        case SA_OPT_BARRIER_SPIN:
+            if (value < 1) return fail(SA_E_INVALID, "SA_OPT_BARRIER_SPIN takes a positive poll count");
+            p->persist_spin = value;
+            return SA_OK;
+        default: return fail(SA_E_INVALID, "unknown option %d", option);
+    }
 }
 
 int sa_plan_layout(const sa_plan* p, int* threads, int* strips, int* chunks) {
@@ -1153,7 +1288,7 @@ int sa_plan_destroy(sa_plan* p) {
                     p->gat_flat,
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
-                    p->smed, p->lbuf, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
+                    p->smed, p->lbuf, p->pbar, p->pcta_off, p->pcta_tgt, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
                     p->dbx, p->dby, p->pml_prof, p->pml_aux, p->pml_ck, p->pml_aux_f, p->ckpt2, p->pml_ck2,
                     p->wgrad, p->hgat, p->hgat_src, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
                     p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx, p->xtgt.off, p->xtgt.point, p->xtgt.coef};
@@ -1314,6 +1449,13 @@ int sa_forward(sa_plan* p, const float* wavelets, float* traces, int save_mode, 
         p->snaps_valid = false;
     }
     CKR(load_transposed(p, wavelets, p->n_src, p->d.nt, p->src_amp, s));
+    if (use_persistent(p, save_mode)) {  // one cooperative launch runs every step
+        CKR(forward_persistent(p, s));
+        CKR(store_transposed(p, p->rec_amp, p->d.nt, p->n_rec, traces, s));
+        p->launches = (p->n_src ? 1 : 0) + 1 + (p->n_rec ? 1 : 0);
+        p->adjoint_pending = false;
+        return SA_OK;
+    }
     CKR(run_loop(p, &p->g_fwd[save_mode], s, [&](cudaStream_t cs) { return issue_forward(p, save_mode, cs); }));
     CKR(store_transposed(p, p->rec_amp, p->d.nt, p->n_rec, traces, s));
     p->launches = (p->n_src ? 1 : 0) + p->fwd_launches[save_mode] + (p->n_rec ? 1 : 0);
