@@ -62,17 +62,25 @@ __device__ bool grid_barrier(unsigned* bar, int* err, int expected, long long sp
 
 __device__ __forceinline__ float2 ld_cg2(const float* p) { return __ldcg(reinterpret_cast<const float2*>(p)); }
 
+// Buoyancy tables of a CTA in shared memory: bx at half-rows [fx0, fx0 + fh) x columns
+// [fy0, fy0 + fw), by at rows [gx0, gx0 + gh) x half-columns [gy0, gy0 + gw).
+struct BTables {
+    const float* bx;
+    const float* by;
+    int fx0, fy0, fw, gx0, gy0, gw;
+};
+
 // G(in) over the output region [ox0, ox1) x [oy0, oy1) of shared array `in` (origin (ix0, iy0),
 // row stride iw; it covers the region and R more on every side); epi(x, y, g) per output point.
 // Staggered kinds stage the x- and y-fluxes in sFX / sFY first. Operation for operation the
 // arithmetic of the step passes' queues and windows.
 template <int KIND, class Epi>
 __device__ __forceinline__ void stencil_region(const Step2D& a, const float2* in, int ix0, int iy0, int iw, int ox0,
-                                               int ox1, int oy0, int oy1, float2* sFX, float2* sFY, Epi epi) {
+                                               int ox1, int oy0, int oy1, float2* sFX, float2* sFY, const BTables& B,
+                                               Epi epi) {
     constexpr bool STAG = KIND != 0, VARB = KIND == 1;
     const int NTH = blockDim.x, tid = threadIdx.x;
     const int ow = oy1 - oy0, oh = ox1 - ox0;
-    const int mp = a.mpitch;
     auto at = [&](int x, int y) { return in[(x - ix0) * iw + (y - iy0)]; };
     if constexpr (STAG) {
         // x-fluxes at half-rows ox0 - 5 .. ox1 + 3 (flux h at h + 1/2), columns of the region
@@ -81,7 +89,7 @@ __device__ __forceinline__ void stencil_region(const Step2D& a, const float2* in
             float2 acc = mul2(a.wx[0], sub2(at(h + 1, y), at(h, y)));
 #pragma unroll
             for (int m = 1; m < 5; m++) acc = fma2(a.wx[m], sub2(at(h + 1 + m, y), at(h - m, y)), acc);
-            if constexpr (VARB) acc = mul2(acc, f2(__ldg(a.bxm + (long long)h * mp + y)));
+            if constexpr (VARB) acc = mul2(acc, f2(B.bx[(h - B.fx0) * B.fw + (y - B.fy0)]));
             sFX[e] = acc;
         }
         // y-fluxes at half-columns oy0 - 5 .. oy1 + 3, rows of the region
@@ -90,7 +98,7 @@ __device__ __forceinline__ void stencil_region(const Step2D& a, const float2* in
             float2 acc = mul2(a.wy[0], sub2(at(x, hc + 1), at(x, hc)));
 #pragma unroll
             for (int m = 1; m < 5; m++) acc = fma2(a.wy[m], sub2(at(x, hc + 1 + m), at(x, hc - m)), acc);
-            if constexpr (VARB) acc = mul2(acc, f2(__ldg(a.bym + (long long)x * mp + hc)));
+            if constexpr (VARB) acc = mul2(acc, f2(B.by[(x - B.gx0) * B.gw + (hc - B.gy0)]));
             sFY[e] = acc;
         }
         __syncthreads();
@@ -128,7 +136,9 @@ struct PersistCfg {
     static constexpr int R = KIND != 0 ? 9 : 5;
     static constexpr int HU = OT4 ? 2 * R : R;  // p[t] halo
     static constexpr int HL = OT4 ? R : 0;      // stage-1 region beyond the tile
-    // shared memory (float2): p[t] region, l region (OT4), flux rows of the larger stage (staggered)
+    // shared memory: float2 arrays of p[t] over the tile and halo, l (OT4), the flux rows of the
+    // larger stage (staggered), p[t-1] and p[t+1] over the tile; float tables of the medium: W
+    // over the stage-1 region, C1, C2, -C3 over the tile, bx and by over the stage-1 flux regions
     __host__ __device__ static constexpr size_t nU(int tx, int ty) { return (size_t)(tx + 2 * HU) * (ty + 2 * HU); }
     __host__ __device__ static constexpr size_t nL(int tx, int ty) { return OT4 ? (size_t)(tx + 2 * HL) * (ty + 2 * HL) : 0; }
     __host__ __device__ static constexpr size_t nF(int tx, int ty) {
@@ -137,100 +147,195 @@ struct PersistCfg {
     __host__ __device__ static constexpr size_t nG(int tx, int ty) {
         return KIND != 0 ? (size_t)(tx + 2 * HL) * (ty + 2 * HL + 9) : 0;
     }
+    __host__ __device__ static constexpr size_t nT(int tx, int ty) { return (size_t)tx * ty; }
+    __host__ __device__ static constexpr size_t nW(int tx, int ty) { return (size_t)(tx + 2 * HL) * (ty + 2 * HL); }
+    __host__ __device__ static constexpr size_t floats2(int tx, int ty) {
+        return nU(tx, ty) + nL(tx, ty) + nF(tx, ty) + nG(tx, ty) + 2 * nT(tx, ty);
+    }
+    __host__ __device__ static constexpr size_t floats1(int tx, int ty) {
+        return nW(tx, ty) + 3 * nT(tx, ty) + (KIND == 1 ? nF(tx, ty) + nG(tx, ty) : 0);
+    }
     __host__ __device__ static constexpr size_t bytes(int tx, int ty) {
-        return (nU(tx, ty) + nL(tx, ty) + nF(tx, ty) + nG(tx, ty)) * sizeof(float2);
+        return floats2(tx, ty) * sizeof(float2) + floats1(tx, ty) * sizeof(float);
     }
 };
 
 template <int KIND, bool OT4>
 __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_constant__ Persist2D P) {
     using CF = PersistCfg<KIND, OT4>;
+    constexpr bool VARB = KIND == 1;
     constexpr int HU = CF::HU, HL = CF::HL;
     const Step2D& a = P.s;
+    const int tx = P.tx, ty = P.ty;
     extern __shared__ __align__(16) float2 psm[];
-    float2* const sU = psm;
-    float2* const sL = sU + CF::nU(P.tx, P.ty);
-    float2* const sFX = sL + CF::nL(P.tx, P.ty);
-    float2* const sFY = sFX + CF::nF(P.tx, P.ty);
+    float2* const sU = psm;                  // p[t], tile and halo
+    float2* const sL = sU + CF::nU(tx, ty);  // l (OT4)
+    float2* const sFX = sL + CF::nL(tx, ty);
+    float2* const sFY = sFX + CF::nF(tx, ty);
+    float2* const sPm = sFY + CF::nG(tx, ty);  // p[t-1] over the tile
+    float2* const sN = sPm + CF::nT(tx, ty);   // p[t+1] over the tile
+    float* const sW = reinterpret_cast<float*>(sN + CF::nT(tx, ty));
+    float* const sC1 = sW + CF::nW(tx, ty);
+    float* const sC2 = sC1 + CF::nT(tx, ty);
+    float* const sC3 = sC2 + CF::nT(tx, ty);
+    float* const sBX = sC3 + CF::nT(tx, ty);
+    float* const sBY = sBX + (VARB ? CF::nF(tx, ty) : 0);
 
     const int tid = threadIdx.x, NTH = blockDim.x, b = blockIdx.x;
     const int ntile = P.tiles_x * P.tiles_y;
     const int pair = b / ntile, tile = b % ntile;
-    const int x0 = (tile / P.tiles_y) * P.tx, y0 = (tile % P.tiles_y) * P.ty;
-    const int x1 = min(x0 + P.tx, a.nx), y1 = min(y0 + P.ty, a.ny);
-    const int uw = P.ty + 2 * HU, lw = P.ty + 2 * HL;
+    const int x0 = (tile / P.tiles_y) * tx, y0 = (tile % P.tiles_y) * ty;
+    const int x1 = min(x0 + tx, a.nx), y1 = min(y0 + ty, a.ny);
+    const int th = x1 - x0, tw = y1 - y0;
+    const int uw = ty + 2 * HU, lw = ty + 2 * HL;
     const int mp = a.mpitch, pitch = a.pitch;
     const long long poff = (long long)pair * a.shot_stride * 2;  // floats per pair
+    const int ux0 = x0 - HU, uy0 = y0 - HU, uh = th + 2 * HU, uwr = tw + 2 * HU;
+    const int lx0 = x0 - HL, ly0 = y0 - HL, lh = th + 2 * HL, lwr = tw + 2 * HL;
+
+    // ---- once: the medium of the CTA's region, p[1] = p[0] = 0 over the tile ------------------
+    for (int e = tid; e < lh * lwr; e += NTH) {
+        const int x = lx0 + e / lwr, y = ly0 + e % lwr;
+        sW[(x - lx0) * lw + (y - ly0)] = __ldg(a.Wm + (long long)x * mp + y);
+    }
+    for (int e = tid; e < th * tw; e += NTH) {
+        const int x = x0 + e / tw, y = y0 + e % tw;
+        const long long q = (long long)x * mp + y;
+        const int k = (x - x0) * ty + (y - y0);
+        sC1[k] = __ldg(a.C1m + q);
+        sC2[k] = __ldg(a.C2m + q);
+        sC3[k] = __ldg(a.NC3m + q);
+        sPm[k] = f2(0.f);
+    }
+    BTables B{sBX, sBY, lx0 - 5, ly0, lw, lx0, ly0 - 5, lw + 9};
+    if constexpr (VARB) {
+        for (int e = tid; e < (lh + 9) * lwr; e += NTH) {
+            const int h = lx0 - 5 + e / lwr, y = ly0 + e % lwr;
+            sBX[(h - B.fx0) * B.fw + (y - B.fy0)] = __ldg(a.bxm + (long long)h * mp + y);
+        }
+        for (int e = tid; e < lh * (lwr + 9); e += NTH) {
+            const int x = lx0 + e / (lwr + 9), hc = ly0 - 5 + e % (lwr + 9);
+            sBY[(x - B.gx0) * B.gw + (hc - B.gy0)] = __ldg(a.bym + (long long)x * mp + hc);
+        }
+    }
+    for (int e = tid; e < uh * uwr; e += NTH) sU[(e / uwr) * uw + e % uwr] = f2(0.f);
+    __syncthreads();
+
+    // receivers whose corners this CTA holds: base corner (row, col) in the tile
+    auto gather_from_smem = [&](int trow) {
+        for (int e = tid; e < P.n_rec; e += NTH) {
+            const Gather G = P.gat[e];
+            if (G.pad / 2 != pair || G.row < x0 || G.row >= x1 || G.col < y0 || G.col >= y1) continue;
+            const float2* f0 = sU + (G.row - ux0) * uw + (G.col - uy0);
+            const float2* f1 = f0 + uw;
+            const float v00 = (G.pad & 1) ? f0[0].y : f0[0].x, v01 = (G.pad & 1) ? f0[1].y : f0[1].x;
+            const float v10 = (G.pad & 1) ? f1[0].y : f1[0].x, v11 = (G.pad & 1) ? f1[1].y : f1[1].x;
+            P.rec_amp[(long long)trow * P.n_rec + G.point] = G.w00 * v00 + G.w01 * v01 + G.w10 * v10 + G.w11 * v11;
+        }
+    };
 
     for (int t = 1; t <= P.nt - 2; t++) {
         const float* cur = ((t & 1) ? P.f1 : P.f0) + poff;
-        float* nxt = ((t & 1) ? P.f0 : P.f1) + poff;  // p[t-1] in, p[t+1] out
-        // 1. p[t] over the tile and its halo
-        const int ux0 = x0 - HU, uy0 = y0 - HU, uh = (x1 - x0) + 2 * HU, uwr = (y1 - y0) + 2 * HU;
-        for (int e = tid; e < uh * uwr; e += NTH) {
-            const int x = ux0 + e / uwr, y = uy0 + e % uwr;
-            const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
-            sU[(x - ux0) * uw + (y - uy0)] = in ? ld_cg2(cur + 2 * ((long long)x * pitch + y)) : f2(0.f);
+        float* nxt = ((t & 1) ? P.f0 : P.f1) + poff;  // p[t+1] out (in place of p[t-1])
+        // 1. p[t]: the halo from global memory (the tile's own points are in sU since last step)
+        if (t > 1) {
+            for (int e = tid; e < uh * uwr; e += NTH) {
+                const int xr = e / uwr, yr = e % uwr, x = ux0 + xr, y = uy0 + yr;
+                if (x >= x0 && x < x1 && y >= y0 && y < y1) continue;
+                const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
+                sU[xr * uw + yr] = in ? ld_cg2(cur + 2 * ((long long)x * pitch + y)) : f2(0.f);
+            }
+            __syncthreads();
+            gather_from_smem(t - 1);  // rec[t-1] = interp(p[t])
         }
-        __syncthreads();
-        // 2-3. the update of the tile (OT4: after l over the tile and R more)
+        // 2-3. the update of the tile into sN (OT4: after l over the tile and R more)
         auto update = [&](int x, int y, float2 Lt) {
-            const long long q = (long long)x * mp + y, idx = 2 * ((long long)x * pitch + y);
+            const int k = (x - x0) * ty + (y - y0);
             const float2 u = sU[(x - ux0) * uw + (y - uy0)];
-            const float2 pm = ld_cg2(nxt + idx);
-            const float2 res = fma2(f2(__ldg(a.C1m + q)), Lt, fma2(f2(__ldg(a.C2m + q)), u, mul2(f2(__ldg(a.NC3m + q)), pm)));
-            __stcg(reinterpret_cast<float2*>(nxt + idx), res);
+            sN[k] = fma2(f2(sC1[k]), Lt, fma2(f2(sC2[k]), u, mul2(f2(sC3[k]), sPm[k])));
         };
         if constexpr (OT4) {
-            const int lx0 = x0 - HL, ly0 = y0 - HL;
-            stencil_region<KIND>(a, sU, ux0, uy0, uw, lx0, x1 + HL, ly0, y1 + HL, sFX, sFY,
+            stencil_region<KIND>(a, sU, ux0, uy0, uw, lx0, x1 + HL, ly0, y1 + HL, sFX, sFY, B,
                                  [&](int x, int y, float2 g) {
                                      const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
-                                     const float W = __ldg(a.Wm + (long long)x * mp + y);
+                                     const float W = sW[(x - lx0) * lw + (y - ly0)];
                                      sL[(x - lx0) * lw + (y - ly0)] = in ? mul2(f2(W), g) : f2(0.f);
                                  });
             __syncthreads();
-            stencil_region<KIND>(a, sL, lx0, ly0, lw, x0, x1, y0, y1, sFX, sFY, [&](int x, int y, float2 g) {
-                const float Wk = __ldg(a.Wm + (long long)x * mp + y) * a.k12;
+            stencil_region<KIND>(a, sL, lx0, ly0, lw, x0, x1, y0, y1, sFX, sFY, B, [&](int x, int y, float2 g) {
+                const float Wk = sW[(x - lx0) * lw + (y - ly0)] * a.k12;
                 update(x, y, fma2(f2(Wk), g, sL[(x - lx0) * lw + (y - ly0)]));
             });
         } else {
-            stencil_region<KIND>(a, sU, ux0, uy0, uw, x0, x1, y0, y1, sFX, sFY, [&](int x, int y, float2 g) {
-                update(x, y, mul2(f2(__ldg(a.Wm + (long long)x * mp + y)), g));
+            stencil_region<KIND>(a, sU, ux0, uy0, uw, x0, x1, y0, y1, sFX, sFY, B, [&](int x, int y, float2 g) {
+                update(x, y, mul2(f2(sW[(x - lx0) * lw + (y - ly0)]), g));
             });
         }
-        __syncthreads();  // the tile's new level is written
+        __syncthreads();
         // 4. this step's sources at the tile's points
         for (int k = P.cta_off[b] + tid; k < P.cta_off[b + 1]; k += NTH) {
             const int tg = P.cta_tgt[k];
             float v = 0.f;
             const float* amp = P.src_amp + (long long)t * P.n_src;
             for (int e = P.toff[tg]; e < P.toff[tg + 1]; e++) v += P.tcoef[e] * amp[P.tpoint[e]];
-            float* f = ((t & 1) ? P.f0 : P.f1) + P.tidx[tg];
-            __stcg(f, __ldcg(f) + v);
+            const long long i = P.tidx[tg] - poff, c2 = i / 2;  // float index within the pair
+            const int x = (int)(c2 / pitch), y = (int)(c2 % pitch);
+            float* s = reinterpret_cast<float*>(sN + (x - x0) * ty + (y - y0)) + (i & 1);
+            *s = *s + v;
         }
-        // 5. every tile of p[t+1] complete, then the receivers of step t
+        __syncthreads();
+        // 5. p[t+1] to global memory and into the tile of sU; p[t] becomes p[t-1]
+        for (int e = tid; e < th * tw; e += NTH) {
+            const int xr = e / tw, yr = e % tw, k = xr * ty + yr;
+            const float2 v = sN[k];
+            float2* u = sU + (xr + HU) * uw + (yr + HU);
+            sPm[k] = *u;
+            *u = v;
+            __stcg(reinterpret_cast<float2*>(nxt + 2 * ((long long)(x0 + xr) * pitch + (y0 + yr))), v);
+        }
         if (!grid_barrier(P.bar, P.err, P.expected, P.spin_limit)) return;
-        const float* level = (t & 1) ? P.f0 : P.f1;
-        for (int e = b * NTH + tid; e < P.n_rec; e += gridDim.x * NTH) {
-            const Gather G = P.gat[e];  // pad = shot: pair pad / 2, lane pad % 2
-            const float* f = level + (long long)(G.pad / 2) * a.shot_stride * 2 + (G.pad & 1);
-            const long long i0 = 2 * ((long long)G.row * pitch + G.col), i1 = i0 + 2 * (long long)pitch;
-            P.rec_amp[(long long)t * P.n_rec + G.point] =
-                G.w00 * __ldcg(f + i0) + G.w01 * __ldcg(f + i0 + 2) + G.w10 * __ldcg(f + i1) + G.w11 * __ldcg(f + i1 + 2);
-        }
     }
+    // the last step's receivers, rec[nt-2] = interp(p[nt-1]), with the halo of p[nt-1]
+    if (P.nt < 3) return;
+    const float* last = (((P.nt - 2) & 1) ? P.f0 : P.f1) + poff;
+    for (int e = tid; e < uh * uwr; e += NTH) {
+        const int xr = e / uwr, yr = e % uwr, x = ux0 + xr, y = uy0 + yr;
+        if (x >= x0 && x < x1 && y >= y0 && y < y1) continue;
+        const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
+        sU[xr * uw + yr] = in ? ld_cg2(last + 2 * ((long long)x * pitch + y)) : f2(0.f);
+    }
+    __syncthreads();
+    gather_from_smem(P.nt - 2);
+}
+
+// Largest dynamic shared memory of a CTA of the kernel: the device's opt-in limit less the
+// kernel's static shared memory (the barrier flag). Configures the kernel for it once.
+template <int KIND, bool OT4>
+int dyn_limit() {
+    static int limit = -1;
+    if (limit < 0) {
+        int dev = 0, optin = 0;
+        cudaFuncAttributes fa{};
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+            cudaFuncGetAttributes(&fa, fdtd2d_persist<KIND, OT4>) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        const int l = optin - (int)fa.sharedSizeBytes;
+        if (cudaFuncSetAttribute(fdtd2d_persist<KIND, OT4>, cudaFuncAttributeMaxDynamicSharedMemorySize, l) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        limit = l;
+    }
+    return limit;
 }
 
 template <int KIND, bool OT4>
 cudaError_t launch_one(int nblocks, size_t smem, cudaStream_t s, const Persist2D& a) {
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(fdtd2d_persist<KIND, OT4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             227 * 1024);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    if ((int)smem > dyn_limit<KIND, OT4>()) return cudaErrorInvalidValue;
     void* args[] = {const_cast<Persist2D*>(&a)};
     return cudaLaunchCooperativeKernel((const void*)fdtd2d_persist<KIND, OT4>, dim3(nblocks), dim3(PERSIST_THREADS),
                                        args, smem, s);
@@ -238,17 +343,13 @@ cudaError_t launch_one(int nblocks, size_t smem, cudaStream_t s, const Persist2D
 
 template <int KIND, bool OT4>
 int blocks_one(size_t smem) {
-    static bool configured = false;
-    if (!configured) {
-        if (cudaFuncSetAttribute(fdtd2d_persist<KIND, OT4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
-            cudaSuccess)
-            return 0;
-        configured = true;
-    }
+    if ((int)smem > dyn_limit<KIND, OT4>()) return 0;
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fdtd2d_persist<KIND, OT4>, PERSIST_THREADS, smem) !=
-        cudaSuccess)
+        cudaSuccess) {
+        cudaGetLastError();
         return 0;
+    }
     return n;
 }
 

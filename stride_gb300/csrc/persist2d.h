@@ -5,7 +5,10 @@
 
 namespace sa {
 
-constexpr int PERSIST_THREADS = 256;
+#ifndef SA_PERSIST_THREADS
+#define SA_PERSIST_THREADS 512
+#endif
+constexpr int PERSIST_THREADS = SA_PERSIST_THREADS;
 
 // Arguments of the persistent forward. Step t reads p[t] from f1 (t odd) or f0 and writes p[t+1]
 // in place of p[t-1], as the step passes do.

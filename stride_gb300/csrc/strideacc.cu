@@ -1002,11 +1002,11 @@ bool persist_layout(sa_plan* p) {
             const int tiles_x = (p->nx + tx - 1) / tx, tiles_y = (p->ny + ty - 1) / ty;
             const long long blocks = (long long)tiles_x * tiles_y * pairs;
             const size_t smem = sa::persist2d_smem(kind, p->ot4, tx, ty);
-            if (smem > 227 * 1024) continue;
             const int per_sm = sa::persist2d_blocks_per_sm(kind, p->ot4, smem);
             if (per_sm < 1 || blocks > (long long)per_sm * sms) continue;
             const int H = (kind == 0 ? 5 : 9) * (p->ot4 ? 2 : 1);
-            const long long cost = (long long)(tx + 2 * H) * (ty + 2 * H);  // points a CTA loads per step
+            // points an SM loads per step: its CTAs share it
+            const long long cost = (blocks + sms - 1) / sms * (long long)(tx + 2 * H) * (ty + 2 * H);
             if (best < 0 || cost < best) {
                 best = cost;
                 p->ptx = tx;
