@@ -60,11 +60,11 @@ extern "C" {
                                    (linear interpolation, sponge): -1 never, 0 when the batch is small
                                    (default), 1 whenever eligible; the traces equal the step passes' bit for
                                    bit, and the call synchronises its stream to check the barrier status */
-#define SA_OPT_BARRIER_EXTRA 2  /* for tests of the timeout path: the persistent launch's grid barrier waits
-                                   for this many CTAs more than it launches, so its first wait gives up and
-                                   sa_forward returns SA_E_TIMEOUT (default 0) */
-#define SA_OPT_BARRIER_SPIN 3   /* polls (about 0.1 us each) before a persistent barrier wait gives up and sets
-                                   the kernel's error flag (default 10^7, about a second) */
+#define SA_OPT_BARRIER_EXTRA 2  /* for tests of the timeout path: each wait of the persistent launch for its
+                                   neighbour tiles asks for this many steps more than it needs, so that no
+                                   wait can complete and sa_forward returns SA_E_TIMEOUT (default 0) */
+#define SA_OPT_BARRIER_SPIN 3   /* polls (each a global-memory load and a 32 ns sleep) before a persistent
+                                   wait gives up and sets the kernel's error flag (default 10^7) */
 
 /* Plan description (stride/physics/iso_acoustic/devito.py:119-183 defaults; shapes are the
  * extended grid of stride/problem/domain.py:48-74). */

@@ -1,22 +1,26 @@
 // Persistent 2D forward for batches too small to fill the GPU with the streaming step passes.
 //
 // One cooperative launch runs every time step of the forward (the loop OperatorDevito.run drives,
-// stride/physics/common/devito.py:1025-1070): each CTA owns a tile of one shot pair, keeps the tile
-// and its halo in shared memory for the step, and CTAs meet at one grid-wide barrier per step.
-// A step of a CTA:
-//   1. p[t] over the tile and a halo of 2R (OT4) or R (OT2) points into shared memory (zero beyond
-//      the grid, Devito's halo of p);
+// stride/physics/common/devito.py:1025-1070). Each CTA owns a tile of one shot pair and keeps in
+// shared memory, for the whole run, the medium of its region, p[t-1] and p[t] of its tile and the
+// halo of p[t]. CTAs synchronise by step flags: a CTA publishes its flag after storing its tile of
+// p[t+1], and before step t+1 waits only for the tiles its halo overlaps. A step of a CTA:
+//   1. (t > 1) wait for the flags of step t-1, then the halo of p[t] from global memory, a ring of
+//      2R (OT4) or R (OT2) points (zero beyond the grid, Devito's halo of p); the receivers of the
+//      step before, rec[t-1] = interp(p[t]) (iso_acoustic/devito.py:364), by the CTA that holds
+//      each receiver's base corner;
 //   2. OT4: l = W G(p[t]) over the tile and R more (zero beyond the grid, as Devito's `laplacian`),
-//      recomputed by each CTA for its halo so that no second barrier is needed;
-//   3. the update of the tile, p[t+1] = C1 Lt + C2 p[t] - C3 p[t-1], in place of p[t-1];
+//      recomputed by each CTA for its halo so that no second exchange is needed;
+//   3. the update of the tile, p[t+1] = C1 Lt + C2 p[t] - C3 p[t-1];
 //   4. the sources of step t at the tile's points (iso_acoustic/devito.py:357-363), each target
 //      point's entries summed in a fixed order;
-//   5. the barrier, then the receivers of step t, rec[t] = interp(p[t+1]) (:364), spread over CTAs.
+//   5. p[t+1] of the tile to global memory and the flag of step t.
 // Every point's arithmetic is the step passes' (fdtd2d.cuh) operation for operation, so the traces
 // equal the streaming forward's bit for bit.
 //
-// The barrier waits are bounded: a wait that gives up sets an error flag, and every CTA leaves the
-// time loop at its next barrier; the host reports SA_E_TIMEOUT.
+// The flag waits are bounded: a wait that gives up sets an error flag, every CTA leaves the time
+// loop at its next wait, and the host reports SA_E_TIMEOUT. The cooperative launch guarantees that
+// every CTA is resident, so that no wait depends on a CTA that cannot start.
 #include <cooperative_groups.h>
 
 #include "fdtd2d.cuh"
@@ -26,38 +30,40 @@ namespace sa {
 
 namespace {
 
-// Grid-wide barrier of a cooperative launch with a bounded wait. Returns false when this CTA's
-// wait gave up or another CTA's did (the error flag); the caller then leaves its time loop.
-__device__ bool grid_barrier(unsigned* bar, int* err, int expected, long long spin_limit) {
+// Waits until the tiles of rows [r0, r1) x columns [c0, c1) (flags base + row tiles_y + column)
+// have published step `need`, each flag polled by one thread with a bounded wait. Returns false
+// when a wait gave up here or elsewhere (the error flag); the caller then leaves its time loop.
+__device__ bool wait_tiles(const int* flag, int* err, int base, int tiles_y, int r0, int r1, int c0, int c1, int need,
+                           long long spin_limit) {
     __shared__ int ok_s;
+    if (threadIdx.x == 0) ok_s = 1;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned* gen = bar + 1;
-        volatile int* verr = err;
-        const unsigned g = *gen;
-        __threadfence();  // this CTA's writes of the step before its arrival
-        const unsigned arrived = atomicAdd(bar, 1u) + 1u;
-        int ok = 1;
-        if (arrived == (unsigned)expected) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);  // release the others
-        } else {
-            long long k = 0;
-            while (*gen == g) {
-                if (*verr || ++k > spin_limit) {
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(100);
+    const int nc = c1 - c0, n = (r1 - r0) * nc;
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const volatile int* f = flag + base + (r0 + e / nc) * tiles_y + c0 + e % nc;
+        const volatile int* verr = err;
+        long long k = 0;
+        while (*f < need) {
+            if (*verr || ++k > spin_limit) {
+                atomicExch(err, 1);
+                ok_s = 0;
+                break;
             }
-            if (!ok) atomicExch(err, 1);
+            __nanosleep(32);
         }
-        __threadfence();
-        ok_s = ok && !*verr;
     }
+    __threadfence();
     __syncthreads();
     return ok_s != 0;
+}
+
+// Publishes step t of CTA b: its stores of the step before the flag.
+__device__ __forceinline__ void publish(int* flag, int b, int t) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicExch(flag + b, t);
+    }
 }
 
 __device__ __forceinline__ float2 ld_cg2(const float* p) { return __ldcg(reinterpret_cast<const float2*>(p)); }
@@ -221,6 +227,23 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
     for (int e = tid; e < uh * uwr; e += NTH) sU[(e / uwr) * uw + e % uwr] = f2(0.f);
     __syncthreads();
 
+    // the tiles whose points the halo covers, this CTA's own included
+    const int nr0 = max(0, x0 - HU) / tx, nr1 = (min(a.nx, x1 + HU) - 1) / tx + 1;
+    const int nc0 = max(0, y0 - HU) / ty, nc1 = (min(a.ny, y1 + HU) - 1) / ty + 1;
+    // p[level] beyond the tile, once those tiles have published it (step level - 1)
+    auto load_halo = [&](const float* f, int level) -> bool {
+        if (!wait_tiles(P.flag, P.err, pair * ntile, P.tiles_y, nr0, nr1, nc0, nc1, level - 1 + P.extra, P.spin_limit))
+            return false;
+        for (int e = tid; e < uh * uwr; e += NTH) {
+            const int xr = e / uwr, yr = e % uwr, x = ux0 + xr, y = uy0 + yr;
+            if (x >= x0 && x < x1 && y >= y0 && y < y1) continue;
+            const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
+            sU[xr * uw + yr] = in ? ld_cg2(f + 2 * ((long long)x * pitch + y)) : f2(0.f);
+        }
+        __syncthreads();
+        return true;
+    };
+
     // receivers whose corners this CTA holds: base corner (row, col) in the tile
     auto gather_from_smem = [&](int trow) {
         for (int e = tid; e < P.n_rec; e += NTH) {
@@ -239,13 +262,7 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
         float* nxt = ((t & 1) ? P.f0 : P.f1) + poff;  // p[t+1] out (in place of p[t-1])
         // 1. p[t]: the halo from global memory (the tile's own points are in sU since last step)
         if (t > 1) {
-            for (int e = tid; e < uh * uwr; e += NTH) {
-                const int xr = e / uwr, yr = e % uwr, x = ux0 + xr, y = uy0 + yr;
-                if (x >= x0 && x < x1 && y >= y0 && y < y1) continue;
-                const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
-                sU[xr * uw + yr] = in ? ld_cg2(cur + 2 * ((long long)x * pitch + y)) : f2(0.f);
-            }
-            __syncthreads();
+            if (!load_halo(cur, t)) return;
             gather_from_smem(t - 1);  // rec[t-1] = interp(p[t])
         }
         // 2-3. the update of the tile into sN (OT4: after l over the tile and R more)
@@ -293,23 +310,16 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
             *u = v;
             __stcg(reinterpret_cast<float2*>(nxt + 2 * ((long long)(x0 + xr) * pitch + (y0 + yr))), v);
         }
-        if (!grid_barrier(P.bar, P.err, P.expected, P.spin_limit)) return;
+        publish(P.flag, b, t);
     }
     // the last step's receivers, rec[nt-2] = interp(p[nt-1]), with the halo of p[nt-1]
     if (P.nt < 3) return;
-    const float* last = (((P.nt - 2) & 1) ? P.f0 : P.f1) + poff;
-    for (int e = tid; e < uh * uwr; e += NTH) {
-        const int xr = e / uwr, yr = e % uwr, x = ux0 + xr, y = uy0 + yr;
-        if (x >= x0 && x < x1 && y >= y0 && y < y1) continue;
-        const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
-        sU[xr * uw + yr] = in ? ld_cg2(last + 2 * ((long long)x * pitch + y)) : f2(0.f);
-    }
-    __syncthreads();
+    if (!load_halo((((P.nt - 2) & 1) ? P.f0 : P.f1) + poff, P.nt - 1)) return;
     gather_from_smem(P.nt - 2);
 }
 
 // Largest dynamic shared memory of a CTA of the kernel: the device's opt-in limit less the
-// kernel's static shared memory (the barrier flag). Configures the kernel for it once.
+// kernel's static shared memory (the wait status). Configures the kernel for it once.
 template <int KIND, bool OT4>
 int dyn_limit() {
     static int limit = -1;

@@ -29,13 +29,13 @@ struct Persist2D {
     const int* tpoint;
     const float* src_amp;        // [nt][n_src]
     int n_src;
-    const Gather* gat;           // receivers, gathered after each step's barrier
+    const Gather* gat;           // receivers, each gathered by the CTA holding its base corner
     int n_rec;
     float* rec_amp;              // [nt][n_rec]
-    unsigned* bar;               // grid barrier: [0] arrivals, [1] generation (zero before the launch)
-    int* err;                    // set to 1 when a barrier wait gives up (zero before the launch)
-    int expected;                // CTAs the barrier waits for: the grid (more only to test the timeout)
-    long long spin_limit;        // polls of a barrier wait before it gives up
+    int* flag;                   // per CTA: the last step whose tile of p[t+1] is stored (zero before the launch)
+    int* err;                    // set to 1 when a flag wait gives up (zero before the launch)
+    int extra;                   // steps a wait asks for beyond the one it needs (nonzero only to test the timeout)
+    long long spin_limit;        // polls of a flag wait before it gives up
 };
 
 // Shared memory of a CTA with tiles of tx x ty points; co-resident CTAs per SM of that size.

@@ -206,7 +206,7 @@ struct sa_plan {
     long long persist_spin = 10000000;
     int ptx = 0, pty = 0, ptiles_x = 0, ptiles_y = 0, pblocks = 0;
     size_t psmem = 0;
-    unsigned* pbar = nullptr;  // [0] arrivals, [1] generation, [2] error flag
+    int* pbar = nullptr;  // step flags of the persistent CTAs, then the error flag
     size_t cap_pbar = 0;
     int *pcta_off = nullptr, *pcta_tgt = nullptr;
     size_t cap_pcta_off = 0, cap_pcta_tgt = 0;
@@ -1046,10 +1046,10 @@ int forward_persistent(sa_plan* p, cudaStream_t s) {
     for (int k = 0; k < p->stgt.n; k++) tgt[fill[owner[k]]++] = k;
     CKR(ensure(&p->pcta_off, &p->cap_pcta_off, cnt.size()));
     CKR(ensure(&p->pcta_tgt, &p->cap_pcta_tgt, std::max<size_t>(1, tgt.size())));
-    CKR(ensure(&p->pbar, &p->cap_pbar, 4));
+    CKR(ensure(&p->pbar, &p->cap_pbar, (size_t)p->pblocks + 1));
     CK(cudaMemcpyAsync(p->pcta_off, cnt.data(), cnt.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     if (!tgt.empty()) CK(cudaMemcpyAsync(p->pcta_tgt, tgt.data(), tgt.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(p->pbar, 0, 4 * sizeof(unsigned), s));
+    CK(cudaMemsetAsync(p->pbar, 0, ((size_t)p->pblocks + 1) * sizeof(int), s));
     CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
     CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
     CK(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * p->n_rec * sizeof(float), s));
@@ -1073,16 +1073,17 @@ int forward_persistent(sa_plan* p, cudaStream_t s) {
     a.gat = p->gat_flat;
     a.n_rec = p->n_rec;
     a.rec_amp = p->rec_amp;
-    a.bar = p->pbar;
-    a.err = reinterpret_cast<int*>(p->pbar + 2);
-    a.expected = p->pblocks + p->persist_extra;
+    a.flag = p->pbar;
+    a.err = p->pbar + p->pblocks;
+    a.extra = p->persist_extra;
     a.spin_limit = p->persist_spin;
     CK(sa::launch_persist2d(p->kind, p->ot4, p->pblocks, p->psmem, s, a));
     int err = 0;
-    CK(cudaMemcpyAsync(&err, p->pbar + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&err, p->pbar + p->pblocks, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    if (err) return fail(SA_E_TIMEOUT, "persistent forward: a grid barrier wait gave up (%d CTAs expected, %d launched)",
-                         a.expected, p->pblocks);
+    if (err)
+        return fail(SA_E_TIMEOUT, "persistent forward: a step-flag wait gave up (%d CTAs, %d steps asked beyond the need)",
+                    p->pblocks, a.extra);
     p->launches = 1;
     return SA_OK;
 }

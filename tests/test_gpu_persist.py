@@ -1,8 +1,9 @@
 """The persistent forward of small batches (one cooperative launch runs every step,
 stride_gb300/csrc/persist2d.cu): its traces equal the streaming step passes' bit for bit for every
-operator variant and for uneven batches; the single-shot workload matches the oracle; and a grid
-barrier that cannot complete (the tests' option makes it wait for one CTA more than launched)
-gives up within its bound: sa_forward returns SA_E_TIMEOUT and the plan keeps working."""
+operator variant and for uneven batches; the single-shot workload matches the oracle; and step-flag
+waits that cannot complete (the tests' option makes each wait ask for one step more than the tiles
+can have published) give up within their bound: sa_forward returns SA_E_TIMEOUT and the plan keeps
+working."""
 
 import numpy as np
 import pytest
@@ -49,8 +50,8 @@ def test_barrier_timeout_is_reported_and_the_plan_recovers():
     c = C.small_case(kernel='OT4', density='variable', alpha=True, n_shots=2, nt=120)
     plan = C.make_plan(c)
     good = _forward(c, plan, 1)
-    plan.set_option(_lib.SA_OPT_BARRIER_SPIN, 20000)  # about 2 ms per wait
-    plan.set_option(_lib.SA_OPT_BARRIER_EXTRA, 1)     # one CTA more than launched: no wait can complete
+    plan.set_option(_lib.SA_OPT_BARRIER_SPIN, 20000)  # milliseconds per wait
+    plan.set_option(_lib.SA_OPT_BARRIER_EXTRA, 1)     # one step ahead of every tile: no wait can complete
     with pytest.raises(_lib.StrideAccError) as e:
         _forward(c, plan, 1)
     assert e.value.code == _lib.SA_E_TIMEOUT
