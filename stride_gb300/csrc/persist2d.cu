@@ -3,24 +3,26 @@
 // One cooperative launch runs every time step of the forward (the loop OperatorDevito.run drives,
 // stride/physics/common/devito.py:1025-1070). Each CTA owns a tile of one shot pair and keeps in
 // shared memory, for the whole run, the medium of its region, p[t-1] and p[t] of its tile and the
-// halo of p[t]. CTAs synchronise by step flags: a CTA publishes its flag after storing its tile of
-// p[t+1], and before step t+1 waits only for the tiles its halo overlaps. A step of a CTA:
-//   1. (t > 1) wait for the flags of step t-1, then the halo of p[t] from global memory, a ring of
-//      2R (OT4) or R (OT2) points (zero beyond the grid, Devito's halo of p); the receivers of the
-//      step before, rec[t-1] = interp(p[t]) (iso_acoustic/devito.py:364), by the CTA that holds
-//      each receiver's base corner;
+// halo of p[t]. CTAs exchange the tiles through global memory as self-validating lines (the value
+// of a point with its level number in one 16-byte store), so that no fence, flag or barrier is
+// needed: a CTA polls the lines of its halo until they hold the level it needs. A step of a CTA:
+//   1. (t > 1) the halo of p[t], a ring of 2R (OT4) or R (OT2) points (zero beyond the grid,
+//      Devito's halo of p); the receivers of the step before, rec[t-1] = interp(p[t])
+//      (iso_acoustic/devito.py:364), by the CTA that holds each receiver's base corner;
 //   2. OT4: l = W G(p[t]) over the tile and R more (zero beyond the grid, as Devito's `laplacian`),
 //      recomputed by each CTA for its halo so that no second exchange is needed;
 //   3. the update of the tile, p[t+1] = C1 Lt + C2 p[t] - C3 p[t-1];
 //   4. the sources of step t at the tile's points (iso_acoustic/devito.py:357-363), each target
 //      point's entries summed in a fixed order;
-//   5. p[t+1] of the tile to global memory and the flag of step t.
-// Every point's arithmetic is the step passes' (fdtd2d.cuh) operation for operation, so the traces
-// equal the streaming forward's bit for bit.
+//   5. p[t+1] of the tile to its exchange lines (two slots, by the parity of the level).
+// A slot is rewritten two levels later, by which time every neighbour has read it: a CTA that
+// writes level t+1 has read level t of each neighbour, which that neighbour wrote after reading
+// its halo of level t-1. Every point's arithmetic is the step passes' (fdtd2d.cuh) operation for
+// operation, so the traces equal the streaming forward's bit for bit.
 //
-// The flag waits are bounded: a wait that gives up sets an error flag, every CTA leaves the time
-// loop at its next wait, and the host reports SA_E_TIMEOUT. The cooperative launch guarantees that
-// every CTA is resident, so that no wait depends on a CTA that cannot start.
+// The polls are bounded: a wait that gives up sets an error flag, every CTA leaves the time loop
+// at its next wait, and the host reports SA_E_TIMEOUT. The cooperative launch guarantees that every
+// CTA is resident, so that no wait depends on a CTA that cannot start.
 #include <cooperative_groups.h>
 
 #include "fdtd2d.cuh"
@@ -30,43 +32,24 @@ namespace sa {
 
 namespace {
 
-// Waits until the tiles of rows [r0, r1) x columns [c0, c1) (flags base + row tiles_y + column)
-// have published step `need`, each flag polled by one thread with a bounded wait. Returns false
-// when a wait gave up here or elsewhere (the error flag); the caller then leaves its time loop.
-__device__ bool wait_tiles(const int* flag, int* err, int base, int tiles_y, int r0, int r1, int c0, int c1, int need,
-                           long long spin_limit) {
-    __shared__ int ok_s;
-    if (threadIdx.x == 0) ok_s = 1;
-    __syncthreads();
-    const int nc = c1 - c0, n = (r1 - r0) * nc;
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const volatile int* f = flag + base + (r0 + e / nc) * tiles_y + c0 + e % nc;
-        const volatile int* verr = err;
-        long long k = 0;
-        while (*f < need) {
-            if (*verr || ++k > spin_limit) {
-                atomicExch(err, 1);
-                ok_s = 0;
-                break;
-            }
-            __nanosleep(32);
-        }
-    }
-    __threadfence();
-    __syncthreads();
-    return ok_s != 0;
+// Exchange lines: p at one point of a shot pair with the level it belongs to, {p0, level, p1, level},
+// stored and loaded as one 16-byte volatile access. A reader takes a line when both level words
+// match; each 8-byte half (value and level) is written and read whole, so a matching line holds
+// that level's values.
+__device__ __forceinline__ void st_line(uint4* q, float2 v, unsigned level) {
+    asm volatile("st.volatile.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(q), "r"(__float_as_uint(v.x)), "r"(level),
+                 "r"(__float_as_uint(v.y)), "r"(level)
+                 : "memory");
 }
 
-// Publishes step t of CTA b: its stores of the step before the flag.
-__device__ __forceinline__ void publish(int* flag, int b, int t) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        atomicExch(flag + b, t);
-    }
+__device__ __forceinline__ uint4 ld_line(const uint4* q) {
+    uint4 v;
+    asm volatile("ld.volatile.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(q)
+                 : "memory");
+    return v;
 }
-
-__device__ __forceinline__ float2 ld_cg2(const float* p) { return __ldcg(reinterpret_cast<const float2*>(p)); }
 
 // Buoyancy tables of a CTA in shared memory: bx at half-rows [fx0, fx0 + fh) x columns
 // [fy0, fy0 + fw), by at rows [gx0, gx0 + gh) x half-columns [gy0, gy0 + gw).
@@ -76,63 +59,98 @@ struct BTables {
     int fx0, fy0, fw, gx0, gy0, gw;
 };
 
+// Rows of padding below the shared arrays that stencil_region reads: a block of NR output rows
+// may run past the region's last row by up to NR - 1 rows, whose loads land in the padding.
+constexpr int PERSIST_NR_MAX = 4;
+
 // G(in) over the output region [ox0, ox1) x [oy0, oy1) of shared array `in` (origin (ix0, iy0),
-// row stride iw; it covers the region and R more on every side); epi(x, y, g) per output point.
-// Staggered kinds stage the x- and y-fluxes in sFX / sFY first. Operation for operation the
-// arithmetic of the step passes' queues and windows.
-template <int KIND, class Epi>
+// row stride iw; it covers the region and R more on every side, and PERSIST_NR_MAX - 1 rows of
+// padding); epi(x, y, g) per output point. A thread computes a block of NR rows of one column,
+// the x-direction loads shared between the rows. Staggered kinds stage the x- and y-fluxes in sFX
+// / sFY first. Operation for operation the arithmetic of the step passes' queues and windows.
+template <int KIND, int NR, class Epi>
 __device__ __forceinline__ void stencil_region(const Step2D& a, const float2* in, int ix0, int iy0, int iw, int ox0,
                                                int ox1, int oy0, int oy1, float2* sFX, float2* sFY, const BTables& B,
                                                Epi epi) {
+    static_assert(NR >= 1 && NR <= PERSIST_NR_MAX, "row block");
     constexpr bool STAG = KIND != 0, VARB = KIND == 1;
     const int NTH = blockDim.x, tid = threadIdx.x;
     const int ow = oy1 - oy0, oh = ox1 - ox0;
-    auto at = [&](int x, int y) { return in[(x - ix0) * iw + (y - iy0)]; };
     if constexpr (STAG) {
         // x-fluxes at half-rows ox0 - 5 .. ox1 + 3 (flux h at h + 1/2), columns of the region
-        for (int e = tid; e < (oh + 9) * ow; e += NTH) {
-            const int h = ox0 - 5 + e / ow, y = oy0 + e % ow;
-            float2 acc = mul2(a.wx[0], sub2(at(h + 1, y), at(h, y)));
+        const int fh = oh + 9, nbf = (fh + NR - 1) / NR;
+        for (int e = tid; e < nbf * ow; e += NTH) {
+            const int rb = e / ow, yc = e - rb * ow, h0 = ox0 - 5 + rb * NR, y = oy0 + yc;
+            const float2* col = in + (h0 - 4 - ix0) * iw + (y - iy0);  // rows h0 - 4 ..
+            float2 w[NR + 9];
 #pragma unroll
-            for (int m = 1; m < 5; m++) acc = fma2(a.wx[m], sub2(at(h + 1 + m, y), at(h - m, y)), acc);
-            if constexpr (VARB) acc = mul2(acc, f2(B.bx[(h - B.fx0) * B.fw + (y - B.fy0)]));
-            sFX[e] = acc;
+            for (int i = 0; i < NR + 9; i++) w[i] = col[i * iw];
+#pragma unroll
+            for (int r = 0; r < NR; r++) {
+                const int h = h0 + r;
+                if (h - (ox0 - 5) >= fh) break;
+                float2 acc = mul2(a.wx[0], sub2(w[r + 5], w[r + 4]));
+#pragma unroll
+                for (int m = 1; m < 5; m++) acc = fma2(a.wx[m], sub2(w[r + 5 + m], w[r + 4 - m]), acc);
+                if constexpr (VARB) acc = mul2(acc, f2(B.bx[(h - B.fx0) * B.fw + (y - B.fy0)]));
+                sFX[(h - (ox0 - 5)) * ow + yc] = acc;
+            }
         }
         // y-fluxes at half-columns oy0 - 5 .. oy1 + 3, rows of the region
         for (int e = tid; e < oh * (ow + 9); e += NTH) {
-            const int x = ox0 + e / (ow + 9), hc = oy0 - 5 + e % (ow + 9);
-            float2 acc = mul2(a.wy[0], sub2(at(x, hc + 1), at(x, hc)));
+            const int xr = e / (ow + 9), x = ox0 + xr, hc = oy0 - 5 + (e - xr * (ow + 9));
+            const float2* row = in + (x - ix0) * iw + (hc - iy0);
+            float2 acc = mul2(a.wy[0], sub2(row[1], row[0]));
 #pragma unroll
-            for (int m = 1; m < 5; m++) acc = fma2(a.wy[m], sub2(at(x, hc + 1 + m), at(x, hc - m)), acc);
+            for (int m = 1; m < 5; m++) acc = fma2(a.wy[m], sub2(row[1 + m], row[-m]), acc);
             if constexpr (VARB) acc = mul2(acc, f2(B.by[(x - B.gx0) * B.gw + (hc - B.gy0)]));
             sFY[e] = acc;
         }
         __syncthreads();
-        for (int e = tid; e < oh * ow; e += NTH) {
-            const int xr = e / ow, yr = e % ow;
-            const float2* fx = sFX + (xr + 5) * ow + yr;     // flux at half-row x (x + 1/2)
-            const float2* fy = sFY + xr * (ow + 9) + yr + 5;  // flux at half-column y
-            float2 gx = mul2(a.wx[0], sub2(fx[0], fx[-ow]));
-            float2 gy = mul2(a.wy[0], sub2(fy[0], fy[-1]));
+        const int nb = (oh + NR - 1) / NR;
+        for (int e = tid; e < nb * ow; e += NTH) {
+            const int rb = e / ow, yc = e - rb * ow, xr0 = rb * NR;
+            const float2* fxc = sFX + xr0 * ow + yc;  // half-rows x - 5 .. of output row x = ox0 + xr0
+            float2 w[NR + 9];
 #pragma unroll
-            for (int m = 1; m < 5; m++) {
-                gx = fma2(a.wx[m], sub2(fx[m * ow], fx[-(1 + m) * ow]), gx);
-                gy = fma2(a.wy[m], sub2(fy[m], fy[-1 - m]), gy);
+            for (int i = 0; i < NR + 9; i++) w[i] = fxc[i * ow];
+#pragma unroll
+            for (int r = 0; r < NR; r++) {
+                const int xr = xr0 + r;
+                if (xr >= oh) break;
+                const float2* fy = sFY + xr * (ow + 9) + yc + 5;  // flux at half-column y
+                float2 gx = mul2(a.wx[0], sub2(w[r + 5], w[r + 4]));
+                float2 gy = mul2(a.wy[0], sub2(fy[0], fy[-1]));
+#pragma unroll
+                for (int m = 1; m < 5; m++) {
+                    gx = fma2(a.wx[m], sub2(w[r + 5 + m], w[r + 4 - m]), gx);
+                    gy = fma2(a.wy[m], sub2(fy[m], fy[-1 - m]), gy);
+                }
+                epi(ox0 + xr, oy0 + yc, add2(gx, gy));
             }
-            epi(ox0 + xr, oy0 + yr, add2(gx, gy));
         }
         __syncthreads();  // the flux rows are reused
     } else {
-        for (int e = tid; e < oh * ow; e += NTH) {
-            const int x = ox0 + e / ow, y = oy0 + e % ow;
-            float2 gx = mul2(a.wx[0], at(x, y));
-            float2 gy = mul2(a.wy[0], at(x, y));
+        const int nb = (oh + NR - 1) / NR;
+        for (int e = tid; e < nb * ow; e += NTH) {
+            const int rb = e / ow, yc = e - rb * ow, xs = ox0 + rb * NR, y = oy0 + yc;
+            const float2* col = in + (xs - ix0) * iw + (y - iy0);  // (xs, y)
+            float2 w[NR + 10];
 #pragma unroll
-            for (int k = 1; k <= 5; k++) {
-                gx = fma2(a.wx[k], add2(at(x + k, y), at(x - k, y)), gx);
-                gy = fma2(a.wy[k], add2(at(x, y + k), at(x, y - k)), gy);
+            for (int i = 0; i < NR + 10; i++) w[i] = col[(i - 5) * iw];
+#pragma unroll
+            for (int r = 0; r < NR; r++) {
+                if (xs + r >= ox1) break;
+                const float2* row = col + r * iw;
+                float2 gx = mul2(a.wx[0], w[r + 5]);
+                float2 gy = mul2(a.wy[0], w[r + 5]);
+#pragma unroll
+                for (int k = 1; k <= 5; k++) {
+                    gx = fma2(a.wx[k], add2(w[r + 5 + k], w[r + 5 - k]), gx);
+                    gy = fma2(a.wy[k], add2(row[k], row[-k]), gy);
+                }
+                epi(xs + r, y, add2(gx, gy));
             }
-            epi(x, y, add2(gx, gy));
         }
     }
 }
@@ -145,10 +163,15 @@ struct PersistCfg {
     // shared memory: float2 arrays of p[t] over the tile and halo, l (OT4), the flux rows of the
     // larger stage (staggered), p[t-1] and p[t+1] over the tile; float tables of the medium: W
     // over the stage-1 region, C1, C2, -C3 over the tile, bx and by over the stage-1 flux regions
-    __host__ __device__ static constexpr size_t nU(int tx, int ty) { return (size_t)(tx + 2 * HU) * (ty + 2 * HU); }
-    __host__ __device__ static constexpr size_t nL(int tx, int ty) { return OT4 ? (size_t)(tx + 2 * HL) * (ty + 2 * HL) : 0; }
+    static constexpr int PADR = PERSIST_NR_MAX - 1;  // rows of padding of the arrays stencil_region reads
+    __host__ __device__ static constexpr size_t nU(int tx, int ty) {
+        return (size_t)(tx + 2 * HU + PADR) * (ty + 2 * HU);
+    }
+    __host__ __device__ static constexpr size_t nL(int tx, int ty) {
+        return OT4 ? (size_t)(tx + 2 * HL + PADR) * (ty + 2 * HL) : 0;
+    }
     __host__ __device__ static constexpr size_t nF(int tx, int ty) {
-        return KIND != 0 ? (size_t)(tx + 2 * HL + 9) * (ty + 2 * HL) : 0;
+        return KIND != 0 ? (size_t)(tx + 2 * HL + 9 + PADR) * (ty + 2 * HL) : 0;
     }
     __host__ __device__ static constexpr size_t nG(int tx, int ty) {
         return KIND != 0 ? (size_t)(tx + 2 * HL) * (ty + 2 * HL + 9) : 0;
@@ -195,7 +218,6 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
     const int th = x1 - x0, tw = y1 - y0;
     const int uw = ty + 2 * HU, lw = ty + 2 * HL;
     const int mp = a.mpitch, pitch = a.pitch;
-    const long long poff = (long long)pair * a.shot_stride * 2;  // floats per pair
     const int ux0 = x0 - HU, uy0 = y0 - HU, uh = th + 2 * HU, uwr = tw + 2 * HU;
     const int lx0 = x0 - HL, ly0 = y0 - HL, lh = th + 2 * HL, lwr = tw + 2 * HL;
 
@@ -227,21 +249,49 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
     for (int e = tid; e < uh * uwr; e += NTH) sU[(e / uwr) * uw + e % uwr] = f2(0.f);
     __syncthreads();
 
-    // the tiles whose points the halo covers, this CTA's own included
-    const int nr0 = max(0, x0 - HU) / tx, nr1 = (min(a.nx, x1 + HU) - 1) / tx + 1;
-    const int nc0 = max(0, y0 - HU) / ty, nc1 = (min(a.ny, y1 + HU) - 1) / ty + 1;
-    // p[level] beyond the tile, once those tiles have published it (step level - 1)
-    auto load_halo = [&](const float* f, int level) -> bool {
-        if (!wait_tiles(P.flag, P.err, pair * ntile, P.tiles_y, nr0, nr1, nc0, nc1, level - 1 + P.extra, P.spin_limit))
-            return false;
-        for (int e = tid; e < uh * uwr; e += NTH) {
-            const int xr = e / uwr, yr = e % uwr, x = ux0 + xr, y = uy0 + yr;
-            if (x >= x0 && x < x1 && y >= y0 && y < y1) continue;
-            const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
-            sU[xr * uw + yr] = in ? ld_cg2(f + 2 * ((long long)x * pitch + y)) : f2(0.f);
+    // p[level] beyond the tile, from the neighbour tiles' exchange lines: a thread loads its lines in
+    // batches of PERSIST_BATCH and reloads the ones that do not hold the level yet, all together,
+    // until they do (a bounded wait)
+    auto load_halo = [&](int level) -> bool {
+        const uint4* src = P.xch + (level & 1) * P.xch_slot + (long long)pair * a.shot_stride;
+        const unsigned want = (unsigned)(level + P.extra);
+        const volatile int* verr = P.err;
+        bool ok = true;
+        for (int e0 = tid; e0 < uh * uwr && ok; e0 += PERSIST_BATCH * NTH) {
+            uint4 v[PERSIST_BATCH];
+            int at[PERSIST_BATCH], gi[PERSIST_BATCH];
+            unsigned pending = 0;
+#pragma unroll
+            for (int k = 0; k < PERSIST_BATCH; k++) {
+                const int e = e0 + k * NTH, xr = e / uwr, yr = e % uwr, x = ux0 + xr, y = uy0 + yr;
+                const bool tile = x >= x0 && x < x1 && y >= y0 && y < y1;
+                at[k] = e < uh * uwr && !tile && x >= 0 && x < a.nx && y >= 0 && y < a.ny ? xr * uw + yr : -1;
+                gi[k] = x * pitch + y;
+                if (at[k] >= 0) {
+                    v[k] = ld_line(src + gi[k]);
+                    pending |= 1u << k;
+                }
+            }
+            for (long long n = 0;; n++) {
+#pragma unroll
+                for (int k = 0; k < PERSIST_BATCH; k++)
+                    if ((pending >> k & 1) && v[k].y == want && v[k].w == want) {
+                        sU[at[k]] = make_float2(__uint_as_float(v[k].x), __uint_as_float(v[k].z));
+                        pending &= ~(1u << k);
+                    }
+                if (!pending) break;
+                if (n >= P.spin_limit || *verr) {
+                    atomicExch(P.err, 1);
+                    ok = false;
+                    break;
+                }
+                PERSIST_POLL_PAUSE;
+#pragma unroll
+                for (int k = 0; k < PERSIST_BATCH; k++)
+                    if (pending >> k & 1) v[k] = ld_line(src + gi[k]);
+            }
         }
-        __syncthreads();
-        return true;
+        return __syncthreads_and(ok) != 0;
     };
 
     // receivers whose corners this CTA holds: base corner (row, col) in the tile
@@ -258,11 +308,10 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
     };
 
     for (int t = 1; t <= P.nt - 2; t++) {
-        const float* cur = ((t & 1) ? P.f1 : P.f0) + poff;
-        float* nxt = ((t & 1) ? P.f0 : P.f1) + poff;  // p[t+1] out (in place of p[t-1])
-        // 1. p[t]: the halo from global memory (the tile's own points are in sU since last step)
+        uint4* out = P.xch + ((t + 1) & 1) * P.xch_slot + (long long)pair * a.shot_stride;  // p[t+1]
+        // 1. p[t]: the halo (the tile's own points are in sU since last step)
         if (t > 1) {
-            if (!load_halo(cur, t)) return;
+            if (!load_halo(t)) return;
             gather_from_smem(t - 1);  // rec[t-1] = interp(p[t])
         }
         // 2-3. the update of the tile into sN (OT4: after l over the tile and R more)
@@ -272,19 +321,19 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
             sN[k] = fma2(f2(sC1[k]), Lt, fma2(f2(sC2[k]), u, mul2(f2(sC3[k]), sPm[k])));
         };
         if constexpr (OT4) {
-            stencil_region<KIND>(a, sU, ux0, uy0, uw, lx0, x1 + HL, ly0, y1 + HL, sFX, sFY, B,
+            stencil_region<KIND, 4>(a, sU, ux0, uy0, uw, lx0, x1 + HL, ly0, y1 + HL, sFX, sFY, B,
                                  [&](int x, int y, float2 g) {
                                      const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
                                      const float W = sW[(x - lx0) * lw + (y - ly0)];
                                      sL[(x - lx0) * lw + (y - ly0)] = in ? mul2(f2(W), g) : f2(0.f);
                                  });
             __syncthreads();
-            stencil_region<KIND>(a, sL, lx0, ly0, lw, x0, x1, y0, y1, sFX, sFY, B, [&](int x, int y, float2 g) {
+            stencil_region<KIND, 2>(a, sL, lx0, ly0, lw, x0, x1, y0, y1, sFX, sFY, B, [&](int x, int y, float2 g) {
                 const float Wk = sW[(x - lx0) * lw + (y - ly0)] * a.k12;
                 update(x, y, fma2(f2(Wk), g, sL[(x - lx0) * lw + (y - ly0)]));
             });
         } else {
-            stencil_region<KIND>(a, sU, ux0, uy0, uw, x0, x1, y0, y1, sFX, sFY, B, [&](int x, int y, float2 g) {
+            stencil_region<KIND, 2>(a, sU, ux0, uy0, uw, x0, x1, y0, y1, sFX, sFY, B, [&](int x, int y, float2 g) {
                 update(x, y, mul2(f2(sW[(x - lx0) * lw + (y - ly0)]), g));
             });
         }
@@ -295,7 +344,7 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
             float v = 0.f;
             const float* amp = P.src_amp + (long long)t * P.n_src;
             for (int e = P.toff[tg]; e < P.toff[tg + 1]; e++) v += P.tcoef[e] * amp[P.tpoint[e]];
-            const long long i = P.tidx[tg] - poff, c2 = i / 2;  // float index within the pair
+            const long long i = P.tidx[tg] - (long long)pair * a.shot_stride * 2, c2 = i / 2;  // float in the pair
             const int x = (int)(c2 / pitch), y = (int)(c2 % pitch);
             float* s = reinterpret_cast<float*>(sN + (x - x0) * ty + (y - y0)) + (i & 1);
             *s = *s + v;
@@ -308,18 +357,17 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
             float2* u = sU + (xr + HU) * uw + (yr + HU);
             sPm[k] = *u;
             *u = v;
-            __stcg(reinterpret_cast<float2*>(nxt + 2 * ((long long)(x0 + xr) * pitch + (y0 + yr))), v);
+            st_line(out + (long long)(x0 + xr) * pitch + (y0 + yr), v, (unsigned)(t + 1));
         }
-        publish(P.flag, b, t);
     }
     // the last step's receivers, rec[nt-2] = interp(p[nt-1]), with the halo of p[nt-1]
     if (P.nt < 3) return;
-    if (!load_halo((((P.nt - 2) & 1) ? P.f0 : P.f1) + poff, P.nt - 1)) return;
+    if (!load_halo(P.nt - 1)) return;
     gather_from_smem(P.nt - 2);
 }
 
 // Largest dynamic shared memory of a CTA of the kernel: the device's opt-in limit less the
-// kernel's static shared memory (the wait status). Configures the kernel for it once.
+// kernel's static shared memory. Configures the kernel for it once.
 template <int KIND, bool OT4>
 int dyn_limit() {
     static int limit = -1;

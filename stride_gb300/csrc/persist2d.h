@@ -9,13 +9,21 @@ namespace sa {
 #define SA_PERSIST_THREADS 512
 #endif
 constexpr int PERSIST_THREADS = SA_PERSIST_THREADS;
+// halo lines a thread has in flight at once
+#ifndef SA_PERSIST_BATCH
+#define SA_PERSIST_BATCH 8
+#endif
+constexpr int PERSIST_BATCH = SA_PERSIST_BATCH;
+// between polls of lines that do not hold their level yet
+#ifndef PERSIST_POLL_PAUSE
+#define PERSIST_POLL_PAUSE __nanosleep(20)
+#endif
 
-// Arguments of the persistent forward. Step t reads p[t] from f1 (t odd) or f0 and writes p[t+1]
-// in place of p[t-1], as the step passes do.
+// Arguments of the persistent forward.
 struct Persist2D {
     Step2D s;                    // grid, pitch, shot stride, medium, weights (field pointers unused)
-    float* f0;
-    float* f1;
+    uint4* xch;                  // exchange lines: slot (level & 1), pair, point x pitch + y (zero before the launch)
+    long long xch_slot;          // lines per slot
     int nt;                      // steps 1 .. nt-2
     int tx, ty;                  // tile rows and columns of a CTA (ty even)
     int tiles_x, tiles_y;        // tiles of one shot pair; CTA b: pair b / (tiles_x tiles_y)
@@ -32,10 +40,9 @@ struct Persist2D {
     const Gather* gat;           // receivers, each gathered by the CTA holding its base corner
     int n_rec;
     float* rec_amp;              // [nt][n_rec]
-    int* flag;                   // per CTA: the last step whose tile of p[t+1] is stored (zero before the launch)
-    int* err;                    // set to 1 when a flag wait gives up (zero before the launch)
-    int extra;                   // steps a wait asks for beyond the one it needs (nonzero only to test the timeout)
-    long long spin_limit;        // polls of a flag wait before it gives up
+    int* err;                    // set to 1 when a wait gives up (zero before the launch)
+    int extra;                   // levels a wait asks for beyond the one it needs (nonzero only to test the timeout)
+    long long spin_limit;        // polls of an exchange line before its wait gives up
 };
 
 // Shared memory of a CTA with tiles of tx x ty points; co-resident CTAs per SM of that size.

@@ -206,7 +206,9 @@ struct sa_plan {
     long long persist_spin = 10000000;
     int ptx = 0, pty = 0, ptiles_x = 0, ptiles_y = 0, pblocks = 0;
     size_t psmem = 0;
-    int* pbar = nullptr;  // step flags of the persistent CTAs, then the error flag
+    int* pbar = nullptr;  // error flag of the persistent launch
+    uint4* pxch = nullptr;  // its exchange lines
+    size_t cap_pxch = 0;
     size_t cap_pbar = 0;
     int *pcta_off = nullptr, *pcta_tgt = nullptr;
     size_t cap_pcta_off = 0, cap_pcta_tgt = 0;
@@ -1029,7 +1031,6 @@ bool use_persistent(sa_plan* p, int save_mode) {
 }
 
 int forward_persistent(sa_plan* p, cudaStream_t s) {
-    const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
     // the sources' targets by owning CTA (tile and shot pair of the target point), in target order
     const int ntile = p->ptiles_x * p->ptiles_y;
     std::vector<int> cnt(p->pblocks + 1, 0), tgt(p->stgt.n);
@@ -1046,17 +1047,18 @@ int forward_persistent(sa_plan* p, cudaStream_t s) {
     for (int k = 0; k < p->stgt.n; k++) tgt[fill[owner[k]]++] = k;
     CKR(ensure(&p->pcta_off, &p->cap_pcta_off, cnt.size()));
     CKR(ensure(&p->pcta_tgt, &p->cap_pcta_tgt, std::max<size_t>(1, tgt.size())));
-    CKR(ensure(&p->pbar, &p->cap_pbar, (size_t)p->pblocks + 1));
+    const size_t slot = (size_t)npairs(p) * p->shot_stride;
+    CKR(ensure(&p->pbar, &p->cap_pbar, 1));
+    CKR(ensure(&p->pxch, &p->cap_pxch, 2 * slot));
     CK(cudaMemcpyAsync(p->pcta_off, cnt.data(), cnt.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     if (!tgt.empty()) CK(cudaMemcpyAsync(p->pcta_tgt, tgt.data(), tgt.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(p->pbar, 0, ((size_t)p->pblocks + 1) * sizeof(int), s));
-    CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
-    CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
+    CK(cudaMemsetAsync(p->pbar, 0, sizeof(int), s));
+    CK(cudaMemsetAsync(p->pxch, 0, 2 * slot * sizeof(uint4), s));  // no line holds a level of this run
     CK(cudaMemsetAsync(p->rec_amp, 0, (size_t)p->d.nt * p->n_rec * sizeof(float), s));
     sa::Persist2D a{};
     a.s = base_args(p);
-    a.f0 = p->field[0];
-    a.f1 = p->field[1];
+    a.xch = p->pxch;
+    a.xch_slot = (long long)slot;
     a.nt = p->d.nt;
     a.tx = p->ptx;
     a.ty = p->pty;
@@ -1073,16 +1075,15 @@ int forward_persistent(sa_plan* p, cudaStream_t s) {
     a.gat = p->gat_flat;
     a.n_rec = p->n_rec;
     a.rec_amp = p->rec_amp;
-    a.flag = p->pbar;
-    a.err = p->pbar + p->pblocks;
+    a.err = p->pbar;
     a.extra = p->persist_extra;
     a.spin_limit = p->persist_spin;
     CK(sa::launch_persist2d(p->kind, p->ot4, p->pblocks, p->psmem, s, a));
     int err = 0;
-    CK(cudaMemcpyAsync(&err, p->pbar + p->pblocks, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&err, p->pbar, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (err)
-        return fail(SA_E_TIMEOUT, "persistent forward: a step-flag wait gave up (%d CTAs, %d steps asked beyond the need)",
+        return fail(SA_E_TIMEOUT, "persistent forward: a halo wait gave up (%d CTAs, %d levels asked beyond the need)",
                     p->pblocks, a.extra);
     p->launches = 1;
     return SA_OK;
@@ -1289,7 +1290,7 @@ int sa_plan_destroy(sa_plan* p) {
                     p->gat_flat,
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
-                    p->smed, p->lbuf, p->pbar, p->pcta_off, p->pcta_tgt, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
+                    p->smed, p->lbuf, p->pbar, p->pxch, p->pcta_off, p->pcta_tgt, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
                     p->dbx, p->dby, p->pml_prof, p->pml_aux, p->pml_ck, p->pml_aux_f, p->ckpt2, p->pml_ck2,
                     p->wgrad, p->hgat, p->hgat_src, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
                     p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx, p->xtgt.off, p->xtgt.point, p->xtgt.coef};
