@@ -37,14 +37,14 @@ namespace {
 // match; each 8-byte half (value and level) is written and read whole, so a matching line holds
 // that level's values.
 __device__ __forceinline__ void st_line(uint4* q, float2 v, unsigned level) {
-    asm volatile("st.volatile.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(q), "r"(__float_as_uint(v.x)), "r"(level),
+    asm volatile("st." PERSIST_LINE_SEM ".global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(q), "r"(__float_as_uint(v.x)), "r"(level),
                  "r"(__float_as_uint(v.y)), "r"(level)
                  : "memory");
 }
 
 __device__ __forceinline__ uint4 ld_line(const uint4* q) {
     uint4 v;
-    asm volatile("ld.volatile.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+    asm volatile("ld." PERSIST_LINE_SEM ".global.v4.u32 {%0, %1, %2, %3}, [%4];"
                  : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
                  : "l"(q)
                  : "memory");
@@ -162,7 +162,9 @@ struct PersistCfg {
     static constexpr int HL = OT4 ? R : 0;      // stage-1 region beyond the tile
     // shared memory: float2 arrays of p[t] over the tile and halo, l (OT4), the flux rows of the
     // larger stage (staggered), p[t-1] and p[t+1] over the tile; float tables of the medium: W
-    // over the stage-1 region, C1, C2, -C3 over the tile, bx and by over the stage-1 flux regions
+    // over the stage-1 region, C1, C2, -C3 over the tile, bx and by over the stage-1 flux regions;
+    // int arrays: the source slots of the tile's points and the CTA's halo points; the float values
+    // of the CTA's sources at the step
     static constexpr int PADR = PERSIST_NR_MAX - 1;  // rows of padding of the arrays stencil_region reads
     __host__ __device__ static constexpr size_t nU(int tx, int ty) {
         return (size_t)(tx + 2 * HU + PADR) * (ty + 2 * HU);
@@ -181,8 +183,13 @@ struct PersistCfg {
     __host__ __device__ static constexpr size_t floats2(int tx, int ty) {
         return nU(tx, ty) + nL(tx, ty) + nF(tx, ty) + nG(tx, ty) + 2 * nT(tx, ty);
     }
+    // halo points of a tile (at most; fewer beyond the grid)
+    __host__ __device__ static constexpr size_t nH(int tx, int ty) {
+        return (size_t)2 * HU * (tx + ty) + (size_t)4 * HU * HU;
+    }
     __host__ __device__ static constexpr size_t floats1(int tx, int ty) {
-        return nW(tx, ty) + 3 * nT(tx, ty) + (KIND == 1 ? nF(tx, ty) + nG(tx, ty) : 0);
+        return nW(tx, ty) + 3 * nT(tx, ty) + (KIND == 1 ? nF(tx, ty) + nG(tx, ty) : 0) + nT(tx, ty) + nH(tx, ty) +
+               PERSIST_SRC_SLOTS;
     }
     __host__ __device__ static constexpr size_t bytes(int tx, int ty) {
         return floats2(tx, ty) * sizeof(float2) + floats1(tx, ty) * sizeof(float);
@@ -202,13 +209,16 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
     float2* const sFX = sL + CF::nL(tx, ty);
     float2* const sFY = sFX + CF::nF(tx, ty);
     float2* const sPm = sFY + CF::nG(tx, ty);  // p[t-1] over the tile
-    float2* const sN = sPm + CF::nT(tx, ty);   // p[t+1] over the tile
+    float2* const sN = sPm + CF::nT(tx, ty);   // p[t+1] over the tile (OT2, or a CTA with more sources than slots)
     float* const sW = reinterpret_cast<float*>(sN + CF::nT(tx, ty));
     float* const sC1 = sW + CF::nW(tx, ty);
     float* const sC2 = sC1 + CF::nT(tx, ty);
     float* const sC3 = sC2 + CF::nT(tx, ty);
     float* const sBX = sC3 + CF::nT(tx, ty);
     float* const sBY = sBX + (VARB ? CF::nF(tx, ty) : 0);
+    int* const sMap = reinterpret_cast<int*>(sBY + (VARB ? CF::nG(tx, ty) : 0));  // source slots + 1, lane 0 | lane 1 << 16
+    int* const sHal = sMap + CF::nT(tx, ty);  // halo points: row | column << 8 relative to (ux0, uy0)
+    float* const sSrc = reinterpret_cast<float*>(sHal + CF::nH(tx, ty));  // this step's source values
 
     const int tid = threadIdx.x, NTH = blockDim.x, b = blockIdx.x;
     const int ntile = P.tiles_x * P.tiles_y;
@@ -220,8 +230,12 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
     const int mp = a.mpitch, pitch = a.pitch;
     const int ux0 = x0 - HU, uy0 = y0 - HU, uh = th + 2 * HU, uwr = tw + 2 * HU;
     const int lx0 = x0 - HL, ly0 = y0 - HL, lh = th + 2 * HL, lwr = tw + 2 * HL;
+    const int sb = P.cta_off[b], ns = P.cta_off[b + 1] - sb;  // this CTA's source targets
+    const int rb = P.rec_off[b], nr = P.rec_off[b + 1] - rb;  // and receivers
+    const bool slots = ns <= PERSIST_SRC_SLOTS;  // sources added in the update (else through sN)
+    const long long pair_floats = (long long)pair * a.shot_stride * 2;
 
-    // ---- once: the medium of the CTA's region, p[1] = p[0] = 0 over the tile ------------------
+    // ---- once: the medium of the CTA's region, p[1] = p[0] = 0, the halo points, the sources ----
     for (int e = tid; e < lh * lwr; e += NTH) {
         const int x = lx0 + e / lwr, y = ly0 + e % lwr;
         sW[(x - lx0) * lw + (y - ly0)] = __ldg(a.Wm + (long long)x * mp + y);
@@ -234,6 +248,7 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
         sC2[k] = __ldg(a.C2m + q);
         sC3[k] = __ldg(a.NC3m + q);
         sPm[k] = f2(0.f);
+        sMap[k] = 0;
     }
     BTables B{sBX, sBY, lx0 - 5, ly0, lw, lx0, ly0 - 5, lw + 9};
     if constexpr (VARB) {
@@ -247,7 +262,33 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
         }
     }
     for (int e = tid; e < uh * uwr; e += NTH) sU[(e / uwr) * uw + e % uwr] = f2(0.f);
+    __shared__ int nhal_s;
+    if (tid == 0) nhal_s = 0;
     __syncthreads();
+    for (int e = tid; e < uh * uwr; e += NTH) {  // in-grid points of the halo, in any order
+        const int xr = e / uwr, yr = e % uwr, x = ux0 + xr, y = uy0 + yr;
+        const bool tile = x >= x0 && x < x1 && y >= y0 && y < y1;
+        if (!tile && x >= 0 && x < a.nx && y >= 0 && y < a.ny) sHal[atomicAdd(&nhal_s, 1)] = xr | yr << 8;
+    }
+    if (slots)
+        for (int j = tid; j < ns; j += NTH) {  // the slot of each target at its point and lane
+            const long long i = P.tidx[P.cta_tgt[sb + j]] - pair_floats, c2 = i / 2;
+            const int x = (int)(c2 / pitch), y = (int)(c2 % pitch);
+            atomicOr(sMap + (x - x0) * ty + (y - y0), (j + 1) << (16 * (int)(i & 1)));
+        }
+    // each target's value at every step, srcv[(sb + j) nt + t], summed in the targets' entry order
+    for (int e = tid; e < ns * P.nt; e += NTH) {
+        const int j = e / P.nt, t = e % P.nt, tg = P.cta_tgt[sb + j];
+        const float* amp = P.src_amp + (long long)t * P.n_src;
+        float v = 0.f;
+        for (int k = P.toff[tg]; k < P.toff[tg + 1]; k++) v += P.tcoef[k] * amp[P.tpoint[k]];
+        P.srcv[(long long)(sb + j) * P.nt + t] = v;
+    }
+    // this thread's receiver, kept in registers (a CTA with more receivers than threads reads the rest)
+    Gather G{};
+    if (tid < nr) G = P.gat[P.rec_idx[rb + tid]];
+    __syncthreads();
+    const int nhal = nhal_s;
 
     // p[level] beyond the tile, from the neighbour tiles' exchange lines: a thread loads its lines in
     // batches of PERSIST_BATCH and reloads the ones that do not hold the level yet, all together,
@@ -257,17 +298,17 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
         const unsigned want = (unsigned)(level + P.extra);
         const volatile int* verr = P.err;
         bool ok = true;
-        for (int e0 = tid; e0 < uh * uwr && ok; e0 += PERSIST_BATCH * NTH) {
+        for (int e0 = tid; e0 < nhal && ok; e0 += PERSIST_BATCH * NTH) {
             uint4 v[PERSIST_BATCH];
             int at[PERSIST_BATCH], gi[PERSIST_BATCH];
             unsigned pending = 0;
 #pragma unroll
             for (int k = 0; k < PERSIST_BATCH; k++) {
-                const int e = e0 + k * NTH, xr = e / uwr, yr = e % uwr, x = ux0 + xr, y = uy0 + yr;
-                const bool tile = x >= x0 && x < x1 && y >= y0 && y < y1;
-                at[k] = e < uh * uwr && !tile && x >= 0 && x < a.nx && y >= 0 && y < a.ny ? xr * uw + yr : -1;
-                gi[k] = x * pitch + y;
-                if (at[k] >= 0) {
+                const int e = e0 + k * NTH;
+                const int hp = e < nhal ? sHal[e] : 0, xr = hp & 255, yr = hp >> 8;
+                at[k] = xr * uw + yr;
+                gi[k] = (ux0 + xr) * pitch + uy0 + yr;
+                if (e < nhal) {
                     v[k] = ld_line(src + gi[k]);
                     pending |= 1u << k;
                 }
@@ -294,76 +335,93 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
         return __syncthreads_and(ok) != 0;
     };
 
-    // receivers whose corners this CTA holds: base corner (row, col) in the tile
-    auto gather_from_smem = [&](int trow) {
-        for (int e = tid; e < P.n_rec; e += NTH) {
-            const Gather G = P.gat[e];
-            if (G.pad / 2 != pair || G.row < x0 || G.row >= x1 || G.col < y0 || G.col >= y1) continue;
-            const float2* f0 = sU + (G.row - ux0) * uw + (G.col - uy0);
-            const float2* f1 = f0 + uw;
-            const float v00 = (G.pad & 1) ? f0[0].y : f0[0].x, v01 = (G.pad & 1) ? f0[1].y : f0[1].x;
-            const float v10 = (G.pad & 1) ? f1[0].y : f1[0].x, v11 = (G.pad & 1) ? f1[1].y : f1[1].x;
-            P.rec_amp[(long long)trow * P.n_rec + G.point] = G.w00 * v00 + G.w01 * v01 + G.w10 * v10 + G.w11 * v11;
-        }
+    // the receivers whose base corner this CTA holds, from p[level] in sU
+    auto gather_one = [&](const Gather& R, int trow) {
+        const float2* f0 = sU + (R.row - ux0) * uw + (R.col - uy0);
+        const float2* f1 = f0 + uw;
+        const float v00 = (R.pad & 1) ? f0[0].y : f0[0].x, v01 = (R.pad & 1) ? f0[1].y : f0[1].x;
+        const float v10 = (R.pad & 1) ? f1[0].y : f1[0].x, v11 = (R.pad & 1) ? f1[1].y : f1[1].x;
+        P.rec_amp[(long long)trow * P.n_rec + R.point] = R.w00 * v00 + R.w01 * v01 + R.w10 * v10 + R.w11 * v11;
+    };
+    auto gather = [&](int trow) {
+        if (tid < nr) gather_one(G, trow);
+        for (int j = tid + NTH; j < nr; j += NTH) gather_one(P.gat[P.rec_idx[rb + j]], trow);
     };
 
     for (int t = 1; t <= P.nt - 2; t++) {
         uint4* out = P.xch + ((t + 1) & 1) * P.xch_slot + (long long)pair * a.shot_stride;  // p[t+1]
+        const float sv = slots && tid < ns ? __ldcg(P.srcv + (long long)(sb + tid) * P.nt + t) : 0.f;
         // 1. p[t]: the halo (the tile's own points are in sU since last step)
         if (t > 1) {
             if (!load_halo(t)) return;
-            gather_from_smem(t - 1);  // rec[t-1] = interp(p[t])
+            gather(t - 1);  // rec[t-1] = interp(p[t])
         }
-        // 2-3. the update of the tile into sN (OT4: after l over the tile and R more)
-        auto update = [&](int x, int y, float2 Lt) {
+        if (slots) {
+            if (tid < ns) sSrc[tid] = sv;
+            for (int j = tid + NTH; j < ns; j += NTH) sSrc[j] = __ldcg(P.srcv + (long long)(sb + j) * P.nt + t);
+        }
+        // 2-3. the update of the tile: p[t+1] = C1 Lt + C2 p[t] - C3 p[t-1], plus the step's sources
+        auto update = [&](int x, int y, float2 Lt) -> float2 {
             const int k = (x - x0) * ty + (y - y0);
             const float2 u = sU[(x - ux0) * uw + (y - uy0)];
-            sN[k] = fma2(f2(sC1[k]), Lt, fma2(f2(sC2[k]), u, mul2(f2(sC3[k]), sPm[k])));
+            return fma2(f2(sC1[k]), Lt, fma2(f2(sC2[k]), u, mul2(f2(sC3[k]), sPm[k])));
         };
+        // p[t+1] at (x, y) out: to the exchange line, p[t] to p[t-1], p[t+1] into the tile of sU
+        auto emit = [&](int x, int y, float2 v) {
+            const int k = (x - x0) * ty + (y - y0), m = sMap[k];
+            if (m & 0xffff) v.x = v.x + sSrc[(m & 0xffff) - 1];
+            if (m >> 16) v.y = v.y + sSrc[(m >> 16) - 1];
+            float2* u = sU + (x - ux0) * uw + (y - uy0);
+            sPm[k] = *u;
+            *u = v;
+            st_line(out + (long long)x * pitch + y, v, (unsigned)(t + 1));
+        };
+        // OT4 with the sources in slots emits each point as it is updated (stage 2 reads only l);
+        // otherwise the new level waits in sN for the sources and the stencil's last reads of p[t]
+        const bool direct = OT4 && slots;
         if constexpr (OT4) {
             stencil_region<KIND, 4>(a, sU, ux0, uy0, uw, lx0, x1 + HL, ly0, y1 + HL, sFX, sFY, B,
-                                 [&](int x, int y, float2 g) {
-                                     const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
-                                     const float W = sW[(x - lx0) * lw + (y - ly0)];
-                                     sL[(x - lx0) * lw + (y - ly0)] = in ? mul2(f2(W), g) : f2(0.f);
-                                 });
+                                    [&](int x, int y, float2 g) {
+                                        const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
+                                        const float W = sW[(x - lx0) * lw + (y - ly0)];
+                                        sL[(x - lx0) * lw + (y - ly0)] = in ? mul2(f2(W), g) : f2(0.f);
+                                    });
             __syncthreads();
             stencil_region<KIND, 2>(a, sL, lx0, ly0, lw, x0, x1, y0, y1, sFX, sFY, B, [&](int x, int y, float2 g) {
                 const float Wk = sW[(x - lx0) * lw + (y - ly0)] * a.k12;
-                update(x, y, fma2(f2(Wk), g, sL[(x - lx0) * lw + (y - ly0)]));
+                const float2 v = update(x, y, fma2(f2(Wk), g, sL[(x - lx0) * lw + (y - ly0)]));
+                if (direct)
+                    emit(x, y, v);
+                else
+                    sN[(x - x0) * ty + (y - y0)] = v;
             });
         } else {
             stencil_region<KIND, 2>(a, sU, ux0, uy0, uw, x0, x1, y0, y1, sFX, sFY, B, [&](int x, int y, float2 g) {
-                update(x, y, mul2(f2(sW[(x - lx0) * lw + (y - ly0)]), g));
+                sN[(x - x0) * ty + (y - y0)] = update(x, y, mul2(f2(sW[(x - lx0) * lw + (y - ly0)]), g));
             });
         }
-        __syncthreads();
-        // 4. this step's sources at the tile's points
-        for (int k = P.cta_off[b] + tid; k < P.cta_off[b + 1]; k += NTH) {
-            const int tg = P.cta_tgt[k];
-            float v = 0.f;
-            const float* amp = P.src_amp + (long long)t * P.n_src;
-            for (int e = P.toff[tg]; e < P.toff[tg + 1]; e++) v += P.tcoef[e] * amp[P.tpoint[e]];
-            const long long i = P.tidx[tg] - (long long)pair * a.shot_stride * 2, c2 = i / 2;  // float in the pair
-            const int x = (int)(c2 / pitch), y = (int)(c2 % pitch);
-            float* s = reinterpret_cast<float*>(sN + (x - x0) * ty + (y - y0)) + (i & 1);
-            *s = *s + v;
-        }
-        __syncthreads();
-        // 5. p[t+1] to global memory and into the tile of sU; p[t] becomes p[t-1]
-        for (int e = tid; e < th * tw; e += NTH) {
-            const int xr = e / tw, yr = e % tw, k = xr * ty + yr;
-            const float2 v = sN[k];
-            float2* u = sU + (xr + HU) * uw + (yr + HU);
-            sPm[k] = *u;
-            *u = v;
-            st_line(out + (long long)(x0 + xr) * pitch + (y0 + yr), v, (unsigned)(t + 1));
+        if (!direct) {
+            __syncthreads();
+            if (!slots) {  // 4. sources beyond the slots, straight into sN
+                for (int j = tid; j < ns; j += NTH) {
+                    const long long i = P.tidx[P.cta_tgt[sb + j]] - pair_floats, c2 = i / 2;
+                    const int x = (int)(c2 / pitch), y = (int)(c2 % pitch);
+                    float* q = reinterpret_cast<float*>(sN + (x - x0) * ty + (y - y0)) + (i & 1);
+                    *q = *q + __ldcg(P.srcv + (long long)(sb + j) * P.nt + t);
+                }
+                __syncthreads();
+            }
+            // 5. p[t+1] out (the slots are empty here when there are none)
+            for (int e = tid; e < th * tw; e += NTH) {
+                const int x = x0 + e / tw, y = y0 + e % tw;
+                emit(x, y, sN[(x - x0) * ty + (y - y0)]);
+            }
         }
     }
     // the last step's receivers, rec[nt-2] = interp(p[nt-1]), with the halo of p[nt-1]
     if (P.nt < 3) return;
     if (!load_halo(P.nt - 1)) return;
-    gather_from_smem(P.nt - 2);
+    gather(P.nt - 2);
 }
 
 // Largest dynamic shared memory of a CTA of the kernel: the device's opt-in limit less the

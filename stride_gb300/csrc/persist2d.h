@@ -9,11 +9,18 @@ namespace sa {
 #define SA_PERSIST_THREADS 512
 #endif
 constexpr int PERSIST_THREADS = SA_PERSIST_THREADS;
+// shared-memory slots of a CTA's source values at a step: a CTA with more targets adds them to
+// the new level in a pass of its own
+constexpr int PERSIST_SRC_SLOTS = 64;
 // halo lines a thread has in flight at once
 #ifndef SA_PERSIST_BATCH
-#define SA_PERSIST_BATCH 8
+#define SA_PERSIST_BATCH 4
 #endif
 constexpr int PERSIST_BATCH = SA_PERSIST_BATCH;
+// memory semantics of the exchange lines' loads and stores
+#ifndef PERSIST_LINE_SEM
+#define PERSIST_LINE_SEM "relaxed.gpu"
+#endif
 // between polls of lines that do not hold their level yet
 #ifndef PERSIST_POLL_PAUSE
 #define PERSIST_POLL_PAUSE __nanosleep(20)
@@ -28,7 +35,8 @@ struct Persist2D {
     int tx, ty;                  // tile rows and columns of a CTA (ty even)
     int tiles_x, tiles_y;        // tiles of one shot pair; CTA b: pair b / (tiles_x tiles_y)
     // source injection by target point (Targets of the plan), each target applied by the CTA that
-    // owns its point: CTA b applies targets cta_tgt[cta_off[b] .. cta_off[b+1])
+    // owns its point: CTA b applies targets cta_tgt[cta_off[b] .. cta_off[b+1]). The owner first
+    // sums each target's entries for every step into srcv[(cta_off[b] + j) nt + t].
     const int* cta_off;
     const int* cta_tgt;
     const long long* tidx;
@@ -37,7 +45,12 @@ struct Persist2D {
     const int* tpoint;
     const float* src_amp;        // [nt][n_src]
     int n_src;
-    const Gather* gat;           // receivers, each gathered by the CTA holding its base corner
+    float* srcv;                 // [targets][nt]
+    // receivers, each gathered by the CTA holding its base corner: CTA b gathers
+    // gat[rec_idx[rec_off[b] .. rec_off[b+1])]
+    const int* rec_off;
+    const int* rec_idx;
+    const Gather* gat;
     int n_rec;
     float* rec_amp;              // [nt][n_rec]
     int* err;                    // set to 1 when a wait gives up (zero before the launch)

@@ -210,8 +210,10 @@ struct sa_plan {
     uint4* pxch = nullptr;  // its exchange lines
     size_t cap_pxch = 0;
     size_t cap_pbar = 0;
-    int *pcta_off = nullptr, *pcta_tgt = nullptr;
-    size_t cap_pcta_off = 0, cap_pcta_tgt = 0;
+    int *pcta_off = nullptr, *pcta_tgt = nullptr, *prec_off = nullptr, *prec_idx = nullptr;
+    size_t cap_pcta_off = 0, cap_pcta_tgt = 0, cap_prec_off = 0, cap_prec_idx = 0;
+    float* psrcv = nullptr;  // the sources' values at every step
+    size_t cap_psrcv = 0;
     // L2 residency of the duplicated medium: every shot pair's CTAs read each of its rows once per
     // pass, just after the previous pass streamed the wavefields through L2; the captured step
     // kernels carry this persisting window
@@ -1045,8 +1047,24 @@ int forward_persistent(sa_plan* p, cudaStream_t s) {
     for (int b = 0; b < p->pblocks; b++) cnt[b + 1] += cnt[b];
     std::vector<int> fill(cnt.begin(), cnt.end() - 1);
     for (int k = 0; k < p->stgt.n; k++) tgt[fill[owner[k]]++] = k;
+    // the receivers by owning CTA (tile and shot pair of the base corner), in receiver order
+    std::vector<int> rcnt(p->pblocks + 1, 0), ridx(p->n_rec), rown(p->n_rec);
+    for (int sh = 0; sh < p->n_shots; sh++)
+        for (int r = p->rec_off[sh]; r < p->rec_off[sh + 1]; r++) {
+            rown[r] = (sh / 2) * ntile + (p->rec_bx[r] / p->ptx) * p->ptiles_y + p->rec_by[r] / p->pty;
+            rcnt[rown[r] + 1]++;
+        }
+    for (int b = 0; b < p->pblocks; b++) rcnt[b + 1] += rcnt[b];
+    std::vector<int> rfill(rcnt.begin(), rcnt.end() - 1);
+    for (int r = 0; r < p->n_rec; r++) ridx[rfill[rown[r]]++] = r;
     CKR(ensure(&p->pcta_off, &p->cap_pcta_off, cnt.size()));
     CKR(ensure(&p->pcta_tgt, &p->cap_pcta_tgt, std::max<size_t>(1, tgt.size())));
+    CKR(ensure(&p->prec_off, &p->cap_prec_off, rcnt.size()));
+    CKR(ensure(&p->prec_idx, &p->cap_prec_idx, std::max<size_t>(1, ridx.size())));
+    CKR(ensure(&p->psrcv, &p->cap_psrcv, std::max<size_t>(1, (size_t)p->stgt.n * p->d.nt)));
+    CK(cudaMemcpyAsync(p->prec_off, rcnt.data(), rcnt.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (!ridx.empty())
+        CK(cudaMemcpyAsync(p->prec_idx, ridx.data(), ridx.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     const size_t slot = (size_t)npairs(p) * p->shot_stride;
     CKR(ensure(&p->pbar, &p->cap_pbar, 1));
     CKR(ensure(&p->pxch, &p->cap_pxch, 2 * slot));
@@ -1072,6 +1090,9 @@ int forward_persistent(sa_plan* p, cudaStream_t s) {
     a.tpoint = p->stgt.point;
     a.src_amp = p->src_amp;
     a.n_src = p->n_src;
+    a.srcv = p->psrcv;
+    a.rec_off = p->prec_off;
+    a.rec_idx = p->prec_idx;
     a.gat = p->gat_flat;
     a.n_rec = p->n_rec;
     a.rec_amp = p->rec_amp;
@@ -1290,7 +1311,7 @@ int sa_plan_destroy(sa_plan* p) {
                     p->gat_flat,
                     p->src_amp, p->rec_amp, p->stage, p->snaps, p->gradb, p->precb, p->ckpt, p->segsnaps,
                     p->afield[0], p->afield[1], p->EA, p->EB, p->EC, p->EG4, p->ES, p->levels, p->Lu, p->Lz,
-                    p->smed, p->lbuf, p->pbar, p->pxch, p->pcta_off, p->pcta_tgt, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
+                    p->smed, p->lbuf, p->pbar, p->pxch, p->prec_off, p->prec_idx, p->psrcv, p->pcta_off, p->pcta_tgt, p->src_flat, p->gat_src, p->hold_vp, p->hold_rho, p->gradrb, p->precrb,
                     p->dbx, p->dby, p->pml_prof, p->pml_aux, p->pml_ck, p->pml_aux_f, p->ckpt2, p->pml_ck2,
                     p->wgrad, p->hgat, p->hgat_src, p->rtgt.idx, p->rtgt.off, p->rtgt.point, p->rtgt.coef, p->stgt.idx,
                     p->stgt.off, p->stgt.point, p->stgt.coef, p->xtgt.idx, p->xtgt.off, p->xtgt.point, p->xtgt.coef};

@@ -32,6 +32,24 @@ def test_persistent_equals_streaming(kernel, density, alpha):
     assert np.array_equal(persistent, streaming)
 
 
+@pytest.mark.parametrize('kernel', ['OT2', 'OT4'])
+def test_persistent_crowded_tiles_equal_streaming(kernel):
+    """Sources and receivers crowded into a few tiles: a CTA with more source targets than its
+    shared-memory slots adds them in a pass of its own, and one with more receivers than threads
+    gathers the rest from global memory."""
+    c = C.small_case(kernel=kernel, density='variable', alpha=True, n_shots=2, nt=160)
+    rng = np.random.default_rng(5)
+    h = c['spacing'][0]
+    centre = np.array([20 * h, 24 * h])
+    c['srcs'] = [centre + rng.uniform(0, 6 * h, (48, 2)) for _ in range(2)]  # 4 targets each, ~190 per pair
+    c['recs'] = [centre + rng.uniform(0, 10 * h, (600, 2)) for _ in range(2)]
+    plan = C.make_plan(c)
+    streaming = _forward(c, plan, -1)
+    persistent = _forward(c, plan, 1)
+    assert np.abs(streaming).max() > 0
+    assert np.array_equal(persistent, streaming)
+
+
 def test_persistent_single_shot_workload_matches_oracle():
     """The single-shot workload (256^2 inner at 0.5 mm, 2000 steps, 128 receivers) runs the
     persistent forward by default."""
