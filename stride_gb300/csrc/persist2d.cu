@@ -160,9 +160,10 @@ struct PersistCfg {
     static constexpr int R = KIND != 0 ? 9 : 5;
     static constexpr int HU = OT4 ? 2 * R : R;  // p[t] halo
     static constexpr int HL = OT4 ? R : 0;      // stage-1 region beyond the tile
-    // shared memory: float2 arrays of p[t] over the tile and halo, l (OT4), the flux rows of the
-    // larger stage (staggered), p[t-1] and p[t+1] over the tile; float tables of the medium: W
-    // over the stage-1 region, C1, C2, -C3 over the tile, bx and by over the stage-1 flux regions;
+    // shared memory: float4 coefficients of the tile's points {C1, C2, -C3, W k12 (OT4) or W};
+    // float2 arrays of p[t] over the tile and halo, l (OT4), the flux rows of the larger stage
+    // (staggered), p[t-1] and p[t+1] over the tile; float tables of the medium: W over the
+    // stage-1 region, bx and by over the stage-1 flux regions;
     // int arrays: the source slots of the tile's points and the CTA's halo points; the float values
     // of the CTA's sources at the step
     static constexpr int PADR = PERSIST_NR_MAX - 1;  // rows of padding of the arrays stencil_region reads
@@ -188,11 +189,10 @@ struct PersistCfg {
         return (size_t)2 * HU * (tx + ty) + (size_t)4 * HU * HU;
     }
     __host__ __device__ static constexpr size_t floats1(int tx, int ty) {
-        return nW(tx, ty) + 3 * nT(tx, ty) + (KIND == 1 ? nF(tx, ty) + nG(tx, ty) : 0) + nT(tx, ty) + nH(tx, ty) +
-               PERSIST_SRC_SLOTS;
+        return nW(tx, ty) + (KIND == 1 ? nF(tx, ty) + nG(tx, ty) : 0) + nT(tx, ty) + nH(tx, ty) + PERSIST_SRC_SLOTS;
     }
     __host__ __device__ static constexpr size_t bytes(int tx, int ty) {
-        return floats2(tx, ty) * sizeof(float2) + floats1(tx, ty) * sizeof(float);
+        return nT(tx, ty) * sizeof(float4) + floats2(tx, ty) * sizeof(float2) + floats1(tx, ty) * sizeof(float);
     }
 };
 
@@ -203,18 +203,16 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
     constexpr int HU = CF::HU, HL = CF::HL;
     const Step2D& a = P.s;
     const int tx = P.tx, ty = P.ty;
-    extern __shared__ __align__(16) float2 psm[];
-    float2* const sU = psm;                  // p[t], tile and halo
+    extern __shared__ __align__(16) float4 psm[];
+    float4* const sC = psm;                                     // coefficients of the tile's points
+    float2* const sU = reinterpret_cast<float2*>(sC + CF::nT(tx, ty));  // p[t], tile and halo
     float2* const sL = sU + CF::nU(tx, ty);  // l (OT4)
     float2* const sFX = sL + CF::nL(tx, ty);
     float2* const sFY = sFX + CF::nF(tx, ty);
     float2* const sPm = sFY + CF::nG(tx, ty);  // p[t-1] over the tile
     float2* const sN = sPm + CF::nT(tx, ty);   // p[t+1] over the tile (OT2, or a CTA with more sources than slots)
     float* const sW = reinterpret_cast<float*>(sN + CF::nT(tx, ty));
-    float* const sC1 = sW + CF::nW(tx, ty);
-    float* const sC2 = sC1 + CF::nT(tx, ty);
-    float* const sC3 = sC2 + CF::nT(tx, ty);
-    float* const sBX = sC3 + CF::nT(tx, ty);
+    float* const sBX = sW + CF::nW(tx, ty);
     float* const sBY = sBX + (VARB ? CF::nF(tx, ty) : 0);
     int* const sMap = reinterpret_cast<int*>(sBY + (VARB ? CF::nG(tx, ty) : 0));  // source slots + 1, lane 0 | lane 1 << 16
     int* const sHal = sMap + CF::nT(tx, ty);  // halo points: row | column << 8 relative to (ux0, uy0)
@@ -244,9 +242,8 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
         const int x = x0 + e / tw, y = y0 + e % tw;
         const long long q = (long long)x * mp + y;
         const int k = (x - x0) * ty + (y - y0);
-        sC1[k] = __ldg(a.C1m + q);
-        sC2[k] = __ldg(a.C2m + q);
-        sC3[k] = __ldg(a.NC3m + q);
+        const float W = __ldg(a.Wm + q);
+        sC[k] = make_float4(__ldg(a.C1m + q), __ldg(a.C2m + q), __ldg(a.NC3m + q), OT4 ? W * a.k12 : W);
         sPm[k] = f2(0.f);
         sMap[k] = 0;
     }
@@ -361,16 +358,18 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
             for (int j = tid + NTH; j < ns; j += NTH) sSrc[j] = __ldcg(P.srcv + (long long)(sb + j) * P.nt + t);
         }
         // 2-3. the update of the tile: p[t+1] = C1 Lt + C2 p[t] - C3 p[t-1], plus the step's sources
-        auto update = [&](int x, int y, float2 Lt) -> float2 {
-            const int k = (x - x0) * ty + (y - y0);
+        auto update = [&](int k, const float4& c, int x, int y, float2 Lt) -> float2 {
             const float2 u = sU[(x - ux0) * uw + (y - uy0)];
-            return fma2(f2(sC1[k]), Lt, fma2(f2(sC2[k]), u, mul2(f2(sC3[k]), sPm[k])));
+            return fma2(f2(c.x), Lt, fma2(f2(c.y), u, mul2(f2(c.z), sPm[k])));
         };
         // p[t+1] at (x, y) out: to the exchange line, p[t] to p[t-1], p[t+1] into the tile of sU
         auto emit = [&](int x, int y, float2 v) {
-            const int k = (x - x0) * ty + (y - y0), m = sMap[k];
-            if (m & 0xffff) v.x = v.x + sSrc[(m & 0xffff) - 1];
-            if (m >> 16) v.y = v.y + sSrc[(m >> 16) - 1];
+            const int k = (x - x0) * ty + (y - y0);
+            if (ns) {
+                const int m = sMap[k];
+                if (m & 0xffff) v.x = v.x + sSrc[(m & 0xffff) - 1];
+                if (m >> 16) v.y = v.y + sSrc[(m >> 16) - 1];
+            }
             float2* u = sU + (x - ux0) * uw + (y - uy0);
             sPm[k] = *u;
             *u = v;
@@ -388,8 +387,9 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
                                     });
             __syncthreads();
             stencil_region<KIND, 2>(a, sL, lx0, ly0, lw, x0, x1, y0, y1, sFX, sFY, B, [&](int x, int y, float2 g) {
-                const float Wk = sW[(x - lx0) * lw + (y - ly0)] * a.k12;
-                const float2 v = update(x, y, fma2(f2(Wk), g, sL[(x - lx0) * lw + (y - ly0)]));
+                const int k = (x - x0) * ty + (y - y0);
+                const float4 c = sC[k];
+                const float2 v = update(k, c, x, y, fma2(f2(c.w), g, sL[(x - lx0) * lw + (y - ly0)]));
                 if (direct)
                     emit(x, y, v);
                 else
@@ -397,7 +397,9 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
             });
         } else {
             stencil_region<KIND, 2>(a, sU, ux0, uy0, uw, x0, x1, y0, y1, sFX, sFY, B, [&](int x, int y, float2 g) {
-                sN[(x - x0) * ty + (y - y0)] = update(x, y, mul2(f2(sW[(x - lx0) * lw + (y - ly0)]), g));
+                const int k = (x - x0) * ty + (y - y0);
+                const float4 c = sC[k];
+                sN[k] = update(k, c, x, y, mul2(f2(c.w), g));
             });
         }
         if (!direct) {

@@ -6,7 +6,7 @@
 namespace sa {
 
 #ifndef SA_PERSIST_THREADS
-#define SA_PERSIST_THREADS 512
+#define SA_PERSIST_THREADS 384
 #endif
 constexpr int PERSIST_THREADS = SA_PERSIST_THREADS;
 // shared-memory slots of a CTA's source values at a step: a CTA with more targets adds them to
