@@ -44,6 +44,9 @@ extern "C" {
 #define SA_INTERP_LINEAR 0    /* bilinear / trilinear SparseTimeFunction (common/devito.py:580-653) */
 #define SA_INTERP_HICKS 1     /* Kaiser-windowed sinc, 8 points per axis (common/devito.py:640-648,843-885);
                                  sources smoothed as the reference's src, receivers not */
+#define SA_INTERP_SINC 2      /* Devito's SparseTimeFunction(interpolation='sinc', r=7) (common/devito.py:
+                                 634-638): Kaiser-windowed sinc of half-width 7, 14 points per axis, no
+                                 smoothing */
 
 #define SA_BOUNDARY_SPONGE 0  /* SpongeBoundary2 (boundaries/devito.py:37-69), the reference's default */
 #define SA_BOUNDARY_CFS_PML 1 /* ComplexFrequencyShiftPML2 (boundaries/devito.py:72-191): auxiliary fields on
@@ -83,7 +86,7 @@ typedef struct sa_desc {
     int max_shots;         /* shots advanced together per launch */
     int checkpoint_interval;   /* steps between checkpoints for SA_SAVE_CHECKPOINTS (0: 50) */
     double checkpoint_budget;  /* bytes the checkpoints may use (0: no limit); widens the interval */
-    int interpolation;         /* SA_INTERP_LINEAR or SA_INTERP_HICKS: sparse-point interpolation */
+    int interpolation;         /* SA_INTERP_LINEAR, SA_INTERP_HICKS or SA_INTERP_SINC: sparse-point interpolation */
     int boundary;              /* SA_BOUNDARY_SPONGE or SA_BOUNDARY_CFS_PML */
     double f_centre;           /* Hz, centre of the propagated band (IsoAcousticDevito._bandwidth[1]): the
                                   CFS-PML's alpha = 0.01 pi f_centre; unused by the sponge */

@@ -238,10 +238,45 @@ def hicks_stencil(coords, origin, spacing, smooth=False):
     return base, w, offs
 
 
+# Kaiser window parameter b by half-width r (Hicks 2002, "Arbitrary source and receiver positioning
+# in finite-difference schemes using Kaiser windowed sinc functions", Geophysics 67(1), table 1).
+SINC_B = {1: 1.24, 2: 2.94, 3: 4.53, 4: 4.14, 5: 5.26, 6: 6.40, 7: 7.51, 8: 8.56, 9: 9.56, 10: 10.64}
+
+
+def sinc_stencil(coords, origin, spacing, r=7):
+    """Kaiser-windowed sinc of half-width r, the interpolation of Devito's
+    SparseTimeFunction(interpolation='sinc', r=7) that stride/physics/common/devito.py:634-638
+    builds: grid points floor(x) - r + 1 .. floor(x) + r along each axis, weight
+    sinc(d) I0(b sqrt(1 - (d/r)^2)) / I0(b) at the distance d = point - x, product over axes.
+    Devito is not installed here: this restates the published method, it is not checked
+    against Devito's own weights. Returns (base [n, dim], weights [n, (2r)**dim],
+    offsets [(2r)**dim, dim])."""
+    import itertools
+    import scipy.special
+    coords = np.asarray(coords, dtype=np.float32).astype(np.float64)
+    grid = (coords - np.asarray(origin, np.float64)) / np.asarray(spacing, np.float64)
+    base = np.floor(grid).astype(np.int64)
+    frac = grid - base
+    n, dim = coords.shape
+    b = SINC_B[r]
+    rel = np.arange(-r + 1, r + 1)
+    d = rel[None, None, :] - frac[:, :, None]                       # [n, dim, 2r]
+    coef = np.sinc(d) * scipy.special.iv(0, b * np.sqrt(np.clip(1 - (d / r) ** 2, 0, None))) / scipy.special.iv(0, b)
+    offs = np.array(list(itertools.product(rel, repeat=dim)), dtype=np.int64)
+    w = np.ones((n, len(offs)))
+    for k, off in enumerate(offs):
+        for a in range(dim):
+            w[:, k] *= coef[:, a, off[a] + r - 1]
+    return base, w, offs
+
+
 def sparse_stencil(interpolation, coords, origin, spacing, smooth):
-    """(base, weights, offsets) of a SparseTimeFunction with the given interpolation."""
+    """(base, weights, offsets) of a SparseTimeFunction with the given interpolation (the Hicks
+    sources smoothed when ``smooth``; sinc has no smoothing)."""
     if interpolation == 'hicks':
         return hicks_stencil(coords, origin, spacing, smooth)
+    if interpolation == 'sinc':
+        return sinc_stencil(coords, origin, spacing)
     base, w = linear_stencil(coords, origin, spacing)
     return base, w, _corner_offsets(base.shape[1])
 
@@ -707,7 +742,7 @@ def adjoint_exact(vp, spacing, dt, nt, absorbing, src_coords, rec_coords, wavele
     (dW/dvp = 2 W / vp), the OT4 term's inner W (dt^2/12 dW (G u)(G z)) and the source
     injection's vp factor. This is the ``exact`` gradient mode (no counterpart in the
     reference, whose imaging condition is iso_acoustic/devito.py:985-1043). ``interpolation``:
-    'linear' or 'hicks' (sources smoothed, receivers not) for both the forward and its transpose."""
+    'linear', 'hicks' (sources smoothed, receivers not) or 'sinc' for both the forward and its transpose."""
     dim = vp.ndim
     shape = vp.shape
     h = max(spacing)

@@ -36,6 +36,7 @@ SA_BOUNDARY_SPONGE = 0
 SA_BOUNDARY_CFS_PML = 1
 SA_INTERP_LINEAR = 0
 SA_INTERP_HICKS = 1
+SA_INTERP_SINC = 2
 SA_GRAD_EXACT = 1
 
 # every symbol include/strideacc.h declares
@@ -212,7 +213,7 @@ class Plan:
         d.max_shots = int(max_shots)
         d.checkpoint_interval = int(checkpoint_interval)
         d.checkpoint_budget = float(checkpoint_budget)
-        d.interpolation = {'linear': SA_INTERP_LINEAR, 'hicks': SA_INTERP_HICKS}[interpolation]
+        d.interpolation = {'linear': SA_INTERP_LINEAR, 'hicks': SA_INTERP_HICKS, 'sinc': SA_INTERP_SINC}[interpolation]
         d.boundary = {'sponge': SA_BOUNDARY_SPONGE, 'pml': SA_BOUNDARY_CFS_PML}[boundary]
         d.f_centre = float(f_centre)
         self.desc = d

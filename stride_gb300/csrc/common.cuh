@@ -40,10 +40,14 @@ __host__ __device__ constexpr float kW1(int k) {
 
 constexpr int GUARD = 40;  // zero rows above and below every pitched medium array (>= 3R + RB + 5)
 
-// A receiver with Hicks interpolation: 8 x 8 support from (row, col), weights wx[i] * wy[j].
-struct HicksGather {
-    int row, col, point, shot;
-    float wx[8], wy[8];
+// Points per axis of the widest sparse-point support (sinc of half-width 7).
+constexpr int SUPPORT_MAX = 14;
+
+// A point with a wide support (Hicks or sinc interpolation): width x width points from (row, col),
+// weights wx[i] * wy[j].
+struct SupportGather {
+    int row, col, point, shot, width;
+    float wx[SUPPORT_MAX], wy[SUPPORT_MAX];
 };
 
 // One point of a gather: rec[t][point] = sum of the four bilinear corner terms; `pad` is the

@@ -86,7 +86,7 @@ __global__ void k_exact_grad2d(const float2* __restrict__ z, const float2* __res
     }
 }
 
-// Source term at each support point of each source (linear corners or the smoothed Hicks
+// Source term at each support point of each source (linear corners or the wide Hicks / sinc
 // support): z w src[trow] (2 dt / h) ES.
 __global__ void k_exact_src2d(const float* __restrict__ z, const ExactSrc2D* __restrict__ e, int n,
                               const float* __restrict__ amp, int ld, int trow, float scale,

@@ -304,17 +304,17 @@ struct Sparse3D {
     const float* coef;        // [n][8] injection coefficients (weight * scale * vp^k at the corner)
 };
 
-// Hicks interpolation in 3D (common/devito.py:640-648,843-885): injection as a flat list of
-// weighted support points (up to 8 x 8 x 8 per source), receivers gathered over the support.
+// Wide interpolation in 3D (Hicks, common/devito.py:640-648,843-885; sinc, :634-638): injection as a
+// flat list of weighted support points (up to 14^3 per source), receivers gathered over the support.
 struct Entries3D {
     const int* shot;          // [n] shot of each entry
     const int* point;         // [n] its sparse point (row of the amplitude table)
     const long long* idx;     // [n] grid offset within a shot's field
     const float* coef;        // [n] weight * scale * vp^k at the support point
 };
-struct HicksGather3D {
-    int x, y, z, point, shot;  // support origin (base - 3 per axis)
-    float wx[8], wy[8], wz[8];
+struct SupportGather3D {
+    int x, y, z, point, shot, width;  // support origin (base - lo per axis) and points per axis
+    float wx[SUPPORT_MAX], wy[SUPPORT_MAX], wz[SUPPORT_MAX];
 };
 
 __global__ void inject3d(const Sparse3D s, int n, const float* amp, int ld, int t, float* field, long long shot_stride,

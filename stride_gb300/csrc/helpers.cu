@@ -32,6 +32,32 @@ void hicks_coefs(double frac, bool smooth, double c[8]) {
     }
 }
 
+// Kaiser-windowed sinc of half-width r (Hicks 2002, "Arbitrary source and receiver positioning in
+// finite-difference schemes using Kaiser windowed sinc functions"), the interpolation of Devito's
+// SparseTimeFunction(interpolation='sinc', r) that stride/physics/common/devito.py:634-638 builds with
+// r = 7: weights at grid offsets -r+1 .. r from the base point (index i: offset i - r + 1),
+// w(x) = sinc(x) I0(b sqrt(1 - (x/r)^2)) / I0(b) at x = offset - frac, with b from the paper's table
+// of window parameters by half-width.
+void sinc_coefs(double frac, int r, double* c) {
+    static const double b_of_r[11] = {0.0, 1.24, 2.94, 4.53, 4.14, 5.26, 6.40, 7.51, 8.56, 9.56, 10.64};
+    const double b = b_of_r[r], den = std::cyl_bessel_i(0.0, b);
+    for (int i = 0; i < 2 * r; i++) {
+        const double x = (double)(i - r + 1) - frac, q = x / r;
+        const double sinc = x == 0.0 ? 1.0 : std::sin(M_PI * x) / (M_PI * x);
+        c[i] = q * q >= 1.0 ? 0.0 : sinc * std::cyl_bessel_i(0.0, b * std::sqrt(1.0 - q * q)) / den;
+    }
+}
+
+int support_coefs(int interp, double frac, bool smooth, double c[SUPPORT_MAX]) {
+    for (int i = 0; i < SUPPORT_MAX; i++) c[i] = 0.0;
+    if (interp == SA_INTERP_SINC) {
+        sinc_coefs(frac, 7, c);
+        return 14;
+    }
+    hicks_coefs(frac, smooth, c);
+    return 8;
+}
+
 // CFS-PML profiles per axis (ComplexFrequencyShiftPML2.apply, stride/physics/boundaries/devito.py:
 // 96-127, with Boundary.damping, boundaries/boundary.py:59-170), FP32 as the reference stores them:
 // sigma 'power' degree 3 with the coefficient 2 ln(1/R) / (absorbing h) (0.67 / h for layers of 15
@@ -215,27 +241,27 @@ __global__ void gather_final2d(const float* __restrict__ field, long long shot_s
     if (e < n) gather_point(field, shot_stride, pitch, g, e, out, ld, trow);
 }
 
-// rec[trow][point] = sum over the 8 x 8 Hicks support of wx[i] wy[j] field(row + i, col + j).
-__global__ void k_hicks_gather2d(const float* __restrict__ field, long long shot_stride, int pitch,
-                                 const HicksGather* __restrict__ g, int n, float* out, int ld, int trow) {
+// rec[trow][point] = sum over the width x width support of wx[i] wy[j] field(row + i, col + j).
+__global__ void k_support_gather2d(const float* __restrict__ field, long long shot_stride, int pitch,
+                                   const SupportGather* __restrict__ g, int n, float* out, int ld, int trow) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
-    const HicksGather G = g[e];
+    const SupportGather& G = g[e];
     const float* f = field + (long long)(G.shot / 2) * shot_stride * 2 + (G.shot & 1);
     float v = 0.f;
-    for (int i = 0; i < 8; i++) {
+    for (int i = 0; i < G.width; i++) {
         const float* row = f + 2 * (long long)(G.row + i) * pitch;
         float r = 0.f;
-        for (int j = 0; j < 8; j++) r += G.wy[j] * row[2 * (G.col + j)];
+        for (int j = 0; j < G.width; j++) r += G.wy[j] * row[2 * (G.col + j)];
         v += G.wx[i] * r;
     }
     out[(long long)trow * ld + G.point] = v;
 }
 
-cudaError_t hicks_gather2d(const float* field, long long shot_stride, int pitch, const HicksGather* g, int n, float* out,
-                           int ld, int trow, cudaStream_t s) {
+cudaError_t support_gather2d(const float* field, long long shot_stride, int pitch, const SupportGather* g, int n,
+                             float* out, int ld, int trow, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_hicks_gather2d<<<(n + 127) / 128, 128, 0, s>>>(field, shot_stride, pitch, g, n, out, ld, trow);
+    k_support_gather2d<<<(n + 127) / 128, 128, 0, s>>>(field, shot_stride, pitch, g, n, out, ld, trow);
     return cudaGetLastError();
 }
 

@@ -89,6 +89,11 @@ cudaError_t exact_src2d(const float* z, const ExactSrc2D* e, int n, const float*
 // 3D plans
 // Hicks coefficients of one axis at the fractional offset frac (index 3 + grid offset, -3..4).
 void hicks_coefs(double frac, bool smooth, double c[8]);
+// Coefficients of one axis of a wide support (SA_INTERP_HICKS or SA_INTERP_SINC) at the fractional
+// offset frac: returns the points per axis; c[i] weighs grid offset i - support_lo(interp).
+int support_coefs(int interp, double frac, bool smooth, double c[SUPPORT_MAX]);
+inline int support_lo(int interp) { return interp == SA_INTERP_SINC ? 6 : 3; }
+inline int support_width(int interp) { return interp == SA_INTERP_SINC ? 14 : 8; }
 // CFS-PML profile tables (sigma, alpha, sigma', alpha' per axis) of a plan description.
 std::vector<float> pml_profile_tables(const sa_desc& d, float vmax);
 
@@ -98,21 +103,21 @@ struct Sponge3 {
 };
 struct Sparse3D;
 struct Entries3D;
-struct HicksGather3D;
+struct SupportGather3D;
 // CFS-PML auxiliary update and boundary term after a 3D OT2 step.
 cudaError_t pml3d(const float* cur, float* nxt, float* aux, const float* prof, const float* C1, const float* vp,
                   int nx, int ny, int nz, int zp, int nshots, long long field, const int* a, const double* h, float dt,
                   int adjoint, float* snap, long long snap_shot_stride, float inv_dt2, cudaStream_t s);
-// Hicks forms of the 3D exact gradient's receiver coefficients and source term.
+// Wide-support (Hicks, sinc) forms of the 3D exact gradient's receiver coefficients and source term.
 cudaError_t xcoef_entries3d(const long long* idx, const float* w, int n, const float* C1, const float* W, float* out,
                             cudaStream_t s);
 cudaError_t exact_src_entries3d(const float* z, const Entries3D& e, const float* w, int n, const float* amp, int ld,
                                 int trow, float scale, const float* ES, long long field, float* gradb, cudaStream_t s);
-// Hicks injection (flat support entries) and gather (8^3 support) of 3D plans.
+// Wide-support injection (flat support entries) and gather (width^3 support) of 3D plans.
 cudaError_t inject_entries3d(const Entries3D& e, int n, const float* amp, int ld, int t, float* field,
                              long long shot_stride, float* snap, long long snap_shot_stride, long long snap_off,
                              float inv_dt2, cudaStream_t s);
-cudaError_t hicks_gather3d(const HicksGather3D* g, int n, const float* field, long long shot_stride, int ny, int zp,
+cudaError_t support_gather3d(const SupportGather3D* g, int n, const float* field, long long shot_stride, int ny, int zp,
                            float* out, int ld, int trow, float scale, cudaStream_t s);
 cudaError_t medium3d(const float* vp_in, const float* rho_in, const float* alpha_in, int nx, int ny, int nz, int zp,
                      int zpb, int density, double db_to_np, const Sponge3& sp, float dt, float* W, float* vp,
@@ -173,7 +178,7 @@ cudaError_t image_raw2d(const float* q, const float* snap, long long snap_stride
 cudaError_t pml2d(const float* cur, float* nxt, float* aux, const float* prof, const float* C1, const float* vp, int nx,
                   int ny, int pitch, long long shot_stride, int npairs, int ax, int ay, float hx, float hy, float dt,
                   int adjoint, float* snap, long long snap_shot_stride, float inv_dt2, cudaStream_t s);
-cudaError_t hicks_gather2d(const float* field, long long shot_stride, int pitch, const HicksGather* g, int n, float* out,
+cudaError_t support_gather2d(const float* field, long long shot_stride, int pitch, const SupportGather* g, int n, float* out,
                            int ld, int trow, cudaStream_t s);
 cudaError_t final_gather2d(const float* field, long long shot_stride, int pitch, const Gather* g, int n, float* out,
                            int ld, int trow, cudaStream_t s);

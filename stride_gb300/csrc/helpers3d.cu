@@ -426,7 +426,7 @@ cudaError_t xcoef3d(const Sparse3D& sp, int n, const float* C1, const float* W, 
     return cudaGetLastError();
 }
 
-// Hicks injection: field[shot][idx[e]] += coef[e] amp[t][point[e]] (and its snapshot / dt^2).
+// Wide-support (Hicks, sinc) injection: field[shot][idx[e]] += coef[e] amp[t][point[e]] (and its snapshot / dt^2).
 __global__ void k_inject_entries3d(const Entries3D e, int n, const float* __restrict__ amp, int ld, int t, float* field,
                                    long long shot_stride, float* snap, long long snap_shot_stride, long long snap_off,
                                    float inv_dt2) {
@@ -438,20 +438,20 @@ __global__ void k_inject_entries3d(const Entries3D e, int n, const float* __rest
     if (snap) atomicAdd(snap + (long long)sh * snap_shot_stride + snap_off + e.idx[k], v * inv_dt2);
 }
 
-// Hicks gather: out[trow][point] = scale * sum over the 8^3 support of wx wy wz field.
-__global__ void k_hicks_gather3d(const HicksGather3D* __restrict__ g, int n, const float* __restrict__ field,
-                                 long long shot_stride, int ny, int zp, float* out, int ld, int trow, float scale) {
+// Wide-support gather: out[trow][point] = scale * sum over the width^3 support of wx wy wz field.
+__global__ void k_support_gather3d(const SupportGather3D* __restrict__ g, int n, const float* __restrict__ field,
+                                   long long shot_stride, int ny, int zp, float* out, int ld, int trow, float scale) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const HicksGather3D G = g[k];
+    const SupportGather3D& G = g[k];
     const float* f = field + (long long)G.shot * shot_stride;
     float v = 0.f;
-    for (int a = 0; a < 8; a++) {
+    for (int a = 0; a < G.width; a++) {
         float va = 0.f;
-        for (int b = 0; b < 8; b++) {
+        for (int b = 0; b < G.width; b++) {
             const float* row = f + ((long long)(G.x + a) * ny + (G.y + b)) * zp + G.z;
             float vb = 0.f;
-            for (int c = 0; c < 8; c++) vb += G.wz[c] * row[c];
+            for (int c = 0; c < G.width; c++) vb += G.wz[c] * row[c];
             va += G.wy[b] * vb;
         }
         v += G.wx[a] * va;
@@ -468,10 +468,10 @@ cudaError_t inject_entries3d(const Entries3D& e, int n, const float* amp, int ld
     return cudaGetLastError();
 }
 
-cudaError_t hicks_gather3d(const HicksGather3D* g, int n, const float* field, long long shot_stride, int ny, int zp,
+cudaError_t support_gather3d(const SupportGather3D* g, int n, const float* field, long long shot_stride, int ny, int zp,
                            float* out, int ld, int trow, float scale, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_hicks_gather3d<<<(n + 127) / 128, 128, 0, s>>>(g, n, field, shot_stride, ny, zp, out, ld, trow, scale);
+    k_support_gather3d<<<(n + 127) / 128, 128, 0, s>>>(g, n, field, shot_stride, ny, zp, out, ld, trow, scale);
     return cudaGetLastError();
 }
 
@@ -551,7 +551,7 @@ cudaError_t pml3d(const float* cur, float* nxt, float* aux, const float* prof, c
     return cudaGetLastError();
 }
 
-// Hicks forms of the 3D exact gradient's point terms: receiver coefficients w C1 W at each
+// Wide-support (Hicks, sinc) forms of the 3D exact gradient's point terms: receiver coefficients w C1 W at each
 // support entry, and the source term z w src[trow] scale ES at each source support entry.
 __global__ void k_xcoef_entries3d(const long long* __restrict__ idx, const float* __restrict__ w, int n,
                                   const float* __restrict__ C1, const float* __restrict__ W, float* out) {

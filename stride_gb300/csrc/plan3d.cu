@@ -170,16 +170,16 @@ struct Plan3D {
     float *Lu = nullptr, *Lz = nullptr, *ones = nullptr, *zeros = nullptr, *r_xcoef = nullptr;
     size_t cap_levels = 0;
     bool exact_valid = false;
-    // Hicks interpolation: injection entries of the sources [0] and receivers [1], receiver gathers
-    bool hicks = false;
+    // wide interpolation (Hicks or sinc): injection entries of the sources [0] and receivers [1], receiver gathers
+    bool wide = false;  // a wide sparse-point support (Hicks or sinc)
     int *e_shot[2] = {}, *e_point[2] = {};
     long long* e_idx[2] = {};
     float* e_coef[2] = {};
     float* e_w[2] = {};  // raw support weights (the exact gradient's point terms)
     float* e_xcoef = nullptr;  // receivers' w C1 W (exact gradient)
     int n_ent[2] = {0, 0};
-    HicksGather3D* hgat = nullptr;
-    HicksGather3D* hgat_src = nullptr;  // sources (smoothed): the wavelet gradient's gathers
+    SupportGather3D* hgat = nullptr;
+    SupportGather3D* hgat_src = nullptr;  // sources (Hicks: smoothed): the wavelet gradient's gathers
     // CFS-PML (SA_BOUNDARY_CFS_PML, OT2): profiles per axis and nine auxiliary fields per shot
     bool pml = false;
     float *pml_prof = nullptr, *pml_aux = nullptr;
@@ -204,7 +204,7 @@ int plan3d_create(const sa_desc& d, Plan3D** out) {
     p->zpb = (p->nz + 12 + 31) / 32 * 32;
     p->kind = d.density == SA_DENSITY_NONE ? 0 : (d.density == SA_DENSITY_VARIABLE ? 1 : 2);
     p->ot4 = d.kernel == SA_KERNEL_OT4;
-    p->hicks = d.interpolation == SA_INTERP_HICKS;
+    p->wide = d.interpolation != SA_INTERP_LINEAR;
     p->pml = d.boundary == SA_BOUNDARY_CFS_PML;
     p->plane = (long long)p->ny * p->zp;
     p->field = (long long)p->nx * p->plane;
@@ -352,33 +352,35 @@ static int build_points(Plan3D* p, int n_shots, const int* off, const float* xyz
     return SA_OK;
 }
 
-// Hicks support of every point (8 per axis from base - 3, within the grid): injection entries
-// (weight * scale * vp^k at the support point; sources smoothed as the reference's src) and the
-// gathers of the 8^3 support (receivers: the traces; sources: the wavelet gradient).
-static int build_hicks(Plan3D* p, int n_shots, const int* off, const float* xyz, bool smooth, double scale,
+// Wide support of every point (Hicks: 8 per axis from base - 3; sinc: 14 from base - 6; within the
+// grid): injection entries (weight * scale * vp^k at the support point; Hicks sources smoothed as the
+// reference's src) and the gathers of the width^3 support (receivers: the traces; sources: the
+// wavelet gradient).
+static int build_support(Plan3D* p, int n_shots, const int* off, const float* xyz, bool smooth, double scale,
                        int vp_power, int which) {
     const int n = off[n_shots];
     std::vector<int> shot, point;
     std::vector<long long> idx;
     std::vector<float> coef, wraw;
-    std::vector<HicksGather3D> hg;
+    std::vector<SupportGather3D> hg;
+    const int interp = p->d.interpolation, lo = support_lo(interp);
     for (int s = 0; s < n_shots; s++)
         for (int i = off[s]; i < off[s + 1]; i++) {
-            int base[3];
-            double c[3][8];
+            int base[3], width = 0;
+            double c[3][SUPPORT_MAX];
             for (int a = 0; a < 3; a++) {
                 const double rel = ((double)xyz[3 * i + a] + p->d.extra[a] * p->d.spacing[a]) / p->d.spacing[a];
                 base[a] = (int)std::floor(rel);
-                if (!(base[a] - 3 >= 0 && base[a] + 4 <= p->d.shape[a] - 1))
-                    return fail3(SA_E_INVALID, "point's Hicks support lies outside the 3D grid");
-                hicks_coefs(rel - base[a], smooth, c[a]);
+                if (!(base[a] - lo >= 0 && base[a] - lo + support_width(interp) - 1 <= p->d.shape[a] - 1))
+                    return fail3(SA_E_INVALID, "point's interpolation support lies outside the 3D grid");
+                width = support_coefs(interp, rel - base[a], smooth, c[a]);
             }
-            for (int u = 0; u < 8; u++)
-                for (int v = 0; v < 8; v++)
-                    for (int w = 0; w < 8; w++) {
+            for (int u = 0; u < width; u++)
+                for (int v = 0; v < width; v++)
+                    for (int w = 0; w < width; w++) {
                         const double ww = c[0][u] * c[1][v] * c[2][w];
                         if (ww == 0.0) continue;
-                        const int x = base[0] - 3 + u, y = base[1] - 3 + v, z = base[2] - 3 + w;
+                        const int x = base[0] - lo + u, y = base[1] - lo + v, z = base[2] - lo + w;
                         const float vv = p->vp_host.empty() ? 0.f : p->vp_host[((size_t)x * p->ny + y) * p->nz + z];
                         const double vpow = vp_power == 2 ? (double)(vv * vv) : (double)vv;
                         shot.push_back(s);
@@ -388,13 +390,14 @@ static int build_hicks(Plan3D* p, int n_shots, const int* off, const float* xyz,
                         wraw.push_back((float)ww);
                     }
             {
-                HicksGather3D G;
-                G.x = base[0] - 3;
-                G.y = base[1] - 3;
-                G.z = base[2] - 3;
+                SupportGather3D G{};
+                G.x = base[0] - lo;
+                G.y = base[1] - lo;
+                G.z = base[2] - lo;
                 G.point = i;
                 G.shot = s;
-                for (int k = 0; k < 8; k++) {
+                G.width = width;
+                for (int k = 0; k < SUPPORT_MAX; k++) {
                     G.wx[k] = (float)c[0][k];
                     G.wy[k] = (float)c[1][k];
                     G.wz[k] = (float)c[2][k];
@@ -416,9 +419,9 @@ static int build_hicks(Plan3D* p, int n_shots, const int* off, const float* xyz,
         CK3(cudaMemcpy(p->e_w[which], wraw.data(), m * sizeof(float), cudaMemcpyHostToDevice));
     }
     p->n_ent[which] = (int)m;
-    HicksGather3D** dst = which == 1 ? &p->hgat : &p->hgat_src;
+    SupportGather3D** dst = which == 1 ? &p->hgat : &p->hgat_src;
     if ((rc = alloc3(dst, std::max<size_t>(1, hg.size()))) != SA_OK) return rc;
-    if (!hg.empty()) CK3(cudaMemcpy(*dst, hg.data(), hg.size() * sizeof(HicksGather3D), cudaMemcpyHostToDevice));
+    if (!hg.empty()) CK3(cudaMemcpy(*dst, hg.data(), hg.size() * sizeof(SupportGather3D), cudaMemcpyHostToDevice));
     (void)n;
     return SA_OK;
 }
@@ -434,10 +437,10 @@ int plan3d_set_geometry(Plan3D* p, int n_shots, const int* so, const float* sx, 
     if (rc == SA_OK)
         rc = build_points(p, n_shots, ro_.data(), rx_.data(), -p->d.dt * p->d.dt, 2, &p->r_shot, &p->r_base, &p->r_w,
                           &p->r_coef);
-    if (rc == SA_OK && p->hicks)
-        rc = build_hicks(p, n_shots, so_.data(), sx_.data(), true, 2.0 * p->d.dt / h, 1, 0);
-    if (rc == SA_OK && p->hicks)
-        rc = build_hicks(p, n_shots, ro_.data(), rx_.data(), false, -p->d.dt * p->d.dt, 2, 1);
+    if (rc == SA_OK && p->wide)
+        rc = build_support(p, n_shots, so_.data(), sx_.data(), true, 2.0 * p->d.dt / h, 1, 0);
+    if (rc == SA_OK && p->wide)
+        rc = build_support(p, n_shots, ro_.data(), rx_.data(), false, -p->d.dt * p->d.dt, 2, 1);
     if (rc != SA_OK) return rc;
     p->so = so_;
     p->ro = ro_;
@@ -533,7 +536,7 @@ static int image_raw_level(Plan3D* p, const Step3D& a, const float* q, bool rho,
 }
 
 // One time level: [pass A] + pass B, then injection into the new level (and its snapshot).
-// which: 0 injects the sources (amp = their samples), 1 the receivers, -1 nothing; linear or Hicks
+// which: 0 injects the sources (amp = their samples), 1 the receivers, -1 nothing; linear or wide (Hicks, sinc)
 // as the plan's interpolation. aux: the CFS-PML auxiliary fields advanced (default: the plan's).
 static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, int which, const float* amp, bool save_now,
                  cudaStream_t s, long long& n, float* aux = nullptr) {
@@ -563,7 +566,7 @@ static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, int which,
     const int npts = which == 0 ? p->n_src : p->n_rec;
     float* snap = save_now ? a.snaps : nullptr;
     const long long soff = (long long)(a.t / a.f) * a.snap_stride;
-    if (p->hicks) {
+    if (p->wide) {
         const Entries3D e{p->e_shot[which], p->e_point[which], p->e_idx[which], p->e_coef[which]};
         CK3(inject_entries3d(e, p->n_ent[which], amp, npts, a.t, prev, p->field, snap, a.snap_shot_stride, soff,
                              inv_dt2, s));
@@ -634,8 +637,8 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
         rc = step3(p, a, cur, prev, 0, p->src_amp, save && !raw && t % a.f == 0, s, n);
         if (rc != SA_OK) return rc;
         if (p->n_rec) {  // rec[t] = interp(p[t+1])
-            if (p->hicks)
-                CK3(hicks_gather3d(p->hgat, p->n_rec, prev, p->field, p->ny, p->zp, p->rec_amp, p->n_rec, t, 1.f, s));
+            if (p->wide)
+                CK3(support_gather3d(p->hgat, p->n_rec, prev, p->field, p->ny, p->zp, p->rec_amp, p->n_rec, t, 1.f, s));
             else
                 CK3(sparse3d_gather(rec, p->n_rec, prev, p->field, p->ny, p->zp, p->rec_amp, p->n_rec, t, s));
             n++;
@@ -682,8 +685,8 @@ int plan3d_forward(Plan3D* p, const float* wavelets, float* traces, int save_mod
 static int wavelet_level(Plan3D* p, const float* q, int t, bool wav, cudaStream_t s, long long& n) {
     if (!wav || !p->n_src) return SA_OK;
     const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
-    if (p->hicks)
-        CK3(hicks_gather3d(p->hgat_src, p->n_src, q, p->field, p->ny, p->zp, p->wgrad, p->n_src, t, -1.f, s));
+    if (p->wide)
+        CK3(support_gather3d(p->hgat_src, p->n_src, q, p->field, p->ny, p->zp, p->wgrad, p->n_src, t, -1.f, s));
     else
         CK3(sparse3d_gather(src, p->n_src, q, p->field, p->ny, p->zp, p->wgrad, p->n_src, t, s, -1.f));
     n++;
@@ -943,7 +946,7 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
         if ((rc = alloc3(&p->r_xcoef, 8 * (size_t)std::max(1, p->n_rec))) != SA_OK) return rc;
         const Sparse3D rec{p->r_shot, p->r_base, p->r_w, p->r_coef};
         CK3(xcoef3d(rec, p->n_rec, p->C1 + G * p->plane, p->W + G * p->plane, p->ny, p->zp, p->r_xcoef, 0));
-        if (p->hicks) {
+        if (p->wide) {
             if ((rc = alloc3(&p->e_xcoef, std::max<size_t>(1, p->n_ent[1]))) != SA_OK) return rc;
             CK3(xcoef_entries3d(p->e_idx[1], p->e_w[1], p->n_ent[1], p->C1 + G * p->plane, p->W + G * p->plane,
                                 p->e_xcoef, 0));
@@ -996,7 +999,7 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
             aa.t = t;
             if ((rc = step3(p, aa, zt, znext, -1, p->rec_amp, false, s, n)) != SA_OK) return rc;
             if (p->n_rec) {  // z[t-1] += w C1 W dL/drec[t-2]
-                if (p->hicks) {
+                if (p->wide) {
                     const Entries3D e{p->e_shot[1], p->e_point[1], p->e_idx[1], p->e_xcoef};
                     CK3(inject_entries3d(e, p->n_ent[1], p->rec_amp, p->n_rec, t - 2, znext, p->field, nullptr, 0, 0,
                                          0.f, s));
@@ -1025,7 +1028,7 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
                              p->ny, p->nz, p->zp, p->n_shots, p->field, inv_dt2, p->gradb, p->precb, s));
             n++;
             if (p->n_src) {
-                if (p->hicks) {
+                if (p->wide) {
                     const Entries3D e{p->e_shot[0], p->e_point[0], p->e_idx[0], p->e_coef[0]};
                     CK3(exact_src_entries3d(zt, e, p->e_w[0], p->n_ent[0], p->src_amp, p->n_src, t - 1, src_scale,
                                             p->ES, p->field, p->gradb, s));

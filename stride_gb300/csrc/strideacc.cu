@@ -179,10 +179,10 @@ struct sa_plan {
     sa::Gather* gat_src = nullptr;
     float* wgrad = nullptr;
     size_t cap_gat_src = 0, cap_wgrad = 0;
-    // Hicks interpolation: receiver gathers run as their own kernel after each step
-    sa::HicksGather* hgat = nullptr;
+    // wide interpolation (Hicks, sinc): receiver gathers run as their own kernel after each step
+    sa::SupportGather* hgat = nullptr;
     size_t cap_hgat = 0;
-    sa::HicksGather* hgat_src = nullptr;  // sources, smoothed and negated: the wavelet gradient
+    sa::SupportGather* hgat_src = nullptr;  // sources (Hicks: smoothed), negated: the wavelet gradient
     size_t cap_hgat_src = 0;
     // source (forward), receiver (adjoint) and exact-gradient receiver injection grouped by target
     // point, each applied by its own kernel after the step
@@ -312,23 +312,26 @@ int build_lists_impl(sa_plan* p) {
     // shots advance in pairs (the two lanes of a float2); CTA index of (pair, chunk, strip)
     auto cta_of = [&](int shot, int x, int y) { return ((shot / 2) * nc + x / p->chunk_rows) * ns + y / p->by; };
     // corner(x, y): the per-corner factor of the coefficient (vp, vp^2 or C1 W there)
-    // linear: the 4 corners; Hicks: the 8 x 8 support from base - 3 (smooth: the sources' smoothing)
-    const bool hicks = p->d.interpolation == SA_INTERP_HICKS;
+    // linear: the 4 corners; Hicks / sinc: the width x width support from base - lo (smooth: the
+    // Hicks sources' smoothing)
+    const int interp = p->d.interpolation;
+    const bool wide = interp != SA_INTERP_LINEAR;
+    const int lo = sa::support_lo(interp);
     auto make_inj = [&](const std::vector<int>& off, const std::vector<int>& bx, const std::vector<int>& by,
                         const std::vector<double>& fx, const std::vector<double>& fy, double scale, auto corner,
                         std::vector<HostInject>& out, bool smooth) {
         out.clear();
         for (int s = 0; s < p->n_shots; s++)
             for (int i = off[s]; i < off[s + 1]; i++) {
-                if (hicks) {
-                    double cxs[8], cys[8];
-                    sa::hicks_coefs(fx[i], smooth, cxs);
-                    sa::hicks_coefs(fy[i], smooth, cys);
-                    for (int a = 0; a < 8; a++)
-                        for (int b = 0; b < 8; b++) {
+                if (wide) {
+                    double cxs[sa::SUPPORT_MAX], cys[sa::SUPPORT_MAX];
+                    const int width = sa::support_coefs(interp, fx[i], smooth, cxs);
+                    sa::support_coefs(interp, fy[i], smooth, cys);
+                    for (int a = 0; a < width; a++)
+                        for (int b = 0; b < width; b++) {
                             const double w = cxs[a] * cys[b];
                             if (w == 0.0) continue;
-                            const int x = bx[i] - 3 + a, y = by[i] - 3 + b;
+                            const int x = bx[i] - lo + a, y = by[i] - lo + b;
                             out.push_back({cta_of(s, x, y), x, y, i, (float)(w * scale * corner(x, y)), s & 1});
                         }
                     continue;
@@ -433,35 +436,36 @@ int build_lists_impl(sa_plan* p) {
     };
     CKR(make_gathers(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, 1.f, &p->gat_flat, &p->cap_gat_flat));
     CKR(make_gathers(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, -1.f, &p->gat_src, &p->cap_gat_src));
-    // Hicks gathers over the 8 x 8 support: receivers (the forward's traces) and, smoothed as the
-    // sources are and negated, the sources (the adjoint's wavelet gradient, -interp(p_a))
-    auto make_hicks = [&](const std::vector<int>& off, const std::vector<int>& bx, const std::vector<int>& by,
+    // gathers over the width x width support: receivers (the forward's traces) and, negated (and for
+    // Hicks smoothed as the sources are), the sources (the adjoint's wavelet gradient, -interp(p_a))
+    auto make_support = [&](const std::vector<int>& off, const std::vector<int>& bx, const std::vector<int>& by,
                           const std::vector<double>& fx, const std::vector<double>& fy, bool smooth, float sign,
-                          sa::HicksGather** dst, size_t* cap) -> int {
-        std::vector<sa::HicksGather> hg;
+                          sa::SupportGather** dst, size_t* cap) -> int {
+        std::vector<sa::SupportGather> hg;
         for (int s = 0; s < p->n_shots; s++)
             for (int r = off[s]; r < off[s + 1]; r++) {
-                sa::HicksGather G;
-                G.row = bx[r] - 3;
-                G.col = by[r] - 3;
+                sa::SupportGather G{};
+                G.row = bx[r] - lo;
+                G.col = by[r] - lo;
                 G.point = r;
                 G.shot = s;
-                double cx[8], cy[8];
-                sa::hicks_coefs(fx[r], smooth, cx);
-                sa::hicks_coefs(fy[r], smooth, cy);
-                for (int k = 0; k < 8; k++) {
+                double cx[sa::SUPPORT_MAX], cy[sa::SUPPORT_MAX];
+                G.width = sa::support_coefs(interp, fx[r], smooth, cx);
+                sa::support_coefs(interp, fy[r], smooth, cy);
+                for (int k = 0; k < sa::SUPPORT_MAX; k++) {
                     G.wx[k] = sign * (float)cx[k];
                     G.wy[k] = (float)cy[k];
                 }
                 hg.push_back(G);
             }
         CKR(ensure(dst, cap, hg.size()));
-        if (!hg.empty()) CK(cudaMemcpy(*dst, hg.data(), hg.size() * sizeof(sa::HicksGather), cudaMemcpyHostToDevice));
+        if (!hg.empty())
+            CK(cudaMemcpy(*dst, hg.data(), hg.size() * sizeof(sa::SupportGather), cudaMemcpyHostToDevice));
         return SA_OK;
     };
-    if (hicks) {
-        CKR(make_hicks(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, false, 1.f, &p->hgat, &p->cap_hgat));
-        CKR(make_hicks(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, true, -1.f, &p->hgat_src,
+    if (wide) {
+        CKR(make_support(p->rec_off, p->rec_bx, p->rec_by, p->rec_fx, p->rec_fy, false, 1.f, &p->hgat, &p->cap_hgat));
+        CKR(make_support(p->src_off, p->src_bx, p->src_by, p->src_fx, p->src_fy, true, -1.f, &p->hgat_src,
                        &p->cap_hgat_src));
     }
     return SA_OK;
@@ -572,7 +576,7 @@ int image_raw_step(const sa_plan* p, const float* q, int t, bool rho, cudaStream
 int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
     const bool save = mode == SA_SAVE_SNAPSHOTS;
     const bool raw = mode == SA_SAVE_RAW;
-    const bool hicks = p->d.interpolation == SA_INTERP_HICKS;
+    const bool wide = p->d.interpolation != SA_INTERP_LINEAR;  // a wide support (Hicks or sinc)
     const size_t fbytes = (size_t)npairs(p) * p->shot_stride * sizeof(float2);
     CK(cudaMemsetAsync(p->field[0], 0, fbytes, s));
     CK(cudaMemsetAsync(p->field[1], 0, fbytes, s));
@@ -600,7 +604,7 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
         const bool save_now = save && t % p->d.undersampling == 0;
         float* snap_now = save_now ? p->snaps + 2 * (long long)(t / p->d.undersampling) * p->snap_stride : nullptr;
         CKR(pml_step(p, a.cur, a.prev, false, snap_now, s, n));
-        if (hicks || !p->n_rec || t == 1) {
+        if (wide || !p->n_rec || t == 1) {
             CKR(inject_sources(p, a.prev, t, p->snaps, p->snap_shot_stride, save_now, s, n));
         } else {  // this step's sources into p[t+1] and the previous step's rec[t-1] = interp(p[t]), one launch
             CK(sa::inject_gather2d(a.prev, p->stgt.idx, p->stgt.off, p->stgt.coef, p->stgt.point, p->stgt.n,
@@ -609,11 +613,11 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
                                    p->rec_amp, p->n_rec, t - 1, s));
             n++;
         }
-        if (p->n_rec && hicks) {  // rec[t] = interp(p[t+1]) over the Hicks support
-            CK(sa::hicks_gather2d(a.prev, p->shot_stride, p->pitch, p->hgat, p->n_rec, p->rec_amp, p->n_rec, t, s));
+        if (p->n_rec && wide) {  // rec[t] = interp(p[t+1]) over the wide support
+            CK(sa::support_gather2d(a.prev, p->shot_stride, p->pitch, p->hgat, p->n_rec, p->rec_amp, p->n_rec, t, s));
             n++;
         }
-        if (p->n_rec && !hicks && t == p->d.nt - 2) {  // the last step's receivers
+        if (p->n_rec && !wide && t == p->d.nt - 2) {  // the last step's receivers
             CK(sa::final_gather2d(a.prev, p->shot_stride, p->pitch, p->gat_flat, p->n_rec, p->rec_amp, p->n_rec, t,
                                   s));
             n++;
@@ -635,8 +639,8 @@ int issue_forward(sa_plan* p, int mode, cudaStream_t s) {
 // The wavelet gradient: -interp(p_a[t]) at the sources into wgrad row t (negated gather weights).
 int wavelet_gather(const sa_plan* p, const float* q, int t, bool wav, cudaStream_t s, long long& n) {
     if (!wav || !p->n_src) return SA_OK;
-    if (p->d.interpolation == SA_INTERP_HICKS)
-        CK(sa::hicks_gather2d(q, p->shot_stride, p->pitch, p->hgat_src, p->n_src, p->wgrad, p->n_src, t, s));
+    if (p->d.interpolation != SA_INTERP_LINEAR)
+        CK(sa::support_gather2d(q, p->shot_stride, p->pitch, p->hgat_src, p->n_src, p->wgrad, p->n_src, t, s));
     else
         CK(sa::final_gather2d(q, p->shot_stride, p->pitch, p->gat_src, p->n_src, p->wgrad, p->n_src, t, s));
     n++;
@@ -1206,7 +1210,7 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
     if (d.kernel != SA_KERNEL_OT2 && d.kernel != SA_KERNEL_OT4)
         return fail(SA_E_INVALID, "Unrecognized kernel %d", d.kernel);
     if (d.density < 0 || d.density > 2) return fail(SA_E_INVALID, "density mode %d", d.density);
-    if (d.interpolation != SA_INTERP_LINEAR && d.interpolation != SA_INTERP_HICKS)
+    if (d.interpolation != SA_INTERP_LINEAR && d.interpolation != SA_INTERP_HICKS && d.interpolation != SA_INTERP_SINC)
         return fail(SA_E_INVALID, "interpolation %d", d.interpolation);
     if (d.boundary != SA_BOUNDARY_SPONGE && d.boundary != SA_BOUNDARY_CFS_PML)
         return fail(SA_E_INVALID, "boundary %d", d.boundary);
@@ -1395,7 +1399,7 @@ int sa_set_geometry(sa_plan* p, int n_shots, const int* src_offsets, const float
     if ((ns && !src_xyz) || (nr && !rec_xyz)) return fail(SA_E_INVALID, "missing coordinates");
     if (p->p3) return sa::plan3d_set_geometry(p->p3, n_shots, src_offsets, src_xyz, rec_offsets, rec_xyz);
     const int dim = p->d.dim;
-    const bool hicks = p->d.interpolation == SA_INTERP_HICKS;
+    const bool wide = p->d.interpolation != SA_INTERP_LINEAR;  // a wide support (Hicks or sinc)
     auto convert = [&](const float* xyz, int n, std::vector<int>& bx, std::vector<int>& by, std::vector<double>& fx,
                        std::vector<double>& fy) -> int {
         bx.resize(n);
@@ -1410,7 +1414,8 @@ int sa_set_geometry(sa_plan* p, int n_shots, const int* src_offsets, const float
                 rel[a] = ((double)xyz[i * dim + a] - origin) / p->d.spacing[a];
                 base[a] = (int)std::floor(rel[a]);
                 const int n_a = a == 0 ? p->nx : p->ny;
-                const int lo = hicks ? 3 : 0, hi = hicks ? 4 : 1;  // support base-lo .. base+hi
+                const int lo = wide ? sa::support_lo(p->d.interpolation) : 0;  // support base-lo .. base+hi
+                const int hi = wide ? sa::support_width(p->d.interpolation) - 1 - lo : 1;
                 if (!(base[a] - lo >= 0 && base[a] + hi <= n_a - 1))
                     return fail(SA_E_INVALID, "point %d lies outside the grid along axis %d", i, a);
             }

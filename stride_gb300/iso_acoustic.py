@@ -36,7 +36,7 @@ logging.addLevelName(PERF, 'PERF')
 
 SUPPORTED_BOUNDARIES = ('sponge_boundary_2', 'complex_frequency_shift_PML_2')
 KNOWN_BOUNDARIES = ('sponge_boundary_2', 'complex_frequency_shift_PML_2', 'sponge_boundary_1')
-SUPPORTED_INTERPOLATION = ('linear', 'hicks')
+SUPPORTED_INTERPOLATION = ('linear', 'hicks', 'sinc')
 KNOWN_INTERPOLATION = ('linear', 'hicks', 'sinc')
 
 
@@ -122,14 +122,14 @@ class IsoAcousticGB300(ProblemTypeBase):
     gradient), with the keyword arguments of IsoAcousticDevito (devito.py:43-114).
 
     Supported: ``kernel`` OT2/OT4 (auto-selected from dt as the reference does),
-    ``boundary_type='sponge_boundary_2'``, ``interpolation_type='linear'``,
+    ``boundary_type='sponge_boundary_2'``, ``interpolation_type`` 'linear', 'hicks' or 'sinc',
     ``attenuation_power=0``, ``diff_source``, ``save_undersampling``, ``save_wavefield``.
     ``platform``, ``devito_config`` and ``devito_args`` are accepted and ignored (the time
     loop always runs on the GPU). ``boundary_type='complex_frequency_shift_PML_2'`` runs with
     kernel OT2 (the combination the reference's own example runs). Gradients: vp, rho and
     the wavelets; alpha raises ValueError('Variable alpha not implemented') as in the
     reference, which has no alpha gradient. Options the reference supports but this build does
-    not (the CFS-PML with OT4, sinc interpolation, attenuation power 2) raise
+    not (the CFS-PML with OT4, attenuation power 2) raise
     NotImplementedError; unknown values raise ValueError as in the reference.
 
     Memory: ``checkpoint_interval=K`` (steps) or ``checkpoint_budget`` (bytes) keeps the wavefield

@@ -199,15 +199,16 @@ def test_exact_gradient_3d(kernel, density, alpha, interval):
     op.close()
 
 
-@pytest.mark.parametrize('density', ['none', 'variable'])
-def test_hicks_3d(density):
-    """Hicks (Kaiser-windowed sinc) sources and receivers on a 3D plan: traces and the vp gradient
-    against the NumPy oracle with the same interpolation (common/devito.py:640-648,843-885)."""
+@pytest.mark.parametrize('density,interp', [('none', 'hicks'), ('variable', 'hicks'), ('variable', 'sinc')])
+def test_hicks_3d(density, interp):
+    """Wide-support sources and receivers on a 3D plan (Hicks, common/devito.py:640-648,843-885;
+    sinc, :634-638): traces and the vp gradient against the NumPy oracle with the same
+    interpolation."""
     c = case3d(kernel='OT4', density=density, alpha=True, n_shots=2, nt=120)
-    plan = make_plan3(c, interpolation='hicks')
+    plan = make_plan3(c, interpolation=interp)
     got, plan = C.gpu_forward(c, plan=plan, save=True)
     origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
-    kw = dict(rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation='hicks')
+    kw = dict(rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation=interp)
     snaps = []
     for s in range(2):
         wav = np.tile(c['wav'][None], (len(c['srcs'][s]), 1))
@@ -289,10 +290,12 @@ def test_wavelet_gradient_hicks_3d():
         k += ns
 
 
-def test_exact_gradient_hicks_3d():
-    """SA_GRAD_EXACT on a 3D plan with Hicks interpolation against the FP64 exact-adjoint oracle."""
+@pytest.mark.parametrize('interp', ['hicks', 'sinc'])
+def test_exact_gradient_hicks_3d(interp):
+    """SA_GRAD_EXACT on a 3D plan with a wide support (Hicks, sinc) against the FP64 exact-adjoint
+    oracle."""
     c = case3d(kernel='OT4', density='variable', alpha=True, inner=20, nt=80, n_shots=2)
-    plan = make_plan3(c, checkpoint_interval=16, interpolation='hicks')
+    plan = make_plan3(c, checkpoint_interval=16, interpolation=interp)
     C.gpu_forward(c, plan=plan, save='checkpoints')
     n_rec = sum(len(r) for r in c['recs'])
     weights = np.random.default_rng(7).standard_normal((n_rec, c['nt']))
@@ -306,7 +309,7 @@ def test_exact_gradient_hicks_3d():
         wav = np.tile(c['wav'][None], (len(c['srcs'][s]), 1))
         gs, _ = npo.adjoint_exact(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][s],
                                   c['recs'][s], wav, weights[k:k + nr], origin, rho=c['rho'], alpha=c['alpha'],
-                                  kernel='OT4', interpolation='hicks')
+                                  kernel='OT4', interpolation=interp)
         ref += gs
         k += nr
     assert np.abs(ref).max() > 0

@@ -63,6 +63,12 @@ def test_shortest_time_axis_and_bounds():
     hicks = C.make_plan(c, interpolation='hicks')
     with pytest.raises(_lib.StrideAccError):
         hicks.set_geometry([0, 1], edge_ok, [0, 1], edge_ok)  # 3 cells of support below, 4 above
+    sinc = C.make_plan(c, interpolation='sinc')  # 6 cells of support below, 7 above
+    near = np.array([[origin + 20.3 * h, origin + 5.2 * h]], np.float32)
+    inside = np.array([[origin + 20.3 * h, origin + 6.2 * h]], np.float32)
+    sinc.set_geometry([0, 1], inside, [0, 1], inside)
+    with pytest.raises(_lib.StrideAccError):
+        sinc.set_geometry([0, 1], near, [0, 1], inside)
     with pytest.raises(_lib.StrideAccError):  # more shots than the plan holds
         plan.set_geometry([0, 1, 2], np.concatenate([edge_ok, edge_ok]), [0, 1, 2], np.concatenate([edge_ok, edge_ok]))
 

@@ -101,11 +101,12 @@ def test_exact_mode_needs_checkpoints():
                      np.zeros(c['vp'].shape, np.float32), exact=True)
 
 
-def test_exact_gradient_hicks():
-    """SA_GRAD_EXACT with Hicks sources and receivers (the forward's support in its transpose)
-    against the FP64 exact-adjoint oracle with the same interpolation."""
+@pytest.mark.parametrize('interp', ['hicks', 'sinc'])
+def test_exact_gradient_hicks(interp):
+    """SA_GRAD_EXACT with wide-support (Hicks, sinc) sources and receivers (the forward's support in
+    its transpose) against the FP64 exact-adjoint oracle with the same interpolation."""
     c = C.small_case(kernel='OT4', density='variable', alpha=True, inner=40, nt=160, n_shots=2, uneven=True)
-    plan = C.make_plan(c, checkpoint_interval=16, interpolation='hicks')
+    plan = C.make_plan(c, checkpoint_interval=16, interpolation=interp)
     n_rec = sum(len(r) for r in c['recs'])
     weights = np.random.default_rng(8).standard_normal((n_rec, c['nt']))
     _, g = _exact(c, plan, weights)
@@ -117,7 +118,7 @@ def test_exact_gradient_hicks():
         wav = np.tile(c['wav'][None], (len(c['srcs'][s]), 1))
         gs, _ = npo.adjoint_exact(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][s],
                                   c['recs'][s], wav, weights[k:k + nr], origin, rho=c['rho'], alpha=c['alpha'],
-                                  kernel='OT4', interpolation='hicks')
+                                  kernel='OT4', interpolation=interp)
         ref += gs
         k += nr
     assert np.abs(ref).max() > 0

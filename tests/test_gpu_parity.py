@@ -103,13 +103,15 @@ def test_wavelet_gradient_parity():
     assert np.array_equal(grad, g2)
 
 
+@pytest.mark.parametrize('interp', ['hicks', 'sinc'])
 @pytest.mark.parametrize('density', ['none', 'variable'])
-def test_hicks_interpolation_parity(density):
-    """Hicks (Kaiser-windowed sinc) sources and receivers: traces and the vp gradient against the
-    NumPy oracle with the same interpolation."""
+def test_hicks_interpolation_parity(density, interp):
+    """Wide-support sources and receivers (Hicks: 8 points per axis, the sources smoothed; sinc:
+    Devito's half-width 7): traces and the vp gradient against the NumPy oracle with the same
+    interpolation."""
     from oracle import numpy_oracle as npo
     c = C.small_case(kernel='OT4', density=density, alpha=True, n_shots=2, uneven=True, nt=200, inner=48)
-    plan = C.make_plan(c, interpolation='hicks')
+    plan = C.make_plan(c, interpolation=interp)
     got, plan = C.gpu_forward(c, plan=plan, save=True)
     origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
     snaps_all = []
@@ -117,7 +119,7 @@ def test_hicks_interpolation_parity(density):
         wav = np.tile(c['wav'][None], (len(c['srcs'][s]), 1))
         ref, snaps = npo.forward(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][s], c['recs'][s],
                                  wav, origin, rho=c['rho'], alpha=c['alpha'], kernel='OT4', save=True,
-                                 interpolation='hicks')
+                                 interpolation=interp)
         assert np.abs(ref).max() > 0
         assert C.rel_l2(got[s], ref) <= 1e-4
         snaps_all.append(snaps)
@@ -130,18 +132,19 @@ def test_hicks_interpolation_parity(density):
     g_ref = np.zeros(c['vp'].shape)
     for s in range(2):
         g, _ = npo.adjoint(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['recs'][s], res[s], origin,
-                           snaps_all[s], rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation='hicks')
+                           snaps_all[s], rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation=interp)
         g_ref += g
     assert C.cosine(grad, g_ref) >= 0.999
     assert C.rel_l2(grad, g_ref) <= 1e-3
 
 
-def test_wavelet_gradient_hicks():
-    """The wavelet gradient with Hicks interpolation: -interp(p_a) over the sources' smoothed 8 x 8
-    support, against the NumPy oracle."""
+@pytest.mark.parametrize('interp', ['hicks', 'sinc'])
+def test_wavelet_gradient_hicks(interp):
+    """The wavelet gradient with a wide support: -interp(p_a) over the sources' support (Hicks:
+    smoothed, 8 x 8; sinc: 14 x 14), against the NumPy oracle."""
     from oracle import numpy_oracle as npo
     c = C.small_case(kernel='OT4', density='variable', alpha=True, n_shots=2, uneven=True, nt=200, inner=48)
-    plan = C.make_plan(c, interpolation='hicks')
+    plan = C.make_plan(c, interpolation=interp)
     got, plan = C.gpu_forward(c, plan=plan, save=True)
     rng = np.random.default_rng(6)
     res = [rng.standard_normal(g.shape).astype(np.float32) * np.abs(g).max() for g in got]
@@ -154,9 +157,9 @@ def test_wavelet_gradient_hicks():
         wav = np.tile(c['wav'][None], (len(c['srcs'][s]), 1))
         _, snaps = npo.forward(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][s], c['recs'][s],
                                wav, origin, rho=c['rho'], alpha=c['alpha'], kernel='OT4', save=True,
-                               interpolation='hicks')
+                               interpolation=interp)
         _, _, g_ref = npo.adjoint(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['recs'][s], res[s], origin,
-                                  snaps, rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation='hicks',
+                                  snaps, rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation=interp,
                                   src_coords=c['srcs'][s])
         ns = len(c['srcs'][s])
         assert np.abs(g_ref).max() > 0

@@ -242,15 +242,35 @@ def test_cfs_pml_absorbs_better_than_the_sponge():
     assert err(pml) < 0.03 and err(pml) < err(sponge) / 3
 
 
-def test_exact_adjoint_dot_product_hicks():
-    """The exact adjoint with Hicks sources (smoothed) and receivers: <F w, r> = <w, F^T r>."""
+def test_sinc_stencil_weights():
+    """The sinc support (half-width 7, 14 points per axis): a point on a grid node is that node
+    alone (sinc vanishes on the other nodes), the weights of any position sum to one within the
+    windowed sinc's ripple, and they are symmetric about the cell centre."""
+    rng = np.random.default_rng(0)
+    base, w, offs = O.sinc_stencil(np.array([[3., 5.]]), (0., 0.), (1., 1.))
+    assert offs.shape == (196, 2) and np.array_equal(base, [[3, 5]])
+    k = int(np.argmax(np.abs(w[0])))
+    assert tuple(offs[k]) == (0, 0) and abs(w[0, k] - 1) < 1e-12
+    assert np.abs(np.delete(w[0], k)).max() < 1e-12
+    pts = rng.uniform(1., 9., (50, 2))
+    _, w, _ = O.sinc_stencil(pts, (0., 0.), (1., 1.))
+    assert np.abs(w.sum(axis=1) - 1).max() < 1e-3
+    _, wa, oa = O.sinc_stencil(np.array([[0.25]]), (0.,), (1.,))
+    _, wb, ob = O.sinc_stencil(np.array([[0.75]]), (0.,), (1.,))
+    assert np.allclose(wa[0], wb[0][::-1], atol=1e-12)  # x at +0.25 mirrors x at +0.75
+
+
+@pytest.mark.parametrize('interp', ['hicks', 'sinc'])
+def test_exact_adjoint_dot_product_hicks(interp):
+    """The exact adjoint with wide-support sources and receivers (Hicks: the sources smoothed;
+    sinc): <F w, r> = <w, F^T r>."""
     c = _exact_case('OT4', 'variable', True)
     r = c['rng'].standard_normal((len(c['rec']), c['nt']))
     w = c['rng'].standard_normal(c['wav'].shape).astype(np.float32).astype(np.float64)
     _, gw = O.adjoint_exact(c['vp'], c['spacing'], c['dt'], c['nt'], c['ab'], c['src'], c['rec'], w, r, c['origin'],
-                            rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation='hicks')
+                            rho=c['rho'], alpha=c['alpha'], kernel='OT4', interpolation=interp)
     tr = O.forward(c['vp'], c['spacing'], c['dt'], c['nt'], c['ab'], c['src'], c['rec'], w, c['origin'], rho=c['rho'],
-                   alpha=c['alpha'], kernel='OT4', dtype=np.float64, interpolation='hicks')[0]
+                   alpha=c['alpha'], kernel='OT4', dtype=np.float64, interpolation=interp)[0]
     lhs = float(np.sum(tr * r))
     rhs = float(np.sum(gw * w))
     assert abs(lhs - rhs) <= 1e-6 * abs(lhs)
