@@ -1214,8 +1214,11 @@ int sa_plan_create(const sa_desc* desc, sa_plan** out) {
         return fail(SA_E_INVALID, "interpolation %d", d.interpolation);
     if (d.boundary != SA_BOUNDARY_SPONGE && d.boundary != SA_BOUNDARY_CFS_PML)
         return fail(SA_E_INVALID, "boundary %d", d.boundary);
+    // With OT4 the reference's PML reads vp^2 laplace(p) where OT2 reads p (iso_acoustic/devito.py:1551):
+    // its auxiliary fields gain two derivatives and a factor vp^2, and the update diverges
     if (d.boundary == SA_BOUNDARY_CFS_PML && d.kernel != SA_KERNEL_OT2)
-        return fail(SA_E_UNSUPPORTED, "the CFS-PML is implemented with OT2");
+        return fail(SA_E_UNSUPPORTED, "the CFS-PML runs with OT2 only: with OT4 the reference's boundary field is "
+                                      "vp^2 laplace(p) and its literal update diverges");
     if (d.boundary == SA_BOUNDARY_CFS_PML && !(d.f_centre > 0)) return fail(SA_E_INVALID, "f_centre");
     if (d.nt < 3 || d.undersampling < 1 || d.max_shots < 1) return fail(SA_E_INVALID, "nt/undersampling/max_shots");
     for (int a = 0; a < d.dim; a++) {

@@ -242,6 +242,28 @@ def test_cfs_pml_absorbs_better_than_the_sponge():
     assert err(pml) < 0.03 and err(pml) < err(sponge) / 3
 
 
+def test_cfs_pml_ot4_literal_reading_diverges():
+    """With OT4 the reference hands the CFS-PML the `laplacian` Function as its boundary field
+    (iso_acoustic/devito.py:1551), and that Function holds vp^2 laplace(p) (:1504-1524,
+    _diff_op :1648-1659), where OT2 hands it p itself. The auxiliary fields then carry two more
+    space derivatives and a factor vp^2, about 1e13 times the OT2 term on this grid, and the
+    update diverges within a few hundred steps even at OT2's time step; OT2 on the same case stays
+    finite and decays. This is why the build rejects the combination (SA_E_UNSUPPORTED)."""
+    h, e, n, nt = 0.5e-3, 20, 40, 400
+    dt = 0.4 * h / 1650
+    src = np.array([[10 * h, 20 * h]])
+    rec = np.array([[30 * h, 20 * h], [20 * h, 38 * h]])
+    w = O.tone_burst(0.5e6, 3, nt, dt)[None]
+    run = lambda kernel: O.forward(np.full((n + 2 * e,) * 2, 1500., np.float32), (h, h), dt, nt, (e, e), src, rec, w,
+                                   (-e * h, -e * h), kernel=kernel, boundary='pml', f_centre=0.5e6)[0]
+    ot2 = run('OT2')
+    assert np.isfinite(ot2).all() and np.abs(ot2).max() < 1
+    with np.errstate(all='ignore'):
+        ot4 = run('OT4')
+    bad = ~np.isfinite(ot4) | (np.abs(ot4) > 1e6)
+    assert bad.any(axis=0)[:nt // 2].any()  # blown up within the first half of the run
+
+
 def test_sinc_stencil_weights():
     """The sinc support (half-width 7, 14 points per axis): a point on a grid node is that node
     alone (sinc vanishes on the other nodes), the weights of any position sum to one within the
