@@ -1,8 +1,11 @@
 // 3D iso-acoustic FDTD time step for sm_103a (stride/physics/iso_acoustic/devito.py:1466-1608 in
-// 3D). The grid is [x][y][z], z contiguous. A CTA owns a TY x TZ tile of (y, z) columns of one
-// shot and streams the x planes of its input field through a shared-memory ring (16-byte
-// cp.async, zero-filled beyond the grid: Devito's zero halo); x-derivatives come from
-// per-thread register queues, y and z derivatives from the shared plane.
+// 3D). The grid is [x][y][z], z contiguous, one array per shot. A CTA owns a TY x TZ tile of
+// (y, z) columns of a PAIR of shots and computes both in packed FP32 (one f32x2 instruction for
+// the two shots): it streams the x planes of its input field through a shared-memory ring of
+// float2 (the two shots interleaved by 4-byte cp.async, zero-filled beyond the grid: Devito's zero
+// halo). The y and z derivatives of a row are taken from its plane as soon as it arrives and wait
+// in a register queue until the x derivatives (per-thread register queues along x) reach that
+// row, so the ring holds only the planes in flight.
 //
 // One application of the spatial operator per pass (a 3D halo of 9 cells around a small tile
 // makes fusing OT4's two applications more expensive than a second pass):
@@ -23,8 +26,8 @@ struct Step3D {
     long long shot_stride;    // floats per shot in a field buffer (nx*ny*zp)
     int chunk_rows;           // output x rows per CTA
     int ty0n;                 // tiles along y
-    int nshots;               // blockIdx.x = shot + nshots * (tile_y + ty0n * tile_z): the shots of a
-                              // tile run together and share the tile's medium through L2
+    int nshots;               // shots; blockIdx.x = pair + npairs * (tile_y + ty0n * tile_z), pair p holding
+                              // shots 2p and 2p + 1 (a lone last shot computes a zero second lane)
     int t;
     const float* in;          // streamed field: u (OT2 / INTERMEDIATE) or l (OT4 FINAL)
     const float* cur;         // p[t] (FINAL: the current level at the output)
@@ -48,46 +51,53 @@ struct Step3D {
 
 __host__ __device__ constexpr int pow2_at_least(int x) { return x <= 1 ? 1 : 2 * pow2_at_least((x + 1) / 2); }
 
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem, bool valid) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    const int sz = valid ? 4 : 0;  // 0: zero-fill, nothing is read
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(sz) : "memory");
+}
+
 template <int KIND, int TY, int TZ, int RB, int PF>
 struct Smem3D {
     static constexpr bool STAG = KIND != 0;
     static constexpr int R = STAG ? 9 : 5;
-    static constexpr int PY = TY + 2 * R;                   // plane rows (y) incl. halo
-    static constexpr int PZ = round4(TZ + 2 * R + 3);       // plane row width (z) from floor4
-    static constexpr int PLANE = PY * PZ;
-    static constexpr int QU = R + RB * (PF + 1);            // planes kept: o .. i + RB*(PF+1) - 1
-    static constexpr int FY = (TY + 9) * TZ;                // y fluxes of one row
+    static constexpr int PY = TY + 2 * R;     // plane rows (y) incl. halo
+    static constexpr int PZ = TZ + 2 * R;     // plane row width (z) incl. halo, from z0 - R
+    static constexpr int PLANE = PY * PZ;     // float2: the two shots of the pair
+    static constexpr int QU = RB * (PF + 1);  // planes in the ring: this iteration's and the prefetched
+    static constexpr int FY = (TY + 9) * TZ;  // y fluxes of one row
     // z fluxes of one row: TZ + 9 per y row, stored at a power-of-two stride so that a flat index
     // splits into (y, z) with a shift and a mask
     static constexpr int WZF = pow2_at_least(TZ + 9);
     static constexpr int FZ = TY * WZF;
-    static constexpr int oU = 0;
+    static constexpr int QG = R + RB;         // rows whose y and z parts wait for their x part
     static constexpr int oFY = QU * PLANE;
     static constexpr int oFZ = oFY + (STAG ? RB * FY : 0);
-    static constexpr int total = oFZ + (STAG ? RB * FZ : 0);
-    static constexpr size_t bytes = (size_t)total * sizeof(float);
+    static constexpr int oG = oFZ + (STAG ? RB * FZ : 0);
+    static constexpr int total = oG + QG * TY * TZ;
+    static constexpr size_t bytes = (size_t)total * sizeof(float2);
 };
 
 template <int QL, int RB>
-__device__ __forceinline__ void qshift1(float (&q)[QL]) {
+__device__ __forceinline__ void qshift2(float2 (&q)[QL]) {
 #pragma unroll
     for (int k = 0; k + RB < QL; k++) q[k] = q[k + RB];
 }
 template <class A>
-__device__ __forceinline__ float dstag_1(const A& v, int hi, int lo, int stride) {
-    float a = kWS(0) * v[hi], b = kWS(0) * v[lo];
+__device__ __forceinline__ float2 dstag2(const A& v, int hi, int lo, int stride) {
+    float2 a = mul2(f2(kWS(0)), v[hi]), b = mul2(f2(kWS(0)), v[lo]);
 #pragma unroll
     for (int m = 1; m < 5; m++) {
-        a = fmaf(kWS(m), v[hi + m * stride], a);
-        b = fmaf(kWS(m), v[lo - m * stride], b);
+        a = fma2(f2(kWS(m)), v[hi + m * stride], a);
+        b = fma2(f2(kWS(m)), v[lo - m * stride], b);
     }
-    return a - b;
+    return sub2(a, b);
 }
 template <class A>
-__device__ __forceinline__ float dcent_1(const A& v, int c, int stride) {
-    float a = kW2(0) * v[c];
+__device__ __forceinline__ float2 dcent2(const A& v, int c, int stride) {
+    float2 a = mul2(f2(kW2(0)), v[c]);
 #pragma unroll
-    for (int k = 1; k <= 5; k++) a = fmaf(kW2(k), v[c + k * stride] + v[c - k * stride], a);
+    for (int k = 1; k <= 5; k++) a = fma2(f2(kW2(k)), add2(v[c + k * stride], v[c - k * stride]), a);
     return a;
 }
 
@@ -96,129 +106,164 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
     using L = Smem3D<KIND, TY, TZ, RB, PF>;
     constexpr int NT = TY * TZ;
     constexpr bool STAG = L::STAG, VARB = KIND == 1;
-    constexpr int R = L::R, QU = L::QU, PY = L::PY, PZ = L::PZ, WZF = L::WZF;
-    constexpr int QB = STAG ? 9 : 10;
+    constexpr int R = L::R, QU = L::QU, PZ = L::PZ, WZF = L::WZF;
+    constexpr int QB = STAG ? 9 : 10;  // x queue: rows i - QB .. i + RB - 1
     constexpr int QL = QB + RB;
+    constexpr int QG = L::QG;          // y/z parts: rows i - R .. i + RB - 1, one slot per row
 
-    extern __shared__ __align__(16) float smem[];
-    float* const sU = smem + L::oU;
-    float* const sFY = smem + L::oFY;
-    float* const sFZ = smem + L::oFZ;
+    extern __shared__ __align__(16) float2 smem2[];
+    float2* const sU = smem2;
+    float2* const sFY = smem2 + L::oFY;
+    float2* const sFZ = smem2 + L::oFZ;
+    float2* const sG = smem2 + L::oG + threadIdx.x;  // this thread's y/z parts: slot s at sG[s NT]
 
     const int tid = threadIdx.x;
     const int tz = tid % TZ, ty = tid / TZ;
-    const int shot = blockIdx.x % a.nshots, tile = blockIdx.x / a.nshots;
+    const int npairs = (a.nshots + 1) / 2;
+    const int pair = blockIdx.x % npairs, tile = blockIdx.x / npairs;
+    const bool hasB = 2 * pair + 1 < a.nshots;
     const int tile_y = tile % a.ty0n, tile_z = tile / a.ty0n;
     const int chunk = blockIdx.y;
     const int y0 = tile_y * TY, z0 = tile_z * TZ;
     const int y = y0 + ty, z = z0 + tz;
     const bool col_in = y < a.ny && z < a.nz;
     const int yc = min(y, a.ny - 1), zc = min(z, a.nz - 1);
-    const int Z0 = (z0 - R) & ~3;  // plane rows start at floor4(z0 - R)
     const int xo0 = chunk * a.chunk_rows, xo1 = min(a.nx, xo0 + a.chunk_rows);
     const int i0 = xo0 - R, i1 = xo1 + R;
     const long long plane = (long long)a.ny * a.zp;
-    const long long soff = (long long)shot * a.shot_stride;
-    const long long col = (long long)yc * a.zp + zc;  // offset of this column in a plane
+    const long long offA = (long long)(2 * pair) * a.shot_stride;
+    const long long offB = hasB ? offA + a.shot_stride : offA;  // a lone shot's lane 1 is zero-filled, not stored
+    const long long col = (long long)yc * a.zp + zc;             // offset of this column in a plane
     const float ihx = 1.f / a.hx, ihy = 1.f / a.hy, ihz = 1.f / a.hz;
     const float ihx2 = ihx * ihx, ihy2 = ihy * ihy, ihz2 = ihz * ihz;
     const float dt2 = a.dt * a.dt;
     const float k12 = (float)((double)a.dt * (double)a.dt / 12.0);
 
     // plane ring: x row r in slot (r - i0) mod QU, kept as a running slot index (sI: row i);
-    // element (yy, zz) at [(yy-y0+R)*PZ + zz - Z0]
+    // element (yy, zz) at [(yy - y0 + R) PZ + zz - z0 + R]
     auto wrap = [](int s) { return s < 0 ? s + QU : (s >= QU ? s - QU : s); };
     auto slotp = [&](int s) { return sU + s * L::PLANE; };
-    constexpr int NQ = PY * (PZ / 4);
+    // the plane elements this thread stages (element tid + q NT): their offset within an x plane
+    // of the field, -1 beyond the grid (the same for every row)
+    constexpr int NS = (L::PLANE + NT - 1) / NT;
+    int gofs[NS];
+#pragma unroll
+    for (int q = 0; q < NS; q++) {
+        const int k = tid + q * NT, py = k / PZ, pz = k - py * PZ;
+        const int yy = y0 - R + py, zz = z0 - R + pz;
+        gofs[q] = k < L::PLANE && yy >= 0 && yy < a.ny && zz >= 0 && zz < a.nz ? yy * a.zp + zz : -1;
+    }
+    const float* const inA = a.in + offA;
+    const float* const inB = a.in + offB;
     auto prefetch = [&](int ii, int si) {  // rows ii, ii+1, ... into slots si, si+1, ...
 #pragma unroll
         for (int rr = 0; rr < RB; rr++) {
             const int r = ii + rr;
             if (r < i1) {
-                float* dst = slotp(wrap(si + rr));
+                float2* dst = slotp(wrap(si + rr)) + tid;
                 const bool row_ok = r >= 0 && r < a.nx;
-                for (int k = tid; k < NQ; k += NT) {
-                    const int py = k / (PZ / 4), q = Z0 + 4 * (k % (PZ / 4));
-                    const int yy = y0 - R + py;
-                    const bool ok = row_ok && yy >= 0 && yy < a.ny && q >= 0 && q + 4 <= a.zp;
-                    const float* g = ok ? a.in + soff + (long long)r * plane + (long long)yy * a.zp + q : a.in;
-                    cp_async16(dst + py * PZ + 4 * (k % (PZ / 4)), g, ok);
+                const float* ga = inA + (row_ok ? (long long)r * plane : 0);
+                const float* gb = inB + (row_ok ? (long long)r * plane : 0);
+#pragma unroll
+                for (int q = 0; q < NS; q++) {
+                    if (q * NT + tid >= L::PLANE) break;
+                    const bool ok = row_ok && gofs[q] >= 0;
+                    const int o = ok ? gofs[q] : 0;
+                    cp_async4(&dst[q * NT].x, ga + o, ok);
+                    cp_async4(&dst[q * NT].y, gb + o, ok && hasB);
                 }
             }
         }
         cp_async_commit();
     };
-    const int me = (ty + R) * PZ + (z - Z0);  // this column's index in a plane
+    const int me = (ty + R) * PZ + (tz + R);  // this column's index in a plane
 
-    float uq[QL], fq[STAG ? QL : 1];
+    // offsets of this thread's y- and z-flux buoyancies within an x plane of byh / bzh
+    constexpr int KY = ((TY + 9) * TZ + NT - 1) / NT, KZ = (TY * WZF + NT - 1) / NT;
+    int byo[VARB ? KY : 1], bzo[VARB ? KZ : 1];
+    if constexpr (VARB) {
+#pragma unroll
+        for (int q = 0; q < KY; q++) {
+            const int k = tid + q * NT;
+            const int ky = min(k / TZ, TY + 8), kz = k % TZ;
+            byo[q] = min(max(y0 - 5 + ky + 6, 0), a.ny + 9) * a.zp + min(z0 + kz, a.nz - 1);
+        }
+#pragma unroll
+        for (int q = 0; q < KZ; q++) {
+            const int k = tid + q * NT;
+            const int ky = min(k / WZF, TY - 1), kz = k % WZF;
+            bzo[q] = min(y0 + ky, a.ny - 1) * a.zpb + min(max(z0 - 5 + kz + 6, 0), a.zpb - 1);
+        }
+    }
+    const long long byplane = (long long)(a.ny + 12) * a.zp, bzplane = (long long)a.ny * a.zpb;
+    const int cidx = y * a.zp + z;  // this column's offset within a field plane (when col_in)
+
+    float2 uq[QL], fq[STAG ? QL : 1];
 #pragma unroll
     for (int k = 0; k < QL; k++) {
-        uq[k] = 0.f;
-        if constexpr (STAG) fq[k] = 0.f;
+        uq[k] = f2(0.f);
+        if constexpr (STAG) fq[k] = f2(0.f);
     }
+    auto gwrap = [](int s) { return s < 0 ? s + QG : (s >= QG ? s - QG : s); };
     const bool do_save = FINAL && a.save && (a.t % a.f == 0);
 
 #pragma unroll 1
     for (int k = 0; k < PF; k++) prefetch(i0 + k * RB, k * RB);
 
     int sI = 0;  // ring slot of row i
+    int gI = 0;  // y/z-part slot of row i (rows i0 .. i0 + R - 1 are never output rows)
 #pragma unroll 1
     for (int i = i0; i < i1; i += RB) {
         const int j = i - R;  // output row of this iteration's first input row
-        constexpr int KY = ((TY + 9) * TZ + NT - 1) / NT, KZ = (TY * WZF + NT - 1) / NT;
         float Wj[RB], bxi[RB], byv[RB][VARB ? KY : 1], bzv[RB][VARB ? KZ : 1];
-        float c1v[RB], c2v[RB], c3v[RB], uov[RB], pmv[RB];
+        float c1v[RB], c2v[RB], c3v[RB];
+        float2 uov[RB], pmv[RB];
 #pragma unroll
         for (int r = 0; r < RB; r++) {
             Wj[r] = __ldg(a.W + (long long)(j + r) * plane + col);
             if constexpr (VARB) {
                 bxi[r] = __ldg(a.bxh + (long long)(i - 5 + r) * plane + col);
-                const int xx = min(max(j + r, -sa::GUARD), a.nx + sa::GUARD - 1);
+                // buoyancies of the y and z fluxes of the arriving row i + r
+                const int xx = min(max(i + r, -sa::GUARD), a.nx + sa::GUARD - 1);
+                const float* byr = a.byh + xx * byplane;
+                const float* bzr = a.bzh + xx * bzplane;
 #pragma unroll
-                for (int q = 0; q < KY; q++) {
-                    const int k = tid + q * NT;
-                    const int ky = min(k / TZ, TY + 8), kz = k % TZ;
-                    const int zz = min(z0 + kz, a.nz - 1), yy = min(max(y0 - 5 + ky + 6, 0), a.ny + 9);
-                    byv[r][q] = __ldg(a.byh + (long long)xx * (a.ny + 12) * a.zp + (long long)yy * a.zp + zz);
-                }
+                for (int q = 0; q < KY; q++) byv[r][q] = __ldg(byr + byo[q]);
 #pragma unroll
-                for (int q = 0; q < KZ; q++) {
-                    const int k = tid + q * NT;
-                    const int ky = min(k / WZF, TY - 1), kz = k % WZF;
-                    const int yy = min(y0 + ky, a.ny - 1), zz = min(max(z0 - 5 + kz + 6, 0), a.zpb - 1);
-                    bzv[r][q] = __ldg(a.bzh + (long long)xx * a.ny * a.zpb + (long long)yy * a.zpb + zz);
-                }
+                for (int q = 0; q < KZ; q++) bzv[r][q] = __ldg(bzr + bzo[q]);
             }
             if constexpr (FINAL) {
                 const int row = j + r;
                 const bool ok = row >= xo0 && row < xo1 && col_in;
-                const long long idx = (long long)row * plane + (long long)y * a.zp + z;
+                const long long idx = ok ? (long long)row * plane + cidx : 0;
                 c1v[r] = ok ? __ldg(a.C1 + idx) : 0.f;
                 c2v[r] = ok ? __ldg(a.C2 + idx) : 0.f;
-                c3v[r] = ok ? __ldg(a.C3 + idx) : 0.f;
-                uov[r] = ok ? a.cur[soff + idx] : 0.f;
-                pmv[r] = ok ? a.prev[soff + idx] : 0.f;
+                c3v[r] = ok ? -__ldg(a.C3 + idx) : 0.f;
+                uov[r] = make_float2(ok ? a.cur[offA + idx] : 0.f, ok && hasB ? a.cur[offB + idx] : 0.f);
+                pmv[r] = make_float2(ok ? a.prev[offA + idx] : 0.f, ok && hasB ? a.prev[offB + idx] : 0.f);
             }
         }
-        (void)byv; (void)bzv; (void)c1v; (void)c2v; (void)c3v; (void)uov; (void)pmv;
+        (void)bxi; (void)byv; (void)bzv; (void)c1v; (void)c2v; (void)c3v; (void)uov; (void)pmv;
         cp_async_wait<PF - 1>();
         __syncthreads();
         prefetch(i + PF * RB, sI + PF * RB);
-        // y/z fluxes of rows j..j+RB-1 (staggered): F_y at half-rows y0-5+k, F_z at z0-5+k
+#pragma unroll
+        for (int r = 0; r < RB; r++) uq[QB + r] = slotp(wrap(sI + r))[me];
+        // the y and z parts of the arriving rows i .. i+RB-1 (only rows that are output rows)
         if constexpr (STAG) {
 #pragma unroll
             for (int r = 0; r < RB; r++) {
-                const float* pl = slotp(wrap(sI - R + r));
+                if (i + r < xo0 || i + r >= xo1) continue;
+                const float2* pl = slotp(wrap(sI + r));
 #pragma unroll
                 for (int q = 0; q < KY; q++) {
                     const int k = tid + q * NT;
                     if (k < (TY + 9) * TZ) {
                         const int ky = k / TZ, kz = k % TZ;
-                        const int hy = y0 - 5 + ky;  // half row hy + 1/2
-                        const int base = (hy - y0 + R) * PZ + (z0 + kz - Z0);
-                        float v = dstag_1(pl, base + PZ, base, PZ) * ihy;
-                        if constexpr (VARB) v *= byv[r][q];
-                        sFY[r * ((TY + 9) * TZ) + k] = v;
+                        const int base = (ky - 5 + R) * PZ + (kz + R);  // half row y0 - 5 + ky (+1/2)
+                        float2 v = mul2(dstag2(pl, base + PZ, base, PZ), f2(ihy));
+                        if constexpr (VARB) v = mul2(v, f2(byv[r][q]));
+                        sFY[r * L::FY + k] = v;
                     }
                 }
 #pragma unroll
@@ -226,70 +271,83 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
                     const int k = tid + q * NT;
                     const int ky = k / WZF, kz = k % WZF;
                     if (ky < TY && kz < TZ + 9) {
-                        const int hz = z0 - 5 + kz;  // half column hz + 1/2
-                        const int base = (ky + R) * PZ + (hz - Z0);
-                        float v = dstag_1(pl, base + 1, base, 1) * ihz;
-                        if constexpr (VARB) v *= bzv[r][q];
+                        const int base = (ky + R) * PZ + (kz - 5 + R);  // half column z0 - 5 + kz (+1/2)
+                        float2 v = mul2(dstag2(pl, base + 1, base, 1), f2(ihz));
+                        if constexpr (VARB) v = mul2(v, f2(bzv[r][q]));
                         sFZ[r * L::FZ + k] = v;
                     }
                 }
             }
             __syncthreads();
-        }
 #pragma unroll
-        for (int r = 0; r < RB; r++) uq[QB + r] = slotp(wrap(sI + r))[me];
-        float res[RB];
+            for (int r = 0; r < RB; r++) {
+                if (i + r < xo0 || i + r >= xo1) continue;
+                const float2* Fy = sFY + r * L::FY;
+                const float2* Fz = sFZ + r * L::FZ;
+                // D- along y at row ty: fluxes at half rows ty-5 .. ty+4 (index ky = half - y0 + 5)
+                const float2 gy = mul2(dstag2(Fy, (ty + 5) * TZ + tz, (ty + 4) * TZ + tz, TZ), f2(ihy));
+                const float2 gz = mul2(dstag2(Fz, ty * WZF + tz + 5, ty * WZF + tz + 4, 1), f2(ihz));
+                sG[gwrap(gI + r) * NT] = add2(gy, gz);
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < RB; r++) {
+                if (i + r < xo0 || i + r >= xo1) continue;
+                const float2* pl = slotp(wrap(sI + r));
+                sG[gwrap(gI + r) * NT] = fma2(dcent2(pl, me, PZ), f2(ihy2), mul2(dcent2(pl, me, 1), f2(ihz2)));
+            }
+        }
+        // the x parts of the output rows j .. j+RB-1, their y and z parts from the queue
+        float2 res[RB];
 #pragma unroll
         for (int r = 0; r < RB; r++) {
-            float gx, gyz;
+            float2 gx;
             if constexpr (STAG) {
-                float v = dstag_1(uq, r + 5, r + 4, 1) * ihx;
-                if constexpr (VARB) v *= bxi[r];
+                float2 v = mul2(dstag2(uq, r + 5, r + 4, 1), f2(ihx));
+                if constexpr (VARB) v = mul2(v, f2(bxi[r]));
                 fq[QB + r] = v;
-                gx = dstag_1(fq, r + 5, r + 4, 1) * ihx;
-                const float* Fy = sFY + r * ((TY + 9) * TZ);
-                const float* Fz = sFZ + r * L::FZ;
-                // D- along y at row ty: fluxes at half rows ty-5 .. ty+4 (index ky = half - y0 + 5)
-                const float gy = dstag_1(Fy, (ty + 5) * TZ + tz, (ty + 4) * TZ + tz, TZ) * ihy;
-                const float gz = dstag_1(Fz, ty * WZF + tz + 5, ty * WZF + tz + 4, 1) * ihz;
-                gyz = gy + gz;
+                gx = mul2(dstag2(fq, r + 5, r + 4, 1), f2(ihx));
             } else {
-                gx = dcent_1(uq, r + 5, 1) * ihx2;
-                const float* pl = slotp(wrap(sI - R + r));
-                gyz = dcent_1(pl, me, PZ) * ihy2 + dcent_1(pl, me, 1) * ihz2;
+                gx = mul2(dcent2(uq, r + 5, 1), f2(ihx2));
             }
-            const float g = gx + gyz;
-            if constexpr (!FINAL) {
-                res[r] = Wj[r] * g;
-            } else if constexpr (OT4) {
+            // the y/z part of row j + r (written by this thread R rows ago; zero-row reads unused)
+            const float2 g = add2(gx, j + r >= xo0 && j + r < xo1 ? sG[gwrap(gI - R + r) * NT] : f2(0.f));
+            if constexpr (FINAL && OT4) {
                 // Lt = l + dt^2/12 W G(l): the streamed l at row j+r is queue entry r (STAG,
                 // rows i-9..) or r+5 (laplace, rows i-10..)
-                res[r] = fmaf(k12, Wj[r] * g, STAG ? uq[r] : uq[r + 5]);
+                res[r] = fma2(f2(k12), mul2(f2(Wj[r]), g), STAG ? uq[r] : uq[r + 5]);
             } else {
-                res[r] = Wj[r] * g;
+                res[r] = mul2(f2(Wj[r]), g);
             }
         }
-        qshift1<QL, RB>(uq);
-        if constexpr (STAG) qshift1<QL, RB>(fq);
+        qshift2<QL, RB>(uq);
+        if constexpr (STAG) qshift2<QL, RB>(fq);
 #pragma unroll
         for (int r = 0; r < RB; r++) {
             const int row = j + r;
             if (row < xo0 || row >= xo1 || !col_in) continue;
-            const long long idx = (long long)row * plane + (long long)y * a.zp + z;
+            const long long idx = (long long)row * plane + cidx;
             if constexpr (!FINAL) {
-                a.out_l[soff + idx] = res[r];
+                a.out_l[offA + idx] = res[r].x;
+                if (hasB) a.out_l[offB + idx] = res[r].y;
             } else {
-                const float u_o = uov[r];
-                const float pm = pmv[r];
-                const float pn = c1v[r] * res[r] + c2v[r] * u_o - c3v[r] * pm;
-                if (do_save) {
-                    a.snaps[(long long)shot * a.snap_shot_stride + (long long)(a.t / a.f) * a.snap_stride + idx] =
-                        a.save == 2 ? u_o : (pn - 2.f * u_o + pm) / dt2;  // 2: raw p[t] (rho gradient)
+                const float2 u_o = uov[r], pm = pmv[r];
+                const float2 pn = fma2(f2(c1v[r]), res[r], fma2(f2(c2v[r]), u_o, mul2(f2(c3v[r]), pm)));
+                if (do_save) {  // 2: raw p[t] (rho gradient), else p.dt2
+                    const float2 sv = a.save == 2 ? u_o
+                                                  : make_float2((pn.x - 2.f * u_o.x + pm.x) / dt2,
+                                                                (pn.y - 2.f * u_o.y + pm.y) / dt2);
+                    float* sa0 = a.snaps + (long long)(2 * pair) * a.snap_shot_stride +
+                                 (long long)(a.t / a.f) * a.snap_stride + idx;
+                    sa0[0] = sv.x;
+                    if (hasB) sa0[a.snap_shot_stride] = sv.y;
                 }
-                a.prev[soff + idx] = pn;
+                a.prev[offA + idx] = pn.x;
+                if (hasB) a.prev[offB + idx] = pn.y;
             }
         }
         sI = sI + RB >= QU ? sI + RB - QU : sI + RB;
+        gI = gwrap(gI + RB);
     }
     cp_async_wait<0>();
 }

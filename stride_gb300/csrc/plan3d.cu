@@ -452,7 +452,7 @@ int plan3d_set_geometry(Plan3D* p, int n_shots, const int* so, const float* sx, 
     if ((rc = alloc3(&p->src_amp, (size_t)p->d.nt * std::max(1, p->n_src))) != SA_OK) return rc;
     if ((rc = alloc3(&p->rec_amp, (size_t)p->d.nt * std::max(1, p->n_rec))) != SA_OK) return rc;
     const int R = p->kind == 0 ? 5 : 9;
-    const int ctas = p->ty0n * p->tz0n * n_shots;
+    const int ctas = p->ty0n * p->tz0n * ((n_shots + 1) / 2);
     p->nchunks = std::max(1, std::min((152 * 4 + ctas - 1) / ctas, p->nx / (4 * R)));
     p->chunk_rows = (p->nx + p->nchunks - 1) / p->nchunks;
     p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
@@ -540,7 +540,7 @@ static int image_raw_level(Plan3D* p, const Step3D& a, const float* q, bool rho,
 // as the plan's interpolation. aux: the CFS-PML auxiliary fields advanced (default: the plan's).
 static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, int which, const float* amp, bool save_now,
                  cudaStream_t s, long long& n, float* aux = nullptr) {
-    const dim3 grid(p->ty0n * p->tz0n * p->n_shots, p->nchunks, 1);
+    const dim3 grid(p->ty0n * p->tz0n * ((p->n_shots + 1) / 2), p->nchunks, 1);  // shot pairs
     a.cur = cur;
     a.prev = prev;
     if (p->ot4) {
@@ -967,7 +967,7 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
     la.C2 = la.C3 = p->zeros + G * p->plane;
     const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
     const Sparse3D recx{p->r_shot, p->r_base, p->r_w, p->r_xcoef};
-    const dim3 grid(p->ty0n * p->tz0n * p->n_shots, p->nchunks, 1);
+    const dim3 grid(p->ty0n * p->tz0n * ((p->n_shots + 1) / 2), p->nchunks, 1);  // shot pairs
     const float inv_dt2 = (float)(1.0 / (p->d.dt * p->d.dt));
     const double h = std::max(p->d.spacing[0], std::max(p->d.spacing[1], p->d.spacing[2]));
     const float src_scale = (float)(2.0 * p->d.dt / h);
