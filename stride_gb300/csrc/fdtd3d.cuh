@@ -64,13 +64,14 @@ struct Smem3D {
     static constexpr int PY = TY + 2 * R;     // plane rows (y) incl. halo
     static constexpr int PZ = TZ + 2 * R;     // plane row width (z) incl. halo, from z0 - R
     static constexpr int PLANE = PY * PZ;     // float2: the two shots of the pair
-    static constexpr int QU = RB * (PF + 1);  // planes in the ring: this iteration's and the prefetched
+    // planes in the ring (this iteration's and the prefetched), a power of two: slots by mask
+    static constexpr int QU = pow2_at_least(RB * (PF + 1));
     static constexpr int FY = (TY + 9) * TZ;  // y fluxes of one row
     // z fluxes of one row: TZ + 9 per y row, stored at a power-of-two stride so that a flat index
     // splits into (y, z) with a shift and a mask
     static constexpr int WZF = pow2_at_least(TZ + 9);
     static constexpr int FZ = TY * WZF;
-    static constexpr int QG = R + RB;         // rows whose y and z parts wait for their x part
+    static constexpr int QG = pow2_at_least(R + RB);  // slots of the y and z parts waiting for their x part
     static constexpr int oFY = QU * PLANE;
     static constexpr int oFZ = oFY + (STAG ? RB * FY : 0);
     static constexpr int oG = oFZ + (STAG ? RB * FZ : 0);
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
     constexpr int R = L::R, QU = L::QU, PZ = L::PZ, WZF = L::WZF;
     constexpr int QB = STAG ? 9 : 10;  // x queue: rows i - QB .. i + RB - 1
     constexpr int QL = QB + RB;
-    constexpr int QG = L::QG;          // y/z parts: rows i - R .. i + RB - 1, one slot per row
+    constexpr int QG = L::QG;          // y/z parts of rows i - R .. i + RB - 1, one slot per row
 
     extern __shared__ __align__(16) float2 smem2[];
     float2* const sU = smem2;
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
 
     // plane ring: x row r in slot (r - i0) mod QU, kept as a running slot index (sI: row i);
     // element (yy, zz) at [(yy - y0 + R) PZ + zz - z0 + R]
-    auto wrap = [](int s) { return s < 0 ? s + QU : (s >= QU ? s - QU : s); };
+    auto wrap = [](int s) { return s & (QU - 1); };
     auto slotp = [&](int s) { return sU + s * L::PLANE; };
     // the plane elements this thread stages (element tid + q NT): their offset within an x plane
     // of the field, -1 beyond the grid (the same for every row)
@@ -204,14 +205,14 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
         uq[k] = f2(0.f);
         if constexpr (STAG) fq[k] = f2(0.f);
     }
-    auto gwrap = [](int s) { return s < 0 ? s + QG : (s >= QG ? s - QG : s); };
+    auto gwrap = [](int s) { return s & (QG - 1); };
     const bool do_save = FINAL && a.save && (a.t % a.f == 0);
 
 #pragma unroll 1
     for (int k = 0; k < PF; k++) prefetch(i0 + k * RB, k * RB);
 
-    int sI = 0;  // ring slot of row i
-    int gI = 0;  // y/z-part slot of row i (rows i0 .. i0 + R - 1 are never output rows)
+    int sI = 0;  // ring slot of row i (taken mod QU)
+    int gI = 0;  // y/z-part slot of row i (mod QG; rows i0 .. i0 + R - 1 are never output rows)
 #pragma unroll 1
     for (int i = i0; i < i1; i += RB) {
         const int j = i - R;  // output row of this iteration's first input row
@@ -346,8 +347,8 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
                 if (hasB) a.prev[offB + idx] = pn.y;
             }
         }
-        sI = sI + RB >= QU ? sI + RB - QU : sI + RB;
-        gI = gwrap(gI + RB);
+        sI += RB;
+        gI += RB;
     }
     cp_async_wait<0>();
 }

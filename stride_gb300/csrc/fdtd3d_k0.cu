@@ -6,7 +6,7 @@
 namespace sa {
 
 namespace {
-constexpr int TY = kTile3dY, TZ = kTile3dZ, RB = 2, PF = 1;
+constexpr int TY = kTile3dY, TZ = kTile3dZ, RB = kRows3d, PF = kPrefetch3d;
 
 template <bool FINAL, bool OT4>
 cudaError_t go(dim3 grid, cudaStream_t s, const Step3D& a) {

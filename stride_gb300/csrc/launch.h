@@ -18,6 +18,13 @@ cudaError_t launch_step3d_k2(bool final_pass, bool ot4, dim3 grid, cudaStream_t 
 #define SA_TZ3 32
 #endif
 constexpr int kTile3dY = SA_TY3, kTile3dZ = SA_TZ3;  // (y, z) tile of a 3D CTA (threads = their product)
+#ifndef SA_RB3
+#define SA_RB3 2
+#endif
+#ifndef SA_PF3
+#define SA_PF3 1
+#endif
+constexpr int kRows3d = SA_RB3, kPrefetch3d = SA_PF3;  // x rows per iteration of a 3D pass, iterations prefetched
 
 inline cudaError_t launch_step3d(int kind, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a) {
     switch (kind) {
