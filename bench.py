@@ -561,7 +561,7 @@ def gb300_arm(args):
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded phantoms)',
             'config': {'workload': workload_name(args.workload, nt), 'grid': list(w['shape']),
                        'shots_per_gpu': n_shots, 'nt': nt, 'kernel': 'OT4',
-                       'layout': dict(zip(('threads', 'strips', 'chunks'), plan.layout)),
+                       'layout': dict(zip(('threads', 'strips' if dim == 2 else 'tiles', 'chunks'), plan.layout)),
                        'gradient': (method + (' (adjoint time includes the forward recompute from checkpoints)'
                                               if method != 'snapshots' else '')) if grad_mode else None,
                        'parallelism': 'shots sharded over %d GPU(s)%s' % (world, ', gradient all-reduce' if grad_mode else ''),

@@ -160,10 +160,15 @@ int sa_adjoint_wavelets(sa_plan* plan, const float* residuals, float* grad_vp, f
 int sa_adjoint_grads(sa_plan* plan, const float* residuals, float* grad_vp, float* prec_vp, float* grad_rho,
                      float* prec_rho, float* grad_wavelets, void* stream);
 
-/* Picks the CTA width and row chunking for the current geometry by timing the candidates
- * (no counterpart in the reference, whose Devito autotuner is optional: common/devito.py:1043).
- * It steps the plan's wavefield buffers, so it returns SA_E_INVALID while a saved wavefield
- * (snapshots or checkpoints of a forward with save) waits for its adjoint. */
+/* Picks the launch layout for the current geometry by timing the candidates (no counterpart in
+ * the reference, whose Devito autotuner is optional: common/devito.py:1043). 2D: the CTA width
+ * and row chunking of the passes, and the time-blocking depth of forwards without a saved
+ * wavefield (one step per launch, or every step in the persistent launch when SA_OPT_PERSISTENT
+ * is automatic). 3D: the (y, z) tile and x chunking. Results are cached per grid, operator,
+ * batch and device for the life of the process, so a second plan of the same shape takes them
+ * without timing. It steps the plan's wavefield buffers, so it returns SA_E_INVALID while a
+ * saved wavefield (snapshots or checkpoints of a forward with save) waits for its adjoint; a 3D
+ * plan refuses while its saved wavefield is held. */
 int sa_autotune(sa_plan* plan, void* stream);
 
 /* Single-shot 2D forward modelling that allocates no device memory (no counterpart in the
@@ -302,9 +307,10 @@ long long sa_launch_count(const sa_plan* plan);
 /* Sets a plan option (SA_OPT_*). No counterpart in the reference. */
 int sa_plan_option(sa_plan* plan, int option, long long value);
 
-/* The launch layout of a 2D plan's time-step passes (after sa_autotune, the tuned one): threads
- * per CTA (two grid columns each), column strips and row chunks of the grid; 3D plans report
- * their fixed tile as threads and 0 strips and chunks. No counterpart in the reference. */
+/* The launch layout of a plan's time-step passes (after sa_autotune, the tuned one). 2D: threads
+ * per CTA (two grid columns each), column strips and row chunks of the grid. 3D: threads per CTA
+ * (one (y, z) column each, two shots per thread), (y, z) tiles and x chunks. No counterpart in the
+ * reference. */
 int sa_plan_layout(const sa_plan* plan, int* threads, int* strips, int* chunks);
 
 /* The checkpoint schedule sa_forward(SA_SAVE_CHECKPOINTS) takes for n_shots shots of a plan with

@@ -6,9 +6,9 @@
 namespace sa {
 
 namespace {
-constexpr int TY = kTile3dY, TZ = kTile3dZ, RB = kRows3d, PF = kPrefetch3d;
+constexpr int RB = kRows3d, PF = kPrefetch3d;
 
-template <bool FINAL, bool OT4>
+template <int TY, int TZ, bool FINAL, bool OT4>
 cudaError_t go(dim3 grid, cudaStream_t s, const Step3D& a) {
     constexpr size_t bytes = Smem3D<1, TY, TZ, RB, PF>::bytes;
     static bool configured = false;
@@ -21,11 +21,18 @@ cudaError_t go(dim3 grid, cudaStream_t s, const Step3D& a) {
     fdtd3d_pass<1, FINAL, OT4, TY, TZ, RB, PF><<<grid, TY * TZ, bytes, s>>>(a);
     return cudaGetLastError();
 }
+
+template <int TY, int TZ>
+cudaError_t go_tile(bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a) {
+    if (!final_pass) return go<TY, TZ, false, true>(grid, s, a);
+    return ot4 ? go<TY, TZ, true, true>(grid, s, a) : go<TY, TZ, true, false>(grid, s, a);
+}
 }  // namespace
 
-cudaError_t launch_step3d_k1(bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a) {
-    if (!final_pass) return go<false, true>(grid, s, a);
-    return ot4 ? go<true, true>(grid, s, a) : go<true, false>(grid, s, a);
+cudaError_t launch_step3d_k1(int tile, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a) {
+    static_assert(kTiles3dN == 2, "tile list");
+    if (tile == 1) return go_tile<kTiles3d[1].ty, kTiles3d[1].tz>(final_pass, ot4, grid, s, a);
+    return go_tile<kTiles3d[0].ty, kTiles3d[0].tz>(final_pass, ot4, grid, s, a);
 }
 
 }  // namespace sa

@@ -8,16 +8,15 @@ cudaError_t launch_step2d_k1(bool ot4, int nt_threads, dim3 grid, cudaStream_t s
 cudaError_t launch_step2d_k2(bool ot4, int nt_threads, dim3 grid, cudaStream_t s, const Step2D& a);
 
 struct Step3D;
-cudaError_t launch_step3d_k0(bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
-cudaError_t launch_step3d_k1(bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
-cudaError_t launch_step3d_k2(bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
-#ifndef SA_TY3
-#define SA_TY3 16
-#endif
-#ifndef SA_TZ3
-#define SA_TZ3 32
-#endif
-constexpr int kTile3dY = SA_TY3, kTile3dZ = SA_TZ3;  // (y, z) tile of a 3D CTA (threads = their product)
+// (y, z) tiles of a 3D CTA (threads = their product), chosen per plan (sa_autotune measures them)
+struct Tile3D {
+    int ty, tz;
+};
+constexpr Tile3D kTiles3d[] = {{16, 32}, {8, 64}};
+constexpr int kTiles3dN = 2;
+cudaError_t launch_step3d_k0(int tile, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
+cudaError_t launch_step3d_k1(int tile, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
+cudaError_t launch_step3d_k2(int tile, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
 #ifndef SA_RB3
 #define SA_RB3 2
 #endif
@@ -26,11 +25,12 @@ constexpr int kTile3dY = SA_TY3, kTile3dZ = SA_TZ3;  // (y, z) tile of a 3D CTA 
 #endif
 constexpr int kRows3d = SA_RB3, kPrefetch3d = SA_PF3;  // x rows per iteration of a 3D pass, iterations prefetched
 
-inline cudaError_t launch_step3d(int kind, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a) {
+inline cudaError_t launch_step3d(int kind, int tile, bool final_pass, bool ot4, dim3 grid, cudaStream_t s,
+                                 const Step3D& a) {
     switch (kind) {
-        case 0: return launch_step3d_k0(final_pass, ot4, grid, s, a);
-        case 1: return launch_step3d_k1(final_pass, ot4, grid, s, a);
-        default: return launch_step3d_k2(final_pass, ot4, grid, s, a);
+        case 0: return launch_step3d_k0(tile, final_pass, ot4, grid, s, a);
+        case 1: return launch_step3d_k1(tile, final_pass, ot4, grid, s, a);
+        default: return launch_step3d_k2(tile, final_pass, ot4, grid, s, a);
     }
 }
 

@@ -6,6 +6,9 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <map>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "../../include/strideacc.h"
@@ -189,9 +192,28 @@ struct Plan3D {
     size_t cap_pml_ck = 0;
     long long launches = 0;
     int chunk_rows = 0, nchunks = 1, ty0n = 1, tz0n = 1;
+    int tile = 0;               // kTiles3d entry of the passes
+    bool layout_fixed = false;  // tile and chunks chosen by sa_autotune (kept across geometries)
 };
 
 long long plan3d_launches(const Plan3D* p) { return p->launches; }
+
+static void set_tile(Plan3D* p, int tile) {
+    p->tile = tile;
+    p->ty0n = (p->ny + kTiles3d[tile].ty - 1) / kTiles3d[tile].ty;
+    p->tz0n = (p->nz + kTiles3d[tile].tz - 1) / kTiles3d[tile].tz;
+}
+
+// x chunks of the passes: enough CTAs for four per SM, each chunk at least 4 R rows deep
+static void set_chunks(Plan3D* p, int nchunks) {
+    p->chunk_rows = (p->nx + nchunks - 1) / nchunks;
+    p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
+}
+static int default_chunks(const Plan3D* p, int n_shots) {
+    const int R = p->kind == 0 ? 5 : 9;
+    const int ctas = p->ty0n * p->tz0n * ((n_shots + 1) / 2);
+    return std::max(1, std::min((152 * 4 + ctas - 1) / ctas, p->nx / (4 * R)));
+}
 
 int plan3d_create(const sa_desc& d, Plan3D** out) {
     *out = nullptr;
@@ -243,8 +265,7 @@ int plan3d_create(const sa_desc& d, Plan3D** out) {
         plan3d_destroy(p);
         return rc;
     }
-    p->ty0n = (p->ny + kTile3dY - 1) / kTile3dY;
-    p->tz0n = (p->nz + kTile3dZ - 1) / kTile3dZ;
+    set_tile(p, 0);
     *out = p;
     return SA_OK;
 }
@@ -451,11 +472,7 @@ int plan3d_set_geometry(Plan3D* p, int n_shots, const int* so, const float* sx, 
     p->n_rec = ro_[n_shots];
     if ((rc = alloc3(&p->src_amp, (size_t)p->d.nt * std::max(1, p->n_src))) != SA_OK) return rc;
     if ((rc = alloc3(&p->rec_amp, (size_t)p->d.nt * std::max(1, p->n_rec))) != SA_OK) return rc;
-    const int R = p->kind == 0 ? 5 : 9;
-    const int ctas = p->ty0n * p->tz0n * ((n_shots + 1) / 2);
-    p->nchunks = std::max(1, std::min((152 * 4 + ctas - 1) / ctas, p->nx / (4 * R)));
-    p->chunk_rows = (p->nx + p->nchunks - 1) / p->nchunks;
-    p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
+    if (!p->layout_fixed) set_chunks(p, default_chunks(p, n_shots));
     p->geometry_set = true;
     p->snaps_valid = false;
     p->ckpt_valid = false;
@@ -546,13 +563,13 @@ static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, int which,
     if (p->ot4) {
         a.in = cur;
         a.out_l = p->Lbuf;
-        CK3(launch_step3d(p->kind, false, true, grid, s, a));
+        CK3(launch_step3d(p->kind, p->tile, false, true, grid, s, a));
         a.in = p->Lbuf;
         n++;
     } else {
         a.in = cur;
     }
-    CK3(launch_step3d(p->kind, true, p->ot4, grid, s, a));
+    CK3(launch_step3d(p->kind, p->tile, true, p->ot4, grid, s, a));
     n++;
     const float inv_dt2 = (float)(1.0 / ((double)a.dt * (double)a.dt));
     if (p->pml) {  // auxiliary fields and the boundary term of the new level (which 1: the adjoint)
@@ -1015,11 +1032,11 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
                 la.t = t - 1;
                 la.cur = la.in = lvl(k, t - 1);
                 la.prev = p->Lu;
-                CK3(launch_step3d(p->kind, true, false, grid, s, la));
+                CK3(launch_step3d(p->kind, p->tile, true, false, grid, s, la));
                 la.t = t;
                 la.cur = la.in = zt;
                 la.prev = p->Lz;
-                CK3(launch_step3d(p->kind, true, false, grid, s, la));
+                CK3(launch_step3d(p->kind, p->tile, true, false, grid, s, la));
                 Lu = p->Lu;
                 Lz = p->Lz;
                 n += 2;
@@ -1058,6 +1075,96 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
         n++;
     }
     p->launches = n;
+    return SA_OK;
+}
+
+// Layout search of a 3D plan: every tile of kTiles3d with the x chunkings that keep chunks at least
+// 4 R rows deep, each timed over a few steps of the two passes on the plan's own wavefield buffers
+// (their contents are overwritten); the fastest is kept. Results are remembered per (grid, operator,
+// shots, device) for the life of the process.
+int plan3d_autotune(Plan3D* p, const char* device_key, int* tile_out, int* chunks_out, bool* cached, cudaStream_t s) {
+    if (!p->medium_set || !p->geometry_set) return fail3(SA_E_INVALID, "autotune needs medium and geometry");
+    if (p->snaps_valid || p->ckpt_valid)
+        return fail3(SA_E_INVALID, "autotune would overwrite the saved wavefield: run it before the saving forward");
+    char key[256];
+    snprintf(key, sizeof(key), "3d:%d,%d,%d:k%d:%s:s%d:%s", p->nx, p->ny, p->nz, p->kind, p->ot4 ? "ot4" : "ot2",
+             p->n_shots, device_key);
+    static std::map<std::string, std::pair<int, int>> cache;
+    static std::mutex mu;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) {
+            set_tile(p, it->second.first);
+            set_chunks(p, it->second.second);
+            p->layout_fixed = true;
+            *tile_out = p->tile;
+            *chunks_out = p->nchunks;
+            *cached = true;
+            return SA_OK;
+        }
+    }
+    const int R = p->kind == 0 ? 5 : 9;
+    const int steps = std::min(6, p->d.nt - 2);
+    cudaEvent_t e0, e1;
+    CK3(cudaEventCreate(&e0));
+    CK3(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bt = p->tile, bc = p->nchunks;
+    for (int tile = 0; tile < kTiles3dN; tile++) {
+        set_tile(p, tile);
+        for (int nc : {1, 2, 3, 4, 6, 8}) {
+            if (p->nx / nc < 4 * R) continue;
+            set_chunks(p, nc);
+            Step3D a = args3(p);
+            a.save = 0;
+            const dim3 grid(p->ty0n * p->tz0n * ((p->n_shots + 1) / 2), p->nchunks, 1);
+            int rc = SA_OK;
+            for (int t = 0; t < 2 + steps && rc == SA_OK; t++) {
+                if (t == 2) CK3(cudaEventRecord(e0, s));
+                a.t = 1 + t;
+                a.cur = p->F[t & 1];
+                a.prev = p->F[(t + 1) & 1];
+                if (p->ot4) {
+                    a.in = a.cur;
+                    a.out_l = p->Lbuf;
+                    CK3(launch_step3d(p->kind, p->tile, false, true, grid, s, a));
+                    a.in = p->Lbuf;
+                } else {
+                    a.in = a.cur;
+                }
+                CK3(launch_step3d(p->kind, p->tile, true, p->ot4, grid, s, a));
+            }
+            CK3(cudaEventRecord(e1, s));
+            CK3(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CK3(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                bt = tile;
+                bc = p->nchunks;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    set_tile(p, bt);
+    set_chunks(p, bc);
+    p->layout_fixed = true;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        cache[key] = {bt, bc};
+    }
+    *tile_out = bt;
+    *chunks_out = p->nchunks;
+    *cached = false;
+    return SA_OK;
+}
+
+int plan3d_layout(const Plan3D* p, int* threads, int* tiles, int* chunks) {
+    *threads = kTiles3d[p->tile].ty * kTiles3d[p->tile].tz;
+    *tiles = p->ty0n * p->tz0n;
+    *chunks = p->nchunks;
     return SA_OK;
 }
 

@@ -20,6 +20,11 @@ int plan3d_adjoint(Plan3D* p, const float* residuals, float* grad, float* prec, 
 // dL/dvp of the discrete forward map at every point, prec the sum over all steps of p.dt2^2.
 int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* prec, cudaStream_t s);
 long long plan3d_launches(const Plan3D* p);
+// Layout search (tile of kTiles3d and x chunks) of a 3D plan; device_key names the GPU for the
+// process-wide cache of results.
+int plan3d_autotune(Plan3D* p, const char* device_key, int* tile, int* chunks, bool* cached, cudaStream_t s);
+// The passes' layout: threads per CTA (the tile's columns), (y, z) tiles, x chunks.
+int plan3d_layout(const Plan3D* p, int* threads, int* tiles, int* chunks);
 // Checkpoint interval K (a multiple of f) and the number of stored checkpoints for a plan whose
 // two state levels take `level_bytes` (SA_SAVE_CHECKPOINTS, both dimensions).
 int choose_checkpoints(const sa_desc& d, double level_bytes, int* K, int* n_ckpt, double ck_levels = 2,

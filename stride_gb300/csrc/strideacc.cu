@@ -4,6 +4,7 @@
 // wavefield of the reference's gradient algorithm and per-shot gradient accumulators. The
 // time loop is captured once into a CUDA graph per mode and replayed.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -11,6 +12,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -202,6 +205,7 @@ struct sa_plan {
     // persistent forward of small batches (persist2d.cu): mode (-1 never, 0 automatic, 1 whenever
     // eligible), the tests' barrier knobs, its tile layout and device state
     int persist_mode = 0;
+    int persist_tuned = -1;  // the autotuner's choice for automatic mode: -1 none, 0 streaming, 1 persistent
     int persist_extra = 0;
     long long persist_spin = 10000000;
     int ptx = 0, pty = 0, ptiles_x = 0, ptiles_y = 0, pblocks = 0;
@@ -1028,15 +1032,22 @@ bool persist_layout(sa_plan* p) {
     return best >= 0;
 }
 
+bool persist_eligible(const sa_plan* p) {
+    return p->d.interpolation == SA_INTERP_LINEAR && p->d.boundary == SA_BOUNDARY_SPONGE;
+}
+
+// Automatic mode: the autotuner's measurement when it took one, else small batches only.
 bool use_persistent(sa_plan* p, int save_mode) {
-    if (p->persist_mode < 0 || save_mode != SA_SAVE_NONE || p->d.interpolation != SA_INTERP_LINEAR ||
-        p->d.boundary != SA_BOUNDARY_SPONGE)
-        return false;
-    if (p->persist_mode == 0 && (long long)npairs(p) * p->nx * p->ny > 152LL * 4096) return false;
+    if (p->persist_mode < 0 || save_mode != SA_SAVE_NONE || !persist_eligible(p)) return false;
+    if (p->persist_mode == 0) {
+        if (p->persist_tuned == 0) return false;
+        if (p->persist_tuned < 0 && (long long)npairs(p) * p->nx * p->ny > 152LL * 4096) return false;
+    }
     return persist_layout(p);
 }
 
-int forward_persistent(sa_plan* p, cudaStream_t s) {
+// nt_run: steps 1 .. nt_run-2 (the autotuner's short runs); 0 for the plan's nt.
+int forward_persistent(sa_plan* p, cudaStream_t s, int nt_run = 0) {
     // the sources' targets by owning CTA (tile and shot pair of the target point), in target order
     const int ntile = p->ptiles_x * p->ptiles_y;
     std::vector<int> cnt(p->pblocks + 1, 0), tgt(p->stgt.n);
@@ -1081,7 +1092,7 @@ int forward_persistent(sa_plan* p, cudaStream_t s) {
     a.s = base_args(p);
     a.xch = p->pxch;
     a.xch_slot = (long long)slot;
-    a.nt = p->d.nt;
+    a.nt = nt_run > 0 ? std::min(nt_run, p->d.nt) : p->d.nt;
     a.tx = p->ptx;
     a.ty = p->pty;
     a.tiles_x = p->ptiles_x;
@@ -1112,6 +1123,24 @@ int forward_persistent(sa_plan* p, cudaStream_t s) {
                     p->pblocks, a.extra);
     p->launches = 1;
     return SA_OK;
+}
+
+// Results of sa_autotune per (grid, operator, batch, device), for the life of the process:
+// {strips, row chunks, time-blocking choice}.
+std::map<std::string, std::array<int, 3>> g_tune;
+std::mutex g_tune_mu;
+
+// The current device's name and SM count (the autotuner caches' device component).
+std::string device_key() {
+    int dev = 0;
+    cudaDeviceProp pr{};
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&pr, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return "unknown";
+    }
+    char b[320];
+    snprintf(b, sizeof(b), "%s/%d", pr.name, pr.multiProcessorCount);
+    return b;
 }
 
 int ensure_fields(sa_plan* p) {
@@ -1161,11 +1190,7 @@ int sa_plan_option(sa_plan* p, int option, long long value) {
 
 int sa_plan_layout(const sa_plan* p, int* threads, int* strips, int* chunks) {
     if (!p || !threads || !strips || !chunks) return fail(SA_E_INVALID, "null argument");
-    if (p->p3) {
-        *threads = sa::kTile3dY * sa::kTile3dZ;
-        *strips = *chunks = 0;
-        return SA_OK;
-    }
+    if (p->p3) return sa::plan3d_layout(p->p3, threads, strips, chunks);
     *threads = p->NT;
     *strips = p->nstrips;
     *chunks = p->nchunks;
@@ -1649,12 +1674,37 @@ int adjoint_impl(sa_plan* p, const float* residuals, float* grad_vp, float* prec
 }  // namespace
 
 int sa_autotune(sa_plan* p, void* stream) {
-    if (p && p->p3) return SA_OK;  // 3D plans use a fixed tile (kTile3dY x kTile3dZ columns per CTA)
-    if (!p || !p->geometry_set || !p->medium_set) return fail(SA_E_INVALID, "autotune needs medium and geometry");
+    if (!p) return fail(SA_E_INVALID, "null plan");
+    const std::string dev = device_key();
+    if (p->p3) {
+        int tile = 0, chunks = 0;
+        bool cached = false;
+        return sa::plan3d_autotune(p->p3, dev.c_str(), &tile, &chunks, &cached, (cudaStream_t)stream);
+    }
+    if (!p->geometry_set || !p->medium_set) return fail(SA_E_INVALID, "autotune needs medium and geometry");
     if (p->adjoint_pending && (p->snaps_valid || p->ckpt_valid))
         return fail(SA_E_INVALID, "autotune between a saving forward and its adjoint would discard the saved "
                                   "wavefield: run the adjoint first");
     cudaStream_t s = (cudaStream_t)stream;
+    char key[256];
+    snprintf(key, sizeof(key), "2d:%d,%d:k%d:%s:p%d:%s", p->nx, p->ny, p->kind, p->ot4 ? "ot4" : "ot2", npairs(p),
+             dev.c_str());
+    {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            p->layout_fixed = true;
+            drop_graphs(p);
+            set_strips(p, it->second[0]);
+            p->chunk_rows = (p->nx + it->second[1] - 1) / it->second[1];
+            p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
+            p->persist_tuned = it->second[2];
+            CKR(build_lists(p));
+            p->snaps_valid = false;
+            p->ckpt_valid = false;
+            return SA_OK;
+        }
+    }
     struct Cand {
         int strips, nchunks;
     };
@@ -1710,12 +1760,30 @@ int sa_autotune(sa_plan* p, void* stream) {
             bc = c;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     set_strips(p, bc.strips);
     p->chunk_rows = (p->nx + bc.nchunks - 1) / bc.nchunks;
     p->nchunks = (p->nx + p->chunk_rows - 1) / p->chunk_rows;
     CKR(build_lists(p));
+    // time-blocking depth of a forward without a saved wavefield: one step per launch (the passes
+    // above) or every step in one launch (the persistent kernel), per step over a short run
+    p->persist_tuned = -1;
+    if (persist_eligible(p) && persist_layout(p)) {
+        const int nrun = std::min(p->d.nt, steps + 2);
+        CKR(forward_persistent(p, s, nrun));  // warm-up: kernel configuration, tables
+        CK(cudaEventRecord(e0, s));
+        CKR(forward_persistent(p, s, nrun));
+        CK(cudaEventRecord(e1, s));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        p->persist_tuned = ms < best ? 1 : 0;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        g_tune[key] = {bc.strips, bc.nchunks, p->persist_tuned};
+    }
     p->snaps_valid = false;
     p->ckpt_valid = false;
     return SA_OK;

@@ -315,3 +315,26 @@ def test_exact_gradient_hicks_3d(interp):
     assert np.abs(ref).max() > 0
     assert C.cosine(g, ref) >= 0.9999
     assert C.rel_l2(g, ref) <= 2e-3
+
+
+def test_autotune_3d_layout_and_cache():
+    """sa_autotune on a 3D plan picks a tile and x chunking by timing them; every point's arithmetic
+    is the same in any layout, so the traces are bitwise unchanged, and a second plan of the same
+    shape takes the cached layout."""
+    c = case3d(kernel='OT4', density='variable', alpha=True, n_shots=3, nt=60)
+    plan = make_plan3(c)
+    before, _ = C.gpu_forward(c, plan=plan)
+    plan.autotune()
+    tuned = plan.layout
+    after, _ = C.gpu_forward(c, plan=plan)
+    for a, b in zip(before, after):
+        assert np.array_equal(a, b)
+    twin = make_plan3(c)
+    C.gpu_forward(c, plan=twin)
+    twin.autotune()
+    assert twin.layout == tuned
+    C.gpu_forward(c, plan=twin, save=True)
+    with pytest.raises(_lib.StrideAccError) as e:  # the saved wavefield would be overwritten
+        twin.autotune()
+    assert e.value.code == _lib.SA_E_INVALID
+

@@ -97,6 +97,25 @@ def test_new_geometry_and_layout_independence():
         assert np.array_equal(a, d)  # every point's arithmetic is the same in any launch shape
 
 
+def test_autotune_cache_and_time_blocking_choice():
+    """A second plan of the same shape takes the first one's tuned layout from the process cache;
+    a single-shot plan, whose batch is too small for the streaming passes, is tuned to the
+    persistent launch (every step in one launch) and its traces are unchanged bitwise."""
+    c = C.small_case(kernel='OT4', density='variable', alpha=True, n_shots=1, nt=200)
+    plan = C.make_plan(c)
+    plan.set_option(_lib.SA_OPT_PERSISTENT, -1)
+    streaming, _ = C.gpu_forward(c, plan=plan)
+    plan.set_option(_lib.SA_OPT_PERSISTENT, 0)
+    plan.autotune()
+    tuned, _ = C.gpu_forward(c, plan=plan)
+    assert plan.launches <= 3  # the persistent launch won
+    assert np.array_equal(tuned[0], streaming[0])
+    twin = C.make_plan(c)
+    C.gpu_forward(c, plan=twin)
+    twin.autotune()
+    assert twin.layout == plan.layout
+
+
 def test_autotune_refuses_to_discard_a_saved_wavefield():
     """sa_autotune steps the plan's wavefield buffers: between a saving forward and its adjoint it
     returns SA_E_INVALID and the saved wavefield still gives the untuned gradient."""
