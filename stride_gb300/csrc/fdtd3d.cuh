@@ -67,9 +67,8 @@ struct Smem3D {
     // planes in the ring (this iteration's and the prefetched), a power of two: slots by mask
     static constexpr int QU = pow2_at_least(RB * (PF + 1));
     static constexpr int FY = (TY + 9) * TZ;  // y fluxes of one row
-    // z fluxes of one row: TZ + 9 per y row, stored at a power-of-two stride so that a flat index
-    // splits into (y, z) with a shift and a mask
-    static constexpr int WZF = pow2_at_least(TZ + 9);
+    // z fluxes of one row: TZ + 9 per y row, densely (every lane of a warp holds one)
+    static constexpr int WZF = TZ + 9;
     static constexpr int FZ = TY * WZF;
     static constexpr int QG = pow2_at_least(R + RB);  // slots of the y and z parts waiting for their x part
     static constexpr int oFY = QU * PLANE;
@@ -192,7 +191,7 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
 #pragma unroll
         for (int q = 0; q < KZ; q++) {
             const int k = tid + q * NT;
-            const int ky = min(k / WZF, TY - 1), kz = k % WZF;
+            const int ky = min(k / WZF, TY - 1), kz = k % WZF;  // (k beyond the row's fluxes: clamped, unused)
             bzo[q] = min(y0 + ky, a.ny - 1) * a.zpb + min(max(z0 - 5 + kz + 6, 0), a.zpb - 1);
         }
     }
@@ -271,7 +270,7 @@ __global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ St
                 for (int q = 0; q < KZ; q++) {
                     const int k = tid + q * NT;
                     const int ky = k / WZF, kz = k % WZF;
-                    if (ky < TY && kz < TZ + 9) {
+                    if (k < L::FZ) {
                         const int base = (ky + R) * PZ + (kz - 5 + R);  // half column z0 - 5 + kz (+1/2)
                         float2 v = mul2(dstag2(pl, base + 1, base, 1), f2(ihz));
                         if constexpr (VARB) v = mul2(v, f2(bzv[r][q]));
