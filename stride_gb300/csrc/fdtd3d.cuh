@@ -102,7 +102,7 @@ __device__ __forceinline__ float2 dcent2(const A& v, int c, int stride) {
 }
 
 template <int KIND, bool FINAL, bool OT4, int TY, int TZ, int RB, int PF>
-__global__ void __launch_bounds__(TY* TZ) fdtd3d_pass(const __grid_constant__ Step3D a) {
+__global__ void __launch_bounds__(TY* TZ, TY* TZ <= 256 ? 2 : 1) fdtd3d_pass(const __grid_constant__ Step3D a) {
     using L = Smem3D<KIND, TY, TZ, RB, PF>;
     constexpr int NT = TY * TZ;
     constexpr bool STAG = L::STAG, VARB = KIND == 1;

@@ -12,7 +12,7 @@ struct Step3D;
 struct Tile3D {
     int ty, tz;
 };
-constexpr Tile3D kTiles3d[] = {{16, 32}, {8, 64}};
+constexpr Tile3D kTiles3d[] = {{16, 32}, {8, 32}};
 constexpr int kTiles3dN = 2;
 cudaError_t launch_step3d_k0(int tile, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
 cudaError_t launch_step3d_k1(int tile, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
