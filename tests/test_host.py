@@ -33,7 +33,6 @@ def test_kernel_selection_matches_reference_rule():
     (dict(boundary_type='nonsense'), ValueError),
     (dict(boundary_type='complex_frequency_shift_PML_2'), NotImplementedError),
     (dict(interpolation_type='cubic'), ValueError),
-    (dict(interpolation_type='sinc'), NotImplementedError),
     (dict(kernel='OT6'), ValueError),
     (dict(checkpoint_interval=-4), ValueError),
     (dict(checkpoint_interval=2.5), ValueError),
@@ -43,6 +42,13 @@ def test_option_errors(kw, exc):
     pde, shot, sub, vp, grid = _setup()
     with pytest.raises(exc):
         pde._check_problem(shot.wavelets, vp, problem=sub, **kw)
+
+
+def test_sinc_interpolation_is_accepted():
+    """interpolation_type='sinc' (common/devito.py:634-638) is accepted and kept."""
+    pde, shot, sub, vp, grid = _setup()
+    pde._check_problem(shot.wavelets, vp, problem=sub, interpolation_type='sinc')
+    assert pde.interpolation_type == 'sinc'
 
 
 def test_cfs_pml_runs_with_ot2_in_2d():
