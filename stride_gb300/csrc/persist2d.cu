@@ -379,14 +379,14 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
         // otherwise the new level waits in sN for the sources and the stencil's last reads of p[t]
         const bool direct = OT4 && slots;
         if constexpr (OT4) {
-            stencil_region<KIND, 4>(a, sU, ux0, uy0, uw, lx0, x1 + HL, ly0, y1 + HL, sFX, sFY, B,
+            stencil_region<KIND, PERSIST_NR1>(a, sU, ux0, uy0, uw, lx0, x1 + HL, ly0, y1 + HL, sFX, sFY, B,
                                     [&](int x, int y, float2 g) {
                                         const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
                                         const float W = sW[(x - lx0) * lw + (y - ly0)];
                                         sL[(x - lx0) * lw + (y - ly0)] = in ? mul2(f2(W), g) : f2(0.f);
                                     });
             __syncthreads();
-            stencil_region<KIND, 2>(a, sL, lx0, ly0, lw, x0, x1, y0, y1, sFX, sFY, B, [&](int x, int y, float2 g) {
+            stencil_region<KIND, PERSIST_NR2>(a, sL, lx0, ly0, lw, x0, x1, y0, y1, sFX, sFY, B, [&](int x, int y, float2 g) {
                 const int k = (x - x0) * ty + (y - y0);
                 const float4 c = sC[k];
                 const float2 v = update(k, c, x, y, fma2(f2(c.w), g, sL[(x - lx0) * lw + (y - ly0)]));

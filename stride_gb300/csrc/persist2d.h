@@ -9,6 +9,13 @@ namespace sa {
 #define SA_PERSIST_THREADS 384
 #endif
 constexpr int PERSIST_THREADS = SA_PERSIST_THREADS;
+// rows of one column a thread computes in the first (l) and the second (update) stencil stage
+#ifndef PERSIST_NR1
+#define PERSIST_NR1 4
+#endif
+#ifndef PERSIST_NR2
+#define PERSIST_NR2 2
+#endif
 // shared-memory slots of a CTA's source values at a step: a CTA with more targets adds them to
 // the new level in a pass of its own
 constexpr int PERSIST_SRC_SLOTS = 64;
