@@ -228,6 +228,7 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
     const int mp = a.mpitch, pitch = a.pitch;
     const int ux0 = x0 - HU, uy0 = y0 - HU, uh = th + 2 * HU, uwr = tw + 2 * HU;
     const int lx0 = x0 - HL, ly0 = y0 - HL, lh = th + 2 * HL, lwr = tw + 2 * HL;
+    const bool inner = lx0 >= 0 && lx0 + lh <= a.nx && ly0 >= 0 && ly0 + lwr <= a.ny;  // stage-1 region in the grid
     const int sb = P.cta_off[b], ns = P.cta_off[b + 1] - sb;  // this CTA's source targets
     const int rb = P.rec_off[b], nr = P.rec_off[b + 1] - rb;  // and receivers
     const bool slots = ns <= PERSIST_SRC_SLOTS;  // sources added in the update (else through sN)
@@ -260,12 +261,17 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
     }
     for (int e = tid; e < uh * uwr; e += NTH) sU[(e / uwr) * uw + e % uwr] = f2(0.f);
     __shared__ int nhal_s;
-    if (tid == 0) nhal_s = 0;
-    __syncthreads();
-    for (int e = tid; e < uh * uwr; e += NTH) {  // in-grid points of the halo, in any order
-        const int xr = e / uwr, yr = e % uwr, x = ux0 + xr, y = uy0 + yr;
-        const bool tile = x >= x0 && x < x1 && y >= y0 && y < y1;
-        if (!tile && x >= 0 && x < a.nx && y >= 0 && y < a.ny) sHal[atomicAdd(&nhal_s, 1)] = xr | yr << 8;
+    if (tid < 32) {  // the in-grid points of the halo in row-major order (warp 0, by ballot)
+        int cnt = 0;
+        for (int e0 = 0; e0 < uh * uwr; e0 += 32) {
+            const int e = e0 + tid, xr = e / uwr, yr = e % uwr, x = ux0 + xr, y = uy0 + yr;
+            const bool tile = x >= x0 && x < x1 && y >= y0 && y < y1;
+            const bool v = e < uh * uwr && !tile && x >= 0 && x < a.nx && y >= 0 && y < a.ny;
+            const unsigned m = __ballot_sync(0xffffffffu, v);
+            if (v) sHal[cnt + __popc(m & ((1u << tid) - 1u))] = xr | yr << 8;
+            cnt += __popc(m);
+        }
+        if (tid == 0) nhal_s = cnt;
     }
     if (slots)
         for (int j = tid; j < ns; j += NTH) {  // the slot of each target at its point and lane
@@ -381,7 +387,7 @@ __global__ void __launch_bounds__(PERSIST_THREADS) fdtd2d_persist(const __grid_c
         if constexpr (OT4) {
             stencil_region<KIND, PERSIST_NR1>(a, sU, ux0, uy0, uw, lx0, x1 + HL, ly0, y1 + HL, sFX, sFY, B,
                                     [&](int x, int y, float2 g) {
-                                        const bool in = x >= 0 && x < a.nx && y >= 0 && y < a.ny;
+                                        const bool in = inner || (x >= 0 && x < a.nx && y >= 0 && y < a.ny);
                                         const float W = sW[(x - lx0) * lw + (y - ly0)];
                                         sL[(x - lx0) * lw + (y - ly0)] = in ? mul2(f2(W), g) : f2(0.f);
                                     });
