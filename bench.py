@@ -279,10 +279,21 @@ def fwi_arm(args):
     from stride_gb300.fwi import LearnedFWI, PlainFWI, generate_pairs, run_to_error, train_unet
     from stride_gb300.unet import UNet
     torch.cuda.set_device(0)
-    step, target, fmax = args.fwi_step, args.fwi_target, 0.5e6
+    target, fmax = args.fwi_target, 0.5e6
     w0 = _fwi_workload(1000)
+    plain = PlainFWI(w0, step_size=1.0)
+    # the plain step size: the fastest to the target on two validation seeds (outside the training
+    # and test seeds), ties broken by the final error; both methods then use it
+    sweep = {}
+    for st in [float(v) for v in args.fwi_steps.split(',')]:
+        plain.set_step_size(st)
+        res = [run_to_error(plain, _fwi_workload(2000 + i)['vp'], target, max_iter=args.fwi_iters, f_max=fmax)
+               for i in range(2)]
+        sweep[st] = (statistics.median([r[0] if r[0] is not None else float('inf') for r in res]),
+                     float(np.mean([r[2][-1] for r in res])))
+    step = min(sweep, key=lambda st: sweep[st])
+    plain.set_step_size(step)
     t0 = time.perf_counter()
-    plain = PlainFWI(w0, step_size=step)
     X, T = generate_pairs(plain, [_fwi_workload(1000 + i)['vp'] for i in range(args.fwi_train)], iterations=5,
                           f_max=fmax)
     torch.cuda.synchronize()
@@ -330,6 +341,8 @@ def fwi_arm(args):
         'warmup': 0, 'ms_per_step': None, 'higher_is_better': False, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32 solver, bf16 network', 'data': 'synthetic (seeded ellipse phantoms)',
         'config': {'workload': WORKLOAD_NAMES['fwi'], 'target_error': target, 'step_size': step,
+                   'step_sweep': {str(k): {'median_s_to_target': v[0], 'mean_final_error': v[1]}
+                                  for k, v in sweep.items()},
                    'train_phantoms': args.fwi_train, 'pairs': int(X.shape[0]), 'epochs': args.fwi_epochs,
                    'test_phantoms': args.fwi_test, 'max_iterations': args.fwi_iters},
         'plain_median_s': med('plain_s'), 'learned_median_s': med('learned_s'),
@@ -638,8 +651,8 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--fwi-train', type=int, default=48, help='training phantoms (fwi workload)')
     ap.add_argument('--fwi-epochs', type=int, default=15)
-    ap.add_argument('--fwi-test', type=int, default=4, help='test phantoms (fwi workload)')
-    ap.add_argument('--fwi-step', type=float, default=2.0)
+    ap.add_argument('--fwi-test', type=int, default=16, help='test phantoms (fwi workload)')
+    ap.add_argument('--fwi-steps', default='1,2,4', help='plain step sizes swept on validation seeds (fwi workload)')
     ap.add_argument('--fwi-target', type=float, default=0.01)
     ap.add_argument('--fwi-iters', type=int, default=25)
     args = ap.parse_args()

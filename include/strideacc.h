@@ -259,8 +259,10 @@ int sa_field_apply_prec(float* grad, float* prec, long long n, double factor, vo
  * (+ bias[N], then ReLU if relu), A and B bf16 with K contiguous (lda, ldb elements, multiples of
  * 8, 16-byte aligned bases), C fp32 (ldc); Cb (optional, ldcb) receives C as bf16. M multiple of
  * 128, K of 16, N of 32. ksplit > 1 splits K over that many CTAs per tile, which add their partial
- * products into C atomically (accumulate only, no bias/ReLU/Cb). *err (device int) is set to 1 if
- * an internal wait timed out. */
+ * products into C atomically (accumulate 1, no bias/ReLU/Cb), or, with accumulate 2, store them to
+ * slabs C + z M ldc, z < the number of splits (at most ksplit; the caller sums them in a fixed order
+ * with sa_nn_sum_slabs, a reproducible result). *err (device int) is set to 1 if an internal wait
+ * timed out. */
 int sa_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb, int M, int N,
                  int K, const float* bias, int relu, int accumulate, int ksplit, int* err, void* stream);
 
@@ -272,13 +274,18 @@ int sa_nn_im2col(const float* x, int ldx, int B, int H, int W, int Cin, void* co
 /* dx (= or +=) the gather of dcol fp32 [B*H*W][Kp] back to the pixels its columns read. */
 int sa_nn_col2im(const float* dcol, int Kp, int B, int H, int W, int Cin, float* dx, int ldx, int accumulate,
                  void* stream);
+/* out[i] (= or += with accumulate) sum over z < n_slabs, in order, of in[z slab + i], i < n: the
+ * fixed-order reduction of sa_gemm_bf16's split-K slabs. */
+int sa_nn_sum_slabs(const float* in, long long slab, int n_slabs, float* out, long long n, int accumulate,
+                    void* stream);
 /* out[c][r] = in[r][c] (bf16), r < R, c < C; output rows C..Cp-1 are zero. */
 int sa_nn_transpose_bf16(const void* in, int ldi, int R, int C, void* out, int ldo, int Cp, void* stream);
 int sa_nn_to_bf16(const float* x, int ldx, long long rows, int C, void* y, int ldy, void* stream);
 /* dy = 0 where y <= 0 (ReLU backward from the activation output). */
 int sa_nn_relu_bwd(float* dy, int ldd, const float* y, int ldy, long long rows, int C, void* stream);
-/* db[c] = sum over rows of dy[r][c]. */
-int sa_nn_bias_grad(const float* dy, int ldd, long long rows, int C, float* db, void* stream);
+/* db[c] = sum over rows of dy[r][c], summed in a fixed order (reproducible); scratch: device
+ * doubles, 128 * C of them. */
+int sa_nn_bias_grad(const float* dy, int ldd, long long rows, int C, float* db, double* scratch, void* stream);
 /* 2x2 max pooling (H, W of the input, even) and its backward (gradient to the first maximum). */
 int sa_nn_maxpool(const float* x, int ldx, int B, int H, int W, int C, float* y, int ldy, void* stream);
 int sa_nn_maxpool_bwd(const float* x, int ldx, const float* dy, int ldd, int B, int H, int W, int C, float* dx,

@@ -62,7 +62,8 @@ template <int BN, int NS>
 __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restrict__ A, int lda,
                                                    const __nv_bfloat16* __restrict__ B, int ldb, float* C, int ldc,
                                                    __nv_bfloat16* Cb, int ldcb, int K, const float* __restrict__ bias,
-                                                   int relu, int accumulate, int chunks_per_split, int* err) {
+                                                   int relu, int accumulate, int chunks_per_split, long long slab,
+                                                   int* err) {
     constexpr int A_BYTES = kBM * kBK * 2;  // 16 KB
     constexpr int B_BYTES = BN * kBK * 2;
     constexpr int STAGE = A_BYTES + B_BYTES;
@@ -110,7 +111,8 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     };
 
-    // split K (gridDim.z > 1): this CTA takes chunks [kb0, kb1) and adds its partial tile to C
+    // split K (gridDim.z > 1): this CTA takes chunks [kb0, kb1) and adds its partial tile to C, or
+    // (slab > 0) stores it to its own slab C + z slab, for a reduction in a fixed order
     const int nk_all = (K + kBK - 1) / kBK;
     const int kb0 = blockIdx.z * chunks_per_split, kb1 = min(nk_all, kb0 + chunks_per_split);
     const int nk = max(0, kb1 - kb0);
@@ -188,8 +190,14 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
             float* crow = C + (long long)m * ldc + n0 + c0;
             if (split) {
+                if (slab) {
+                    float* srow = crow + blockIdx.z * slab;
 #pragma unroll
-                for (int q = 0; q < 16; q++) atomicAdd(crow + q, __uint_as_float(r[q]));
+                    for (int q = 0; q < 16; q++) srow[q] = __uint_as_float(r[q]);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 16; q++) atomicAdd(crow + q, __uint_as_float(r[q]));
+                }
                 continue;
             }
 #pragma unroll
@@ -226,8 +234,9 @@ cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int 
     const int nk = (K + kBK - 1) / kBK;
     const int per = (nk + ksplit - 1) / ksplit;
     const dim3 grid(M / kBM, N / BN, (nk + per - 1) / per);
+    const long long slab = accumulate == 2 && grid.z > 1 ? (long long)M * ldc : 0;
     k_umma_gemm<BN, NS><<<grid, 128, bytes, s>>>(A, lda, B, ldb, C, ldc, Cb, ldcb, K, bias, relu, accumulate, per,
-                                                 err);
+                                                 slab, err);
     return cudaGetLastError();
 }
 
@@ -236,8 +245,10 @@ cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int 
 extern "C" int sa_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb,
                             int M, int N, int K, const float* bias, int relu, int accumulate, int ksplit, int* err,
                             void* stream) {
-    if (ksplit < 1 || (ksplit > 1 && (bias || relu || Cb || !accumulate)))
-        return (sa::set_last_error("sa_gemm_bf16: split K adds plain partial products into C (accumulate only)"),
+    if (ksplit < 1 || (ksplit > 1 && (bias || relu || Cb || !accumulate)) || accumulate < 0 || accumulate > 2 ||
+        (accumulate == 2 && ksplit < 2))
+        return (sa::set_last_error("sa_gemm_bf16: split K adds plain partial products into C (accumulate 1) or "
+                                   "stores them to slabs (accumulate 2)"),
                 SA_E_INVALID);
     if (!A || !B || !C || !err || M <= 0 || N <= 0 || K <= 0 || M % kBM || K % 16 || (N % 32))
         return (sa::set_last_error("sa_gemm_bf16: M must be a multiple of 128, K of 16, N of 32"), SA_E_INVALID);

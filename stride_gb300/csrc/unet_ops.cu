@@ -104,19 +104,37 @@ __global__ void k_relu_bwd(float* dy, int ldd, const float* __restrict__ y, int 
 }
 
 // db[c] = sum over rows of dy[r][c] (FP64 partials, one atomic per block and channel block).
-__global__ void k_bias_grad(const float* __restrict__ dy, int ldd, long long rows, int C, float* db) {
+// Bias gradient in two fixed-order stages (a reproducible sum): block b of the first sums rows
+// b*8 + y, advancing by gridDim.x * 8, into part[b][c]; the second sums the parts in block order.
+constexpr int kBiasBlocks = 128;
+__global__ void k_bias_grad(const float* __restrict__ dy, int ldd, long long rows, int C, double* part) {
     const int c = blockIdx.y * 32 + threadIdx.x;
     double s = 0.0;
     if (c < C)
         for (long long r = blockIdx.x * (long long)blockDim.y + threadIdx.y; r < rows; r += (long long)gridDim.x * blockDim.y)
             s += dy[r * ldd + c];
-    __shared__ double part[8][33];
-    part[threadIdx.y][threadIdx.x] = s;
+    __shared__ double sh[8][33];
+    sh[threadIdx.y][threadIdx.x] = s;
     __syncthreads();
     if (threadIdx.y == 0 && c < C) {
         double t = 0.0;
-        for (int k = 0; k < (int)blockDim.y; k++) t += part[k][threadIdx.x];
-        atomicAdd(db + c, (float)t);
+        for (int k = 0; k < (int)blockDim.y; k++) t += sh[k][threadIdx.x];
+        part[(long long)blockIdx.x * C + c] = t;
+    }
+}
+__global__ void k_bias_sum(const double* __restrict__ part, int nparts, int C, float* db) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    double t = 0.0;
+    for (int b = 0; b < nparts; b++) t += part[(long long)b * C + c];
+    db[c] = (float)t;
+}
+__global__ void k_sum_slabs(const float* __restrict__ in, long long slab, int nz, float* out, long long n,
+                            int accumulate) {
+    GRID_LOOP(i, n) {
+        float t = in[i];
+        for (int z = 1; z < nz; z++) t += in[z * slab + i];
+        out[i] = accumulate ? out[i] + t : t;
     }
 }
 
@@ -290,12 +308,21 @@ int sa_nn_relu_bwd(float* dy, int ldd, const float* y, int ldy, long long rows, 
     return SA_OK;
 }
 
-int sa_nn_bias_grad(const float* dy, int ldd, long long rows, int C, float* db, void* stream) {
-    if (!dy || !db || rows < 1 || C < 1) return fail_n(SA_E_INVALID, "sa_nn_bias_grad: bad arguments");
+int sa_nn_bias_grad(const float* dy, int ldd, long long rows, int C, float* db, double* scratch, void* stream) {
+    if (!dy || !db || !scratch || rows < 1 || C < 1) return fail_n(SA_E_INVALID, "sa_nn_bias_grad: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
-    CKN(cudaMemsetAsync(db, 0, C * sizeof(float), s));
-    const dim3 grid((unsigned)std::min<long long>((rows + 7) / 8, 1024), (C + 31) / 32);
-    k_bias_grad<<<grid, dim3(32, 8), 0, s>>>(dy, ldd, rows, C, db);
+    const int nb = (int)std::min<long long>((rows + 7) / 8, kBiasBlocks);
+    k_bias_grad<<<dim3(nb, (C + 31) / 32), dim3(32, 8), 0, s>>>(dy, ldd, rows, C, scratch);
+    k_bias_sum<<<(C + 127) / 128, 128, 0, s>>>(scratch, nb, C, db);
+    CKN(cudaGetLastError());
+    return SA_OK;
+}
+
+int sa_nn_sum_slabs(const float* in, long long slab, int n_slabs, float* out, long long n, int accumulate,
+                    void* stream) {
+    if (!in || !out || n_slabs < 1 || n < 0 || slab < n) return fail_n(SA_E_INVALID, "sa_nn_sum_slabs: bad arguments");
+    if (n == 0) return SA_OK;
+    k_sum_slabs<<<nblocks(n), 256, 0, (cudaStream_t)stream>>>(in, slab, n_slabs, out, n, accumulate);
     CKN(cudaGetLastError());
     return SA_OK;
 }

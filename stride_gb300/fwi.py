@@ -134,6 +134,11 @@ class PlainFWI:
         self.optimiser = GradientDescent(step_size=step_size, slowness=True)
         self.history = []
 
+    def set_step_size(self, step_size):
+        """The gradient-descent step (the reference's step_size)."""
+        self.step_size = step_size
+        self.optimiser = GradientDescent(step_size=step_size, slowness=True)
+
     def reset(self, vp_true, vp0=1500.):
         """A new true model on the same grid and acquisition: observed data recomputed, vp restarted."""
         self.vp_true = torch.as_tensor(np.ascontiguousarray(vp_true, np.float32), device=self.device)

@@ -61,6 +61,7 @@ class _Conv:
         self.wb = torch.empty((self.coutp, self.kp), dtype=torch.bfloat16, device=dev)
         self.wt = torch.empty((self.kp, self.coutp), dtype=torch.bfloat16, device=dev)
         self.err = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.bscratch = torch.empty(128 * self.coutp, dtype=torch.float64, device=dev)  # bias-gradient parts
         self.pack()
 
     def params(self):
@@ -95,7 +96,7 @@ class _Conv:
         P = B * H * W
         if self.relu:
             _ck(lib.sa_nn_relu_bwd(_p(dy), self.coutp, _p(y), self.coutp, P, self.coutp, _s()))
-        _ck(lib.sa_nn_bias_grad(_p(dy), self.coutp, P, self.coutp, _p(self.gb), _s()))
+        _ck(lib.sa_nn_bias_grad(_p(dy), self.coutp, P, self.coutp, _p(self.gb), _p(self.bscratch), _s()))
         dyb = torch.empty((P, self.coutp), dtype=torch.bfloat16, device=dy.device)
         _ck(lib.sa_nn_to_bf16(_p(dy), self.coutp, P, self.coutp, _p(dyb), self.coutp, _s()))
         # weight gradient: dW[mw][kp] = dy^T col (K = pixels, split over CTAs)
@@ -103,9 +104,19 @@ class _Conv:
         _ck(lib.sa_nn_transpose_bf16(_p(dyb), self.coutp, P, self.coutp, _p(dyT), P, self.mw, _s()))
         colT = torch.empty((self.kp, P), dtype=torch.bfloat16, device=dy.device)
         _ck(lib.sa_nn_transpose_bf16(_p(col), self.kp, P, self.kp, _p(colT), P, self.kp, _s()))
-        dw = torch.zeros((self.mw, self.kp), device=dy.device)
+        # split K over the pixels: each split stores its partial product to its own slab, summed in a
+        # fixed order (reproducible training)
         ksplit = max(1, min(64, P // 2048))
-        self.gemm(dyT, P, colT, P, dw, self.kp, self.mw, self.kp, P, accumulate=True, ksplit=ksplit)
+        dw = torch.zeros((self.mw, self.kp), device=dy.device)
+        if ksplit > 1:
+            nk = -(-P // 64)
+            per = -(-nk // ksplit)
+            nz = -(-nk // per)  # splits the GEMM launches
+            slabs = torch.empty((nz, self.mw, self.kp), device=dy.device)
+            self.gemm(dyT, P, colT, P, slabs, self.kp, self.mw, self.kp, P, accumulate=2, ksplit=ksplit)
+            _ck(lib.sa_nn_sum_slabs(_p(slabs), self.mw * self.kp, nz, _p(dw), self.mw * self.kp, 0, _s()))
+        else:
+            self.gemm(dyT, P, colT, P, dw, self.kp, self.mw, self.kp, P, accumulate=True)
         self.gw.copy_(dw[:self.cout, :self.kr])
         if not need_dx:
             return None

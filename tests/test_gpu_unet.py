@@ -61,6 +61,30 @@ def test_gemm_split_k():
     assert float((C.double() - ref).norm() / ref.norm()) <= 1e-5
 
 
+def test_gemm_split_k_slabs_are_reproducible():
+    """Split K into slabs (accumulate 2) and their fixed-order sum: the product, bit for bit the same
+    on every run."""
+    g = torch.Generator(device='cpu').manual_seed(4)
+    M, N, K = 256, 64, 64 * 37 + 32
+    A = torch.randn((M, K), generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn((N, K), generator=g).to(torch.bfloat16).cuda()
+    nk = -(-K // 64)
+    per = -(-nk // 5)
+    nz = -(-nk // per)
+    outs = []
+    for _ in range(3):
+        slabs = torch.full((nz, M, N), float('nan'), device='cuda')  # every slab element is written
+        _gemm(A, B, C=slabs[0], accumulate=2, ksplit=5)
+        out = torch.empty((M, N), device='cuda')
+        _lib.check(_lib.load().sa_nn_sum_slabs(_lib._ptr(slabs), M * N, nz, _lib._ptr(out), M * N, 0,
+                                               _lib._stream(torch.cuda.current_stream())))
+        torch.cuda.synchronize()
+        outs.append(out)
+    ref = A.double() @ B.double().T
+    assert float((outs[0].double() - ref).norm() / ref.norm()) <= 1e-5
+    assert torch.equal(outs[0], outs[1]) and torch.equal(outs[0], outs[2])
+
+
 def _reference_net(net, x, target):
     """The same U-Net in float64 PyTorch on the CPU (weights as the BF16 the GEMMs use)."""
     F = torch.nn.functional
@@ -143,3 +167,26 @@ def test_unet_training_reduces_loss():
         losses.append(float(loss.item()))
     assert net.errors() == 0
     assert losses[-1] < 0.3 * losses[0], losses[::10]
+
+
+def test_unet_training_is_reproducible():
+    """Training is deterministic (split-K slabs summed in a fixed order, fixed-order bias sums):
+    two networks from the same seed, trained on the same batches, end bit for bit equal."""
+    from stride_gb300.unet import UNet
+    torch.manual_seed(3)
+    B, H, W = 4, 64, 64
+    x = torch.randn(B, H, W, 2, device='cuda')
+    target = torch.randn(B, H, W, device='cuda')
+    nets = []
+    for _ in range(2):
+        net = UNet(seed=5)
+        for _ in range(8):
+            y = net.forward(x)
+            _, d = net.mse(y, target)
+            net.backward(d)
+            net.adam_step(lr=1e-3)
+        nets.append(net)
+    for (a, _, _, _), (b, _, _, _) in zip((p for l in nets[0].layers() for p in l.params()),
+                                          (p for l in nets[1].layers() for p in l.params())):
+        assert torch.equal(a, b)
+
