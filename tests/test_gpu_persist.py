@@ -1,8 +1,8 @@
 """The persistent forward of small batches (one cooperative launch runs every step,
 stride_gb300/csrc/persist2d.cu): its traces equal the streaming step passes' bit for bit for every
-operator variant and for uneven batches; the single-shot workload matches the oracle; and step-flag
-waits that cannot complete (the tests' option makes each wait ask for one step more than the tiles
-can have published) give up within their bound: sa_forward returns SA_E_TIMEOUT and the plan keeps
+operator variant and for uneven batches; the single-shot workload matches the oracle; and halo
+waits that cannot complete (the tests' option makes each wait ask for a level one beyond what any
+tile publishes) give up within their bound: sa_forward returns SA_E_TIMEOUT and the plan keeps
 working."""
 
 import numpy as np
@@ -64,12 +64,12 @@ def test_persistent_single_shot_workload_matches_oracle():
     assert C.rel_l2(got[0], ref) <= 1e-4
 
 
-def test_barrier_timeout_is_reported_and_the_plan_recovers():
+def test_wait_timeout_is_reported_and_the_plan_recovers():
     c = C.small_case(kernel='OT4', density='variable', alpha=True, n_shots=2, nt=120)
     plan = C.make_plan(c)
     good = _forward(c, plan, 1)
     plan.set_option(_lib.SA_OPT_BARRIER_SPIN, 20000)  # milliseconds per wait
-    plan.set_option(_lib.SA_OPT_BARRIER_EXTRA, 1)     # one step ahead of every tile: no wait can complete
+    plan.set_option(_lib.SA_OPT_BARRIER_EXTRA, 1)     # a level beyond every tile's: no wait can complete
     with pytest.raises(_lib.StrideAccError) as e:
         _forward(c, plan, 1)
     assert e.value.code == _lib.SA_E_TIMEOUT
