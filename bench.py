@@ -314,7 +314,7 @@ def fwi_arm(args):
     ev1.record()
     torch.cuda.synchronize()
     fwd_ms = ev0.elapsed_time(ev1) / 5
-    flops = sum(2.0 * layer.saved[2] * layer.saved[3] * layer.saved[4] * layer.coutp * layer.kp
+    flops = sum(2.0 * layer.saved[3] * layer.saved[4] * layer.saved[5] * layer.coutp * layer.kp
                 for layer in net.layers())
     learned = LearnedFWI(w0, net, step_size=step)
     # one untimed iteration of each solver on a seed outside the test set, so that first-use costs

@@ -266,6 +266,15 @@ int sa_field_apply_prec(float* grad, float* prec, long long n, double factor, vo
 int sa_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb, int M, int N,
                  int K, const float* bias, int relu, int accumulate, int ksplit, int* err, void* stream);
 
+/* 3x3 convolution (padding 1) as an implicit GEMM on the tcgen05 tensor cores: C[P][N] = A W^T
+ * (+ bias, ReLU; Cb optional bf16 copy), P = B*H*W pixels (a multiple of 128), where A[P][Kp] is the
+ * im2col of x built in shared memory, never in HBM: column (ky*3+kx)*Cin+ci of pixel p is channel ci
+ * of its neighbour (ky-1, kx-1) in x, bf16 NHWC [P][ldx] (zero outside the image and for columns
+ * >= 9*Cin). Wt bf16 [N][ldw] with the same column order; Cin and ldx multiples of 8, Kp >= 9*Cin a
+ * multiple of 16, N of 32. *err as for sa_gemm_bf16. */
+int sa_conv3x3_bf16(const void* x, int ldx, int B, int H, int W, int Cin, const void* Wt, int ldw, float* C, int ldc,
+                    void* Cb, int ldcb, int N, int Kp, const float* bias, int relu, int* err, void* stream);
+
 /* U-Net layer kernels (NHWC fp32 activations [pixels][channels] with channel stride ld; bf16 GEMM
  * operands; B images of H x W). No counterpart in the reference. */
 /* col bf16 [B*H*W][Kp]: column (ky*3+kx)*Cin+ci of pixel p = x at the 3x3 neighbour (zero outside

@@ -49,7 +49,7 @@ EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometr
            'sa_field_scale', 'sa_field_gaussian', 'sa_field_apply_prec', 'sa_gemm_bf16', 'sa_nn_im2col',
            'sa_nn_col2im', 'sa_nn_transpose_bf16', 'sa_nn_to_bf16', 'sa_nn_relu_bwd', 'sa_nn_bias_grad',
            'sa_nn_maxpool', 'sa_nn_maxpool_bwd', 'sa_nn_upsample', 'sa_nn_upsample_bwd', 'sa_nn_copy_channels',
-           'sa_nn_pack_weights', 'sa_nn_adam', 'sa_nn_mse', 'sa_nn_sum_slabs')
+           'sa_nn_pack_weights', 'sa_nn_adam', 'sa_nn_mse', 'sa_nn_sum_slabs', 'sa_conv3x3_bf16')
 
 
 class SaDesc(ctypes.Structure):
@@ -120,6 +120,7 @@ def load():
     lib.sa_nn_relu_bwd.argtypes = [P, I, P, I, L, I, P]
     lib.sa_nn_bias_grad.argtypes = [P, I, L, I, P, P, P]
     lib.sa_nn_sum_slabs.argtypes = [P, L, I, P, L, I, P]
+    lib.sa_conv3x3_bf16.argtypes = [P, I, I, I, I, I, P, I, P, I, P, I, I, I, P, I, P, P]
     lib.sa_nn_maxpool.argtypes = [P, I, I, I, I, I, P, I, P]
     lib.sa_nn_maxpool_bwd.argtypes = [P, I, P, I, I, I, I, I, P, I, I, P]
     lib.sa_nn_upsample.argtypes = [P, I, I, I, I, I, P, I, P]

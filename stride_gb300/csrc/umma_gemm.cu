@@ -31,6 +31,18 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)_
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
 }
+__device__ __forceinline__ void cp_async16z(uint32_t dst, const void* src, bool valid) {  // zero-fill if !valid
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+
+// Implicit-GEMM A operand of a 3x3 convolution (padding 1): row m of A is pixel m of B images of
+// H x W, column k = (ky 3 + kx) Cin + ci the input channel ci of its (ky - 1, kx - 1) neighbour,
+// read from the bf16 NHWC activations (row stride ldx) and zero outside the image or for
+// k >= 9 Cin. Cin is a multiple of 8, so a 16-byte group of 8 columns never straddles two taps.
+struct ConvA {
+    int H, W, Cin, ldx;  // Cin 0: A is a plain matrix (lda)
+};
 
 // tcgen05 shared-memory matrix descriptor: start >> 4 (bits 0-13), leading byte offset >> 4
 // (16-29), stride byte offset >> 4 (32-45), fixed 0b001 (46-48), no swizzle (61-63 = 0).
@@ -63,7 +75,7 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
                                                    const __nv_bfloat16* __restrict__ B, int ldb, float* C, int ldc,
                                                    __nv_bfloat16* Cb, int ldcb, int K, const float* __restrict__ bias,
                                                    int relu, int accumulate, int chunks_per_split, long long slab,
-                                                   int* err) {
+                                                   const ConvA conv, int* err) {
     constexpr int A_BYTES = kBM * kBK * 2;  // 16 KB
     constexpr int B_BYTES = BN * kBK * 2;
     constexpr int STAGE = A_BYTES + B_BYTES;
@@ -96,11 +108,25 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
         const uint32_t sa = sbase + stage * STAGE, sb = sa + A_BYTES;
         const int k0 = kb * kBK;
         const int ng = min(kBK, K - k0) >> 3;  // k groups of 8 in this chunk
-        for (int c = tid; c < kBM * 8; c += 128) {
-            const int m = c >> 3, g = c & 7;
-            if (g < ng)
-                cp_async16(sa + g * (kBM * 16) + (m >> 3) * 128 + (m & 7) * 16,
-                           A + (long long)(m0 + m) * lda + k0 + g * 8);
+        if (conv.Cin == 0) {
+            for (int c = tid; c < kBM * 8; c += 128) {
+                const int m = c >> 3, g = c & 7;
+                if (g < ng)
+                    cp_async16(sa + g * (kBM * 16) + (m >> 3) * 128 + (m & 7) * 16,
+                               A + (long long)(m0 + m) * lda + k0 + g * 8);
+            }
+        } else {
+            const int HW = conv.H * conv.W;
+            for (int c = tid; c < kBM * 8; c += 128) {
+                const int m = c >> 3, g = c & 7;
+                if (g >= ng) continue;
+                const int p = m0 + m, b = p / HW, q = p - b * HW, y = q / conv.W, x = q - y * conv.W;
+                const int k = k0 + g * 8, tap = k / conv.Cin, ci = k - tap * conv.Cin;
+                const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+                const bool ok = tap < 9 && yy >= 0 && yy < conv.H && xx >= 0 && xx < conv.W;
+                const __nv_bfloat16* src = ok ? A + ((long long)(b * conv.H + yy) * conv.W + xx) * conv.ldx + ci : A;
+                cp_async16z(sa + g * (kBM * 16) + (m >> 3) * 128 + (m & 7) * 16, src, ok);
+            }
         }
         for (int c = tid; c < BN * 8; c += 128) {
             const int n = c >> 3, g = c & 7;
@@ -221,7 +247,7 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
 template <int BN>
 cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C, int ldc,
                    __nv_bfloat16* Cb, int ldcb, int M, int N, int K, const float* bias, int relu, int accumulate,
-                   int ksplit, int* err, cudaStream_t s) {
+                   int ksplit, int* err, cudaStream_t s, ConvA conv = ConvA{0, 0, 0, 0}) {
     constexpr int NS = BN >= 128 ? 3 : 4;  // stages: 96 KB (BN 128) or <= 96 KB (BN <= 64) of shared memory
     const size_t bytes = NS * (size_t)(kBM * kBK * 2 + BN * kBK * 2);
     static bool configured = false;
@@ -236,7 +262,7 @@ cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int 
     const dim3 grid(M / kBM, N / BN, (nk + per - 1) / per);
     const long long slab = accumulate == 2 && grid.z > 1 ? (long long)M * ldc : 0;
     k_umma_gemm<BN, NS><<<grid, 128, bytes, s>>>(A, lda, B, ldb, C, ldc, Cb, ldcb, K, bias, relu, accumulate, per,
-                                                 slab, err);
+                                                 slab, conv, err);
     return cudaGetLastError();
 }
 
@@ -267,6 +293,33 @@ extern "C" int sa_gemm_bf16(const void* A, int lda, const void* B, int ldb, floa
         e = launch<64>(a, lda, b, ldb, C, ldc, cb, ldcb, M, N, K, bias, relu, accumulate, ksplit, err, s);
     else
         e = launch<32>(a, lda, b, ldb, C, ldc, cb, ldcb, M, N, K, bias, relu, accumulate, ksplit, err, s);
+    if (e != cudaSuccess) return (sa::set_last_error(cudaGetErrorString(e)), SA_E_CUDA);
+    return SA_OK;
+}
+
+extern "C" int sa_conv3x3_bf16(const void* x, int ldx, int B, int H, int W, int Cin, const void* Wt, int ldw, float* C,
+                               int ldc, void* Cb, int ldcb, int N, int Kp, const float* bias, int relu, int* err,
+                               void* stream) {
+    const long long P = (long long)B * H * W;
+    if (!x || !Wt || !C || !err || B < 1 || H < 1 || W < 1 || Cin < 8 || Cin % 8 || P % kBM || P > INT32_MAX ||
+        Kp < 9 * Cin || Kp % 16 || N % 32 || ldx < Cin || ldx % 8 || ldw < Kp || ldw % 8 || ldc < N ||
+        (Cb && ldcb < N) || ((uintptr_t)x & 15) || ((uintptr_t)Wt & 15))
+        return (sa::set_last_error("sa_conv3x3_bf16: pixels a multiple of 128, Cin and ldx multiples of 8, "
+                                   "Kp >= 9 Cin a multiple of 16, N of 32, 16-byte aligned operands"),
+                SA_E_INVALID);
+    const auto* a = static_cast<const __nv_bfloat16*>(x);
+    const auto* b = static_cast<const __nv_bfloat16*>(Wt);
+    auto* cb = static_cast<__nv_bfloat16*>(Cb);
+    const ConvA conv{H, W, Cin, ldx};
+    cudaStream_t s = (cudaStream_t)stream;
+    const int M = (int)P;
+    cudaError_t e;
+    if (N % 128 == 0)
+        e = launch<128>(a, 0, b, ldw, C, ldc, cb, ldcb, M, N, Kp, bias, relu, 0, 1, err, s, conv);
+    else if (N % 64 == 0)
+        e = launch<64>(a, 0, b, ldw, C, ldc, cb, ldcb, M, N, Kp, bias, relu, 0, 1, err, s, conv);
+    else
+        e = launch<32>(a, 0, b, ldw, C, ldc, cb, ldcb, M, N, Kp, bias, relu, 0, 1, err, s, conv);
     if (e != cudaSuccess) return (sa::set_last_error(cudaGetErrorString(e)), SA_E_CUDA);
     return SA_OK;
 }

@@ -78,22 +78,33 @@ class _Conv:
     def forward(self, x, B, H, W):
         lib = _lib.load()
         P = B * H * W
+        y = torch.empty((P, self.coutp), device=x.device)
+        if self.k == 3 and self.cin % 8 == 0:
+            # implicit GEMM: the 3x3 neighbourhoods are gathered in shared memory from a bf16 copy of x
+            xb = torch.empty((P, self.cin), dtype=torch.bfloat16, device=x.device)
+            _ck(lib.sa_nn_to_bf16(_p(x), x.shape[1], P, self.cin, _p(xb), self.cin, _s()))
+            _ck(lib.sa_conv3x3_bf16(_p(xb), self.cin, B, H, W, self.cin, _p(self.wb), self.kp, _p(y), self.coutp,
+                                    None, 0, self.coutp, self.kp, _p(self.b), int(self.relu), _p(self.err), _s()))
+            self.saved = (None, x, y, B, H, W)  # the weight gradient's im2col is built in backward
+            return y
         col = torch.empty((P, self.kp), dtype=torch.bfloat16, device=x.device)
         if self.k == 3:
             _ck(lib.sa_nn_im2col(_p(x), x.shape[1], B, H, W, self.cin, _p(col), self.kp, _s()))
         else:
             col.zero_()
             _ck(lib.sa_nn_to_bf16(_p(x), x.shape[1], P, self.cin, _p(col), self.kp, _s()))
-        y = torch.empty((P, self.coutp), device=x.device)
         self.gemm(col, self.kp, self.wb, self.kp, y, self.coutp, P, self.coutp, self.kp, bias=self.b, relu=self.relu)
-        self.saved = (col, y, B, H, W)
+        self.saved = (col, x, y, B, H, W)
         return y
 
     def backward(self, dy, need_dx=True):
         """dy [P][coutp] (modified in place by the ReLU backward); returns dx [P][cin] or None."""
         lib = _lib.load()
-        col, y, B, H, W = self.saved
+        col, x, y, B, H, W = self.saved
         P = B * H * W
+        if col is None:
+            col = torch.empty((P, self.kp), dtype=torch.bfloat16, device=dy.device)
+            _ck(lib.sa_nn_im2col(_p(x), x.shape[1], B, H, W, self.cin, _p(col), self.kp, _s()))
         if self.relu:
             _ck(lib.sa_nn_relu_bwd(_p(dy), self.coutp, _p(y), self.coutp, P, self.coutp, _s()))
         _ck(lib.sa_nn_bias_grad(_p(dy), self.coutp, P, self.coutp, _p(self.gb), _p(self.bscratch), _s()))

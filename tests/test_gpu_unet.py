@@ -61,6 +61,35 @@ def test_gemm_split_k():
     assert float((C.double() - ref).norm() / ref.norm()) <= 1e-5
 
 
+@pytest.mark.parametrize("B,H,W,Cin,N", [(2, 16, 8, 8, 32), (1, 16, 16, 32, 64), (2, 8, 24, 64, 128),
+                                         (1, 32, 4, 16, 32)])
+def test_conv3x3_implicit_gemm(B, H, W, Cin, N):
+    """The implicit-GEMM 3x3 convolution (neighbourhoods gathered in shared memory, zero padding at
+    the image edges, columns (ky*3+kx)*Cin+ci) against an FP64 convolution of the same bf16 values,
+    with bias and ReLU."""
+    g = torch.Generator(device='cpu').manual_seed(B * 1000 + H * 10 + Cin)
+    x = torch.randn((B, H, W, Cin), generator=g).to(torch.bfloat16)
+    K = 9 * Cin
+    Kp = (K + 31) // 32 * 32
+    w = torch.randn((N, 3, 3, Cin), generator=g).to(torch.bfloat16)  # [N][ky][kx][ci]
+    Wt = torch.zeros((N, Kp), dtype=torch.bfloat16)
+    Wt[:, :K] = w.reshape(N, K)
+    bias = torch.randn(N, generator=g)
+    P = B * H * W
+    C = torch.zeros((P, N), device='cuda')
+    err = torch.zeros(1, dtype=torch.int32, device='cuda')
+    xd, Wd, bd = x.reshape(P, Cin).contiguous().cuda(), Wt.cuda(), bias.cuda()
+    _lib.check(_lib.load().sa_conv3x3_bf16(_lib._ptr(xd), Cin, B, H, W, Cin, _lib._ptr(Wd), Kp, _lib._ptr(C), N,
+                                           None, 0, N, Kp, _lib._ptr(bd), 1, _lib._ptr(err),
+                                           _lib._stream(torch.cuda.current_stream())))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    ref = torch.nn.functional.conv2d(x.double().permute(0, 3, 1, 2), w.double().permute(0, 3, 1, 2),
+                                     bias.double(), padding=1).permute(0, 2, 3, 1).reshape(P, N).relu()
+    rel = float((C.cpu().double() - ref).norm() / ref.norm())
+    assert rel <= 1e-5, rel
+
+
 def test_gemm_split_k_slabs_are_reproducible():
     """Split K into slabs (accumulate 2) and their fixed-order sum: the product, bit for bit the same
     on every run."""
