@@ -54,6 +54,7 @@ WORKLOADS = {
     'exact64': ('batched', 64, 'fwdadj'),   # exact gradient (autograd backward), checkpoints every 50 steps
     '3dgrad8': ('3d', 8, 'fwdadj'),         # 3D gradient of 8 shots, checkpoints under a 150 GB budget
     'fwi': ('single', 32, 'fwi'),           # plain vs learned-preconditioned FWI, wall time to a vp error
+    'unet': ('single', 0, 'unet'),          # the learned preconditioner's network: forward at batch 4, 256^2
     'rho64': ('batched', 64, 'fwdadj'),     # vp and rho gradients from the raw saved wavefield
     'pml64': ('batched', 64, 'fwdadj'),     # vp gradient with the CFS-PML boundary (OT2)
     'ckpt64': ('batched', 64, 'fwdadj'),    # the default gradient from checkpoints every 50 steps with recompute
@@ -95,6 +96,10 @@ WORKLOAD_NAMES = {
            '500 kHz, f_max 0.5 MHz: plain (reference loop, GPU pipelines) vs U-Net-preconditioned (BF16 tcgen05, '
            'trained on plain-FWI paths of held-out seeds), wall time to the target relative vp error',
 }
+
+
+WORKLOAD_NAMES['unet'] = ('learned preconditioner U-Net (4 levels, 32-64-128-256 channels, BF16 tcgen05, implicit-GEMM '
+                          '3x3 convolutions) forward on a batch of 4 inputs of 256^2 x 2 channels')
 
 
 def workload_name(name, nt):
@@ -259,6 +264,7 @@ def _points(w, workload):
 
 
 METRIC = {'fwdadj': 'GPts/s (forward+adjoint vp gradient)', 'fwd': 'GPts/s (forward)',
+          'unet': 'TFLOP/s (U-Net forward, tensor-core GEMM FLOPs of every convolution)',
           'fwi': 'seconds to the target relative vp error (learned-preconditioned FWI, median over test phantoms)'}
 
 
@@ -270,6 +276,54 @@ def _fwi_workload(seed):
     w['src'] = [w['geometry'][[s]] for s in shots]
     w['rec'] = [w['geometry'] for _ in shots]
     return w
+
+
+def unet_arm(args):
+    """The U-Net's forward pass (the learned FWI's inference) on a batch of 4 seeded 256^2 inputs:
+    tensor-core GEMM FLOPs of every convolution over the CUDA-event time of the pass."""
+    import torch
+    from stride_gb300.unet import UNet
+    torch.cuda.set_device(0)
+    g = torch.Generator(device='cpu').manual_seed(0)
+    x = torch.randn((4, 256, 256, 2), generator=g).cuda()
+    net = UNet(seed=0)
+    for _ in range(args.warmup):
+        net.forward(x)
+    torch.cuda.synchronize()
+    flush = torch.empty(64 * 2**20, dtype=torch.float32, device='cuda')  # the activations fit in L2
+    times = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            net.forward(x)
+            e1.record()
+            times.append((e0, e1))
+        torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in times) / len(times)
+    flops = sum(2.0 * layer.saved[3] * layer.saved[4] * layer.saved[5] * layer.coutp * layer.kp
+                for layer in net.layers())
+    tflops = flops / (ms * 1e-3) / 1e12
+    peak = 1883.3
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            peak, src = float(json.load(f)['bf16_tflops']), 'measured'
+    except Exception:
+        src = 'fallback'
+    line = {
+        'metric': METRIC['unet'], 'value': tflops, 'unit': 'TFLOP/s', 'n_gpus': 1, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'bf16 operands, fp32 accumulation', 'data': 'synthetic (seeded normal inputs, He-initialised weights)',
+        'config': {'workload': WORKLOAD_NAMES['unet'], 'batch': 4, 'image': [256, 256],
+                   'l2_flush': 'L2 flushed between timed passes (256 MB write, outside the passes\' events)'},
+        'roofline': {'bound': 'tensor', 'achieved': tflops, 'peak': peak, 'unit': 'TFLOP/s', 'frac': tflops / peak,
+                     'peak_source': src, 'traffic': None, 'kernel': 'k_umma_gemm (every convolution of the pass)'},
+        'cpu_baseline': None, 'e2e': None, 'gpu_launches': None, 'clocks': clk.summary(),
+        'gemm_timeouts': net.errors(),
+    }
+    print(json.dumps(line))
+    return 0
 
 
 def fwi_arm(args):
@@ -659,6 +713,12 @@ def main():
     if args.gpus > 1 and 'WORLD_SIZE' not in os.environ:
         # one process per GPU: this script again as --gpus ranks under torch.distributed.run
         return launch_ranks(args.gpus, [os.path.abspath(__file__)] + sys.argv[1:])
+    if args.workload == 'unet':
+        if args.impl == 'reference':
+            print(json.dumps({'impl': 'reference', 'unavailable': 'the U-Net is the learned part, which has no '
+                              'counterpart in the reference'}))
+            return 0
+        return unet_arm(args)
     if args.workload == 'fwi':
         if args.impl == 'reference':
             print(json.dumps({'impl': 'reference', 'unavailable': 'the fwi workload compares two GPU methods; its '
