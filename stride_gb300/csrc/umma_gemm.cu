@@ -102,6 +102,16 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = tmem_base_sh;
 
+    // implicit GEMM: the (y, x) of this thread's A rows (tid >> 3) + 16 i, packed y << 16 | x
+    int rowyx[8];
+    if (conv.Cin) {
+        const int HW = conv.H * conv.W;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int p = m0 + (tid >> 3) + 16 * i, q = p % HW, y = q / conv.W;
+            rowyx[i] = y << 16 | (q - y * conv.W);
+        }
+    }
     // stage loader: A rows m (128) and B rows n (BN), k group g (8 per chunk), 16 bytes each
     // (the last chunk may be shorter: K is a multiple of 16, a chunk holds K - k0 <= 64 columns)
     auto load = [&](int kb, int stage) {
@@ -116,15 +126,19 @@ __global__ void __launch_bounds__(128) k_umma_gemm(const __nv_bfloat16* __restri
                                A + (long long)(m0 + m) * lda + k0 + g * 8);
             }
         } else {
-            const int HW = conv.H * conv.W;
-            for (int c = tid; c < kBM * 8; c += 128) {
-                const int m = c >> 3, g = c & 7;
-                if (g >= ng) continue;
-                const int p = m0 + m, b = p / HW, q = p - b * HW, y = q / conv.W, x = q - y * conv.W;
-                const int k = k0 + g * 8, tap = k / conv.Cin, ci = k - tap * conv.Cin;
-                const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
-                const bool ok = tap < 9 && yy >= 0 && yy < conv.H && xx >= 0 && xx < conv.W;
-                const __nv_bfloat16* src = ok ? A + ((long long)(b * conv.H + yy) * conv.W + xx) * conv.ldx + ci : A;
+            // this thread's group g = tid & 7 of every chunk, rows (tid >> 3) + 16 i: the tap and channel of
+            // its columns once per chunk, the rows' pixels precomputed
+            const int g = tid & 7;
+            const int k = k0 + g * 8, tap = k / conv.Cin, ci = k - tap * conv.Cin;
+            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+            const bool col_ok = g < ng && tap < 9;
+            const long long toff = (long long)(dy * conv.W + dx) * conv.ldx + ci;
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const int m = (tid >> 3) + 16 * i;
+                const int yy = (rowyx[i] >> 16) + dy, xx = (rowyx[i] & 0xffff) + dx;
+                const bool ok = col_ok && yy >= 0 && yy < conv.H && xx >= 0 && xx < conv.W;
+                const __nv_bfloat16* src = ok ? A + (long long)(m0 + m) * conv.ldx + toff : A;
                 cp_async16z(sa + g * (kBM * 16) + (m >> 3) * 128 + (m & 7) * 16, src, ok);
             }
         }
