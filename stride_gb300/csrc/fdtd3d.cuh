@@ -16,6 +16,7 @@
 // Sparse operations (source/receiver injection, receiver interpolation) run in small kernels
 // after the FINAL pass.
 #pragma once
+#include <type_traits>
 #include "common.cuh"
 #include "fdtd2d.cuh"
 
@@ -26,8 +27,10 @@ struct Step3D {
     long long shot_stride;    // floats per shot in a field buffer (nx*ny*zp)
     int chunk_rows;           // output x rows per CTA
     int ty0n;                 // tiles along y
-    int nshots;               // shots; blockIdx.x = pair + npairs * (tile_y + ty0n * tile_z), pair p holding
-                              // shots 2p and 2p + 1 (a lone last shot computes a zero second lane)
+    int nshots;               // shots of the batch
+    int shot0, npairs;        // this launch: two lanes, blockIdx.x = pair + npairs * (tile_y + ty0n * tile_z),
+                              // pair p holding shots shot0 + 2p and shot0 + 2p + 1; one lane (a lone shot),
+                              // blockIdx.x = tile, shot shot0
     int t;
     const float* in;          // streamed field: u (OT2 / INTERMEDIATE) or l (OT4 FINAL)
     const float* cur;         // p[t] (FINAL: the current level at the output)
@@ -57,13 +60,13 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem, bool val
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(sz) : "memory");
 }
 
-template <int KIND, int TY, int TZ, int RB, int PF>
+template <int KIND, int TY, int TZ, int RB, int PF, int LANES = 2>
 struct Smem3D {
     static constexpr bool STAG = KIND != 0;
     static constexpr int R = STAG ? 9 : 5;
     static constexpr int PY = TY + 2 * R;     // plane rows (y) incl. halo
     static constexpr int PZ = TZ + 2 * R;     // plane row width (z) incl. halo, from z0 - R
-    static constexpr int PLANE = PY * PZ;     // float2: the two shots of the pair
+    static constexpr int PLANE = PY * PZ;     // values of the lanes (float2: the two shots of a pair)
     // planes in the ring (this iteration's and the prefetched), a power of two: slots by mask
     static constexpr int QU = pow2_at_least(RB * (PF + 1));
     static constexpr int FY = (TY + 9) * TZ;  // y fluxes of one row
@@ -75,35 +78,49 @@ struct Smem3D {
     static constexpr int oFZ = oFY + (STAG ? RB * FY : 0);
     static constexpr int oG = oFZ + (STAG ? RB * FZ : 0);
     static constexpr int total = oG + QG * TY * TZ;
-    static constexpr size_t bytes = (size_t)total * sizeof(float2);
+    static constexpr size_t bytes = (size_t)total * sizeof(float) * LANES;
 };
 
-template <int QL, int RB>
-__device__ __forceinline__ void qshift2(float2 (&q)[QL]) {
+// Lane arithmetic: V = float2 (a pair of shots, one f32x2 instruction) or float (a lone shot).
+template <class V> __device__ __forceinline__ V vs(float v);
+template <> __device__ __forceinline__ float vs<float>(float v) { return v; }
+template <> __device__ __forceinline__ float2 vs<float2>(float v) { return f2(v); }
+__device__ __forceinline__ float vfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ float2 vfma(float2 a, float2 b, float2 c) { return fma2(a, b, c); }
+__device__ __forceinline__ float vmul(float a, float b) { return a * b; }
+__device__ __forceinline__ float2 vmul(float2 a, float2 b) { return mul2(a, b); }
+__device__ __forceinline__ float vadd(float a, float b) { return a + b; }
+__device__ __forceinline__ float2 vadd(float2 a, float2 b) { return add2(a, b); }
+__device__ __forceinline__ float vsub(float a, float b) { return fmaf(b, -1.f, a); }
+__device__ __forceinline__ float2 vsub(float2 a, float2 b) { return sub2(a, b); }
+
+template <int QL, int RB, class V>
+__device__ __forceinline__ void qshift(V (&q)[QL]) {
 #pragma unroll
     for (int k = 0; k + RB < QL; k++) q[k] = q[k + RB];
 }
-template <class A>
-__device__ __forceinline__ float2 dstag2(const A& v, int hi, int lo, int stride) {
-    float2 a = mul2(f2(kWS(0)), v[hi]), b = mul2(f2(kWS(0)), v[lo]);
+template <class V, class A>
+__device__ __forceinline__ V dstag(const A& v, int hi, int lo, int stride) {
+    V a = vmul(vs<V>(kWS(0)), v[hi]), b = vmul(vs<V>(kWS(0)), v[lo]);
 #pragma unroll
     for (int m = 1; m < 5; m++) {
-        a = fma2(f2(kWS(m)), v[hi + m * stride], a);
-        b = fma2(f2(kWS(m)), v[lo - m * stride], b);
+        a = vfma(vs<V>(kWS(m)), v[hi + m * stride], a);
+        b = vfma(vs<V>(kWS(m)), v[lo - m * stride], b);
     }
-    return sub2(a, b);
+    return vsub(a, b);
 }
-template <class A>
-__device__ __forceinline__ float2 dcent2(const A& v, int c, int stride) {
-    float2 a = mul2(f2(kW2(0)), v[c]);
+template <class V, class A>
+__device__ __forceinline__ V dcent(const A& v, int c, int stride) {
+    V a = vmul(vs<V>(kW2(0)), v[c]);
 #pragma unroll
-    for (int k = 1; k <= 5; k++) a = fma2(f2(kW2(k)), add2(v[c + k * stride], v[c - k * stride]), a);
+    for (int k = 1; k <= 5; k++) a = vfma(vs<V>(kW2(k)), vadd(v[c + k * stride], v[c - k * stride]), a);
     return a;
 }
 
-template <int KIND, bool FINAL, bool OT4, int TY, int TZ, int RB, int PF>
+template <int KIND, bool FINAL, bool OT4, int TY, int TZ, int RB, int PF, int LANES>
 __global__ void __launch_bounds__(TY* TZ, TY* TZ <= 256 ? 2 : 1) fdtd3d_pass(const __grid_constant__ Step3D a) {
-    using L = Smem3D<KIND, TY, TZ, RB, PF>;
+    using L = Smem3D<KIND, TY, TZ, RB, PF, LANES>;
+    using V = typename std::conditional<LANES == 2, float2, float>::type;
     constexpr int NT = TY * TZ;
     constexpr bool STAG = L::STAG, VARB = KIND == 1;
     constexpr int R = L::R, QU = L::QU, PZ = L::PZ, WZF = L::WZF;
@@ -111,17 +128,18 @@ __global__ void __launch_bounds__(TY* TZ, TY* TZ <= 256 ? 2 : 1) fdtd3d_pass(con
     constexpr int QL = QB + RB;
     constexpr int QG = L::QG;          // y/z parts of rows i - R .. i + RB - 1, one slot per row
 
-    extern __shared__ __align__(16) float2 smem2[];
-    float2* const sU = smem2;
-    float2* const sFY = smem2 + L::oFY;
-    float2* const sFZ = smem2 + L::oFZ;
-    float2* const sG = smem2 + L::oG + threadIdx.x;  // this thread's y/z parts: slot s at sG[s NT]
+    extern __shared__ __align__(16) float smem_f[];
+    V* const smem2 = reinterpret_cast<V*>(smem_f);
+    V* const sU = smem2;
+    V* const sFY = smem2 + L::oFY;
+    V* const sFZ = smem2 + L::oFZ;
+    V* const sG = smem2 + L::oG + threadIdx.x;  // this thread's y/z parts: slot s at sG[s NT]
 
     const int tid = threadIdx.x;
     const int tz = tid % TZ, ty = tid / TZ;
-    const int npairs = (a.nshots + 1) / 2;
+    const int npairs = LANES == 2 ? a.npairs : 1;
     const int pair = blockIdx.x % npairs, tile = blockIdx.x / npairs;
-    const bool hasB = 2 * pair + 1 < a.nshots;
+    constexpr bool hasB = LANES == 2;
     const int tile_y = tile % a.ty0n, tile_z = tile / a.ty0n;
     const int chunk = blockIdx.y;
     const int y0 = tile_y * TY, z0 = tile_z * TZ;
@@ -131,8 +149,9 @@ __global__ void __launch_bounds__(TY* TZ, TY* TZ <= 256 ? 2 : 1) fdtd3d_pass(con
     const int xo0 = chunk * a.chunk_rows, xo1 = min(a.nx, xo0 + a.chunk_rows);
     const int i0 = xo0 - R, i1 = xo1 + R;
     const long long plane = (long long)a.ny * a.zp;
-    const long long offA = (long long)(2 * pair) * a.shot_stride;
-    const long long offB = hasB ? offA + a.shot_stride : offA;  // a lone shot's lane 1 is zero-filled, not stored
+    const int shotA = a.shot0 + (LANES == 2 ? 2 * pair : 0);
+    const long long offA = (long long)shotA * a.shot_stride;
+    const long long offB = offA + a.shot_stride;  // the pair's second shot (two lanes only)
     const long long col = (long long)yc * a.zp + zc;             // offset of this column in a plane
     const float ihx = 1.f / a.hx, ihy = 1.f / a.hy, ihz = 1.f / a.hz;
     const float ihx2 = ihx * ihx, ihy2 = ihy * ihy, ihz2 = ihz * ihz;
@@ -160,17 +179,18 @@ __global__ void __launch_bounds__(TY* TZ, TY* TZ <= 256 ? 2 : 1) fdtd3d_pass(con
         for (int rr = 0; rr < RB; rr++) {
             const int r = ii + rr;
             if (r < i1) {
-                float2* dst = slotp(wrap(si + rr)) + tid;
+                V* dst = slotp(wrap(si + rr)) + tid;
                 const bool row_ok = r >= 0 && r < a.nx;
                 const float* ga = inA + (row_ok ? (long long)r * plane : 0);
-                const float* gb = inB + (row_ok ? (long long)r * plane : 0);
+                [[maybe_unused]] const float* gb = inB + (row_ok ? (long long)r * plane : 0);
 #pragma unroll
                 for (int q = 0; q < NS; q++) {
                     if (q * NT + tid >= L::PLANE) break;
                     const bool ok = row_ok && gofs[q] >= 0;
                     const int o = ok ? gofs[q] : 0;
-                    cp_async4(&dst[q * NT].x, ga + o, ok);
-                    cp_async4(&dst[q * NT].y, gb + o, ok && hasB);
+                    float* d = reinterpret_cast<float*>(dst + q * NT);
+                    cp_async4(d, ga + o, ok);
+                    if constexpr (hasB) cp_async4(d + 1, gb + o, ok);
                 }
             }
         }
@@ -198,11 +218,11 @@ __global__ void __launch_bounds__(TY* TZ, TY* TZ <= 256 ? 2 : 1) fdtd3d_pass(con
     const long long byplane = (long long)(a.ny + 12) * a.zp, bzplane = (long long)a.ny * a.zpb;
     const int cidx = y * a.zp + z;  // this column's offset within a field plane (when col_in)
 
-    float2 uq[QL], fq[STAG ? QL : 1];
+    V uq[QL], fq[STAG ? QL : 1];
 #pragma unroll
     for (int k = 0; k < QL; k++) {
-        uq[k] = f2(0.f);
-        if constexpr (STAG) fq[k] = f2(0.f);
+        uq[k] = vs<V>(0.f);
+        if constexpr (STAG) fq[k] = vs<V>(0.f);
     }
     auto gwrap = [](int s) { return s & (QG - 1); };
     const bool do_save = FINAL && a.save && (a.t % a.f == 0);
@@ -217,7 +237,7 @@ __global__ void __launch_bounds__(TY* TZ, TY* TZ <= 256 ? 2 : 1) fdtd3d_pass(con
         const int j = i - R;  // output row of this iteration's first input row
         float Wj[RB], bxi[RB], byv[RB][VARB ? KY : 1], bzv[RB][VARB ? KZ : 1];
         float c1v[RB], c2v[RB], c3v[RB];
-        float2 uov[RB], pmv[RB];
+        V uov[RB], pmv[RB];
 #pragma unroll
         for (int r = 0; r < RB; r++) {
             Wj[r] = __ldg(a.W + (long long)(j + r) * plane + col);
@@ -239,8 +259,13 @@ __global__ void __launch_bounds__(TY* TZ, TY* TZ <= 256 ? 2 : 1) fdtd3d_pass(con
                 c1v[r] = ok ? __ldg(a.C1 + idx) : 0.f;
                 c2v[r] = ok ? __ldg(a.C2 + idx) : 0.f;
                 c3v[r] = ok ? -__ldg(a.C3 + idx) : 0.f;
-                uov[r] = make_float2(ok ? a.cur[offA + idx] : 0.f, ok && hasB ? a.cur[offB + idx] : 0.f);
-                pmv[r] = make_float2(ok ? a.prev[offA + idx] : 0.f, ok && hasB ? a.prev[offB + idx] : 0.f);
+                if constexpr (LANES == 2) {
+                    uov[r] = make_float2(ok ? a.cur[offA + idx] : 0.f, ok ? a.cur[offB + idx] : 0.f);
+                    pmv[r] = make_float2(ok ? a.prev[offA + idx] : 0.f, ok ? a.prev[offB + idx] : 0.f);
+                } else {
+                    uov[r] = ok ? a.cur[offA + idx] : 0.f;
+                    pmv[r] = ok ? a.prev[offA + idx] : 0.f;
+                }
             }
         }
         (void)bxi; (void)byv; (void)bzv; (void)c1v; (void)c2v; (void)c3v; (void)uov; (void)pmv;
@@ -254,15 +279,15 @@ __global__ void __launch_bounds__(TY* TZ, TY* TZ <= 256 ? 2 : 1) fdtd3d_pass(con
 #pragma unroll
             for (int r = 0; r < RB; r++) {
                 if (i + r < xo0 || i + r >= xo1) continue;
-                const float2* pl = slotp(wrap(sI + r));
+                const V* pl = slotp(wrap(sI + r));
 #pragma unroll
                 for (int q = 0; q < KY; q++) {
                     const int k = tid + q * NT;
                     if (k < (TY + 9) * TZ) {
                         const int ky = k / TZ, kz = k % TZ;
                         const int base = (ky - 5 + R) * PZ + (kz + R);  // half row y0 - 5 + ky (+1/2)
-                        float2 v = mul2(dstag2(pl, base + PZ, base, PZ), f2(ihy));
-                        if constexpr (VARB) v = mul2(v, f2(byv[r][q]));
+                        V v = vmul(dstag<V>(pl, base + PZ, base, PZ), vs<V>(ihy));
+                        if constexpr (VARB) v = vmul(v, vs<V>(byv[r][q]));
                         sFY[r * L::FY + k] = v;
                     }
                 }
@@ -272,8 +297,8 @@ __global__ void __launch_bounds__(TY* TZ, TY* TZ <= 256 ? 2 : 1) fdtd3d_pass(con
                     const int ky = k / WZF, kz = k % WZF;
                     if (k < L::FZ) {
                         const int base = (ky + R) * PZ + (kz - 5 + R);  // half column z0 - 5 + kz (+1/2)
-                        float2 v = mul2(dstag2(pl, base + 1, base, 1), f2(ihz));
-                        if constexpr (VARB) v = mul2(v, f2(bzv[r][q]));
+                        V v = vmul(dstag<V>(pl, base + 1, base, 1), vs<V>(ihz));
+                        if constexpr (VARB) v = vmul(v, vs<V>(bzv[r][q]));
                         sFZ[r * L::FZ + k] = v;
                     }
                 }
@@ -282,68 +307,71 @@ __global__ void __launch_bounds__(TY* TZ, TY* TZ <= 256 ? 2 : 1) fdtd3d_pass(con
 #pragma unroll
             for (int r = 0; r < RB; r++) {
                 if (i + r < xo0 || i + r >= xo1) continue;
-                const float2* Fy = sFY + r * L::FY;
-                const float2* Fz = sFZ + r * L::FZ;
+                const V* Fy = sFY + r * L::FY;
+                const V* Fz = sFZ + r * L::FZ;
                 // D- along y at row ty: fluxes at half rows ty-5 .. ty+4 (index ky = half - y0 + 5)
-                const float2 gy = mul2(dstag2(Fy, (ty + 5) * TZ + tz, (ty + 4) * TZ + tz, TZ), f2(ihy));
-                const float2 gz = mul2(dstag2(Fz, ty * WZF + tz + 5, ty * WZF + tz + 4, 1), f2(ihz));
-                sG[gwrap(gI + r) * NT] = add2(gy, gz);
+                const V gy = vmul(dstag<V>(Fy, (ty + 5) * TZ + tz, (ty + 4) * TZ + tz, TZ), vs<V>(ihy));
+                const V gz = vmul(dstag<V>(Fz, ty * WZF + tz + 5, ty * WZF + tz + 4, 1), vs<V>(ihz));
+                sG[gwrap(gI + r) * NT] = vadd(gy, gz);
             }
         } else {
 #pragma unroll
             for (int r = 0; r < RB; r++) {
                 if (i + r < xo0 || i + r >= xo1) continue;
-                const float2* pl = slotp(wrap(sI + r));
-                sG[gwrap(gI + r) * NT] = fma2(dcent2(pl, me, PZ), f2(ihy2), mul2(dcent2(pl, me, 1), f2(ihz2)));
+                const V* pl = slotp(wrap(sI + r));
+                sG[gwrap(gI + r) * NT] = vfma(dcent<V>(pl, me, PZ), vs<V>(ihy2), vmul(dcent<V>(pl, me, 1), vs<V>(ihz2)));
             }
         }
         // the x parts of the output rows j .. j+RB-1, their y and z parts from the queue
-        float2 res[RB];
+        V res[RB];
 #pragma unroll
         for (int r = 0; r < RB; r++) {
-            float2 gx;
+            V gx;
             if constexpr (STAG) {
-                float2 v = mul2(dstag2(uq, r + 5, r + 4, 1), f2(ihx));
-                if constexpr (VARB) v = mul2(v, f2(bxi[r]));
+                V v = vmul(dstag<V>(uq, r + 5, r + 4, 1), vs<V>(ihx));
+                if constexpr (VARB) v = vmul(v, vs<V>(bxi[r]));
                 fq[QB + r] = v;
-                gx = mul2(dstag2(fq, r + 5, r + 4, 1), f2(ihx));
+                gx = vmul(dstag<V>(fq, r + 5, r + 4, 1), vs<V>(ihx));
             } else {
-                gx = mul2(dcent2(uq, r + 5, 1), f2(ihx2));
+                gx = vmul(dcent<V>(uq, r + 5, 1), vs<V>(ihx2));
             }
             // the y/z part of row j + r (written by this thread R rows ago; zero-row reads unused)
-            const float2 g = add2(gx, j + r >= xo0 && j + r < xo1 ? sG[gwrap(gI - R + r) * NT] : f2(0.f));
+            const V g = vadd(gx, j + r >= xo0 && j + r < xo1 ? sG[gwrap(gI - R + r) * NT] : vs<V>(0.f));
             if constexpr (FINAL && OT4) {
                 // Lt = l + dt^2/12 W G(l): the streamed l at row j+r is queue entry r (STAG,
                 // rows i-9..) or r+5 (laplace, rows i-10..)
-                res[r] = fma2(f2(k12), mul2(f2(Wj[r]), g), STAG ? uq[r] : uq[r + 5]);
+                res[r] = vfma(vs<V>(k12), vmul(vs<V>(Wj[r]), g), STAG ? uq[r] : uq[r + 5]);
             } else {
-                res[r] = mul2(f2(Wj[r]), g);
+                res[r] = vmul(vs<V>(Wj[r]), g);
             }
         }
-        qshift2<QL, RB>(uq);
-        if constexpr (STAG) qshift2<QL, RB>(fq);
+        qshift<QL, RB>(uq);
+        if constexpr (STAG) qshift<QL, RB>(fq);
 #pragma unroll
         for (int r = 0; r < RB; r++) {
             const int row = j + r;
             if (row < xo0 || row >= xo1 || !col_in) continue;
             const long long idx = (long long)row * plane + cidx;
+            // lane values: .x and .y of a pair, the value itself for a lone shot
+            const float* rv = reinterpret_cast<const float*>(&res[r]);
             if constexpr (!FINAL) {
-                a.out_l[offA + idx] = res[r].x;
-                if (hasB) a.out_l[offB + idx] = res[r].y;
+                a.out_l[offA + idx] = rv[0];
+                if constexpr (hasB) a.out_l[offB + idx] = rv[1];
             } else {
-                const float2 u_o = uov[r], pm = pmv[r];
-                const float2 pn = fma2(f2(c1v[r]), res[r], fma2(f2(c2v[r]), u_o, mul2(f2(c3v[r]), pm)));
+                const V u_o = uov[r], pm = pmv[r];
+                const V pn = vfma(vs<V>(c1v[r]), res[r], vfma(vs<V>(c2v[r]), u_o, vmul(vs<V>(c3v[r]), pm)));
+                const float* pnv = reinterpret_cast<const float*>(&pn);
                 if (do_save) {  // 2: raw p[t] (rho gradient), else p.dt2
-                    const float2 sv = a.save == 2 ? u_o
-                                                  : make_float2((pn.x - 2.f * u_o.x + pm.x) / dt2,
-                                                                (pn.y - 2.f * u_o.y + pm.y) / dt2);
-                    float* sa0 = a.snaps + (long long)(2 * pair) * a.snap_shot_stride +
+                    const float* uv = reinterpret_cast<const float*>(&u_o);
+                    const float* pv = reinterpret_cast<const float*>(&pm);
+                    float* sa0 = a.snaps + (long long)shotA * a.snap_shot_stride +
                                  (long long)(a.t / a.f) * a.snap_stride + idx;
-                    sa0[0] = sv.x;
-                    if (hasB) sa0[a.snap_shot_stride] = sv.y;
+#pragma unroll
+                    for (int l = 0; l < LANES; l++)
+                        sa0[l * a.snap_shot_stride] = a.save == 2 ? uv[l] : (pnv[l] - 2.f * uv[l] + pv[l]) / dt2;
                 }
-                a.prev[offA + idx] = pn.x;
-                if (hasB) a.prev[offB + idx] = pn.y;
+                a.prev[offA + idx] = pnv[0];
+                if constexpr (hasB) a.prev[offB + idx] = pnv[1];
             }
         }
         sI += RB;

@@ -14,9 +14,12 @@ struct Tile3D {
 };
 constexpr Tile3D kTiles3d[] = {{16, 32}, {8, 32}};
 constexpr int kTiles3dN = 2;
-cudaError_t launch_step3d_k0(int tile, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
-cudaError_t launch_step3d_k1(int tile, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
-cudaError_t launch_step3d_k2(int tile, bool final_pass, bool ot4, dim3 grid, cudaStream_t s, const Step3D& a);
+cudaError_t launch_step3d_k0(int tile, int lanes, bool final_pass, bool ot4, dim3 grid, cudaStream_t s,
+                             const Step3D& a);
+cudaError_t launch_step3d_k1(int tile, int lanes, bool final_pass, bool ot4, dim3 grid, cudaStream_t s,
+                             const Step3D& a);
+cudaError_t launch_step3d_k2(int tile, int lanes, bool final_pass, bool ot4, dim3 grid, cudaStream_t s,
+                             const Step3D& a);
 #ifndef SA_RB3
 #define SA_RB3 2
 #endif
@@ -25,12 +28,13 @@ cudaError_t launch_step3d_k2(int tile, bool final_pass, bool ot4, dim3 grid, cud
 #endif
 constexpr int kRows3d = SA_RB3, kPrefetch3d = SA_PF3;  // x rows per iteration of a 3D pass, iterations prefetched
 
-inline cudaError_t launch_step3d(int kind, int tile, bool final_pass, bool ot4, dim3 grid, cudaStream_t s,
+// lanes 2: a.npairs pairs from shot a.shot0; lanes 1: the lone shot a.shot0
+inline cudaError_t launch_step3d(int kind, int tile, int lanes, bool final_pass, bool ot4, dim3 grid, cudaStream_t s,
                                  const Step3D& a) {
     switch (kind) {
-        case 0: return launch_step3d_k0(tile, final_pass, ot4, grid, s, a);
-        case 1: return launch_step3d_k1(tile, final_pass, ot4, grid, s, a);
-        default: return launch_step3d_k2(tile, final_pass, ot4, grid, s, a);
+        case 0: return launch_step3d_k0(tile, lanes, final_pass, ot4, grid, s, a);
+        case 1: return launch_step3d_k1(tile, lanes, final_pass, ot4, grid, s, a);
+        default: return launch_step3d_k2(tile, lanes, final_pass, ot4, grid, s, a);
     }
 }
 

@@ -552,25 +552,50 @@ static int image_raw_level(Plan3D* p, const Step3D& a, const float* q, bool rho,
     return SA_OK;
 }
 
+// One pass over every shot of the plan: the shot pairs in one launch (two lanes), a lone last shot
+// of an odd batch in a one-lane launch. Returns the launches made (or a negative error).
+static int pass3(Plan3D* p, bool final_pass, bool ot4, Step3D a, cudaStream_t s) {
+    const int np = p->n_shots / 2, tiles = p->ty0n * p->tz0n;
+    int made = 0;
+    if (np > 0) {
+        a.shot0 = 0;
+        a.npairs = np;
+        const cudaError_t e = launch_step3d(p->kind, p->tile, 2, final_pass, ot4, dim3(tiles * np, p->nchunks, 1), s, a);
+        if (e != cudaSuccess) return fail3(SA_E_CUDA, cudaGetErrorString(e));
+        made++;
+    }
+    if (p->n_shots & 1) {
+        a.shot0 = p->n_shots - 1;
+        a.npairs = 1;
+        const cudaError_t e = launch_step3d(p->kind, p->tile, 1, final_pass, ot4, dim3(tiles, p->nchunks, 1), s, a);
+        if (e != cudaSuccess) return fail3(SA_E_CUDA, cudaGetErrorString(e));
+        made++;
+    }
+    return made;
+}
+#define PASS3(final_pass, ot4, a)                                \
+    do {                                                         \
+        const int m_ = pass3(p, (final_pass), (ot4), (a), s);    \
+        if (m_ < 0) return m_;                                   \
+        n += m_;                                                 \
+    } while (0)
+
 // One time level: [pass A] + pass B, then injection into the new level (and its snapshot).
 // which: 0 injects the sources (amp = their samples), 1 the receivers, -1 nothing; linear or wide (Hicks, sinc)
 // as the plan's interpolation. aux: the CFS-PML auxiliary fields advanced (default: the plan's).
 static int step3(Plan3D* p, Step3D& a, const float* cur, float* prev, int which, const float* amp, bool save_now,
                  cudaStream_t s, long long& n, float* aux = nullptr) {
-    const dim3 grid(p->ty0n * p->tz0n * ((p->n_shots + 1) / 2), p->nchunks, 1);  // shot pairs
     a.cur = cur;
     a.prev = prev;
     if (p->ot4) {
         a.in = cur;
         a.out_l = p->Lbuf;
-        CK3(launch_step3d(p->kind, p->tile, false, true, grid, s, a));
+        PASS3(false, true, a);
         a.in = p->Lbuf;
-        n++;
     } else {
         a.in = cur;
     }
-    CK3(launch_step3d(p->kind, p->tile, true, p->ot4, grid, s, a));
-    n++;
+    PASS3(true, p->ot4, a);
     const float inv_dt2 = (float)(1.0 / ((double)a.dt * (double)a.dt));
     if (p->pml) {  // auxiliary fields and the boundary term of the new level (which 1: the adjoint)
         CK3(pml3d(cur, prev, aux ? aux : p->pml_aux, p->pml_prof, p->C1 + (long long)GUARD * p->plane, p->vp, p->nx, p->ny, p->nz,
@@ -984,7 +1009,6 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
     la.C2 = la.C3 = p->zeros + G * p->plane;
     const Sparse3D src{p->s_shot, p->s_base, p->s_w, p->s_coef};
     const Sparse3D recx{p->r_shot, p->r_base, p->r_w, p->r_xcoef};
-    const dim3 grid(p->ty0n * p->tz0n * ((p->n_shots + 1) / 2), p->nchunks, 1);  // shot pairs
     const float inv_dt2 = (float)(1.0 / (p->d.dt * p->d.dt));
     const double h = std::max(p->d.spacing[0], std::max(p->d.spacing[1], p->d.spacing[2]));
     const float src_scale = (float)(2.0 * p->d.dt / h);
@@ -1032,14 +1056,13 @@ int plan3d_adjoint_exact(Plan3D* p, const float* residuals, float* grad, float* 
                 la.t = t - 1;
                 la.cur = la.in = lvl(k, t - 1);
                 la.prev = p->Lu;
-                CK3(launch_step3d(p->kind, p->tile, true, false, grid, s, la));
+                PASS3(true, false, la);
                 la.t = t;
                 la.cur = la.in = zt;
                 la.prev = p->Lz;
-                CK3(launch_step3d(p->kind, p->tile, true, false, grid, s, la));
+                PASS3(true, false, la);
                 Lu = p->Lu;
                 Lz = p->Lz;
-                n += 2;
             }
             CK3(exact_grad3d(zt, lvl(k, t), lvl(k, t - 1), lvl(k, t - 2), Lu, Lz, p->EA, p->EB, p->EC, p->EG4, p->nx,
                              p->ny, p->nz, p->zp, p->n_shots, p->field, inv_dt2, p->gradb, p->precb, s));
@@ -1118,9 +1141,8 @@ int plan3d_autotune(Plan3D* p, const char* device_key, int* tile_out, int* chunk
             set_chunks(p, nc);
             Step3D a = args3(p);
             a.save = 0;
-            const dim3 grid(p->ty0n * p->tz0n * ((p->n_shots + 1) / 2), p->nchunks, 1);
-            int rc = SA_OK;
-            for (int t = 0; t < 2 + steps && rc == SA_OK; t++) {
+            long long n = 0;
+            for (int t = 0; t < 2 + steps; t++) {
                 if (t == 2) CK3(cudaEventRecord(e0, s));
                 a.t = 1 + t;
                 a.cur = p->F[t & 1];
@@ -1128,12 +1150,12 @@ int plan3d_autotune(Plan3D* p, const char* device_key, int* tile_out, int* chunk
                 if (p->ot4) {
                     a.in = a.cur;
                     a.out_l = p->Lbuf;
-                    CK3(launch_step3d(p->kind, p->tile, false, true, grid, s, a));
+                    PASS3(false, true, a);
                     a.in = p->Lbuf;
                 } else {
                     a.in = a.cur;
                 }
-                CK3(launch_step3d(p->kind, p->tile, true, p->ot4, grid, s, a));
+                PASS3(true, p->ot4, a);
             }
             CK3(cudaEventRecord(e1, s));
             CK3(cudaEventSynchronize(e1));
