@@ -1,11 +1,12 @@
 // 3D iso-acoustic FDTD time step for sm_103a (stride/physics/iso_acoustic/devito.py:1466-1608 in
 // 3D). The grid is [x][y][z], z contiguous, one array per shot. A CTA owns a TY x TZ tile of
 // (y, z) columns of a PAIR of shots and computes both in packed FP32 (one f32x2 instruction for
-// the two shots): it streams the x planes of its input field through a shared-memory ring of
-// float2 (the two shots interleaved by 4-byte cp.async, zero-filled beyond the grid: Devito's zero
-// halo). The y and z derivatives of a row are taken from its plane as soon as it arrives and wait
-// in a register queue until the x derivatives (per-thread register queues along x) reach that
-// row, so the ring holds only the planes in flight.
+// the two shots; a lone shot of an odd batch runs the same code with one lane): it streams the x
+// planes of its input field through a shared-memory ring (the two shots interleaved by 4-byte
+// cp.async, zero-filled beyond the grid: Devito's zero halo). The y and z derivatives of a row are
+// taken from its plane as soon as it arrives and wait in a per-thread shared-memory ring until the
+// x derivatives (per-thread register queues along x) reach that row, so the plane ring holds only
+// the planes in flight.
 //
 // One application of the spatial operator per pass (a 3D halo of 9 cells around a small tile
 // makes fusing OT4's two applications more expensive than a second pass):
