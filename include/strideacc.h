@@ -310,6 +310,13 @@ int sa_nn_pack_weights(const float* w, int Cout, int Kr, void* wb, void* wt, int
 /* Adam step (bias-corrected, step >= 1) on fp32 master weights. */
 int sa_nn_adam(float* w, const float* g, float* m, float* v, long long n, float lr, float b1, float b2, float eps,
                int step, void* stream);
+/* Adam's bias corrections for steps 1..nsteps, c12[2k] = 1 - b1^(k+1), c12[2k+1] = 1 - b2^(k+1)
+ * (the values sa_nn_adam forms), into device memory (synchronous). */
+int sa_nn_adam_corrections(float b1, float b2, int nsteps, float* c12);
+/* sa_nn_adam with the step read from device memory (*step, clamped to 1..nsteps) and its bias
+ * corrections from c12: the form a captured training step (CUDA graph) replays. */
+int sa_nn_adam_dev(float* w, const float* g, float* m, float* v, long long n, float lr, float b1, float b2, float eps,
+                   const float* c12, int nsteps, const int* step, void* stream);
 /* *loss = mean (out - target)^2 (FP64, device), dout = 2 (out - target) / n. */
 int sa_nn_mse(const float* out, int ldo, const float* target, long long n, float* dout, int ldd, double* loss,
               void* stream);

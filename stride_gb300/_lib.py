@@ -49,7 +49,8 @@ EXPORTS = ('sa_plan_create', 'sa_plan_destroy', 'sa_set_medium', 'sa_set_geometr
            'sa_field_scale', 'sa_field_gaussian', 'sa_field_apply_prec', 'sa_gemm_bf16', 'sa_nn_im2col',
            'sa_nn_col2im', 'sa_nn_transpose_bf16', 'sa_nn_to_bf16', 'sa_nn_relu_bwd', 'sa_nn_bias_grad',
            'sa_nn_maxpool', 'sa_nn_maxpool_bwd', 'sa_nn_upsample', 'sa_nn_upsample_bwd', 'sa_nn_copy_channels',
-           'sa_nn_pack_weights', 'sa_nn_adam', 'sa_nn_mse', 'sa_nn_sum_slabs', 'sa_conv3x3_bf16')
+           'sa_nn_pack_weights', 'sa_nn_adam', 'sa_nn_mse', 'sa_nn_sum_slabs', 'sa_conv3x3_bf16',
+           'sa_nn_adam_corrections', 'sa_nn_adam_dev')
 
 
 class SaDesc(ctypes.Structure):
@@ -128,6 +129,8 @@ def load():
     lib.sa_nn_copy_channels.argtypes = [P, I, L, I, P, I, I, P]
     lib.sa_nn_pack_weights.argtypes = [P, I, I, P, P, I, I, P]
     lib.sa_nn_adam.argtypes = [P, P, P, P, L, F, F, F, F, I, P]
+    lib.sa_nn_adam_corrections.argtypes = [F, F, I, P]
+    lib.sa_nn_adam_dev.argtypes = [P, P, P, P, L, F, F, F, F, P, I, P, P]
     lib.sa_nn_mse.argtypes = [P, I, P, L, P, I, P, P]
     for name in EXPORTS:
         if name not in ('sa_launch_count',):

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "../../include/strideacc.h"
 #include "helpers.h"
@@ -246,6 +247,22 @@ __global__ void k_adam(float* w, const float* __restrict__ g, float* m, float* v
     }
 }
 
+// The same update with the step read on the device (a captured training step): bias corrections
+// c12[2 (step - 1)], c12[2 (step - 1) + 1], the step clamped to the table.
+__global__ void k_adam_dev(float* w, const float* __restrict__ g, float* m, float* v, long long n, float lr, float b1,
+                           float b2, float eps, const float* __restrict__ c12, int nsteps, const int* step) {
+    const int k = min(max(*step, 1), nsteps) - 1;
+    const float c1 = c12[2 * k], c2 = c12[2 * k + 1];
+    GRID_LOOP(q, n) {
+        const float gg = g[q];
+        const float mm = b1 * m[q] + (1.f - b1) * gg;
+        const float vv = b2 * v[q] + (1.f - b2) * gg * gg;
+        m[q] = mm;
+        v[q] = vv;
+        w[q] -= lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+    }
+}
+
 // loss += sum (out - t)^2 / n (FP64), dout = 2 (out - t) / n; out has channel stride ldo
 __global__ void k_mse(const float* __restrict__ out, int ldo, const float* __restrict__ t, long long n, float* dout,
                       int ldd, double* loss) {
@@ -381,6 +398,27 @@ int sa_nn_adam(float* w, const float* g, float* m, float* v, long long n, float 
     if (n == 0) return SA_OK;
     const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
     k_adam<<<nblocks(n), 256, 0, (cudaStream_t)stream>>>(w, g, m, v, n, lr, b1, b2, eps, c1, c2);
+    CKN(cudaGetLastError());
+    return SA_OK;
+}
+
+int sa_nn_adam_corrections(float b1, float b2, int nsteps, float* c12) {
+    if (!c12 || nsteps < 1) return fail_n(SA_E_INVALID, "sa_nn_adam_corrections: bad arguments");
+    std::vector<float> h(2 * (size_t)nsteps);
+    for (int k = 0; k < nsteps; k++) {  // as sa_nn_adam forms them
+        h[2 * k] = 1.f - powf(b1, (float)(k + 1));
+        h[2 * k + 1] = 1.f - powf(b2, (float)(k + 1));
+    }
+    CKN(cudaMemcpy(c12, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return SA_OK;
+}
+
+int sa_nn_adam_dev(float* w, const float* g, float* m, float* v, long long n, float lr, float b1, float b2, float eps,
+                   const float* c12, int nsteps, const int* step, void* stream) {
+    if (!w || !g || !m || !v || !c12 || !step || n < 0 || nsteps < 1)
+        return fail_n(SA_E_INVALID, "sa_nn_adam_dev: bad arguments");
+    if (n == 0) return SA_OK;
+    k_adam_dev<<<nblocks(n), 256, 0, (cudaStream_t)stream>>>(w, g, m, v, n, lr, b1, b2, eps, c12, nsteps, step);
     CKN(cudaGetLastError());
     return SA_OK;
 }

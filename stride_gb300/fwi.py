@@ -296,21 +296,32 @@ def generate_pairs(fwi, phantoms_vp, iterations=5, f_max=None):
     return torch.cat(xs), torch.cat(ts)
 
 
-def train_unet(net, X, T, epochs=20, batch=4, lr=1e-3, seed=0):
-    """Adam on the mean squared error of the predicted update; returns the per-epoch losses."""
+def train_unet(net, X, T, epochs=20, batch=4, lr=1e-3, seed=0, graph=True):
+    """Adam on the mean squared error of the predicted update; returns the per-epoch losses. With
+    graph, every step replays one captured training step (unet.GraphTrainer), bit for bit the eager
+    step."""
+    from .unet import GraphTrainer
     g = torch.Generator(device='cpu').manual_seed(seed)
     n = X.shape[0]
     losses = []
+    trainer = GraphTrainer(net, batch, X.shape[1], X.shape[2], X.shape[3], lr=lr) if graph and n >= batch else None
     for _ in range(epochs):
         perm = torch.randperm(n, generator=g)
         tot = 0.
+        if trainer is not None:
+            trainer.loss_sum.zero_()
         for i in range(0, n - batch + 1, batch):
             idx = perm[i:i + batch].to(X.device)
+            if trainer is not None:
+                trainer.train_step(X[idx], T[idx])
+                continue
             y = net.forward(X[idx].contiguous())
             loss, d = net.mse(y, T[idx].contiguous())
             net.backward(d)
             net.adam_step(lr=lr)
             tot += float(loss.item())
+        if trainer is not None:
+            tot = float(trainer.loss_sum.item())
         losses.append(tot / max(1, n // batch))
     return losses
 

@@ -18,7 +18,7 @@ import torch
 
 from . import _lib, h5
 
-__all__ = ['UNet']
+__all__ = ['UNet', 'GraphTrainer']
 
 
 def _up(x, m):
@@ -249,6 +249,15 @@ class UNet:
                 _ck(lib.sa_nn_adam(_p(w), _p(g), _p(m), _p(v), w.numel(), lr, b1, b2, eps, self.step_count, _s()))
             layer.pack()
 
+    def adam_step_dev(self, lr, b1, b2, eps, c12, nsteps, step):
+        """adam_step with the step count in device memory (a captured training step)."""
+        lib = _lib.load()
+        for layer in self.layers():
+            for w, g, m, v in layer.params():
+                _ck(lib.sa_nn_adam_dev(_p(w), _p(g), _p(m), _p(v), w.numel(), lr, b1, b2, eps, _p(c12), nsteps,
+                                       _p(step), _s()))
+            layer.pack()
+
     def mse(self, y, target):
         """Mean squared error of channel 0 of forward()'s result y against target [B, H, W] and its
         gradient, shaped for backward()."""
@@ -279,3 +288,48 @@ class UNet:
     def load(self, filename):
         """Weights from a file written by ``dump``."""
         self.load_state_dict(h5.HDF5(filename, mode='r').load(lazy=False))
+
+
+class GraphTrainer:
+    """One Adam step of a UNet on batches of a fixed shape (forward, MSE, backward, Adam, BF16
+    repack) captured once as a CUDA graph and replayed per batch: one launch instead of the
+    step's few hundred kernel calls from the host. The step count lives in device memory and the
+    bias corrections in a table formed as adam_step forms them, so a replayed step is bit for bit
+    the eager step. The loss is summed on the device (loss_sum)."""
+
+    def __init__(self, net, B, H, W, cin, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, max_steps=1 << 16):
+        lib = _lib.load()
+        dev = net.device
+        self.net = net
+        self.x = torch.zeros((B, H, W, cin), device=dev)
+        self.t = torch.zeros((B, H, W), device=dev)
+        self.step = torch.full((1,), net.step_count, dtype=torch.int32, device=dev)
+        self.max_steps = max_steps
+        self.c12 = torch.empty(2 * max_steps, device=dev)
+        _ck(lib.sa_nn_adam_corrections(b1, b2, max_steps, _p(self.c12)))
+        self.loss_sum = torch.zeros(1, dtype=torch.float64, device=dev)
+        # warm-up on a side stream: kernel attributes set, no weight updated
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            y = net.forward(self.x)
+            _, d = net.mse(y, self.t)
+            net.backward(d)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            y = net.forward(self.x)
+            loss, d = net.mse(y, self.t)
+            net.backward(d)
+            self.step += 1
+            net.adam_step_dev(lr, b1, b2, eps, self.c12, max_steps, self.step)
+            self.loss_sum += loss
+
+    def train_step(self, x, t):
+        """One step on the batch x [B, H, W, cin], target t [B, H, W]."""
+        self.x.copy_(x)
+        self.t.copy_(t)
+        self.graph.replay()
+        self.net.step_count += 1
+

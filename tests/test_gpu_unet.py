@@ -219,3 +219,30 @@ def test_unet_training_is_reproducible():
                                           (p for l in nets[1].layers() for p in l.params())):
         assert torch.equal(a, b)
 
+
+
+def test_graph_training_step_equals_eager():
+    """A training step captured as a CUDA graph and replayed (unet.GraphTrainer) leaves the network
+    bit for bit where the eager steps do, loss included."""
+    from stride_gb300.unet import GraphTrainer, UNet
+    torch.manual_seed(4)
+    B, H, W = 4, 64, 64
+    xs = [torch.randn(B, H, W, 2, device='cuda') for _ in range(5)]
+    ts = [torch.randn(B, H, W, device='cuda') for _ in range(5)]
+    eager = UNet(seed=7)
+    loss_eager = 0.0
+    for x, t in zip(xs, ts):
+        y = eager.forward(x)
+        loss, d = eager.mse(y, t)
+        eager.backward(d)
+        eager.adam_step(lr=1e-3)
+        loss_eager += float(loss.item())
+    graphed = UNet(seed=7)
+    trainer = GraphTrainer(graphed, B, H, W, 2, lr=1e-3)
+    for x, t in zip(xs, ts):
+        trainer.train_step(x, t)
+    assert float(trainer.loss_sum.item()) == loss_eager
+    assert eager.errors() == 0 and graphed.errors() == 0
+    for la, lb in zip(eager.layers(), graphed.layers()):
+        for (a, _, _, _), (b, _, _, _) in zip(la.params(), lb.params()):
+            assert torch.equal(a, b)
