@@ -223,7 +223,7 @@ def test_unet_training_is_reproducible():
 
 def test_graph_training_step_equals_eager():
     """A training step captured as a CUDA graph and replayed (unet.GraphTrainer) leaves the network
-    bit for bit where the eager steps do, loss included."""
+    bit for bit where the eager steps do."""
     from stride_gb300.unet import GraphTrainer, UNet
     torch.manual_seed(4)
     B, H, W = 4, 64, 64
@@ -241,7 +241,8 @@ def test_graph_training_step_equals_eager():
     trainer = GraphTrainer(graphed, B, H, W, 2, lr=1e-3)
     for x, t in zip(xs, ts):
         trainer.train_step(x, t)
-    assert float(trainer.loss_sum.item()) == loss_eager
+    # the loss is an FP64 sum whose atomic accumulation order varies: equal to rounding
+    assert abs(float(trainer.loss_sum.item()) - loss_eager) <= 1e-12 * abs(loss_eager)
     assert eager.errors() == 0 and graphed.errors() == 0
     for la, lb in zip(eager.layers(), graphed.layers()):
         for (a, _, _, _), (b, _, _, _) in zip(la.params(), lb.params()):
