@@ -32,23 +32,23 @@ namespace sa {
 
 namespace {
 
-// Exchange lines: p at one point of a shot pair with the level it belongs to, {p0, level, p1, level},
-// stored and loaded as one 16-byte volatile access. A reader takes a line when both level words
-// match; each 8-byte half (value and level) is written and read whole, so a matching line holds
-// that level's values.
+// Exchange lines: p at one point of a shot pair with the level it belongs to, {p0, level, p1, level}
+// as 32-bit words, stored and loaded as one 16-byte access of two 64-bit elements, each a value in
+// its low word and the level in its high word. The memory model treats the elements of a vector
+// access as separate accesses, each naturally aligned 64-bit element as one single-copy atomic
+// access: a reader takes a line when both level words match, and each element then holds that
+// level's value.
 __device__ __forceinline__ void st_line(uint4* q, float2 v, unsigned level) {
-    asm volatile("st." PERSIST_LINE_SEM ".global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(q), "r"(__float_as_uint(v.x)), "r"(level),
-                 "r"(__float_as_uint(v.y)), "r"(level)
+    const unsigned long long hi = (unsigned long long)level << 32;
+    asm volatile("st." PERSIST_LINE_SEM ".global.v2.u64 [%0], {%1, %2};" ::"l"(q),
+                 "l"(hi | __float_as_uint(v.x)), "l"(hi | __float_as_uint(v.y))
                  : "memory");
 }
 
 __device__ __forceinline__ uint4 ld_line(const uint4* q) {
-    uint4 v;
-    asm volatile("ld." PERSIST_LINE_SEM ".global.v4.u32 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "l"(q)
-                 : "memory");
-    return v;
+    unsigned long long e0, e1;
+    asm volatile("ld." PERSIST_LINE_SEM ".global.v2.u64 {%0, %1}, [%2];" : "=l"(e0), "=l"(e1) : "l"(q) : "memory");
+    return make_uint4((unsigned)e0, (unsigned)(e0 >> 32), (unsigned)e1, (unsigned)(e1 >> 32));
 }
 
 // Buoyancy tables of a CTA in shared memory: bx at half-rows [fx0, fx0 + fh) x columns
