@@ -75,6 +75,61 @@ def test_numpy_matches_golden():
     np.testing.assert_array_equal(pp, g['prec'])
 
 
+def _refined_traces(level, kernel):
+    """A homogeneous 2D shot (vp 1500) at h = 2 mm / 2^level and dt = 0.4 h / 1500 (fixed CFL),
+    over the same physical domain (110 mm inner, a 20 mm sponge) and time window (51 us), in the
+    FP64 oracle. The source (a Gaussian derivative, sigma 3 us) and the receivers (20-30 mm away,
+    so that nothing returns from the sponge within the window) sit on nodes of the coarsest
+    grid; the coordinates are given 1e-3 h below the nodes so that the reference's eps shift
+    (iso_acoustic/devito.py:307-309) puts them on the nodes at every level. The injection
+    amplitude 2 dt vp / h (:357-363) makes the same continuous source at every level."""
+    h = 2e-3 / 2 ** level
+    n, ab = 55 * 2 ** level + 1, 10 * 2 ** level
+    dt = 0.4 * h / 1500.
+    nt = 96 * 2 ** level + 1
+    t = np.arange(nt) * dt
+    sig = 3e-6
+    wav = -(t - 5 * sig) / sig * np.exp(-0.5 * ((t - 5 * sig) / sig) ** 2)
+    c = 54e-3
+    offs = [(20, 0), (0, 24), (-14, 14), (30, -6), (-22, -18)]
+    src = np.array([[c, c]]) - 1e-3 * h
+    rec = np.array([[c + a * 1e-3, c + b * 1e-3] for a, b in offs]) - 1e-3 * h
+    vp = np.full((n + 2 * ab,) * 2, 1500., np.float32)
+    tr, _ = O.forward(vp, (h, h), dt, nt, (ab, ab), src.astype(np.float32), rec.astype(np.float32), wav[None],
+                      (-ab * h, -ab * h), kernel=kernel, dtype=np.float64)
+    # rec[k] of a level is p at time (k + 1) dt: the coarse samples 1 .. nt - 2 on every level
+    k = np.arange(1, 96)
+    return tr[:, (k + 1) * 2 ** level - 1].astype(np.float64)
+
+
+def test_self_convergence_under_refinement():
+    """The oracle converges under h/2, dt/2 refinement at fixed CFL: the trace differences between
+    successive levels fall by 4 per level (second order; measured 2.00 for OT2 and 2.03 for OT4,
+    whose update is fourth order in time but whose point source enters without the dt^2/12
+    correction, so that the source term is second order). OT4's differences are the smaller."""
+    err = {}
+    for kernel in ('OT2', 'OT4'):
+        s = [_refined_traces(level, kernel) for level in range(3)]
+        e = [np.linalg.norm(s[i] - s[i + 1]) / np.linalg.norm(s[2]) for i in range(2)]
+        order = np.log2(e[0] / e[1])
+        assert 1.8 <= order <= 2.3, (kernel, e, order)
+        err[kernel] = e
+    assert err['OT4'][1] < 0.6 * err['OT2'][1] and err['OT2'][1] < 5e-3
+
+
+@pytest.mark.parametrize('kernel,rho_mode,alpha', [('OT4', 'variable', True), ('OT2', 'constant', False)])
+def test_fp32_noise_floor(kernel, rho_mode, alpha):
+    """The FP32 oracle against the same oracle in FP64: the FP32 rounding of a 300-step shot
+    (measured 0.9-4.0e-6 relative) lies well below the 1e-4 trace tolerance of the parity tests."""
+    from tests import _cases as C
+    c = C.small_case(kernel=kernel, density=rho_mode, alpha=alpha, nt=300)
+    origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
+    tr = [O.forward(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][0], c['recs'][0], c['wav'][None],
+                    origin, rho=c['rho'], alpha=c['alpha'], kernel=kernel, dtype=d)[0].astype(np.float64)
+          for d in (np.float32, np.float64)]
+    assert np.linalg.norm(tr[0] - tr[1]) <= 1e-5 * np.linalg.norm(tr[1])
+
+
 @pytest.mark.parametrize('dim,n', [(2, 40), (3, 22)])
 @pytest.mark.parametrize('kernel', ['OT2', 'OT4'])
 @pytest.mark.parametrize('rho_mode', ['none', 'variable', 'constant'])
