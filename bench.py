@@ -49,6 +49,7 @@ WORKLOADS = {
     'fwdadj64': ('batched', 64, 'fwdadj'),  # default: the fwd+adj vp gradient of the headline metric
     'fwd256': ('batched', 256, 'fwd'),      # batched forward, one shot per transducer
     'single': ('single', 1, 'fwd'),         # single-shot forward, 256^2 at 0.5 mm, vp only
+    'single256': ('single', 1, 'fwd'),      # the same with 256^2 as the whole grid, sponge included
     '3d': ('3d', 8, 'fwd'),                 # 3D forward, 296^3, 8 shots per launch
     '3dgrad': ('3d', 1, 'fwdadj'),          # 3D fwd+adj vp gradient of one shot (snapshots in HBM)
     'exact64': ('batched', 64, 'fwdadj'),   # exact gradient (autograd backward), checkpoints every 50 steps
@@ -71,12 +72,16 @@ GRADIENT = {
 }
 # time step of the workload's grid as a CFL number (OT2 needs one below its stability limit)
 CFL = {'pml64': 0.4}
+# inner grid of a workload smaller than its generator's
+INNER = {'single256': 216}
 WORKLOAD_NAMES = {
     'fwdadj64': '2D fwd+adj vp gradient: 552^2 extended (512^2 at 0.25 mm + 20 sponge), vp/rho/alpha phantom, '
                 '64 shots x 256 receivers, 4000 steps, OT4, f=4',
     'fwd256': '2D batched forward: 552^2 extended, vp/rho/alpha phantom, 256 shots x 256 receivers, 4000 steps, OT4',
     'single': '2D single-shot forward: 296^2 extended (256^2 at 0.5 mm + 20 sponge), vp phantom, 128 receivers, '
               '2000 steps, OT4',
+    'single256': '2D single-shot forward: 256^2 extended (216^2 at 0.5 mm + 20 sponge), vp phantom, 128 receivers, '
+                 '2000 steps, OT4',
     '3d': '3D forward: 296^3 extended (256^3 at 0.5 mm + 20 sponge), vp/rho/alpha phantom, 8 shots x 512 receivers, '
           '3000 steps, OT4',
     '3dgrad': '3D fwd+adj vp gradient: 296^3 extended, vp/rho/alpha phantom, 1 shot x 512 receivers, 3000 steps, '
@@ -114,7 +119,7 @@ def workload_config(name='fwdadj64', nt=None, n_shots=None, rank=0):
     if gen == '3d':
         w = phantoms.workload3d(seed=0, nt=nt, n_shots=n_shots)
     else:
-        w = phantoms.workload(gen, seed=0, nt=nt, cfl=CFL.get(name, 0.6))
+        w = phantoms.workload(gen, seed=0, nt=nt, cfl=CFL.get(name, 0.6), inner=INNER.get(name))
     ntr = len(w['geometry'])
     stride = max(1, ntr // n_shots)
     first = rank % stride
