@@ -216,18 +216,28 @@ class PlainFWI:
         return misfit, grad, prec
 
     def direction(self, grad, prec):
-        """Processed update direction (Data.apply_prec, then mask / smooth / norm)."""
-        g, _ = apply_prec(grad, prec)
-        g = self.mask.forward(g, self.inner)
+        """Processed update direction over the inner grid: the reference's gradient is the inner
+        region of the plan's (get_grad_vp, iso_acoustic/devito.py:1062-1097; the buffers of
+        Data.clear_grad, problem/data.py:352-372), so Data.apply_prec normalises by the inner
+        points and MaskField ramps at the inner field's own edges, then smooth and norm (against
+        the whole model, as NormField reads the variable's extended data)."""
+        g, _ = apply_prec(grad[self.inner].contiguous(), prec[self.inner].contiguous())
+        g = self.mask.forward(g, (slice(None),) * g.dim())
         g = self.smooth.forward(g)
         return self.normf.forward(g, variable=self.vp, transform=lambda x: 1 / x)
+
+    def take_step(self, d):
+        """The optimiser's update of the inner model (LocalOptimiser.update_variable on
+        variable.data, optimisers/optimiser.py:273-298), then the clip of the whole model."""
+        v = self.vp[self.inner].contiguous()
+        self.optimiser.step(v, d)
+        self.vp[self.inner] = v
+        self.vp.copy_(self.clip.forward(self.vp))
 
     def iterate(self, f_max=None):
         t0 = time.perf_counter()
         misfit, grad, prec = self.gradient(f_max)
-        d = self.direction(grad, prec)
-        self.optimiser.step(self.vp, d)
-        self.vp.copy_(self.clip.forward(self.vp))
+        self.take_step(self.direction(grad, prec))
         torch.cuda.synchronize(self.device)
         rec = dict(misfit=misfit, error=self.error(), seconds=time.perf_counter() - t0, f_max=f_max)
         self.history.append(rec)
@@ -270,9 +280,7 @@ class LearnedFWI(PlainFWI):
         if accepted:
             self.vp.copy_(cand)
         else:
-            d = self.direction(grad, prec)
-            self.optimiser.step(self.vp, d)
-            self.vp.copy_(self.clip.forward(self.vp))
+            self.take_step(self.direction(grad, prec))
         torch.cuda.synchronize(self.device)
         rec = dict(misfit=misfit, error=self.error(), seconds=time.perf_counter() - t0, f_max=f_max,
                    learned=bool(accepted))
@@ -290,9 +298,7 @@ def generate_pairs(fwi, phantoms_vp, iterations=5, f_max=None):
             _, grad, prec = fwi.gradient(f_max)
             xs.append(features(grad, fwi.vp, fwi.inner))
             ts.append(((fwi.vp_true - fwi.vp)[fwi.inner] / VP_SCALE)[None].contiguous())
-            d = fwi.direction(grad, prec)
-            fwi.optimiser.step(fwi.vp, d)
-            fwi.vp.copy_(fwi.clip.forward(fwi.vp))
+            fwi.take_step(fwi.direction(grad, prec))
     return torch.cat(xs), torch.cat(ts)
 
 
