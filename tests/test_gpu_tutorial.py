@@ -30,3 +30,26 @@ def test_cuda_path_reproduces_the_recorded_tutorial_losses():
                               obs_case['absorbing'], obs_case['srcs'][0], obs_case['recs'][0], w[None], origin,
                               kernel='OT2')
     assert C.rel_l2(obs[0], ref) <= 1e-4
+
+
+def test_product_pipelines_reproduce_the_recorded_total_loss():
+    """The same first iteration through the product's own GPU trace pipelines and FWI driver
+    (fwi.PlainFWI.misfit: filters, mute, norm per shot, L2 on the device) against the tutorial's
+    recorded total over the 15 shots (26.2682). The filters' cosine tables depend only on their
+    period: f_max 0.42 MHz at relaxation 1 gives the recorded run's 31-tap table (1 / f = 14.88)."""
+    import torch
+    from stride_gb300 import fwi
+
+    g = T.load()
+    shots = g['shot_ids'].tolist()
+    c = T.case(g, g['vp_true'], T.wavelet(g), shots)
+    w = dict(shape=c['vp'].shape, spacing=c['spacing'], extra=c['extra'], absorbing=c['absorbing'], dt=c['dt'],
+             nt=c['nt'], vp=c['vp'], rho=None, alpha=None, shots=shots, src=c['srcs'], rec=c['recs'],
+             wavelet=c['wav'].astype(np.float32))
+    plain = fwi.PlainFWI(w, kernel='OT2')
+    try:
+        total = plain.misfit(torch.full(c['vp'].shape, 1500., device=plain.device), f_max=0.42e6)
+    finally:
+        plain.close()
+    recorded = float(np.sum(g['losses']))
+    assert abs(total - recorded) <= 3e-3 * recorded, (total, recorded)
