@@ -271,7 +271,7 @@ int sa_gemm_bf16(const void* A, int lda, const void* B, int ldb, float* C, int l
  * im2col of x built in shared memory, never in HBM: column (ky*3+kx)*Cin+ci of pixel p is channel ci
  * of its neighbour (ky-1, kx-1) in x, bf16 NHWC [P][ldx] (zero outside the image and for columns
  * >= 9*Cin). Wt bf16 [N][ldw] with the same column order; Cin and ldx multiples of 8, Kp >= 9*Cin a
- * multiple of 16, N of 32. *err as for sa_gemm_bf16. */
+ * multiple of 16, N of 32, H <= 32767, W <= 65535. *err as for sa_gemm_bf16. */
 int sa_conv3x3_bf16(const void* x, int ldx, int B, int H, int W, int Cin, const void* Wt, int ldw, float* C, int ldc,
                     void* Cb, int ldcb, int N, int Kp, const float* bias, int relu, int* err, void* stream);
 

@@ -315,11 +315,12 @@ extern "C" int sa_conv3x3_bf16(const void* x, int ldx, int B, int H, int W, int 
                                int ldc, void* Cb, int ldcb, int N, int Kp, const float* bias, int relu, int* err,
                                void* stream) {
     const long long P = (long long)B * H * W;
-    if (!x || !Wt || !C || !err || B < 1 || H < 1 || W < 1 || Cin < 8 || Cin % 8 || P % kBM || P > INT32_MAX ||
+    if (!x || !Wt || !C || !err || B < 1 || H < 1 || W < 1 || H > 32767 || W > 65535 || Cin < 8 || Cin % 8 ||
+        P % kBM || P > INT32_MAX ||
         Kp < 9 * Cin || Kp % 16 || N % 32 || ldx < Cin || ldx % 8 || ldw < Kp || ldw % 8 || ldc < N ||
         (Cb && ldcb < N) || ((uintptr_t)x & 15) || ((uintptr_t)Wt & 15))
-        return (sa::set_last_error("sa_conv3x3_bf16: pixels a multiple of 128, Cin and ldx multiples of 8, "
-                                   "Kp >= 9 Cin a multiple of 16, N of 32, 16-byte aligned operands"),
+        return (sa::set_last_error("sa_conv3x3_bf16: pixels a multiple of 128, H <= 32767 and W <= 65535, Cin and "
+                                   "ldx multiples of 8, Kp >= 9 Cin a multiple of 16, N of 32, 16-byte aligned operands"),
                 SA_E_INVALID);
     const auto* a = static_cast<const __nv_bfloat16*>(x);
     const auto* b = static_cast<const __nv_bfloat16*>(Wt);
