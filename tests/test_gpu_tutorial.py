@@ -63,8 +63,8 @@ def test_gradient_step_reproduces_the_recorded_second_iteration():
     iteration at the updated model, each within 0.5 % (the oracle's chain: within 0.22 %).
 
     The recorded run injected the adjoint source as the reference's non-fw3d branch does,
-    rec.inject(p_a, -rec[t-1] dt^2 vp^2) before the stencil (iso_acoustic/devito.py:746-747,
-    787-788); this checkout forces the fw3d branch (:725), whose injection is the plan's. The older
+    rec.inject(p_a, -rec[t-1] dt^2 vp^2) before the stencil (iso_acoustic/devito.py:750-751,
+    793-794); this checkout forces the fw3d branch (:725), whose injection is the plan's. The older
     reading is the current one on the adjoint source delayed by two samples (it differs only by the
     first level's single injection; on this case the gradients agree to 7e-6)."""
     import torch
