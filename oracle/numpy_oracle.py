@@ -601,7 +601,7 @@ def rho_term(s, buoy, spacing):
 
 def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
             rho=None, alpha=None, kernel=None, undersampling=4, dtype=np.float32, src_coords=None,
-            interpolation='linear', raw=False, rho_grad=False, boundary='sponge', f_centre=None):
+            interpolation='linear', raw=False, rho_grad=False, boundary='sponge', f_centre=None, fw3d=True):
     """Reverse-time adjoint and vp imaging condition of the reference
     (iso_acoustic/devito.py:689-920, 985-1043): backward update of p_a[t-1],
     injection of -res[t] dt^2 vp^2 at the receivers (fw3d_mode, :725,748-753), and on
@@ -616,7 +616,10 @@ def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
     (``rho_term``) are recomputed (the Eqs under the undersampling condition), and on every step
     grad += held p_a[t], prec += held^2 (the Incs, which no conditional dimension guards). The
     time spacing f dt of the undersampled derivative is the physical one (unpinned: Devito
-    is not available to confirm it). Returns (grad, prec, grad_rho, prec_rho[, gsrc]) with
+    is not available to confirm it). ``fw3d=False``: the reference's other injection branch, which
+    its before_adjoint forces off (iso_acoustic/devito.py:725): -res[t-1] dt^2 vp^2 into p_a[t]
+    before the stencil (:750-751, 793-794) instead of -res[t] dt^2 vp^2 into p_a[t-1] after it.
+    Returns (grad, prec, grad_rho, prec_rho[, gsrc]) with
     ``rho_grad``. ``boundary='pml'``: the CFS-PML's adjoint as Devito forms it (time derivative
     and first space derivative transposed, boundaries/devito.py:135-149)."""
     dim = vp.ndim
@@ -654,7 +657,15 @@ def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
     pml = _pml_state(boundary, vp, spacing, absorbing, f_centre, dtype)
     if pml is not None:
         damp = np.zeros_like(damp)
+    def inject(field, row):
+        for c, off in enumerate(offs):
+            idx = tuple(rb[:, d] + off[d] for d in range(dim))
+            amp = -res[row].astype(np.float64) * dt * dt * med.vp2[idx].astype(np.float64)
+            np.add.at(field, idx, (rw[:, c] * amp).astype(dtype))
+
     for t in range(nt - 1 - f, 0, -1):
+        if not fw3d:
+            inject(q, t - 1)
         if gsrc is not None:
             gsrc[t] = -_gather(q, sb, sw, dim, soffs)
         if pml is None:
@@ -662,10 +673,8 @@ def adjoint(vp, spacing, dt, nt, absorbing, rec_coords, residual, origin, snaps,
         else:
             Lt = _pml_Lt(pml, med, q, kernel, dt, w2, ws, spacing, absorbing, True)
         qn = _update(med, damp, Lt, q, qp, dt)
-        for c, off in enumerate(offs):
-            idx = tuple(rb[:, d] + off[d] for d in range(dim))
-            amp = -res[t].astype(np.float64) * dt * dt * med.vp2[idx].astype(np.float64)
-            np.add.at(qn, idx, (rw[:, c] * amp).astype(dtype))
+        if fw3d:
+            inject(qn, t)
         if raw:
             if t % f == 0:
                 n = t // f

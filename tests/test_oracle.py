@@ -1,8 +1,10 @@
 """The oracle (CPU restatements) against known answers, golden fixtures and each other.
 
-No GPU. Parity of the restatement with Devito itself is unpinned (Devito is not vendored and
-cannot be installed here); these checks pin it to the reference's own analytic check, to
-fixtures, and to the independent C restatement.
+No GPU. Devito is not vendored and cannot be installed here; besides the losses the reference's
+imaging tutorial recorded from Devito (tests/test_pin_tutorial.py), these checks pin the
+restatement to the reference's own analytic check, to fixtures, to the independent C
+restatement and to properties of the scheme (self-convergence, the FP32 noise floor, adjoint
+identities).
 """
 
 import os
@@ -351,3 +353,28 @@ def test_exact_adjoint_dot_product_hicks(interp):
     lhs = float(np.sum(tr * r))
     rhs = float(np.sum(gw * w))
     assert abs(lhs - rhs) <= 1e-6 * abs(lhs)
+
+
+def test_older_adjoint_injection_is_the_current_one_two_samples_later():
+    """The reference's non-fw3d adjoint injection (-res[t-1] dt^2 vp^2 into p_a[t] before the stencil,
+    iso_acoustic/devito.py:750-751, 793-794), which the recorded imaging tutorial used, equals its
+    fw3d branch (forced on at :725; the branch the plan implements) on the residual delayed by two
+    samples, bit for bit when the residual is zero where only the older reading reads it (the first
+    sample's window weight, and sample nt - 2 - f, which it injects into the first level)."""
+    from tests import _cases as C
+    c = C.small_case(kernel='OT2', density='variable', alpha=True, nt=200)
+    origin = tuple(-e * h for e, h in zip(c['extra'], c['spacing']))
+    kw = dict(rho=c['rho'], alpha=c['alpha'], kernel='OT2', undersampling=4)
+    _, snaps = O.forward(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['srcs'][0], c['recs'][0],
+                         c['wav'][None], origin, save=True, **kw)
+    r = np.random.default_rng(5).standard_normal((len(c['recs'][0]), c['nt'])).astype(np.float32)
+    r[:, 0] = 0
+    r[:, c['nt'] - 2 - 4:] = 0
+    late = np.zeros_like(r)
+    late[:, 2:] = r[:, :-2]
+    old = O.adjoint(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['recs'][0], r, origin, snaps,
+                    fw3d=False, **kw)
+    new = O.adjoint(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['recs'][0], late, origin, snaps, **kw)
+    assert np.array_equal(old[0], new[0]) and np.array_equal(old[1], new[1])
+    same = O.adjoint(c['vp'], c['spacing'], c['dt'], c['nt'], c['absorbing'], c['recs'][0], r, origin, snaps, **kw)
+    assert C.cosine(same[0], old[0]) < 0.999  # the two readings differ on the same residual
