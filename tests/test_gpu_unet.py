@@ -1,7 +1,6 @@
 """Learned preconditioner kernels: the tcgen05 BF16 GEMM against an FP64 product of the same
 bf16 operands."""
 
-import numpy as np
 import pytest
 
 torch = pytest.importorskip('torch')
