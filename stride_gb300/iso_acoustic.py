@@ -125,7 +125,8 @@ class IsoAcousticGB300(ProblemTypeBase):
     ``boundary_type='sponge_boundary_2'``, ``interpolation_type`` 'linear', 'hicks' or 'sinc',
     ``attenuation_power=0``, ``diff_source``, ``save_undersampling``, ``save_wavefield``.
     ``platform``, ``devito_config`` and ``devito_args`` are accepted and ignored (the time
-    loop always runs on the GPU). ``boundary_type='complex_frequency_shift_PML_2'`` runs with
+    loop always runs on the GPU), and so is ``fw3d_mode``: the reference forces its fw3d adjoint
+    injection on (devito.py:724-725), which is the one this class runs. ``boundary_type='complex_frequency_shift_PML_2'`` runs with
     kernel OT2 (the combination the reference's own example runs). Gradients: vp, rho and
     the wavelets; alpha raises ValueError('Variable alpha not implemented') as in the
     reference, which has no alpha gradient. Options the reference supports but this build does
